@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Benchmark: frames/s of the plain GLRaycaster-equivalent ray march at
+1920x1080 on a 1024^3 uint16 lit volume (workload ``plain_large_lit``).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one frame at the next of 120 seeded orbit poses (plain method,
+full quality, LOD 0).  ``value`` times K frames back to back on the renderer's
+stream with CUDA events, the brick pool (2.25 GB) already resident in HBM;
+consecutive frames use different poses and the inputs exceed L2.  ``e2e`` times
+the same frames through the C ABI with the image read back to pinned host
+memory each step.  ``--impl reference`` times the CPU restatement of the
+reference's ray march (the oracle) on all host cores on a bounded sample of
+rows of each frame.  Multi-GPU runs are independent replicas (the path does
+not shard): rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "frames/s @1080p, 1024^3 u16: plain raycast (lit)"
+LIT_BYTES_PER_SAMPLE = 7 * 8 * 2 + 16   # 7 trilinear lookups of 8 u16 texels + FP32 TF entry
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=40)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="plain_large_lit")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="target CPU time of the bounded CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--frame-ert", type=float, default=1.0)
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks + throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(impl):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1 and impl == "ours":
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def read_profile_traffic(workload):
+    """DRAM bytes per launch of the ray-march kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / f"raycast_{workload}.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_volume(w, torch):
+    """Generates the workload's volume in HBM and bricks it on the GPU."""
+    from tuvok_gb300 import Volume, generate_volume_device
+    n = w.dims[0] * w.dims[1] * w.dims[2]
+    nbytes = n * np.dtype(w.dtype).itemsize
+    raw = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    generate_volume_device(raw.data_ptr(), w.dims, w.dtype, w.blobs(), w.noise_amp,
+                           w.noise_octaves, w.noise_cell, w.seed, int(w.int_noise), w.vmax)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    vol = Volume(raw.data_ptr(), brick_size=w.brick_size, overlap=w.overlap, dims=w.dims,
+                 dtype=w.dtype)
+    torch.cuda.synchronize()
+    brick_s = time.perf_counter() - t0
+    return vol, raw, brick_s
+
+
+def configure(r, w, vol, frame_ert):
+    r.RegisterDataset(vol)
+    r.Set1DTransFloat(w.tf())
+    r.SetRendermode(0)
+    r.SetUseLighting(w.lighting)
+    r.SetLightModel(w.light_model, 0.2, 0.6, 0.2, 32.0)
+    r.SetSampleRateModifier(w.srm)
+    r.SetFrameTermination(frame_ert)
+    r.Resize(w.width, w.height)
+
+
+def cpu_baseline(w, raw_host, poses, seconds, samples_per_frame, threads):
+    """Times the oracle (CPU restatement of the reference march) on every
+    r-th row of one frame, r chosen for about `seconds` of work."""
+    import oracle as O
+    t0 = time.perf_counter()
+    prep = O.Prepared(raw_host, w.brick_size, w.overlap, w.tf(), srm=w.srm, lighting=w.lighting,
+                      light_model=w.light_model, threads=threads)
+    setup_s = time.perf_counter() - t0
+    eye, at, up = poses[0]
+    # calibrate on a sparse pass, then size the sample
+    stride = 64
+    _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                          row_stride=stride, threads=threads)
+    rate = max(n / max(t, 1e-6), 1.0)
+    target = rate * seconds
+    stride = max(1, min(w.height, int(math.ceil(samples_per_frame / max(target, 1.0)))))
+    _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                          row_stride=stride, threads=threads)
+    rows = len(range(0, w.height, stride))
+    frac = rows / w.height
+    prep.close()
+    return {"fps": frac / t, "msamples_s": n / t / 1e6, "rows": rows, "stride": stride,
+            "march_s": t, "setup_s": setup_s, "samples": n}
+
+
+def run_reference(args):
+    """--impl reference: the oracle's CPU march on all host cores, bounded
+    samples of each frame; rank 0 only."""
+    ws, rank, local = dist_setup("reference")
+    if rank != 0:
+        return
+    import torch
+    import oracle as O
+    from tuvok_gb300.build import build_oracle
+    from tuvok_gb300.workloads import WORKLOADS
+    build_oracle()
+    w = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    torch.cuda.set_device(local)
+    # input creation only: the volume is generated on the GPU and copied out
+    vol, raw, _ = make_volume(w, torch)
+    raw_host = raw.cpu().numpy().view(w.dtype).reshape(w.dims[2], w.dims[1], w.dims[0])
+    del vol, raw
+    torch.cuda.empty_cache()
+    prep = O.Prepared(raw_host, w.brick_size, w.overlap, w.tf(), srm=w.srm,
+                      lighting=w.lighting, light_model=w.light_model, threads=threads)
+    poses = w.poses()
+    # per-step sample: every `stride`-th row, sized so the run stays within minutes
+    eye, at, up = poses[0]
+    _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                          row_stride=64, threads=threads)
+    per_row = t / len(range(0, w.height, 64))
+    budget = 150.0 / max(args.steps + args.warmup, 1)
+    stride = max(1, int(math.ceil(per_row * w.height / budget)))
+    rows = len(range(0, w.height, stride))
+    for i in range(args.warmup):
+        eye, at, up = poses[i % len(poses)]
+        prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height, row_stride=stride,
+                    row_phase=i % stride, threads=threads)
+    total_t, total_n = 0.0, 0
+    for i in range(args.steps):
+        eye, at, up = poses[(args.warmup + i) % len(poses)]
+        _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                              row_stride=stride, row_phase=i % stride, threads=threads)
+        total_t += t
+        total_n += n
+    prep.close()
+    frac = rows / w.height
+    fps = args.steps * frac / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded blobs + value noise, generated on the GPU, copied to host)",
+        "config": {"workload": w.name, "dims": list(w.dims), "brick": list(w.brick_size),
+                   "width": w.width, "height": w.height, "srm": w.srm,
+                   "lighting": "blinn-phong" if w.light_model else "reference"},
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"every {stride}-th row ({rows} of {w.height}) per frame, "
+                                   f"{args.steps} poses; {total_n / total_t / 1e6:.2f} "
+                                   f"Msamples/s"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from tuvok_gb300 import Renderer
+    from tuvok_gb300.workloads import WORKLOADS
+    ws, rank, local = dist_setup("ours")
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    vol, raw, brick_s = make_volume(w, torch)
+    raw_bytes = raw.numel()
+    raw_host = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        raw_host = raw.cpu().numpy().view(w.dtype).reshape(w.dims[2], w.dims[1], w.dims[0])
+    del raw
+    torch.cuda.empty_cache()
+    pool_bytes = vol.info.device_bytes
+    r = Renderer()
+    configure(r, w, vol, args.frame_ert)
+    poses = w.poses()
+    ext = torch.cuda.ExternalStream(r.GetStream())
+
+    def frame(i):
+        eye, at, up = poses[i % len(poses)]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        r.Paint()
+
+    for i in range(args.warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier(ws)
+        torch.cuda.synchronize()
+        start.record(ext)
+        for i in range(K):
+            ev[i][0].record(ext)
+            frame(args.warmup + i)
+            ev[i][1].record(ext)
+        stop.record(ext)
+        torch.cuda.synchronize()
+        barrier(ws)
+    ms = start.elapsed_time(stop)
+    ms = max_over_ranks(ws, ms)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    value = ws * K / (ms / 1000.0)
+
+    # samples per frame of the timed poses (deterministic; re-rendered untimed)
+    samples, shaded, kms, vis = [], [], [], []
+    for i in range(K):
+        frame(args.warmup + i)
+        st = r.GetStats()
+        samples.append(st.samples)
+        shaded.append(st.shaded_samples)
+        kms.append(st.last_paint_ms)
+        vis.append(st.bricks_visible)
+    mean_samples = float(np.mean(samples))
+    kernel_ms = float(np.mean(step_ms))
+    peak, peak_kind = measured_peaks()
+    achieved = mean_samples * LIT_BYTES_PER_SAMPLE / (kernel_ms / 1000.0) / 1e9
+    traffic = read_profile_traffic(w.name)
+
+    # end to end through the C ABI: view upload, paint, image to pinned host memory
+    img = torch.empty((w.height, w.width, 4), dtype=torch.float32, pin_memory=True)
+    img_np = img.numpy()
+    for i in range(args.warmup):
+        frame(i)
+        r.ReadBackPixels(img_np)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for i in range(K):
+        frame(args.warmup + i)
+        r.ReadBackPixels(img_np)
+    e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
+    e2e = ws * K / e2e_s
+    dev_brick_bytes = 112  # sizeof(tvk::DevBrick)
+    h2d = int(np.mean(vis)) * dev_brick_bytes
+    d2h = w.width * w.height * 16 + 32
+
+    cpu = None
+    if raw_host is not None:
+        threads = os.cpu_count() or 1
+        c = cpu_baseline(w, raw_host, poses, args.cpu_seconds, mean_samples, threads)
+        cpu = {"value": c["fps"], "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"oracle march on every {c['stride']}-th row ({c['rows']} of "
+                         f"{w.height}) of pose 0, {c['march_s']:.1f} s, "
+                         f"{c['msamples_s']:.2f} Msamples/s; set-up (CPU bricking) "
+                         f"{c['setup_s']:.1f} s not timed"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": K,
+            "warmup": args.warmup, "ms_per_step": ms / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blobs + value noise, generated on the GPU)",
+            "config": {"workload": w.name, "dims": list(w.dims), "voxel": "u16 (12-bit)",
+                       "brick": list(w.brick_size), "width": w.width, "height": w.height,
+                       "srm": w.srm, "lighting": "blinn-phong ka0.2 kd0.6 ks0.2 n32",
+                       "poses": len(poses), "frame_ert": args.frame_ert,
+                       "l2": f"inputs larger than L2 (brick pool {pool_bytes / 1e9:.2f} GB); "
+                             "each step a different pose",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind,
+                         "note": f"algorithmic bytes = reference samples x "
+                                 f"{LIT_BYTES_PER_SAMPLE} B (7 trilinear u16 lookups + FP32 TF)"},
+            "msamples_per_s": mean_samples / (kernel_ms / 1000.0) / 1e6,
+            "samples_per_frame": mean_samples,
+            "shaded_fraction": float(np.sum(shaded) / max(np.sum(samples), 1)),
+            "kernel_ms_lib_events": float(np.mean(kms)),
+            "bricking": {"seconds": brick_s, "raw_bytes": raw_bytes, "pool_bytes": pool_bytes,
+                         "gb_per_s": (raw_bytes + pool_bytes) / brick_s / 1e9},
+            "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": K,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

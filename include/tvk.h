@@ -1,0 +1,258 @@
+/*
+ * tvk.h -- C ABI of tuvok_gb300, a GB300 (sm_103a) implementation of Tuvok's
+ * volume-rendering hot path: LOD-0 bricking with ghost voxels, per-brick
+ * min/max and histograms, and the brick-by-brick GLRaycaster ray march
+ * (1D/2D transfer functions, central-difference lighting, front-to-back
+ * compositing with early ray termination, brick-level empty-space skipping).
+ *
+ * Conventions
+ *  - Every entry point returns tvk_status; no C++ exception crosses the ABI.
+ *    tvk_last_error() returns a message for the calling thread's last failure.
+ *  - One host thread drives one renderer handle.  Each renderer owns one CUDA
+ *    stream; all device work of a call is ordered on it.
+ *  - Volumes hold their bricks in device memory (HBM); renderers share volumes
+ *    read-only.  A volume must outlive the renderers it is attached to.
+ *  - Images are RGBA float32, premultiplied colour, row 0 = bottom row
+ *    (OpenGL window convention), width*height*4 floats.
+ *  - Brick keys are Tuvok's (timestep, lod, 1D index = x + y*bx + z*bx*by).
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the Tuvok source tree).
+ */
+#ifndef TVK_H
+#define TVK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TVK_ABI_VERSION 1
+
+typedef enum tvk_status {
+  TVK_OK = 0,
+  TVK_ERR_INVALID_ARG = 1,   /* bad pointer, size, key or mode */
+  TVK_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  TVK_ERR_OUT_OF_MEMORY = 3, /* device or pinned allocation failed */
+  TVK_ERR_UNSUPPORTED = 4,   /* valid request this build does not handle */
+  TVK_ERR_STATE = 5,         /* call order: e.g. paint without volume or TF */
+  TVK_ERR_INTERNAL = 6
+} tvk_status;
+
+typedef enum tvk_dtype { TVK_U8 = 0, TVK_U16 = 1 } tvk_dtype;
+
+/* AbstrRenderer::ERenderMode (Renderer/AbstrRenderer.h:120-126) */
+typedef enum tvk_render_mode {
+  TVK_RM_1DTRANS = 0,
+  TVK_RM_2DTRANS = 1,
+  TVK_RM_ISOSURFACE = 2
+} tvk_render_mode;
+
+/* Lighting models: the reference model of Shaders/lighting.glsl:33-43 and a
+ * selectable Blinn-Phong (ka, kd, ks, shininess). */
+typedef enum tvk_light_model {
+  TVK_LIGHT_REFERENCE = 0,
+  TVK_LIGHT_BLINN_PHONG = 1
+} tvk_light_model;
+
+typedef struct tvk_volume tvk_volume;
+typedef struct tvk_renderer tvk_renderer;
+
+/* BrickMD (IO/Brick.h:58-62): centre and extents in model space (volume
+ * normalised to max extent 1, centred at 0) and voxel counts incl. ghost. */
+typedef struct tvk_brick_md {
+  float center[3];
+  float extents[3];
+  uint32_t n_voxels[3];
+} tvk_brick_md;
+
+/* MinMaxBlock (Basics/MinMaxBlock.h:10-38) */
+typedef struct tvk_minmax {
+  double min_scalar, max_scalar, min_gradient, max_gradient;
+} tvk_minmax;
+
+typedef struct tvk_volume_info {
+  uint64_t dims[3];
+  tvk_dtype dtype;
+  uint32_t bit_width;        /* Dataset::GetBitWidth: 8 or 16 */
+  uint32_t brick_size[3];    /* incl. overlap, as Tuvok counts it */
+  uint32_t overlap;
+  uint32_t lod_count;        /* ExtendedOctree LOD table length */
+  uint64_t lod0_bricks;      /* bricks resident on the device (LOD 0) */
+  double range_min, range_max;   /* Dataset::GetRange */
+  double max_gradient;       /* Dataset::MaxGradientMagnitude */
+  uint64_t device_bytes;     /* brick pool + metadata held in HBM */
+} tvk_volume_info;
+
+/* Per-frame statistics of the last paint. */
+typedef struct tvk_stats {
+  uint64_t samples;          /* ray-march steps the reference loop executes */
+  uint64_t shaded_samples;   /* of those, steps whose voxels were fetched */
+  uint64_t bricks_visible;   /* LOD-0 bricks passing ContainsData */
+  uint64_t bricks_total;
+  uint64_t kernel_launches;  /* kernels this library launched for the frame */
+  float last_paint_ms;       /* device time of the last paint (CUDA events) */
+} tvk_stats;
+
+/* ---------------------------------------------------------------- misc */
+
+const char* tvk_status_string(tvk_status s);
+/* Message of the calling thread's last failing call ("" if none). */
+const char* tvk_last_error(void);
+int tvk_abi_version(void);
+
+/* ---------------------------------------------------------------- volumes */
+
+/* Bricks a flat volume (x fastest) on the GPU: LOD-0 bricks with `overlap`
+ * ghost voxels per side, zero or clamp-to-edge borders, per-brick min/max
+ * over the whole brick, the global 1D histogram of inner voxels, a 256-bin
+ * histogram per brick and the maximum gradient magnitude.
+ * Replaces ExtendedOctreeConverter::Convert's LOD-0 stage
+ * (IO/UVF/ExtendedOctree/ExtendedOctreeConverter.cpp:128-280, GetInputBrick
+ * :288-373, ClampToEdge :376-462, ComputeBrickStats .inc:408-444),
+ * Histogram1DDataBlock::ComputeTemplate (IO/UVF/Histogram1DDataBlock.cpp:120-161)
+ * and the max-gradient pass of Histogram2DDataBlock (:349-397).
+ * `voxels` is host memory (copied in) for tvk_volume_create and device memory
+ * for tvk_volume_create_device.  brick_size includes the overlap. */
+tvk_status tvk_volume_create(const void* voxels, tvk_dtype dtype, const uint64_t dims[3],
+                             const uint32_t brick_size[3], uint32_t overlap,
+                             int clamp_to_edge, tvk_volume** out);
+tvk_status tvk_volume_create_device(const void* device_voxels, tvk_dtype dtype,
+                                    const uint64_t dims[3], const uint32_t brick_size[3],
+                                    uint32_t overlap, int clamp_to_edge, tvk_volume** out);
+tvk_status tvk_volume_destroy(tvk_volume* v);
+tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out);
+
+/* ExtendedOctree::GetLoDSize / GetBrickCount (ExtendedOctree.cpp:241-262). */
+tvk_status tvk_volume_get_lod(const tvk_volume* v, uint32_t lod, uint64_t size[3],
+                              uint64_t brick_count[3]);
+
+/* BrickedDataset::GetBrickMetadata (IO/BrickedDataset.h:62) for a LOD-0 key;
+ * values follow UVFDataset::ComputeMetadataTOC (IO/uvfDataset.cpp:242-288). */
+tvk_status tvk_volume_get_brick_md(const tvk_volume* v, uint64_t timestep, uint64_t lod,
+                                   uint64_t index, tvk_brick_md* out);
+
+/* Dataset::GetBrick(key, std::vector<T>&) (IO/Dataset.h:93-100): copies one
+ * brick (x fastest, ghost included) to host memory of `bytes` bytes. */
+tvk_status tvk_volume_get_brick(const tvk_volume* v, uint64_t timestep, uint64_t lod,
+                                uint64_t index, void* host_out, size_t bytes);
+
+/* BrickedDataset::MaxMinForKey (IO/BrickedDataset.h:73). */
+tvk_status tvk_volume_get_minmax(const tvk_volume* v, uint64_t timestep, uint64_t lod,
+                                 uint64_t index, tvk_minmax* out);
+
+/* Global histogram, 2^(8*bytes) bins (Histogram1DDataBlock::GetHistogram);
+ * *trimmed_len = last non-zero bin + 1.  `bins` may exceed 2^(8*bytes). */
+tvk_status tvk_volume_get_histogram(const tvk_volume* v, uint64_t* host_out, size_t bins,
+                                    uint64_t* trimmed_len);
+
+/* 256-bin histograms of every LOD-0 brick's inner voxels, brick-major
+ * (new: the reference stores only the global histogram); bin = value >> shift
+ * with shift = max(0, bits(range_max) - 8). */
+tvk_status tvk_volume_get_brick_histograms(const tvk_volume* v, uint32_t* host_out,
+                                           size_t n_bricks, uint32_t* shift);
+
+/* LinearIndexDataset::IndexFrom4D / IndexTo4D (IO/LinearIndexDataset.cpp:7-39). */
+tvk_status tvk_volume_index_from_4d(const tvk_volume* v, const uint64_t xyzl[4],
+                                    uint64_t* index);
+tvk_status tvk_volume_index_to_4d(const tvk_volume* v, uint64_t lod, uint64_t index,
+                                  uint64_t xyzl[4]);
+
+/* ---------------------------------------------------------------- renderer */
+
+/* MasterController::RequestNewVolumeRenderer (Controller/MasterController.cpp:145-200)
+ * for the GLRaycaster type.  Defaults follow AbstrRenderer's constructor
+ * (Renderer/AbstrRenderer.cpp:64-170): FOV 50, near 0.01, far 1000, eye
+ * (0,0,1.6), sample-rate modifier 1, 1D TF mode, no lighting. */
+tvk_status tvk_renderer_create(tvk_renderer** out);
+tvk_status tvk_renderer_destroy(tvk_renderer* r);
+
+/* AbstrRenderer::RegisterDataset / LoadDataset (Renderer/AbstrRenderer.h:460). */
+tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v);
+
+/* AbstrRenderer::Set1DTrans + Changed1DTrans (AbstrRenderer.h:189-195) with
+ * TransferFunction1D::Set's byte semantics (IO/TransferFunction1D.cpp:146-177):
+ * colour channels are stretched to [0,1] by their min/max, alpha is byte/255;
+ * the table is then uploaded as GL_RGBA8 (GetByteArray, :311-330). */
+tvk_status tvk_set_tf1d_rgba8(tvk_renderer* r, const uint8_t* rgba, uint32_t n);
+/* Float RGBA table.  rgba8_upload != 0 reproduces the GL_RGBA8 upload
+ * (clamp, x255, truncate); 0 keeps FP32 entries. */
+tvk_status tvk_set_tf1d_float(tvk_renderer* r, const float* rgba, uint32_t n, int rgba8_upload);
+/* 2D TF (TransferFunction2D, IO/TransferFunction2D.cpp:222-264) as a float
+ * table of h rows (gradient axis, row 0 at t = 0) by w columns (value axis). */
+tvk_status tvk_set_tf2d_float(tvk_renderer* r, const float* rgba, uint32_t w, uint32_t h,
+                              int rgba8_upload);
+
+/* AbstrRenderer::SetRendermode / SetUseLighting / SetSampleRateModifier /
+ * SetIsoValue (AbstrRenderer.h:323, 414-418). */
+tvk_status tvk_set_render_mode(tvk_renderer* r, tvk_render_mode mode);
+tvk_status tvk_set_lighting(tvk_renderer* r, int enable);
+tvk_status tvk_set_sample_rate_modifier(tvk_renderer* r, float srm);
+tvk_status tvk_set_isovalue(tvk_renderer* r, float isovalue);
+
+/* AbstrRenderer::SetColors (AbstrRenderer.h:621): ambient/diffuse/specular
+ * RGBA (colour * w is used) and light direction in eye space. */
+tvk_status tvk_set_colors(tvk_renderer* r, const float ambient[4], const float diffuse[4],
+                          const float specular[4], const float light_dir[3]);
+/* Selects the lighting model; ka/kd/ks/shininess are used by Blinn-Phong. */
+tvk_status tvk_set_light_model(tvk_renderer* r, tvk_light_model model, float ka, float kd,
+                               float ks, float shininess);
+
+/* AbstrRenderer::SetViewParameters (AbstrRenderer.h:250-261) plus the eye/at/up
+ * of GLRenderer::SetViewPort (Renderer/GL/GLRenderer.cpp:905-917). */
+tvk_status tvk_set_view(tvk_renderer* r, const float eye[3], const float at[3],
+                        const float up[3], float fovy_deg, float znear, float zfar);
+/* AbstrRenderer::SetRotation/SetTranslation (AbstrRenderer.h:206-213): 4x4
+ * row-vector matrices (Tuvok layout, translation in elements 12..14); must be
+ * rigid.  modelview = rotation * translation * view. */
+tvk_status tvk_set_model_transform(tvk_renderer* r, const float rotation[16],
+                                   const float translation[16]);
+
+/* AbstrRenderer::Resize (AbstrRenderer.h:431). */
+tvk_status tvk_resize(tvk_renderer* r, uint32_t width, uint32_t height);
+
+/* Frame-level early termination: stop visiting bricks once the frame alpha
+ * reaches `threshold` (1 = never, the reference behaviour; GLRaycaster blends
+ * every brick). */
+tvk_status tvk_set_frame_termination(tvk_renderer* r, float threshold);
+
+/* AbstrRenderer::Paint (AbstrRenderer.h:433) for the full-quality capture
+ * path: plans the LOD-0 brick list (AbstrRenderer.cpp:999-1100), then ray
+ * marches every pixel on the renderer's stream.  Asynchronous. */
+tvk_status tvk_paint(tvk_renderer* r);
+
+/* GLRenderer::GetLastFBO + GLFBOTex::ReadBackPixels (GLRenderer.h:105,
+ * GLFBOTex.cpp:401): device pointer of the last frame and a blocking copy to
+ * host memory (width*height*4 floats). */
+tvk_status tvk_get_image_device(tvk_renderer* r, const float** device_rgba, uint32_t* width,
+                                uint32_t* height);
+tvk_status tvk_read_image(tvk_renderer* r, float* host_rgba, size_t n_floats);
+/* Per-pixel executed sample counts of the last paint (u32 per pixel). */
+tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t n);
+
+/* The renderer's CUDA stream (cudaStream_t) for callers that order their own
+ * work after a paint. */
+tvk_status tvk_renderer_get_stream(tvk_renderer* r, void** stream);
+/* Blocks until the renderer's stream is idle and fills *out for the last paint. */
+tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out);
+
+/* ---------------------------------------------------------------- synthetic data */
+
+/* Fills device memory with a seeded volume: the sum of Gaussian blobs (7
+ * floats each: cx, cy, cz, sigma, peak, 0, 0; voxel units, centre at voxel
+ * centres) plus value noise of `noise_octaves` octaves (cell size halving from
+ * noise_cell, amplitude noise_amp) or, with int_noise != 0, uniform integer
+ * noise in [-noise_amp, noise_amp]; rounded and clamped to [0, vmax].
+ * Input creation for tests and benchmarks only. */
+tvk_status tvk_generate_volume(void* device_out, tvk_dtype dtype, const uint64_t dims[3],
+                               const float* host_blobs, uint32_t n_blobs, float noise_amp,
+                               uint32_t noise_octaves, float noise_cell, uint64_t seed,
+                               int int_noise, float vmax);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TVK_H */

@@ -1,0 +1,261 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` use it as the checker / CPU baseline.  The
+product (tuvok_gb300, libtvk.so) never imports or calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "liboracle.so"
+REF_PATH = Path(__file__).resolve().parent / "_ref" / "libtuvok_ref.so"
+
+_u64p = C.POINTER(C.c_uint64)
+_u32p = C.POINTER(C.c_uint32)
+
+
+class Scene(C.Structure):
+    _fields_ = [
+        ("raw", C.c_void_p), ("dtype", C.c_int), ("dims", C.c_uint64 * 3),
+        ("brick_size", C.c_uint32 * 3), ("overlap", C.c_uint32), ("clamp_to_edge", C.c_int),
+        ("user_scale", C.c_double * 3), ("tf", C.POINTER(C.c_float)), ("tf_w", C.c_uint32),
+        ("tf_h", C.c_uint32), ("tf_rgba8", C.c_int), ("render_mode", C.c_int),
+        ("lighting", C.c_int), ("light_model", C.c_int), ("ambient", C.c_float * 4),
+        ("diffuse", C.c_float * 4), ("specular", C.c_float * 4), ("light_dir", C.c_float * 3),
+        ("bp_ka", C.c_float), ("bp_kd", C.c_float), ("bp_ks", C.c_float),
+        ("bp_shininess", C.c_float), ("isovalue", C.c_float),
+        ("sample_rate_modifier", C.c_float), ("frame_ert", C.c_float), ("eye", C.c_float * 3),
+        ("at", C.c_float * 3), ("up", C.c_float * 3), ("fovy_deg", C.c_float),
+        ("znear", C.c_float), ("zfar", C.c_float), ("width", C.c_uint32),
+        ("height", C.c_uint32), ("use_double", C.c_int), ("row_stride", C.c_uint32),
+        ("row_phase", C.c_uint32), ("threads", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} missing: run tuvok_gb300/build.py")
+        L = C.CDLL(str(LIB_PATH))
+        L.orc_lod_table.argtypes = [_u64p, _u32p, C.c_uint32, _u64p, _u64p, C.c_int]
+        L.orc_lod_table.restype = C.c_int
+        L.orc_brick_size.argtypes = [_u64p, _u64p, _u32p, C.c_uint32, _u64p, _u64p]
+        L.orc_brick_size.restype = None
+        L.orc_lod0_brick.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
+                                     _u64p, C.c_void_p]
+        L.orc_lod0_brick.restype = None
+        L.orc_brick_stats.argtypes = [C.c_void_p, C.c_int, C.c_uint64,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_brick_stats.restype = None
+        L.orc_histogram1d.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, _u64p]
+        L.orc_histogram1d.restype = C.c_uint64
+        L.orc_brick_hist256.argtypes = [C.c_void_p, C.c_int, _u64p, C.c_uint32, C.c_uint32,
+                                        _u32p]
+        L.orc_brick_hist256.restype = None
+        L.orc_brick_metadata.argtypes = [_u64p, _u64p, _u32p, C.c_uint32,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_float),
+                                         C.POINTER(C.c_float), _u32p]
+        L.orc_brick_metadata.restype = None
+        L.orc_max_gradient.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int]
+        L.orc_max_gradient.restype = C.c_double
+        L.orc_render.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p]
+        L.orc_render.restype = C.c_uint64
+        L.orc_round_half.argtypes = [C.c_float]
+        L.orc_round_half.restype = C.c_float
+        L.orc_render_timed.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_render_timed.restype = C.c_uint64
+        L.orc_prepare.argtypes = [C.POINTER(Scene)]
+        L.orc_prepare.restype = C.c_void_p
+        L.orc_render_prepared.argtypes = [C.c_void_p, C.POINTER(Scene), C.POINTER(C.c_float),
+                                          _u32p, C.POINTER(C.c_double)]
+        L.orc_render_prepared.restype = C.c_uint64
+        L.orc_release.argtypes = [C.c_void_p]
+        L.orc_release.restype = None
+        _lib = L
+    return _lib
+
+
+def _u64(v):
+    return (C.c_uint64 * len(v))(*[int(x) for x in v])
+
+
+def _u32(v):
+    return (C.c_uint32 * len(v))(*[int(x) for x in v])
+
+
+def _dt(arr):
+    return 0 if arr.dtype == np.uint8 else 1
+
+
+def lod_table(dims, brick_size, overlap):
+    sizes = (C.c_uint64 * (3 * 64))()
+    counts = (C.c_uint64 * (3 * 64))()
+    n = lib().orc_lod_table(_u64(dims), _u32(brick_size), overlap, sizes, counts, 64)
+    return ([tuple(sizes[3 * i:3 * i + 3]) for i in range(n)],
+            [tuple(counts[3 * i:3 * i + 3]) for i in range(n)])
+
+
+def brick_size(lod_size, brick_count, bsize, overlap, coords):
+    out = (C.c_uint64 * 3)()
+    lib().orc_brick_size(_u64(lod_size), _u64(brick_count), _u32(bsize), overlap, _u64(coords),
+                         out)
+    return tuple(out)
+
+
+def lod0_brick(raw, bsize, overlap, clamp, coords):
+    """raw: numpy [z, y, x]; returns the brick as [z, y, x]."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    sizes, counts = lod_table(dims, bsize, overlap)
+    bs = brick_size(sizes[0], counts[0], bsize, overlap, coords)
+    out = np.zeros((bs[2], bs[1], bs[0]), dtype=raw.dtype)
+    lib().orc_lod0_brick(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims), _u32(bsize),
+                         overlap, int(clamp), _u64(coords), out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def brick_stats(brick):
+    mn, mx = C.c_double(), C.c_double()
+    b = np.ascontiguousarray(brick)
+    lib().orc_brick_stats(b.ctypes.data_as(C.c_void_p), _dt(b), b.size, C.byref(mn), C.byref(mx))
+    return mn.value, mx.value
+
+
+def histogram1d(raw, bsize, overlap):
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    out = np.zeros(1 << (8 * raw.dtype.itemsize), dtype=np.uint64)
+    n = lib().orc_histogram1d(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
+                              _u32(bsize), overlap, out.ctypes.data_as(_u64p))
+    return out, int(n)
+
+
+def brick_hist256(brick, overlap, shift):
+    b = np.ascontiguousarray(brick)
+    out = np.zeros(256, dtype=np.uint32)
+    n = (b.shape[2], b.shape[1], b.shape[0])
+    lib().orc_brick_hist256(b.ctypes.data_as(C.c_void_p), _dt(b), _u64(n), overlap, shift,
+                            out.ctypes.data_as(_u32p))
+    return out
+
+
+def brick_metadata(lod_size, brick_count, bsize, overlap, aspect=(1.0, 1.0, 1.0)):
+    nb = brick_count[0] * brick_count[1] * brick_count[2]
+    c = np.zeros((nb, 3), dtype=np.float32)
+    e = np.zeros((nb, 3), dtype=np.float32)
+    n = np.zeros((nb, 3), dtype=np.uint32)
+    lib().orc_brick_metadata(_u64(lod_size), _u64(brick_count), _u32(bsize), overlap,
+                             (C.c_double * 3)(*aspect), c.ctypes.data_as(C.POINTER(C.c_float)),
+                             e.ctypes.data_as(C.POINTER(C.c_float)), n.ctypes.data_as(_u32p))
+    return c, e, n
+
+
+def max_gradient(raw, bsize, overlap, clamp=False):
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    return lib().orc_max_gradient(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
+                                  _u32(bsize), overlap, int(clamp))
+
+
+def round_half(x):
+    return lib().orc_round_half(float(x))
+
+
+def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), at=(0, 0, 0),
+               up=(0, 1, 0), fovy=50.0, znear=0.01, zfar=1000.0, srm=1.0, mode=0,
+               lighting=False, light_model=0, tf_rgba8=False, clamp=False,
+               ambient=(1, 1, 1, 0.1), diffuse=(1, 1, 1, 1), specular=(1, 1, 1, 1),
+               light_dir=(0, 0, -1), bp=(0.2, 0.6, 0.2, 32.0), frame_ert=1.0,
+               use_double=False, row_stride=1, row_phase=0, threads=0):
+    """Scene struct for the oracle; returns (scene, arrays that must stay alive)."""
+    raw = np.ascontiguousarray(raw)
+    tf = np.ascontiguousarray(np.asarray(tf, dtype=np.float32))
+    s = Scene()
+    s.raw = raw.ctypes.data_as(C.c_void_p)
+    s.dtype = _dt(raw)
+    s.dims[:] = (raw.shape[2], raw.shape[1], raw.shape[0])
+    s.brick_size[:] = tuple(bsize)
+    s.overlap = overlap
+    s.clamp_to_edge = int(clamp)
+    s.user_scale[:] = (1.0, 1.0, 1.0)
+    s.tf = tf.ctypes.data_as(C.POINTER(C.c_float))
+    if tf.ndim == 3:
+        s.tf_h, s.tf_w = tf.shape[0], tf.shape[1]
+    else:
+        s.tf_h, s.tf_w = 1, tf.shape[0]
+    s.tf_rgba8 = int(tf_rgba8)
+    s.render_mode = int(mode)
+    s.lighting = int(bool(lighting))
+    s.light_model = int(light_model)
+    s.ambient[:] = ambient
+    s.diffuse[:] = diffuse
+    s.specular[:] = specular
+    s.light_dir[:] = light_dir
+    s.bp_ka, s.bp_kd, s.bp_ks, s.bp_shininess = bp
+    s.sample_rate_modifier = srm
+    s.frame_ert = frame_ert
+    s.eye[:] = eye
+    s.at[:] = at
+    s.up[:] = up
+    s.fovy_deg, s.znear, s.zfar = fovy, znear, zfar
+    s.width, s.height = width, height
+    s.use_double = int(use_double)
+    s.row_stride, s.row_phase = row_stride, row_phase
+    s.threads = threads
+    return s, (raw, tf)
+
+
+def render(raw, bsize, overlap, tf, *, width, height, want_counts=False, **kw):
+    """Oracle render of raw ([z, y, x]) -> (image [h, w, 4], samples, counts|None)."""
+    s, keep = make_scene(raw, bsize, overlap, tf, width=width, height=height, **kw)
+    img = np.zeros((height, width, 4), dtype=np.float32)
+    counts = np.zeros((height, width), dtype=np.uint32) if want_counts else None
+    n = lib().orc_render(C.byref(s), img.ctypes.data_as(C.POINTER(C.c_float)),
+                         counts.ctypes.data_as(_u32p) if want_counts else None)
+    del keep
+    return img, int(n), counts
+
+
+class Prepared:
+    """Oracle scene bricked once; render() takes a camera each call."""
+
+    def __init__(self, raw, bsize, overlap, tf, **kw):
+        self._scene, self._keep = make_scene(raw, bsize, overlap, tf, **kw)
+        self._kw = kw
+        self._h = lib().orc_prepare(C.byref(self._scene))
+
+    def render(self, *, eye, width, height, at=(0, 0, 0), up=(0, 1, 0), row_stride=1,
+               row_phase=0, threads=0, use_double=False):
+        cam = Scene()
+        cam.eye[:] = eye
+        cam.at[:] = at
+        cam.up[:] = up
+        cam.fovy_deg = self._scene.fovy_deg
+        cam.znear, cam.zfar = self._scene.znear, self._scene.zfar
+        cam.width, cam.height = width, height
+        cam.row_stride, cam.row_phase = row_stride, row_phase
+        cam.threads = threads
+        cam.use_double = int(use_double)
+        img = np.zeros((height, width, 4), dtype=np.float32)
+        t = C.c_double()
+        n = lib().orc_render_prepared(self._h, C.byref(cam),
+                                      img.ctypes.data_as(C.POINTER(C.c_float)), None,
+                                      C.byref(t))
+        return img, int(n), t.value
+
+    def close(self):
+        if self._h:
+            lib().orc_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

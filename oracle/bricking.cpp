@@ -1,0 +1,296 @@
+// bricking.cpp -- CPU restatement of Tuvok's LOD-0 bricking, per-brick
+// statistics, histograms and brick metadata.
+//
+// TEST INFRASTRUCTURE ONLY (the checker for tuvok_gb300's CUDA bricking path).
+// Each function follows the reference routine named in its comment; paths are
+// relative to the Tuvok source tree.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace {
+
+template <class T>
+inline const T* as(const void* p) { return static_cast<const T*>(p); }
+
+}  // namespace
+
+extern "C" int orc_lod_table(const uint64_t dims[3], const uint32_t brick_size[3],
+                             uint32_t overlap, uint64_t* lod_sizes,
+                             uint64_t* brick_counts, int max_lods) {
+  // ExtendedOctree::ComputeMetadata, ExtendedOctree.cpp:188-243: halve each
+  // axis with ceil until every axis is 1; brick count = ceil(size / usable).
+  uint64_t v[3] = {dims[0], dims[1], dims[2]};
+  const uint64_t usable[3] = {brick_size[0] - 2ull * overlap,
+                              brick_size[1] - 2ull * overlap,
+                              brick_size[2] - 2ull * overlap};
+  int n = 0;
+  bool first = true;
+  do {
+    if (!first) {
+      for (int a = 0; a < 3; ++a)
+        if (v[a] > 1) v[a] = uint64_t(std::ceil(v[a] / 2.0));
+    }
+    first = false;
+    if (n < max_lods) {
+      for (int a = 0; a < 3; ++a) {
+        lod_sizes[3 * n + a] = v[a];
+        brick_counts[3 * n + a] = uint64_t(std::ceil(v[a] / double(usable[a])));
+      }
+    }
+    ++n;
+  } while (v[0] > 1 || v[1] > 1 || v[2] > 1);
+  return n;
+}
+
+extern "C" void orc_brick_size(const uint64_t lod_size[3], const uint64_t brick_count[3],
+                               const uint32_t brick_size[3], uint32_t overlap,
+                               const uint64_t coords[3], uint64_t out[3]) {
+  // ExtendedOctree::ComputeBrickSize, ExtendedOctree.cpp:276-285.
+  for (int a = 0; a < 3; ++a) {
+    const uint64_t core = brick_size[a] - 2ull * overlap;
+    const bool last = coords[a] == brick_count[a] - 1;
+    out[a] = (last && (lod_size[a] % core)) ? (2ull * overlap + lod_size[a] % core)
+                                            : brick_size[a];
+  }
+}
+
+namespace {
+
+template <class T>
+void lod0_brick(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                bool clamp, const uint64_t c[3], T* out) {
+  uint64_t lod[3 * 64], cnt[3 * 64];
+  orc_lod_table(dims, B, ov, lod, cnt, 64);
+  uint64_t bs[3];
+  orc_brick_size(lod, cnt, B, ov, c, bs);
+  const uint64_t total = dims[0] * dims[1] * dims[2];
+  // GetInputBrick, ExtendedOctreeConverter.cpp:288-373.  Without clamping the
+  // brick starts zeroed (:300-302).  With clamping the reference leaves the
+  // previous brick's bytes in place before ClampToEdge overwrites the borders;
+  // those are all overwritten for bricks whose reads stay inside the file, so a
+  // zero start gives the same result there.
+  std::fill(out, out + bs[0] * bs[1] * bs[2], T(0));
+  const uint64_t xs = c[0] == 0 ? ov : 0, ys = c[1] == 0 ? ov : 0, zs = c[2] == 0 ? ov : 0;
+  const uint64_t ye = bs[1] - ((c[1] == cnt[1] - 1) ? ov : 0);
+  const uint64_t ze = bs[2] - ((c[2] == cnt[2] - 1) ? ov : 0);
+  uint64_t line = bs[0];
+  if (c[0] == 0) line -= ov;
+  if (c[0] == cnt[0] - 1) line -= ov;
+  for (uint64_t z = 0; z < ze - zs; ++z) {
+    for (uint64_t y = 0; y < ye - ys; ++y) {
+      // byte offset into the raw file, in voxels (:335-338); unsigned wrap-around
+      // of the "0-(overlap-xStart)" term is intended and cancels out.
+      const uint64_t in = (0 - (uint64_t(ov) - xs) + c[0] * (B[0] - 2ull * ov)) +
+                          (y - (uint64_t(ov) - ys) + c[1] * (B[1] - 2ull * ov)) * dims[0] +
+                          (z - (uint64_t(ov) - zs) + c[2] * (B[2] - 2ull * ov)) * dims[0] * dims[1];
+      const uint64_t o = xs + (y + ys) * bs[0] + (z + zs) * bs[0] * bs[1];
+      // LargeRAWFile::ReadRAW: a read past the end of the file is short.
+      for (uint64_t i = 0; i < line; ++i)
+        out[o + i] = (in + i < total) ? raw[in + i] : T(0);
+    }
+  }
+  if (!clamp) return;
+  // ClampToEdge, ExtendedOctreeConverter.cpp:376-462, in its order x, y, z.
+  const bool s[3] = {c[0] == 0, c[1] == 0, c[2] == 0};
+  const bool e[3] = {c[0] == cnt[0] - 1, c[1] == cnt[1] - 1, c[2] == cnt[2] - 1};
+  auto at = [&](uint64_t x, uint64_t y, uint64_t z) -> T& {
+    return out[x + y * bs[0] + z * bs[0] * bs[1]];
+  };
+  if (s[0])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t y = 0; y < bs[1]; ++y)
+        for (uint64_t o = 0; o < ov; ++o) at(ov - 1 - o, y, z) = at(ov, y, z);
+  if (e[0])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t y = 0; y < bs[1]; ++y)
+        for (uint64_t o = 0; o < ov; ++o) at(bs[0] - ov + o, y, z) = at(bs[0] - 1 - ov, y, z);
+  if (s[1])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, ov - 1 - o, z) = at(x, ov, z);
+  if (e[1])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, bs[1] - ov + o, z) = at(x, bs[1] - 1 - ov, z);
+  if (s[2])
+    for (uint64_t y = 0; y < bs[1]; ++y)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, y, ov - 1 - o) = at(x, y, ov);
+  if (e[2])
+    for (uint64_t y = 0; y < bs[1]; ++y)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, y, bs[2] - ov + o) = at(x, y, bs[2] - 1 - ov);
+}
+
+template <class T>
+void stats(const T* p, uint64_t n, double* mn, double* mx) {
+  // ComputeBrickStats<T>, ExtendedOctreeConverter.inc:408-444: every voxel of
+  // the brick, ghost included, compared as double.
+  double lo = std::numeric_limits<double>::max();
+  double hi = -std::numeric_limits<double>::max();
+  for (uint64_t i = 0; i < n; ++i) {
+    const double cur = static_cast<double>(p[i]);
+    lo = cur < lo ? cur : lo;
+    hi = cur > hi ? cur : hi;
+  }
+  *mn = lo;
+  *mx = hi;
+}
+
+template <class T>
+uint64_t hist1d(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                uint64_t* hist) {
+  // Histogram1DDataBlock::ComputeTemplate<T>, Histogram1DDataBlock.cpp:120-161:
+  // every LOD-0 brick, inner voxels only.
+  const uint64_t nb = uint64_t(1) << (8 * sizeof(T));
+  std::fill(hist, hist + nb, 0ull);
+  uint64_t lod[3 * 64], cnt[3 * 64];
+  orc_lod_table(dims, B, ov, lod, cnt, 64);
+  std::vector<T> brick(uint64_t(B[0]) * B[1] * B[2]);
+  for (uint64_t bz = 0; bz < cnt[2]; ++bz)
+    for (uint64_t by = 0; by < cnt[1]; ++by)
+      for (uint64_t bx = 0; bx < cnt[0]; ++bx) {
+        const uint64_t c[3] = {bx, by, bz};
+        uint64_t bs[3];
+        orc_brick_size(lod, cnt, B, ov, c, bs);
+        lod0_brick<T>(raw, dims, B, ov, false, c, brick.data());
+        for (uint64_t z = ov; z < bs[2] - ov; ++z)
+          for (uint64_t y = ov; y < bs[1] - ov; ++y)
+            for (uint64_t x = ov; x < bs[0] - ov; ++x)
+              hist[size_t(brick[x + y * bs[0] + z * bs[0] * bs[1]])]++;
+      }
+  uint64_t len = nb;
+  while (len > 0 && hist[len - 1] == 0) --len;
+  return len;
+}
+
+template <class T>
+void hist256(const T* p, const uint64_t n[3], uint32_t ov, uint32_t shift, uint32_t* h) {
+  std::fill(h, h + 256, 0u);
+  for (uint64_t z = ov; z < n[2] - ov; ++z)
+    for (uint64_t y = ov; y < n[1] - ov; ++y)
+      for (uint64_t x = ov; x < n[0] - ov; ++x) {
+        const uint32_t v = uint32_t(p[x + y * n[0] + z * n[0] * n[1]]) >> shift;
+        h[v > 255 ? 255 : v]++;
+      }
+}
+
+}  // namespace
+
+extern "C" void orc_lod0_brick(const void* raw, int dtype, const uint64_t dims[3],
+                               const uint32_t brick_size[3], uint32_t overlap,
+                               int clamp_to_edge, const uint64_t coords[3], void* out) {
+  if (dtype == 0)
+    lod0_brick<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                        coords, static_cast<uint8_t*>(out));
+  else
+    lod0_brick<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                         coords, static_cast<uint16_t*>(out));
+}
+
+extern "C" void orc_brick_stats(const void* brick, int dtype, uint64_t n_voxels,
+                                double* min_out, double* max_out) {
+  if (dtype == 0)
+    stats<uint8_t>(as<uint8_t>(brick), n_voxels, min_out, max_out);
+  else
+    stats<uint16_t>(as<uint16_t>(brick), n_voxels, min_out, max_out);
+}
+
+extern "C" uint64_t orc_histogram1d(const void* raw, int dtype, const uint64_t dims[3],
+                                    const uint32_t brick_size[3], uint32_t overlap,
+                                    uint64_t* hist) {
+  if (dtype == 0) return hist1d<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, hist);
+  return hist1d<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, hist);
+}
+
+extern "C" void orc_brick_hist256(const void* brick, int dtype, const uint64_t n[3],
+                                  uint32_t overlap, uint32_t shift, uint32_t* hist) {
+  if (dtype == 0)
+    hist256<uint8_t>(as<uint8_t>(brick), n, overlap, shift, hist);
+  else
+    hist256<uint16_t>(as<uint16_t>(brick), n, overlap, shift, hist);
+}
+
+extern "C" void orc_brick_metadata(const uint64_t lod_size[3], const uint64_t brick_count[3],
+                                   const uint32_t brick_size[3], uint32_t overlap,
+                                   const double aspect[3], float* centers, float* extents,
+                                   uint32_t* n_voxels) {
+  // UVFDataset::ComputeMetadataTOC, uvfDataset.cpp:242-288.  Loop order x, y, z
+  // with the corner accumulated in float, exactly as the reference does.
+  const float asp[3] = {float(aspect[0]), float(aspect[1]), float(aspect[2])};
+  float nd[3] = {float(lod_size[0]) * asp[0], float(lod_size[1]) * asp[1],
+                 float(lod_size[2]) * asp[2]};
+  const float maxv = std::max(nd[0], std::max(nd[1], nd[2]));
+  for (int a = 0; a < 3; ++a) nd[a] /= maxv;
+  float corner[3] = {0, 0, 0};
+  float ext[3] = {0, 0, 0};
+  for (uint64_t x = 0; x < brick_count[0]; ++x) {
+    corner[1] = 0;
+    for (uint64_t y = 0; y < brick_count[1]; ++y) {
+      corner[2] = 0;
+      for (uint64_t z = 0; z < brick_count[2]; ++z) {
+        const uint64_t c[3] = {x, y, z};
+        uint64_t bs[3];
+        orc_brick_size(lod_size, brick_count, brick_size, overlap, c, bs);
+        const uint64_t k = z * brick_count[0] * brick_count[1] + y * brick_count[0] + x;
+        for (int a = 0; a < 3; ++a) {
+          ext[a] = float(bs[a] - 2ull * overlap) * asp[a] / maxv;
+          centers[3 * k + a] = (corner[a] + ext[a] / 2.0f) - nd[a] * 0.5f;
+          extents[3 * k + a] = ext[a];
+          n_voxels[3 * k + a] = uint32_t(bs[a]);
+        }
+        corner[2] += ext[2];
+      }
+      corner[1] += ext[1];
+    }
+    corner[0] += ext[0];
+  }
+}
+
+namespace {
+template <class T>
+double max_gradient(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                    bool clamp) {
+  // Histogram2DDataBlock::ComputeTemplate<T> first loop + ComputeGradient
+  // (Histogram2DDataBlock.cpp:327-345, 363-397): central differences over the
+  // inner voxels of every LOD-0 brick, normalised by 2 * max(T), in double.
+  uint64_t lod[3 * 64], cnt[3 * 64];
+  orc_lod_table(dims, B, ov, lod, cnt, 64);
+  std::vector<T> brick(uint64_t(B[0]) * B[1] * B[2]);
+  const double nf = double(std::numeric_limits<T>::max());
+  double best = 0;
+  for (uint64_t bz = 0; bz < cnt[2]; ++bz)
+    for (uint64_t by = 0; by < cnt[1]; ++by)
+      for (uint64_t bx = 0; bx < cnt[0]; ++bx) {
+        const uint64_t c[3] = {bx, by, bz};
+        uint64_t bs[3];
+        orc_brick_size(lod, cnt, B, ov, c, bs);
+        lod0_brick<T>(raw, dims, B, ov, clamp, c, brick.data());
+        const uint64_t sx = bs[0], sxy = bs[0] * bs[1];
+        for (uint64_t z = ov; z < bs[2] - ov; ++z)
+          for (uint64_t y = ov; y < bs[1] - ov; ++y)
+            for (uint64_t x = ov; x < bs[0] - ov; ++x) {
+              const uint64_t i = x + y * sx + z * sxy;
+              const double gx = (double(brick[i - 1]) - double(brick[i + 1])) / (nf * 2);
+              const double gy = (double(brick[i - sx]) - double(brick[i + sx])) / (nf * 2);
+              const double gz = (double(brick[i - sxy]) - double(brick[i + sxy])) / (nf * 2);
+              const double l = std::sqrt(gx * gx + gy * gy + gz * gz);
+              if (l > best) best = l;
+            }
+      }
+  return best;
+}
+}  // namespace
+
+extern "C" double orc_max_gradient(const void* raw, int dtype, const uint64_t dims[3],
+                                   const uint32_t brick_size[3], uint32_t overlap,
+                                   int clamp_to_edge) {
+  if (dtype == 0)
+    return max_gradient<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0);
+  return max_gradient<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0);
+}

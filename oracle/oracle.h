@@ -1,0 +1,147 @@
+/*
+ * oracle.h -- CPU restatement of Tuvok's volume-rendering hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA path of
+ * tuvok_gb300 is compared against.  Only the test suite, the smoke check and the
+ * CPU-baseline leg of bench.py load it; the product library never links or calls
+ * it, and nothing it computes is ever shipped as a result.
+ *
+ * Every function states the reference file:line it restates (paths are relative
+ * to the Tuvok source tree).  Parity of the bricking/statistics half is pinned
+ * against the reference's own ExtendedOctreeConverter (built from the reference
+ * sources by oracle/ref/Makefile) and the golden vectors of IO/test/rebricking.h.
+ * The rendering half restates GLSL that can only run through OpenGL; no golden
+ * images exist in the reference, so its parity is pinned only by this
+ * restatement (stated in the test headers).
+ */
+#ifndef TVK_ORACLE_H
+#define TVK_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- LOD table / brick geometry (IO/UVF/ExtendedOctree/ExtendedOctree.cpp) ---- */
+
+/* ExtendedOctree::ComputeMetadata (ExtendedOctree.cpp:188-243).  Writes up to
+ * max_lods entries of per-LOD voxel sizes (3 x u64) and brick counts (3 x u64).
+ * Returns the LOD count. */
+int orc_lod_table(const uint64_t dims[3], const uint32_t brick_size[3],
+                  uint32_t overlap, uint64_t* lod_sizes, uint64_t* brick_counts,
+                  int max_lods);
+
+/* ExtendedOctree::ComputeBrickSize (ExtendedOctree.cpp:276-285). */
+void orc_brick_size(const uint64_t lod_size[3], const uint64_t brick_count[3],
+                    const uint32_t brick_size[3], uint32_t overlap,
+                    const uint64_t coords[3], uint64_t out[3]);
+
+/* ExtendedOctreeConverter::GetInputBrick + ClampToEdge
+ * (ExtendedOctreeConverter.cpp:288-373, 376-462): one LOD-0 brick including its
+ * overlap, x fastest.  dtype 0 = u8, 1 = u16.  `out` holds the brick's voxels. */
+void orc_lod0_brick(const void* raw, int dtype, const uint64_t dims[3],
+                    const uint32_t brick_size[3], uint32_t overlap,
+                    int clamp_to_edge, const uint64_t coords[3], void* out);
+
+/* ExtendedOctreeConverter::ComputeBrickStats<T> (ExtendedOctreeConverter.inc:408-444). */
+void orc_brick_stats(const void* brick, int dtype, uint64_t n_voxels,
+                     double* min_out, double* max_out);
+
+/* Histogram1DDataBlock::ComputeTemplate<T> (Histogram1DDataBlock.cpp:120-161):
+ * histogram of the inner voxels of every LOD-0 brick.  `hist` has 2^(8*bytes)
+ * bins.  Returns the trimmed length (last non-zero bin + 1). */
+uint64_t orc_histogram1d(const void* raw, int dtype, const uint64_t dims[3],
+                         const uint32_t brick_size[3], uint32_t overlap,
+                         uint64_t* hist);
+
+/* Per-brick 256-bin histogram of a brick's inner voxels (new in this build:
+ * the reference keeps only the global histogram).  bin = value >> shift. */
+void orc_brick_hist256(const void* brick, int dtype, const uint64_t n[3],
+                       uint32_t overlap, uint32_t shift, uint32_t* hist);
+
+/* UVFDataset::ComputeMetadataTOC (uvfDataset.cpp:242-288) for LOD `lod`:
+ * per-brick centre/extents (float, model space) and n_voxels, in brick index
+ * order z*bx*by + y*bx + x.  aspect = per-axis LOD aspect (1 at LOD 0). */
+void orc_brick_metadata(const uint64_t lod_size[3], const uint64_t brick_count[3],
+                        const uint32_t brick_size[3], uint32_t overlap,
+                        const double aspect[3], float* centers, float* extents,
+                        uint32_t* n_voxels);
+
+/* MaxGradientMagnitude as Histogram2DDataBlock::ComputeTemplate<T> finds it
+ * (Histogram2DDataBlock.cpp:327-345, 363-397). */
+double orc_max_gradient(const void* raw, int dtype, const uint64_t dims[3],
+                        const uint32_t brick_size[3], uint32_t overlap,
+                        int clamp_to_edge);
+
+/* ---- Ray march (Shaders/GLRaycaster-*.glsl) ---- */
+
+enum { ORC_RM_1D = 0, ORC_RM_2D = 1, ORC_RM_ISO = 2 };
+enum { ORC_LIGHT_REFERENCE = 0, ORC_LIGHT_BLINN_PHONG = 1 };
+
+typedef struct orc_scene {
+  /* volume, bricked by the oracle itself */
+  const void* raw;
+  int dtype;                /* 0 = u8, 1 = u16 */
+  uint64_t dims[3];
+  uint32_t brick_size[3];   /* including overlap, as Tuvok counts it */
+  uint32_t overlap;
+  int clamp_to_edge;
+  double user_scale[3];     /* Dataset::GetScale, normally 1 */
+  /* transfer function: RGBA float table; tf_rgba8 != 0 reproduces the GL_RGBA8
+   * upload (truncate x255, /255 on lookup) */
+  const float* tf;
+  uint32_t tf_w, tf_h;      /* tf_h = 1 for 1D */
+  int tf_rgba8;
+  int render_mode;          /* ORC_RM_* */
+  int lighting;
+  int light_model;          /* ORC_LIGHT_* */
+  float ambient[4], diffuse[4], specular[4], light_dir[3];
+  float bp_ka, bp_kd, bp_ks, bp_shininess;
+  float isovalue;           /* iso mode: data units */
+  float sample_rate_modifier;
+  float frame_ert;          /* stop visiting bricks once frame alpha >= this; 1 = never */
+  /* camera: Tuvok's SetViewParameters + BuildLookAt + Perspective */
+  float eye[3], at[3], up[3];
+  float fovy_deg, znear, zfar;
+  uint32_t width, height;
+  int use_double;           /* 1: evaluate the march in FP64 (error reporting) */
+  /* optional: render only rows with y % row_stride == row_phase (CPU baseline) */
+  uint32_t row_stride, row_phase;
+  int threads;              /* OpenMP threads, 0 = default */
+} orc_scene;
+
+/* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row
+ * (gl_FragCoord.y = 0.5).  Returns the number of executed samples; the sample
+ * count of each pixel goes to samples_per_pixel when it is not NULL. */
+uint64_t orc_render(const orc_scene* scene, float* out_rgba,
+                    uint32_t* samples_per_pixel);
+
+/* orc_render with the wall time of the set-up (bricking, statistics) and of
+ * the march itself. */
+uint64_t orc_render_timed(const orc_scene* scene, float* out_rgba,
+                          uint32_t* samples_per_pixel, double* setup_s, double* march_s);
+
+/* Bricks the scene's volume once (returns a handle) so that several cameras
+ * can be rendered without repeating the set-up; orc_render_prepared takes the
+ * camera, viewport, row selection, threads and precision from `cam`. */
+void* orc_prepare(const orc_scene* scene);
+uint64_t orc_render_prepared(void* prepared, const orc_scene* cam, float* out_rgba,
+                             uint32_t* samples_per_pixel, double* march_s);
+void orc_release(void* prepared);
+
+/* IEEE binary16 round-to-nearest-even of a float, returned as float (the
+ * RGBA16F ray-entry buffer of GLRaycaster.cpp:97). */
+float orc_round_half(float x);
+
+/* ---- Synthetic inputs (CPU twin of the GPU generator; input creation only) ---- */
+void orc_generate_blobs(void* out, int dtype, const uint64_t dims[3],
+                        const float* blobs, uint32_t n_blobs, float noise_amp,
+                        uint32_t noise_octaves, float noise_cell, uint64_t seed,
+                        int int_noise, float vmax, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

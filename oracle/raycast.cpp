@@ -1,0 +1,610 @@
+// raycast.cpp -- scalar CPU restatement of Tuvok's brick-by-brick GLSL ray
+// caster (GLRaycaster) including the OpenGL fixed-function behaviour it relies on.
+//
+// TEST INFRASTRUCTURE ONLY (the checker for tuvok_gb300's CUDA ray march).
+// Sources restated (paths relative to the Tuvok tree):
+//   Shaders/GLRaycaster-1D-FS.glsl:51-82, GLRaycaster-1D-light-FS.glsl:84-134,
+//   GLRaycaster-2D-FS.glsl:53-94, GLRaycaster-2D-light-FS.glsl:61-117,
+//   Volume3D.glsl:39-60, VRender1D.glsl:39-57, VRender1DLit.glsl:49-72,
+//   lighting.glsl:33-50, Compositing.glsl:33-38;
+//   Renderer/GL/GLRaycaster.cpp:93-99 (RGBA16F entry buffer), :239-300
+//   (step size / opacity correction), :302-345 + :589-612 (eye->texture matrix),
+//   :348-478 (near plane + per-brick passes);
+//   Renderer/GL/GLRenderer.cpp:133-155 (blend ONE_MINUS_DST_ALPHA, ONE),
+//   :1813-1819 (CalculateScaling), :2890-2913 (light colours);
+//   Renderer/AbstrRenderer.cpp:860-866 (MaxValue), :953-997 (ContainsData),
+//   :999-1100 (brick list); Basics/Vectors.h:1250-1276 (LookAt, Perspective);
+//   IO/uvfDataset.cpp:1747-1774 (texture coordinates of a brick).
+//
+// Fixed-function semantics pinned here (no source states them):
+//   * volume texture: texel-centre trilinear, clamp to edge, texel value =
+//     raw / (2^bits - 1); lerp(a,b,f) = fma(f, b - a, a), x then y then z;
+//   * transfer function: GL_NEAREST, clamp to edge;
+//   * RGBA16F: IEEE binary16 round to nearest even;
+//   * framebuffer blend in FP32: dst = fma(src, 1 - dst.a, dst).
+// The march itself never fuses a multiply and an add unless written as fma
+// (the file is built with -ffp-contract=off), so the FP32 path is an exact
+// statement of the arithmetic the CUDA kernel performs.
+#include "oracle.h"
+
+#include <algorithm>
+#include <cfenv>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" float orc_round_half(float x) {
+  // IEEE 754 binary16, round to nearest, ties to even.
+  if (std::isnan(x) || std::isinf(x) || x == 0.0f) return x;
+  const double ax = std::fabs(double(x));
+  int e = std::ilogb(ax);
+  if (e < -14) e = -14;  // subnormal spacing 2^-24
+  const double sp = std::ldexp(1.0, e - 10);
+  double r = std::nearbyint(ax / sp) * sp;
+  if (r >= 65520.0) r = INFINITY;
+  return float(std::copysign(r, double(x)));
+}
+
+namespace {
+
+struct Mat34d { double m[3][4]; };
+
+struct View {
+  double mv[3][4];     // model -> eye
+  double inv[3][4];    // eye -> model
+  float kx, ky;        // ray direction scale (aspect * tan(fov/2), tan(fov/2))
+  float inv_w2, inv_h2;
+};
+
+View make_view(const orc_scene& s) {
+  // Basics/Vectors.h:1250-1263 BuildLookAt (computed in double here).
+  const double eye[3] = {s.eye[0], s.eye[1], s.eye[2]};
+  double F[3] = {double(s.at[0]) - eye[0], double(s.at[1]) - eye[1], double(s.at[2]) - eye[2]};
+  double U[3] = {s.up[0], s.up[1], s.up[2]};
+  auto cross = [](const double a[3], const double b[3], double o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  auto norm = [](double v[3]) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int i = 0; i < 3; ++i) v[i] /= l;
+  };
+  double S[3], U2[3];
+  cross(F, U, S);
+  cross(S, F, U2);
+  norm(F);
+  norm(U2);
+  norm(S);
+  View v;
+  const double* rows[3] = {S, U2, F};
+  for (int r = 0; r < 3; ++r) {
+    const double sg = (r == 2) ? -1.0 : 1.0;
+    double d = 0;
+    for (int c = 0; c < 3; ++c) {
+      v.mv[r][c] = sg * rows[r][c];
+      d += rows[r][c] * eye[c];
+    }
+    v.mv[r][3] = -sg * d;
+  }
+  // rigid inverse: R^T, -R^T t
+  for (int r = 0; r < 3; ++r) {
+    double t = 0;
+    for (int c = 0; c < 3; ++c) {
+      v.inv[r][c] = v.mv[c][r];
+      t += v.mv[c][r] * v.mv[c][3];
+    }
+    v.inv[r][3] = -t;
+  }
+  // Vectors.h:1265-1276 Perspective; the inverse projection of pixel centres.
+  const double th = std::tan(double(s.fovy_deg) * (3.14159265358979323846 / 180.0) / 2.0);
+  const double aspect = double(s.width) / double(s.height);
+  v.kx = float(aspect * th);
+  v.ky = float(th);
+  v.inv_w2 = float(2.0 / double(s.width));
+  v.inv_h2 = float(2.0 / double(s.height));
+  return v;
+}
+
+struct BrickR {
+  float pmin[3], pmax[3];
+  float tmin[3], tmax[3];  // texture coordinates of the inner region
+  float tex[3][4];   // eye -> brick texture coordinates
+  float step;        // fRayStepsize
+  uint32_t n[3];
+  std::vector<uint8_t> data;
+};
+
+// Affine map used for every matrix*point product of the march.
+template <class T>
+inline T affine_row(const float r[4], T x, T y, T z) {
+  return std::fma(T(r[0]), x, std::fma(T(r[1]), y, std::fma(T(r[2]), z, T(r[3]))));
+}
+
+template <class T>
+struct Vol {
+  const BrickR* b;
+  int dtype;
+  T inv_max;
+  T fetch(int x, int y, int z) const {
+    const size_t i = size_t(x) + size_t(y) * b->n[0] + size_t(z) * b->n[0] * b->n[1];
+    if (dtype == 0) return T(b->data[i]);
+    return T(reinterpret_cast<const uint16_t*>(b->data.data())[i]);
+  }
+  // texel-centre trilinear with clamp-to-edge
+  T sample(T tx, T ty, T tz) const {
+    const T t[3] = {tx, ty, tz};
+    int i0[3], i1[3];
+    T f[3];
+    for (int a = 0; a < 3; ++a) {
+      T u = std::fma(t[a], T(b->n[a]), T(-0.5));
+      u = std::fmin(std::fmax(u, T(0)), T(b->n[a] - 1));
+      i0[a] = int(u);
+      f[a] = u - T(i0[a]);
+      i1[a] = std::min(i0[a] + 1, int(b->n[a]) - 1);
+    }
+    auto lerp = [](T a, T c, T w) { return std::fma(w, c - a, a); };
+    const T c00 = lerp(fetch(i0[0], i0[1], i0[2]), fetch(i1[0], i0[1], i0[2]), f[0]);
+    const T c10 = lerp(fetch(i0[0], i1[1], i0[2]), fetch(i1[0], i1[1], i0[2]), f[0]);
+    const T c01 = lerp(fetch(i0[0], i0[1], i1[2]), fetch(i1[0], i0[1], i1[2]), f[0]);
+    const T c11 = lerp(fetch(i0[0], i1[1], i1[2]), fetch(i1[0], i1[1], i1[2]), f[0]);
+    const T c0 = lerp(c00, c10, f[1]);
+    const T c1 = lerp(c01, c11, f[1]);
+    return lerp(c0, c1, f[2]) * inv_max;
+  }
+};
+
+template <class T>
+inline T len3(T x, T y, T z) { return std::sqrt((x * x + y * y) + z * z); }
+
+template <class T>
+inline T dot3(const T a[3], const T b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+template <class T>
+inline T pow_int_or_real(T x, float e) {
+  // exponents 8 (reference) and 32 (Blinn-Phong) by repeated squaring
+  if (e == 8.0f) { T a = x * x; a = a * a; return a * a; }
+  if (e == 32.0f) { T a = x * x; a = a * a; a = a * a; a = a * a; return a * a; }
+  return std::pow(x, T(e));
+}
+
+struct Setup {
+  const orc_scene* s;
+  View view;
+  std::vector<BrickR> bricks;
+  std::vector<int> visible;   // bricks that pass ContainsData
+  float trans_scale, grad_scale, step_scale;
+  std::vector<float> tf;      // effective RGBA (after RGBA8 truncation if any)
+  float light_a[3], light_d[3], light_s[3];
+  float domain_scale[3];
+  double norm_mat[3][3];
+};
+
+template <class T>
+void lighting_ref(const Setup& st, const T pos[3], const T N[3], const T tfc[3], T out[3]) {
+  // lighting.glsl:33-43 via VRender1DLit.glsl:67-68 (diffuse colour * TF colour)
+  T p[3] = {-pos[0], -pos[1], -pos[2]};
+  const T lp = len3(p[0], p[1], p[2]);
+  T V[3] = {p[0] / lp, p[1] / lp, p[2] / lp};
+  const T d = dot3(N, V);
+  T R[3];
+  for (int i = 0; i < 3; ++i) R[i] = V[i] - (T(2) * d) * N[i];
+  const T lr = len3(R[0], R[1], R[2]);
+  for (int i = 0; i < 3; ++i) R[i] = R[i] / lr;
+  const T L[3] = {T(st.s->light_dir[0]), T(st.s->light_dir[1]), T(st.s->light_dir[2])};
+  const T diff = std::fmax(std::fabs(dot3(N, L)), T(0));
+  const T spec = pow_int_or_real(std::fmax(dot3(R, L), T(0)), 8.0f);
+  for (int i = 0; i < 3; ++i) {
+    const T dcol = T(st.light_d[i]) * tfc[i];
+    T c = T(st.light_a[i]) + dcol * diff;
+    c = c + T(st.light_s[i]) * spec;
+    out[i] = std::fmin(std::fmax(c, T(0)), T(1));
+  }
+}
+
+template <class T>
+void lighting_bp(const Setup& st, const T pos[3], const T Nin[3], const T tfc[3], T out[3]) {
+  // Blinn-Phong (selectable model): two-sided, half vector, ka/kd/ks/shininess.
+  const orc_scene& s = *st.s;
+  T p[3] = {-pos[0], -pos[1], -pos[2]};
+  const T lp = len3(p[0], p[1], p[2]);
+  T V[3] = {p[0] / lp, p[1] / lp, p[2] / lp};
+  T N[3] = {Nin[0], Nin[1], Nin[2]};
+  if (dot3(N, V) < T(0)) { N[0] = -N[0]; N[1] = -N[1]; N[2] = -N[2]; }
+  const T Lt[3] = {-T(s.light_dir[0]), -T(s.light_dir[1]), -T(s.light_dir[2])};
+  T H[3] = {Lt[0] + V[0], Lt[1] + V[1], Lt[2] + V[2]};
+  const T lh = len3(H[0], H[1], H[2]);
+  for (int i = 0; i < 3; ++i) H[i] = H[i] / lh;
+  const T diff = std::fmax(dot3(N, Lt), T(0));
+  const T spec = pow_int_or_real(std::fmax(dot3(N, H), T(0)), s.bp_shininess);
+  for (int i = 0; i < 3; ++i) {
+    T c = T(s.bp_ka) * tfc[i];
+    c = c + (T(s.bp_kd) * tfc[i]) * diff;
+    c = c + T(s.bp_ks) * spec;
+    out[i] = std::fmin(std::fmax(c, T(0)), T(1));
+  }
+}
+
+template <class T>
+void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_in,
+                 float t_out, T col[4], uint64_t& samples) {
+  const orc_scene& s = *st.s;
+  Vol<T> vol{&b, s.dtype, T(s.dtype == 0 ? 1.0f / 255.0f : 1.0f / 65535.0f)};
+  // GLRaycaster.cpp:93-99: entry eye position passes through an RGBA16F target
+  float en[3], ex[3];
+  for (int a = 0; a < 3; ++a) {
+    en[a] = orc_round_half(dir[a] * t_in);
+    ex[a] = dir[a] * t_out;
+  }
+  // GLRaycaster-1D-FS.glsl:60-69
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = std::sqrt((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row<float>(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row<float>(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float q = len / b.step;
+  const int n = int(q) + 1;
+  T inc[3], pos[3], epos[3], einc[3];
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = T(tout[a] - tin[a]) / T(q);
+    pos[a] = T(tin[a]);
+    epos[a] = T(en[a]);
+  }
+  // GLRaycaster-1D-light-FS.glsl:100-107: eye-space increment of the lit march
+  {
+    const T ddx = T(ex[0]) - T(en[0]), ddy = T(ex[1]) - T(en[1]), ddz = T(ex[2]) - T(en[2]);
+    const T l = len3(ddx, ddy, ddz);
+    einc[0] = (ddx / l) * T(b.step);
+    einc[1] = (ddy / l) * T(b.step);
+    einc[2] = (ddz / l) * T(b.step);
+  }
+  const T vstep[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
+  const bool lit = s.lighting != 0;
+  const bool two_d = s.render_mode == ORC_RM_2D;
+  const uint32_t W = s.tf_w, H = s.tf_h;
+  T c[4] = {0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    const T v = vol.sample(pos[0], pos[1], pos[2]);
+    T g[3] = {0, 0, 0};
+    if (lit || two_d) {
+      // Volume3D.glsl:43-54 (note Yp is taken at -step.y)
+      const T xp = vol.sample(pos[0] + vstep[0], pos[1], pos[2]);
+      const T xm = vol.sample(pos[0] + (-vstep[0]), pos[1], pos[2]);
+      const T yp = vol.sample(pos[0], pos[1] + (-vstep[1]), pos[2]);
+      const T ym = vol.sample(pos[0], pos[1] + vstep[1], pos[2]);
+      const T zp = vol.sample(pos[0], pos[1], pos[2] + vstep[2]);
+      const T zm = vol.sample(pos[0], pos[1], pos[2] + (-vstep[2]));
+      g[0] = (xm - xp) / T(2);
+      g[1] = (yp - ym) / T(2);
+      g[2] = (zm - zp) / T(2);
+    }
+    size_t ti;
+    if (!two_d) {
+      // VRender1D.glsl:43-47, texture1D with GL_NEAREST + clamp to edge
+      const T u = v * T(st.trans_scale);
+      T fi = std::floor(u * T(W));
+      fi = std::fmin(std::fmax(fi, T(0)), T(W - 1));
+      ti = size_t(fi);
+    } else {
+      // GLRaycaster-2D-FS.glsl:75-80
+      const T mag = len3(g[0], g[1], g[2]);
+      const T u = v * T(st.trans_scale);
+      const T w = T(1) - mag * T(st.grad_scale);
+      T fx = std::floor(u * T(W)), fy = std::floor(w * T(H));
+      fx = std::fmin(std::fmax(fx, T(0)), T(W - 1));
+      fy = std::fmin(std::fmax(fy, T(0)), T(H - 1));
+      ti = size_t(fy) * W + size_t(fx);
+    }
+    const float* e = &st.tf[4 * ti];
+    T src[4] = {T(e[0]), T(e[1]), T(e[2]), T(e[3])};
+    // VRender1D.glsl:53: opacity correction
+    src[3] = T(1) - std::pow(T(1) - src[3], T(st.step_scale));
+    if (lit) {
+      // Volume3D.glsl:56-60: normal = normalize(NormalMatrix * (g * DomainScale))
+      const T gs[3] = {g[0] * T(st.domain_scale[0]), g[1] * T(st.domain_scale[1]),
+                       g[2] * T(st.domain_scale[2])};
+      T N[3];
+      for (int r = 0; r < 3; ++r)
+        N[r] = std::fma(T(float(st.norm_mat[r][2])), gs[2],
+                        std::fma(T(float(st.norm_mat[r][1])), gs[1],
+                                 T(float(st.norm_mat[r][0])) * gs[0]));
+      const T l = len3(N[0], N[1], N[2]);
+      if (l > T(0)) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+      T lc[3];
+      const T tfc[3] = {src[0], src[1], src[2]};
+      if (s.light_model == ORC_LIGHT_BLINN_PHONG)
+        lighting_bp<T>(st, epos, N, tfc, lc);
+      else
+        lighting_ref<T>(st, epos, N, tfc, lc);
+      src[0] = lc[0]; src[1] = lc[1]; src[2] = lc[2];
+      if (two_d) {  // GLRaycaster-2D-light-FS.glsl:107
+        src[3] = std::fmin(std::fmax(src[3], T(0)), T(1));
+      }
+    }
+    // Compositing.glsl:33-38 UnderCompositing
+    const T w = T(1) - c[3];
+    c[0] = std::fma(src[0] * w, src[3], c[0]);
+    c[1] = std::fma(src[1] * w, src[3], c[1]);
+    c[2] = std::fma(src[2] * w, src[3], c[2]);
+    c[3] = std::fma(src[3], w, c[3]);
+    for (int a = 0; a < 3; ++a) {
+      pos[a] = pos[a] + inc[a];
+      epos[a] = epos[a] + einc[a];
+    }
+    if (c[3] >= T(0.99f)) break;
+  }
+  for (int a = 0; a < 4; ++a) col[a] = c[a];
+}
+
+template <class T>
+void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_t* spp,
+                  uint64_t& samples) {
+  const orc_scene& s = *st.s;
+  const View& v = st.view;
+  // gl_FragCoord at the pixel centre -> eye-space ray through it (z = -1)
+  const float nx = (float(px) + 0.5f) * v.inv_w2 - 1.0f;
+  const float ny = (float(py) + 0.5f) * v.inv_h2 - 1.0f;
+  const float dir[3] = {nx * v.kx, ny * v.ky, -1.0f};
+  float o[3], d[3];
+  for (int a = 0; a < 3; ++a) {
+    o[a] = float(v.inv[a][3]);
+    d[a] = std::fma(float(v.inv[a][2]), dir[2],
+                    std::fma(float(v.inv[a][1]), dir[1], float(v.inv[a][0]) * dir[0]));
+  }
+  float inv[3];
+  for (int a = 0; a < 3; ++a) inv[a] = 1.0f / d[a];
+  struct Hit { float t0, t1; int b; };
+  std::vector<Hit> hits;
+  for (int bi : st.visible) {
+    const BrickR& b = st.bricks[bi];
+    float tn = -INFINITY, tf = INFINITY;
+    for (int a = 0; a < 3; ++a) {
+      const float t0 = (b.pmin[a] - o[a]) * inv[a];
+      const float t1 = (b.pmax[a] - o[a]) * inv[a];
+      tn = std::fmax(tn, std::fmin(t0, t1));
+      tf = std::fmin(tf, std::fmax(t0, t1));
+    }
+    // near-plane quad (GLRaycaster.cpp:350-369) supplies the entry when the
+    // front faces are clipped; a back face behind the far plane is clipped.
+    const float ti = std::fmax(tn, s.znear);
+    if (!(tf > ti) || tf > s.zfar) continue;
+    hits.push_back({ti, tf, bi});
+  }
+  std::sort(hits.begin(), hits.end(), [](const Hit& a, const Hit& b) {
+    return a.t0 < b.t0 || (a.t0 == b.t0 && a.b < b.b);
+  });
+  T frame[4] = {0, 0, 0, 0};
+  const uint64_t before = samples;
+  for (const Hit& h : hits) {
+    if (frame[3] >= T(s.frame_ert)) break;
+    T c[4];
+    brick_march<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
+    // GLRenderer.cpp:151-153 blend (ONE_MINUS_DST_ALPHA, ONE) into RGBA32F
+    const T w = T(1) - frame[3];
+    for (int a = 0; a < 4; ++a) frame[a] = std::fma(c[a], w, frame[a]);
+  }
+  for (int a = 0; a < 4; ++a) out[a] = float(frame[a]);
+  if (spp) *spp = uint32_t(samples - before);
+}
+
+Setup build_setup(const orc_scene& s) {
+  Setup st;
+  st.s = &s;
+  const int bytes = s.dtype == 0 ? 1 : 2;
+  uint64_t lod[3 * 64], cnt[3 * 64];
+  orc_lod_table(s.dims, s.brick_size, s.overlap, lod, cnt, 64);
+  const uint64_t nb = cnt[0] * cnt[1] * cnt[2];
+  std::vector<float> ctr(3 * nb), ext(3 * nb);
+  std::vector<uint32_t> nv(3 * nb);
+  const double asp[3] = {1, 1, 1};
+  orc_brick_metadata(lod, cnt, s.brick_size, s.overlap, asp, ctr.data(), ext.data(), nv.data());
+
+  // AbstrRenderer.cpp:1003-1012: scale applied to brick metadata
+  const float us[3] = {float(s.user_scale[0]), float(s.user_scale[1]), float(s.user_scale[2])};
+  float dcs[3];
+  const float dmax = float(std::max(s.dims[0], std::max(s.dims[1], s.dims[2])));
+  for (int a = 0; a < 3; ++a) dcs[a] = us[a] * float(s.dims[a]) / dmax;
+  const float dcmax = std::max(dcs[0], std::max(dcs[1], dcs[2]));
+  float vs[3];
+  for (int a = 0; a < 3; ++a) vs[a] = us[a] / dcmax;
+
+  // data range (dataset GetRange) and TF non-zero limits
+  const uint64_t nvox = s.dims[0] * s.dims[1] * s.dims[2];
+  double rmax = 0;
+#pragma omp parallel for reduction(max : rmax)
+  for (int64_t ii = 0; ii < int64_t(nvox); ++ii) {
+    const uint64_t i = uint64_t(ii);
+    const double x = bytes == 1 ? double(static_cast<const uint8_t*>(s.raw)[i])
+                                : double(static_cast<const uint16_t*>(s.raw)[i]);
+    rmax = std::max(rmax, x);
+  }
+  // GLRenderer.cpp:1813-1819 CalculateScaling: (2^bits-1)/MaxValue
+  const uint32_t imax = (1u << (8 * bytes)) - 1;
+  st.trans_scale = float(double(imax) / rmax);
+  // GLRenderer.cpp:1840-1841: fGradientScale = 1 / MaxGradientMagnitude
+  st.grad_scale = 1.0f;
+  if (s.render_mode == ORC_RM_2D) {
+    const float mg = float(orc_max_gradient(s.raw, s.dtype, s.dims, s.brick_size, s.overlap,
+                                            s.clamp_to_edge));
+    st.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
+  }
+  const float srm = s.sample_rate_modifier;
+  st.step_scale = 1.0f / srm * 1.0f;  // GLRaycaster.cpp:257 at LOD 0
+
+  // transfer function as the GPU sees it
+  const size_t ntf = size_t(s.tf_w) * s.tf_h;
+  st.tf.assign(s.tf, s.tf + 4 * ntf);
+  if (s.tf_rgba8) {
+    // TransferFunction1D.cpp:311-330 GetByteArray (clamp, x255, truncate),
+    // sampled back as UNORM8
+    for (float& x : st.tf) {
+      const unsigned char b = (unsigned char)(std::max(0.0f, std::min(x, 1.0f)) * 255);
+      x = float(b) / 255.0f;
+    }
+  }
+  // TransferFunction1D.cpp:362-371 ComputeNonZeroLimits over alpha (1D); for 2D
+  // the value range of any non-zero alpha column.
+  uint64_t nz_lo = s.tf_w, nz_hi = 0;
+  for (uint32_t y = 0; y < s.tf_h; ++y)
+    for (uint32_t x = 0; x < s.tf_w; ++x)
+      if (st.tf[4 * (size_t(y) * s.tf_w + x) + 3] != 0) {
+        nz_lo = std::min<uint64_t>(nz_lo, x);
+        nz_hi = std::max<uint64_t>(nz_hi, x);
+      }
+  // AbstrRenderer.cpp:959-974 ContainsData for RM_1DTRANS
+  const double rescale = rmax / double(s.tf_w - 1);
+  const double lo = double(nz_lo) * rescale, hi = double(nz_hi) * rescale;
+
+  // lights (GLRenderer.cpp:2890-2893): colour.xyz * colour.w
+  for (int a = 0; a < 3; ++a) {
+    st.light_a[a] = s.ambient[a] * s.ambient[3];
+    st.light_d[a] = s.diffuse[a] * s.diffuse[3];
+    st.light_s[a] = s.specular[a] * s.specular[3];
+    st.domain_scale[a] = 1.0f / float(s.user_scale[a]);
+  }
+  st.bricks.resize(nb);
+  std::vector<char> contains_flag(nb, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t kk = 0; kk < int64_t(nb); ++kk) {
+        const uint64_t k = uint64_t(kk);
+        const uint64_t x = k % cnt[0], y = (k / cnt[0]) % cnt[1], z = k / (cnt[0] * cnt[1]);
+        BrickR& b = st.bricks[k];
+        float c[3], e[3];
+        for (int a = 0; a < 3; ++a) {
+          b.n[a] = nv[3 * k + a];
+          e[a] = ext[3 * k + a] * vs[a];
+          c[a] = ctr[3 * k + a] * vs[a];
+          b.pmin[a] = c[a] - e[a] / 2.0f;
+          b.pmax[a] = c[a] + e[a] / 2.0f;
+        }
+        // UVFDataset::GetTextCoords (uvfDataset.cpp:1766-1767)
+        for (int a = 0; a < 3; ++a) {
+          b.tmin[a] = float(s.overlap) / float(b.n[a]);
+          b.tmax[a] = 1.0f - b.tmin[a];
+        }
+        // GLRaycaster.cpp:255: step = min over axes of ext * (1/n) * 0.5 / srm
+        float stp = INFINITY;
+        for (int a = 0; a < 3; ++a) {
+          const float vsz = 1.0f / float(b.n[a]);
+          stp = std::min(stp, e[a] * vsz * 0.5f * 1.0f / srm);
+        }
+        b.step = stp;
+        const uint64_t co[3] = {x, y, z};
+        b.data.resize(size_t(b.n[0]) * b.n[1] * b.n[2] * bytes);
+        orc_lod0_brick(s.raw, s.dtype, s.dims, s.brick_size, s.overlap, s.clamp_to_edge, co,
+                       b.data.data());
+        double mn, mx;
+        orc_brick_stats(b.data.data(), s.dtype, uint64_t(b.n[0]) * b.n[1] * b.n[2], &mn, &mx);
+        contains_flag[k] = (hi >= mn && lo <= mx) ? 1 : 0;
+  }
+  for (uint64_t k = 0; k < nb; ++k)
+    if (contains_flag[k]) st.visible.push_back(int(k));
+  return st;
+}
+
+// Camera-dependent part: view and per-brick eye -> texture matrices
+// (GLRaycaster.cpp:589-612 ComputeEyeToTextureMatrix).
+void apply_view(Setup& st) {
+  st.view = make_view(*st.s);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) st.norm_mat[r][c] = st.view.mv[r][c];
+  for (BrickR& b : st.bricks) {
+    for (int a = 0; a < 3; ++a) {
+      const double sc = double((b.tmin[a] - b.tmax[a]) / (b.pmin[a] - b.pmax[a]));
+      for (int j = 0; j < 3; ++j) b.tex[a][j] = float(sc * st.view.inv[a][j]);
+      b.tex[a][3] = float(sc * (st.view.inv[a][3] - double(b.pmax[a])) + double(b.tmax[a]));
+    }
+  }
+}
+
+struct Prepared {
+  orc_scene scene;  // volume/TF/mode part; the camera part is replaced per render
+  Setup st;
+};
+
+uint64_t march_all(Setup& st, float* out, uint32_t* spp, double* march_s) {
+  const orc_scene& s = *st.s;
+#ifdef _OPENMP
+  if (s.threads > 0) omp_set_num_threads(s.threads);
+#endif
+  apply_view(st);
+  const auto t1 = std::chrono::steady_clock::now();
+  const uint32_t stride = s.row_stride ? s.row_stride : 1;
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+  for (int64_t py = 0; py < int64_t(s.height); ++py) {
+    if (uint32_t(py) % stride != s.row_phase % stride) continue;
+    uint64_t local = 0;
+    for (uint32_t px = 0; px < s.width; ++px) {
+      const size_t i = size_t(py) * s.width + px;
+      if (s.use_double)
+        render_pixel<double>(st, px, uint32_t(py), out + 4 * i, spp ? spp + i : nullptr, local);
+      else
+        render_pixel<float>(st, px, uint32_t(py), out + 4 * i, spp ? spp + i : nullptr, local);
+    }
+    total += local;
+  }
+  const auto t2 = std::chrono::steady_clock::now();
+  if (march_s) *march_s = std::chrono::duration<double>(t2 - t1).count();
+  return total;
+}
+
+}  // namespace
+
+extern "C" uint64_t orc_render_timed(const orc_scene* sc, float* out, uint32_t* spp,
+                                     double* setup_s, double* march_s) {
+#ifdef _OPENMP
+  if (sc->threads > 0) omp_set_num_threads(sc->threads);
+#endif
+  const auto t0 = std::chrono::steady_clock::now();
+  Setup st = build_setup(*sc);
+  const auto t1 = std::chrono::steady_clock::now();
+  if (setup_s) *setup_s = std::chrono::duration<double>(t1 - t0).count();
+  return march_all(st, out, spp, march_s);
+}
+
+extern "C" uint64_t orc_render(const orc_scene* sc, float* out, uint32_t* spp) {
+  return orc_render_timed(sc, out, spp, nullptr, nullptr);
+}
+
+extern "C" void* orc_prepare(const orc_scene* sc) {
+#ifdef _OPENMP
+  if (sc->threads > 0) omp_set_num_threads(sc->threads);
+#endif
+  Prepared* p = new Prepared();
+  p->scene = *sc;
+  p->st = build_setup(p->scene);
+  p->st.s = &p->scene;
+  return p;
+}
+
+extern "C" uint64_t orc_render_prepared(void* h, const orc_scene* cam, float* out,
+                                        uint32_t* spp, double* march_s) {
+  Prepared* p = static_cast<Prepared*>(h);
+  orc_scene& s = p->scene;
+  for (int a = 0; a < 3; ++a) {
+    s.eye[a] = cam->eye[a];
+    s.at[a] = cam->at[a];
+    s.up[a] = cam->up[a];
+  }
+  s.fovy_deg = cam->fovy_deg;
+  s.znear = cam->znear;
+  s.zfar = cam->zfar;
+  s.width = cam->width;
+  s.height = cam->height;
+  s.row_stride = cam->row_stride;
+  s.row_phase = cam->row_phase;
+  s.threads = cam->threads;
+  s.use_double = cam->use_double;
+  return march_all(p->st, out, spp, march_s);
+}
+
+extern "C" void orc_release(void* h) { delete static_cast<Prepared*>(h); }

@@ -1,0 +1,67 @@
+"""Binding of oracle/_ref/libtuvok_ref.so: the reference's own
+ExtendedOctreeConverter, built from the reference sources by oracle/ref/Makefile.
+
+Present only where the reference sources were available at build time; tests
+that need it skip otherwise.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PATH = Path(__file__).resolve().parent.parent / "oracle" / "_ref" / "libtuvok_ref.so"
+_lib = None
+
+
+def available():
+    return PATH.exists()
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(str(PATH))
+        L.ref_convert.restype = C.c_void_p
+        L.ref_convert.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
+                                  C.POINTER(C.c_uint32), C.c_uint32, C.c_int, C.c_int, C.c_char_p]
+        L.ref_brick_count.argtypes = [C.c_void_p]
+        L.ref_brick_count.restype = C.c_uint64
+        L.ref_lod_count.argtypes = [C.c_void_p]
+        L.ref_lod_count.restype = C.c_uint64
+        L.ref_brick_info.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint64), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
+        L.ref_brick_info.restype = None
+        L.ref_brick_data.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
+        L.ref_brick_data.restype = None
+        L.ref_free.argtypes = [C.c_void_p]
+        L.ref_free.restype = None
+        _lib = L
+    return _lib
+
+
+def convert(raw, brick_size, overlap, clamp=False, median=False, scratch="/tmp"):
+    """Runs the reference converter on raw ([z, y, x]); returns a list of dicts
+    {coords: (x, y, z, lod), size: (x, y, z), min, max, data: [z, y, x]}."""
+    L = _load()
+    raw = np.ascontiguousarray(raw)
+    dims = (C.c_uint64 * 3)(raw.shape[2], raw.shape[1], raw.shape[0])
+    h = L.ref_convert(raw.ctypes.data_as(C.c_void_p), 0 if raw.dtype == np.uint8 else 1, dims,
+                      (C.c_uint32 * 3)(*brick_size), overlap, int(clamp), int(median),
+                      scratch.encode())
+    if not h:
+        raise RuntimeError("reference conversion failed")
+    out = []
+    try:
+        for i in range(L.ref_brick_count(h)):
+            c = (C.c_uint64 * 4)()
+            s = (C.c_uint64 * 3)()
+            mn, mx = C.c_double(), C.c_double()
+            L.ref_brick_info(h, i, c, s, C.byref(mn), C.byref(mx))
+            data = np.zeros((s[2], s[1], s[0]), dtype=raw.dtype)
+            L.ref_brick_data(h, i, data.ctypes.data_as(C.c_void_p))
+            out.append({"coords": tuple(c), "size": tuple(s), "min": mn.value, "max": mx.value,
+                        "data": data})
+    finally:
+        L.ref_free(h)
+    return out

@@ -1,0 +1,115 @@
+"""GPU bricking through the C ABI against the reference and the oracle.
+
+Bit-exact: every LOD-0 brick (ghost voxels included) equals the brick the
+reference's own ExtendedOctreeConverter wrote (tests/golden fixtures), per-brick
+min/max equals its statistics, the global histogram counts every voxel once,
+per-brick histograms, brick metadata and the maximum gradient magnitude equal
+the oracle's.  Voxels the reference leaves undefined (a clamped brick whose
+scanline read runs past the end of the file keeps the previous brick's bytes)
+are excluded; the GPU writes the clamped value of zero there.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from tuvok_gb300 import Volume
+from tuvok_gb300.workloads import PLAIN_SMALL, numpy_blob_volume
+from test_oracle_golden import FIXTURES, load, past_eof_mask
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_gpu_bricks_equal_reference_converter(cuda_ok, path):
+    d, dims, bsize, ov, clamp = load(path)
+    raw = d["raw"]
+    vol = Volume(raw, brick_size=bsize, overlap=ov, clamp_to_edge=clamp)
+    lod_sizes, lod_counts = O.lod_table(dims, bsize, ov)
+    assert vol.GetLODLevelCount() == len(lod_sizes)
+    assert vol.GetBrickLayout(0) == lod_counts[0]
+    for lod in range(len(lod_sizes)):
+        assert vol.GetDomainSize(lod) == lod_sizes[lod]
+        assert vol.GetBrickLayout(lod) == lod_counts[lod]
+    for i, c in enumerate(d["coords"]):
+        if c[3] != 0:
+            continue
+        idx = vol.IndexFrom4D(c[0], c[1], c[2], 0)
+        assert vol.IndexTo4D(0, idx) == (c[0], c[1], c[2], 0)
+        b = vol.GetBrick((0, 0, idx))
+        ref = d[f"brick{i}"]
+        assert b.shape == ref.shape
+        undefined = np.zeros(b.shape, dtype=bool)
+        if clamp:
+            undefined = past_eof_mask(dims, bsize, ov, lod_counts[0], c[:3], b.shape)
+        np.testing.assert_array_equal(b[~undefined], ref[~undefined], err_msg=str(tuple(c)))
+        mm = vol.MaxMinForKey((0, 0, idx))
+        if not undefined.any():
+            assert (mm.min_scalar, mm.max_scalar) == tuple(d["minmax"][i])
+        assert (mm.min_scalar, mm.max_scalar) == O.brick_stats(b)
+    h, n = vol.GetHistogram()
+    np.testing.assert_array_equal(h, np.bincount(raw.reshape(-1).astype(np.int64),
+                                                 minlength=h.size))
+    assert n == int(raw.max()) + 1
+    assert vol.GetRange() == (float(raw.min()), float(raw.max()))
+
+
+@pytest.mark.parametrize("dims,dtype,bs,ov,clamp", [
+    ((37, 29, 23), np.uint8, 16, 1, False),
+    ((37, 29, 23), np.uint16, 16, 1, True),
+    ((70, 40, 33), np.uint16, 34, 1, False),
+    ((25, 14, 13), np.uint8, 16, 2, False),
+    ((64, 64, 64), np.uint8, 66, 1, False),  # one brick per axis
+])
+def test_gpu_statistics_equal_oracle(cuda_ok, dims, dtype, bs, ov, clamp):
+    vmax = 255 if dtype == np.uint8 else 4095
+    raw = numpy_blob_volume(dims, dtype, 6, (3, 9), (vmax * 0.3, vmax * 0.9), vmax, seed=11,
+                            noise=3)
+    vol = Volume(raw, brick_size=(bs, bs, bs), overlap=ov, clamp_to_edge=clamp)
+    sizes, counts = O.lod_table(dims, (bs, bs, bs), ov)
+    c, e, n = O.brick_metadata(sizes[0], counts[0], (bs, bs, bs), ov)
+    hist, shift = vol.GetBrickHistograms()
+    assert shift == max(0, int(raw.max()).bit_length() - 8)
+    nb = counts[0][0] * counts[0][1] * counts[0][2]
+    for k in range(nb):
+        x, y, z, _ = vol.IndexTo4D(0, k)
+        ob = O.lod0_brick(raw, (bs, bs, bs), ov, clamp, (x, y, z))
+        gb = vol.GetBrick((0, 0, k))
+        np.testing.assert_array_equal(gb, ob)
+        md = vol.GetBrickMetadata((0, 0, k))
+        assert tuple(md.center) == tuple(c[k]) and tuple(md.extents) == tuple(e[k])
+        assert tuple(md.n_voxels) == tuple(n[k])
+        np.testing.assert_array_equal(hist[k], O.brick_hist256(ob, ov, shift))
+    mg = O.max_gradient(raw, (bs, bs, bs), ov, clamp)
+    assert vol.MaxGradientMagnitude() == float(np.float32(mg))
+
+
+def test_gpu_bricking_plain_small_full_size(cuda_ok):
+    """The 256^3 uint8 configuration at full size: every brick bit-exact."""
+    w = PLAIN_SMALL
+    raw = numpy_blob_volume((128, 128, 128), np.uint8, 16, (4, 20), (64, 255), 255, seed=5,
+                            noise=4)
+    raw = np.tile(raw, (2, 2, 2))  # 256^3 from a cheaper 128^3 source
+    vol = Volume(raw, brick_size=w.brick_size, overlap=w.overlap)
+    assert vol.GetBrickCount(0) == 64
+    assert sum(np.prod(vol.GetBrickLayout(l)) for l in range(vol.GetLODLevelCount())) == 79
+    for k in range(64):
+        x, y, z, _ = vol.IndexTo4D(0, k)
+        ob = O.lod0_brick(raw, w.brick_size, w.overlap, False, (x, y, z))
+        np.testing.assert_array_equal(vol.GetBrick((0, 0, k)), ob)
+        mm = vol.MaxMinForKey((0, 0, k))
+        assert (mm.min_scalar, mm.max_scalar) == O.brick_stats(ob)
+
+
+def test_gpu_brick_key_errors(cuda_ok):
+    raw = np.zeros((8, 8, 8), dtype=np.uint8)
+    vol = Volume(raw, brick_size=(6, 6, 6), overlap=1)
+    from tuvok_gb300 import TvkError
+    with pytest.raises(TvkError):
+        vol.GetBrick((0, 0, 10 ** 6))
+    with pytest.raises(TvkError) as e:
+        vol.GetBrick((0, 1, 0))
+    assert "UNSUPPORTED" in str(e.value)
+    with pytest.raises(TvkError):
+        vol.IndexFrom4D(9, 0, 0, 0)

@@ -1,0 +1,146 @@
+"""The CPU oracle's bricking half, pinned against the reference.
+
+* IO/test/rebricking.h golden vectors (8x8x1 uint16 ramp, brick 16, overlap 2:
+  12x12x5 bricks, inner voxels equal the ramp, min/max including ghost);
+* fixtures made by the reference's own ExtendedOctreeConverter
+  (tests/golden/make_golden.py): every LOD-0 brick and its statistics;
+* the live reference converter on fresh random inputs, where it was built.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+import refconv
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+FIXTURES = sorted(GOLDEN.glob("*.npz"))
+
+
+def load(path):
+    d = np.load(path)
+    x, y, z, bs, ov, clamp = (int(v) for v in d["meta"])
+    return d, (x, y, z), (bs, bs, bs), ov, bool(clamp)
+
+
+def test_rebricking_h_ramp():
+    # IO/test/rebricking.h:12-35, 214-242
+    raw = np.arange(64, dtype=np.uint16).reshape(1, 8, 8)
+    sizes, counts = O.lod_table((8, 8, 1), (16, 16, 16), 2)
+    assert sizes[0] == (8, 8, 1) and counts[0] == (1, 1, 1)
+    assert len(sizes) == 4  # 8 -> 4 -> 2 -> 1, one brick each
+    b = O.lod0_brick(raw, (16, 16, 16), 2, False, (0, 0, 0))
+    assert b.shape == (5, 12, 12)  # rebricking.h:223-225 (x=12, y=12, z=5)
+    assert (b[2, 2:10, 2:10] == raw[0]).all()  # rebricking.h:176-187
+    assert O.brick_stats(b) == (0.0, 63.0)  # min 0 from the zero ghost
+    # everything outside the inner 8x8x1 is ghost and zero without clamping
+    m = np.ones_like(b, dtype=bool)
+    m[2, 2:10, 2:10] = False
+    assert (b[m] == 0).all()
+
+
+def test_lod_tables_of_the_configs():
+    # 256^3 at brick 66/overlap 1 -> 9 LODs, 79 bricks;
+    # 1024^3 at brick 130/overlap 1 -> 11 LODs, 592 bricks
+    s, c = O.lod_table((256, 256, 256), (66, 66, 66), 1)
+    assert len(s) == 9 and sum(a * b * d for a, b, d in c) == 79
+    s, c = O.lod_table((1024, 1024, 1024), (130, 130, 130), 1)
+    assert len(s) == 11 and sum(a * b * d for a, b, d in c) == 592
+
+
+def past_eof_mask(dims, bsize, ov, counts, coords, shape):
+    """Voxels whose scanline read in GetInputBrick (ExtendedOctreeConverter.cpp:
+    288-373) starts past the end of the raw file.  Without clamping the brick
+    buffer was zeroed first, so they read 0; with clamping the reference leaves
+    whatever the previous brick left in its reused buffer there (undefined), and
+    ClampToEdge (:376-462) copies such voxels on into the border planes."""
+    nz, ny, nx = shape
+    core = [b - 2 * ov for b in bsize]
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    g = []
+    inside = np.ones(shape, dtype=bool)
+    for a, loc in enumerate((i, j, k)):
+        first, last = coords[a] == 0, coords[a] == counts[a] - 1
+        if first:
+            loc = np.maximum(loc, ov)
+        if last:
+            loc = np.minimum(loc, shape[2 - a] - 1 - ov)
+        s = ov if first else 0
+        e = shape[2 - a] - (ov if last else 0)
+        inside &= (loc >= s) & (loc < e)
+        g.append(coords[a] * core[a] + loc - ov)
+    lin = g[0] + g[1] * dims[0] + g[2] * dims[0] * dims[1]
+    return inside & (lin >= dims[0] * dims[1] * dims[2])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_oracle_lod0_equals_reference_converter(path):
+    d, dims, bsize, ov, clamp = load(path)
+    raw = d["raw"]
+    coords, sizes, minmax = d["coords"], d["sizes"], d["minmax"]
+    lod_sizes, lod_counts = O.lod_table(dims, bsize, ov)
+    # the converter's brick list covers every LOD of the oracle's table
+    assert len(coords) == sum(a * b * c for a, b, c in lod_counts)
+    n0 = 0
+    for i, c in enumerate(coords):
+        if c[3] != 0:
+            continue
+        n0 += 1
+        b = O.lod0_brick(raw, bsize, ov, clamp, tuple(c[:3]))
+        assert b.shape == tuple(sizes[i][::-1])
+        ref = d[f"brick{i}"]
+        undefined = np.zeros(b.shape, dtype=bool)
+        if clamp:
+            undefined = past_eof_mask(dims, bsize, ov, lod_counts[0], c[:3], b.shape)
+        np.testing.assert_array_equal(b[~undefined], ref[~undefined], err_msg=f"brick {tuple(c)}")
+        if not undefined.any():
+            assert O.brick_stats(b) == tuple(minmax[i])
+    assert n0 == lod_counts[0][0] * lod_counts[0][1] * lod_counts[0][2]
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_oracle_histogram_counts_every_voxel_once(path):
+    d, dims, bsize, ov, clamp = load(path)
+    raw = d["raw"]
+    h, n = O.histogram1d(raw, bsize, ov)
+    ref = np.bincount(raw.reshape(-1).astype(np.int64), minlength=h.size)
+    np.testing.assert_array_equal(h, ref)
+    assert n == int(raw.max()) + 1
+
+
+def test_oracle_metadata_tiles_the_unit_box():
+    sizes, counts = O.lod_table((37, 29, 23), (16, 16, 16), 1)
+    c, e, n = O.brick_metadata(sizes[0], counts[0], (16, 16, 16), 1)
+    lo = (c - e / 2).min(axis=0)
+    hi = (c + e / 2).max(axis=0)
+    norm = np.array([37, 29, 23]) / 37.0
+    np.testing.assert_allclose(lo, -norm / 2, atol=1e-6)
+    np.testing.assert_allclose(hi, norm / 2, atol=1e-6)
+    assert (n[:, 0] <= 16).all()
+
+
+@pytest.mark.skipif(not refconv.available(), reason="reference converter not built here")
+@pytest.mark.parametrize("dims,dtype,bs,ov,clamp", [
+    ((50, 20, 17), np.uint8, 18, 1, False),
+    ((50, 20, 17), np.uint16, 18, 1, True),
+    ((31, 31, 9), np.uint16, 10, 3, False),
+])
+def test_oracle_matches_live_reference(dims, dtype, bs, ov, clamp, tmp_path):
+    rng = np.random.default_rng(7)
+    raw = rng.integers(0, 200, size=dims[::-1]).astype(dtype)
+    bricks = refconv.convert(raw, (bs, bs, bs), ov, clamp=clamp, scratch=str(tmp_path))
+    for b in bricks:
+        if b["coords"][3] != 0:
+            continue
+        mine = O.lod0_brick(raw, (bs, bs, bs), ov, clamp, b["coords"][:3])
+        np.testing.assert_array_equal(mine, b["data"])
+        assert O.brick_stats(mine) == (b["min"], b["max"])
+
+
+def test_round_half_is_ieee_rne():
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.normal(0, 2, 2000), rng.uniform(-70000, 70000, 200),
+                         [1e-8, 3e-8, 6e-5, 65504.0, 65519.99, 65520.0, 0.0, -0.0]])
+    for x in xs.astype(np.float32):
+        assert O.round_half(x) == float(np.float32(np.float16(x))), x

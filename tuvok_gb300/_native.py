@@ -1,0 +1,126 @@
+"""ctypes binding of libtvk.so (the C ABI declared in include/tvk.h).
+
+The library is built in-tree by ``tuvok_gb300.build``.  There is no fallback:
+if the shared library is missing or fails to load, importing this module
+raises, so nothing silently runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libtvk.so"
+
+TVK_OK = 0
+TVK_U8, TVK_U16 = 0, 1
+TVK_RM_1DTRANS, TVK_RM_2DTRANS, TVK_RM_ISOSURFACE = 0, 1, 2
+TVK_LIGHT_REFERENCE, TVK_LIGHT_BLINN_PHONG = 0, 1
+
+STATUS_NAMES = {0: "TVK_OK", 1: "TVK_ERR_INVALID_ARG", 2: "TVK_ERR_CUDA",
+                3: "TVK_ERR_OUT_OF_MEMORY", 4: "TVK_ERR_UNSUPPORTED", 5: "TVK_ERR_STATE",
+                6: "TVK_ERR_INTERNAL"}
+
+
+class TvkError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class BrickMD(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("extents", C.c_float * 3),
+                ("n_voxels", C.c_uint32 * 3)]
+
+
+class MinMax(C.Structure):
+    _fields_ = [("min_scalar", C.c_double), ("max_scalar", C.c_double),
+                ("min_gradient", C.c_double), ("max_gradient", C.c_double)]
+
+
+class VolumeInfo(C.Structure):
+    _fields_ = [("dims", C.c_uint64 * 3), ("dtype", C.c_int), ("bit_width", C.c_uint32),
+                ("brick_size", C.c_uint32 * 3), ("overlap", C.c_uint32),
+                ("lod_count", C.c_uint32), ("lod0_bricks", C.c_uint64),
+                ("range_min", C.c_double), ("range_max", C.c_double),
+                ("max_gradient", C.c_double), ("device_bytes", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
+                ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("last_paint_ms", C.c_float)]
+
+
+_u64p = C.POINTER(C.c_uint64)
+_u32p = C.POINTER(C.c_uint32)
+_f32p = C.POINTER(C.c_float)
+_vp = C.c_void_p
+
+# name -> argtypes (every function returns tvk_status unless listed in _RET)
+PROTOTYPES = {
+    "tvk_status_string": [C.c_int],
+    "tvk_last_error": [],
+    "tvk_abi_version": [],
+    "tvk_volume_create": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, C.POINTER(_vp)],
+    "tvk_volume_create_device": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, C.POINTER(_vp)],
+    "tvk_volume_destroy": [_vp],
+    "tvk_volume_get_info": [_vp, C.POINTER(VolumeInfo)],
+    "tvk_volume_get_lod": [_vp, C.c_uint32, _u64p, _u64p],
+    "tvk_volume_get_brick_md": [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(BrickMD)],
+    "tvk_volume_get_brick": [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _vp, C.c_size_t],
+    "tvk_volume_get_minmax": [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(MinMax)],
+    "tvk_volume_get_histogram": [_vp, _u64p, C.c_size_t, _u64p],
+    "tvk_volume_get_brick_histograms": [_vp, _u32p, C.c_size_t, _u32p],
+    "tvk_volume_index_from_4d": [_vp, _u64p, _u64p],
+    "tvk_volume_index_to_4d": [_vp, C.c_uint64, C.c_uint64, _u64p],
+    "tvk_renderer_create": [C.POINTER(_vp)],
+    "tvk_renderer_destroy": [_vp],
+    "tvk_renderer_set_volume": [_vp, _vp],
+    "tvk_set_tf1d_rgba8": [_vp, C.POINTER(C.c_uint8), C.c_uint32],
+    "tvk_set_tf1d_float": [_vp, _f32p, C.c_uint32, C.c_int],
+    "tvk_set_tf2d_float": [_vp, _f32p, C.c_uint32, C.c_uint32, C.c_int],
+    "tvk_set_render_mode": [_vp, C.c_int],
+    "tvk_set_lighting": [_vp, C.c_int],
+    "tvk_set_sample_rate_modifier": [_vp, C.c_float],
+    "tvk_set_isovalue": [_vp, C.c_float],
+    "tvk_set_colors": [_vp, _f32p, _f32p, _f32p, _f32p],
+    "tvk_set_light_model": [_vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float],
+    "tvk_set_view": [_vp, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_float],
+    "tvk_set_model_transform": [_vp, _f32p, _f32p],
+    "tvk_resize": [_vp, C.c_uint32, C.c_uint32],
+    "tvk_set_frame_termination": [_vp, C.c_float],
+    "tvk_paint": [_vp],
+    "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
+    "tvk_read_image": [_vp, _f32p, C.c_size_t],
+    "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],
+    "tvk_renderer_get_stream": [_vp, C.POINTER(_vp)],
+    "tvk_get_stats": [_vp, C.POINTER(Stats)],
+    "tvk_generate_volume": [_vp, C.c_int, _u64p, _f32p, C.c_uint32, C.c_float, C.c_uint32,
+                            C.c_float, C.c_uint64, C.c_int, C.c_float],
+}
+_RET = {"tvk_status_string": C.c_char_p, "tvk_last_error": C.c_char_p,
+        "tvk_abi_version": C.c_int}
+
+_lib = None
+
+
+def lib():
+    """Loads libtvk.so once; raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(str(LIB_PATH))
+        for name, args in PROTOTYPES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RET.get(name, C.c_int)
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != TVK_OK:
+        msg = lib().tvk_last_error().decode(errors="replace")
+        raise TvkError(status, msg)

@@ -1,0 +1,1078 @@
+// api.cpp -- C ABI of tuvok_gb300: volumes (GPU bricking) and renderers (GPU
+// ray march) with the host-side planning of Tuvok's AbstrRenderer.
+//
+// Host arithmetic that feeds the kernels (brick metadata, texture matrices, step
+// sizes, transfer-function tables) follows the reference's own evaluation order
+// and is compiled with -ffp-contract=off, so the values handed to the GPU do not
+// depend on the host compiler or CPU.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tvk_internal.h"
+
+namespace tvk {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void fail(tvk_status s, const std::string& msg) { throw Error{s, msg}; }
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  const tvk_status s = (e == cudaErrorMemoryAllocation) ? TVK_ERR_OUT_OF_MEMORY : TVK_ERR_CUDA;
+  fail(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class F>
+tvk_status guarded(F&& f) {
+  try {
+    f();
+    g_last_error.clear();
+    return TVK_OK;
+  } catch (const Error& e) {
+    g_last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return TVK_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return TVK_ERR_INTERNAL;
+  } catch (...) {
+    g_last_error = "unknown failure";
+    return TVK_ERR_INTERNAL;
+  }
+}
+
+#define REQUIRE(cond, msg) \
+  do {                     \
+    if (!(cond)) ::tvk::fail(TVK_ERR_INVALID_ARG, msg); \
+  } while (0)
+
+// Device buffer owned by RAII.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void ensure(size_t n) {
+    if (n <= bytes && p) return;
+    release();
+    TVK_CUDA(cudaMalloc(&p, n ? n : 1));
+    bytes = n;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() { if (p) cudaFreeHost(p); }
+  void ensure(size_t n) {
+    if (n <= bytes && p) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    TVK_CUDA(cudaMallocHost(&p, n ? n : 1));
+    bytes = n;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ------------------------------------------------------------ LOD / metadata
+
+// ExtendedOctree::ComputeMetadata (IO/UVF/ExtendedOctree/ExtendedOctree.cpp:188-243).
+std::vector<LodInfo> lod_table(const uint64_t dims[3], const uint32_t B[3], uint32_t ov) {
+  std::vector<LodInfo> t;
+  uint64_t v[3] = {dims[0], dims[1], dims[2]};
+  double asp[3] = {1, 1, 1};
+  const uint64_t usable[3] = {B[0] - 2ull * ov, B[1] - 2ull * ov, B[2] - 2ull * ov};
+  do {
+    LodInfo l;
+    if (!t.empty()) {
+      for (int a = 0; a < 3; ++a) {
+        if (v[a] > 1) {
+          const uint64_t h = uint64_t(std::ceil(v[a] / 2.0));
+          asp[a] *= (v[a] % 2) ? double(float(v[a]) / float(h)) : 2.0;
+          v[a] = h;
+        }
+      }
+      const double m = std::max(asp[0], std::max(asp[1], asp[2]));
+      for (int a = 0; a < 3; ++a) asp[a] /= m;
+    }
+    for (int a = 0; a < 3; ++a) {
+      l.size[a] = v[a];
+      l.bricks[a] = uint64_t(std::ceil(v[a] / double(usable[a])));
+      l.aspect[a] = asp[a];
+    }
+    t.push_back(l);
+  } while (v[0] > 1 || v[1] > 1 || v[2] > 1);
+  return t;
+}
+
+// ExtendedOctree::ComputeBrickSize (ExtendedOctree.cpp:276-285).
+void brick_size(const LodInfo& l, const uint32_t B[3], uint32_t ov, const uint64_t c[3],
+                uint32_t out[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const uint64_t core = B[a] - 2ull * ov;
+    const bool last = c[a] == l.bricks[a] - 1;
+    out[a] = uint32_t((last && (l.size[a] % core)) ? (2ull * ov + l.size[a] % core) : B[a]);
+  }
+}
+
+// UVFDataset::ComputeMetadataTOC (IO/uvfDataset.cpp:242-288): x, y, z loop
+// order, corner accumulated in float.
+void brick_metadata(const LodInfo& l, const uint32_t B[3], uint32_t ov,
+                    std::vector<tvk_brick_md>& md) {
+  md.assign(l.bricks[0] * l.bricks[1] * l.bricks[2], tvk_brick_md{});
+  const float asp[3] = {float(l.aspect[0]), float(l.aspect[1]), float(l.aspect[2])};
+  float nd[3] = {float(l.size[0]) * asp[0], float(l.size[1]) * asp[1], float(l.size[2]) * asp[2]};
+  const float maxv = std::max(nd[0], std::max(nd[1], nd[2]));
+  for (int a = 0; a < 3; ++a) nd[a] /= maxv;
+  float corner[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
+  for (uint64_t x = 0; x < l.bricks[0]; ++x) {
+    corner[1] = 0;
+    for (uint64_t y = 0; y < l.bricks[1]; ++y) {
+      corner[2] = 0;
+      for (uint64_t z = 0; z < l.bricks[2]; ++z) {
+        const uint64_t c[3] = {x, y, z};
+        uint32_t bs[3];
+        brick_size(l, B, ov, c, bs);
+        tvk_brick_md& m = md[z * l.bricks[0] * l.bricks[1] + y * l.bricks[0] + x];
+        for (int a = 0; a < 3; ++a) {
+          ext[a] = float(bs[a] - 2u * ov) * asp[a] / maxv;
+          m.center[a] = (corner[a] + ext[a] / 2.0f) - nd[a] * 0.5f;
+          m.extents[a] = ext[a];
+          m.n_voxels[a] = bs[a];
+        }
+        corner[2] += ext[2];
+      }
+      corner[1] += ext[1];
+    }
+    corner[0] += ext[0];
+  }
+}
+
+uint32_t bits_of(uint64_t v) {
+  uint32_t b = 0;
+  while (v) { ++b; v >>= 1; }
+  return b;
+}
+
+// ------------------------------------------------------------ volume build
+
+void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
+  const uint64_t nvox = V->dims[0] * V->dims[1] * V->dims[2];
+  uint64_t launches = 0;
+  V->lods = lod_table(V->dims, V->brick_size, V->overlap);
+  const LodInfo& l0 = V->lods[0];
+  V->n_bricks = l0.bricks[0] * l0.bricks[1] * l0.bricks[2];
+  REQUIRE(V->n_bricks < (1ull << 31), "too many bricks");
+  brick_metadata(l0, V->brick_size, V->overlap, V->md);
+  V->offsets.resize(V->n_bricks);
+  V->sizes.resize(3 * V->n_bricks);
+  const uint64_t align = 256 / V->bytes;  // brick starts on 256-byte boundaries
+  uint64_t off = 0;
+  uint32_t max_bz = 0;
+  for (uint64_t b = 0; b < V->n_bricks; ++b) {
+    for (int a = 0; a < 3; ++a) V->sizes[3 * b + a] = V->md[b].n_voxels[a];
+    max_bz = std::max(max_bz, V->md[b].n_voxels[2]);
+    V->offsets[b] = off;
+    const uint64_t n = uint64_t(V->sizes[3 * b]) * V->sizes[3 * b + 1] * V->sizes[3 * b + 2];
+    off += (n + align - 1) / align * align;
+  }
+  V->pool_bytes = off * V->bytes;
+  TVK_CUDA(cudaMalloc(&V->d_pool, V->pool_bytes));
+
+  DevBuf d_off, d_sizes, d_scratch;
+  d_off.ensure(V->n_bricks * sizeof(uint64_t));
+  d_sizes.ensure(V->n_bricks * 3 * sizeof(uint32_t));
+  TVK_CUDA(cudaMemcpyAsync(d_off.p, V->offsets.data(), V->n_bricks * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->n_bricks * 3 * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+  // scratch: bmin, bmax, bhist, hist, max_grad bits, raw min/max
+  const uint64_t gbins = uint64_t(1) << (8 * V->bytes);
+  const size_t sz_bmin = V->n_bricks * 4, sz_bh = V->n_bricks * 256 * 4, sz_h = gbins * 8;
+  const size_t total = 2 * sz_bmin + sz_bh + sz_h + 8 + 8 + 64;
+  d_scratch.ensure(total);
+  uint8_t* base = d_scratch.as<uint8_t>();
+  BrickScratch sc;
+  sc.hist = reinterpret_cast<unsigned long long*>(base);
+  sc.max_grad_bits = reinterpret_cast<unsigned long long*>(base + sz_h);
+  sc.raw_minmax = reinterpret_cast<uint32_t*>(base + sz_h + 8);
+  sc.bmin = reinterpret_cast<uint32_t*>(base + sz_h + 16);
+  sc.bmax = sc.bmin + V->n_bricks;
+  sc.bhist = sc.bmax + V->n_bricks;
+  TVK_CUDA(cudaMemsetAsync(sc.hist, 0, sz_h, s));
+  TVK_CUDA(cudaMemsetAsync(sc.bmin, 0xff, sz_bmin, s));
+  TVK_CUDA(cudaMemsetAsync(sc.bmax, 0, sz_bmin, s));
+  TVK_CUDA(cudaMemsetAsync(sc.bhist, 0, sz_bh, s));
+
+  // pass 1: data range (Dataset::GetRange), needed for the per-brick bin shift
+  launch_raw_minmax(d_raw, V->bytes, nvox, sc.raw_minmax, s, &launches);
+  uint32_t mm[2];
+  TVK_CUDA(cudaMemcpyAsync(mm, sc.raw_minmax, sizeof(mm), cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaStreamSynchronize(s));
+  V->range_min = mm[0];
+  V->range_max = mm[1];
+  const uint32_t b = bits_of(mm[1]);
+  V->hist_shift = b > 8 ? b - 8 : 0;
+
+  // pass 2: bricks + statistics + histograms
+  BrickGrid g;
+  for (int a = 0; a < 3; ++a) {
+    g.dims[a] = V->dims[a];
+    g.B[a] = V->brick_size[a];
+    g.cnt[a] = uint32_t(l0.bricks[a]);
+  }
+  g.ov = V->overlap;
+  g.clamp = V->clamp ? 1 : 0;
+  g.total = nvox;
+  launch_brick_lod0(d_raw, V->bytes, g, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                    V->n_bricks, V->d_pool, sc, V->hist_shift, uint32_t(mm[1]) + 1, s, &launches);
+  // pass 3: maximum gradient magnitude over inner voxels
+  launch_max_gradient(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                      V->n_bricks, V->overlap, max_bz, sc.max_grad_bits, s, &launches);
+
+  std::vector<uint32_t> bmin(V->n_bricks), bmax(V->n_bricks);
+  V->hist.resize(gbins);
+  V->bhist.resize(V->n_bricks * 256);
+  unsigned long long mg = 0;
+  TVK_CUDA(cudaMemcpyAsync(bmin.data(), sc.bmin, sz_bmin, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaMemcpyAsync(bmax.data(), sc.bmax, sz_bmin, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaMemcpyAsync(V->hist.data(), sc.hist, sz_h, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaMemcpyAsync(V->bhist.data(), sc.bhist, sz_bh, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaMemcpyAsync(&mg, sc.max_grad_bits, 8, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaStreamSynchronize(s));
+  V->bmin.resize(V->n_bricks);
+  V->bmax.resize(V->n_bricks);
+  for (uint64_t i = 0; i < V->n_bricks; ++i) {
+    V->bmin[i] = bmin[i];
+    V->bmax[i] = bmax[i];
+  }
+  double mgd;
+  std::memcpy(&mgd, &mg, 8);
+  V->max_grad = mgd;
+  uint64_t len = gbins;
+  while (len > 0 && V->hist[len - 1] == 0) --len;
+  V->hist_trimmed = len;
+}
+
+tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, const uint64_t dims[3],
+                          const uint32_t bsz[3], uint32_t ov, int clamp) {
+  REQUIRE(src && dims && bsz, "null argument");
+  REQUIRE(dtype == TVK_U8 || dtype == TVK_U16, "dtype must be TVK_U8 or TVK_U16");
+  for (int a = 0; a < 3; ++a) {
+    REQUIRE(dims[a] >= 1, "volume dimensions must be >= 1");
+    REQUIRE(bsz[a] > 2 * ov, "brick size must exceed twice the overlap (ExtendedOctree.cpp:196)");
+    REQUIRE(bsz[a] <= 4096, "brick size above 4096");
+  }
+  REQUIRE(dims[0] * dims[1] * dims[2] < (1ull << 40), "volume too large");
+  std::unique_ptr<tvk_volume> V(new tvk_volume());
+  TVK_CUDA(cudaGetDevice(&V->device));
+  V->dtype = dtype;
+  V->bytes = dtype == TVK_U8 ? 1 : 2;
+  for (int a = 0; a < 3; ++a) {
+    V->dims[a] = dims[a];
+    V->brick_size[a] = bsz[a];
+  }
+  V->overlap = ov;
+  V->clamp = clamp != 0;
+  cudaStream_t s;
+  TVK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  const size_t raw_bytes = size_t(dims[0] * dims[1] * dims[2]) * V->bytes;
+  try {
+    if (on_device) {
+      build_volume(V.get(), src, s);
+    } else {
+      DevBuf d_raw;
+      d_raw.ensure(raw_bytes);
+      TVK_CUDA(cudaMemcpyAsync(d_raw.p, src, raw_bytes, cudaMemcpyHostToDevice, s));
+      build_volume(V.get(), d_raw.p, s);
+      TVK_CUDA(cudaStreamSynchronize(s));
+    }
+  } catch (...) {
+    cudaStreamSynchronize(s);
+    if (V->d_pool) cudaFree(V->d_pool);
+    V->d_pool = nullptr;
+    throw;
+  }
+  return V.release();
+}
+
+uint64_t key_check(const tvk_volume* v, uint64_t ts, uint64_t lod, uint64_t idx) {
+  REQUIRE(v, "null volume");
+  REQUIRE(ts == 0, "only timestep 0 exists");
+  if (lod != 0) fail(TVK_ERR_UNSUPPORTED, "only LOD 0 bricks are resident on the device");
+  REQUIRE(idx < v->n_bricks, "brick index out of range");
+  return idx;
+}
+
+// ------------------------------------------------------------ view math
+
+struct View {
+  double mv[3][4];   // model -> eye
+  double inv[3][4];  // eye -> model
+  float kx, ky, inv_w2, inv_h2;
+};
+
+// Basics/Vectors.h:1250-1263 (BuildLookAt) and :1265-1276 (Perspective), in
+// double, rounded to float where the kernel consumes them.
+View make_view(const float eye_f[3], const float at[3], const float up[3], float fovy,
+               uint32_t w, uint32_t h, const double model[3][4]) {
+  const double eye[3] = {eye_f[0], eye_f[1], eye_f[2]};
+  double F[3] = {double(at[0]) - eye[0], double(at[1]) - eye[1], double(at[2]) - eye[2]};
+  double U[3] = {up[0], up[1], up[2]};
+  auto cross = [](const double a[3], const double b[3], double o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  auto norm = [](double v[3]) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int i = 0; i < 3; ++i) v[i] /= l;
+  };
+  double S[3], U2[3];
+  cross(F, U, S);
+  cross(S, F, U2);
+  norm(F);
+  norm(U2);
+  norm(S);
+  double view[3][4];
+  const double* rows[3] = {S, U2, F};
+  for (int r = 0; r < 3; ++r) {
+    const double sg = (r == 2) ? -1.0 : 1.0;
+    double d = 0;
+    for (int c = 0; c < 3; ++c) {
+      view[r][c] = sg * rows[r][c];
+      d += rows[r][c] * eye[c];
+    }
+    view[r][3] = -sg * d;
+  }
+  View v;
+  // modelview = view o model (column-vector form); model is identity unless set
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 4; ++c) {
+      double acc = (c == 3) ? view[r][3] : 0.0;
+      for (int k = 0; k < 3; ++k) acc += view[r][k] * model[k][c];
+      v.mv[r][c] = acc;
+    }
+  }
+  for (int r = 0; r < 3; ++r) {
+    double t = 0;
+    for (int c = 0; c < 3; ++c) {
+      v.inv[r][c] = v.mv[c][r];
+      t += v.mv[c][r] * v.mv[c][3];
+    }
+    v.inv[r][3] = -t;
+  }
+  const double th = std::tan(double(fovy) * (3.14159265358979323846 / 180.0) / 2.0);
+  const double aspect = double(w) / double(h);
+  v.kx = float(aspect * th);
+  v.ky = float(th);
+  v.inv_w2 = float(2.0 / double(w));
+  v.inv_h2 = float(2.0 / double(h));
+  return v;
+}
+
+}  // namespace tvk
+
+// ------------------------------------------------------------ renderer state
+
+struct tvk_renderer {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_staged = nullptr;
+  const tvk_volume* vol = nullptr;
+  // transfer function (effective RGBA as the GPU samples it)
+  std::vector<float> tf;
+  uint32_t tf_w = 0, tf_h = 0;
+  bool tf_2d = false;
+  bool tf_dirty = true;
+  tvk_render_mode mode = TVK_RM_1DTRANS;
+  bool lighting = false;
+  tvk_light_model light_model = TVK_LIGHT_REFERENCE;
+  float bp[4] = {0.2f, 0.6f, 0.2f, 32.0f};
+  // AbstrRenderer.cpp:162-168 defaults
+  float ambient[4] = {1, 1, 1, 0.1f}, diffuse[4] = {1, 1, 1, 1}, specular[4] = {1, 1, 1, 1};
+  float light_dir[3] = {0, 0, -1};
+  float srm = 1.0f;
+  float isovalue = 0.5f;
+  float frame_ert = 1.0f;
+  // AbstrRenderer.cpp:64-69 defaults
+  float eye[3] = {0, 0, 1.6f}, at[3] = {0, 0, 0}, up[3] = {0, 1, 0};
+  float fovy = 50.0f, znear = 0.01f, zfar = 1000.0f;
+  double model[3][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+  uint32_t width = 0, height = 0;
+  // device buffers
+  tvk::DevBuf d_img, d_spp, d_bricks, d_tf, d_tfcol, d_counters;
+  tvk::PinnedBuf h_bricks, h_counters;
+  tvk::PinnedBuf h_tf;
+  float tf_step_scale = -1.0f;  // step scale the device table was built for
+  tvk_stats stats{};
+  uint64_t launches = 0;
+  bool painted = false;
+};
+
+namespace tvk {
+namespace {
+
+void upload_tf(tvk_renderer* R, float step_scale) {
+  if (!R->tf_dirty && R->tf_step_scale == step_scale) return;
+  const size_t n = size_t(R->tf_w) * R->tf_h;
+  // the previous upload may still be reading the staging buffer
+  TVK_CUDA(cudaStreamSynchronize(R->stream));
+  R->h_tf.ensure(n * sizeof(float4) + R->tf_w);
+  float* t = R->h_tf.as<float>();
+  uint8_t* col = reinterpret_cast<uint8_t*>(t + 4 * n);
+  std::fill(col, col + R->tf_w, uint8_t(0));
+  for (size_t i = 0; i < n; ++i) {
+    t[4 * i + 0] = R->tf[4 * i + 0];
+    t[4 * i + 1] = R->tf[4 * i + 1];
+    t[4 * i + 2] = R->tf[4 * i + 2];
+    // VRender1D.glsl:53 opacity correction, evaluated per table entry
+    const float a = R->tf[4 * i + 3];
+    t[4 * i + 3] = 1.0f - std::pow(1.0f - a, step_scale);
+    if (a != 0.0f) col[i % R->tf_w] = 1;
+  }
+  R->d_tf.ensure(n * sizeof(float4));
+  R->d_tfcol.ensure(R->tf_w);
+  TVK_CUDA(cudaMemcpyAsync(R->d_tf.p, t, n * sizeof(float4), cudaMemcpyHostToDevice, R->stream));
+  TVK_CUDA(cudaMemcpyAsync(R->d_tfcol.p, col, R->tf_w, cudaMemcpyHostToDevice, R->stream));
+  R->tf_dirty = false;
+  R->tf_step_scale = step_scale;
+}
+
+void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgba8) {
+  R->tf.assign(rgba, rgba + size_t(4) * w * h);
+  if (rgba8) {
+    // TransferFunction1D.cpp:311-330 GetByteArray, sampled back as UNORM8
+    for (float& x : R->tf) {
+      const unsigned char b = (unsigned char)(std::max(0.0f, std::min(x, 1.0f)) * 255);
+      x = float(b) / 255.0f;
+    }
+  }
+  R->tf_w = w;
+  R->tf_h = h;
+  R->tf_2d = h > 1;
+  R->tf_dirty = true;
+}
+
+void paint(tvk_renderer* R) {
+  const tvk_volume* V = R->vol;
+  if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
+  if (R->tf.empty()) fail(TVK_ERR_STATE, "no transfer function set");
+  if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
+  if (R->mode == TVK_RM_ISOSURFACE) fail(TVK_ERR_UNSUPPORTED, "isosurface mode is not built yet");
+  if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
+  if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
+  TVK_CUDA(cudaSetDevice(R->device));
+  const uint64_t launches0 = R->launches;
+
+  // GLRaycaster.cpp:253-257: fStepScale at LOD 0
+  const float srm = R->srm;
+  const float step_scale = 1.0f / srm * 1.0f;
+  upload_tf(R, step_scale);
+
+  const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
+
+  // AbstrRenderer.cpp:1003-1012: scale of the brick boxes
+  const double user_scale[3] = {1, 1, 1};
+  const float us[3] = {float(user_scale[0]), float(user_scale[1]), float(user_scale[2])};
+  const float dmax = float(std::max(V->dims[0], std::max(V->dims[1], V->dims[2])));
+  float dcs[3];
+  for (int a = 0; a < 3; ++a) dcs[a] = us[a] * float(V->dims[a]) / dmax;
+  const float dcmax = std::max(dcs[0], std::max(dcs[1], dcs[2]));
+  float vs[3];
+  for (int a = 0; a < 3; ++a) vs[a] = us[a] / dcmax;
+
+  // AbstrRenderer.cpp:953-997 ContainsData with TF non-zero limits
+  // (TransferFunction1D.cpp:362-371; TF2D's value axis for 2D)
+  uint64_t nz_lo = R->tf_w, nz_hi = 0;
+  for (uint32_t y = 0; y < R->tf_h; ++y)
+    for (uint32_t x = 0; x < R->tf_w; ++x)
+      if (R->tf[4 * (size_t(y) * R->tf_w + x) + 3] != 0) {
+        nz_lo = std::min<uint64_t>(nz_lo, x);
+        nz_hi = std::max<uint64_t>(nz_hi, x);
+      }
+  const double rmax = V->range_max;
+  const double rescale = rmax / double(R->tf_w - 1);
+  const double lo = double(nz_lo) * rescale, hi = double(nz_hi) * rescale;
+
+  // per-brick records of the visible LOD-0 bricks (BuildSubFrameBrickList)
+  TVK_CUDA(cudaEventSynchronize(R->ev_staged));
+  R->h_bricks.ensure(V->n_bricks * sizeof(DevBrick));
+  DevBrick* hb = R->h_bricks.as<DevBrick>();
+  uint32_t nvis = 0;
+  for (uint64_t k = 0; k < V->n_bricks; ++k) {
+    if (!(hi >= V->bmin[k] && lo <= V->bmax[k])) continue;
+    const tvk_brick_md& m = V->md[k];
+    DevBrick& b = hb[nvis++];
+    std::memset(&b, 0, sizeof(b));
+    float e[3], c[3], tmin[3], tmax[3];
+    for (int a = 0; a < 3; ++a) {
+      b.n[a] = m.n_voxels[a];
+      e[a] = m.extents[a] * vs[a];
+      c[a] = m.center[a] * vs[a];
+      b.pmin[a] = c[a] - e[a] / 2.0f;
+      b.pmax[a] = c[a] + e[a] / 2.0f;
+      // UVFDataset::GetTextCoords (uvfDataset.cpp:1766-1767)
+      tmin[a] = float(V->overlap) / float(b.n[a]);
+      tmax[a] = 1.0f - tmin[a];
+    }
+    // GLRaycaster.cpp:589-612 ComputeEyeToTextureMatrix
+    for (int a = 0; a < 3; ++a) {
+      const double sc = double((tmin[a] - tmax[a]) / (b.pmin[a] - b.pmax[a]));
+      for (int j = 0; j < 3; ++j) b.tex[a][j] = float(sc * view.inv[a][j]);
+      b.tex[a][3] = float(sc * (view.inv[a][3] - double(b.pmax[a])) + double(tmax[a]));
+    }
+    // GLRaycaster.cpp:255 fRayStepsize
+    float stp = std::numeric_limits<float>::infinity();
+    for (int a = 0; a < 3; ++a) {
+      const float vsz = 1.0f / float(b.n[a]);
+      stp = std::min(stp, e[a] * vsz * 0.5f * 1.0f / srm);
+    }
+    b.step = stp;
+    b.off = V->offsets[k];
+  }
+  R->d_bricks.ensure(std::max<size_t>(1, V->n_bricks) * sizeof(DevBrick));
+  if (nvis)
+    TVK_CUDA(cudaMemcpyAsync(R->d_bricks.p, hb, nvis * sizeof(DevBrick), cudaMemcpyHostToDevice,
+                             R->stream));
+  TVK_CUDA(cudaEventRecord(R->ev_staged, R->stream));
+
+  RenderParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.pool = V->d_pool;
+  P.bytes = V->bytes;
+  P.bricks = R->d_bricks.as<DevBrick>();
+  P.n_bricks = nvis;
+  P.tf = R->d_tf.as<float4>();
+  P.tf_col_nonzero = R->d_tfcol.as<uint8_t>();
+  P.tf_w = R->tf_w;
+  P.tf_h = R->tf_h;
+  P.mode = R->mode;
+  P.lighting = R->lighting ? 1 : 0;
+  P.light_model = R->light_model;
+  // GLRenderer.cpp:1813-1819 CalculateScaling
+  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
+  P.trans_scale = float(double(imax) / rmax);
+  const float mg = float(V->max_grad);
+  P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;  // GLRenderer.cpp:1840-1841
+  P.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  for (int a = 0; a < 3; ++a) {
+    // GLRenderer.cpp:2890-2893: colour.xyz * colour.w
+    P.light_a[a] = R->ambient[a] * R->ambient[3];
+    P.light_d[a] = R->diffuse[a] * R->diffuse[3];
+    P.light_s[a] = R->specular[a] * R->specular[3];
+    P.light_dir[a] = R->light_dir[a];
+    P.domain_scale[a] = 1.0f / float(user_scale[a]);
+    for (int j = 0; j < 3; ++j) P.norm_mat[a][j] = float(view.mv[a][j]);
+    for (int j = 0; j < 4; ++j) P.inv[a][j] = float(view.inv[a][j]);
+  }
+  P.bp_ka = R->bp[0];
+  P.bp_kd = R->bp[1];
+  P.bp_ks = R->bp[2];
+  P.bp_shininess = R->bp[3];
+  P.kx = view.kx;
+  P.ky = view.ky;
+  P.inv_w2 = view.inv_w2;
+  P.inv_h2 = view.inv_h2;
+  P.znear = R->znear;
+  P.zfar = R->zfar;
+  P.frame_ert = R->frame_ert;
+  P.max_q = 1.0e6f;
+  P.width = R->width;
+  P.height = R->height;
+  const size_t npix = size_t(R->width) * R->height;
+  R->d_img.ensure(npix * sizeof(float4));
+  R->d_spp.ensure(npix * sizeof(uint32_t));
+  R->d_counters.ensure(4 * sizeof(unsigned long long));
+  P.out = R->d_img.as<float4>();
+  P.spp = R->d_spp.as<uint32_t>();
+  P.counters = R->d_counters.as<unsigned long long>();
+  TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
+  TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
+  launch_raycast(P, R->stream, &R->launches);
+  TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
+  R->h_counters.ensure(4 * sizeof(unsigned long long));
+  TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, R->stream));
+  R->stats.bricks_visible = nvis;
+  R->stats.bricks_total = V->n_bricks;
+  R->stats.kernel_launches = R->launches - launches0;
+  R->painted = true;
+}
+
+}  // namespace
+}  // namespace tvk
+
+// ------------------------------------------------------------------ C ABI
+
+using tvk::guarded;
+
+extern "C" {
+
+const char* tvk_status_string(tvk_status s) {
+  switch (s) {
+    case TVK_OK: return "ok";
+    case TVK_ERR_INVALID_ARG: return "invalid argument";
+    case TVK_ERR_CUDA: return "CUDA error";
+    case TVK_ERR_OUT_OF_MEMORY: return "out of memory";
+    case TVK_ERR_UNSUPPORTED: return "unsupported";
+    case TVK_ERR_STATE: return "invalid state";
+    case TVK_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+const char* tvk_last_error(void) { return tvk::g_last_error.c_str(); }
+
+int tvk_abi_version(void) { return TVK_ABI_VERSION; }
+
+tvk_status tvk_volume_create(const void* voxels, tvk_dtype dtype, const uint64_t dims[3],
+                             const uint32_t brick_size[3], uint32_t overlap, int clamp_to_edge,
+                             tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(out, "null output handle");
+    *out = tvk::create_volume(voxels, false, dtype, dims, brick_size, overlap, clamp_to_edge);
+  });
+}
+
+tvk_status tvk_volume_create_device(const void* device_voxels, tvk_dtype dtype,
+                                    const uint64_t dims[3], const uint32_t brick_size[3],
+                                    uint32_t overlap, int clamp_to_edge, tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(out, "null output handle");
+    *out = tvk::create_volume(device_voxels, true, dtype, dims, brick_size, overlap,
+                              clamp_to_edge);
+  });
+}
+
+tvk_status tvk_volume_destroy(tvk_volume* v) {
+  return guarded([&] {
+    if (!v) return;
+    if (v->d_pool) cudaFree(v->d_pool);
+    delete v;
+  });
+}
+
+tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out) {
+  return guarded([&] {
+    REQUIRE(v && out, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    for (int a = 0; a < 3; ++a) {
+      out->dims[a] = v->dims[a];
+      out->brick_size[a] = v->brick_size[a];
+    }
+    out->dtype = v->dtype;
+    out->bit_width = 8u * v->bytes;
+    out->overlap = v->overlap;
+    out->lod_count = uint32_t(v->lods.size());
+    out->lod0_bricks = v->n_bricks;
+    out->range_min = v->range_min;
+    out->range_max = v->range_max;
+    out->max_gradient = double(float(v->max_grad));
+    out->device_bytes = v->pool_bytes;
+  });
+}
+
+tvk_status tvk_volume_get_lod(const tvk_volume* v, uint32_t lod, uint64_t size[3],
+                              uint64_t brick_count[3]) {
+  return guarded([&] {
+    REQUIRE(v && size && brick_count, "null argument");
+    REQUIRE(lod < v->lods.size(), "LOD out of range");
+    for (int a = 0; a < 3; ++a) {
+      size[a] = v->lods[lod].size[a];
+      brick_count[a] = v->lods[lod].bricks[a];
+    }
+  });
+}
+
+tvk_status tvk_volume_get_brick_md(const tvk_volume* v, uint64_t ts, uint64_t lod, uint64_t index,
+                                   tvk_brick_md* out) {
+  return guarded([&] {
+    REQUIRE(out, "null argument");
+    *out = v->md[tvk::key_check(v, ts, lod, index)];
+  });
+}
+
+tvk_status tvk_volume_get_brick(const tvk_volume* v, uint64_t ts, uint64_t lod, uint64_t index,
+                                void* host_out, size_t bytes) {
+  return guarded([&] {
+    const uint64_t k = tvk::key_check(v, ts, lod, index);
+    REQUIRE(host_out, "null argument");
+    const size_t n = size_t(v->sizes[3 * k]) * v->sizes[3 * k + 1] * v->sizes[3 * k + 2] * v->bytes;
+    REQUIRE(bytes >= n, "output buffer smaller than the brick");
+    TVK_CUDA(cudaSetDevice(v->device));
+    TVK_CUDA(cudaMemcpy(host_out, static_cast<const uint8_t*>(v->d_pool) + v->offsets[k] * v->bytes,
+                        n, cudaMemcpyDeviceToHost));
+  });
+}
+
+tvk_status tvk_volume_get_minmax(const tvk_volume* v, uint64_t ts, uint64_t lod, uint64_t index,
+                                 tvk_minmax* out) {
+  return guarded([&] {
+    const uint64_t k = tvk::key_check(v, ts, lod, index);
+    REQUIRE(out, "null argument");
+    // MaxMinDataBlock::SetDataFromFlatVector (IO/UVF/MaxMinDataBlock.cpp:175-195)
+    out->min_scalar = v->bmin[k];
+    out->max_scalar = v->bmax[k];
+    out->min_gradient = -std::numeric_limits<double>::max();
+    out->max_gradient = std::numeric_limits<double>::max();
+  });
+}
+
+tvk_status tvk_volume_get_histogram(const tvk_volume* v, uint64_t* host_out, size_t bins,
+                                    uint64_t* trimmed_len) {
+  return guarded([&] {
+    REQUIRE(v && host_out, "null argument");
+    std::memset(host_out, 0, bins * sizeof(uint64_t));
+    const size_t n = std::min(bins, v->hist.size());
+    for (size_t i = 0; i < n; ++i) host_out[i] = v->hist[i];
+    if (trimmed_len) *trimmed_len = v->hist_trimmed;
+  });
+}
+
+tvk_status tvk_volume_get_brick_histograms(const tvk_volume* v, uint32_t* host_out,
+                                           size_t n_bricks, uint32_t* shift) {
+  return guarded([&] {
+    REQUIRE(v && host_out, "null argument");
+    REQUIRE(n_bricks >= v->n_bricks, "output holds fewer bricks than the volume");
+    std::memcpy(host_out, v->bhist.data(), v->bhist.size() * sizeof(uint32_t));
+    if (shift) *shift = v->hist_shift;
+  });
+}
+
+tvk_status tvk_volume_index_from_4d(const tvk_volume* v, const uint64_t xyzl[4], uint64_t* index) {
+  return guarded([&] {
+    REQUIRE(v && xyzl && index, "null argument");
+    REQUIRE(xyzl[3] < v->lods.size(), "LOD out of range");
+    const tvk::LodInfo& l = v->lods[xyzl[3]];
+    REQUIRE(xyzl[0] < l.bricks[0] && xyzl[1] < l.bricks[1] && xyzl[2] < l.bricks[2],
+            "brick coordinate out of range");
+    *index = xyzl[0] + xyzl[1] * l.bricks[0] + xyzl[2] * l.bricks[0] * l.bricks[1];
+  });
+}
+
+tvk_status tvk_volume_index_to_4d(const tvk_volume* v, uint64_t lod, uint64_t index,
+                                  uint64_t xyzl[4]) {
+  return guarded([&] {
+    REQUIRE(v && xyzl, "null argument");
+    REQUIRE(lod < v->lods.size(), "LOD out of range");
+    const tvk::LodInfo& l = v->lods[lod];
+    REQUIRE(index < l.bricks[0] * l.bricks[1] * l.bricks[2], "brick index out of range");
+    xyzl[0] = index % l.bricks[0];
+    xyzl[1] = (index / l.bricks[0]) % l.bricks[1];
+    xyzl[2] = index / (l.bricks[0] * l.bricks[1]);
+    xyzl[3] = lod;
+  });
+}
+
+tvk_status tvk_renderer_create(tvk_renderer** out) {
+  return guarded([&] {
+    REQUIRE(out, "null output handle");
+    std::unique_ptr<tvk_renderer> R(new tvk_renderer());
+    TVK_CUDA(cudaGetDevice(&R->device));
+    TVK_CUDA(cudaStreamCreateWithFlags(&R->stream, cudaStreamNonBlocking));
+    TVK_CUDA(cudaEventCreate(&R->ev_start));
+    TVK_CUDA(cudaEventCreate(&R->ev_stop));
+    TVK_CUDA(cudaEventCreateWithFlags(&R->ev_staged, cudaEventDisableTiming));
+    TVK_CUDA(cudaEventRecord(R->ev_staged, R->stream));
+    *out = R.release();
+  });
+}
+
+tvk_status tvk_renderer_destroy(tvk_renderer* r) {
+  return guarded([&] {
+    if (!r) return;
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->ev_start) cudaEventDestroy(r->ev_start);
+    if (r->ev_stop) cudaEventDestroy(r->ev_stop);
+    if (r->ev_staged) cudaEventDestroy(r->ev_staged);
+    if (r->stream) cudaStreamDestroy(r->stream);
+    delete r;
+  });
+}
+
+tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->vol = v;
+  });
+}
+
+tvk_status tvk_set_tf1d_rgba8(tvk_renderer* r, const uint8_t* rgba, uint32_t n) {
+  return guarded([&] {
+    REQUIRE(r && rgba && n >= 2, "need a renderer and at least two TF entries");
+    // TransferFunction1D::Set (TransferFunction1D.cpp:146-177): colour channels
+    // lerped from their per-channel [min, max] onto [0, 1], alpha byte/255.
+    uint8_t mn[4] = {255, 255, 255, 255}, mx[4] = {0, 0, 0, 0};
+    for (uint32_t i = 0; i < n; ++i)
+      for (int c = 0; c < 4; ++c) {
+        mn[c] = std::min(mn[c], rgba[4 * i + c]);
+        mx[c] = std::max(mx[c], rgba[4 * i + c]);
+      }
+    // MathTools::lerp (Basics/MathTools.h:81-84):
+    //   out(omin + (value - imin) * (double(omax - omin) / (imax - imin)))
+    // A constant channel divides by zero; the NaN it yields becomes 0 in the
+    // RGBA8 upload below, as in the reference.
+    auto lerp = [](int value, int imin, int imax) {
+      const double q = double(1.0f - 0.0f) / double(imax - imin);
+      return float(0.0f + double(value - imin) * q);
+    };
+    std::vector<float> f(size_t(4) * n);
+    for (uint32_t i = 0; i < n; ++i) {
+      for (int c = 0; c < 3; ++c) f[4 * i + c] = lerp(rgba[4 * i + c], mn[c], mx[c]);
+      f[4 * i + 3] = lerp(rgba[4 * i + 3], 0, 255);
+    }
+    tvk::set_tf(r, f.data(), n, 1, true);
+  });
+}
+
+tvk_status tvk_set_tf1d_float(tvk_renderer* r, const float* rgba, uint32_t n, int rgba8_upload) {
+  return guarded([&] {
+    REQUIRE(r && rgba && n >= 2, "need a renderer and at least two TF entries");
+    tvk::set_tf(r, rgba, n, 1, rgba8_upload != 0);
+  });
+}
+
+tvk_status tvk_set_tf2d_float(tvk_renderer* r, const float* rgba, uint32_t w, uint32_t h,
+                              int rgba8_upload) {
+  return guarded([&] {
+    REQUIRE(r && rgba && w >= 2 && h >= 2, "need a renderer and a TF of at least 2x2");
+    tvk::set_tf(r, rgba, w, h, rgba8_upload != 0);
+  });
+}
+
+tvk_status tvk_set_render_mode(tvk_renderer* r, tvk_render_mode mode) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(mode == TVK_RM_1DTRANS || mode == TVK_RM_2DTRANS || mode == TVK_RM_ISOSURFACE,
+            "unknown render mode");
+    r->mode = mode;
+  });
+}
+
+tvk_status tvk_set_lighting(tvk_renderer* r, int enable) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->lighting = enable != 0;
+  });
+}
+
+tvk_status tvk_set_sample_rate_modifier(tvk_renderer* r, float srm) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(srm > 0.0f && srm < 1e4f, "sample rate modifier must be in (0, 1e4)");
+    r->srm = srm;
+  });
+}
+
+tvk_status tvk_set_isovalue(tvk_renderer* r, float isovalue) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->isovalue = isovalue;
+  });
+}
+
+tvk_status tvk_set_colors(tvk_renderer* r, const float ambient[4], const float diffuse[4],
+                          const float specular[4], const float light_dir[3]) {
+  return guarded([&] {
+    REQUIRE(r && ambient && diffuse && specular && light_dir, "null argument");
+    for (int a = 0; a < 4; ++a) {
+      r->ambient[a] = ambient[a];
+      r->diffuse[a] = diffuse[a];
+      r->specular[a] = specular[a];
+    }
+    for (int a = 0; a < 3; ++a) r->light_dir[a] = light_dir[a];
+  });
+}
+
+tvk_status tvk_set_light_model(tvk_renderer* r, tvk_light_model model, float ka, float kd,
+                               float ks, float shininess) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(model == TVK_LIGHT_REFERENCE || model == TVK_LIGHT_BLINN_PHONG, "unknown model");
+    REQUIRE(shininess >= 0.0f, "shininess must be >= 0");
+    r->light_model = model;
+    r->bp[0] = ka;
+    r->bp[1] = kd;
+    r->bp[2] = ks;
+    r->bp[3] = shininess;
+  });
+}
+
+tvk_status tvk_set_view(tvk_renderer* r, const float eye[3], const float at[3], const float up[3],
+                        float fovy_deg, float znear, float zfar) {
+  return guarded([&] {
+    REQUIRE(r && eye && at && up, "null argument");
+    REQUIRE(fovy_deg > 0.0f && fovy_deg < 180.0f, "field of view must be in (0, 180)");
+    REQUIRE(znear > 0.0f && zfar > znear, "need 0 < znear < zfar");
+    for (int a = 0; a < 3; ++a) {
+      r->eye[a] = eye[a];
+      r->at[a] = at[a];
+      r->up[a] = up[a];
+    }
+    r->fovy = fovy_deg;
+    r->znear = znear;
+    r->zfar = zfar;
+  });
+}
+
+tvk_status tvk_set_model_transform(tvk_renderer* r, const float rotation[16],
+                                   const float translation[16]) {
+  return guarded([&] {
+    REQUIRE(r && rotation && translation, "null argument");
+    // row-vector matrices (Basics/Vectors.h): p' = p * Rot * Trans; as a
+    // column-vector affine map: M[row][col] = Trans^T * Rot^T
+    double Rm[3][4], Tm[3][4];
+    for (int row = 0; row < 3; ++row)
+      for (int col = 0; col < 4; ++col) {
+        Rm[row][col] = rotation[col * 4 + row];
+        Tm[row][col] = translation[col * 4 + row];
+      }
+    for (int row = 0; row < 3; ++row)
+      for (int col = 0; col < 4; ++col) {
+        double acc = (col == 3) ? Tm[row][3] : 0.0;
+        for (int k = 0; k < 3; ++k) acc += Tm[row][k] * Rm[k][col];
+        r->model[row][col] = acc;
+      }
+    // rigidity check: the upper 3x3 must be orthonormal
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double d = 0;
+        for (int k = 0; k < 3; ++k) d += r->model[k][i] * r->model[k][j];
+        if (std::fabs(d - (i == j ? 1.0 : 0.0)) > 1e-4)
+          tvk::fail(TVK_ERR_INVALID_ARG, "model transform must be rigid");
+      }
+  });
+}
+
+tvk_status tvk_resize(tvk_renderer* r, uint32_t width, uint32_t height) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(width >= 1 && height >= 1 && width <= 16384 && height <= 16384,
+            "viewport must be 1..16384 pixels per side");
+    r->width = width;
+    r->height = height;
+  });
+}
+
+tvk_status tvk_set_frame_termination(tvk_renderer* r, float threshold) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(threshold > 0.0f && threshold <= 1.0f, "threshold must be in (0, 1]");
+    r->frame_ert = threshold;
+  });
+}
+
+tvk_status tvk_paint(tvk_renderer* r) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    tvk::paint(r);
+  });
+}
+
+tvk_status tvk_get_image_device(tvk_renderer* r, const float** device_rgba, uint32_t* width,
+                                uint32_t* height) {
+  return guarded([&] {
+    REQUIRE(r && device_rgba, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    *device_rgba = r->d_img.as<const float>();
+    if (width) *width = r->width;
+    if (height) *height = r->height;
+  });
+}
+
+tvk_status tvk_read_image(tvk_renderer* r, float* host_rgba, size_t n_floats) {
+  return guarded([&] {
+    REQUIRE(r && host_rgba, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    const size_t n = size_t(r->width) * r->height * 4;
+    REQUIRE(n_floats >= n, "output buffer smaller than the image");
+    TVK_CUDA(cudaMemcpyAsync(host_rgba, r->d_img.p, n * sizeof(float), cudaMemcpyDeviceToHost,
+                             r->stream));
+    TVK_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t n) {
+  return guarded([&] {
+    REQUIRE(r && host_counts, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    const size_t np = size_t(r->width) * r->height;
+    REQUIRE(n >= np, "output buffer smaller than the image");
+    TVK_CUDA(cudaMemcpyAsync(host_counts, r->d_spp.p, np * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, r->stream));
+    TVK_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+tvk_status tvk_renderer_get_stream(tvk_renderer* r, void** stream) {
+  return guarded([&] {
+    REQUIRE(r && stream, "null argument");
+    *stream = r->stream;
+  });
+}
+
+tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out) {
+  return guarded([&] {
+    REQUIRE(r && out, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    TVK_CUDA(cudaStreamSynchronize(r->stream));
+    const unsigned long long* c = r->h_counters.as<unsigned long long>();
+    r->stats.samples = c[0];
+    r->stats.shaded_samples = c[1];
+    float ms = 0;
+    TVK_CUDA(cudaEventElapsedTime(&ms, r->ev_start, r->ev_stop));
+    r->stats.last_paint_ms = ms;
+    if (c[2] != 0)
+      tvk::fail(TVK_ERR_INTERNAL, "ray march guard tripped on " + std::to_string(c[2]) + " rays");
+    *out = r->stats;
+  });
+}
+
+tvk_status tvk_generate_volume(void* device_out, tvk_dtype dtype, const uint64_t dims[3],
+                               const float* host_blobs, uint32_t n_blobs, float noise_amp,
+                               uint32_t noise_octaves, float noise_cell, uint64_t seed,
+                               int int_noise, float vmax) {
+  return guarded([&] {
+    REQUIRE(device_out && dims, "null argument");
+    REQUIRE(n_blobs == 0 || host_blobs, "null blob table");
+    REQUIRE(dtype == TVK_U8 || dtype == TVK_U16, "bad dtype");
+    REQUIRE(noise_octaves == 0 || noise_cell > 0, "noise cell must be > 0");
+    tvk::DevBuf d_blobs;
+    d_blobs.ensure(size_t(7) * std::max<uint32_t>(1, n_blobs) * sizeof(float));
+    if (n_blobs)
+      TVK_CUDA(cudaMemcpy(d_blobs.p, host_blobs, size_t(7) * n_blobs * sizeof(float),
+                          cudaMemcpyHostToDevice));
+    tvk::launch_generate(device_out, dtype == TVK_U8 ? 1 : 2, dims, d_blobs.as<float>(), n_blobs,
+                         noise_amp, noise_octaves, noise_cell, seed, int_noise, vmax, 0);
+    TVK_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+}  // extern "C"

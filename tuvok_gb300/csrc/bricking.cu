@@ -1,0 +1,246 @@
+// bricking.cu -- LOD-0 bricking, per-brick statistics and histograms on sm_103a.
+//
+// One pass over the flat volume writes every brick of LOD 0 (ghost voxels
+// included) into the brick pool, and on the way accumulates
+//   * per-brick min/max over the whole brick (ExtendedOctreeConverter::
+//     ComputeBrickStats, IO/UVF/ExtendedOctree/ExtendedOctreeConverter.inc:408-444),
+//   * the global histogram of inner voxels (Histogram1DDataBlock::ComputeTemplate,
+//     IO/UVF/Histogram1DDataBlock.cpp:120-161),
+//   * a 256-bin histogram of each brick's inner voxels.
+// A second kernel finds the maximum gradient magnitude over inner voxels
+// (Histogram2DDataBlock::ComputeGradient/ComputeTemplate, Histogram2DDataBlock.cpp:327-397).
+//
+// The voxel a brick position reads follows GetInputBrick
+// (ExtendedOctreeConverter.cpp:288-373) exactly: the reference copies x-scanlines
+// at linear file offsets, so a ghost read past the end of an x-line continues on
+// the next line, and a read past the end of the file yields zero.  Clamping
+// (ClampToEdge, :376-462) replicates the outermost inner plane on volume borders.
+//
+// All of this is integer work and HBM-bound: reads are contiguous along x, the
+// pool is written in the same order, histograms live in shared memory and are
+// merged with one atomic per non-zero bin and CTA.
+#include "tvk_internal.h"
+
+namespace tvk {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kSmemGlobalBins = 11776;  // keeps the CTA under 48 KB of smem
+
+template <class T>
+__global__ void raw_minmax_kernel(const T* __restrict__ raw, uint64_t n, uint32_t* minmax) {
+  uint32_t lo = 0xffffffffu, hi = 0;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t v = raw[i];
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&minmax[0], lo);
+    atomicMax(&minmax[1], hi);
+  }
+}
+
+// Source voxel of brick-local position (i, j, k) of brick (cx, cy, cz).
+template <class T>
+__device__ __forceinline__ T source_voxel(const T* __restrict__ raw, const BrickGrid& g,
+                                          const uint32_t c[3], const uint32_t bs[3],
+                                          uint32_t i, uint32_t j, uint32_t k) {
+  const uint32_t loc[3] = {i, j, k};
+  uint64_t gc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    uint32_t l = loc[a];
+    const bool first = c[a] == 0, last = c[a] == g.cnt[a] - 1;
+    if (g.clamp) {
+      if (first && l < g.ov) l = g.ov;
+      if (last && l > bs[a] - 1 - g.ov) l = bs[a] - 1 - g.ov;
+    }
+    const uint32_t s = first ? g.ov : 0;
+    const uint32_t e = bs[a] - (last ? g.ov : 0);
+    if (l < s || l >= e) return T(0);
+    gc[a] = uint64_t(c[a]) * (g.B[a] - 2u * g.ov) + l - g.ov;
+  }
+  const uint64_t L = gc[0] + gc[1] * g.dims[0] + gc[2] * g.dims[0] * g.dims[1];
+  return L < g.total ? raw[L] : T(0);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+brick_lod0_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __restrict__ offsets,
+                  const uint32_t* __restrict__ sizes, T* __restrict__ pool, BrickScratch sc,
+                  uint32_t shift, uint32_t smem_bins, uint32_t z_chunk) {
+  extern __shared__ uint32_t smem[];
+  uint32_t* bh = smem;            // 256 per-brick bins
+  uint32_t* gh = smem + 256;      // global bins (smem_bins of them, may be 0)
+  const uint32_t b = blockIdx.x;
+  for (uint32_t i = threadIdx.x; i < 256 + smem_bins; i += blockDim.x) smem[i] = 0;
+  __syncthreads();
+
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
+  const uint32_t z0 = blockIdx.y * z_chunk;
+  const uint32_t z1 = min(bs[2], z0 + z_chunk);
+  T* out = pool + offsets[b];
+  const uint32_t sxy = bs[0] * bs[1];
+  uint32_t lo = 0xffffffffu, hi = 0;
+  if (z0 < z1) {
+    const uint32_t n = (z1 - z0) * sxy;
+    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+      const uint32_t k = z0 + t / sxy;
+      const uint32_t r = t - (k - z0) * sxy;
+      const uint32_t j = r / bs[0];
+      const uint32_t i = r - j * bs[0];
+      const T v = source_voxel<T>(raw, g, c, bs, i, j, k);
+      out[uint64_t(k) * sxy + r] = v;
+      const uint32_t u = v;
+      lo = min(lo, u);
+      hi = max(hi, u);
+      const bool inner = i >= g.ov && i < bs[0] - g.ov && j >= g.ov && j < bs[1] - g.ov &&
+                         k >= g.ov && k < bs[2] - g.ov;
+      if (inner) {
+        atomicAdd(&bh[min(u >> shift, 255u)], 1u);
+        if (u < smem_bins)
+          atomicAdd(&gh[u], 1u);
+        else
+          atomicAdd(&sc.hist[u], 1ull);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0 && lo <= hi) {
+    atomicMin(&sc.bmin[b], lo);
+    atomicMax(&sc.bmax[b], hi);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x)
+    if (bh[i]) atomicAdd(&sc.bhist[256u * b + i], bh[i]);
+  for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x)
+    if (gh[i]) atomicAdd(&sc.hist[i], (unsigned long long)gh[i]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                    const uint32_t* __restrict__ sizes, uint32_t ov, uint32_t z_chunk,
+                    unsigned long long* out_bits) {
+  // Every inner voxel: Q = dx^2 + dy^2 + dz^2 of the central differences.  Distinct
+  // integer Q values give |grad| values whose relative gap (>= 1/(2Q)) far exceeds
+  // double rounding, so the maximum |grad| sits at a voxel of maximum Q; only those
+  // lanes evaluate the reference's double expression and publish its bits.
+  const uint32_t b = blockIdx.x;
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const T* p = pool + offsets[b];
+  const uint32_t ix = bs[0] - 2 * ov, iy = bs[1] - 2 * ov;
+  const uint32_t z0 = ov + blockIdx.y * z_chunk;
+  const uint32_t z1 = min(bs[2] - ov, z0 + z_chunk);
+  const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
+  const double nf2 = double(T(~T(0))) * 2.0;
+  long long best_q = -1;
+  double best_f = 0.0;
+  const uint32_t n = (z1 > z0) ? (z1 - z0) * ix * iy : 0;
+  // iterate in whole warps so the warp-wide reduction below is uniform
+  const uint32_t n_pad = (n + 31u) & ~31u;
+  for (uint32_t t = threadIdx.x; t < n_pad; t += blockDim.x) {
+    long long q = -1;
+    int dx = 0, dy = 0, dz = 0;
+    if (t < n) {
+      const uint32_t k = z0 + t / (ix * iy);
+      const uint32_t r = t % (ix * iy);
+      const uint32_t j = ov + r / ix;
+      const uint32_t i = ov + r % ix;
+      const uint64_t c = uint64_t(i) + uint64_t(j) * sx + uint64_t(k) * sxy;
+      dx = int(p[c - 1]) - int(p[c + 1]);
+      dy = int(p[c - sx]) - int(p[c + sx]);
+      dz = int(p[c - sxy]) - int(p[c + sxy]);
+      q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
+    }
+    long long wq = q;
+    for (int o = 16; o > 0; o >>= 1) wq = max(wq, (long long)__shfl_xor_sync(0xffffffffu, wq, o));
+    if (q >= 0 && q == wq) {
+      const double gx = __ddiv_rn(double(dx), nf2);
+      const double gy = __ddiv_rn(double(dy), nf2);
+      const double gz = __ddiv_rn(double(dz), nf2);
+      const double s = __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz));
+      const double f = __dsqrt_rn(s);
+      if (q > best_q || (q == best_q && f > best_f)) {
+        best_q = q;
+        best_f = f;
+      }
+    }
+  }
+  if (best_q >= 0) {
+    // positive doubles order like their bit patterns
+    atomicMax(out_bits, (unsigned long long)__double_as_longlong(best_f));
+  }
+}
+
+uint32_t blocks_for(uint64_t n) {
+  const uint64_t b = (n + kThreads - 1) / kThreads;
+  return uint32_t(b < 152ull * 16 ? (b ? b : 1) : 152ull * 16);
+}
+
+}  // namespace
+
+void launch_raw_minmax(const void* raw, int bytes, uint64_t n, uint32_t* minmax, cudaStream_t s,
+                       uint64_t* launches) {
+  const uint32_t init[2] = {0xffffffffu, 0u};
+  TVK_CUDA(cudaMemcpyAsync(minmax, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  if (bytes == 1)
+    raw_minmax_kernel<uint8_t><<<blocks_for(n), kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(raw), n, minmax);
+  else
+    raw_minmax_kernel<uint16_t><<<blocks_for(n), kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(raw), n, minmax);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g, const uint64_t* d_offsets,
+                       const uint32_t* d_sizes, uint64_t n_bricks, void* pool,
+                       const BrickScratch& sc, uint32_t hist_shift, uint32_t global_bins,
+                       cudaStream_t s, uint64_t* launches) {
+  const uint32_t z_chunk = 8;
+  const dim3 grid(uint32_t(n_bricks), (g.B[2] + z_chunk - 1) / z_chunk);
+  const uint32_t smem_bins = global_bins <= kSmemGlobalBins ? global_bins : 0;
+  const size_t smem = (256 + smem_bins) * sizeof(uint32_t);
+  if (bytes == 1)
+    brick_lod0_kernel<uint8_t><<<grid, kThreads, smem, s>>>(
+        static_cast<const uint8_t*>(raw), g, d_offsets, d_sizes, static_cast<uint8_t*>(pool), sc,
+        hist_shift, smem_bins, z_chunk);
+  else
+    brick_lod0_kernel<uint16_t><<<grid, kThreads, smem, s>>>(
+        static_cast<const uint16_t*>(raw), g, d_offsets, d_sizes, static_cast<uint16_t*>(pool),
+        sc, hist_shift, smem_bins, z_chunk);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
+                         const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
+                         uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
+                         uint64_t* launches) {
+  TVK_CUDA(cudaMemsetAsync(out_bits, 0, sizeof(unsigned long long), s));
+  // without overlap a brick holds no neighbours of its boundary voxels
+  if (ov == 0 || max_bz <= 2 * ov) return;
+  const uint32_t z_chunk = 4;
+  const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
+  if (bytes == 1)
+    max_gradient_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(pool), d_offsets, d_sizes, ov, z_chunk, out_bits);
+  else
+    max_gradient_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(pool), d_offsets, d_sizes, ov, z_chunk, out_bits);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+}  // namespace tvk

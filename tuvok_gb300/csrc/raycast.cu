@@ -1,0 +1,327 @@
+// raycast.cu -- brick-by-brick front-to-back ray march on sm_103a.
+//
+// Restates Tuvok's GLRaycaster: for every pixel, every non-empty LOD-0 brick the
+// pixel's ray crosses is marched on its own (Shaders/GLRaycaster-1D-FS.glsl:51-82,
+// -1D-light-FS.glsl:84-134, -2D-FS.glsl:53-94, -2D-light-FS.glsl:61-117) from its
+// RGBA16F-rounded entry point (Renderer/GL/GLRaycaster.cpp:93-99) with the brick's
+// own step size and opacity correction (:239-300), and the per-brick colour is
+// blended into the frame with (ONE_MINUS_DST_ALPHA, ONE) (GLRenderer.cpp:151-153)
+// in the order the ray meets the bricks.
+//
+// One thread per pixel, warps on 8x4 pixel tiles so neighbouring rays touch the
+// same brick cache lines.  The arithmetic is the oracle's, operation for
+// operation: this file is compiled with -fmad=false, every fused multiply-add is
+// an explicit fmaf, sqrt and division are IEEE, and opacity correction comes from
+// a host-built table (1 - powf(1 - a, s) per TF entry).  Work the reference does
+// but that cannot change the pixel is skipped: gradients and lighting of samples
+// whose corrected alpha is 0 (their compositing adds exactly zero).
+#include <cuda_fp16.h>
+
+#include "tvk_internal.h"
+
+namespace tvk {
+namespace {
+
+constexpr int kMaxHits = 64;
+
+__device__ __forceinline__ float affine_row(const float r[4], float x, float y, float z) {
+  return fmaf(r[0], x, fmaf(r[1], y, fmaf(r[2], z, r[3])));
+}
+
+__device__ __forceinline__ float len3(float x, float y, float z) {
+  return sqrtf((x * x + y * y) + z * z);
+}
+
+template <class T>
+struct BrickView {
+  const T* __restrict__ p;
+  int n0, n1, n2;
+  float fn0, fn1, fn2;
+  uint32_t sx, sxy;
+
+  __device__ __forceinline__ float fetch(int x, int y, int z) const {
+    return float(__ldg(p + (size_t(x) + size_t(y) * sx + size_t(z) * sxy)));
+  }
+  // texel-centre trilinear, clamp to edge, raw units
+  __device__ __forceinline__ float sample_raw(float tx, float ty, float tz) const {
+    float u0 = fmaf(tx, fn0, -0.5f);
+    float u1 = fmaf(ty, fn1, -0.5f);
+    float u2 = fmaf(tz, fn2, -0.5f);
+    u0 = fminf(fmaxf(u0, 0.0f), float(n0 - 1));
+    u1 = fminf(fmaxf(u1, 0.0f), float(n1 - 1));
+    u2 = fminf(fmaxf(u2, 0.0f), float(n2 - 1));
+    const int x0 = int(u0), y0 = int(u1), z0 = int(u2);
+    const float fx = u0 - float(x0), fy = u1 - float(y0), fz = u2 - float(z0);
+    const int x1 = min(x0 + 1, n0 - 1), y1 = min(y0 + 1, n1 - 1), z1 = min(z0 + 1, n2 - 1);
+    const float v000 = fetch(x0, y0, z0), v100 = fetch(x1, y0, z0);
+    const float v010 = fetch(x0, y1, z0), v110 = fetch(x1, y1, z0);
+    const float v001 = fetch(x0, y0, z1), v101 = fetch(x1, y0, z1);
+    const float v011 = fetch(x0, y1, z1), v111 = fetch(x1, y1, z1);
+    const float c00 = fmaf(fx, v100 - v000, v000);
+    const float c10 = fmaf(fx, v110 - v010, v010);
+    const float c01 = fmaf(fx, v101 - v001, v001);
+    const float c11 = fmaf(fx, v111 - v011, v011);
+    const float c0 = fmaf(fy, c10 - c00, c00);
+    const float c1 = fmaf(fy, c11 - c01, c01);
+    return fmaf(fz, c1 - c0, c0);
+  }
+};
+
+__device__ __forceinline__ float pow_int_or_real(float x, float e) {
+  if (e == 8.0f) { float a = x * x; a = a * a; return a * a; }
+  if (e == 32.0f) { float a = x * x; a = a * a; a = a * a; a = a * a; return a * a; }
+  return powf(x, e);
+}
+
+__device__ __forceinline__ void lighting_ref(const RenderParams& P, const float pos[3],
+                                             const float N[3], const float tfc[3], float out[3]) {
+  // Shaders/lighting.glsl:33-43
+  const float p0 = -pos[0], p1 = -pos[1], p2 = -pos[2];
+  const float lp = len3(p0, p1, p2);
+  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  const float d = (N[0] * V0 + N[1] * V1) + N[2] * V2;
+  float R0 = V0 - (2.0f * d) * N[0];
+  float R1 = V1 - (2.0f * d) * N[1];
+  float R2 = V2 - (2.0f * d) * N[2];
+  const float lr = len3(R0, R1, R2);
+  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+  const float* L = P.light_dir;
+  const float diff = fmaxf(fabsf((N[0] * L[0] + N[1] * L[1]) + N[2] * L[2]), 0.0f);
+  const float spec = pow_int_or_real(fmaxf((R0 * L[0] + R1 * L[1]) + R2 * L[2], 0.0f), 8.0f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float dcol = P.light_d[i] * tfc[i];
+    float c = P.light_a[i] + dcol * diff;
+    c = c + P.light_s[i] * spec;
+    out[i] = fminf(fmaxf(c, 0.0f), 1.0f);
+  }
+}
+
+__device__ __forceinline__ void lighting_bp(const RenderParams& P, const float pos[3],
+                                            const float Nin[3], const float tfc[3], float out[3]) {
+  const float p0 = -pos[0], p1 = -pos[1], p2 = -pos[2];
+  const float lp = len3(p0, p1, p2);
+  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  float N0 = Nin[0], N1 = Nin[1], N2 = Nin[2];
+  if ((N0 * V0 + N1 * V1) + N2 * V2 < 0.0f) { N0 = -N0; N1 = -N1; N2 = -N2; }
+  const float L0 = -P.light_dir[0], L1 = -P.light_dir[1], L2 = -P.light_dir[2];
+  float H0 = L0 + V0, H1 = L1 + V1, H2 = L2 + V2;
+  const float lh = len3(H0, H1, H2);
+  H0 = H0 / lh; H1 = H1 / lh; H2 = H2 / lh;
+  const float diff = fmaxf((N0 * L0 + N1 * L1) + N2 * L2, 0.0f);
+  const float spec = pow_int_or_real(fmaxf((N0 * H0 + N1 * H1) + N2 * H2, 0.0f), P.bp_shininess);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float c = P.bp_ka * tfc[i];
+    c = c + (P.bp_kd * tfc[i]) * diff;
+    c = c + P.bp_ks * spec;
+    out[i] = fminf(fmaxf(c, 0.0f), 1.0f);
+  }
+}
+
+// Marches one brick; returns the brick's premultiplied RGBA.
+template <class T>
+__device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBrick& b,
+                                              const float dir[3], float t_in, float t_out,
+                                              uint32_t& samples, uint32_t& shaded) {
+  float en[3], ex[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    en[a] = __half2float(__float2half_rn(dir[a] * t_in));
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float q = len / b.step;
+  float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!(q < P.max_q)) {
+    atomicAdd(&P.counters[2], 1ull);
+    return c;
+  }
+  const int n = int(q) + 1;
+  float pos[3], inc[3], epos[3], einc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = (tout[a] - tin[a]) / q;
+    pos[a] = tin[a];
+    epos[a] = en[a];
+  }
+  einc[0] = (dx / len) * b.step;
+  einc[1] = (dy / len) * b.step;
+  einc[2] = (dz / len) * b.step;
+
+  BrickView<T> vol;
+  vol.p = static_cast<const T*>(P.pool) + b.off;
+  vol.n0 = int(b.n[0]); vol.n1 = int(b.n[1]); vol.n2 = int(b.n[2]);
+  vol.fn0 = float(b.n[0]); vol.fn1 = float(b.n[1]); vol.fn2 = float(b.n[2]);
+  vol.sx = b.n[0]; vol.sxy = b.n[0] * b.n[1];
+  const float vs0 = 1.0f / float(b.n[0]), vs1 = 1.0f / float(b.n[1]), vs2 = 1.0f / float(b.n[2]);
+  const bool lit = P.lighting != 0;
+  const bool two_d = P.mode == TVK_RM_2DTRANS;
+  const float W = float(P.tf_w), H = float(P.tf_h);
+  const float im = P.inv_max_raw;
+
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    ++shaded;
+    const float v = vol.sample_raw(pos[0], pos[1], pos[2]) * im;
+    const float u = v * P.trans_scale;
+    float fx = floorf(u * W);
+    fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
+    float4 src;
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+    bool need_grad = lit;
+    if (two_d) need_grad = P.tf_col_nonzero[int(fx)] != 0;
+    if (!two_d) {
+      src = __ldg(&P.tf[int(fx)]);
+      need_grad = lit && src.w != 0.0f;
+    }
+    if (need_grad) {
+      // Volume3D.glsl:43-54 (Yp sampled at -step.y)
+      const float xp = vol.sample_raw(pos[0] + vs0, pos[1], pos[2]) * im;
+      const float xm = vol.sample_raw(pos[0] + (-vs0), pos[1], pos[2]) * im;
+      const float yp = vol.sample_raw(pos[0], pos[1] + (-vs1), pos[2]) * im;
+      const float ym = vol.sample_raw(pos[0], pos[1] + vs1, pos[2]) * im;
+      const float zp = vol.sample_raw(pos[0], pos[1], pos[2] + vs2) * im;
+      const float zm = vol.sample_raw(pos[0], pos[1], pos[2] + (-vs2)) * im;
+      g0 = (xm - xp) / 2.0f;
+      g1 = (yp - ym) / 2.0f;
+      g2 = (zm - zp) / 2.0f;
+    }
+    if (two_d) {
+      if (need_grad) {
+        const float mag = len3(g0, g1, g2);
+        const float w = 1.0f - mag * P.grad_scale;
+        float fy = floorf(w * H);
+        fy = fminf(fmaxf(fy, 0.0f), H - 1.0f);
+        src = __ldg(&P.tf[int(fy) * P.tf_w + int(fx)]);
+      } else {
+        src = make_float4(0.f, 0.f, 0.f, 0.f);  // whole column transparent
+      }
+      need_grad = need_grad && lit && src.w != 0.0f;
+    }
+    if (lit && need_grad) {
+      const float gs0 = g0 * P.domain_scale[0], gs1 = g1 * P.domain_scale[1],
+                  gs2 = g2 * P.domain_scale[2];
+      float N[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        N[r] = fmaf(P.norm_mat[r][2], gs2, fmaf(P.norm_mat[r][1], gs1, P.norm_mat[r][0] * gs0));
+      const float l = len3(N[0], N[1], N[2]);
+      if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+      const float tfc[3] = {src.x, src.y, src.z};
+      float lc[3];
+      if (P.light_model == TVK_LIGHT_BLINN_PHONG)
+        lighting_bp(P, epos, N, tfc, lc);
+      else
+        lighting_ref(P, epos, N, tfc, lc);
+      src.x = lc[0]; src.y = lc[1]; src.z = lc[2];
+      if (two_d) src.w = fminf(fmaxf(src.w, 0.0f), 1.0f);
+    }
+    // Compositing.glsl:33-38 UnderCompositing
+    const float w = 1.0f - c.w;
+    c.x = fmaf(src.x * w, src.w, c.x);
+    c.y = fmaf(src.y * w, src.w, c.y);
+    c.z = fmaf(src.z * w, src.w, c.z);
+    c.w = fmaf(src.w, w, c.w);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      pos[a] = pos[a] + inc[a];
+      epos[a] = epos[a] + einc[a];
+    }
+    if (c.w >= 0.99f) break;
+  }
+  return c;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) raycast_kernel(const RenderParams P) {
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const uint32_t py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  if (px >= P.width || py >= P.height) return;
+
+  const float nx = (float(px) + 0.5f) * P.inv_w2 - 1.0f;
+  const float ny = (float(py) + 0.5f) * P.inv_h2 - 1.0f;
+  const float dir[3] = {nx * P.kx, ny * P.ky, -1.0f};
+  float o[3], inv[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = P.inv[a][3];
+    const float d = fmaf(P.inv[a][2], dir[2], fmaf(P.inv[a][1], dir[1], P.inv[a][0] * dir[0]));
+    inv[a] = 1.0f / d;
+  }
+
+  // bricks this ray crosses, ordered by entry distance (ties by brick order)
+  float h_t0[kMaxHits], h_t1[kMaxHits];
+  int h_b[kMaxHits];
+  int nh = 0;
+  for (uint32_t bi = 0; bi < P.n_bricks; ++bi) {
+    const DevBrick& b = P.bricks[bi];
+    float tn = -INFINITY, tf = INFINITY;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float t0 = (__ldg(&b.pmin[a]) - o[a]) * inv[a];
+      const float t1 = (__ldg(&b.pmax[a]) - o[a]) * inv[a];
+      tn = fmaxf(tn, fminf(t0, t1));
+      tf = fminf(tf, fmaxf(t0, t1));
+    }
+    const float ti = fmaxf(tn, P.znear);
+    if (!(tf > ti) || tf > P.zfar) continue;
+    if (nh == kMaxHits) {
+      atomicAdd(&P.counters[2], 1ull);
+      break;
+    }
+    int j = nh++;
+    while (j > 0 && h_t0[j - 1] > ti) {  // stable: equal entries keep brick order
+      h_t0[j] = h_t0[j - 1]; h_t1[j] = h_t1[j - 1]; h_b[j] = h_b[j - 1];
+      --j;
+    }
+    h_t0[j] = ti; h_t1[j] = tf; h_b[j] = int(bi);
+  }
+
+  float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t samples = 0, shaded = 0;
+  for (int h = 0; h < nh; ++h) {
+    if (frame.w >= P.frame_ert) break;
+    const DevBrick b = P.bricks[h_b[h]];
+    const float4 c = march_brick<T>(P, b, dir, h_t0[h], h_t1[h], samples, shaded);
+    const float w = 1.0f - frame.w;
+    frame.x = fmaf(c.x, w, frame.x);
+    frame.y = fmaf(c.y, w, frame.y);
+    frame.z = fmaf(c.z, w, frame.z);
+    frame.w = fmaf(c.w, w, frame.w);
+  }
+  const size_t pix = size_t(py) * P.width + px;
+  P.out[pix] = frame;
+  if (P.spp) P.spp[pix] = samples;
+  // frame totals: one atomic per warp (lanes off the image have returned)
+  const uint32_t active = __activemask();
+  const uint32_t s = __reduce_add_sync(active, samples);
+  const uint32_t sh = __reduce_add_sync(active, shaded);
+  if (lane == uint32_t(__ffs(active) - 1)) {
+    atomicAdd(&P.counters[0], (unsigned long long)s);
+    atomicAdd(&P.counters[1], (unsigned long long)sh);
+  }
+}
+
+}  // namespace
+
+void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
+  const dim3 block(128);
+  const dim3 grid((p.width + 15) / 16, (p.height + 7) / 8);
+  if (p.bytes == 1)
+    raycast_kernel<uint8_t><<<grid, block, 0, s>>>(p);
+  else
+    raycast_kernel<uint16_t><<<grid, block, 0, s>>>(p);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+}  // namespace tvk

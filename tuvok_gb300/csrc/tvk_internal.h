@@ -1,0 +1,142 @@
+// tvk_internal.h -- shared host/device definitions of the tuvok_gb300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tvk.h"
+
+namespace tvk {
+
+// ------------------------------------------------------------------ errors
+
+struct Error {
+  tvk_status status;
+  std::string msg;
+};
+
+[[noreturn]] void fail(tvk_status s, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what);
+#define TVK_CUDA(call) ::tvk::check_cuda((call), #call)
+
+// ------------------------------------------------------------------ bricking
+
+// One LOD of the ExtendedOctree table (IO/UVF/ExtendedOctree/ExtendedOctree.h).
+struct LodInfo {
+  uint64_t size[3];
+  uint64_t bricks[3];
+  double aspect[3];
+};
+
+// Device-side accumulators of the bricking pass (global scratch memory).
+struct BrickScratch {
+  uint32_t* bmin;       // per brick
+  uint32_t* bmax;       // per brick
+  uint32_t* bhist;      // per brick x 256
+  unsigned long long* hist;  // global histogram, 2^(8*bytes) bins
+  unsigned long long* max_grad_bits;  // IEEE double bits of the max |grad|
+  uint32_t* raw_minmax;  // [min, max] of the raw volume
+};
+
+// Geometry of the LOD-0 brick grid handed to the bricking kernels.
+struct BrickGrid {
+  uint64_t dims[3];
+  uint32_t B[3];        // max brick size incl. overlap
+  uint32_t ov;
+  uint32_t cnt[3];      // bricks per axis
+  int clamp;
+  uint64_t total;       // voxels of the raw volume
+};
+
+void launch_raw_minmax(const void* raw, int bytes, uint64_t n, uint32_t* minmax,
+                       cudaStream_t s, uint64_t* launches);
+void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g,
+                       const uint64_t* d_offsets, const uint32_t* d_sizes, uint64_t n_bricks,
+                       void* pool, const BrickScratch& sc, uint32_t hist_shift,
+                       uint32_t global_bins, cudaStream_t s, uint64_t* launches);
+void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
+                         const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
+                         uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
+                         uint64_t* launches);
+void launch_generate(void* out, int bytes, const uint64_t dims[3], const float* d_blobs,
+                     uint32_t n_blobs, float noise_amp, uint32_t octaves, float cell,
+                     uint64_t seed, int int_noise, float vmax, cudaStream_t s);
+
+// ------------------------------------------------------------------ ray march
+
+// Per-brick record of one frame (host-computed, uploaded per paint).
+struct alignas(16) DevBrick {
+  float pmin[3];
+  float step;           // fRayStepsize
+  float pmax[3];
+  uint32_t pad0;
+  float tex[3][4];      // eye -> brick texture coordinates
+  uint32_t n[3];        // voxels incl. ghost
+  uint32_t pad1;
+  unsigned long long off;  // voxel offset of the brick in the pool
+  unsigned long long pad2;
+};
+
+struct RenderParams {
+  const void* pool;
+  int bytes;                 // 1 or 2
+  const DevBrick* bricks;    // visible bricks only, compact
+  uint32_t n_bricks;
+  const float4* tf;          // rgb + opacity-corrected alpha
+  const uint8_t* tf_col_nonzero;  // 2D: per value column, any alpha > 0
+  uint32_t tf_w, tf_h;
+  int mode;                  // tvk_render_mode
+  int lighting;
+  int light_model;
+  float trans_scale, grad_scale;
+  float inv_max_raw;
+  float light_a[3], light_d[3], light_s[3], light_dir[3];
+  float bp_ka, bp_kd, bp_ks, bp_shininess;
+  float norm_mat[3][3];
+  float domain_scale[3];
+  float inv[3][4];           // eye -> model (rigid)
+  float kx, ky, inv_w2, inv_h2;
+  float znear, zfar;
+  float frame_ert;
+  float max_q;               // guard on len/step
+  uint32_t width, height;
+  float4* out;
+  uint32_t* spp;             // per-pixel sample counts (may be null)
+  unsigned long long* counters;  // [samples, shaded, errors]
+};
+
+void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
+
+}  // namespace tvk
+
+// ------------------------------------------------------------------ handles
+
+struct tvk_volume {
+  int device = 0;
+  tvk_dtype dtype = TVK_U8;
+  int bytes = 1;
+  uint64_t dims[3] = {0, 0, 0};
+  uint32_t brick_size[3] = {0, 0, 0};
+  uint32_t overlap = 0;
+  bool clamp = false;
+  std::vector<tvk::LodInfo> lods;
+  uint64_t n_bricks = 0;  // LOD 0
+  std::vector<tvk_brick_md> md;
+  std::vector<uint64_t> offsets;  // voxels, per brick
+  std::vector<uint32_t> sizes;    // 3 per brick
+  std::vector<double> bmin, bmax;
+  std::vector<unsigned long long> hist;
+  std::vector<uint32_t> bhist;
+  uint32_t hist_shift = 0;
+  uint64_t hist_trimmed = 0;
+  double range_min = 0, range_max = 0, max_grad = 0;
+  void* d_pool = nullptr;
+  size_t pool_bytes = 0;
+};
+
+struct tvk_renderer;
+
+static_assert(sizeof(tvk::DevBrick) == 112, "DevBrick layout is part of the per-frame upload size");

@@ -1,0 +1,269 @@
+"""Python mirror of Tuvok's renderer and dataset interfaces over the C ABI.
+
+``Volume`` stands where Tuvok's bricked dataset (``BrickedDataset`` /
+``UVFDataset`` built by ``ExtendedOctreeConverter``) stands; ``Renderer``
+keeps ``AbstrRenderer``'s method names (Renderer/AbstrRenderer.h) so callers
+and tests read like the reference's.  All compute runs in libtvk.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from ._native import check, lib
+
+
+def _u64(v):
+    return (C.c_uint64 * len(v))(*[int(x) for x in v])
+
+
+def _u32(v):
+    return (C.c_uint32 * len(v))(*[int(x) for x in v])
+
+
+def _f32(v):
+    return (C.c_float * len(v))(*[float(x) for x in v])
+
+
+class Volume:
+    """A volume bricked on the GPU (LOD 0 with ghost voxels + statistics).
+
+    ``data`` is a numpy array indexed [z, y, x] (x fastest in memory), or a
+    device pointer (int) together with ``dims`` and ``dtype``.
+    """
+
+    def __init__(self, data, brick_size=(64, 64, 64), overlap=1, clamp_to_edge=False,
+                 dims=None, dtype=None):
+        h = C.c_void_p()
+        bs = _u32(brick_size)
+        if isinstance(data, np.ndarray):
+            arr = np.ascontiguousarray(data)
+            if arr.dtype == np.uint8:
+                dt = N.TVK_U8
+            elif arr.dtype == np.uint16:
+                dt = N.TVK_U16
+            else:
+                raise TypeError("volumes are uint8 or uint16")
+            z, y, x = arr.shape
+            check(lib().tvk_volume_create(arr.ctypes.data_as(C.c_void_p), dt, _u64((x, y, z)),
+                                          bs, overlap, int(clamp_to_edge), C.byref(h)))
+        else:
+            if dims is None or dtype is None:
+                raise ValueError("a device pointer needs dims=(x, y, z) and dtype")
+            dt = N.TVK_U8 if np.dtype(dtype) == np.uint8 else N.TVK_U16
+            check(lib().tvk_volume_create_device(C.c_void_p(int(data)), dt, _u64(dims), bs,
+                                                 overlap, int(clamp_to_edge), C.byref(h)))
+        self._h = h
+        self.info = N.VolumeInfo()
+        check(lib().tvk_volume_get_info(self._h, C.byref(self.info)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            check(lib().tvk_volume_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- dataset interface (IO/Dataset.h, IO/BrickedDataset.h)
+    @property
+    def np_dtype(self):
+        return np.uint8 if self.info.dtype == N.TVK_U8 else np.uint16
+
+    def GetDomainSize(self, lod=0):
+        s, b = _u64((0, 0, 0)), _u64((0, 0, 0))
+        check(lib().tvk_volume_get_lod(self._h, lod, s, b))
+        return tuple(s)
+
+    def GetBrickLayout(self, lod=0):
+        s, b = _u64((0, 0, 0)), _u64((0, 0, 0))
+        check(lib().tvk_volume_get_lod(self._h, lod, s, b))
+        return tuple(b)
+
+    def GetLODLevelCount(self):
+        return int(self.info.lod_count)
+
+    def GetRange(self):
+        return (self.info.range_min, self.info.range_max)
+
+    def MaxGradientMagnitude(self):
+        return self.info.max_gradient
+
+    def GetBrickCount(self, lod=0):
+        b = self.GetBrickLayout(lod)
+        return b[0] * b[1] * b[2]
+
+    def GetBrickMetadata(self, key):
+        ts, lod, idx = key
+        md = N.BrickMD()
+        check(lib().tvk_volume_get_brick_md(self._h, ts, lod, idx, C.byref(md)))
+        return md
+
+    def GetBrick(self, key):
+        """Brick voxels (ghost included) as a numpy array [z, y, x]."""
+        md = self.GetBrickMetadata(key)
+        nx, ny, nz = md.n_voxels
+        out = np.empty((nz, ny, nx), dtype=self.np_dtype)
+        ts, lod, idx = key
+        check(lib().tvk_volume_get_brick(self._h, ts, lod, idx, out.ctypes.data_as(C.c_void_p),
+                                         out.nbytes))
+        return out
+
+    def MaxMinForKey(self, key):
+        ts, lod, idx = key
+        mm = N.MinMax()
+        check(lib().tvk_volume_get_minmax(self._h, ts, lod, idx, C.byref(mm)))
+        return mm
+
+    def GetHistogram(self):
+        bins = 1 << (8 * (1 if self.info.dtype == N.TVK_U8 else 2))
+        out = np.zeros(bins, dtype=np.uint64)
+        tl = C.c_uint64()
+        check(lib().tvk_volume_get_histogram(self._h, out.ctypes.data_as(N._u64p), bins,
+                                             C.byref(tl)))
+        return out, int(tl.value)
+
+    def GetBrickHistograms(self):
+        n = int(self.info.lod0_bricks)
+        out = np.zeros((n, 256), dtype=np.uint32)
+        sh = C.c_uint32()
+        check(lib().tvk_volume_get_brick_histograms(self._h, out.ctypes.data_as(N._u32p), n,
+                                                    C.byref(sh)))
+        return out, int(sh.value)
+
+    def IndexFrom4D(self, x, y, z, lod):
+        out = C.c_uint64()
+        check(lib().tvk_volume_index_from_4d(self._h, _u64((x, y, z, lod)), C.byref(out)))
+        return int(out.value)
+
+    def IndexTo4D(self, lod, idx):
+        out = _u64((0, 0, 0, 0))
+        check(lib().tvk_volume_index_to_4d(self._h, lod, idx, out))
+        return tuple(out)
+
+
+class Renderer:
+    """GLRaycaster-equivalent renderer (AbstrRenderer's API over libtvk.so)."""
+
+    RM_1DTRANS, RM_2DTRANS, RM_ISOSURFACE = (N.TVK_RM_1DTRANS, N.TVK_RM_2DTRANS,
+                                              N.TVK_RM_ISOSURFACE)
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().tvk_renderer_create(C.byref(h)))
+        self._h = h
+        self._w = self._h_px = 0
+        self._vol = None
+
+    def close(self):
+        if self._h:
+            check(lib().tvk_renderer_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- AbstrRenderer surface
+    def RegisterDataset(self, vol: Volume):
+        self._vol = vol
+        check(lib().tvk_renderer_set_volume(self._h, vol.handle))
+
+    def Set1DTrans(self, rgba_bytes):
+        a = np.ascontiguousarray(np.asarray(rgba_bytes, dtype=np.uint8).reshape(-1))
+        check(lib().tvk_set_tf1d_rgba8(self._h, a.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                       a.size // 4))
+
+    def Set1DTransFloat(self, rgba, rgba8_upload=False):
+        a = np.ascontiguousarray(np.asarray(rgba, dtype=np.float32).reshape(-1))
+        check(lib().tvk_set_tf1d_float(self._h, a.ctypes.data_as(N._f32p), a.size // 4,
+                                       int(rgba8_upload)))
+
+    def Set2DTransFloat(self, rgba, rgba8_upload=False):
+        a = np.ascontiguousarray(np.asarray(rgba, dtype=np.float32))
+        h, w = a.shape[0], a.shape[1]
+        check(lib().tvk_set_tf2d_float(self._h, a.reshape(-1).ctypes.data_as(N._f32p), w, h,
+                                       int(rgba8_upload)))
+
+    def SetRendermode(self, mode):
+        check(lib().tvk_set_render_mode(self._h, int(mode)))
+
+    def SetUseLighting(self, on):
+        check(lib().tvk_set_lighting(self._h, int(bool(on))))
+
+    def SetSampleRateModifier(self, srm):
+        check(lib().tvk_set_sample_rate_modifier(self._h, float(srm)))
+
+    def SetIsoValue(self, v):
+        check(lib().tvk_set_isovalue(self._h, float(v)))
+
+    def SetColors(self, ambient, diffuse, specular, light_dir):
+        check(lib().tvk_set_colors(self._h, _f32(ambient), _f32(diffuse), _f32(specular),
+                                   _f32(light_dir)))
+
+    def SetLightModel(self, model, ka=0.2, kd=0.6, ks=0.2, shininess=32.0):
+        check(lib().tvk_set_light_model(self._h, int(model), ka, kd, ks, shininess))
+
+    def SetViewParameters(self, fov, znear, zfar, eye=(0, 0, 1.6), at=(0, 0, 0), up=(0, 1, 0)):
+        check(lib().tvk_set_view(self._h, _f32(eye), _f32(at), _f32(up), float(fov),
+                                 float(znear), float(zfar)))
+
+    def SetFrameTermination(self, threshold):
+        check(lib().tvk_set_frame_termination(self._h, float(threshold)))
+
+    def Resize(self, w, h):
+        check(lib().tvk_resize(self._h, int(w), int(h)))
+        self._w, self._h_px = int(w), int(h)
+
+    def Paint(self):
+        check(lib().tvk_paint(self._h))
+
+    def ReadBackPixels(self, out=None):
+        """Last frame as float32 [height, width, 4], row 0 = bottom row."""
+        if out is None:
+            out = np.empty((self._h_px, self._w, 4), dtype=np.float32)
+        check(lib().tvk_read_image(self._h, out.ctypes.data_as(N._f32p), out.size))
+        return out
+
+    def ReadSampleCounts(self):
+        out = np.empty((self._h_px, self._w), dtype=np.uint32)
+        check(lib().tvk_read_sample_counts(self._h, out.ctypes.data_as(N._u32p), out.size))
+        return out
+
+    def GetStats(self):
+        s = N.Stats()
+        check(lib().tvk_get_stats(self._h, C.byref(s)))
+        return s
+
+    def GetStream(self):
+        s = C.c_void_p()
+        check(lib().tvk_renderer_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def GetLastFBO(self):
+        p = C.c_void_p()
+        w, h = C.c_uint32(), C.c_uint32()
+        check(lib().tvk_get_image_device(self._h, C.byref(p), C.byref(w), C.byref(h)))
+        return p.value, w.value, h.value
+
+
+def generate_volume_device(ptr, dims, dtype, blobs, noise_amp, octaves, cell, seed, int_noise,
+                           vmax):
+    """Fills device memory at ``ptr`` with a seeded blob volume (see tvk.h)."""
+    b = np.ascontiguousarray(np.asarray(blobs, dtype=np.float32).reshape(-1))
+    dt = N.TVK_U8 if np.dtype(dtype) == np.uint8 else N.TVK_U16
+    check(lib().tvk_generate_volume(C.c_void_p(int(ptr)), dt, _u64(dims),
+                                    b.ctypes.data_as(N._f32p), b.size // 7, float(noise_amp),
+                                    int(octaves), float(cell), int(seed), int(int_noise),
+                                    float(vmax)))
