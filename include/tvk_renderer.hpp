@@ -1,0 +1,166 @@
+// tvk_renderer.hpp -- header-only C++ shim over the C ABI (tvk.h) that keeps
+// Tuvok's renderer and dataset method names, so code written against
+// AbstrRenderer (Renderer/AbstrRenderer.h:112-881) and BrickedDataset
+// (IO/BrickedDataset.h:46-96) ports by changing the class names.  Errors throw
+// tvk::Exception (the reference throws tuvok::Exception / std::runtime_error
+// or returns false with a T_ERROR log).
+#ifndef TVK_RENDERER_HPP
+#define TVK_RENDERER_HPP
+
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "tvk.h"
+
+namespace tvk {
+
+struct Exception : std::runtime_error {
+  tvk_status status;
+  Exception(tvk_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(tvk_status s) {
+  if (s != TVK_OK)
+    throw Exception(s, std::string(tvk_status_string(s)) + ": " + tvk_last_error());
+}
+
+// IO/Brick.h:57: BrickKey = (timestep, LOD, 1D index)
+using BrickKey = std::tuple<uint64_t, uint64_t, uint64_t>;
+
+// A volume bricked on the GPU (the LOD-0 level of what
+// ExtendedOctreeConverter::Convert produces, with per-brick statistics).
+class BrickedVolume {
+ public:
+  BrickedVolume(const void* host_voxels, tvk_dtype dtype, std::array<uint64_t, 3> dims,
+                std::array<uint32_t, 3> brick_size, uint32_t overlap, bool clamp_to_edge = false) {
+    check(tvk_volume_create(host_voxels, dtype, dims.data(), brick_size.data(), overlap,
+                            clamp_to_edge ? 1 : 0, &v_));
+  }
+  ~BrickedVolume() { tvk_volume_destroy(v_); }
+  BrickedVolume(const BrickedVolume&) = delete;
+  BrickedVolume& operator=(const BrickedVolume&) = delete;
+
+  tvk_volume* handle() const { return v_; }
+
+  tvk_volume_info Info() const {
+    tvk_volume_info i;
+    check(tvk_volume_get_info(v_, &i));
+    return i;
+  }
+  std::pair<double, double> GetRange() const {
+    const tvk_volume_info i = Info();
+    return {i.range_min, i.range_max};
+  }
+  float MaxGradientMagnitude() const { return float(Info().max_gradient); }
+  uint64_t GetLODLevelCount() const { return Info().lod_count; }
+  std::array<uint64_t, 3> GetDomainSize(uint32_t lod = 0) const {
+    std::array<uint64_t, 3> s, b;
+    check(tvk_volume_get_lod(v_, lod, s.data(), b.data()));
+    return s;
+  }
+  std::array<uint64_t, 3> GetBrickLayout(uint32_t lod = 0) const {
+    std::array<uint64_t, 3> s, b;
+    check(tvk_volume_get_lod(v_, lod, s.data(), b.data()));
+    return b;
+  }
+  tvk_brick_md GetBrickMetadata(const BrickKey& k) const {
+    tvk_brick_md m;
+    check(tvk_volume_get_brick_md(v_, std::get<0>(k), std::get<1>(k), std::get<2>(k), &m));
+    return m;
+  }
+  template <class T>
+  bool GetBrick(const BrickKey& k, std::vector<T>& out) const {
+    const tvk_brick_md m = GetBrickMetadata(k);
+    out.resize(size_t(m.n_voxels[0]) * m.n_voxels[1] * m.n_voxels[2]);
+    check(tvk_volume_get_brick(v_, std::get<0>(k), std::get<1>(k), std::get<2>(k), out.data(),
+                               out.size() * sizeof(T)));
+    return true;
+  }
+  tvk_minmax MaxMinForKey(const BrickKey& k) const {
+    tvk_minmax m;
+    check(tvk_volume_get_minmax(v_, std::get<0>(k), std::get<1>(k), std::get<2>(k), &m));
+    return m;
+  }
+  BrickKey IndexFrom4D(uint64_t x, uint64_t y, uint64_t z, uint64_t lod,
+                       uint64_t timestep = 0) const {
+    const uint64_t xyzl[4] = {x, y, z, lod};
+    uint64_t idx = 0;
+    check(tvk_volume_index_from_4d(v_, xyzl, &idx));
+    return BrickKey(timestep, lod, idx);
+  }
+
+ private:
+  tvk_volume* v_ = nullptr;
+};
+
+// The renderer, named after AbstrRenderer's methods.
+class Renderer {
+ public:
+  enum ERenderMode { RM_1DTRANS = TVK_RM_1DTRANS, RM_2DTRANS = TVK_RM_2DTRANS,
+                     RM_ISOSURFACE = TVK_RM_ISOSURFACE };
+
+  Renderer() { check(tvk_renderer_create(&r_)); }
+  ~Renderer() { tvk_renderer_destroy(r_); }
+  Renderer(const Renderer&) = delete;
+  Renderer& operator=(const Renderer&) = delete;
+
+  bool RegisterDataset(const BrickedVolume& v) {
+    check(tvk_renderer_set_volume(r_, v.handle()));
+    return true;
+  }
+  // AbstrRenderer::Set1DTrans(const std::vector<unsigned char>&)
+  void Set1DTrans(const std::vector<unsigned char>& rgba) {
+    check(tvk_set_tf1d_rgba8(r_, rgba.data(), uint32_t(rgba.size() / 4)));
+  }
+  void Set1DTransFloat(const std::vector<float>& rgba, bool rgba8_upload = false) {
+    check(tvk_set_tf1d_float(r_, rgba.data(), uint32_t(rgba.size() / 4), rgba8_upload));
+  }
+  void Set2DTransFloat(const std::vector<float>& rgba, uint32_t w, uint32_t h) {
+    check(tvk_set_tf2d_float(r_, rgba.data(), w, h, 0));
+  }
+  void SetRendermode(ERenderMode m) { check(tvk_set_render_mode(r_, tvk_render_mode(m))); }
+  void SetUseLighting(bool on) { check(tvk_set_lighting(r_, on ? 1 : 0)); }
+  void SetSampleRateModifier(float f) { check(tvk_set_sample_rate_modifier(r_, f)); }
+  void SetIsoValue(float v) { check(tvk_set_isovalue(r_, v)); }
+  void SetColors(const float ambient[4], const float diffuse[4], const float specular[4],
+                 const float light_dir[3]) {
+    check(tvk_set_colors(r_, ambient, diffuse, specular, light_dir));
+  }
+  void SetViewParameters(float fov, float znear, float zfar, const float eye[3],
+                         const float at[3], const float up[3]) {
+    check(tvk_set_view(r_, eye, at, up, fov, znear, zfar));
+  }
+  void Resize(uint32_t w, uint32_t h) {
+    check(tvk_resize(r_, w, h));
+    w_ = w;
+    h_ = h;
+  }
+  bool Paint() {
+    check(tvk_paint(r_));
+    return true;
+  }
+  // GLRenderer::GetLastFBO + GLFBOTex::ReadBackPixels
+  std::vector<float> ReadBackPixels() {
+    std::vector<float> img(size_t(w_) * h_ * 4);
+    check(tvk_read_image(r_, img.data(), img.size()));
+    return img;
+  }
+  tvk_stats Stats() {
+    tvk_stats s;
+    check(tvk_get_stats(r_, &s));
+    return s;
+  }
+  tvk_renderer* handle() const { return r_; }
+
+ private:
+  tvk_renderer* r_ = nullptr;
+  uint32_t w_ = 0, h_ = 0;
+};
+
+}  // namespace tvk
+
+#endif  // TVK_RENDERER_HPP
