@@ -238,6 +238,43 @@ tvk_status tvk_renderer_get_stream(tvk_renderer* r, void** stream);
 /* Blocks until the renderer's stream is idle and fills *out for the last paint. */
 tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out);
 
+/* ---------------------------------------------------------------- allocation-free bricking */
+
+/* Most entry points allocate device memory as they go (tvk_volume_create
+ * allocates its brick pool and statistics scratch).  Some callers cannot allow
+ * that at call time: a host that gives the library a fixed device-memory budget
+ * up front, or code that records work into a stream capture or draws only from
+ * its own pre-sized pool.  For them this entry point bricks up to
+ * TVK_NOALLOC_MAX_BRICKS LOD-0 bricks of a volume that is already in device
+ * memory and allocates nothing: the caller passes every input and output, and
+ * the per-brick min/max and histogram accumulators live in a fixed array inside
+ * the library (about 66 KB on every GPU that loads it, held until the process
+ * exits).  It has no counterpart in the reference.
+ *
+ * The bricks' voxels are the same as tvk_volume_create / tvk_volume_get_brick
+ * return (GetInputBrick + ClampToEdge semantics); they are written back to back
+ * in the order of brick_coords (x, y, z triples, LOD 0) into device_bricks_out.
+ * device_minmax_out receives one tvk_minmax and device_hist_out 256 counts per
+ * brick (inner voxels, bin = value >> hist_shift; pass the shift that
+ * tvk_volume_get_brick_histograms reports to get the same bins).  Work is
+ * queued on `stream` (a cudaStream_t, NULL for the legacy default stream) and
+ * the call returns without waiting.
+ *   - count above TVK_NOALLOC_MAX_BRICKS, or an output smaller than the
+ *     bricks, is rejected with TVK_ERR_INVALID_ARG and a message;
+ *   - the fixed accumulators are shared: each call clears what it uses, and
+ *     calls whose GPU work overlaps (different streams or host threads) race;
+ *   - the first call on a device looks up the accumulators' device address for
+ *     that device (the current device); make that first call before any stream
+ *     capture starts. */
+#define TVK_NOALLOC_MAX_BRICKS 64
+tvk_status tvk_brick_lod0_noalloc(const void* device_voxels, tvk_dtype dtype,
+                                  const uint64_t dims[3], const uint32_t brick_size[3],
+                                  uint32_t overlap, int clamp_to_edge,
+                                  const uint64_t* brick_coords, uint32_t count,
+                                  uint32_t hist_shift, void* device_bricks_out, size_t out_bytes,
+                                  tvk_minmax* device_minmax_out, uint32_t* device_hist_out,
+                                  void* stream);
+
 /* ---------------------------------------------------------------- synthetic data */
 
 /* Fills device memory with a seeded volume: the sum of Gaussian blobs (7

@@ -97,6 +97,8 @@ PROTOTYPES = {
     "tvk_get_stats": [_vp, C.POINTER(Stats)],
     "tvk_generate_volume": [_vp, C.c_int, _u64p, _f32p, C.c_uint32, C.c_float, C.c_uint32,
                             C.c_float, C.c_uint64, C.c_int, C.c_float],
+    "tvk_brick_lod0_noalloc": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, _u64p,
+                               C.c_uint32, C.c_uint32, _vp, C.c_size_t, _vp, _vp, _vp],
 }
 _RET = {"tvk_status_string": C.c_char_p, "tvk_last_error": C.c_char_p,
         "tvk_abi_version": C.c_int}

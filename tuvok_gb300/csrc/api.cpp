@@ -25,6 +25,8 @@ thread_local std::string g_last_error;
 
 void fail(tvk_status s, const std::string& msg) { throw Error{s, msg}; }
 
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 void check_cuda(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return;
   const tvk_status s = (e == cudaErrorMemoryAllocation) ? TVK_ERR_OUT_OF_MEMORY : TVK_ERR_CUDA;

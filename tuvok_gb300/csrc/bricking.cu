@@ -19,6 +19,11 @@
 // All of this is integer work and HBM-bound: reads are contiguous along x, the
 // pool is written in the same order, histograms live in shared memory and are
 // merged with one atomic per non-zero bin and CTA.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+
 #include "tvk_internal.h"
 
 namespace tvk {
@@ -243,4 +248,216 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
   ++*launches;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free LOD-0 bricking (tvk_brick_lod0_noalloc).
+//
+// Callers that cannot allocate device memory at call time -- a host that hands
+// the library a fixed memory budget up front, or code running under a stream
+// capture or inside a pre-sized memory pool -- still need the per-brick
+// statistics, which the regular path accumulates in device scratch it
+// allocates per volume.  This variant keeps that scratch in a file-scope
+// __device__ array instead: every GPU that loads the library holds
+// kNoAllocScratchWords 32-bit words (about 66 KB) of it until the process exits,
+// enough for kNoAllocMaxBricks bricks per call.  The array is shared by all
+// calls: each call clears the part it uses before accumulating, and calls
+// whose work overlaps on the GPU (on different streams, or from several host
+// threads) race on it.  Host code cannot use the array's name as a device
+// address, so its address is looked up once per device, with that device
+// current, on the first call made on that device; make that first call before
+// any stream capture begins.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxBricks = TVK_NOALLOC_MAX_BRICKS;
+constexpr uint32_t kNoAllocWordsPerBrick = 2 + 256;  // min, max, 256 bins
+constexpr uint32_t kNoAllocScratchWords = kNoAllocMaxBricks * kNoAllocWordsPerBrick;
+
+__device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
+
+struct NoAllocBatch {
+  uint32_t coords[kNoAllocMaxBricks][3];
+  uint32_t sizes[kNoAllocMaxBricks][3];
+  unsigned long long out_offset[kNoAllocMaxBricks];  // voxels into the output
+  uint32_t count;
+};
+
+__global__ void noalloc_clear_kernel(uint32_t* scratch, uint32_t count) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count * kNoAllocWordsPerBrick;
+       i += gridDim.x * blockDim.x)
+    scratch[i] = (i % kNoAllocWordsPerBrick == 0) ? 0xffffffffu : 0u;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+noalloc_brick_kernel(const T* __restrict__ raw, BrickGrid g, NoAllocBatch batch,
+                     T* __restrict__ out, uint32_t* scratch, uint32_t shift, uint32_t z_chunk) {
+  __shared__ uint32_t bh[256];
+  const uint32_t b = blockIdx.x;
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) bh[i] = 0;
+  __syncthreads();
+  const uint32_t bs[3] = {batch.sizes[b][0], batch.sizes[b][1], batch.sizes[b][2]};
+  const uint32_t c[3] = {batch.coords[b][0], batch.coords[b][1], batch.coords[b][2]};
+  const uint32_t z0 = blockIdx.y * z_chunk;
+  const uint32_t z1 = min(bs[2], z0 + z_chunk);
+  T* dst = out + batch.out_offset[b];
+  const uint32_t sxy = bs[0] * bs[1];
+  uint32_t lo = 0xffffffffu, hi = 0;
+  if (z0 < z1) {
+    const uint32_t n = (z1 - z0) * sxy;
+    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+      const uint32_t k = z0 + t / sxy;
+      const uint32_t r = t - (k - z0) * sxy;
+      const uint32_t j = r / bs[0];
+      const uint32_t i = r - j * bs[0];
+      const T v = source_voxel<T>(raw, g, c, bs, i, j, k);
+      dst[uint64_t(k) * sxy + r] = v;
+      const uint32_t u = v;
+      lo = min(lo, u);
+      hi = max(hi, u);
+      if (i >= g.ov && i < bs[0] - g.ov && j >= g.ov && j < bs[1] - g.ov && k >= g.ov &&
+          k < bs[2] - g.ov)
+        atomicAdd(&bh[min(u >> shift, 255u)], 1u);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  uint32_t* mine = scratch + b * kNoAllocWordsPerBrick;
+  if ((threadIdx.x & 31) == 0 && lo <= hi) {
+    atomicMin(&mine[0], lo);
+    atomicMax(&mine[1], hi);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x)
+    if (bh[i]) atomicAdd(&mine[2 + i], bh[i]);
+}
+
+__global__ void noalloc_finish_kernel(const uint32_t* scratch, uint32_t count,
+                                      tvk_minmax* minmax_out, uint32_t* hist_out) {
+  const uint32_t b = blockIdx.x;
+  if (b >= count) return;
+  const uint32_t* mine = scratch + b * kNoAllocWordsPerBrick;
+  if (threadIdx.x == 0) {
+    // MaxMinDataBlock::SetDataFromFlatVector (IO/UVF/MaxMinDataBlock.cpp:175-195)
+    tvk_minmax m;
+    m.min_scalar = double(mine[0]);
+    m.max_scalar = double(mine[1]);
+    m.min_gradient = -1.7976931348623157e308;
+    m.max_gradient = 1.7976931348623157e308;
+    minmax_out[b] = m;
+  }
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist_out[256u * b + i] = mine[2 + i];
+}
+
+// Device address of g_noalloc_scratch, looked up once per device.
+uint32_t* noalloc_scratch_for_current_device() {
+  static std::mutex mu;
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  TVK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) fail(TVK_ERR_UNSUPPORTED, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      fail(TVK_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") +
+                             cudaGetErrorString(e));
+    addr[dev] = p;
+  }
+  return static_cast<uint32_t*>(addr[dev]);
+}
+
+void brick_lod0_noalloc(const void* raw, tvk_dtype dtype, const uint64_t dims[3],
+                        const uint32_t bsz[3], uint32_t ov, int clamp, const uint64_t* coords,
+                        uint32_t count, uint32_t shift, void* bricks_out, size_t out_bytes,
+                        tvk_minmax* minmax_out, uint32_t* hist_out, cudaStream_t s) {
+  if (!raw || !dims || !bsz || !coords || !bricks_out || !minmax_out || !hist_out)
+    fail(TVK_ERR_INVALID_ARG, "null argument");
+  if (dtype != TVK_U8 && dtype != TVK_U16) fail(TVK_ERR_INVALID_ARG, "dtype must be u8 or u16");
+  if (count == 0 || count > kNoAllocMaxBricks)
+    fail(TVK_ERR_INVALID_ARG, "count must be 1.." + std::to_string(kNoAllocMaxBricks) +
+                                  " bricks per call (the fixed scratch holds that many)");
+  if (shift > 16) fail(TVK_ERR_INVALID_ARG, "histogram shift above 16");
+  const int bytes = dtype == TVK_U8 ? 1 : 2;
+  BrickGrid g;
+  uint64_t lod_size[3];
+  for (int a = 0; a < 3; ++a) {
+    if (dims[a] < 1) fail(TVK_ERR_INVALID_ARG, "volume dimensions must be >= 1");
+    if (bsz[a] <= 2 * ov || bsz[a] > 4096)
+      fail(TVK_ERR_INVALID_ARG, "brick size must exceed twice the overlap and be <= 4096");
+    const uint64_t usable = bsz[a] - 2ull * ov;
+    g.dims[a] = dims[a];
+    g.B[a] = bsz[a];
+    g.cnt[a] = uint32_t((dims[a] + usable - 1) / usable);  // ExtendedOctree.cpp:231-236
+    lod_size[a] = dims[a];
+  }
+  g.ov = ov;
+  g.clamp = clamp ? 1 : 0;
+  g.total = dims[0] * dims[1] * dims[2];
+  NoAllocBatch batch;
+  std::memset(&batch, 0, sizeof(batch));
+  batch.count = count;
+  uint64_t off = 0;
+  uint32_t max_z = 0;
+  for (uint32_t b = 0; b < count; ++b) {
+    for (int a = 0; a < 3; ++a) {
+      const uint64_t c = coords[3 * b + a];
+      if (c >= g.cnt[a]) fail(TVK_ERR_INVALID_ARG, "brick coordinate out of range");
+      const uint64_t core = bsz[a] - 2ull * ov;
+      const bool last = c == g.cnt[a] - 1;  // ExtendedOctree::ComputeBrickSize
+      batch.sizes[b][a] =
+          uint32_t((last && (lod_size[a] % core)) ? (2ull * ov + lod_size[a] % core) : bsz[a]);
+      batch.coords[b][a] = uint32_t(c);
+    }
+    batch.out_offset[b] = off;
+    off += uint64_t(batch.sizes[b][0]) * batch.sizes[b][1] * batch.sizes[b][2];
+    max_z = std::max(max_z, batch.sizes[b][2]);
+  }
+  if (off * bytes > out_bytes)
+    fail(TVK_ERR_INVALID_ARG, "output buffer holds " + std::to_string(out_bytes) +
+                                  " bytes, the bricks need " + std::to_string(off * bytes));
+  uint32_t* scratch = noalloc_scratch_for_current_device();
+  noalloc_clear_kernel<<<8, 256, 0, s>>>(scratch, count);
+  TVK_CUDA(cudaGetLastError());
+  const uint32_t z_chunk = 8;
+  const dim3 grid(count, (max_z + z_chunk - 1) / z_chunk);
+  if (bytes == 1)
+    noalloc_brick_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(raw), g, batch, static_cast<uint8_t*>(bricks_out), scratch,
+        shift, z_chunk);
+  else
+    noalloc_brick_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(raw), g, batch, static_cast<uint16_t*>(bricks_out), scratch,
+        shift, z_chunk);
+  TVK_CUDA(cudaGetLastError());
+  noalloc_finish_kernel<<<count, 256, 0, s>>>(scratch, count, minmax_out, hist_out);
+  TVK_CUDA(cudaGetLastError());
+}
+
+}  // namespace
 }  // namespace tvk
+
+extern "C" tvk_status tvk_brick_lod0_noalloc(const void* device_voxels, tvk_dtype dtype,
+                                             const uint64_t dims[3], const uint32_t brick_size[3],
+                                             uint32_t overlap, int clamp_to_edge,
+                                             const uint64_t* brick_coords, uint32_t count,
+                                             uint32_t hist_shift, void* device_bricks_out,
+                                             size_t out_bytes, tvk_minmax* device_minmax_out,
+                                             uint32_t* device_hist_out, void* stream) {
+  try {
+    tvk::brick_lod0_noalloc(device_voxels, dtype, dims, brick_size, overlap, clamp_to_edge,
+                            brick_coords, count, hist_shift, device_bricks_out, out_bytes,
+                            device_minmax_out, device_hist_out, static_cast<cudaStream_t>(stream));
+    tvk::set_last_error("");
+    return TVK_OK;
+  } catch (const tvk::Error& e) {
+    tvk::set_last_error(e.msg);
+    return e.status;
+  } catch (...) {
+    tvk::set_last_error("unknown failure");
+    return TVK_ERR_INTERNAL;
+  }
+}

@@ -20,6 +20,8 @@ struct Error {
 
 [[noreturn]] void fail(tvk_status s, const std::string& msg);
 void check_cuda(cudaError_t e, const char* what);
+// Sets the calling thread's message returned by tvk_last_error().
+void set_last_error(const std::string& msg);
 #define TVK_CUDA(call) ::tvk::check_cuda((call), #call)
 
 // ------------------------------------------------------------------ bricking
