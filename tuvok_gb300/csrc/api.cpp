@@ -253,6 +253,32 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   // pass 3: maximum gradient magnitude over inner voxels
   launch_max_gradient(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                       V->n_bricks, V->overlap, max_bz, sc.max_grad_bits, s, &launches);
+  // pass 4: macro-cell min/max for empty-space skipping inside bricks
+  V->cell_offsets.resize(V->n_bricks);
+  V->cell_counts.resize(V->n_bricks);
+  V->cell_dims.resize(V->n_bricks);
+  uint32_t max_cells = 0;
+  V->total_cells = 0;
+  for (uint64_t k = 0; k < V->n_bricks; ++k) {
+    const uint32_t cx = cells_per_axis(V->sizes[3 * k]), cy = cells_per_axis(V->sizes[3 * k + 1]),
+                   cz = cells_per_axis(V->sizes[3 * k + 2]);
+    V->cell_dims[k] = cx | (cy << 10) | (cz << 20);
+    V->cell_counts[k] = cx * cy * cz;
+    V->cell_offsets[k] = V->total_cells;
+    V->total_cells += V->cell_counts[k];
+    max_cells = std::max(max_cells, V->cell_counts[k]);
+  }
+  TVK_CUDA(cudaMalloc(&V->d_cells, V->total_cells * sizeof(uint32_t)));
+  TVK_CUDA(cudaMalloc(&V->d_cell_meta, V->n_bricks * (sizeof(uint64_t) + sizeof(uint32_t))));
+  uint64_t* d_cell_off = static_cast<uint64_t*>(V->d_cell_meta);
+  uint32_t* d_cell_cnt = reinterpret_cast<uint32_t*>(d_cell_off + V->n_bricks);
+  TVK_CUDA(cudaMemcpyAsync(d_cell_off, V->cell_offsets.data(), V->n_bricks * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_cell_cnt, V->cell_counts.data(), V->n_bricks * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+  launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                     d_cell_off, V->n_bricks, max_cells, static_cast<uint32_t*>(V->d_cells), s,
+                     &launches);
 
   std::vector<uint32_t> bmin(V->n_bricks), bmax(V->n_bricks);
   V->hist.resize(gbins);
@@ -276,6 +302,13 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   uint64_t len = gbins;
   while (len > 0 && V->hist[len - 1] == 0) --len;
   V->hist_trimmed = len;
+}
+
+void free_volume_device(tvk_volume* V) {
+  for (void** p : {&V->d_pool, &V->d_cells, &V->d_cell_meta}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
 }
 
 tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, const uint64_t dims[3],
@@ -317,8 +350,7 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
     }
   } catch (...) {
     cudaStreamSynchronize(s);
-    if (V->d_pool) cudaFree(V->d_pool);
-    V->d_pool = nullptr;
+    free_volume_device(V.get());
     throw;
   }
   return V.release();
@@ -433,6 +465,11 @@ struct tvk_renderer {
   tvk::PinnedBuf h_bricks, h_counters;
   tvk::PinnedBuf h_tf;
   float tf_step_scale = -1.0f;  // step scale the device table was built for
+  // empty-cell bits for the current TF and volume
+  tvk::DevBuf d_empty, d_empty_meta, d_tfpfx;
+  std::vector<uint64_t> empty_word_off;
+  bool empty_valid = false;
+  bool cell_skip = true;
   tvk_stats stats{};
   uint64_t launches = 0;
   bool painted = false;
@@ -457,14 +494,56 @@ void upload_tf(tvk_renderer* R, float step_scale) {
     // VRender1D.glsl:53 opacity correction, evaluated per table entry
     const float a = R->tf[4 * i + 3];
     t[4 * i + 3] = 1.0f - std::pow(1.0f - a, step_scale);
-    if (a != 0.0f) col[i % R->tf_w] = 1;
+    // a sample whose corrected alpha is exactly 0 adds exactly nothing
+    if (t[4 * i + 3] != 0.0f) col[i % R->tf_w] = 1;
   }
   R->d_tf.ensure(n * sizeof(float4));
   R->d_tfcol.ensure(R->tf_w);
   TVK_CUDA(cudaMemcpyAsync(R->d_tf.p, t, n * sizeof(float4), cudaMemcpyHostToDevice, R->stream));
   TVK_CUDA(cudaMemcpyAsync(R->d_tfcol.p, col, R->tf_w, cudaMemcpyHostToDevice, R->stream));
+  // prefix counts of value columns with any non-zero corrected alpha
+  std::vector<uint32_t> pfx(R->tf_w + 1, 0);
+  for (uint32_t x = 0; x < R->tf_w; ++x) pfx[x + 1] = pfx[x] + (col[x] ? 1u : 0u);
+  R->d_tfpfx.ensure(pfx.size() * sizeof(uint32_t));
+  TVK_CUDA(cudaMemcpy(R->d_tfpfx.p, pfx.data(), pfx.size() * sizeof(uint32_t),
+                      cudaMemcpyHostToDevice));
   R->tf_dirty = false;
   R->tf_step_scale = step_scale;
+  R->empty_valid = false;
+}
+
+// Empty-cell bits of every LOD-0 brick for the current TF (re-run when the TF,
+// the sample rate or the volume changes).
+void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale) {
+  if (R->empty_valid) return;
+  R->empty_word_off.resize(V->n_bricks);
+  uint64_t words = 0;
+  uint32_t max_words = 0;
+  for (uint64_t k = 0; k < V->n_bricks; ++k) {
+    R->empty_word_off[k] = words;
+    const uint32_t w = (V->cell_counts[k] + 31) / 32;
+    words += w;
+    max_words = std::max(max_words, w);
+  }
+  R->d_empty.ensure(std::max<uint64_t>(1, words) * sizeof(uint32_t));
+  R->d_empty_meta.ensure(V->n_bricks * sizeof(uint64_t));
+  TVK_CUDA(cudaMemcpyAsync(R->d_empty_meta.p, R->empty_word_off.data(),
+                           V->n_bricks * sizeof(uint64_t), cudaMemcpyHostToDevice, R->stream));
+  EmptyCellParams p;
+  p.cell_minmax = static_cast<const uint32_t*>(V->d_cells);
+  p.cell_offsets = static_cast<const uint64_t*>(V->d_cell_meta);
+  p.cell_counts = reinterpret_cast<const uint32_t*>(p.cell_offsets + V->n_bricks);
+  p.word_offsets = R->d_empty_meta.as<uint64_t>();
+  p.n_bricks = V->n_bricks;
+  p.nz_prefix = R->d_tfpfx.as<uint32_t>();
+  p.tf_w = R->tf_w;
+  p.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  p.trans_scale = trans_scale;
+  p.bits = R->d_empty.as<uint32_t>();
+  launch_empty_cells(p, max_words, R->stream, &R->launches);
+  // the word offsets above were copied from pageable memory; keep them alive
+  TVK_CUDA(cudaStreamSynchronize(R->stream));
+  R->empty_valid = true;
 }
 
 void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgba8) {
@@ -497,6 +576,10 @@ void paint(tvk_renderer* R) {
   const float srm = R->srm;
   const float step_scale = 1.0f / srm * 1.0f;
   upload_tf(R, step_scale);
+  // GLRenderer.cpp:1813-1819 CalculateScaling
+  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
+  const float trans_scale = float(double(imax) / V->range_max);
+  if (R->cell_skip) update_empty_cells(R, V, trans_scale);
 
   const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
 
@@ -558,6 +641,8 @@ void paint(tvk_renderer* R) {
     }
     b.step = stp;
     b.off = V->offsets[k];
+    b.cells = V->cell_dims[k];
+    b.empty_off = R->cell_skip ? R->empty_word_off[k] : 0;
   }
   R->d_bricks.ensure(std::max<size_t>(1, V->n_bricks) * sizeof(DevBrick));
   if (nvis)
@@ -578,9 +663,8 @@ void paint(tvk_renderer* R) {
   P.mode = R->mode;
   P.lighting = R->lighting ? 1 : 0;
   P.light_model = R->light_model;
-  // GLRenderer.cpp:1813-1819 CalculateScaling
-  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
-  P.trans_scale = float(double(imax) / rmax);
+  P.empty_bits = R->cell_skip ? R->d_empty.as<uint32_t>() : nullptr;
+  P.trans_scale = trans_scale;
   const float mg = float(V->max_grad);
   P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;  // GLRenderer.cpp:1840-1841
   P.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
@@ -676,7 +760,7 @@ tvk_status tvk_volume_create_device(const void* device_voxels, tvk_dtype dtype,
 tvk_status tvk_volume_destroy(tvk_volume* v) {
   return guarded([&] {
     if (!v) return;
-    if (v->d_pool) cudaFree(v->d_pool);
+    tvk::free_volume_device(v);
     delete v;
   });
 }
@@ -823,6 +907,7 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
   return guarded([&] {
     REQUIRE(r, "null renderer");
     r->vol = v;
+    r->empty_valid = false;
   });
 }
 

@@ -248,6 +248,55 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
   ++*launches;
 }
 
+namespace {
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                   const uint32_t* __restrict__ sizes, const uint64_t* __restrict__ cell_off,
+                   uint32_t* __restrict__ cells) {
+  // one thread per macro cell of brick blockIdx.y: min/max over voxels
+  // c*kCell .. (c+1)*kCell on each axis, clamped to the brick
+  const uint32_t b = blockIdx.y;
+  const uint32_t n0 = sizes[3 * b], n1 = sizes[3 * b + 1], n2 = sizes[3 * b + 2];
+  const uint32_t cx = cells_per_axis(n0), cy = cells_per_axis(n1), cz = cells_per_axis(n2);
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cx * cy * cz) return;
+  const uint32_t x = c % cx, y = (c / cx) % cy, z = c / (cx * cy);
+  const T* p = pool + offsets[b];
+  const uint32_t x0 = x << kCellShift, x1 = min(x0 + kCell, n0 - 1);
+  const uint32_t y0 = y << kCellShift, y1 = min(y0 + kCell, n1 - 1);
+  const uint32_t z0 = z << kCellShift, z1 = min(z0 + kCell, n2 - 1);
+  uint32_t lo = 0xffffu, hi = 0;
+  for (uint32_t k = z0; k <= z1; ++k)
+    for (uint32_t j = y0; j <= y1; ++j) {
+      const T* row = p + (uint64_t(k) * n1 + j) * n0;
+      for (uint32_t i = x0; i <= x1; ++i) {
+        const uint32_t v = row[i];
+        lo = min(lo, v);
+        hi = max(hi, v);
+      }
+    }
+  cells[cell_off[b] + c] = lo | (hi << 16);
+}
+
+}  // namespace
+
+void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, const uint64_t* d_cell_offsets,
+                        uint64_t n_bricks, uint32_t max_cells_per_brick, uint32_t* cells,
+                        cudaStream_t s, uint64_t* launches) {
+  const dim3 grid((max_cells_per_brick + kThreads - 1) / kThreads, uint32_t(n_bricks));
+  if (bytes == 1)
+    cell_minmax_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(pool), d_offsets, d_sizes, d_cell_offsets, cells);
+  else
+    cell_minmax_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(pool), d_offsets, d_sizes, d_cell_offsets, cells);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
 // ---------------------------------------------------------------------------
 // Allocation-free LOD-0 bricking (tvk_brick_lod0_noalloc).
 //

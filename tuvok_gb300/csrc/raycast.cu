@@ -50,6 +50,10 @@ struct BrickView {
     u0 = fminf(fmaxf(u0, 0.0f), float(n0 - 1));
     u1 = fminf(fmaxf(u1, 0.0f), float(n1 - 1));
     u2 = fminf(fmaxf(u2, 0.0f), float(n2 - 1));
+    return sample_u(u0, u1, u2);
+  }
+  // the same from voxel coordinates already clamped to [0, n-1]
+  __device__ __forceinline__ float sample_u(float u0, float u1, float u2) const {
     const int x0 = int(u0), y0 = int(u1), z0 = int(u2);
     const float fx = u0 - float(x0), fy = u1 - float(y0), fz = u2 - float(z0);
     const int x1 = min(x0 + 1, n0 - 1), y1 = min(y0 + 1, n1 - 1), z1 = min(z0 + 1, n2 - 1);
@@ -166,11 +170,56 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   const bool two_d = P.mode == TVK_RM_2DTRANS;
   const float W = float(P.tf_w), H = float(P.tf_h);
   const float im = P.inv_max_raw;
+  // macro cells of kCell^3 voxel positions (see DevBrick::cells)
+  const uint32_t* __restrict__ empty = P.empty_bits ? P.empty_bits + b.empty_off : nullptr;
+  const int ncx = int(b.cells & 1023u), ncy = int((b.cells >> 10) & 1023u);
+  const float du0 = inc[0] * vol.fn0, du1 = inc[1] * vol.fn1, du2 = inc[2] * vol.fn2;
+  const float idu0 = 1.0f / fabsf(du0), idu1 = 1.0f / fabsf(du1), idu2 = 1.0f / fabsf(du2);
 
   for (int i = 0; i < n; ++i) {
     ++samples;
+    const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
+    const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
+    const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
+    const float u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
+    const float u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
+    const float u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+    if (empty) {
+      const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
+                cz = int(u2) >> kCellShift;
+      const uint32_t cell = uint32_t((cz * ncy + cy) * ncx + cx);
+      if ((__ldg(&empty[cell >> 5]) >> (cell & 31)) & 1u) {
+        // Every voxel a trilinear lookup from this cell can touch maps to TF
+        // entries with zero corrected alpha, so this step adds exactly zero.
+        // Further steps are skipped while they provably stay in the cell: the
+        // position keeps the reference's accumulated additions, and the margin
+        // of 1/64 voxel covers their rounding (< 1e-3 voxel over a cell).
+        int k = 0;
+        if (uu0 == u0 && uu1 == u1 && uu2 == u2) {
+          const float lo0 = float(cx << kCellShift), lo1 = float(cy << kCellShift),
+                      lo2 = float(cz << kCellShift);
+          const float d0 = du0 > 0.0f ? lo0 + float(kCell) - uu0 : uu0 - lo0;
+          const float d1 = du1 > 0.0f ? lo1 + float(kCell) - uu1 : uu1 - lo1;
+          const float d2 = du2 > 0.0f ? lo2 + float(kCell) - uu2 : uu2 - lo2;
+          const float m = fminf(fminf((d0 - 0.015625f) * idu0, (d1 - 0.015625f) * idu1),
+                                (d2 - 0.015625f) * idu2);
+          k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
+        }
+        samples += uint32_t(k);
+        for (int j = 0; j <= k; ++j) {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+          if (lit) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
+          }
+        }
+        i += k;
+        continue;
+      }
+    }
     ++shaded;
-    const float v = vol.sample_raw(pos[0], pos[1], pos[2]) * im;
+    const float v = vol.sample_u(u0, u1, u2) * im;
     const float u = v * P.trans_scale;
     float fx = floorf(u * W);
     fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
@@ -311,7 +360,44 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RenderParams P) {
   }
 }
 
+// TF entry a raw value maps to, exactly as the march computes it
+__device__ __forceinline__ int tf_index(uint32_t raw, float im, float ts, float W) {
+  const float v = float(raw) * im;
+  const float u = v * ts;
+  float fx = floorf(u * W);
+  fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
+  return int(fx);
+}
+
+__global__ void empty_cells_kernel(const EmptyCellParams P) {
+  // one thread per 32-cell word of brick blockIdx.y
+  const uint32_t b = blockIdx.y;
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t ncell = P.cell_counts[b];
+  if (w * 32 >= ncell) return;
+  const uint32_t* cm = P.cell_minmax + P.cell_offsets[b];
+  const float W = float(P.tf_w);
+  uint32_t bits = 0;
+  for (uint32_t j = 0; j < 32 && w * 32 + j < ncell; ++j) {
+    const uint32_t mm = cm[w * 32 + j];
+    // trilinear results lie in [min, max] and the index is monotone in the
+    // value, so the cell reaches exactly the entries lo..hi
+    const int lo = tf_index(mm & 0xffffu, P.inv_max_raw, P.trans_scale, W);
+    const int hi = tf_index(mm >> 16, P.inv_max_raw, P.trans_scale, W);
+    if (P.nz_prefix[hi + 1] == P.nz_prefix[lo]) bits |= 1u << j;
+  }
+  P.bits[P.word_offsets[b] + w] = bits;
+}
+
 }  // namespace
+
+void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, cudaStream_t s,
+                        uint64_t* launches) {
+  const dim3 grid((max_words_per_brick + 127) / 128, uint32_t(p.n_bricks));
+  empty_cells_kernel<<<grid, 128, 0, s>>>(p);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 block(128);

@@ -69,24 +69,57 @@ void launch_generate(void* out, int bytes, const uint64_t dims[3], const float* 
 
 // ------------------------------------------------------------------ ray march
 
+// Macro cells for empty-space skipping inside a brick: cell c on an axis
+// covers sample positions u in [c*kCell, (c+1)*kCell) (voxel coordinates after
+// clamping to [0, n-1]); its min/max cover voxels c*kCell .. (c+1)*kCell
+// (clamped), every voxel a trilinear lookup from such a position can touch.
+constexpr int kCellShift = 3;
+constexpr int kCell = 1 << kCellShift;
+__host__ __device__ inline uint32_t cells_per_axis(uint32_t n) {
+  return ((n - 1) >> kCellShift) + 1;
+}
+
 // Per-brick record of one frame (host-computed, uploaded per paint).
 struct alignas(16) DevBrick {
   float pmin[3];
   float step;           // fRayStepsize
   float pmax[3];
-  uint32_t pad0;
+  uint32_t cells;       // cells per axis, packed x | y << 10 | z << 20
   float tex[3][4];      // eye -> brick texture coordinates
   uint32_t n[3];        // voxels incl. ghost
   uint32_t pad1;
-  unsigned long long off;  // voxel offset of the brick in the pool
-  unsigned long long pad2;
+  unsigned long long off;        // voxel offset of the brick in the pool
+  unsigned long long empty_off;  // word offset of the brick's empty-cell bits
 };
+
+// Per-cell min/max of every LOD-0 brick (volume creation); packed min | max << 16.
+void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, const uint64_t* d_cell_offsets,
+                        uint64_t n_bricks, uint32_t max_cells_per_brick, uint32_t* cells,
+                        cudaStream_t s, uint64_t* launches);
+
+// Empty-cell bits for the current transfer function (1 = every reachable TF
+// entry has zero corrected alpha).
+struct EmptyCellParams {
+  const uint32_t* cell_minmax;         // volume cells
+  const uint64_t* cell_offsets;        // per brick, first cell
+  const uint32_t* cell_counts;         // per brick, cells in total
+  const uint64_t* word_offsets;        // per brick, first word of its bits
+  uint64_t n_bricks;
+  const uint32_t* nz_prefix;           // prefix count of non-zero TF entries / columns
+  uint32_t tf_w;
+  float inv_max_raw, trans_scale;
+  uint32_t* bits;
+};
+void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, cudaStream_t s,
+                        uint64_t* launches);
 
 struct RenderParams {
   const void* pool;
   int bytes;                 // 1 or 2
   const DevBrick* bricks;    // visible bricks only, compact
   uint32_t n_bricks;
+  const uint32_t* empty_bits;  // empty-cell bits (null: no skipping inside bricks)
   const float4* tf;          // rgb + opacity-corrected alpha
   const uint8_t* tf_col_nonzero;  // 2D: per value column, any alpha > 0
   uint32_t tf_w, tf_h;
@@ -137,6 +170,13 @@ struct tvk_volume {
   double range_min = 0, range_max = 0, max_grad = 0;
   void* d_pool = nullptr;
   size_t pool_bytes = 0;
+  // macro cells of the LOD-0 bricks
+  std::vector<uint64_t> cell_offsets;   // per brick, first cell
+  std::vector<uint32_t> cell_counts;    // per brick
+  std::vector<uint32_t> cell_dims;      // packed x | y << 10 | z << 20
+  uint64_t total_cells = 0;
+  void* d_cells = nullptr;              // uint32 per cell
+  void* d_cell_meta = nullptr;          // cell offsets (u64) + counts (u32) per brick
 };
 
 struct tvk_renderer;

@@ -121,7 +121,15 @@ PLAIN_LARGE_LIT = Workload(
     int_noise=False, brick_core=128, overlap=1, width=1920, height=1080, srm=1.5,
     lighting=True, light_model=1, tf_kind="bands4096", seed=4321)
 
-WORKLOADS = {w.name: w for w in (PLAIN_SMALL, PLAIN_LARGE_LIT)}
+# The large lit scene at half resolution (512^3, blobs and noise cells scaled
+# by 1/2): the profiling case whose brick pool (~280 MB) still exceeds L2.
+PLAIN_MEDIUM_LIT = Workload(
+    name="plain_medium_lit", dims=(512, 512, 512), dtype=np.uint16, vmax=4095, n_blobs=256,
+    sigma=(8, 40), peak=(512, 3584), noise_amp=409.5, noise_octaves=3, noise_cell=64.0,
+    int_noise=False, brick_core=128, overlap=1, width=1920, height=1080, srm=1.5,
+    lighting=True, light_model=1, tf_kind="bands4096", seed=4321)
+
+WORKLOADS = {w.name: w for w in (PLAIN_SMALL, PLAIN_LARGE_LIT, PLAIN_MEDIUM_LIT)}
 
 
 def numpy_blob_volume(dims, dtype, n_blobs, sigma, peak, vmax, seed, noise=0):
