@@ -611,8 +611,39 @@ void paint(tvk_renderer* R) {
   R->h_bricks.ensure(V->n_bricks * sizeof(DevBrick));
   DevBrick* hb = R->h_bricks.as<DevBrick>();
   uint32_t nvis = 0;
+  // Front-to-back order valid for every ray: bricks sorted by L1 distance of
+  // their grid coordinates from the eye's brick cell.  Along a ray that
+  // distance grows at every crossing into the next brick, so this order
+  // restates the per-ray entry-distance order of the brick loop
+  // (AbstrRenderer.cpp:1097 sorts by corner distance instead).
+  const LodInfo& l0 = V->lods[0];
+  int64_t eye_cell[3];
+  for (int a = 0; a < 3; ++a) {
+    const double o = view.inv[a][3];
+    const uint64_t stride = a == 0 ? 1 : (a == 1 ? l0.bricks[0] : l0.bricks[0] * l0.bricks[1]);
+    int64_t e = int64_t(l0.bricks[a]);
+    for (uint64_t i = 0; i < l0.bricks[a]; ++i) {
+      const tvk_brick_md& m = V->md[i * stride];
+      const double lo_b = double(m.center[a] * vs[a] - m.extents[a] * vs[a] / 2.0f);
+      const double hi_b = double(m.center[a] * vs[a] + m.extents[a] * vs[a] / 2.0f);
+      if (i == 0 && o < lo_b) { e = -1; break; }
+      if (o < hi_b) { e = int64_t(i); break; }
+    }
+    eye_cell[a] = e;
+  }
+  std::vector<std::pair<uint64_t, uint64_t>> order;  // (L1 distance, brick)
+  order.reserve(V->n_bricks);
   for (uint64_t k = 0; k < V->n_bricks; ++k) {
     if (!(hi >= V->bmin[k] && lo <= V->bmax[k])) continue;
+    const int64_t c[3] = {int64_t(k % l0.bricks[0]), int64_t((k / l0.bricks[0]) % l0.bricks[1]),
+                          int64_t(k / (l0.bricks[0] * l0.bricks[1]))};
+    uint64_t d = 0;
+    for (int a = 0; a < 3; ++a) d += uint64_t(std::llabs(c[a] - eye_cell[a]));
+    order.emplace_back(d, k);
+  }
+  std::sort(order.begin(), order.end());
+  for (const auto& ok : order) {
+    const uint64_t k = ok.second;
     const tvk_brick_md& m = V->md[k];
     DevBrick& b = hb[nvis++];
     std::memset(&b, 0, sizeof(b));
@@ -677,6 +708,7 @@ void paint(tvk_renderer* R) {
     P.domain_scale[a] = 1.0f / float(user_scale[a]);
     for (int j = 0; j < 3; ++j) P.norm_mat[a][j] = float(view.mv[a][j]);
     for (int j = 0; j < 4; ++j) P.inv[a][j] = float(view.inv[a][j]);
+    for (int j = 0; j < 4; ++j) P.mv[a][j] = float(view.mv[a][j]);
   }
   P.bp_ka = R->bp[0];
   P.bp_kd = R->bp[1];

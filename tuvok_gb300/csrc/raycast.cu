@@ -22,7 +22,11 @@
 namespace tvk {
 namespace {
 
-constexpr int kMaxHits = 64;
+// CTAs of 128 threads the register allocation must leave room for per SM
+// (occupancy against spills; measured on GB300).
+#ifndef TVK_RAYCAST_MIN_BLOCKS
+#define TVK_RAYCAST_MIN_BLOCKS 6
+#endif
 
 __device__ __forceinline__ float affine_row(const float r[4], float x, float y, float z) {
   return fmaf(r[0], x, fmaf(r[1], y, fmaf(r[2], z, r[3])));
@@ -70,6 +74,98 @@ struct BrickView {
     return fmaf(fz, c1 - c0, c0);
   }
 };
+
+// Footprint of a centre sample, kept so the six central-difference lookups
+// (each one voxel away along one axis) reuse its index math and its voxels.
+// Every lookup still evaluates exactly the oracle's trilinear: the unshifted
+// axes' coordinates are the centre's (the same float expression), and a
+// voxel is taken from the centre's registers only when its index is equal.
+struct Foot {
+  int x0, x1, y0, y1, z0, z1;
+  float fx, fy, fz;
+  float v000, v100, v010, v110, v001, v101, v011, v111;
+};
+
+template <class T>
+__device__ __forceinline__ float centre_sample(const BrickView<T>& B, float u0, float u1,
+                                               float u2, Foot& f) {
+  f.x0 = int(u0); f.y0 = int(u1); f.z0 = int(u2);
+  f.fx = u0 - float(f.x0); f.fy = u1 - float(f.y0); f.fz = u2 - float(f.z0);
+  f.x1 = min(f.x0 + 1, B.n0 - 1); f.y1 = min(f.y0 + 1, B.n1 - 1); f.z1 = min(f.z0 + 1, B.n2 - 1);
+  f.v000 = B.fetch(f.x0, f.y0, f.z0); f.v100 = B.fetch(f.x1, f.y0, f.z0);
+  f.v010 = B.fetch(f.x0, f.y1, f.z0); f.v110 = B.fetch(f.x1, f.y1, f.z0);
+  f.v001 = B.fetch(f.x0, f.y0, f.z1); f.v101 = B.fetch(f.x1, f.y0, f.z1);
+  f.v011 = B.fetch(f.x0, f.y1, f.z1); f.v111 = B.fetch(f.x1, f.y1, f.z1);
+  const float c00 = fmaf(f.fx, f.v100 - f.v000, f.v000);
+  const float c10 = fmaf(f.fx, f.v110 - f.v010, f.v010);
+  const float c01 = fmaf(f.fx, f.v101 - f.v001, f.v001);
+  const float c11 = fmaf(f.fx, f.v111 - f.v011, f.v011);
+  const float c0 = fmaf(f.fy, c10 - c00, c00);
+  const float c1 = fmaf(f.fy, c11 - c01, c01);
+  return fmaf(f.fz, c1 - c0, c0);
+}
+
+// lookup with the x coordinate replaced by u (clamped voxel coordinate)
+template <class T>
+__device__ __forceinline__ float shifted_x(const BrickView<T>& B, const Foot& f, float u) {
+  const int a = int(u), b = min(a + 1, B.n0 - 1);
+  const float w = u - float(a);
+  float a00, a10, a01, a11, b00, b10, b01, b11;  // [y][z]
+  if (a == f.x0) { a00 = f.v000; a10 = f.v010; a01 = f.v001; a11 = f.v011; }
+  else if (a == f.x1) { a00 = f.v100; a10 = f.v110; a01 = f.v101; a11 = f.v111; }
+  else { a00 = B.fetch(a, f.y0, f.z0); a10 = B.fetch(a, f.y1, f.z0);
+         a01 = B.fetch(a, f.y0, f.z1); a11 = B.fetch(a, f.y1, f.z1); }
+  if (b == f.x1) { b00 = f.v100; b10 = f.v110; b01 = f.v101; b11 = f.v111; }
+  else if (b == f.x0) { b00 = f.v000; b10 = f.v010; b01 = f.v001; b11 = f.v011; }
+  else { b00 = B.fetch(b, f.y0, f.z0); b10 = B.fetch(b, f.y1, f.z0);
+         b01 = B.fetch(b, f.y0, f.z1); b11 = B.fetch(b, f.y1, f.z1); }
+  const float c00 = fmaf(w, b00 - a00, a00), c10 = fmaf(w, b10 - a10, a10);
+  const float c01 = fmaf(w, b01 - a01, a01), c11 = fmaf(w, b11 - a11, a11);
+  const float c0 = fmaf(f.fy, c10 - c00, c00), c1 = fmaf(f.fy, c11 - c01, c01);
+  return fmaf(f.fz, c1 - c0, c0);
+}
+
+template <class T>
+__device__ __forceinline__ float shifted_y(const BrickView<T>& B, const Foot& f, float u) {
+  const int a = int(u), b = min(a + 1, B.n1 - 1);
+  const float w = u - float(a);
+  float a00, a10, a01, a11, b00, b10, b01, b11;  // [x][z]
+  if (a == f.y0) { a00 = f.v000; a10 = f.v100; a01 = f.v001; a11 = f.v101; }
+  else if (a == f.y1) { a00 = f.v010; a10 = f.v110; a01 = f.v011; a11 = f.v111; }
+  else { a00 = B.fetch(f.x0, a, f.z0); a10 = B.fetch(f.x1, a, f.z0);
+         a01 = B.fetch(f.x0, a, f.z1); a11 = B.fetch(f.x1, a, f.z1); }
+  if (b == f.y1) { b00 = f.v010; b10 = f.v110; b01 = f.v011; b11 = f.v111; }
+  else if (b == f.y0) { b00 = f.v000; b10 = f.v100; b01 = f.v001; b11 = f.v101; }
+  else { b00 = B.fetch(f.x0, b, f.z0); b10 = B.fetch(f.x1, b, f.z0);
+         b01 = B.fetch(f.x0, b, f.z1); b11 = B.fetch(f.x1, b, f.z1); }
+  const float c00 = fmaf(f.fx, a10 - a00, a00), c10 = fmaf(f.fx, b10 - b00, b00);
+  const float c01 = fmaf(f.fx, a11 - a01, a01), c11 = fmaf(f.fx, b11 - b01, b01);
+  const float c0 = fmaf(w, c10 - c00, c00), c1 = fmaf(w, c11 - c01, c01);
+  return fmaf(f.fz, c1 - c0, c0);
+}
+
+template <class T>
+__device__ __forceinline__ float shifted_z(const BrickView<T>& B, const Foot& f, float u) {
+  const int a = int(u), b = min(a + 1, B.n2 - 1);
+  const float w = u - float(a);
+  float a00, a10, a01, a11, b00, b10, b01, b11;  // [x][y]
+  if (a == f.z0) { a00 = f.v000; a10 = f.v100; a01 = f.v010; a11 = f.v110; }
+  else if (a == f.z1) { a00 = f.v001; a10 = f.v101; a01 = f.v011; a11 = f.v111; }
+  else { a00 = B.fetch(f.x0, f.y0, a); a10 = B.fetch(f.x1, f.y0, a);
+         a01 = B.fetch(f.x0, f.y1, a); a11 = B.fetch(f.x1, f.y1, a); }
+  if (b == f.z1) { b00 = f.v001; b10 = f.v101; b01 = f.v011; b11 = f.v111; }
+  else if (b == f.z0) { b00 = f.v000; b10 = f.v100; b01 = f.v010; b11 = f.v110; }
+  else { b00 = B.fetch(f.x0, f.y0, b); b10 = B.fetch(f.x1, f.y0, b);
+         b01 = B.fetch(f.x0, f.y1, b); b11 = B.fetch(f.x1, f.y1, b); }
+  const float c00 = fmaf(f.fx, a10 - a00, a00), c10 = fmaf(f.fx, a11 - a01, a01);
+  const float c01 = fmaf(f.fx, b10 - b00, b00), c11 = fmaf(f.fx, b11 - b01, b01);
+  const float c0 = fmaf(f.fy, c10 - c00, c00), c1 = fmaf(f.fy, c11 - c01, c01);
+  return fmaf(w, c1 - c0, c0);
+}
+
+__device__ __forceinline__ float clamp_u(float t, float fn, int n) {
+  return fminf(fmaxf(fmaf(t, fn, -0.5f), 0.0f), float(n - 1));
+}
 
 __device__ __forceinline__ float pow_int_or_real(float x, float e) {
   if (e == 8.0f) { float a = x * x; a = a * a; return a * a; }
@@ -176,50 +272,57 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   const float du0 = inc[0] * vol.fn0, du1 = inc[1] * vol.fn1, du2 = inc[2] * vol.fn2;
   const float idu0 = 1.0f / fabsf(du0), idu1 = 1.0f / fabsf(du1), idu2 = 1.0f / fabsf(du2);
 
-  for (int i = 0; i < n; ++i) {
-    ++samples;
-    const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
-    const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
-    const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
-    const float u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
-    const float u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
-    const float u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
-    if (empty) {
+  int i = 0;
+  while (i < n) {
+    // Phase 1: run over empty macro cells.  Every voxel a trilinear lookup
+    // from such a cell can touch maps to TF entries with zero corrected
+    // alpha, so those steps add exactly zero.  Steps are skipped in bulk while
+    // they provably stay in the cell: the position keeps the reference's
+    // accumulated additions, and the margin of 1/64 voxel covers their
+    // rounding (< 1e-3 voxel across a cell).  Lanes of a warp reconverge
+    // before shading.
+    float u0, u1, u2;
+    for (;;) {
+      const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
+      const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
+      const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
+      u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
+      u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
+      u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+      if (!empty) break;
       const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
                 cz = int(u2) >> kCellShift;
       const uint32_t cell = uint32_t((cz * ncy + cy) * ncx + cx);
-      if ((__ldg(&empty[cell >> 5]) >> (cell & 31)) & 1u) {
-        // Every voxel a trilinear lookup from this cell can touch maps to TF
-        // entries with zero corrected alpha, so this step adds exactly zero.
-        // Further steps are skipped while they provably stay in the cell: the
-        // position keeps the reference's accumulated additions, and the margin
-        // of 1/64 voxel covers their rounding (< 1e-3 voxel over a cell).
-        int k = 0;
-        if (uu0 == u0 && uu1 == u1 && uu2 == u2) {
-          const float lo0 = float(cx << kCellShift), lo1 = float(cy << kCellShift),
-                      lo2 = float(cz << kCellShift);
-          const float d0 = du0 > 0.0f ? lo0 + float(kCell) - uu0 : uu0 - lo0;
-          const float d1 = du1 > 0.0f ? lo1 + float(kCell) - uu1 : uu1 - lo1;
-          const float d2 = du2 > 0.0f ? lo2 + float(kCell) - uu2 : uu2 - lo2;
-          const float m = fminf(fminf((d0 - 0.015625f) * idu0, (d1 - 0.015625f) * idu1),
-                                (d2 - 0.015625f) * idu2);
-          k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
-        }
-        samples += uint32_t(k);
-        for (int j = 0; j <= k; ++j) {
-#pragma unroll
-          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
-          if (lit) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
-          }
-        }
-        i += k;
-        continue;
+      if (!((__ldg(&empty[cell >> 5]) >> (cell & 31)) & 1u)) break;
+      int k = 0;
+      if (uu0 == u0 && uu1 == u1 && uu2 == u2) {
+        const float lo0 = float(cx << kCellShift), lo1 = float(cy << kCellShift),
+                    lo2 = float(cz << kCellShift);
+        const float d0 = du0 > 0.0f ? lo0 + float(kCell) - uu0 : uu0 - lo0;
+        const float d1 = du1 > 0.0f ? lo1 + float(kCell) - uu1 : uu1 - lo1;
+        const float d2 = du2 > 0.0f ? lo2 + float(kCell) - uu2 : uu2 - lo2;
+        const float m = fminf(fminf((d0 - 0.015625f) * idu0, (d1 - 0.015625f) * idu1),
+                              (d2 - 0.015625f) * idu2);
+        k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
       }
+      samples += uint32_t(k + 1);
+      for (int j = 0; j <= k; ++j) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+        if (lit) {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
+        }
+      }
+      i += k + 1;
+      if (i >= n) break;
     }
+    if (i >= n) break;
+    // Phase 2: the reference's step i
+    ++samples;
     ++shaded;
-    const float v = vol.sample_u(u0, u1, u2) * im;
+    Foot foot;
+    const float v = centre_sample(vol, u0, u1, u2, foot) * im;
     const float u = v * P.trans_scale;
     float fx = floorf(u * W);
     fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
@@ -233,12 +336,12 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
     }
     if (need_grad) {
       // Volume3D.glsl:43-54 (Yp sampled at -step.y)
-      const float xp = vol.sample_raw(pos[0] + vs0, pos[1], pos[2]) * im;
-      const float xm = vol.sample_raw(pos[0] + (-vs0), pos[1], pos[2]) * im;
-      const float yp = vol.sample_raw(pos[0], pos[1] + (-vs1), pos[2]) * im;
-      const float ym = vol.sample_raw(pos[0], pos[1] + vs1, pos[2]) * im;
-      const float zp = vol.sample_raw(pos[0], pos[1], pos[2] + vs2) * im;
-      const float zm = vol.sample_raw(pos[0], pos[1], pos[2] + (-vs2)) * im;
+      const float xp = shifted_x(vol, foot, clamp_u(pos[0] + vs0, vol.fn0, vol.n0)) * im;
+      const float xm = shifted_x(vol, foot, clamp_u(pos[0] + (-vs0), vol.fn0, vol.n0)) * im;
+      const float yp = shifted_y(vol, foot, clamp_u(pos[1] + (-vs1), vol.fn1, vol.n1)) * im;
+      const float ym = shifted_y(vol, foot, clamp_u(pos[1] + vs1, vol.fn1, vol.n1)) * im;
+      const float zp = shifted_z(vol, foot, clamp_u(pos[2] + vs2, vol.fn2, vol.n2)) * im;
+      const float zm = shifted_z(vol, foot, clamp_u(pos[2] + (-vs2), vol.fn2, vol.n2)) * im;
       g0 = (xm - xp) / 2.0f;
       g1 = (yp - ym) / 2.0f;
       g2 = (zm - zp) / 2.0f;
@@ -284,17 +387,47 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       pos[a] = pos[a] + inc[a];
       epos[a] = epos[a] + einc[a];
     }
+    ++i;
     if (c.w >= 0.99f) break;
   }
   return c;
 }
 
+constexpr uint32_t kCandChunk = 1024;
+
+// Conservative: can any pixel ray of the 16x8 tile at (tx0, ty0) meet brick b?
+// A ray through a pixel centre meets the box only if the centre lies in the
+// box's projection, hence in the bounding rectangle of its projected corners;
+// a 2-pixel margin covers rounding.  Bricks reaching behind the near plane
+// are always kept (the per-ray slab test decides).
+__device__ __forceinline__ bool footprint_touches_tile(const RenderParams& P, const DevBrick& b,
+                                                       float tx0, float ty0) {
+  float xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+  const float hw = 0.5f * float(P.width), hh = 0.5f * float(P.height);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const float x = (c & 1) ? b.pmax[0] : b.pmin[0];
+    const float y = (c & 2) ? b.pmax[1] : b.pmin[1];
+    const float z = (c & 4) ? b.pmax[2] : b.pmin[2];
+    const float ex = fmaf(P.mv[0][0], x, fmaf(P.mv[0][1], y, fmaf(P.mv[0][2], z, P.mv[0][3])));
+    const float ey = fmaf(P.mv[1][0], x, fmaf(P.mv[1][1], y, fmaf(P.mv[1][2], z, P.mv[1][3])));
+    const float ez = fmaf(P.mv[2][0], x, fmaf(P.mv[2][1], y, fmaf(P.mv[2][2], z, P.mv[2][3])));
+    if (ez > -0.5f * P.znear) return true;
+    const float iz = 1.0f / (-ez);
+    const float sx = (ex * iz / P.kx + 1.0f) * hw - 0.5f;
+    const float sy = (ey * iz / P.ky + 1.0f) * hh - 0.5f;
+    xmin = fminf(xmin, sx); xmax = fmaxf(xmax, sx);
+    ymin = fminf(ymin, sy); ymax = fmaxf(ymax, sy);
+  }
+  return xmax >= tx0 - 2.0f && xmin <= tx0 + 17.0f && ymax >= ty0 - 2.0f && ymin <= ty0 + 9.0f;
+}
+
 template <class T>
-__global__ void __launch_bounds__(128) raycast_kernel(const RenderParams P) {
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
   const uint32_t py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
-  if (px >= P.width || py >= P.height) return;
+  const bool active = px < P.width && py < P.height;
 
   const float nx = (float(px) + 0.5f) * P.inv_w2 - 1.0f;
   const float ny = (float(py) + 0.5f) * P.inv_h2 - 1.0f;
@@ -307,54 +440,69 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RenderParams P) {
     inv[a] = 1.0f / d;
   }
 
-  // bricks this ray crosses, ordered by entry distance (ties by brick order)
-  float h_t0[kMaxHits], h_t1[kMaxHits];
-  int h_b[kMaxHits];
-  int nh = 0;
-  for (uint32_t bi = 0; bi < P.n_bricks; ++bi) {
-    const DevBrick& b = P.bricks[bi];
-    float tn = -INFINITY, tf = INFINITY;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float t0 = (__ldg(&b.pmin[a]) - o[a]) * inv[a];
-      const float t1 = (__ldg(&b.pmax[a]) - o[a]) * inv[a];
-      tn = fmaxf(tn, fminf(t0, t1));
-      tf = fminf(tf, fmaxf(t0, t1));
-    }
-    const float ti = fmaxf(tn, P.znear);
-    if (!(tf > ti) || tf > P.zfar) continue;
-    if (nh == kMaxHits) {
-      atomicAdd(&P.counters[2], 1ull);
-      break;
-    }
-    int j = nh++;
-    while (j > 0 && h_t0[j - 1] > ti) {  // stable: equal entries keep brick order
-      h_t0[j] = h_t0[j - 1]; h_t1[j] = h_t1[j - 1]; h_b[j] = h_b[j - 1];
-      --j;
-    }
-    h_t0[j] = ti; h_t1[j] = tf; h_b[j] = int(bi);
-  }
+  // The host lists the visible bricks in a front-to-back order that holds for
+  // every ray (increasing L1 grid distance from the eye's brick cell, which
+  // strictly grows whenever a ray crosses into the next brick).  Each CTA
+  // keeps, in that order, the bricks whose screen footprint can touch its
+  // 16x8-pixel tile; each ray then marches those its own slab test hits.
+  __shared__ uint16_t cand[kCandChunk];
+  __shared__ uint32_t warp_cnt[4];
+  __shared__ uint32_t n_cand;
+  const float tx0 = float(blockIdx.x * 16), ty0 = float(blockIdx.y * 8);
 
   float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t samples = 0, shaded = 0;
-  for (int h = 0; h < nh; ++h) {
-    if (frame.w >= P.frame_ert) break;
-    const DevBrick b = P.bricks[h_b[h]];
-    const float4 c = march_brick<T>(P, b, dir, h_t0[h], h_t1[h], samples, shaded);
-    const float w = 1.0f - frame.w;
-    frame.x = fmaf(c.x, w, frame.x);
-    frame.y = fmaf(c.y, w, frame.y);
-    frame.z = fmaf(c.z, w, frame.z);
-    frame.w = fmaf(c.w, w, frame.w);
+  for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
+    const uint32_t end = min(P.n_bricks, base + kCandChunk);
+    __syncthreads();  // the previous chunk's list is no longer read
+    if (tid == 0) n_cand = 0;
+    for (uint32_t s = base; s < end; s += blockDim.x) {
+      const uint32_t i = s + tid;
+      const bool keep = i < end && footprint_touches_tile(P, P.bricks[i], tx0, ty0);
+      const uint32_t m = __ballot_sync(0xffffffffu, keep);
+      __syncthreads();
+      if (lane == 0) warp_cnt[warp] = __popc(m);
+      __syncthreads();
+      uint32_t off = n_cand;
+      for (uint32_t w2 = 0; w2 < warp; ++w2) off += warp_cnt[w2];
+      if (keep) cand[off + __popc(m & ((1u << lane) - 1u))] = uint16_t(i - base);
+      __syncthreads();
+      if (tid == 0) n_cand += warp_cnt[0] + warp_cnt[1] + warp_cnt[2] + warp_cnt[3];
+    }
+    __syncthreads();
+    if (!active) continue;
+    const uint32_t nc = n_cand;
+    for (uint32_t c = 0; c < nc; ++c) {
+      if (frame.w >= P.frame_ert) break;
+      const DevBrick& bg = P.bricks[base + cand[c]];
+      float tn = -INFINITY, tf = INFINITY;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float t0 = (__ldg(&bg.pmin[a]) - o[a]) * inv[a];
+        const float t1 = (__ldg(&bg.pmax[a]) - o[a]) * inv[a];
+        tn = fmaxf(tn, fminf(t0, t1));
+        tf = fminf(tf, fmaxf(t0, t1));
+      }
+      const float ti = fmaxf(tn, P.znear);
+      if (!(tf > ti) || tf > P.zfar) continue;
+      const DevBrick b = bg;
+      const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded);
+      const float w = 1.0f - frame.w;
+      frame.x = fmaf(col.x, w, frame.x);
+      frame.y = fmaf(col.y, w, frame.y);
+      frame.z = fmaf(col.z, w, frame.z);
+      frame.w = fmaf(col.w, w, frame.w);
+    }
   }
-  const size_t pix = size_t(py) * P.width + px;
-  P.out[pix] = frame;
-  if (P.spp) P.spp[pix] = samples;
-  // frame totals: one atomic per warp (lanes off the image have returned)
-  const uint32_t active = __activemask();
-  const uint32_t s = __reduce_add_sync(active, samples);
-  const uint32_t sh = __reduce_add_sync(active, shaded);
-  if (lane == uint32_t(__ffs(active) - 1)) {
+  if (active) {
+    const size_t pix = size_t(py) * P.width + px;
+    P.out[pix] = frame;
+    if (P.spp) P.spp[pix] = samples;
+  }
+  // frame totals: one atomic per warp
+  const uint32_t s = __reduce_add_sync(0xffffffffu, samples);
+  const uint32_t sh = __reduce_add_sync(0xffffffffu, shaded);
+  if (lane == 0) {
     atomicAdd(&P.counters[0], (unsigned long long)s);
     atomicAdd(&P.counters[1], (unsigned long long)sh);
   }
