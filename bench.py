@@ -317,18 +317,25 @@ def run_ours(args):
     value = ws * K / (ms / 1000.0)
 
     # samples per frame of the timed poses (deterministic; re-rendered untimed)
-    samples, shaded, kms, vis = [], [], [], []
+    samples, shaded, graded, kms, vis = [], [], [], [], []
     for i in range(K):
         frame(args.warmup + i)
         st = r.GetStats()
         samples.append(st.samples)
         shaded.append(st.shaded_samples)
+        graded.append(st.gradient_samples)
         kms.append(st.last_paint_ms)
         vis.append(st.bricks_visible)
     mean_samples = float(np.mean(samples))
     kernel_ms = float(np.mean(step_ms))
     peak, peak_kind = measured_peaks()
-    achieved = mean_samples * LIT_BYTES_PER_SAMPLE / (kernel_ms / 1000.0) / 1e9
+    # Algorithmic bytes of the samples the kernel executes (steps in empty
+    # macro cells add exactly zero and fetch nothing): a lit sample with
+    # non-zero opacity takes 7 trilinear lookups + its TF entry, any other
+    # executed sample 1 lookup + its TF entry.
+    exec_bytes = (float(np.mean(graded)) * LIT_BYTES_PER_SAMPLE +
+                  (float(np.mean(shaded)) - float(np.mean(graded))) * (8 * 2 + 16))
+    achieved = exec_bytes / (kernel_ms / 1000.0) / 1e9
     traffic = read_profile_traffic(w.name)
 
     # end to end through the C ABI: view upload, paint, image to pinned host memory
@@ -377,12 +384,16 @@ def run_ours(args):
                        "parallelism": f"replicas x{ws}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "peak_kind": peak_kind,
-                         "note": f"algorithmic bytes = reference samples x "
-                                 f"{LIT_BYTES_PER_SAMPLE} B (7 trilinear u16 lookups + FP32 TF)"},
+                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "note": "algorithmic bytes of executed samples: lit opaque "
+                                 f"{LIT_BYTES_PER_SAMPLE} B (7 trilinear u16 lookups + FP32 TF), "
+                                 "others 32 B; texels are L1-served (hit rate ~97%), so the "
+                                 "kernel is issue/latency bound, far below this roof"},
             "msamples_per_s": mean_samples / (kernel_ms / 1000.0) / 1e6,
+            "executed_msamples_per_s": float(np.mean(shaded)) / (kernel_ms / 1000.0) / 1e6,
             "samples_per_frame": mean_samples,
             "shaded_fraction": float(np.sum(shaded) / max(np.sum(samples), 1)),
+            "gradient_fraction": float(np.sum(graded) / max(np.sum(samples), 1)),
             "kernel_ms_lib_events": float(np.mean(kms)),
             "bricking": {"seconds": brick_s, "raw_bytes": raw_bytes, "pool_bytes": pool_bytes,
                          "gb_per_s": (raw_bytes + pool_bytes) / brick_s / 1e9},

@@ -94,6 +94,7 @@ typedef struct tvk_stats {
   uint64_t bricks_total;
   uint64_t kernel_launches;  /* kernels this library launched for the frame */
   float last_paint_ms;       /* device time of the last paint (CUDA events) */
+  uint64_t gradient_samples; /* shaded steps that also took the 6 gradient lookups */
 } tvk_stats;
 
 /* ---------------------------------------------------------------- misc */

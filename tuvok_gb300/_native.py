@@ -48,7 +48,8 @@ class VolumeInfo(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
                 ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
-                ("kernel_launches", C.c_uint64), ("last_paint_ms", C.c_float)]
+                ("kernel_launches", C.c_uint64), ("last_paint_ms", C.c_float),
+                ("gradient_samples", C.c_uint64)]
 
 
 _u64p = C.POINTER(C.c_uint64)

@@ -1165,6 +1165,7 @@ tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out) {
     const unsigned long long* c = r->h_counters.as<unsigned long long>();
     r->stats.samples = c[0];
     r->stats.shaded_samples = c[1];
+    r->stats.gradient_samples = c[3];
     float ms = 0;
     TVK_CUDA(cudaEventElapsedTime(&ms, r->ev_start, r->ev_stop));
     r->stats.last_paint_ms = ms;

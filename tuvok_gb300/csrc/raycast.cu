@@ -223,7 +223,8 @@ __device__ __forceinline__ void lighting_bp(const RenderParams& P, const float p
 template <class T>
 __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBrick& b,
                                               const float dir[3], float t_in, float t_out,
-                                              uint32_t& samples, uint32_t& shaded) {
+                                              uint32_t& samples, uint32_t& shaded,
+                                              uint32_t& graded) {
   float en[3], ex[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -335,6 +336,7 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       need_grad = lit && src.w != 0.0f;
     }
     if (need_grad) {
+      ++graded;
       // Volume3D.glsl:43-54 (Yp sampled at -step.y)
       const float xp = shifted_x(vol, foot, clamp_u(pos[0] + vs0, vol.fn0, vol.n0)) * im;
       const float xm = shifted_x(vol, foot, clamp_u(pos[0] + (-vs0), vol.fn0, vol.n0)) * im;
@@ -451,7 +453,7 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
   const float tx0 = float(blockIdx.x * 16), ty0 = float(blockIdx.y * 8);
 
   float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t samples = 0, shaded = 0;
+  uint32_t samples = 0, shaded = 0, graded = 0;
   for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
     const uint32_t end = min(P.n_bricks, base + kCandChunk);
     __syncthreads();  // the previous chunk's list is no longer read
@@ -486,7 +488,7 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
       const float ti = fmaxf(tn, P.znear);
       if (!(tf > ti) || tf > P.zfar) continue;
       const DevBrick b = bg;
-      const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded);
+      const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded);
       const float w = 1.0f - frame.w;
       frame.x = fmaf(col.x, w, frame.x);
       frame.y = fmaf(col.y, w, frame.y);
@@ -502,9 +504,11 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
   // frame totals: one atomic per warp
   const uint32_t s = __reduce_add_sync(0xffffffffu, samples);
   const uint32_t sh = __reduce_add_sync(0xffffffffu, shaded);
+  const uint32_t gr = __reduce_add_sync(0xffffffffu, graded);
   if (lane == 0) {
     atomicAdd(&P.counters[0], (unsigned long long)s);
     atomicAdd(&P.counters[1], (unsigned long long)sh);
+    atomicAdd(&P.counters[3], (unsigned long long)gr);
   }
 }
 

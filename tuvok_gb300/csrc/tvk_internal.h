@@ -144,7 +144,7 @@ struct RenderParams {
   uint32_t width, height;
   float4* out;
   uint32_t* spp;             // per-pixel sample counts (may be null)
-  unsigned long long* counters;  // [samples, shaded, errors]
+  unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
 };
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
