@@ -193,6 +193,12 @@ tvk_status tvk_set_lighting(tvk_renderer* r, int enable);
 tvk_status tvk_set_sample_rate_modifier(tvk_renderer* r, float srm);
 tvk_status tvk_set_isovalue(tvk_renderer* r, float isovalue);
 
+/* AbstrRenderer::SetIsosurfaceColor (AbstrRenderer.h:423); default 0.5 grey.
+ * Isosurface mode (GLRaycaster-ISO-FS + RefineIsosurface + Compose-FS) needs
+ * no transfer function; tvk_renderer_set_volume resets the isovalue to half
+ * the data range (AbstrRenderer.cpp:252-259). */
+tvk_status tvk_set_iso_color(tvk_renderer* r, const float rgb[3]);
+
 /* AbstrRenderer::SetColors (AbstrRenderer.h:621): ambient/diffuse/specular
  * RGBA (colour * w is used) and light direction in eye space. */
 tvk_status tvk_set_colors(tvk_renderer* r, const float ambient[4], const float diffuse[4],

@@ -32,7 +32,7 @@ class Scene(C.Structure):
         ("at", C.c_float * 3), ("up", C.c_float * 3), ("fovy_deg", C.c_float),
         ("znear", C.c_float), ("zfar", C.c_float), ("width", C.c_uint32),
         ("height", C.c_uint32), ("use_double", C.c_int), ("row_stride", C.c_uint32),
-        ("row_phase", C.c_uint32), ("threads", C.c_int),
+        ("row_phase", C.c_uint32), ("threads", C.c_int), ("iso_color", C.c_float * 3),
     ]
 
 
@@ -175,7 +175,8 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
                lighting=False, light_model=0, tf_rgba8=False, clamp=False,
                ambient=(1, 1, 1, 0.1), diffuse=(1, 1, 1, 1), specular=(1, 1, 1, 1),
                light_dir=(0, 0, -1), bp=(0.2, 0.6, 0.2, 32.0), frame_ert=1.0,
-               use_double=False, row_stride=1, row_phase=0, threads=0):
+               use_double=False, row_stride=1, row_phase=0, threads=0, isovalue=None,
+               iso_color=(0.5, 0.5, 0.5)):
     """Scene struct for the oracle; returns (scene, arrays that must stay alive)."""
     raw = np.ascontiguousarray(raw)
     tf = np.ascontiguousarray(np.asarray(tf, dtype=np.float32))
@@ -211,6 +212,11 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
     s.use_double = int(use_double)
     s.row_stride, s.row_phase = row_stride, row_phase
     s.threads = threads
+    if isovalue is None:
+        # AbstrRenderer.cpp:252-259: half the data range once a dataset is loaded
+        isovalue = float(np.float32(float(raw.max()) - float(raw.min())) / np.float32(2.0))
+    s.isovalue = isovalue
+    s.iso_color[:] = iso_color
     return s, (raw, tf)
 
 

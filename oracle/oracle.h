@@ -109,6 +109,7 @@ typedef struct orc_scene {
   /* optional: render only rows with y % row_stride == row_phase (CPU baseline) */
   uint32_t row_stride, row_phase;
   int threads;              /* OpenMP threads, 0 = default */
+  float iso_color[3];       /* AbstrRenderer m_vIsoColor (default 0.5 grey) */
 } orc_scene;
 
 /* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row

@@ -179,6 +179,9 @@ struct Setup {
   std::vector<BrickR> bricks;
   std::vector<int> visible;   // bricks that pass ContainsData
   float trans_scale, grad_scale, step_scale;
+  float iso_norm;             // fIsoval (AbstrRenderer::GetNormalizedIsovalue)
+  float proj_x, proj_y;       // vProjParam (CullingLOD::GetDepthScaleParams)
+  float iso_diffuse[3];       // diffuse colour * m_vIsoColor (GLRenderer.cpp:2807)
   std::vector<float> tf;      // effective RGBA (after RGBA8 truncation if any)
   float light_a[3], light_d[3], light_s[3];
   float domain_scale[3];
@@ -344,6 +347,101 @@ void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_i
   for (int a = 0; a < 4; ++a) col[a] = c[a];
 }
 
+// GLRaycaster-ISO-FS.glsl:51-105 for one brick: first sample >= fIsoval,
+// RefineIsosurface.glsl:37-52 (5 bisection steps from half a step back), the
+// eye-space hit interpolated by |hit - entry| / |exit - entry| in texture
+// space, its non-linear depth and the normal (Volume3D.glsl:56-60).
+template <class T>
+bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in, float t_out,
+               T hit_eye[3], T& fpar, T nrm[3], T& depth, uint64_t& samples) {
+  const orc_scene& s = *st.s;
+  Vol<T> vol{&b, s.dtype, T(s.dtype == 0 ? 1.0f / 255.0f : 1.0f / 65535.0f)};
+  float en[3], ex[3];
+  for (int a = 0; a < 3; ++a) {
+    en[a] = orc_round_half(dir[a] * t_in);
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = std::sqrt((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row<float>(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row<float>(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const T len_tex = len3(T(tout[0] - tin[0]), T(tout[1] - tin[1]), T(tout[2] - tin[2]));
+  const float q = len / b.step;
+  if (!(q < 1.0e6f)) return false;
+  const int n = int(q) + 1;
+  T inc[3], pos[3];
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = T(tout[a] - tin[a]) / T(q);
+    pos[a] = T(tin[a]);
+  }
+  const T iso = T(st.iso_norm);
+  bool hit = false;
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    if (vol.sample(pos[0], pos[1], pos[2]) >= iso) { hit = true; break; }
+    for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+  }
+  if (!hit) return false;
+  T d[3], cur[3];
+  for (int a = 0; a < 3; ++a) {
+    d[a] = inc[a] / T(2);
+    cur[a] = pos[a] - d[a];
+  }
+  for (int k = 0; k < 5; ++k) {
+    for (int a = 0; a < 3; ++a) d[a] = d[a] / T(2);
+    const bool above = vol.sample(cur[0], cur[1], cur[2]) >= iso;
+    for (int a = 0; a < 3; ++a) cur[a] = above ? cur[a] - d[a] : cur[a] + d[a];
+  }
+  fpar = len3(cur[0] - T(tin[0]), cur[1] - T(tin[1]), cur[2] - T(tin[2])) / len_tex;
+  for (int a = 0; a < 3; ++a) hit_eye[a] = T(en[a]) * (T(1) - fpar) + T(ex[a]) * fpar;
+  depth = T(st.proj_x) + (T(st.proj_y) / -hit_eye[2]);
+  // normal at the refined position
+  const T vs[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
+  const T xp = vol.sample(cur[0] + vs[0], cur[1], cur[2]);
+  const T xm = vol.sample(cur[0] + (-vs[0]), cur[1], cur[2]);
+  const T yp = vol.sample(cur[0], cur[1] + (-vs[1]), cur[2]);
+  const T ym = vol.sample(cur[0], cur[1] + vs[1], cur[2]);
+  const T zp = vol.sample(cur[0], cur[1], cur[2] + vs[2]);
+  const T zm = vol.sample(cur[0], cur[1], cur[2] + (-vs[2]));
+  const T g[3] = {(xm - xp) / T(2), (yp - ym) / T(2), (zm - zp) / T(2)};
+  const T gs[3] = {g[0] * T(st.domain_scale[0]), g[1] * T(st.domain_scale[1]),
+                   g[2] * T(st.domain_scale[2])};
+  for (int r = 0; r < 3; ++r)
+    nrm[r] = std::fma(T(float(st.norm_mat[r][2])), gs[2],
+                      std::fma(T(float(st.norm_mat[r][1])), gs[1],
+                               T(float(st.norm_mat[r][0])) * gs[0]));
+  const T l = len3(nrm[0], nrm[1], nrm[2]);
+  if (l > T(0)) { nrm[0] = nrm[0] / l; nrm[1] = nrm[1] / l; nrm[2] = nrm[2] / l; }
+  return true;
+}
+
+// Compose-FS.glsl:40-63 Lighting of the nearest hit (N.z made non-negative;
+// diffuse from |N . -L|, specular exponent 8).
+template <class T>
+void iso_compose(const Setup& st, const T pos[3], const T nin[3], T out[3]) {
+  const T N[3] = {nin[0], nin[1], std::fabs(nin[2])};
+  T p[3] = {T(0) - pos[0], T(0) - pos[1], T(0) - pos[2]};
+  const T lp = len3(p[0], p[1], p[2]);
+  const T V[3] = {p[0] / lp, p[1] / lp, p[2] / lp};
+  const T d = dot3(N, V);
+  T R[3];
+  for (int i = 0; i < 3; ++i) R[i] = V[i] - (T(2) * d) * N[i];
+  const T lr = len3(R[0], R[1], R[2]);
+  for (int i = 0; i < 3; ++i) R[i] = R[i] / lr;
+  const T L[3] = {T(st.s->light_dir[0]), T(st.s->light_dir[1]), T(st.s->light_dir[2])};
+  const T nL[3] = {-L[0], -L[1], -L[2]};
+  const T diff = std::fmax(std::fabs(dot3(N, nL)), T(0));
+  const T spec = pow_int_or_real(std::fmax(dot3(R, L), T(0)), 8.0f);
+  for (int i = 0; i < 3; ++i) {
+    T c = T(st.light_a[i]) + T(st.iso_diffuse[i]) * diff;
+    c = c + T(st.light_s[i]) * spec;
+    out[i] = std::fmin(std::fmax(c, T(0)), T(1));
+  }
+}
+
 template <class T>
 void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_t* spp,
                   uint64_t& samples) {
@@ -383,13 +481,35 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
   });
   T frame[4] = {0, 0, 0, 0};
   const uint64_t before = samples;
-  for (const Hit& h : hits) {
-    if (frame[3] >= T(s.frame_ert)) break;
-    T c[4];
-    brick_march<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
-    // GLRenderer.cpp:151-153 blend (ONE_MINUS_DST_ALPHA, ONE) into RGBA32F
-    const T w = T(1) - frame[3];
-    for (int a = 0; a < 4; ++a) frame[a] = std::fma(c[a], w, frame[a]);
+  if (s.render_mode == ORC_RM_ISO) {
+    // every brick writes its refined hit through a depth test (DF_LESS on a
+    // buffer cleared to 1, GLRenderer.cpp:140-141, GLRaycaster.cpp:423-433)
+    T best_depth = T(1), pos[3] = {0, 0, 0}, nrm[3] = {0, 0, 0}, fpar = 0;
+    bool any = false;
+    for (const Hit& h : hits) {
+      T hp[3], hn[3], f, depth;
+      if (!iso_brick<T>(st, st.bricks[h.b], dir, h.t0, h.t1, hp, f, hn, depth, samples)) continue;
+      if (!(depth < best_depth)) continue;
+      best_depth = depth;
+      for (int a = 0; a < 3; ++a) { pos[a] = hp[a]; nrm[a] = hn[a]; }
+      fpar = f;
+      any = true;
+    }
+    // Compose-FS.glsl:49-76: alpha (the interpolation parameter) 0 means no hit
+    if (any && fpar != T(0)) {
+      T c[3];
+      iso_compose<T>(st, pos, nrm, c);
+      frame[0] = c[0]; frame[1] = c[1]; frame[2] = c[2]; frame[3] = T(1);
+    }
+  } else {
+    for (const Hit& h : hits) {
+      if (frame[3] >= T(s.frame_ert)) break;
+      T c[4];
+      brick_march<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
+      // GLRenderer.cpp:151-153 blend (ONE_MINUS_DST_ALPHA, ONE) into RGBA32F
+      const T w = T(1) - frame[3];
+      for (int a = 0; a < 4; ++a) frame[a] = std::fma(c[a], w, frame[a]);
+    }
   }
   for (int a = 0; a < 4; ++a) out[a] = float(frame[a]);
   if (spp) *spp = uint32_t(samples - before);
@@ -469,7 +589,14 @@ Setup build_setup(const orc_scene& s) {
     st.light_d[a] = s.diffuse[a] * s.diffuse[3];
     st.light_s[a] = s.specular[a] * s.specular[3];
     st.domain_scale[a] = 1.0f / float(s.user_scale[a]);
+    st.iso_diffuse[a] = st.light_d[a] * s.iso_color[a];
   }
+  // AbstrRenderer.cpp:412-424: fIsoval = isovalue / 2^bits (not 2^bits - 1)
+  st.iso_norm = float(double(s.isovalue) / double(1u << (8 * bytes)));
+  // CullingLOD.cpp:69-72
+  st.proj_x = s.zfar / (s.zfar - s.znear);
+  st.proj_y = (s.zfar * s.znear / (s.znear - s.zfar));
+  const bool iso_mode = s.render_mode == ORC_RM_ISO;
   st.bricks.resize(nb);
   std::vector<char> contains_flag(nb, 0);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -503,7 +630,11 @@ Setup build_setup(const orc_scene& s) {
                        b.data.data());
         double mn, mx;
         orc_brick_stats(b.data.data(), s.dtype, uint64_t(b.n[0]) * b.n[1] * b.n[2], &mn, &mx);
-        contains_flag[k] = (hi >= mn && lo <= mx) ? 1 : 0;
+        // ContainsData: value range vs TF limits, or the isovalue (uvfDataset.cpp:1201-1215)
+        if (iso_mode)
+          contains_flag[k] = (double(s.isovalue) <= mx) ? 1 : 0;
+        else
+          contains_flag[k] = (hi >= mn && lo <= mx) ? 1 : 0;
   }
   for (uint64_t k = 0; k < nb; ++k)
     if (contains_flag[k]) st.visible.push_back(int(k));

@@ -118,6 +118,41 @@ def test_gpu_render_matches_oracle(cuda_ok, scenes, case):
         assert img[..., 3].max() > 0.05, "scene should not be empty"
 
 
+@pytest.mark.parametrize("vk,iso,eye", [
+    ("u8", None, (0.3, 0.4, 1.5)),
+    ("u8", 150.0, (-0.9, 0.5, 1.1)),
+    ("u16", None, (0.2, -0.6, 1.4)),
+    ("u16", 2500.0, (1.2, 0.3, -0.9)),
+    ("u8", 120.0, (0.05, 0.02, 0.1)),  # camera inside the volume
+], ids=["u8_default", "u8_150", "u16_default", "u16_2500", "u8_inside"])
+def test_gpu_isosurface_matches_oracle(cuda_ok, scenes, vk, iso, eye):
+    """GLRaycaster-ISO-FS + RefineIsosurface + Compose-FS: the nearest refined
+    hit of all bricks (depth test), lit by the compose pass."""
+    raw = scenes[vk]
+    vol = Volume(raw, brick_size=(18, 18, 18), overlap=1)
+    r = Renderer()
+    r.RegisterDataset(vol)
+    r.SetRendermode(Renderer.RM_ISOSURFACE)
+    if iso is not None:
+        r.SetIsoValue(iso)
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+    r.Resize(96, 80)
+    r.Paint()
+    img = r.ReadBackPixels()
+    cnt = r.ReadSampleCounts()
+    st = r.GetStats()
+    ref, n, rc = O.render(raw, (18, 18, 18), 1, ramp_tf(16), width=96, height=80, eye=eye,
+                          mode=2, isovalue=iso, want_counts=True)
+    compare(img, ref, f"iso {vk} {iso}")
+    # the GPU stops visiting bricks whose entry lies behind the nearest hit
+    # (they cannot pass the depth test); rays without a hit walk them all
+    assert (cnt <= rc).all()
+    miss = ref[..., 3] == 0
+    np.testing.assert_array_equal(cnt[miss], rc[miss])
+    assert st.samples <= n
+    assert (img[..., 3] > 0).mean() > 0.02, "surface should cover part of the frame"
+
+
 def test_gpu_render_rgba8_bytes_interface(cuda_ok, scenes):
     """Set1DTrans(bytes): TransferFunction1D::Set stretches colour channels by
     their min/max (TransferFunction1D.cpp:146-177) and uploads GL_RGBA8."""

@@ -85,6 +85,7 @@ PROTOTYPES = {
     "tvk_set_sample_rate_modifier": [_vp, C.c_float],
     "tvk_set_isovalue": [_vp, C.c_float],
     "tvk_set_colors": [_vp, _f32p, _f32p, _f32p, _f32p],
+    "tvk_set_iso_color": [_vp, _f32p],
     "tvk_set_light_model": [_vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float],
     "tvk_set_view": [_vp, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_float],
     "tvk_set_model_transform": [_vp, _f32p, _f32p],

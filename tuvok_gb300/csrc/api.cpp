@@ -469,6 +469,9 @@ struct tvk_renderer {
   tvk::DevBuf d_empty, d_empty_meta, d_tfpfx;
   std::vector<uint64_t> empty_word_off;
   bool empty_valid = false;
+  bool empty_iso = false;
+  float empty_iso_norm = 0.0f;
+  float iso_color[3] = {0.5f, 0.5f, 0.5f};  // AbstrRenderer.cpp:86 m_vIsoColor
   bool cell_skip = true;
   tvk_stats stats{};
   uint64_t launches = 0;
@@ -514,8 +517,10 @@ void upload_tf(tvk_renderer* R, float step_scale) {
 
 // Empty-cell bits of every LOD-0 brick for the current TF (re-run when the TF,
 // the sample rate or the volume changes).
-void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale) {
-  if (R->empty_valid) return;
+void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale, bool iso_mode,
+                        float iso_norm) {
+  if (R->empty_valid && R->empty_iso == iso_mode && (!iso_mode || R->empty_iso_norm == iso_norm))
+    return;
   R->empty_word_off.resize(V->n_bricks);
   uint64_t words = 0;
   uint32_t max_words = 0;
@@ -539,11 +544,15 @@ void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale)
   p.tf_w = R->tf_w;
   p.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
   p.trans_scale = trans_scale;
+  p.iso_mode = iso_mode ? 1 : 0;
+  p.iso_norm = iso_norm;
   p.bits = R->d_empty.as<uint32_t>();
   launch_empty_cells(p, max_words, R->stream, &R->launches);
   // the word offsets above were copied from pageable memory; keep them alive
   TVK_CUDA(cudaStreamSynchronize(R->stream));
   R->empty_valid = true;
+  R->empty_iso = iso_mode;
+  R->empty_iso_norm = iso_norm;
 }
 
 void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgba8) {
@@ -564,9 +573,9 @@ void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgb
 void paint(tvk_renderer* R) {
   const tvk_volume* V = R->vol;
   if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
-  if (R->tf.empty()) fail(TVK_ERR_STATE, "no transfer function set");
+  const bool iso_mode = R->mode == TVK_RM_ISOSURFACE;
+  if (!iso_mode && R->tf.empty()) fail(TVK_ERR_STATE, "no transfer function set");
   if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
-  if (R->mode == TVK_RM_ISOSURFACE) fail(TVK_ERR_UNSUPPORTED, "isosurface mode is not built yet");
   if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
   if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
   TVK_CUDA(cudaSetDevice(R->device));
@@ -575,11 +584,13 @@ void paint(tvk_renderer* R) {
   // GLRaycaster.cpp:253-257: fStepScale at LOD 0
   const float srm = R->srm;
   const float step_scale = 1.0f / srm * 1.0f;
-  upload_tf(R, step_scale);
+  if (!R->tf.empty()) upload_tf(R, step_scale);
   // GLRenderer.cpp:1813-1819 CalculateScaling
   const uint32_t imax = (1u << (8 * V->bytes)) - 1;
   const float trans_scale = float(double(imax) / V->range_max);
-  if (R->cell_skip) update_empty_cells(R, V, trans_scale);
+  // AbstrRenderer.cpp:412-424 GetNormalizedIsovalue: isovalue / 2^bits
+  const float iso_norm = float(double(R->isovalue) / double(1u << (8 * V->bytes)));
+  if (R->cell_skip) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
 
   const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
 
@@ -634,7 +645,9 @@ void paint(tvk_renderer* R) {
   std::vector<std::pair<uint64_t, uint64_t>> order;  // (L1 distance, brick)
   order.reserve(V->n_bricks);
   for (uint64_t k = 0; k < V->n_bricks; ++k) {
-    if (!(hi >= V->bmin[k] && lo <= V->bmax[k])) continue;
+    // ContainsData (uvfDataset.cpp:1201-1215): TF value limits, or the isovalue
+    if (iso_mode ? !(double(R->isovalue) <= V->bmax[k]) : !(hi >= V->bmin[k] && lo <= V->bmax[k]))
+      continue;
     const int64_t c[3] = {int64_t(k % l0.bricks[0]), int64_t((k / l0.bricks[0]) % l0.bricks[1]),
                           int64_t(k / (l0.bricks[0] * l0.bricks[1]))};
     uint64_t d = 0;
@@ -721,6 +734,12 @@ void paint(tvk_renderer* R) {
   P.znear = R->znear;
   P.zfar = R->zfar;
   P.frame_ert = R->frame_ert;
+  P.iso_norm = iso_norm;
+  // CullingLOD.cpp:69-72 GetDepthScaleParams
+  P.proj_x = R->zfar / (R->zfar - R->znear);
+  P.proj_y = (R->zfar * R->znear / (R->znear - R->zfar));
+  for (int a = 0; a < 3; ++a)  // GLRenderer.cpp:2807-2808
+    P.iso_diffuse[a] = (R->diffuse[a] * R->diffuse[3]) * R->iso_color[a];
   P.max_q = 1.0e6f;
   P.width = R->width;
   P.height = R->height;
@@ -940,6 +959,8 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
     REQUIRE(r, "null renderer");
     r->vol = v;
     r->empty_valid = false;
+    // AbstrRenderer.cpp:252-259: the isovalue starts at half the data range
+    if (v) r->isovalue = float(v->range_max - v->range_min) / 2.0f;
   });
 }
 
@@ -1014,6 +1035,13 @@ tvk_status tvk_set_isovalue(tvk_renderer* r, float isovalue) {
   return guarded([&] {
     REQUIRE(r, "null renderer");
     r->isovalue = isovalue;
+  });
+}
+
+tvk_status tvk_set_iso_color(tvk_renderer* r, const float rgb[3]) {
+  return guarded([&] {
+    REQUIRE(r && rgb, "null argument");
+    for (int a = 0; a < 3; ++a) r->iso_color[a] = rgb[a];
   });
 }
 

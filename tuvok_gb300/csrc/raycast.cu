@@ -395,6 +395,158 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   return c;
 }
 
+// GLRaycaster-ISO-FS.glsl:51-105 for one brick: first step whose sample is
+// >= fIsoval, RefineIsosurface.glsl:37-52, the eye-space hit interpolated by
+// |hit - entry| / |exit - entry| in texture space, its non-linear depth and the
+// normal at the refined position.  Returns false when the ray misses.
+struct IsoHit {
+  float pos[3];  // eye space
+  float f;       // interpolation parameter (alpha of the hit buffer)
+  float n[3];
+  float depth;
+};
+
+template <class T>
+__device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick& b,
+                                          const float dir[3], float t_in, float t_out,
+                                          IsoHit& h, uint32_t& samples, uint32_t& shaded) {
+  float en[3], ex[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    en[a] = __half2float(__float2half_rn(dir[a] * t_in));
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float len_tex = len3(tout[0] - tin[0], tout[1] - tin[1], tout[2] - tin[2]);
+  const float q = len / b.step;
+  if (!(q < P.max_q)) return false;
+  const int n = int(q) + 1;
+  float pos[3], inc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = (tout[a] - tin[a]) / q;
+    pos[a] = tin[a];
+  }
+  BrickView<T> vol;
+  vol.p = static_cast<const T*>(P.pool) + b.off;
+  vol.n0 = int(b.n[0]); vol.n1 = int(b.n[1]); vol.n2 = int(b.n[2]);
+  vol.fn0 = float(b.n[0]); vol.fn1 = float(b.n[1]); vol.fn2 = float(b.n[2]);
+  vol.sx = b.n[0]; vol.sxy = b.n[0] * b.n[1];
+  const float im = P.inv_max_raw;
+  const float iso = P.iso_norm;
+  // cells whose maximum stays below the isovalue cannot produce a hit
+  const uint32_t* __restrict__ empty = P.empty_bits ? P.empty_bits + b.empty_off : nullptr;
+  const int ncx = int(b.cells & 1023u), ncy = int((b.cells >> 10) & 1023u);
+  const float du0 = inc[0] * vol.fn0, du1 = inc[1] * vol.fn1, du2 = inc[2] * vol.fn2;
+  const float idu0 = 1.0f / fabsf(du0), idu1 = 1.0f / fabsf(du1), idu2 = 1.0f / fabsf(du2);
+  bool hit = false;
+  int i = 0;
+  while (i < n) {
+    const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
+    const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
+    const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
+    const float u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
+    const float u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
+    const float u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+    if (empty) {
+      const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
+                cz = int(u2) >> kCellShift;
+      const uint32_t cell = uint32_t((cz * ncy + cy) * ncx + cx);
+      if ((__ldg(&empty[cell >> 5]) >> (cell & 31)) & 1u) {
+        int k = 0;
+        if (uu0 == u0 && uu1 == u1 && uu2 == u2) {
+          const float lo0 = float(cx << kCellShift), lo1 = float(cy << kCellShift),
+                      lo2 = float(cz << kCellShift);
+          const float d0 = du0 > 0.0f ? lo0 + float(kCell) - uu0 : uu0 - lo0;
+          const float d1 = du1 > 0.0f ? lo1 + float(kCell) - uu1 : uu1 - lo1;
+          const float d2 = du2 > 0.0f ? lo2 + float(kCell) - uu2 : uu2 - lo2;
+          const float m = fminf(fminf((d0 - 0.015625f) * idu0, (d1 - 0.015625f) * idu1),
+                                (d2 - 0.015625f) * idu2);
+          k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
+        }
+        samples += uint32_t(k + 1);
+        for (int j = 0; j <= k; ++j) {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+        }
+        i += k + 1;
+        continue;
+      }
+    }
+    ++samples;
+    ++shaded;
+    if (vol.sample_u(u0, u1, u2) * im >= iso) { hit = true; break; }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+    ++i;
+  }
+  if (!hit) return false;
+  float d[3], cur[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    d[a] = inc[a] / 2.0f;
+    cur[a] = pos[a] - d[a];
+  }
+  for (int k = 0; k < 5; ++k) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d[a] = d[a] / 2.0f;
+    const bool above = vol.sample_raw(cur[0], cur[1], cur[2]) * im >= iso;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cur[a] = above ? cur[a] - d[a] : cur[a] + d[a];
+  }
+  h.f = len3(cur[0] - tin[0], cur[1] - tin[1], cur[2] - tin[2]) / len_tex;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) h.pos[a] = en[a] * (1.0f - h.f) + ex[a] * h.f;
+  h.depth = P.proj_x + (P.proj_y / -h.pos[2]);
+  const float vs0 = 1.0f / float(b.n[0]), vs1 = 1.0f / float(b.n[1]), vs2 = 1.0f / float(b.n[2]);
+  const float xp = vol.sample_raw(cur[0] + vs0, cur[1], cur[2]) * im;
+  const float xm = vol.sample_raw(cur[0] + (-vs0), cur[1], cur[2]) * im;
+  const float yp = vol.sample_raw(cur[0], cur[1] + (-vs1), cur[2]) * im;
+  const float ym = vol.sample_raw(cur[0], cur[1] + vs1, cur[2]) * im;
+  const float zp = vol.sample_raw(cur[0], cur[1], cur[2] + vs2) * im;
+  const float zm = vol.sample_raw(cur[0], cur[1], cur[2] + (-vs2)) * im;
+  const float gs0 = ((xm - xp) / 2.0f) * P.domain_scale[0];
+  const float gs1 = ((yp - ym) / 2.0f) * P.domain_scale[1];
+  const float gs2 = ((zm - zp) / 2.0f) * P.domain_scale[2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    h.n[r] = fmaf(P.norm_mat[r][2], gs2, fmaf(P.norm_mat[r][1], gs1, P.norm_mat[r][0] * gs0));
+  const float l = len3(h.n[0], h.n[1], h.n[2]);
+  if (l > 0.0f) { h.n[0] = h.n[0] / l; h.n[1] = h.n[1] / l; h.n[2] = h.n[2] / l; }
+  return true;
+}
+
+// Compose-FS.glsl:40-63: lighting of the nearest hit.
+__device__ __forceinline__ float4 iso_compose(const RenderParams& P, const IsoHit& h) {
+  const float N0 = h.n[0], N1 = h.n[1], N2 = fabsf(h.n[2]);
+  const float p0 = 0.0f - h.pos[0], p1 = 0.0f - h.pos[1], p2 = 0.0f - h.pos[2];
+  const float lp = len3(p0, p1, p2);
+  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  const float d = (N0 * V0 + N1 * V1) + N2 * V2;
+  float R0 = V0 - (2.0f * d) * N0, R1 = V1 - (2.0f * d) * N1, R2 = V2 - (2.0f * d) * N2;
+  const float lr = len3(R0, R1, R2);
+  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+  const float* L = P.light_dir;
+  const float nl0 = -L[0], nl1 = -L[1], nl2 = -L[2];
+  const float diff = fmaxf(fabsf((N0 * nl0 + N1 * nl1) + N2 * nl2), 0.0f);
+  const float spec = pow_int_or_real(fmaxf((R0 * L[0] + R1 * L[1]) + R2 * L[2], 0.0f), 8.0f);
+  float c[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float x = P.light_a[i] + P.iso_diffuse[i] * diff;
+    x = x + P.light_s[i] * spec;
+    c[i] = fminf(fmaxf(x, 0.0f), 1.0f);
+  }
+  return make_float4(c[0], c[1], c[2], 1.0f);
+}
+
 constexpr uint32_t kCandChunk = 1024;
 
 // Conservative: can any pixel ray of the 16x8 tile at (tx0, ty0) meet brick b?
@@ -424,7 +576,9 @@ __device__ __forceinline__ bool footprint_touches_tile(const RenderParams& P, co
   return xmax >= tx0 - 2.0f && xmin <= tx0 + 17.0f && ymax >= ty0 - 2.0f && ymin <= ty0 + 9.0f;
 }
 
-template <class T>
+// kIso: isosurface mode (nearest refined hit + compose); otherwise the
+// compositing modes (1D/2D TF, lit or unlit)
+template <class T, bool kIso>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -454,6 +608,10 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
 
   float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t samples = 0, shaded = 0, graded = 0;
+  constexpr bool iso_mode = kIso;
+  IsoHit best;
+  float best_depth = 1.0f;  // depth buffer cleared to 1, test DF_LESS
+  bool have_hit = false;
   for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
     const uint32_t end = min(P.n_bricks, base + kCandChunk);
     __syncthreads();  // the previous chunk's list is no longer read
@@ -488,6 +646,19 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
       const float ti = fmaxf(tn, P.znear);
       if (!(tf > ti) || tf > P.zfar) continue;
       const DevBrick b = bg;
+      if (iso_mode) {
+        // A later brick's hit lies beyond its (RGBA16F-rounded) entry, so
+        // once that entry is behind the nearest hit it cannot pass the
+        // depth test; bricks come in increasing entry order along the ray.
+        if (have_hit && ti * (1.0f - 2e-3f) - 1e-4f > -best.pos[2]) break;
+        IsoHit h;
+        if (iso_brick<T>(P, b, dir, ti, tf, h, samples, shaded) && h.depth < best_depth) {
+          best = h;
+          best_depth = h.depth;
+          have_hit = true;
+        }
+        continue;
+      }
       const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded);
       const float w = 1.0f - frame.w;
       frame.x = fmaf(col.x, w, frame.x);
@@ -496,6 +667,9 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
       frame.w = fmaf(col.w, w, frame.w);
     }
   }
+  // Compose-FS.glsl:58-61: no hit, or an interpolation parameter of exactly 0,
+  // leaves the pixel empty
+  if (iso_mode && have_hit && best.f != 0.0f) frame = iso_compose(P, best);
   if (active) {
     const size_t pix = size_t(py) * P.width + px;
     P.out[pix] = frame;
@@ -532,6 +706,11 @@ __global__ void empty_cells_kernel(const EmptyCellParams P) {
   uint32_t bits = 0;
   for (uint32_t j = 0; j < 32 && w * 32 + j < ncell; ++j) {
     const uint32_t mm = cm[w * 32 + j];
+    if (P.iso_mode) {
+      // samples never exceed the cell maximum, so below fIsoval means no hit
+      if (float(mm >> 16) * P.inv_max_raw < P.iso_norm) bits |= 1u << j;
+      continue;
+    }
     // trilinear results lie in [min, max] and the index is monotone in the
     // value, so the cell reaches exactly the entries lo..hi
     const int lo = tf_index(mm & 0xffffu, P.inv_max_raw, P.trans_scale, W);
@@ -554,10 +733,14 @@ void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 block(128);
   const dim3 grid((p.width + 15) / 16, (p.height + 7) / 8);
-  if (p.bytes == 1)
-    raycast_kernel<uint8_t><<<grid, block, 0, s>>>(p);
-  else
-    raycast_kernel<uint16_t><<<grid, block, 0, s>>>(p);
+  const bool iso = p.mode == TVK_RM_ISOSURFACE;
+  if (p.bytes == 1) {
+    if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);
+    else raycast_kernel<uint8_t, false><<<grid, block, 0, s>>>(p);
+  } else {
+    if (iso) raycast_kernel<uint16_t, true><<<grid, block, 0, s>>>(p);
+    else raycast_kernel<uint16_t, false><<<grid, block, 0, s>>>(p);
+  }
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }

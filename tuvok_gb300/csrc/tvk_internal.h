@@ -112,6 +112,8 @@ struct EmptyCellParams {
   const uint32_t* nz_prefix;           // prefix count of non-zero TF entries / columns
   uint32_t tf_w;
   float inv_max_raw, trans_scale;
+  int iso_mode;                        // 1: empty = cell maximum below iso_norm
+  float iso_norm;
   uint32_t* bits;
 };
 void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, cudaStream_t s,
@@ -140,6 +142,9 @@ struct RenderParams {
   float kx, ky, inv_w2, inv_h2;
   float znear, zfar;
   float frame_ert;
+  float iso_norm;            // fIsoval
+  float proj_x, proj_y;      // vProjParam
+  float iso_diffuse[3];      // diffuse colour * iso colour
   float max_q;               // guard on len/step
   uint32_t width, height;
   float4* out;

@@ -208,6 +208,9 @@ class Renderer:
     def SetIsoValue(self, v):
         check(lib().tvk_set_isovalue(self._h, float(v)))
 
+    def SetIsosurfaceColor(self, rgb):
+        check(lib().tvk_set_iso_color(self._h, _f32(rgb)))
+
     def SetColors(self, ambient, diffuse, specular, light_dir):
         check(lib().tvk_set_colors(self._h, _f32(ambient), _f32(diffuse), _f32(specular),
                                    _f32(light_dir)))
