@@ -80,6 +80,9 @@ def lib():
         L.orc_render_prepared.restype = C.c_uint64
         L.orc_release.argtypes = [C.c_void_p]
         L.orc_release.restype = None
+        L.orc_build_octree.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
+                                       C.c_int, C.c_void_p, C.c_uint64, _u64p, C.c_uint64]
+        L.orc_build_octree.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -164,6 +167,31 @@ def max_gradient(raw, bsize, overlap, clamp=False):
     dims = (raw.shape[2], raw.shape[1], raw.shape[0])
     return lib().orc_max_gradient(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
                                   _u32(bsize), overlap, int(clamp))
+
+
+def build_octree(raw, bsize, overlap, clamp=False, median=False):
+    """Every brick of every LOD in TOC order: list of [z, y, x] arrays."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    sizes, counts = lod_table(dims, bsize, overlap)
+    shapes = []
+    for l, (ls, lc) in enumerate(zip(sizes, counts)):
+        for z in range(lc[2]):
+            for y in range(lc[1]):
+                for x in range(lc[0]):
+                    shapes.append(brick_size(ls, lc, bsize, overlap, (x, y, z)))
+    total = sum(s[0] * s[1] * s[2] for s in shapes)
+    pool = np.zeros(total, dtype=raw.dtype)
+    offs = np.zeros(len(shapes), dtype=np.uint64)
+    n = lib().orc_build_octree(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
+                               _u32(bsize), overlap, int(clamp), int(median),
+                               pool.ctypes.data_as(C.c_void_p), total,
+                               offs.ctypes.data_as(_u64p), len(shapes))
+    assert n == len(shapes), n
+    out = []
+    for s, o in zip(shapes, offs):
+        out.append(pool[int(o):int(o) + s[0] * s[1] * s[2]].reshape(s[2], s[1], s[0]))
+    return out
 
 
 def round_half(x):

@@ -7,6 +7,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -293,4 +294,309 @@ extern "C" double orc_max_gradient(const void* raw, int dtype, const uint64_t di
   if (dtype == 0)
     return max_gradient<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0);
   return max_gradient<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0);
+}
+
+// ---------------------------------------------------------------- LOD hierarchy
+
+namespace {
+
+template <class T>
+void order2(T& a, T& b) { if (a > b) std::swap(a, b); }
+
+// VolumeTools.h:196-210: median of a, b, c (d ignored) or the mean of four
+template <class T>
+T filter4(T a, T b, T c, T d, bool median) {
+  if (median) {
+    order2(a, b);
+    order2(b, c);
+    return std::max(a, b);
+  }
+  return T((double(a) + double(b) + double(c) + double(d)) / double(4));
+}
+
+template <class T>
+T filter2(T a, T b, bool median) {
+  if (median) return a;
+  return T((double(a) + double(b)) / double(2));
+}
+
+template <class T>
+void insert4(T& a, T& b, T& c, T& d, T& p) {
+  // VolumeTools.h:212-227 InsertIntoQuadruple
+  if (p > c) {
+    order2(d, p);
+  } else {
+    if (p < b) {
+      d = c;
+      c = b;
+      b = p;
+      order2(a, b);
+    } else {
+      d = c;
+      c = p;
+    }
+  }
+}
+
+template <class T>
+T filter8(T a, T b, T c, T d, T e, T f, T g, T h, bool median) {
+  // VolumeTools.h:242-262: 7-value median network, or the mean of eight
+  if (median) {
+    order2(a, b);
+    order2(c, d);
+    order2(a, c);
+    order2(b, d);
+    order2(b, c);
+    insert4(a, b, c, d, e);
+    insert4(a, b, c, d, f);
+    return std::max(std::min(d, g), c);
+  }
+  return T((double(a) + double(b) + double(c) + double(d) + double(e) + double(f) + double(g) +
+            double(h)) / double(8));
+}
+
+struct Tree {
+  uint64_t dims[3];
+  uint32_t B[3];
+  uint32_t ov;
+  std::vector<std::array<uint64_t, 3>> lod_size, lod_cnt;
+  std::vector<uint64_t> lod_first;  // TOC index of each LOD's first brick
+  std::vector<uint64_t> off;        // voxel offset per TOC index
+  std::array<uint64_t, 3> size(uint64_t l, uint64_t x, uint64_t y, uint64_t z) const {
+    uint64_t ls[3] = {lod_size[l][0], lod_size[l][1], lod_size[l][2]};
+    uint64_t lc[3] = {lod_cnt[l][0], lod_cnt[l][1], lod_cnt[l][2]};
+    uint64_t c[3] = {x, y, z}, o[3];
+    orc_brick_size(ls, lc, B, ov, c, o);
+    return {o[0], o[1], o[2]};
+  }
+  uint64_t index(uint64_t l, uint64_t x, uint64_t y, uint64_t z) const {
+    return lod_first[l] + x + y * lod_cnt[l][0] + z * lod_cnt[l][0] * lod_cnt[l][1];
+  }
+};
+
+// DownsampleBricktoBrick (.inc:1-248): one child brick into the target.
+template <class T>
+void downsample_child(const Tree& t, T* target, const std::array<uint64_t, 3>& ts,
+                      const T* src, const std::array<uint64_t, 3>& ss, const uint64_t toff[3],
+                      bool median) {
+  const uint64_t ov = t.ov;
+  const uint64_t ex = (ss[0] - 2 * ov) / 2, ey = (ss[1] - 2 * ov) / 2, ez = (ss[2] - 2 * ov) / 2;
+  const bool odx = ss[0] % 2, ody = ss[1] % 2, odz = ss[2] % 2;
+  auto S = [&](uint64_t x, uint64_t y, uint64_t z) -> T {
+    return src[x + y * ss[0] + z * ss[0] * ss[1]];
+  };
+  auto D = [&](uint64_t x, uint64_t y, uint64_t z) -> T& {
+    return target[(x + ov + toff[0]) + (y + ov + toff[1]) * ts[0] +
+                  (z + ov + toff[2]) * ts[0] * ts[1]];
+  };
+  for (uint64_t z = 0; z < ez; ++z)
+    for (uint64_t y = 0; y < ey; ++y)
+      for (uint64_t x = 0; x < ex; ++x) {
+        const uint64_t X = 2 * x + ov, Y = 2 * y + ov, Z = 2 * z + ov;
+        D(x, y, z) = filter8<T>(S(X, Y, Z), S(X, Y, Z + 1), S(X, Y + 1, Z), S(X, Y + 1, Z + 1),
+                                S(X + 1, Y, Z), S(X + 1, Y, Z + 1), S(X + 1, Y + 1, Z),
+                                S(X + 1, Y + 1, Z + 1), median);
+      }
+  if (odx)
+    for (uint64_t z = 0; z < ez; ++z)
+      for (uint64_t y = 0; y < ey; ++y) {
+        const uint64_t X = 2 * ex + ov, Y = 2 * y + ov, Z = 2 * z + ov;
+        D(ex, y, z) = filter4<T>(S(X, Y, Z), S(X, Y, Z + 1), S(X, Y + 1, Z), S(X, Y + 1, Z + 1),
+                                 median);
+      }
+  if (ody)
+    for (uint64_t z = 0; z < ez; ++z)
+      for (uint64_t x = 0; x < ex; ++x) {
+        const uint64_t X = 2 * x + ov, Y = 2 * ey + ov, Z = 2 * z + ov;
+        D(x, ey, z) = filter4<T>(S(X, Y, Z), S(X, Y, Z + 1), S(X + 1, Y, Z), S(X + 1, Y, Z + 1),
+                                 median);
+      }
+  if (odz)
+    for (uint64_t y = 0; y < ey; ++y)
+      for (uint64_t x = 0; x < ex; ++x) {
+        const uint64_t X = 2 * x + ov, Y = 2 * y + ov, Z = 2 * ez + ov;
+        D(x, y, ez) = filter4<T>(S(X, Y, Z), S(X, Y + 1, Z), S(X + 1, Y, Z), S(X + 1, Y + 1, Z),
+                                 median);
+      }
+  if (odx && ody)
+    for (uint64_t z = 0; z < ez; ++z) {
+      const uint64_t X = 2 * ex + ov, Y = 2 * ey + ov, Z = 2 * z + ov;
+      D(ex, ey, z) = filter2<T>(S(X, Y, Z), S(X, Y, Z + 1), median);
+    }
+  if (ody && odz)
+    for (uint64_t x = 0; x < ex; ++x) {
+      const uint64_t X = 2 * x + ov, Y = 2 * ey + ov, Z = 2 * ez + ov;
+      D(x, ey, ez) = filter2<T>(S(X, Y, Z), S(X + 1, Y, Z), median);
+    }
+  if (odx && odz)
+    for (uint64_t y = 0; y < ey; ++y) {
+      const uint64_t X = 2 * ex + ov, Y = 2 * y + ov, Z = 2 * ez + ov;
+      D(ex, y, ez) = filter2<T>(S(X, Y, Z), S(X, Y + 1, Z), median);
+    }
+  if (odx && ody && odz) D(ex, ey, ez) = S(2 * ex + ov, 2 * ey + ov, 2 * ez + ov);
+}
+
+// CopyBrickToBrick (.cpp:1153-1202)
+template <class T>
+void copy_region(const T* src, const std::array<uint64_t, 3>& ss, T* dst,
+                 const std::array<uint64_t, 3>& ds, const uint64_t so[3], const uint64_t dof[3],
+                 const uint64_t r[3]) {
+  for (uint64_t z = 0; z < r[2]; ++z)
+    for (uint64_t y = 0; y < r[1]; ++y)
+      for (uint64_t x = 0; x < r[0]; ++x)
+        dst[(dof[0] + x) + (dof[1] + y) * ds[0] + (dof[2] + z) * ds[0] * ds[1]] =
+            src[(so[0] + x) + (so[1] + y) * ss[0] + (so[2] + z) * ss[0] * ss[1]];
+}
+
+template <class T>
+void clamp_brick(T* d, const std::array<uint64_t, 3>& bs, uint64_t ov, const bool s[3],
+                 const bool e[3]) {
+  // ClampToEdge (.cpp:376-462), same order as for LOD 0
+  auto at = [&](uint64_t x, uint64_t y, uint64_t z) -> T& {
+    return d[x + y * bs[0] + z * bs[0] * bs[1]];
+  };
+  if (s[0])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t y = 0; y < bs[1]; ++y)
+        for (uint64_t o = 0; o < ov; ++o) at(ov - 1 - o, y, z) = at(ov, y, z);
+  if (e[0])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t y = 0; y < bs[1]; ++y)
+        for (uint64_t o = 0; o < ov; ++o) at(bs[0] - ov + o, y, z) = at(bs[0] - 1 - ov, y, z);
+  if (s[1])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, ov - 1 - o, z) = at(x, ov, z);
+  if (e[1])
+    for (uint64_t z = 0; z < bs[2]; ++z)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, bs[1] - ov + o, z) = at(x, bs[1] - 1 - ov, z);
+  if (s[2])
+    for (uint64_t y = 0; y < bs[1]; ++y)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, y, ov - 1 - o) = at(x, y, ov);
+  if (e[2])
+    for (uint64_t y = 0; y < bs[1]; ++y)
+      for (uint64_t o = 0; o < ov; ++o)
+        for (uint64_t x = 0; x < bs[0]; ++x) at(x, y, bs[2] - ov + o) = at(x, y, bs[2] - 1 - ov);
+}
+
+// FillOverlap (.cpp:1203-1372) for one LOD, bricks in z, y, x order
+template <class T>
+void fill_overlap(const Tree& t, T* pool, uint64_t l, bool clamp) {
+  const uint64_t ov = t.ov;
+  const auto& cnt = t.lod_cnt[l];
+  for (uint64_t z = 0; z < cnt[2]; ++z)
+    for (uint64_t y = 0; y < cnt[1]; ++y)
+      for (uint64_t x = 0; x < cnt[0]; ++x) {
+        const bool lf = x > 0, rt = x < cnt[0] - 1, tp = y > 0, bt = y < cnt[1] - 1;
+        const bool fr = z > 0, bk = z < cnt[2] - 1;
+        const auto ts = t.size(l, x, y, z);
+        T* dst = pool + t.off[t.index(l, x, y, z)];
+        auto copy = [&](int64_t dx, int64_t dy, int64_t dz, uint64_t sx0, uint64_t sy0,
+                        uint64_t sz0, uint64_t dx0, uint64_t dy0, uint64_t dz0, uint64_t rx,
+                        uint64_t ry, uint64_t rz) {
+          const uint64_t nx = x + dx, ny = y + dy, nz = z + dz;
+          const auto ss = t.size(l, nx, ny, nz);
+          const T* src = pool + t.off[t.index(l, nx, ny, nz)];
+          const uint64_t so[3] = {sx0, sy0, sz0}, dof[3] = {dx0, dy0, dz0};
+          const uint64_t r[3] = {rx == ~0ull ? ss[0] : rx, ry == ~0ull ? ss[1] : ry,
+                                 rz == ~0ull ? ss[2] : rz};
+          copy_region<T>(src, ss, dst, ts, so, dof, r);
+        };
+        const uint64_t A = ~0ull;
+        if (rt) copy(1, 0, 0, ov, 0, 0, ts[0] - ov, 0, 0, ov, A, A);
+        if (bt) copy(0, 1, 0, 0, ov, 0, 0, ts[1] - ov, 0, A, ov, A);
+        if (bk) copy(0, 0, 1, 0, 0, ov, 0, 0, ts[2] - ov, A, A, ov);
+        if (lf) copy(-1, 0, 0, t.size(l, x - 1, y, z)[0] - 2 * ov, 0, 0, 0, 0, 0, ov, A, A);
+        if (tp) copy(0, -1, 0, 0, t.size(l, x, y - 1, z)[1] - 2 * ov, 0, 0, 0, 0, A, ov, A);
+        if (fr) copy(0, 0, -1, 0, 0, t.size(l, x, y, z - 1)[2] - 2 * ov, 0, 0, 0, A, A, ov);
+        if (bt && rt) copy(1, 1, 0, ov, ov, 0, ts[0] - ov, ts[1] - ov, 0, ov, ov, A);
+        if (rt && bk) copy(1, 0, 1, ov, 0, ov, ts[0] - ov, 0, ts[2] - ov, ov, A, ov);
+        if (bt && bk) copy(0, 1, 1, 0, ov, ov, 0, ts[1] - ov, ts[2] - ov, A, ov, ov);
+        if (rt && bt && bk) copy(1, 1, 1, ov, ov, ov, ts[0] - ov, ts[1] - ov, ts[2] - ov, ov, ov, ov);
+        if (clamp) {
+          const bool s[3] = {!lf, !tp, !fr}, e[3] = {!rt, !bt, !bk};
+          clamp_brick<T>(dst, ts, ov, s, e);
+        }
+      }
+}
+
+template <class T>
+int64_t build_octree(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                     bool clamp, bool median, T* pool, uint64_t pool_voxels, uint64_t* offsets,
+                     uint64_t max_bricks) {
+  Tree t;
+  for (int a = 0; a < 3; ++a) {
+    t.dims[a] = dims[a];
+    t.B[a] = B[a];
+  }
+  t.ov = ov;
+  uint64_t ls[3 * 64], lc[3 * 64];
+  const int nl = orc_lod_table(dims, B, ov, ls, lc, 64);
+  uint64_t n = 0, vox = 0;
+  for (int l = 0; l < nl; ++l) {
+    t.lod_size.push_back({ls[3 * l], ls[3 * l + 1], ls[3 * l + 2]});
+    t.lod_cnt.push_back({lc[3 * l], lc[3 * l + 1], lc[3 * l + 2]});
+    t.lod_first.push_back(n);
+    for (uint64_t z = 0; z < lc[3 * l + 2]; ++z)
+      for (uint64_t y = 0; y < lc[3 * l + 1]; ++y)
+        for (uint64_t x = 0; x < lc[3 * l]; ++x) {
+          const auto s = t.size(l, x, y, z);
+          t.off.push_back(vox);
+          vox += s[0] * s[1] * s[2];
+          ++n;
+        }
+  }
+  if (n > max_bricks || vox > pool_voxels) return -1;
+  std::fill(pool, pool + vox, T(0));
+  for (uint64_t i = 0; i < n; ++i) offsets[i] = t.off[i];
+  // LOD 0 (PermuteInputData)
+  for (uint64_t z = 0; z < lc[2]; ++z)
+    for (uint64_t y = 0; y < lc[1]; ++y)
+      for (uint64_t x = 0; x < lc[0]; ++x) {
+        const uint64_t c[3] = {x, y, z};
+        lod0_brick<T>(raw, dims, B, ov, clamp, c, pool + t.off[t.index(0, x, y, z)]);
+      }
+  // ComputeHierarchy (.inc:358-398)
+  const uint64_t split[3] = {uint64_t(std::ceil((B[0] - 2.0 * ov) / 2.0)),
+                             uint64_t(std::ceil((B[1] - 2.0 * ov) / 2.0)),
+                             uint64_t(std::ceil((B[2] - 2.0 * ov) / 2.0))};
+  for (int l = 1; l < nl; ++l) {
+    const auto& cnt = t.lod_cnt[l];
+    const auto& lower = t.lod_cnt[l - 1];
+    for (uint64_t z = 0; z < cnt[2]; ++z)
+      for (uint64_t y = 0; y < cnt[1]; ++y)
+        for (uint64_t x = 0; x < cnt[0]; ++x) {
+          const auto ts = t.size(l, x, y, z);
+          T* dst = pool + t.off[t.index(l, x, y, z)];
+          const bool hr = x * 2 + 1 < lower[0], hb = y * 2 + 1 < lower[1], hk = z * 2 + 1 < lower[2];
+          for (int k = 0; k < 8; ++k) {
+            const uint64_t cx = k & 1, cy = (k >> 1) & 1, cz = (k >> 2) & 1;
+            if ((cx && !hr) || (cy && !hb) || (cz && !hk)) continue;
+            const uint64_t toff[3] = {cx ? split[0] : 0, cy ? split[1] : 0, cz ? split[2] : 0};
+            const uint64_t sx = 2 * x + cx, sy = 2 * y + cy, sz = 2 * z + cz;
+            downsample_child<T>(t, dst, ts, pool + t.off[t.index(l - 1, sx, sy, sz)],
+                                t.size(l - 1, sx, sy, sz), toff, median);
+          }
+        }
+    fill_overlap<T>(t, pool, l, clamp);
+  }
+  return int64_t(n);
+}
+
+}  // namespace
+
+extern "C" int64_t orc_build_octree(const void* raw, int dtype, const uint64_t dims[3],
+                                    const uint32_t brick_size[3], uint32_t overlap,
+                                    int clamp_to_edge, int median, void* pool,
+                                    uint64_t pool_voxels, uint64_t* brick_offsets,
+                                    uint64_t max_bricks) {
+  if (dtype == 0)
+    return build_octree<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                                 median != 0, static_cast<uint8_t*>(pool), pool_voxels,
+                                 brick_offsets, max_bricks);
+  return build_octree<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                                median != 0, static_cast<uint16_t*>(pool), pool_voxels,
+                                brick_offsets, max_bricks);
 }

@@ -68,6 +68,20 @@ void orc_brick_metadata(const uint64_t lod_size[3], const uint64_t brick_count[3
                         const double aspect[3], float* centers, float* extents,
                         uint32_t* n_voxels);
 
+/* ExtendedOctreeConverter::Convert's whole octree (ExtendedOctreeConverter.cpp:
+ * 128-280): LOD 0 by orc_lod0_brick, every coarser LOD by DownsampleBrick /
+ * DownsampleBricktoBrick (.inc:1-356; mean in double truncated to T, or the
+ * 7-value median network of VolumeTools::Filter) followed by FillOverlap
+ * (.cpp:1203-1372) in the reference's sequential order.  Bricks are written
+ * back to back in TOC order (LOD-major, then z, y, x) into `pool`;
+ * brick_offsets (voxels) gets one entry per brick.  Ghost voxels the reference
+ * leaves holding a previous brick's bytes (clamp mode only) are zero here.
+ * Returns the brick count, or -1 if pool_voxels or max_bricks is too small. */
+int64_t orc_build_octree(const void* raw, int dtype, const uint64_t dims[3],
+                         const uint32_t brick_size[3], uint32_t overlap, int clamp_to_edge,
+                         int median, void* pool, uint64_t pool_voxels,
+                         uint64_t* brick_offsets, uint64_t max_bricks);
+
 /* MaxGradientMagnitude as Histogram2DDataBlock::ComputeTemplate<T> finds it
  * (Histogram2DDataBlock.cpp:327-345, 363-397). */
 double orc_max_gradient(const void* raw, int dtype, const uint64_t dims[3],

@@ -29,6 +29,11 @@ CASES = [
     ("wrap25x14x13_u8", (25, 14, 13), np.uint8, 16, 2, False, 255, 5),
     ("cube64_u8", (64, 64, 64), np.uint8, 34, 1, False, 255, 6),
 ]
+# the same converter with the 7-value median filter instead of the mean
+MEDIAN_CASES = [
+    ("median37x29x23_u8", (37, 29, 23), np.uint8, 16, 1, False, 255, 7),
+    ("median40x33x20_u16", (40, 33, 20), np.uint16, 12, 2, False, 4095, 8),
+]
 
 
 def make_input(dims, dtype, vmax, seed):
@@ -42,11 +47,13 @@ def make_input(dims, dtype, vmax, seed):
 def main():
     if not refconv.available():
         raise SystemExit("oracle/_ref/libtuvok_ref.so missing: build it with make -C oracle/ref")
-    for name, dims, dtype, bs, ov, clamp, vmax, seed in CASES:
+    cases = [c + (False,) for c in CASES] + [c + (True,) for c in MEDIAN_CASES]
+    for name, dims, dtype, bs, ov, clamp, vmax, seed, median in cases:
         raw = make_input(dims, dtype, vmax, seed)
-        bricks = refconv.convert(raw, (bs, bs, bs), ov, clamp=clamp)
+        bricks = refconv.convert(raw, (bs, bs, bs), ov, clamp=clamp, median=median)
         arrays = {"raw": raw,
                   "meta": np.array([dims[0], dims[1], dims[2], bs, ov, int(clamp)], dtype=np.int64),
+                  "median": np.array([int(median)], dtype=np.int64),
                   "coords": np.array([b["coords"] for b in bricks], dtype=np.int64),
                   "sizes": np.array([b["size"] for b in bricks], dtype=np.int64),
                   "minmax": np.array([(b["min"], b["max"]) for b in bricks], dtype=np.float64)}

@@ -99,6 +99,32 @@ def test_oracle_lod0_equals_reference_converter(path):
     assert n0 == lod_counts[0][0] * lod_counts[0][1] * lod_counts[0][2]
 
 
+def is_median(d):
+    return "median" in d.files and bool(d["median"][0])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_oracle_octree_equals_reference_converter(path):
+    """Every LOD >= 1 brick: DownsampleBrick (mean or median) + FillOverlap in
+    the reference's sequential order, including the corner ghosts it leaves
+    at zero.  With clamping the reference reuses an uncleared buffer, so only
+    inner voxels are defined there."""
+    d, dims, bsize, ov, clamp = load(path)
+    bricks = O.build_octree(d["raw"], bsize, ov, clamp=clamp, median=is_median(d))
+    assert len(bricks) == len(d["coords"])
+    for i, c in enumerate(d["coords"]):
+        if c[3] == 0:
+            continue
+        ref = d[f"brick{i}"]
+        assert bricks[i].shape == ref.shape
+        if clamp:
+            np.testing.assert_array_equal(bricks[i][ov:-ov, ov:-ov, ov:-ov],
+                                          ref[ov:-ov, ov:-ov, ov:-ov], err_msg=str(tuple(c)))
+        else:
+            np.testing.assert_array_equal(bricks[i], ref, err_msg=str(tuple(c)))
+            assert O.brick_stats(bricks[i]) == tuple(d["minmax"][i])
+
+
 @pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
 def test_oracle_histogram_counts_every_voxel_once(path):
     d, dims, bsize, ov, clamp = load(path)
