@@ -123,6 +123,21 @@ tvk_status tvk_volume_create(const void* voxels, tvk_dtype dtype, const uint64_t
 tvk_status tvk_volume_create_device(const void* device_voxels, tvk_dtype dtype,
                                     const uint64_t dims[3], const uint32_t brick_size[3],
                                     uint32_t overlap, int clamp_to_edge, tvk_volume** out);
+/* Flags of tvk_volume_create_ex. */
+enum {
+  TVK_VOLUME_CLAMP_TO_EDGE = 1, /* replicate border voxels into the ghost layer */
+  TVK_VOLUME_DEVICE_INPUT = 2,  /* `voxels` is device memory */
+  TVK_VOLUME_MEDIAN = 4,        /* coarser LODs by the 7-value median, not the mean */
+  TVK_VOLUME_LOD0_ONLY = 8      /* skip the coarser LODs */
+};
+/* As tvk_volume_create, with every LOD of ExtendedOctreeConverter::Convert:
+ * LOD >= 1 bricks come from ComputeHierarchy / DownsampleBrick
+ * (ExtendedOctreeConverter.inc:1-398) and FillOverlap (.cpp:1203-1372), and
+ * get min/max statistics.  tvk_volume_create and _create_device build every
+ * LOD with the mean filter. */
+tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint64_t dims[3],
+                                const uint32_t brick_size[3], uint32_t overlap, uint32_t flags,
+                                tvk_volume** out);
 tvk_status tvk_volume_destroy(tvk_volume* v);
 tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out);
 
@@ -130,7 +145,7 @@ tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out);
 tvk_status tvk_volume_get_lod(const tvk_volume* v, uint32_t lod, uint64_t size[3],
                               uint64_t brick_count[3]);
 
-/* BrickedDataset::GetBrickMetadata (IO/BrickedDataset.h:62) for a LOD-0 key;
+/* BrickedDataset::GetBrickMetadata (IO/BrickedDataset.h:62) for any built LOD;
  * values follow UVFDataset::ComputeMetadataTOC (IO/uvfDataset.cpp:242-288). */
 tvk_status tvk_volume_get_brick_md(const tvk_volume* v, uint64_t timestep, uint64_t lod,
                                    uint64_t index, tvk_brick_md* out);

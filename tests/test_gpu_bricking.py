@@ -102,14 +102,69 @@ def test_gpu_bricking_plain_small_full_size(cuda_ok):
         assert (mm.min_scalar, mm.max_scalar) == O.brick_stats(ob)
 
 
+@pytest.mark.parametrize("path", FIXTURES, ids=[p.stem for p in FIXTURES])
+def test_gpu_octree_equals_reference_converter(cuda_ok, path):
+    """Every LOD >= 1 brick (DownsampleBrick + FillOverlap) against the
+    reference converter; with clamping only inner voxels are defined there."""
+    from test_oracle_golden import is_median
+    d, dims, bsize, ov, clamp = load(path)
+    vol = Volume(d["raw"], brick_size=bsize, overlap=ov, clamp_to_edge=clamp, median=is_median(d))
+    for i, c in enumerate(d["coords"]):
+        x, y, z, lod = (int(v) for v in c)
+        if lod == 0:
+            continue
+        k = vol.IndexFrom4D(x, y, z, lod)
+        b = vol.GetBrick((0, lod, k))
+        ref = d[f"brick{i}"]
+        assert b.shape == ref.shape, (tuple(c), b.shape, ref.shape)
+        if clamp:
+            np.testing.assert_array_equal(b[ov:-ov, ov:-ov, ov:-ov], ref[ov:-ov, ov:-ov, ov:-ov],
+                                          err_msg=str(tuple(c)))
+        else:
+            np.testing.assert_array_equal(b, ref, err_msg=str(tuple(c)))
+            mm = vol.MaxMinForKey((0, lod, k))
+            assert (mm.min_scalar, mm.max_scalar) == tuple(d["minmax"][i])
+
+
+@pytest.mark.parametrize("dims,dtype,bs,ov,clamp,median", [
+    ((61, 47, 39), np.uint16, 18, 1, False, False),
+    ((61, 47, 39), np.uint8, 18, 1, True, False),
+    ((50, 50, 50), np.uint8, 10, 1, False, True),
+    ((33, 70, 21), np.uint16, 14, 2, False, True),
+])
+def test_gpu_octree_equals_oracle(cuda_ok, dims, dtype, bs, ov, clamp, median):
+    vmax = 255 if dtype == np.uint8 else 4095
+    raw = numpy_blob_volume(dims, dtype, 9, (2, 8), (vmax * 0.2, vmax), vmax, seed=41, noise=5)
+    vol = Volume(raw, brick_size=(bs, bs, bs), overlap=ov, clamp_to_edge=clamp, median=median)
+    ref = O.build_octree(raw, (bs, bs, bs), ov, clamp=clamp, median=median)
+    sizes, counts = O.lod_table(dims, (bs, bs, bs), ov)
+    i = 0
+    for lod, lc in enumerate(counts):
+        for k in range(lc[0] * lc[1] * lc[2]):
+            b = vol.GetBrick((0, lod, k))
+            if clamp and lod > 0:  # both sides define inner voxels only
+                np.testing.assert_array_equal(b[ov:-ov, ov:-ov, ov:-ov],
+                                              ref[i][ov:-ov, ov:-ov, ov:-ov])
+            else:
+                np.testing.assert_array_equal(b, ref[i], err_msg=f"lod {lod} brick {k}")
+                mm = vol.MaxMinForKey((0, lod, k))
+                assert (mm.min_scalar, mm.max_scalar) == O.brick_stats(ref[i])
+            i += 1
+    assert i == len(ref)
+
+
 def test_gpu_brick_key_errors(cuda_ok):
     raw = np.zeros((8, 8, 8), dtype=np.uint8)
     vol = Volume(raw, brick_size=(6, 6, 6), overlap=1)
     from tuvok_gb300 import TvkError
     with pytest.raises(TvkError):
         vol.GetBrick((0, 0, 10 ** 6))
-    with pytest.raises(TvkError) as e:
-        vol.GetBrick((0, 1, 0))
-    assert "UNSUPPORTED" in str(e.value)
+    assert vol.GetBrick((0, 1, 0)).shape == (6, 6, 6)  # LOD 1: 4^3 inner + ghost
+    with pytest.raises(TvkError):
+        vol.GetBrick((0, vol.GetLODLevelCount(), 0))
     with pytest.raises(TvkError):
         vol.IndexFrom4D(9, 0, 0, 0)
+    only0 = Volume(raw, brick_size=(6, 6, 6), overlap=1, lod0_only=True)
+    with pytest.raises(TvkError) as e:
+        only0.GetBrick((0, 1, 0))
+    assert "UNSUPPORTED" in str(e.value)

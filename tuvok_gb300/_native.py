@@ -64,6 +64,7 @@ PROTOTYPES = {
     "tvk_abi_version": [],
     "tvk_volume_create": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, C.POINTER(_vp)],
     "tvk_volume_create_device": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, C.POINTER(_vp)],
+    "tvk_volume_create_ex": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_uint32, C.POINTER(_vp)],
     "tvk_volume_destroy": [_vp],
     "tvk_volume_get_info": [_vp, C.POINTER(VolumeInfo)],
     "tvk_volume_get_lod": [_vp, C.c_uint32, _u64p, _u64p],

@@ -187,28 +187,42 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   const LodInfo& l0 = V->lods[0];
   V->n_bricks = l0.bricks[0] * l0.bricks[1] * l0.bricks[2];
   REQUIRE(V->n_bricks < (1ull << 31), "too many bricks");
-  brick_metadata(l0, V->brick_size, V->overlap, V->md);
-  V->offsets.resize(V->n_bricks);
-  V->sizes.resize(3 * V->n_bricks);
+  // bricks of every LOD in TOC order (LOD-major, then z, y, x); LOD 0 first
+  const size_t n_lods = V->build_lods ? V->lods.size() : 1;
+  V->lod_first.assign(1, 0);
+  V->md.clear();
+  for (size_t l = 0; l < n_lods; ++l) {
+    std::vector<tvk_brick_md> m;
+    brick_metadata(V->lods[l], V->brick_size, V->overlap, m);
+    V->md.insert(V->md.end(), m.begin(), m.end());
+    V->lod_first.push_back(V->md.size());
+  }
+  V->total_bricks = V->md.size();
+  V->offsets.resize(V->total_bricks);
+  V->sizes.resize(3 * V->total_bricks);
+  std::vector<uint64_t> voxels(V->total_bricks);
   const uint64_t align = 256 / V->bytes;  // brick starts on 256-byte boundaries
   uint64_t off = 0;
   uint32_t max_bz = 0;
-  for (uint64_t b = 0; b < V->n_bricks; ++b) {
+  for (uint64_t b = 0; b < V->total_bricks; ++b) {
     for (int a = 0; a < 3; ++a) V->sizes[3 * b + a] = V->md[b].n_voxels[a];
-    max_bz = std::max(max_bz, V->md[b].n_voxels[2]);
+    if (b < V->n_bricks) max_bz = std::max(max_bz, V->md[b].n_voxels[2]);
     V->offsets[b] = off;
-    const uint64_t n = uint64_t(V->sizes[3 * b]) * V->sizes[3 * b + 1] * V->sizes[3 * b + 2];
-    off += (n + align - 1) / align * align;
+    voxels[b] = uint64_t(V->sizes[3 * b]) * V->sizes[3 * b + 1] * V->sizes[3 * b + 2];
+    off += (voxels[b] + align - 1) / align * align;
   }
   V->pool_bytes = off * V->bytes;
   TVK_CUDA(cudaMalloc(&V->d_pool, V->pool_bytes));
 
-  DevBuf d_off, d_sizes, d_scratch;
-  d_off.ensure(V->n_bricks * sizeof(uint64_t));
-  d_sizes.ensure(V->n_bricks * 3 * sizeof(uint32_t));
-  TVK_CUDA(cudaMemcpyAsync(d_off.p, V->offsets.data(), V->n_bricks * sizeof(uint64_t),
+  DevBuf d_off, d_sizes, d_scratch, d_vox;
+  d_off.ensure(V->total_bricks * sizeof(uint64_t));
+  d_sizes.ensure(V->total_bricks * 3 * sizeof(uint32_t));
+  d_vox.ensure(V->total_bricks * sizeof(uint64_t));
+  TVK_CUDA(cudaMemcpyAsync(d_off.p, V->offsets.data(), V->total_bricks * sizeof(uint64_t),
                            cudaMemcpyHostToDevice, s));
-  TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->n_bricks * 3 * sizeof(uint32_t),
+  TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_vox.p, voxels.data(), V->total_bricks * sizeof(uint64_t),
                            cudaMemcpyHostToDevice, s));
   // scratch: bmin, bmax, bhist, hist, max_grad bits, raw min/max
   const uint64_t gbins = uint64_t(1) << (8 * V->bytes);
@@ -279,6 +293,26 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                      d_cell_off, V->n_bricks, max_cells, static_cast<uint32_t*>(V->d_cells), s,
                      &launches);
+  // pass 5: the coarser LODs (ComputeHierarchy + FillOverlap) and their min/max
+  DevBuf d_lmm, d_wave;
+  std::vector<uint32_t> lmin, lmax;
+  if (V->total_bricks > V->n_bricks) {
+    d_lmm.ensure(2 * V->total_bricks * sizeof(uint32_t));
+    uint64_t max_lod_bricks = 0;
+    for (size_t l = 1; l < n_lods; ++l)
+      max_lod_bricks = std::max<uint64_t>(max_lod_bricks, V->lod_first[l + 1] - V->lod_first[l]);
+    d_wave.ensure(max_lod_bricks * sizeof(uint32_t));
+    std::vector<LodInfo> built(V->lods.begin(), V->lods.begin() + n_lods);
+    build_lod_levels(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_vox.as<uint64_t>(), built,
+                     V->lod_first, V->brick_size, V->overlap, V->clamp, V->median,
+                     d_lmm.as<uint32_t>(), d_lmm.as<uint32_t>() + V->total_bricks,
+                     d_wave.as<uint32_t>(), s, &launches);
+    lmin.resize(V->total_bricks);
+    lmax.resize(V->total_bricks);
+    TVK_CUDA(cudaMemcpyAsync(lmin.data(), d_lmm.p, V->total_bricks * 4, cudaMemcpyDeviceToHost, s));
+    TVK_CUDA(cudaMemcpyAsync(lmax.data(), d_lmm.as<uint32_t>() + V->total_bricks,
+                             V->total_bricks * 4, cudaMemcpyDeviceToHost, s));
+  }
 
   std::vector<uint32_t> bmin(V->n_bricks), bmax(V->n_bricks);
   V->hist.resize(gbins);
@@ -290,11 +324,11 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   TVK_CUDA(cudaMemcpyAsync(V->bhist.data(), sc.bhist, sz_bh, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaMemcpyAsync(&mg, sc.max_grad_bits, 8, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaStreamSynchronize(s));
-  V->bmin.resize(V->n_bricks);
-  V->bmax.resize(V->n_bricks);
-  for (uint64_t i = 0; i < V->n_bricks; ++i) {
-    V->bmin[i] = bmin[i];
-    V->bmax[i] = bmax[i];
+  V->bmin.resize(V->total_bricks);
+  V->bmax.resize(V->total_bricks);
+  for (uint64_t i = 0; i < V->total_bricks; ++i) {
+    V->bmin[i] = i < V->n_bricks ? bmin[i] : lmin[i];
+    V->bmax[i] = i < V->n_bricks ? bmax[i] : lmax[i];
   }
   double mgd;
   std::memcpy(&mgd, &mg, 8);
@@ -312,7 +346,8 @@ void free_volume_device(tvk_volume* V) {
 }
 
 tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, const uint64_t dims[3],
-                          const uint32_t bsz[3], uint32_t ov, int clamp) {
+                          const uint32_t bsz[3], uint32_t ov, int clamp, bool median = false,
+                          bool build_lods = true) {
   REQUIRE(src && dims && bsz, "null argument");
   REQUIRE(dtype == TVK_U8 || dtype == TVK_U16, "dtype must be TVK_U8 or TVK_U16");
   for (int a = 0; a < 3; ++a) {
@@ -331,6 +366,8 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
   }
   V->overlap = ov;
   V->clamp = clamp != 0;
+  V->median = median;
+  V->build_lods = build_lods;
   cudaStream_t s;
   TVK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   struct StreamGuard {
@@ -356,12 +393,15 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
   return V.release();
 }
 
+// Global (TOC) index of a brick key (timestep, LOD, 1D index within the LOD).
 uint64_t key_check(const tvk_volume* v, uint64_t ts, uint64_t lod, uint64_t idx) {
   REQUIRE(v, "null volume");
   REQUIRE(ts == 0, "only timestep 0 exists");
-  if (lod != 0) fail(TVK_ERR_UNSUPPORTED, "only LOD 0 bricks are resident on the device");
-  REQUIRE(idx < v->n_bricks, "brick index out of range");
-  return idx;
+  REQUIRE(lod < v->lods.size(), "LOD out of range");
+  if (lod + 1 >= v->lod_first.size())
+    fail(TVK_ERR_UNSUPPORTED, "the volume was created with LOD 0 only");
+  REQUIRE(idx < v->lod_first[lod + 1] - v->lod_first[lod], "brick index out of range");
+  return v->lod_first[lod] + idx;
 }
 
 // ------------------------------------------------------------ view math
@@ -805,6 +845,21 @@ tvk_status tvk_volume_create_device(const void* device_voxels, tvk_dtype dtype,
     REQUIRE(out, "null output handle");
     *out = tvk::create_volume(device_voxels, true, dtype, dims, brick_size, overlap,
                               clamp_to_edge);
+  });
+}
+
+tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint64_t dims[3],
+                                const uint32_t brick_size[3], uint32_t overlap, uint32_t flags,
+                                tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(out, "null output handle");
+    REQUIRE((flags & ~uint32_t(TVK_VOLUME_CLAMP_TO_EDGE | TVK_VOLUME_DEVICE_INPUT |
+                               TVK_VOLUME_MEDIAN | TVK_VOLUME_LOD0_ONLY)) == 0,
+            "unknown volume flag");
+    *out = tvk::create_volume(voxels, (flags & TVK_VOLUME_DEVICE_INPUT) != 0, dtype, dims,
+                              brick_size, overlap, (flags & TVK_VOLUME_CLAMP_TO_EDGE) ? 1 : 0,
+                              (flags & TVK_VOLUME_MEDIAN) != 0,
+                              (flags & TVK_VOLUME_LOD0_ONLY) == 0);
   });
 }
 

@@ -1,0 +1,329 @@
+// lod.cu -- coarser LODs of the brick octree on sm_103a.
+//
+// ExtendedOctreeConverter::ComputeHierarchy (IO/UVF/ExtendedOctree/
+// ExtendedOctreeConverter.inc:358-398) builds LOD l from LOD l-1 brick by brick:
+// DownsampleBrick filters up to eight child bricks into each target (2x2x2 mean
+// computed in double and truncated, or the 7-value median network of
+// VolumeTools::Filter; 4- and 2-sample filters on odd borders), then
+// FillOverlap (ExtendedOctreeConverter.cpp:1203-1372) copies the ghost layers
+// from up to ten neighbours, bricks in z, y, x order.  FillOverlap is order
+// dependent: a brick reads its lower neighbours after they were filled and its
+// higher neighbours before (so some corner ghosts end up zero).  Processing the
+// bricks in wavefronts of equal x+y+z reproduces exactly that state: a brick's
+// lower face neighbours lie on the previous wavefront and every brick it reads
+// on the higher side lies on a later one.
+//
+// Downsampling: one thread per target voxel, mean as integer sum >> k (exact:
+// the double sum of at most eight 16-bit values is exact and dividing by a
+// power of two then truncating is the same shift).  FillOverlap: one CTA per
+// brick of the wavefront; each ghost voxel takes the source of the last copy
+// (in the reference's order) whose target region holds it.
+#include "tvk_internal.h"
+
+namespace tvk {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <class T>
+__device__ __forceinline__ void order2(T& a, T& b) {
+  if (a > b) { const T t = a; a = b; b = t; }
+}
+
+template <class T>
+__device__ __forceinline__ T median8(T a, T b, T c, T d, T e, T f, T g) {
+  // VolumeTools.h:242-262 (the eighth value is not used)
+  order2(a, b); order2(c, d); order2(a, c); order2(b, d); order2(b, c);
+  // InsertIntoQuadruple (VolumeTools.h:212-227) of e, then f
+  T* p[2] = {&e, &f};
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    T& v = *p[q];
+    if (v > c) {
+      order2(d, v);
+    } else if (v < b) {
+      d = c; c = b; b = v; order2(a, b);
+    } else {
+      d = c; c = v;
+    }
+  }
+  return max(min(d, g), c);
+}
+
+template <class T>
+__device__ __forceinline__ T median4(T a, T b, T c) {
+  order2(a, b);
+  order2(b, c);
+  return max(a, b);
+}
+
+// Geometry of one LOD for the kernels.
+struct LodGeom {
+  uint32_t cnt[3];        // bricks per axis
+  uint32_t lod_size[3];
+  uint64_t first;         // TOC index of the first brick
+};
+
+__device__ __forceinline__ uint32_t brick_extent(const LodGeom& g, const uint32_t B[3],
+                                                 uint32_t ov, int a, uint32_t c) {
+  // ExtendedOctree::ComputeBrickSize (ExtendedOctree.cpp:276-285)
+  const uint32_t core = B[a] - 2 * ov;
+  const bool last = c == g.cnt[a] - 1;
+  return (last && (g.lod_size[a] % core)) ? 2 * ov + g.lod_size[a] % core : B[a];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, LodGeom lo,
+                  LodGeom hi, uint32_t B0, uint32_t B1, uint32_t B2, uint32_t ov, int median,
+                  uint32_t z_chunk) {
+  const uint32_t B[3] = {B0, B1, B2};
+  const uint32_t b = blockIdx.x;
+  const uint32_t c[3] = {b % hi.cnt[0], (b / hi.cnt[0]) % hi.cnt[1], b / (hi.cnt[0] * hi.cnt[1])};
+  uint32_t n[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) n[a] = brick_extent(hi, B, ov, a, c[a]);
+  T* dst = pool + offsets[hi.first + b];
+  const uint32_t z0 = blockIdx.y * z_chunk, z1 = min(n[2], z0 + z_chunk);
+  if (z0 >= z1) return;
+  const uint32_t sxy = n[0] * n[1];
+  const uint32_t total = (z1 - z0) * sxy;
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t k = z0 + t / sxy, r = t % sxy, j = r / n[0], i = r % n[0];
+    const uint32_t v[3] = {i, j, k};
+    T out = T(0);
+    bool covered = true;
+    uint32_t child[3], l[3], cs[3];
+    int pair[3];  // 1: two samples along the axis, 0: the odd boundary sample
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (v[a] < ov || v[a] >= n[a] - ov) { covered = false; break; }
+      const uint32_t tt = v[a] - ov;
+      const uint32_t split = (B[a] - 2 * ov + 1) / 2;  // ceil(core / 2)
+      const uint32_t cc = tt >= split ? 1u : 0u;
+      child[a] = 2 * c[a] + cc;
+      if (child[a] >= lo.cnt[a]) { covered = false; break; }
+      l[a] = tt - cc * split;
+      cs[a] = brick_extent(lo, B, ov, a, child[a]);
+      const uint32_t even = (cs[a] - 2 * ov) / 2;
+      if (l[a] < even) pair[a] = 1;
+      else if (l[a] == even && (cs[a] & 1u)) pair[a] = 0;
+      else { covered = false; break; }
+    }
+    if (covered) {
+      const T* src = pool + offsets[lo.first + child[0] + child[1] * lo.cnt[0] +
+                                    child[2] * lo.cnt[0] * lo.cnt[1]];
+      const uint32_t X = 2 * l[0] + ov, Y = 2 * l[1] + ov, Z = 2 * l[2] + ov;
+      auto S = [&](uint32_t x, uint32_t y, uint32_t z) -> T {
+        return src[x + (uint64_t(y) + uint64_t(z) * cs[1]) * cs[0]];
+      };
+      const int np = pair[0] + pair[1] + pair[2];
+      if (np == 3) {
+        // DownsampleBricktoBrick p0..p7 order (.inc:28-35)
+        const T a0 = S(X, Y, Z), a1 = S(X, Y, Z + 1), a2 = S(X, Y + 1, Z), a3 = S(X, Y + 1, Z + 1);
+        const T a4 = S(X + 1, Y, Z), a5 = S(X + 1, Y, Z + 1), a6 = S(X + 1, Y + 1, Z),
+                a7 = S(X + 1, Y + 1, Z + 1);
+        out = median ? median8<T>(a0, a1, a2, a3, a4, a5, a6)
+                     : T((uint32_t(a0) + a1 + a2 + a3 + a4 + a5 + a6 + a7) >> 3);
+      } else if (np == 2) {
+        T a0, a1, a2, a3;
+        if (!pair[0]) {  // plane at the end of x: p0, p1, p2, p3
+          a0 = S(X, Y, Z); a1 = S(X, Y, Z + 1); a2 = S(X, Y + 1, Z); a3 = S(X, Y + 1, Z + 1);
+        } else if (!pair[1]) {  // end of y: p0, p1, p4, p5
+          a0 = S(X, Y, Z); a1 = S(X, Y, Z + 1); a2 = S(X + 1, Y, Z); a3 = S(X + 1, Y, Z + 1);
+        } else {  // end of z: p0, p2, p4, p6
+          a0 = S(X, Y, Z); a1 = S(X, Y + 1, Z); a2 = S(X + 1, Y, Z); a3 = S(X + 1, Y + 1, Z);
+        }
+        out = median ? median4<T>(a0, a1, a2) : T((uint32_t(a0) + a1 + a2 + a3) >> 2);
+      } else if (np == 1) {
+        T a0 = S(X, Y, Z), a1;
+        if (pair[2]) a1 = S(X, Y, Z + 1);       // x/y line: p0, p1
+        else if (pair[0]) a1 = S(X + 1, Y, Z);  // y/z line: p0, p4
+        else a1 = S(X, Y + 1, Z);               // x/z line: p0, p2
+        out = median ? a0 : T((uint32_t(a0) + a1) >> 1);
+      } else {
+        out = S(X, Y, Z);  // odd corner copies *p0 (.inc:244-246)
+      }
+    }
+    dst[uint64_t(k) * sxy + r] = out;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+fill_overlap_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, LodGeom g,
+                    const uint32_t* __restrict__ wave, uint32_t B0, uint32_t B1, uint32_t B2,
+                    uint32_t ov, int clamp) {
+  const uint32_t B[3] = {B0, B1, B2};
+  const uint32_t b = wave[blockIdx.x];
+  const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
+  uint32_t n[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) n[a] = brick_extent(g, B, ov, a, c[a]);
+  T* dst = pool + offsets[g.first + b];
+  const bool has_lo[3] = {c[0] > 0, c[1] > 0, c[2] > 0};
+  const bool has_hi[3] = {c[0] + 1 < g.cnt[0], c[1] + 1 < g.cnt[1], c[2] + 1 < g.cnt[2]};
+  auto brick_ptr = [&](int dx, int dy, int dz) -> const T* {
+    return pool + offsets[g.first + (c[0] + dx) + (c[1] + dy) * g.cnt[0] +
+                          (c[2] + dz) * g.cnt[0] * g.cnt[1]];
+  };
+  const uint32_t total = n[0] * n[1] * n[2];
+  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+    const uint32_t i = t % n[0], j = (t / n[0]) % n[1], k = t / (n[0] * n[1]);
+    const bool xh = i >= n[0] - ov, yh = j >= n[1] - ov, zh = k >= n[2] - ov;
+    const bool xl = i < ov, yl = j < ov, zl = k < ov;
+    // the last copy of FillOverlap whose target region holds (i, j, k)
+    int dx = 0, dy = 0, dz = 0;
+    bool found = true;
+    if (has_hi[0] && has_hi[1] && has_hi[2] && xh && yh && zh) { dx = 1; dy = 1; dz = 1; }
+    else if (has_hi[1] && has_hi[2] && yh && zh) { dy = 1; dz = 1; }
+    else if (has_hi[0] && has_hi[2] && xh && zh) { dx = 1; dz = 1; }
+    else if (has_hi[0] && has_hi[1] && xh && yh) { dx = 1; dy = 1; }
+    else if (has_lo[2] && zl) { dz = -1; }
+    else if (has_lo[1] && yl) { dy = -1; }
+    else if (has_lo[0] && xl) { dx = -1; }
+    else if (has_hi[2] && zh) { dz = 1; }
+    else if (has_hi[1] && yh) { dy = 1; }
+    else if (has_hi[0] && xh) { dx = 1; }
+    else found = false;
+    if (!found) continue;
+    // source coordinates: a higher neighbour's first inner layers, a lower
+    // neighbour's last inner layers, the same index along the other axes
+    uint32_t s[3] = {i, j, k};
+    uint32_t ns[3];
+    const int d[3] = {dx, dy, dz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      ns[a] = d[a] == 0 ? n[a] : brick_extent(g, B, ov, a, c[a] + d[a]);
+      if (d[a] > 0) s[a] = s[a] - (n[a] - ov) + ov;
+      else if (d[a] < 0) s[a] = s[a] + ns[a] - 2 * ov;
+    }
+    const T* src = brick_ptr(dx, dy, dz);
+    dst[t] = src[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * ns[1]) * ns[0]];
+  }
+  if (!clamp) return;
+  // ClampToEdge (ExtendedOctreeConverter.cpp:376-462) on sides without a
+  // neighbour: x, then y, then z, each reading the previous step's result
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      const uint32_t v[3] = {t % n[0], (t / n[0]) % n[1], t / (n[0] * n[1])};
+      uint32_t from = v[a];
+      if (!has_lo[a] && v[a] < ov) from = ov;
+      else if (!has_hi[a] && v[a] >= n[a] - ov) from = n[a] - 1 - ov;
+      else continue;
+      uint32_t s[3] = {v[0], v[1], v[2]};
+      s[a] = from;
+      dst[t] = dst[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * n[1]) * n[0]];
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+brick_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                    const uint64_t* __restrict__ voxels, uint64_t first, uint32_t* out_min,
+                    uint32_t* out_max) {
+  // ComputeBrickStats<T> (.inc:408-444): every voxel of the brick
+  const uint64_t b = first + blockIdx.x;
+  const T* p = pool + offsets[b];
+  const uint64_t nv = voxels[b];
+  uint32_t lo = 0xffffffffu, hi = 0;
+  for (uint64_t t = threadIdx.x; t < nv; t += blockDim.x) {
+    const uint32_t v = p[t];
+    lo = min(lo, v);
+    hi = max(hi, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  __shared__ uint32_t slo[kThreads / 32], shi[kThreads / 32];
+  if ((threadIdx.x & 31) == 0) { slo[threadIdx.x >> 5] = lo; shi[threadIdx.x >> 5] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kThreads / 32; ++w) { lo = min(lo, slo[w]); hi = max(hi, shi[w]); }
+    out_min[blockIdx.x] = lo;
+    out_max[blockIdx.x] = hi;
+  }
+}
+
+}  // namespace
+
+void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const uint64_t* d_voxels,
+                      const std::vector<LodInfo>& lods, const std::vector<uint64_t>& lod_first,
+                      const uint32_t B[3], uint32_t ov, bool clamp, bool median,
+                      uint32_t* d_min, uint32_t* d_max, uint32_t* d_wave, cudaStream_t s,
+                      uint64_t* launches) {
+  auto geom = [&](size_t l) {
+    LodGeom g;
+    for (int a = 0; a < 3; ++a) {
+      g.cnt[a] = uint32_t(lods[l].bricks[a]);
+      g.lod_size[a] = uint32_t(lods[l].size[a]);
+    }
+    g.first = lod_first[l];
+    return g;
+  };
+  std::vector<uint32_t> wave_host;
+  for (size_t l = 1; l < lods.size(); ++l) {
+    const LodGeom lo = geom(l - 1), hi = geom(l);
+    const uint64_t nb = uint64_t(hi.cnt[0]) * hi.cnt[1] * hi.cnt[2];
+    const uint32_t z_chunk = 8;
+    const dim3 grid(uint32_t(nb), (B[2] + z_chunk - 1) / z_chunk);
+    if (bytes == 1)
+      downsample_kernel<uint8_t><<<grid, kThreads, 0, s>>>(static_cast<uint8_t*>(pool), d_offsets,
+                                                           lo, hi, B[0], B[1], B[2], ov,
+                                                           median ? 1 : 0, z_chunk);
+    else
+      downsample_kernel<uint16_t><<<grid, kThreads, 0, s>>>(static_cast<uint16_t*>(pool),
+                                                            d_offsets, lo, hi, B[0], B[1], B[2],
+                                                            ov, median ? 1 : 0, z_chunk);
+    TVK_CUDA(cudaGetLastError());
+    ++*launches;
+    // FillOverlap, one launch per wavefront x + y + z = w, in increasing w
+    const uint32_t nw = hi.cnt[0] + hi.cnt[1] + hi.cnt[2] - 2;
+    wave_host.clear();
+    std::vector<uint32_t> starts;
+    for (uint32_t w = 0; w < nw; ++w) {
+      starts.push_back(uint32_t(wave_host.size()));
+      for (uint32_t z = 0; z < hi.cnt[2]; ++z)
+        for (uint32_t y = 0; y < hi.cnt[1]; ++y) {
+          if (y + z > w || w - y - z >= hi.cnt[0]) continue;
+          const uint32_t x = w - y - z;
+          wave_host.push_back(x + y * hi.cnt[0] + z * hi.cnt[0] * hi.cnt[1]);
+        }
+    }
+    starts.push_back(uint32_t(wave_host.size()));
+    TVK_CUDA(cudaMemcpyAsync(d_wave, wave_host.data(), wave_host.size() * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, s));
+    for (uint32_t w = 0; w < nw; ++w) {
+      const uint32_t cnt = starts[w + 1] - starts[w];
+      if (!cnt) continue;
+      if (bytes == 1)
+        fill_overlap_kernel<uint8_t><<<cnt, kThreads, 0, s>>>(
+            static_cast<uint8_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
+            clamp ? 1 : 0);
+      else
+        fill_overlap_kernel<uint16_t><<<cnt, kThreads, 0, s>>>(
+            static_cast<uint16_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
+            clamp ? 1 : 0);
+      TVK_CUDA(cudaGetLastError());
+      ++*launches;
+    }
+    // the wave list is pageable host memory reused by the next level
+    TVK_CUDA(cudaStreamSynchronize(s));
+    if (bytes == 1)
+      brick_minmax_kernel<uint8_t><<<uint32_t(nb), kThreads, 0, s>>>(
+          static_cast<const uint8_t*>(pool), d_offsets, d_voxels, hi.first, d_min + hi.first,
+          d_max + hi.first);
+    else
+      brick_minmax_kernel<uint16_t><<<uint32_t(nb), kThreads, 0, s>>>(
+          static_cast<const uint16_t*>(pool), d_offsets, d_voxels, hi.first, d_min + hi.first,
+          d_max + hi.first);
+    TVK_CUDA(cudaGetLastError());
+    ++*launches;
+  }
+}
+
+}  // namespace tvk

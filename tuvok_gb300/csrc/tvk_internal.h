@@ -63,6 +63,13 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
                          const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
                          uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
                          uint64_t* launches);
+// LODs 1.. of the octree in place in the pool (lod.cu); min/max of every
+// LOD>=1 brick into d_min/d_max (indexed by TOC index).
+void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const uint64_t* d_voxels,
+                      const std::vector<LodInfo>& lods, const std::vector<uint64_t>& lod_first,
+                      const uint32_t B[3], uint32_t ov, bool clamp, bool median,
+                      uint32_t* d_min, uint32_t* d_max, uint32_t* d_wave, cudaStream_t s,
+                      uint64_t* launches);
 void launch_generate(void* out, int bytes, const uint64_t dims[3], const float* d_blobs,
                      uint32_t n_blobs, float noise_amp, uint32_t octaves, float cell,
                      uint64_t seed, int int_noise, float vmax, cudaStream_t s);
@@ -167,6 +174,10 @@ struct tvk_volume {
   uint32_t overlap = 0;
   bool clamp = false;
   std::vector<tvk::LodInfo> lods;
+  bool build_lods = true;   // coarser LODs too (ComputeHierarchy)
+  bool median = false;      // 7-value median instead of the mean
+  std::vector<uint64_t> lod_first;  // TOC index of each built LOD's first brick (+ end)
+  uint64_t total_bricks = 0;  // all built LODs
   uint64_t n_bricks = 0;  // LOD 0
   std::vector<tvk_brick_md> md;
   std::vector<uint64_t> offsets;  // voxels, per brick

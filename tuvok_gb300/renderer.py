@@ -34,10 +34,14 @@ class Volume:
     device pointer (int) together with ``dims`` and ``dtype``.
     """
 
+    CLAMP_TO_EDGE, DEVICE_INPUT, MEDIAN, LOD0_ONLY = 1, 2, 4, 8
+
     def __init__(self, data, brick_size=(64, 64, 64), overlap=1, clamp_to_edge=False,
-                 dims=None, dtype=None):
+                 dims=None, dtype=None, median=False, lod0_only=False):
         h = C.c_void_p()
         bs = _u32(brick_size)
+        flags = ((self.CLAMP_TO_EDGE if clamp_to_edge else 0) | (self.MEDIAN if median else 0) |
+                 (self.LOD0_ONLY if lod0_only else 0))
         if isinstance(data, np.ndarray):
             arr = np.ascontiguousarray(data)
             if arr.dtype == np.uint8:
@@ -47,14 +51,14 @@ class Volume:
             else:
                 raise TypeError("volumes are uint8 or uint16")
             z, y, x = arr.shape
-            check(lib().tvk_volume_create(arr.ctypes.data_as(C.c_void_p), dt, _u64((x, y, z)),
-                                          bs, overlap, int(clamp_to_edge), C.byref(h)))
+            check(lib().tvk_volume_create_ex(arr.ctypes.data_as(C.c_void_p), dt,
+                                             _u64((x, y, z)), bs, overlap, flags, C.byref(h)))
         else:
             if dims is None or dtype is None:
                 raise ValueError("a device pointer needs dims=(x, y, z) and dtype")
             dt = N.TVK_U8 if np.dtype(dtype) == np.uint8 else N.TVK_U16
-            check(lib().tvk_volume_create_device(C.c_void_p(int(data)), dt, _u64(dims), bs,
-                                                 overlap, int(clamp_to_edge), C.byref(h)))
+            check(lib().tvk_volume_create_ex(C.c_void_p(int(data)), dt, _u64(dims), bs, overlap,
+                                             flags | self.DEVICE_INPUT, C.byref(h)))
         self._h = h
         self.info = N.VolumeInfo()
         check(lib().tvk_volume_get_info(self._h, C.byref(self.info)))
