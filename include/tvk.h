@@ -164,6 +164,21 @@ tvk_status tvk_volume_get_minmax(const tvk_volume* v, uint64_t timestep, uint64_
 tvk_status tvk_volume_get_histogram(const tvk_volume* v, uint64_t* host_out, size_t bins,
                                     uint64_t* trimmed_len);
 
+/* Value x |gradient| histogram of the LOD-0 inner voxels, computed on the GPU
+ * on each call: Histogram2DDataBlock::Compute / ComputeTemplate
+ * (IO/UVF/Histogram2DDataBlock.cpp:69-126, 349-438) with the arguments
+ * RAWConverter passes (IO/RAWConverter.cpp:655-662).  host_out receives
+ * value_bins rows of 256 gradient bins (entries >= value_bins * 256);
+ * value_bins = 0 uses the trimmed 1D histogram's length.  The value bin is the
+ * raw value, or value * (value_bins - 1) / range_max when range_max exceeds
+ * value_bins - 1; the gradient bin is min(255, |g| / max|g| * 255).  A
+ * constant volume (max|g| = 0) puts every voxel in gradient bin 0.
+ * *max_gradient = Histogram2DDataBlock::GetMaxGradMagnitude (a float).
+ * TVK_ERR_UNSUPPORTED for overlap 0 (the reference reads outside the brick). */
+tvk_status tvk_volume_get_histogram2d(const tvk_volume* v, uint64_t* host_out, size_t value_bins,
+                                      size_t entries, uint64_t* value_bins_used,
+                                      float* max_gradient);
+
 /* 256-bin histograms of every LOD-0 brick's inner voxels, brick-major
  * (new: the reference stores only the global histogram); bin = value >> shift
  * with shift = max(0, bits(range_max) - 8). */

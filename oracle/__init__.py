@@ -66,6 +66,9 @@ def lib():
         L.orc_brick_metadata.restype = None
         L.orc_max_gradient.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int]
         L.orc_max_gradient.restype = C.c_double
+        L.orc_histogram2d.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
+                                      C.c_uint64, C.c_double, _u64p]
+        L.orc_histogram2d.restype = C.c_double
         L.orc_render.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p]
         L.orc_render.restype = C.c_uint64
         L.orc_round_half.argtypes = [C.c_float]
@@ -167,6 +170,24 @@ def max_gradient(raw, bsize, overlap, clamp=False):
     dims = (raw.shape[2], raw.shape[1], raw.shape[0])
     return lib().orc_max_gradient(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
                                   _u32(bsize), overlap, int(clamp))
+
+
+def histogram2d(raw, bsize, overlap, clamp=False, value_bins=None, max_nonzero=None):
+    """[value_bins, 256] value x |gradient| counts and the maximum |gradient|.
+
+    Defaults follow RAWConverter: value_bins = the trimmed 1D histogram's
+    length, max_nonzero = the volume's maximum value."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    if value_bins is None:
+        value_bins = int(raw.max()) + 1
+    if max_nonzero is None:
+        max_nonzero = float(raw.max())
+    out = np.zeros((value_bins, 256), dtype=np.uint64)
+    g = lib().orc_histogram2d(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims), _u32(bsize),
+                              overlap, int(clamp), value_bins, max_nonzero,
+                              out.ctypes.data_as(_u64p))
+    return out, g
 
 
 def build_octree(raw, bsize, overlap, clamp=False, median=False):

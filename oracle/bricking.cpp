@@ -254,17 +254,17 @@ extern "C" void orc_brick_metadata(const uint64_t lod_size[3], const uint64_t br
 }
 
 namespace {
-template <class T>
-double max_gradient(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
-                    bool clamp) {
-  // Histogram2DDataBlock::ComputeTemplate<T> first loop + ComputeGradient
-  // (Histogram2DDataBlock.cpp:327-345, 363-397): central differences over the
-  // inner voxels of every LOD-0 brick, normalised by 2 * max(T), in double.
+// Visits every inner voxel of every LOD-0 brick (bricks in TOC order, voxels z, y,
+// x) with its value and |gradient|: Histogram2DDataBlock::ComputeGradient
+// (Histogram2DDataBlock.cpp:327-345), central differences normalised by
+// 2 * max(T) in double, DOUBLEVECTOR3::length() = sqrt(x*x + y*y + z*z).
+template <class T, class F>
+void for_each_gradient(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                       bool clamp, F&& f) {
   uint64_t lod[3 * 64], cnt[3 * 64];
   orc_lod_table(dims, B, ov, lod, cnt, 64);
   std::vector<T> brick(uint64_t(B[0]) * B[1] * B[2]);
   const double nf = double(std::numeric_limits<T>::max());
-  double best = 0;
   for (uint64_t bz = 0; bz < cnt[2]; ++bz)
     for (uint64_t by = 0; by < cnt[1]; ++by)
       for (uint64_t bx = 0; bx < cnt[0]; ++bx) {
@@ -280,13 +280,56 @@ double max_gradient(const T* raw, const uint64_t dims[3], const uint32_t B[3], u
               const double gx = (double(brick[i - 1]) - double(brick[i + 1])) / (nf * 2);
               const double gy = (double(brick[i - sx]) - double(brick[i + sx])) / (nf * 2);
               const double gz = (double(brick[i - sxy]) - double(brick[i + sxy])) / (nf * 2);
-              const double l = std::sqrt(gx * gx + gy * gy + gz * gz);
-              if (l > best) best = l;
+              f(brick[i], std::sqrt(gx * gx + gy * gy + gz * gz));
             }
       }
+}
+
+template <class T>
+double max_gradient(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                    bool clamp) {
+  // Histogram2DDataBlock::ComputeTemplate<T> first loop (Histogram2DDataBlock.cpp:363-397)
+  double best = 0;
+  for_each_gradient<T>(raw, dims, B, ov, clamp, [&](T, double l) {
+    if (l > best) best = l;
+  });
   return best;
 }
+
+template <class T>
+double histogram2d(const T* raw, const uint64_t dims[3], const uint32_t B[3], uint32_t ov,
+                   bool clamp, uint64_t value_bins, double max_nonzero, uint64_t* hist) {
+  // Histogram2DDataBlock::ComputeTemplate<T> second loop (Histogram2DDataBlock.cpp:399-435):
+  // gradient bin = min(255, size_t(|g| / max|g| * 255.0f)); value bin = the raw
+  // value, or value * (bins - 1) / max_nonzero when the value range exceeds the
+  // bins; both clamped to the table.  A constant volume (max |g| = 0) divides
+  // 0 by 0 there, which C++ leaves undefined; this restatement puts those
+  // voxels in gradient bin 0.
+  const double gmax = max_gradient<T>(raw, dims, B, ov, clamp);
+  std::fill(hist, hist + value_bins * 256, uint64_t(0));
+  for_each_gradient<T>(raw, dims, B, ov, clamp, [&](T v, double l) {
+    uint64_t g = 0;
+    if (gmax > 0) g = std::min<uint64_t>(255, uint64_t(l / gmax * 255.0f));
+    uint64_t vb = (max_nonzero <= double(value_bins - 1))
+                      ? uint64_t(v)
+                      : uint64_t(double(v) * double(value_bins - 1) / max_nonzero);
+    if (vb > value_bins - 1) vb = value_bins - 1;
+    hist[vb * 256 + g]++;
+  });
+  return gmax;
+}
 }  // namespace
+
+extern "C" double orc_histogram2d(const void* raw, int dtype, const uint64_t dims[3],
+                                  const uint32_t brick_size[3], uint32_t overlap,
+                                  int clamp_to_edge, uint64_t value_bins, double max_nonzero,
+                                  uint64_t* hist) {
+  if (dtype == 0)
+    return histogram2d<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                                value_bins, max_nonzero, hist);
+  return histogram2d<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                               value_bins, max_nonzero, hist);
+}
 
 extern "C" double orc_max_gradient(const void* raw, int dtype, const uint64_t dims[3],
                                    const uint32_t brick_size[3], uint32_t overlap,

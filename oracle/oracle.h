@@ -88,6 +88,13 @@ double orc_max_gradient(const void* raw, int dtype, const uint64_t dims[3],
                         const uint32_t brick_size[3], uint32_t overlap,
                         int clamp_to_edge);
 
+/* The 2D value x |gradient| histogram of Histogram2DDataBlock::ComputeTemplate<T>
+ * (Histogram2DDataBlock.cpp:349-438): `hist` holds value_bins rows of 256
+ * gradient bins.  Returns the maximum gradient magnitude. */
+double orc_histogram2d(const void* raw, int dtype, const uint64_t dims[3],
+                       const uint32_t brick_size[3], uint32_t overlap, int clamp_to_edge,
+                       uint64_t value_bins, double max_nonzero, uint64_t* hist);
+
 /* ---- Ray march (Shaders/GLRaycaster-*.glsl) ---- */
 
 enum { ORC_RM_1D = 0, ORC_RM_2D = 1, ORC_RM_ISO = 2 };

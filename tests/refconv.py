@@ -1,5 +1,6 @@
 """Binding of oracle/_ref/libtuvok_ref.so: the reference's own
-ExtendedOctreeConverter, built from the reference sources by oracle/ref/Makefile.
+ExtendedOctreeConverter and UVF histogram blocks, built from the reference
+sources by oracle/ref/Makefile.
 
 Present only where the reference sources were available at build time; tests
 that need it skip otherwise.
@@ -36,6 +37,13 @@ def _load():
         L.ref_brick_data.restype = None
         L.ref_free.argtypes = [C.c_void_p]
         L.ref_free.restype = None
+        L.ref_histograms.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint32), C.c_uint32, C.c_int, C.c_char_p,
+                                     C.c_uint64, C.POINTER(C.c_uint64), C.c_size_t,
+                                     C.POINTER(C.c_size_t),
+                                     C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_size_t),
+                                     C.POINTER(C.c_float)]
+        L.ref_histograms.restype = C.c_int
         _lib = L
     return _lib
 
@@ -65,3 +73,27 @@ def convert(raw, brick_size, overlap, clamp=False, median=False, scratch="/tmp")
     finally:
         L.ref_free(h)
     return out
+
+
+def histograms(raw, brick_size, overlap, clamp=False, value_bins=0, scratch="/tmp"):
+    """The reference's Histogram1DDataBlock and Histogram2DDataBlock of raw
+    ([z, y, x]) as RAWConverter computes them: (hist1d, hist2d [bins, 256],
+    max gradient magnitude as float).  value_bins != 0 overrides the 2D
+    histogram's value-bin count (default: the 1D histogram's length)."""
+    L = _load()
+    raw = np.ascontiguousarray(raw)
+    dims = (C.c_uint64 * 3)(raw.shape[2], raw.shape[1], raw.shape[0])
+    cap1 = 1 << (8 * raw.dtype.itemsize)
+    h1 = np.zeros(cap1, dtype=np.uint64)
+    h2 = np.zeros(max(cap1, value_bins) * 256, dtype=np.uint64)
+    n1, nv = C.c_size_t(), C.c_size_t()
+    g = C.c_float()
+    rc = L.ref_histograms(raw.ctypes.data_as(C.c_void_p), 0 if raw.dtype == np.uint8 else 1,
+                          dims, (C.c_uint32 * 3)(*brick_size), overlap, int(clamp),
+                          scratch.encode(), value_bins,
+                          h1.ctypes.data_as(C.POINTER(C.c_uint64)), cap1,
+                          C.byref(n1), h2.ctypes.data_as(C.POINTER(C.c_uint64)), h2.size,
+                          C.byref(nv), C.byref(g))
+    if rc != 0:
+        raise RuntimeError(f"reference histograms failed ({rc})")
+    return h1[:n1.value], h2[:nv.value * 256].reshape(nv.value, 256), g.value

@@ -153,6 +153,60 @@ def test_gpu_octree_equals_oracle(cuda_ok, dims, dtype, bs, ov, clamp, median):
     assert i == len(ref)
 
 
+@pytest.mark.parametrize("dims,dtype,bs,ov,clamp,bins", [
+    ((37, 29, 23), np.uint8, 16, 1, False, 0),
+    ((30, 20, 25), np.uint16, 12, 2, False, 0),
+    ((40, 33, 21), np.uint8, 18, 1, True, 0),
+    ((40, 33, 21), np.uint8, 18, 1, False, 64),
+    ((26, 19, 31), np.uint16, 14, 1, False, 300),
+    ((70, 64, 45), np.uint16, 34, 1, False, 0),
+])
+def test_gpu_histogram2d_equals_oracle(cuda_ok, dims, dtype, bs, ov, clamp, bins):
+    """Histogram2DDataBlock's value x |gradient| counts, bin for bin."""
+    vmax = 255 if dtype == np.uint8 else 4095
+    raw = numpy_blob_volume(dims, dtype, 6, (3, 9), (vmax * 0.3, vmax * 0.9), vmax, seed=3,
+                            noise=3)
+    vol = Volume(raw, brick_size=(bs, bs, bs), overlap=ov, clamp_to_edge=clamp)
+    h, g = vol.Get2DHistogram(bins)
+    n = int(raw.max()) + 1
+    ref, rg = O.histogram2d(raw, (bs, bs, bs), ov, clamp, value_bins=bins or n)
+    assert h.shape == ref.shape
+    np.testing.assert_array_equal(h, ref)
+    assert g == float(np.float32(rg))
+
+
+def test_gpu_histogram2d_flat_and_no_overlap(cuda_ok):
+    raw = np.full((16, 16, 16), 40, dtype=np.uint8)
+    vol = Volume(raw, brick_size=(10, 10, 10), overlap=1, clamp_to_edge=True)
+    h, g = vol.Get2DHistogram()
+    # clamped borders, so max |g| = 0: every voxel lands in gradient bin 0
+    assert g == 0.0 and h.shape == (41, 256) and int(h[40, 0]) == raw.size
+    assert int(h.sum()) == raw.size
+    raw[7:9, 6:10, 5:8] = 90
+    vol = Volume(raw, brick_size=(10, 10, 10), overlap=1)
+    ref, _ = O.histogram2d(raw, (10, 10, 10), 1)
+    np.testing.assert_array_equal(vol.Get2DHistogram()[0], ref)
+    from tuvok_gb300 import TvkError
+    with pytest.raises(TvkError) as e:
+        Volume(raw, brick_size=(8, 8, 8), overlap=0).Get2DHistogram()
+    assert "UNSUPPORTED" in str(e.value)
+
+
+def test_gpu_histogram2d_full_size_properties(cuda_ok):
+    """256^3 uint8: every inner voxel counted once, each value row sums to the
+    1D histogram, and the top gradient bin is occupied."""
+    w = PLAIN_SMALL
+    raw = numpy_blob_volume((128, 128, 128), np.uint8, 16, (4, 20), (64, 255), 255, seed=5,
+                            noise=4)
+    raw = np.tile(raw, (2, 2, 2))
+    vol = Volume(raw, brick_size=w.brick_size, overlap=w.overlap)
+    h, g = vol.Get2DHistogram()
+    h1, n = vol.GetHistogram()
+    assert h.shape == (n, 256)
+    np.testing.assert_array_equal(h.sum(axis=1), h1[:n])
+    assert int(h[:, 254:].sum()) >= 1 and g == vol.MaxGradientMagnitude()
+
+
 def test_gpu_brick_key_errors(cuda_ok):
     raw = np.zeros((8, 8, 8), dtype=np.uint8)
     vol = Volume(raw, brick_size=(6, 6, 6), overlap=1)

@@ -164,6 +164,38 @@ def test_oracle_matches_live_reference(dims, dtype, bs, ov, clamp, tmp_path):
         assert O.brick_stats(mine) == (b["min"], b["max"])
 
 
+@pytest.mark.skipif(not refconv.available(), reason="reference converter not built here")
+@pytest.mark.parametrize("dims,dtype,bs,ov,clamp,bins", [
+    ((37, 29, 23), np.uint8, 16, 1, False, 0),
+    ((30, 20, 25), np.uint16, 12, 2, False, 0),
+    ((40, 33, 21), np.uint8, 18, 1, True, 0),
+    ((40, 33, 21), np.uint8, 18, 1, False, 64),     # values scaled into fewer bins
+    ((26, 19, 31), np.uint16, 14, 1, False, 300),
+    ((16, 16, 16), np.uint8, 10, 1, False, 0),      # flat volume with one bump
+])
+def test_oracle_histograms_equal_live_reference(dims, dtype, bs, ov, clamp, bins, tmp_path):
+    """Histogram1DDataBlock and Histogram2DDataBlock of the reference, run on the
+    same input, against the oracle's restatement."""
+    from tuvok_gb300.workloads import numpy_blob_volume
+    vmax = 255 if dtype == np.uint8 else 4095
+    if dims == (16, 16, 16):
+        raw = np.full(dims[::-1], 40, dtype=dtype)
+        raw[7:9, 6:10, 5:8] = 90
+    else:
+        raw = numpy_blob_volume(dims, dtype, 6, (3, 9), (vmax * 0.3, vmax * 0.9), vmax, seed=3,
+                                noise=3)
+    h1, h2, g = refconv.histograms(raw, (bs, bs, bs), ov, clamp, value_bins=bins,
+                                   scratch=str(tmp_path))
+    o1, n = O.histogram1d(raw, (bs, bs, bs), ov)
+    assert len(h1) == n
+    np.testing.assert_array_equal(h1, o1[:n])
+    o2, og = O.histogram2d(raw, (bs, bs, bs), ov, clamp, value_bins=bins or n)
+    assert h2.shape == o2.shape
+    np.testing.assert_array_equal(h2, o2)
+    assert g == float(np.float32(og))
+    assert int(h2.sum()) == raw.size
+
+
 def test_round_half_is_ieee_rne():
     rng = np.random.default_rng(3)
     xs = np.concatenate([rng.normal(0, 2, 2000), rng.uniform(-70000, 70000, 200),

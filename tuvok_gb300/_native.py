@@ -72,6 +72,7 @@ PROTOTYPES = {
     "tvk_volume_get_brick": [_vp, C.c_uint64, C.c_uint64, C.c_uint64, _vp, C.c_size_t],
     "tvk_volume_get_minmax": [_vp, C.c_uint64, C.c_uint64, C.c_uint64, C.POINTER(MinMax)],
     "tvk_volume_get_histogram": [_vp, _u64p, C.c_size_t, _u64p],
+    "tvk_volume_get_histogram2d": [_vp, _u64p, C.c_size_t, C.c_size_t, _u64p, _f32p],
     "tvk_volume_get_brick_histograms": [_vp, _u32p, C.c_size_t, _u32p],
     "tvk_volume_index_from_4d": [_vp, _u64p, _u64p],
     "tvk_volume_index_to_4d": [_vp, C.c_uint64, C.c_uint64, _u64p],

@@ -338,6 +338,46 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   V->hist_trimmed = len;
 }
 
+// Histogram2DDataBlock::ComputeTemplate<T> second pass (Histogram2DDataBlock.cpp:399-435)
+// over the LOD-0 bricks already in the pool, with the maximum gradient of the
+// first pass that build_volume ran.  `bins` rows of 256 gradient bins.
+void compute_histogram2d(const tvk_volume* V, uint64_t bins, uint64_t* host_out) {
+  uint32_t max_bz = 0;
+  for (uint64_t b = 0; b < V->n_bricks; ++b) max_bz = std::max(max_bz, V->sizes[3 * b + 2]);
+  const double nf2 = double(V->bytes == 1 ? 255 : 65535) * 2.0;
+  Hist2DParams hp{};
+  hp.ov = V->overlap;
+  hp.value_bins = uint32_t(bins);
+  hp.max_nonzero = V->range_max;
+  hp.scale_values = V->range_max > double(bins - 1) ? 1u : 0u;
+  hp.gmax = V->max_grad;
+  // |g| = sqrt(Q) / (2 max(T)) up to double rounding, so Q is recovered exactly
+  const double qr = V->max_grad * nf2;
+  hp.qmax = (long long)std::llround(qr * qr);
+  hp.inv_qmax = hp.qmax > 0 ? 1.0f / float(hp.qmax) : 0.0f;
+  const size_t out_bytes = bins * 256 * sizeof(uint64_t);
+  DevBuf d_off, d_sizes, d_hist;
+  d_off.ensure(V->n_bricks * sizeof(uint64_t));
+  d_sizes.ensure(V->n_bricks * 3 * sizeof(uint32_t));
+  d_hist.ensure(out_bytes);
+  cudaStream_t s;
+  TVK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  TVK_CUDA(cudaMemcpyAsync(d_off.p, V->offsets.data(), V->n_bricks * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->n_bricks * 3 * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemsetAsync(d_hist.p, 0, out_bytes, s));
+  uint64_t launches = 0;
+  launch_histogram2d(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                     V->n_bricks, max_bz, hp, d_hist.as<unsigned long long>(), s, &launches);
+  TVK_CUDA(cudaMemcpyAsync(host_out, d_hist.p, out_bytes, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaStreamSynchronize(s));
+}
+
 void free_volume_device(tvk_volume* V) {
   for (void** p : {&V->d_pool, &V->d_cells, &V->d_cell_meta}) {
     if (*p) cudaFree(*p);
@@ -945,6 +985,24 @@ tvk_status tvk_volume_get_histogram(const tvk_volume* v, uint64_t* host_out, siz
     const size_t n = std::min(bins, v->hist.size());
     for (size_t i = 0; i < n; ++i) host_out[i] = v->hist[i];
     if (trimmed_len) *trimmed_len = v->hist_trimmed;
+  });
+}
+
+tvk_status tvk_volume_get_histogram2d(const tvk_volume* v, uint64_t* host_out, size_t value_bins,
+                                      size_t entries, uint64_t* value_bins_used,
+                                      float* max_gradient) {
+  return guarded([&] {
+    REQUIRE(v && host_out, "null argument");
+    const uint64_t bins = value_bins ? value_bins : v->hist_trimmed;
+    REQUIRE(bins >= 1 && bins <= 65536, "value_bins must be 1 .. 65536");
+    REQUIRE(entries >= bins * 256, "output holds fewer than value_bins * 256 entries");
+    if (v->overlap == 0)
+      tvk::fail(TVK_ERR_UNSUPPORTED, "central differences need an overlap of at least 1");
+    TVK_CUDA(cudaSetDevice(v->device));
+    tvk::compute_histogram2d(v, bins, host_out);
+    if (value_bins_used) *value_bins_used = bins;
+    // Histogram2DDataBlock::m_fMaxGradMagnitude is a float
+    if (max_gradient) *max_gradient = float(v->max_grad);
   });
 }
 

@@ -8,7 +8,8 @@
 //     IO/UVF/Histogram1DDataBlock.cpp:120-161),
 //   * a 256-bin histogram of each brick's inner voxels.
 // A second kernel finds the maximum gradient magnitude over inner voxels
-// (Histogram2DDataBlock::ComputeGradient/ComputeTemplate, Histogram2DDataBlock.cpp:327-397).
+// (Histogram2DDataBlock::ComputeGradient/ComputeTemplate, Histogram2DDataBlock.cpp:327-397);
+// a third, run on request, fills the value x |gradient| histogram (:399-435).
 //
 // The voxel a brick position reads follows GetInputBrick
 // (ExtendedOctreeConverter.cpp:288-373) exactly: the reference copies x-scanlines
@@ -188,6 +189,70 @@ max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ off
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+histogram2d_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                   const uint32_t* __restrict__ sizes, Hist2DParams hp,
+                   unsigned long long* __restrict__ hist) {
+  // Value x |grad| counts over the inner voxels (Histogram2DDataBlock.cpp:399-435).
+  // The gradient bin is floor(|g| / max|g| * 255) evaluated in double by the
+  // reference.  Mathematically |g| / max|g| = sqrt(Q / Qmax) for the integer
+  // squared difference sums Q, so a float estimate decides the bin unless it
+  // lies within 1e-3 of a bin boundary (the estimate's error is below 1e-4);
+  // only those voxels evaluate the reference's double expression.
+  const uint32_t b = blockIdx.x;
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const T* p = pool + offsets[b];
+  const uint32_t ix = bs[0] - 2 * hp.ov, iy = bs[1] - 2 * hp.ov;
+  const uint32_t z0 = hp.ov + blockIdx.y * hp.z_chunk;
+  const uint32_t z1 = min(bs[2] - hp.ov, z0 + hp.z_chunk);
+  const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
+  const double nf2 = double(T(~T(0))) * 2.0;
+  const uint32_t n = (z1 > z0) ? (z1 - z0) * ix * iy : 0;
+  const uint32_t n_pad = (n + 31u) & ~31u;
+  for (uint32_t t = threadIdx.x; t < n_pad; t += blockDim.x) {
+    uint32_t key = 0xffffffffu;
+    if (t < n) {
+      const uint32_t k = z0 + t / (ix * iy);
+      const uint32_t r = t % (ix * iy);
+      const uint32_t j = hp.ov + r / ix;
+      const uint32_t i = hp.ov + r % ix;
+      const uint64_t c = uint64_t(i) + uint64_t(j) * sx + uint64_t(k) * sxy;
+      const int dx = int(p[c - 1]) - int(p[c + 1]);
+      const int dy = int(p[c - sx]) - int(p[c + sx]);
+      const int dz = int(p[c - sxy]) - int(p[c + sxy]);
+      const long long q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
+      uint32_t g = 0;
+      if (q > 0 && hp.qmax > 0) {
+        const float est = sqrtf(float(q) * hp.inv_qmax) * 255.0f;
+        const float fl = floorf(est);
+        if (est - fl > 1e-3f && fl + 1.0f - est > 1e-3f) {
+          g = min(255u, uint32_t(fl));
+        } else {
+          const double gx = __ddiv_rn(double(dx), nf2);
+          const double gy = __ddiv_rn(double(dy), nf2);
+          const double gz = __ddiv_rn(double(dz), nf2);
+          const double len = __dsqrt_rn(
+              __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz)));
+          const double rel = __dmul_rn(__ddiv_rn(len, hp.gmax), 255.0);
+          g = rel >= 255.0 ? 255u : uint32_t(rel);
+        }
+      }
+      const uint32_t v = p[c];
+      uint32_t vb = hp.scale_values
+                        ? uint32_t(__ddiv_rn(__dmul_rn(double(v), double(hp.value_bins - 1)),
+                                             hp.max_nonzero))
+                        : v;
+      vb = min(vb, hp.value_bins - 1);
+      key = vb * 256u + g;
+    }
+    // one atomic per distinct bin in the warp
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && (threadIdx.x & 31u) == uint32_t(__ffs(peers) - 1))
+      atomicAdd(&hist[key], (unsigned long long)__popc(peers));
+  }
+}
+
 uint32_t blocks_for(uint64_t n) {
   const uint64_t b = (n + kThreads - 1) / kThreads;
   return uint32_t(b < 152ull * 16 ? (b ? b : 1) : 152ull * 16);
@@ -244,6 +309,24 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
   else
     max_gradient_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
         static_cast<const uint16_t*>(pool), d_offsets, d_sizes, ov, z_chunk, out_bits);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_histogram2d(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, uint32_t max_bz,
+                        Hist2DParams hp, unsigned long long* hist, cudaStream_t s,
+                        uint64_t* launches) {
+  // central differences need a ghost layer on every side of the inner voxels
+  if (hp.ov == 0 || max_bz <= 2 * hp.ov) return;
+  hp.z_chunk = 4;
+  const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * hp.ov + hp.z_chunk - 1) / hp.z_chunk);
+  if (bytes == 1)
+    histogram2d_kernel<uint8_t><<<grid, kThreads, 0, s>>>(static_cast<const uint8_t*>(pool),
+                                                          d_offsets, d_sizes, hp, hist);
+  else
+    histogram2d_kernel<uint16_t><<<grid, kThreads, 0, s>>>(static_cast<const uint16_t*>(pool),
+                                                           d_offsets, d_sizes, hp, hist);
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }

@@ -63,6 +63,20 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
                          const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
                          uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
                          uint64_t* launches);
+// value x |gradient| histogram of the LOD-0 inner voxels (Histogram2DDataBlock)
+struct Hist2DParams {
+  uint32_t ov, z_chunk;
+  uint32_t value_bins;    // rows of 256 gradient bins
+  uint32_t scale_values;  // 1: bin = value * (value_bins - 1) / max_nonzero
+  double max_nonzero;
+  double gmax;            // maximum |gradient| (double, as the reference finds it)
+  long long qmax;         // its integer squared central-difference sum
+  float inv_qmax;
+};
+void launch_histogram2d(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, uint32_t max_bz,
+                        Hist2DParams hp, unsigned long long* hist, cudaStream_t s,
+                        uint64_t* launches);
 // LODs 1.. of the octree in place in the pool (lod.cu); min/max of every
 // LOD>=1 brick into d_min/d_max (indexed by TOC index).
 void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const uint64_t* d_voxels,

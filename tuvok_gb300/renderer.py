@@ -136,6 +136,17 @@ class Volume:
                                              C.byref(tl)))
         return out, int(tl.value)
 
+    def Get2DHistogram(self, value_bins=0):
+        """(counts [value_bins, 256] uint64, max gradient magnitude as float32);
+        value_bins 0 = the trimmed 1D histogram's length."""
+        bins = value_bins or self.GetHistogram()[1]
+        out = np.zeros((bins, 256), dtype=np.uint64)
+        used = C.c_uint64()
+        g = C.c_float()
+        check(lib().tvk_volume_get_histogram2d(self._h, out.ctypes.data_as(N._u64p), bins,
+                                               out.size, C.byref(used), C.byref(g)))
+        return out[:used.value], g.value
+
     def GetBrickHistograms(self):
         n = int(self.info.lod0_bricks)
         out = np.zeros((n, 256), dtype=np.uint32)
