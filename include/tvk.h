@@ -150,6 +150,33 @@ tvk_status tvk_volume_get_lod(const tvk_volume* v, uint32_t lod, uint64_t size[3
 tvk_status tvk_volume_get_brick_md(const tvk_volume* v, uint64_t timestep, uint64_t lod,
                                    uint64_t index, tvk_brick_md* out);
 
+/* MaxMinForKey modes of a rebricked volume (DynamicBrickingDS::MinMaxMode,
+ * IO/DynamicBrickingDS.h): the source brick's statistics, or the min/max of
+ * the target brick's own voxels (ghost included; computed when rebricking for
+ * both PRECOMPUTE and DYNAMIC, which give the same values). */
+typedef enum {
+  TVK_MM_SOURCE = 0,
+  TVK_MM_PRECOMPUTE = 1,
+  TVK_MM_DYNAMIC = 2
+} tvk_minmax_mode;
+
+/* DynamicBrickingDS::DynamicBrickingDS + Rebrick (IO/DynamicBrickingDS.cpp:133-139,
+ * 1090-1180): a new volume whose bricks of brick_size voxels (ghost included)
+ * are windows of src's bricks, gathered on the GPU for every built LOD.  Each
+ * axis' brick_size - 2*overlap must divide the source's inner brick size
+ * (TVK_ERR_INVALID_ARG "x dimension is not an integer multiple of original
+ * brick size." where the reference throws std::runtime_error).  The result
+ * answers the dataset queries (get_info: brick_size = GetMaxBrickSize; get_lod,
+ * get_brick_md, get_brick, get_minmax per minmax_mode, index_*); histograms are
+ * the source's (forwarded, as in the reference) and it is not renderable
+ * (TVK_ERR_UNSUPPORTED).  The source may be destroyed afterwards. */
+tvk_status tvk_volume_rebrick(const tvk_volume* src, const uint32_t brick_size[3], int minmax_mode,
+                              tvk_volume** out);
+
+/* BrickedDataset::GetMaxUsedBrickSizes (IO/BrickedDataset.cpp:139-145): the
+ * largest n_voxels per axis over every brick. */
+tvk_status tvk_volume_get_max_used_brick_size(const tvk_volume* v, uint32_t out[3]);
+
 /* Dataset::GetBrick(key, std::vector<T>&) (IO/Dataset.h:93-100): copies one
  * brick (x fastest, ghost included) to host memory of `bytes` bytes. */
 tvk_status tvk_volume_get_brick(const tvk_volume* v, uint64_t timestep, uint64_t lod,

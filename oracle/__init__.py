@@ -69,6 +69,11 @@ def lib():
         L.orc_histogram2d.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
                                       C.c_uint64, C.c_double, _u64p]
         L.orc_histogram2d.restype = C.c_double
+        L.orc_rebrick.argtypes = [C.c_int, _u64p, _u32p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                  _u64p, C.POINTER(C.c_double), C.POINTER(C.c_double), _u32p,
+                                  C.c_int, C.c_uint64, _u32p, C.POINTER(C.c_float), _u64p,
+                                  C.POINTER(C.c_double), C.c_void_p, C.c_uint64, _u64p, _u64p]
+        L.orc_rebrick.restype = C.c_int64
         L.orc_render.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p]
         L.orc_render.restype = C.c_uint64
         L.orc_round_half.argtypes = [C.c_float]
@@ -314,3 +319,67 @@ class Prepared:
 
     def __del__(self):
         self.close()
+
+
+class RebrickError(ValueError):
+    """The reference's DynamicBrickingDS throws (code -1) or would read outside
+    a source brick (code -2)."""
+
+    def __init__(self, code):
+        super().__init__("not an integer multiple of the source brick size" if code == -1
+                         else "a target brick reads outside its source brick")
+        self.code = code
+
+
+def rebrick(raw, src_bsize, overlap, tgt_bsize, mm_mode=1, clamp=False, median=False,
+            lod0_only=False):
+    """DynamicBrickingDS over the ExtendedOctree of raw: a list of dicts per
+    target brick in TOC order {lod, index, n_voxels, center, extents,
+    src_index, min, max, data [z, y, x]}.  mm_mode 0 = MM_SOURCE, 1 =
+    MM_PRECOMPUTE, 2 = MM_DYNAMIC."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    src = build_octree(raw, src_bsize, overlap, clamp=clamp, median=median)
+    sizes, counts = lod_table(dims, src_bsize, overlap)
+    n_built = 1 if lod0_only else len(sizes)
+    offs = np.zeros(len(src), dtype=np.uint64)
+    o = 0
+    for i, b in enumerate(src):
+        offs[i] = o
+        o += b.size
+    pool = np.concatenate([b.reshape(-1) for b in src])
+    mn = np.array([float(b.min()) for b in src])
+    mx = np.array([float(b.max()) for b in src])
+    need = C.c_uint64()
+    args = [_dt(raw), _u64(dims), _u32(src_bsize), overlap, n_built,
+            pool.ctypes.data_as(C.c_void_p), offs.ctypes.data_as(_u64p),
+            mn.ctypes.data_as(C.POINTER(C.c_double)), mx.ctypes.data_as(C.POINTER(C.c_double)),
+            _u32(tgt_bsize), mm_mode]
+    n = lib().orc_rebrick(*args, 0, None, None, None, None, None, 0, None, C.byref(need))
+    if n < 0:
+        raise RebrickError(int(n))
+    info = np.zeros((n, 4), dtype=np.uint32)
+    geom = np.zeros((n, 6), dtype=np.float32)
+    sidx = np.zeros(n, dtype=np.uint64)
+    mm = np.zeros((n, 2), dtype=np.float64)
+    out = np.zeros(int(need.value), dtype=raw.dtype)
+    ooff = np.zeros(n, dtype=np.uint64)
+    n2 = lib().orc_rebrick(*args, n, info.ctypes.data_as(_u32p),
+                           geom.ctypes.data_as(C.POINTER(C.c_float)), sidx.ctypes.data_as(_u64p),
+                           mm.ctypes.data_as(C.POINTER(C.c_double)),
+                           out.ctypes.data_as(C.c_void_p), out.size, ooff.ctypes.data_as(_u64p),
+                           C.byref(need))
+    assert n2 == n
+    res = []
+    per_lod = {}
+    for t in range(n):
+        lod = int(info[t, 0])
+        nx, ny, nz = (int(v) for v in info[t, 1:])
+        k = per_lod.get(lod, 0)
+        per_lod[lod] = k + 1
+        o = int(ooff[t])
+        res.append({"lod": lod, "index": k, "n_voxels": (nx, ny, nz),
+                    "center": tuple(geom[t, :3]), "extents": tuple(geom[t, 3:]),
+                    "src_index": int(sidx[t]), "min": mm[t, 0], "max": mm[t, 1],
+                    "data": out[o:o + nx * ny * nz].reshape(nz, ny, nx)})
+    return res

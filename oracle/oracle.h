@@ -95,6 +95,25 @@ double orc_histogram2d(const void* raw, int dtype, const uint64_t dims[3],
                        const uint32_t brick_size[3], uint32_t overlap, int clamp_to_edge,
                        uint64_t value_bins, double max_nonzero, uint64_t* hist);
 
+/* ---- DynamicBrickingDS (IO/DynamicBrickingDS.cpp) ---- */
+
+/* Re-cuts a bricked source (pool + TOC offsets as orc_build_octree writes them,
+ * n_built_lods LODs present, per-brick min/max) into bricks of tgt_brick voxels
+ * (ghost included).  Per target brick t in TOC order: info[4t..] = lod,
+ * n_voxels x/y/z; geom[6t..] = centre xyz, extents xyz; src_index[t] = source
+ * TOC index; minmax[2t..] = MaxMinForKey for mm_mode (0 MM_SOURCE, 1
+ * MM_PRECOMPUTE, 2 MM_DYNAMIC); voxels at out_pool + out_offsets[t].  Only
+ * bricks that fit max_out / pool_cap are written.  Returns the target brick
+ * count (*pool_needed = voxels of all of them), -1 where the reference throws
+ * (not an integer multiple), -2 where its copy would read outside a source
+ * brick. */
+int64_t orc_rebrick(int dtype, const uint64_t dims[3], const uint32_t src_brick[3],
+                    uint32_t overlap, uint32_t n_built_lods, const void* src_pool,
+                    const uint64_t* src_offsets, const double* src_min, const double* src_max,
+                    const uint32_t tgt_brick[3], int mm_mode, uint64_t max_out, uint32_t* info,
+                    float* geom, uint64_t* src_index, double* minmax, void* out_pool,
+                    uint64_t pool_cap, uint64_t* out_offsets, uint64_t* pool_needed);
+
 /* ---- Ray march (Shaders/GLRaycaster-*.glsl) ---- */
 
 enum { ORC_RM_1D = 0, ORC_RM_2D = 1, ORC_RM_ISO = 2 };

@@ -15,6 +15,7 @@ TVK_OK = 0
 TVK_U8, TVK_U16 = 0, 1
 TVK_RM_1DTRANS, TVK_RM_2DTRANS, TVK_RM_ISOSURFACE = 0, 1, 2
 TVK_LIGHT_REFERENCE, TVK_LIGHT_BLINN_PHONG = 0, 1
+TVK_MM_SOURCE, TVK_MM_PRECOMPUTE, TVK_MM_DYNAMIC = 0, 1, 2
 
 STATUS_NAMES = {0: "TVK_OK", 1: "TVK_ERR_INVALID_ARG", 2: "TVK_ERR_CUDA",
                 3: "TVK_ERR_OUT_OF_MEMORY", 4: "TVK_ERR_UNSUPPORTED", 5: "TVK_ERR_STATE",
@@ -74,6 +75,8 @@ PROTOTYPES = {
     "tvk_volume_get_histogram": [_vp, _u64p, C.c_size_t, _u64p],
     "tvk_volume_get_histogram2d": [_vp, _u64p, C.c_size_t, C.c_size_t, _u64p, _f32p],
     "tvk_volume_get_brick_histograms": [_vp, _u32p, C.c_size_t, _u32p],
+    "tvk_volume_rebrick": [_vp, _u32p, C.c_int, C.POINTER(_vp)],
+    "tvk_volume_get_max_used_brick_size": [_vp, _u32p],
     "tvk_volume_index_from_4d": [_vp, _u64p, _u64p],
     "tvk_volume_index_to_4d": [_vp, C.c_uint64, C.c_uint64, _u64p],
     "tvk_renderer_create": [C.POINTER(_vp)],

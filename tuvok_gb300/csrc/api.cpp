@@ -993,6 +993,9 @@ tvk_status tvk_volume_get_histogram2d(const tvk_volume* v, uint64_t* host_out, s
                                       float* max_gradient) {
   return guarded([&] {
     REQUIRE(v && host_out, "null argument");
+    if (v->rebricked)
+      tvk::fail(TVK_ERR_UNSUPPORTED,
+                "a rebricked volume forwards its histograms to the source volume; query that");
     const uint64_t bins = value_bins ? value_bins : v->hist_trimmed;
     REQUIRE(bins >= 1 && bins <= 65536, "value_bins must be 1 .. 65536");
     REQUIRE(entries >= bins * 256, "output holds fewer than value_bins * 256 entries");
@@ -1010,9 +1013,30 @@ tvk_status tvk_volume_get_brick_histograms(const tvk_volume* v, uint32_t* host_o
                                            size_t n_bricks, uint32_t* shift) {
   return guarded([&] {
     REQUIRE(v && host_out, "null argument");
+    if (v->rebricked)
+      tvk::fail(TVK_ERR_UNSUPPORTED, "per-brick histograms exist for bricked source volumes only");
     REQUIRE(n_bricks >= v->n_bricks, "output holds fewer bricks than the volume");
     std::memcpy(host_out, v->bhist.data(), v->bhist.size() * sizeof(uint32_t));
     if (shift) *shift = v->hist_shift;
+  });
+}
+
+tvk_status tvk_volume_rebrick(const tvk_volume* src, const uint32_t brick_size[3], int minmax_mode,
+                              tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(src && brick_size && out, "null argument");
+    *out = nullptr;
+    *out = tvk::rebrick_volume(src, brick_size, minmax_mode);
+  });
+}
+
+tvk_status tvk_volume_get_max_used_brick_size(const tvk_volume* v, uint32_t out[3]) {
+  return guarded([&] {
+    REQUIRE(v && out, "null argument");
+    // BrickedDataset::GetMaxUsedBrickSizes (IO/BrickedDataset.cpp:139-145)
+    out[0] = out[1] = out[2] = 0;
+    for (uint64_t k = 0; k < v->total_bricks; ++k)
+      for (int a = 0; a < 3; ++a) out[a] = std::max(out[a], v->md[k].n_voxels[a]);
   });
 }
 
@@ -1070,6 +1094,8 @@ tvk_status tvk_renderer_destroy(tvk_renderer* r) {
 tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
   return guarded([&] {
     REQUIRE(r, "null renderer");
+    if (v && v->rebricked)
+      tvk::fail(TVK_ERR_UNSUPPORTED, "rendering runs on bricked source volumes, not rebricked ones");
     r->vol = v;
     r->empty_valid = false;
     // AbstrRenderer.cpp:252-259: the isovalue starts at half the data range

@@ -63,6 +63,18 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
                          const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
                          uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
                          uint64_t* launches);
+// ExtendedOctree tables and UVF metadata (api.cpp)
+std::vector<LodInfo> lod_table(const uint64_t dims[3], const uint32_t B[3], uint32_t ov);
+void brick_size(const LodInfo& l, const uint32_t B[3], uint32_t ov, const uint64_t c[3],
+                uint32_t out[3]);
+void brick_metadata(const LodInfo& l, const uint32_t B[3], uint32_t ov,
+                    std::vector<tvk_brick_md>& md);
+
+// DynamicBrickingDS (rebrick.cu): a new volume whose bricks are windows of the
+// source's bricks, gathered on the GPU.  mm_mode: 0 MM_SOURCE, 1 MM_PRECOMPUTE,
+// 2 MM_DYNAMIC.
+tvk_volume* rebrick_volume(const tvk_volume* src, const uint32_t brick_size[3], int mm_mode);
+
 // value x |gradient| histogram of the LOD-0 inner voxels (Histogram2DDataBlock)
 struct Hist2DParams {
   uint32_t ov, z_chunk;
@@ -211,6 +223,10 @@ struct tvk_volume {
   uint64_t total_cells = 0;
   void* d_cells = nullptr;              // uint32 per cell
   void* d_cell_meta = nullptr;          // cell offsets (u64) + counts (u32) per brick
+  // DynamicBrickingDS volumes: bricks cut from a source volume's bricks
+  bool rebricked = false;
+  int mm_mode = 0;
+  std::vector<uint64_t> src_index;      // source TOC index per brick
 };
 
 struct tvk_renderer;

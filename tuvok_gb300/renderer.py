@@ -35,9 +35,15 @@ class Volume:
     """
 
     CLAMP_TO_EDGE, DEVICE_INPUT, MEDIAN, LOD0_ONLY = 1, 2, 4, 8
+    MM_SOURCE, MM_PRECOMPUTE, MM_DYNAMIC = N.TVK_MM_SOURCE, N.TVK_MM_PRECOMPUTE, N.TVK_MM_DYNAMIC
 
     def __init__(self, data, brick_size=(64, 64, 64), overlap=1, clamp_to_edge=False,
-                 dims=None, dtype=None, median=False, lod0_only=False):
+                 dims=None, dtype=None, median=False, lod0_only=False, _handle=None):
+        if _handle is not None:
+            self._h = _handle
+            self.info = N.VolumeInfo()
+            check(lib().tvk_volume_get_info(self._h, C.byref(self.info)))
+            return
         h = C.c_void_p()
         bs = _u32(brick_size)
         flags = ((self.CLAMP_TO_EDGE if clamp_to_edge else 0) | (self.MEDIAN if median else 0) |
@@ -154,6 +160,21 @@ class Volume:
         check(lib().tvk_volume_get_brick_histograms(self._h, out.ctypes.data_as(N._u32p), n,
                                                     C.byref(sh)))
         return out, int(sh.value)
+
+    def Rebrick(self, brick_size, mm_mode=MM_PRECOMPUTE):
+        """DynamicBrickingDS(self, brick_size, mm_mode): a new Volume of smaller
+        bricks (ghost included in brick_size) cut from this one's."""
+        h = C.c_void_p()
+        check(lib().tvk_volume_rebrick(self._h, _u32(brick_size), int(mm_mode), C.byref(h)))
+        return Volume(None, _handle=h)
+
+    def GetMaxBrickSize(self):
+        return tuple(self.info.brick_size)
+
+    def GetMaxUsedBrickSizes(self):
+        out = _u32((0, 0, 0))
+        check(lib().tvk_volume_get_max_used_brick_size(self._h, out))
+        return tuple(out)
 
     def IndexFrom4D(self, x, y, z, lod):
         out = C.c_uint64()
