@@ -41,7 +41,7 @@ def test_rebricking_h_ramp():
 
 
 def test_lod_tables_of_the_configs():
-    # 256^3 at brick 66/overlap 1 -> 9 LODs, 79 bricks;
+    # ExtendedOctree::ComputeMetadata: 256^3 at brick 66/overlap 1 -> 9 LODs, 79 bricks;
     # 1024^3 at brick 130/overlap 1 -> 11 LODs, 592 bricks
     s, c = O.lod_table((256, 256, 256), (66, 66, 66), 1)
     assert len(s) == 9 and sum(a * b * d for a, b, d in c) == 79
