@@ -282,10 +282,70 @@ tvk_status tvk_resize(tvk_renderer* r, uint32_t width, uint32_t height);
  * every brick). */
 tvk_status tvk_set_frame_termination(tvk_renderer* r, float threshold);
 
-/* AbstrRenderer::Paint (AbstrRenderer.h:433) for the full-quality capture
- * path: plans the LOD-0 brick list (AbstrRenderer.cpp:999-1100), then ray
- * marches every pixel on the renderer's stream.  Asynchronous. */
+/* AbstrRenderer::Paint (AbstrRenderer.h:433) for one fixed-quality frame:
+ * plans the brick list of the current LOD (AbstrRenderer.cpp:999-1100, LOD 0
+ * unless tvk_set_lod chose another), then ray marches every pixel on the
+ * renderer's stream.  Asynchronous. */
 tvk_status tvk_paint(tvk_renderer* r);
+
+/* m_iCurrentLOD for tvk_paint: the bricks of this LOD are rendered, with
+ * fStepScale = (1/srm) * max(domain(0) / domain(lod)) and the LOD's brick
+ * aspect in the texture coordinates (GLRaycaster.cpp:253-257,
+ * uvfDataset.cpp:1747-1774).  TVK_ERR_UNSUPPORTED at paint time for LODs the
+ * volume was not built with. */
+tvk_status tvk_set_lod(tvk_renderer* r, uint32_t lod);
+
+/* decreaseScreenResNow / decreaseSamplingRateNow for tvk_paint: render at
+ * 1/screen_res_dec_factor of the viewport (GLRenderer::SetViewPort,
+ * GLRenderer.cpp:864-889) and stretch the result over the viewport with
+ * bilinear filtering (CopyOverCompletedRegion, :717-747), and/or divide the
+ * sample rate by sample_dec_factor (GLRaycaster.cpp:253-254). */
+tvk_status tvk_set_reduced_quality(tvk_renderer* r, int decrease_screen_res,
+                                   int decrease_sampling_rate);
+
+/* AbstrRenderer::SetPerfMeasures (AbstrRenderer.cpp:1435-1454): target frame
+ * rate (0 = none, 10 s per frame), whether reduced-quality intermediate
+ * subframes are allowed, and the two decrease factors (default 2, 2). */
+tvk_status tvk_set_perf_measures(tvk_renderer* r, uint32_t min_framerate,
+                                 int low_res_intermediate, float screen_res_dec_factor,
+                                 float sample_dec_factor);
+
+/* AbstrRenderer::SetLODLimits (AbstrRenderer.cpp:1456-1459): coarsest_skip
+ * LODs are never used as the start LOD; finest is the finest LOD used. */
+tvk_status tvk_set_lod_limits(tvk_renderer* r, uint32_t coarsest_skip, uint32_t finest);
+
+/* m_eRendererTarget == RT_CAPTURE: progressive frames render LOD 0 only. */
+tvk_status tvk_set_capture_mode(tvk_renderer* r, int capture);
+
+/* AbstrRenderer::ComputeMinLODForCurrentView (AbstrRenderer.cpp:789-803) with
+ * CullingLOD::GetLODLevel (CullingLOD.cpp:126-138): the finest LOD the
+ * current view needs (screen-space error of one pixel). */
+tvk_status tvk_compute_min_lod(tvk_renderer* r, uint32_t* lod);
+
+typedef struct tvk_subframe_info {
+  uint32_t lod;                  /* LOD the subframe rendered */
+  int decreased_screen_res;      /* 1: rendered at reduced resolution, upscaled */
+  int decreased_sampling_rate;   /* 1: rendered at the reduced sample rate */
+  uint32_t render_width, render_height;
+  uint32_t min_lod, start_lod;   /* the frame's plan */
+  float ms;                      /* GPU time of the subframe */
+  int frame_complete;            /* 1: nothing finer is left for this view */
+} tvk_subframe_info;
+
+/* One subframe of Tuvok's progressive frame: AbstrRenderer::PlanFrame
+ * (AbstrRenderer.cpp:1125-1212) picks the LOD and quality, the subframe is
+ * rendered and timed (blocking), and CompletedASubframe (:651-670) records the
+ * time that ComputeMaxLODForCurrentView (:681-787) uses to choose the next
+ * frame's start LOD and whether to decrease resolution or sample rate.
+ * new_frame = 1 starts a frame for the current view (the reference's blank
+ * region).  The sequence is: start LOD (at reduced quality when the planner
+ * asks for it), the same LOD at full quality, then one LOD finer per call down
+ * to the view's minimum LOD; after that info->frame_complete = 1 and calls
+ * render nothing until the next new frame. */
+tvk_status tvk_paint_progressive(tvk_renderer* r, int new_frame, tvk_subframe_info* info);
+
+/* Size of the last ray-marched image (the viewport, or the reduced one). */
+tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* height);
 
 /* GLRenderer::GetLastFBO + GLFBOTex::ReadBackPixels (GLRenderer.h:105,
  * GLFBOTex.cpp:401): device pointer of the last frame and a blocking copy to
@@ -293,7 +353,8 @@ tvk_status tvk_paint(tvk_renderer* r);
 tvk_status tvk_get_image_device(tvk_renderer* r, const float** device_rgba, uint32_t* width,
                                 uint32_t* height);
 tvk_status tvk_read_image(tvk_renderer* r, float* host_rgba, size_t n_floats);
-/* Per-pixel executed sample counts of the last paint (u32 per pixel). */
+/* Per-pixel executed sample counts of the last paint (u32 per pixel of the
+ * ray-marched image, tvk_get_render_size). */
 tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t n);
 
 /* The renderer's CUDA stream (cudaStream_t) for callers that order their own

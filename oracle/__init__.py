@@ -33,6 +33,9 @@ class Scene(C.Structure):
         ("znear", C.c_float), ("zfar", C.c_float), ("width", C.c_uint32),
         ("height", C.c_uint32), ("use_double", C.c_int), ("row_stride", C.c_uint32),
         ("row_phase", C.c_uint32), ("threads", C.c_int), ("iso_color", C.c_float * 3),
+        ("lod", C.c_uint32), ("median", C.c_int), ("decrease_screen_res", C.c_int),
+        ("decrease_sampling_rate", C.c_int), ("screen_res_dec_factor", C.c_float),
+        ("sample_dec_factor", C.c_float),
     ]
 
 
@@ -74,6 +77,10 @@ def lib():
                                   C.c_int, C.c_uint64, _u32p, C.POINTER(C.c_float), _u64p,
                                   C.POINTER(C.c_double), C.c_void_p, C.c_uint64, _u64p, _u64p]
         L.orc_rebrick.restype = C.c_int64
+        L.orc_render_size.argtypes = [C.POINTER(Scene), _u32p, _u32p]
+        L.orc_render_size.restype = None
+        L.orc_lod_aspect.argtypes = [_u64p, C.c_uint32, C.POINTER(C.c_double)]
+        L.orc_lod_aspect.restype = None
         L.orc_render.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p]
         L.orc_render.restype = C.c_uint64
         L.orc_round_half.argtypes = [C.c_float]
@@ -230,7 +237,8 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
                ambient=(1, 1, 1, 0.1), diffuse=(1, 1, 1, 1), specular=(1, 1, 1, 1),
                light_dir=(0, 0, -1), bp=(0.2, 0.6, 0.2, 32.0), frame_ert=1.0,
                use_double=False, row_stride=1, row_phase=0, threads=0, isovalue=None,
-               iso_color=(0.5, 0.5, 0.5)):
+               iso_color=(0.5, 0.5, 0.5), lod=0, median=False, dec_screen=False,
+               dec_sampling=False, screen_dec=2.0, sample_dec=2.0):
     """Scene struct for the oracle; returns (scene, arrays that must stay alive)."""
     raw = np.ascontiguousarray(raw)
     tf = np.ascontiguousarray(np.asarray(tf, dtype=np.float32))
@@ -265,6 +273,9 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
     s.width, s.height = width, height
     s.use_double = int(use_double)
     s.row_stride, s.row_phase = row_stride, row_phase
+    s.lod, s.median = lod, int(median)
+    s.decrease_screen_res, s.decrease_sampling_rate = int(dec_screen), int(dec_sampling)
+    s.screen_res_dec_factor, s.sample_dec_factor = screen_dec, sample_dec
     s.threads = threads
     if isovalue is None:
         # AbstrRenderer.cpp:252-259: half the data range once a dataset is loaded
@@ -278,7 +289,9 @@ def render(raw, bsize, overlap, tf, *, width, height, want_counts=False, **kw):
     """Oracle render of raw ([z, y, x]) -> (image [h, w, 4], samples, counts|None)."""
     s, keep = make_scene(raw, bsize, overlap, tf, width=width, height=height, **kw)
     img = np.zeros((height, width, 4), dtype=np.float32)
-    counts = np.zeros((height, width), dtype=np.uint32) if want_counts else None
+    rw, rh = C.c_uint32(), C.c_uint32()
+    lib().orc_render_size(C.byref(s), C.byref(rw), C.byref(rh))
+    counts = np.zeros((rh.value, rw.value), dtype=np.uint32) if want_counts else None
     n = lib().orc_render(C.byref(s), img.ctypes.data_as(C.POINTER(C.c_float)),
                          counts.ctypes.data_as(_u32p) if want_counts else None)
     del keep

@@ -48,6 +48,26 @@ extern "C" int orc_lod_table(const uint64_t dims[3], const uint32_t brick_size[3
   return n;
 }
 
+extern "C" void orc_lod_aspect(const uint64_t dims[3], uint32_t lod, double out[3]) {
+  // ExtendedOctree::ComputeMetadata (ExtendedOctree.cpp:188-243): an axis that
+  // halves from an odd size gains size / ceil(size / 2) (in float), an even one
+  // 2; the result is normalised by its largest component every level.
+  uint64_t v[3] = {dims[0], dims[1], dims[2]};
+  double asp[3] = {1, 1, 1};
+  for (uint32_t l = 1; l <= lod; ++l) {
+    for (int a = 0; a < 3; ++a) {
+      if (v[a] > 1) {
+        const uint64_t h = (v[a] + 1) / 2;
+        asp[a] *= (v[a] % 2) ? double(float(v[a]) / float(h)) : 2.0;
+        v[a] = h;
+      }
+    }
+    const double m = std::max(asp[0], std::max(asp[1], asp[2]));
+    for (int a = 0; a < 3; ++a) asp[a] /= m;
+  }
+  for (int a = 0; a < 3; ++a) out[a] = asp[a];
+}
+
 extern "C" void orc_brick_size(const uint64_t lod_size[3], const uint64_t brick_count[3],
                                const uint32_t brick_size[3], uint32_t overlap,
                                const uint64_t coords[3], uint64_t out[3]) {

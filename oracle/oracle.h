@@ -32,6 +32,10 @@ int orc_lod_table(const uint64_t dims[3], const uint32_t brick_size[3],
                   uint32_t overlap, uint64_t* lod_sizes, uint64_t* brick_counts,
                   int max_lods);
 
+/* The aspect of LOD `lod` as ExtendedOctree::ComputeMetadata accumulates it
+ * (ExtendedOctree.cpp:188-243; GetBrickAspect :292-294). */
+void orc_lod_aspect(const uint64_t dims[3], uint32_t lod, double out[3]);
+
 /* ExtendedOctree::ComputeBrickSize (ExtendedOctree.cpp:276-285). */
 void orc_brick_size(const uint64_t lod_size[3], const uint64_t brick_count[3],
                     const uint32_t brick_size[3], uint32_t overlap,
@@ -150,11 +154,21 @@ typedef struct orc_scene {
   uint32_t row_stride, row_phase;
   int threads;              /* OpenMP threads, 0 = default */
   float iso_color[3];       /* AbstrRenderer m_vIsoColor (default 0.5 grey) */
+  /* level of detail and reduced quality (AbstrRenderer m_iCurrentLOD,
+   * decreaseScreenResNow / decreaseSamplingRateNow and their factors) */
+  uint32_t lod;             /* LOD >= 1 bricks come from orc_build_octree */
+  int median;               /* ComputeHierarchy filter of those LODs */
+  int decrease_screen_res, decrease_sampling_rate;
+  float screen_res_dec_factor, sample_dec_factor;
 } orc_scene;
 
 /* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row
  * (gl_FragCoord.y = 0.5).  Returns the number of executed samples; the sample
- * count of each pixel goes to samples_per_pixel when it is not NULL. */
+ * count of each pixel goes to samples_per_pixel when it is not NULL.  With
+ * decrease_screen_res the march runs at the reduced size (the counts are of
+ * that image, orc_render_size) and is stretched bilinearly over the viewport. */
+void orc_render_size(const orc_scene* scene, uint32_t* width, uint32_t* height);
+
 uint64_t orc_render(const orc_scene* scene, float* out_rgba,
                     uint32_t* samples_per_pixel);
 

@@ -519,13 +519,41 @@ Setup build_setup(const orc_scene& s) {
   Setup st;
   st.s = &s;
   const int bytes = s.dtype == 0 ? 1 : 2;
-  uint64_t lod[3 * 64], cnt[3 * 64];
-  orc_lod_table(s.dims, s.brick_size, s.overlap, lod, cnt, 64);
+  uint64_t lod_all[3 * 64], cnt_all[3 * 64];
+  const int n_lods = orc_lod_table(s.dims, s.brick_size, s.overlap, lod_all, cnt_all, 64);
+  // the rendered LOD (AbstrRenderer m_iCurrentLOD); its bricks, metadata and aspect
+  const uint32_t L = std::min<uint32_t>(s.lod, uint32_t(n_lods - 1));
+  const uint64_t* lod = &lod_all[3 * L];
+  const uint64_t* cnt = &cnt_all[3 * L];
   const uint64_t nb = cnt[0] * cnt[1] * cnt[2];
   std::vector<float> ctr(3 * nb), ext(3 * nb);
   std::vector<uint32_t> nv(3 * nb);
-  const double asp[3] = {1, 1, 1};
+  double asp[3];
+  orc_lod_aspect(s.dims, L, asp);
   orc_brick_metadata(lod, cnt, s.brick_size, s.overlap, asp, ctr.data(), ext.data(), nv.data());
+  // LOD >= 1 bricks: the ComputeHierarchy + FillOverlap restatement
+  std::vector<uint8_t> octree;
+  std::vector<uint64_t> octree_off;
+  uint64_t lod_first = 0;
+  if (L > 0) {
+    uint64_t total_vox = 0, total_bricks = 0;
+    for (int l = 0; l < n_lods; ++l) {
+      const uint64_t* ls = &lod_all[3 * l];
+      const uint64_t* lc = &cnt_all[3 * l];
+      if (uint32_t(l) == L) lod_first = total_bricks;
+      for (uint64_t k = 0; k < lc[0] * lc[1] * lc[2]; ++k) {
+        const uint64_t c3[3] = {k % lc[0], (k / lc[0]) % lc[1], k / (lc[0] * lc[1])};
+        uint64_t bs[3];
+        orc_brick_size(ls, lc, s.brick_size, s.overlap, c3, bs);
+        total_vox += bs[0] * bs[1] * bs[2];
+        ++total_bricks;
+      }
+    }
+    octree.resize(total_vox * bytes);
+    octree_off.resize(total_bricks);
+    orc_build_octree(s.raw, s.dtype, s.dims, s.brick_size, s.overlap, s.clamp_to_edge, s.median,
+                     octree.data(), total_vox, octree_off.data(), total_bricks);
+  }
 
   // AbstrRenderer.cpp:1003-1012: scale applied to brick metadata
   const float us[3] = {float(s.user_scale[0]), float(s.user_scale[1]), float(s.user_scale[2])};
@@ -556,8 +584,13 @@ Setup build_setup(const orc_scene& s) {
                                             s.clamp_to_edge));
     st.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
   }
-  const float srm = s.sample_rate_modifier;
-  st.step_scale = 1.0f / srm * 1.0f;  // GLRaycaster.cpp:257 at LOD 0
+  // GLRaycaster.cpp:253-257: sample rate divided while decreasing it; the
+  // opacity-correction exponent grows with the LOD's voxel size
+  const float srm = s.sample_rate_modifier /
+                    (s.decrease_sampling_rate ? s.sample_dec_factor : 1.0f);
+  float dom = 0.0f;
+  for (int a = 0; a < 3; ++a) dom = std::max(dom, float(lod_all[a]) / float(lod[a]));
+  st.step_scale = 1.0f / srm * dom;
 
   // transfer function as the GPU sees it
   const size_t ntf = size_t(s.tf_w) * s.tf_h;
@@ -612,10 +645,11 @@ Setup build_setup(const orc_scene& s) {
           b.pmin[a] = c[a] - e[a] / 2.0f;
           b.pmax[a] = c[a] + e[a] / 2.0f;
         }
-        // UVFDataset::GetTextCoords (uvfDataset.cpp:1766-1767)
+        // UVFDataset::GetTextCoords (uvfDataset.cpp:1747-1774): the upper
+        // corner is scaled by the LOD's brick aspect
         for (int a = 0; a < 3; ++a) {
           b.tmin[a] = float(s.overlap) / float(b.n[a]);
-          b.tmax[a] = 1.0f - b.tmin[a];
+          b.tmax[a] = (1.0f - b.tmin[a]) * float(asp[a]);
         }
         // GLRaycaster.cpp:255: step = min over axes of ext * (1/n) * 0.5 / srm
         float stp = INFINITY;
@@ -625,9 +659,13 @@ Setup build_setup(const orc_scene& s) {
         }
         b.step = stp;
         const uint64_t co[3] = {x, y, z};
-        b.data.resize(size_t(b.n[0]) * b.n[1] * b.n[2] * bytes);
-        orc_lod0_brick(s.raw, s.dtype, s.dims, s.brick_size, s.overlap, s.clamp_to_edge, co,
-                       b.data.data());
+        const size_t nbytes = size_t(b.n[0]) * b.n[1] * b.n[2] * bytes;
+        b.data.resize(nbytes);
+        if (L == 0)
+          orc_lod0_brick(s.raw, s.dtype, s.dims, s.brick_size, s.overlap, s.clamp_to_edge, co,
+                         b.data.data());
+        else
+          std::memcpy(b.data.data(), octree.data() + octree_off[lod_first + k] * bytes, nbytes);
         double mn, mx;
         orc_brick_stats(b.data.data(), s.dtype, uint64_t(b.n[0]) * b.n[1] * b.n[2], &mn, &mx);
         // ContainsData: value range vs TF limits, or the isovalue (uvfDataset.cpp:1201-1215)
@@ -661,7 +699,64 @@ struct Prepared {
   Setup st;
 };
 
+// GLRenderer::SetViewPort (GLRenderer.cpp:864-889): the viewport scaled by
+// 1/m_fScreenResDecFactor, rounded to the nearest pixel.
+void render_size(const orc_scene& s, uint32_t* w, uint32_t* h) {
+  *w = s.width;
+  *h = s.height;
+  if (s.decrease_screen_res) {
+    const float rescale = 1.0f / s.screen_res_dec_factor;
+    *w = std::max(1u, uint32_t(float(s.width) * rescale + 0.5f));
+    *h = std::max(1u, uint32_t(float(s.height) * rescale + 0.5f));
+  }
+}
+
+// GLRenderer::CopyOverCompletedRegion / FullscreenQuadRegion (GLRenderer.cpp:
+// 688-747): viewport pixel x reads texel position (x + 0.5) * rescale - 0.5 of
+// the reduced image with GL_LINEAR, clamped to its edge.
+void upscale(const float* low, uint32_t lw, uint32_t lh, float* out, uint32_t w, uint32_t h,
+             float rescale) {
+  auto lerp = [](float a, float b, float t) { return std::fma(t, b - a, a); };
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const float u = (float(x) + 0.5f) * rescale - 0.5f;
+      const float v = (float(y) + 0.5f) * rescale - 0.5f;
+      const float fu = std::floor(u), fv = std::floor(v);
+      const float wx = u - fu, wy = v - fv;
+      const int x0 = std::min(std::max(int(fu), 0), int(lw) - 1);
+      const int x1 = std::min(std::max(int(fu) + 1, 0), int(lw) - 1);
+      const int y0 = std::min(std::max(int(fv), 0), int(lh) - 1);
+      const int y1 = std::min(std::max(int(fv) + 1, 0), int(lh) - 1);
+      for (int c = 0; c < 4; ++c) {
+        const float* r0 = low + 4 * size_t(y0) * lw;
+        const float* r1 = low + 4 * size_t(y1) * lw;
+        const float a = lerp(r0[4 * x0 + c], r0[4 * x1 + c], wx);
+        const float b = lerp(r1[4 * x0 + c], r1[4 * x1 + c], wx);
+        out[4 * (size_t(y) * w + x) + c] = lerp(a, b, wy);
+      }
+    }
+}
+
+uint64_t march_rows(Setup& st, float* out, uint32_t* spp, double* march_s);
+
 uint64_t march_all(Setup& st, float* out, uint32_t* spp, double* march_s) {
+  uint32_t rw, rh;
+  render_size(*st.s, &rw, &rh);
+  if (rw == st.s->width && rh == st.s->height) return march_rows(st, out, spp, march_s);
+  // reduced viewport: march the smaller image with its own projection, then stretch it
+  const orc_scene* full = st.s;
+  orc_scene low = *full;
+  low.width = rw;
+  low.height = rh;
+  std::vector<float> img(size_t(rw) * rh * 4, 0.0f);
+  st.s = &low;
+  const uint64_t n = march_rows(st, img.data(), spp, march_s);
+  st.s = full;
+  upscale(img.data(), rw, rh, out, full->width, full->height, 1.0f / full->screen_res_dec_factor);
+  return n;
+}
+
+uint64_t march_rows(Setup& st, float* out, uint32_t* spp, double* march_s) {
   const orc_scene& s = *st.s;
 #ifdef _OPENMP
   if (s.threads > 0) omp_set_num_threads(s.threads);
@@ -739,3 +834,7 @@ extern "C" uint64_t orc_render_prepared(void* h, const orc_scene* cam, float* ou
 }
 
 extern "C" void orc_release(void* h) { delete static_cast<Prepared*>(h); }
+
+extern "C" void orc_render_size(const orc_scene* sc, uint32_t* w, uint32_t* h) {
+  render_size(*sc, w, h);
+}

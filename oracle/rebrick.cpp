@@ -59,27 +59,6 @@ float lerp_ref(In value, In imin, In imax, float omin, float omax) {
   return float(omin + (value - imin) * (static_cast<double>(omax - omin) / (imax - imin)));
 }
 
-// ExtendedOctree::ComputeMetadata's per-LOD aspect (ExtendedOctree.cpp:188-243)
-void lod_aspects(const uint64_t dims[3], int n_lods, std::vector<std::array<double, 3>>& out) {
-  uint64_t v[3] = {dims[0], dims[1], dims[2]};
-  std::array<double, 3> asp = {1, 1, 1};
-  out.clear();
-  for (int l = 0; l < n_lods; ++l) {
-    if (l > 0) {
-      for (int a = 0; a < 3; ++a) {
-        if (v[a] > 1) {
-          const uint64_t h = (v[a] + 1) / 2;
-          asp[a] *= (v[a] % 2) ? double(float(v[a]) / float(h)) : 2.0;
-          v[a] = h;
-        }
-      }
-      const double m = std::max(asp[0], std::max(asp[1], asp[2]));
-      for (int a = 0; a < 3; ++a) asp[a] /= m;
-    }
-    out.push_back(asp);
-  }
-}
-
 template <class T>
 int64_t rebrick(const uint64_t dims[3], const uint32_t src_brick[3], uint32_t ov,
                 uint32_t n_built, const T* src_pool, const uint64_t* src_offsets,
@@ -98,8 +77,7 @@ int64_t rebrick(const uint64_t dims[3], const uint32_t src_brick[3], uint32_t ov
   uint64_t lsz[3 * 64], lcnt[3 * 64];
   const int n_lods = orc_lod_table(dims, src_brick, ov, lsz, lcnt, 64);
   const int lods = std::min<int>(n_lods, int(n_built));
-  std::vector<std::array<double, 3>> asp;
-  lod_aspects(dims, n_lods, asp);
+  double asp_single[3];
   // source TOC index of each LOD's first brick
   std::vector<uint64_t> src_first(n_lods + 1, 0);
   for (int l = 0; l < n_lods; ++l)
@@ -113,8 +91,8 @@ int64_t rebrick(const uint64_t dims[3], const uint32_t src_brick[3], uint32_t ov
   {
     float c[3], e[3];
     uint32_t n[3];
-    orc_brick_metadata(&lsz[3 * single], &lcnt[3 * single], src_brick, ov, asp[single].data(),
-                       c, e, n);
+    orc_lod_aspect(dims, uint32_t(single), asp_single);
+    orc_brick_metadata(&lsz[3 * single], &lcnt[3 * single], src_brick, ov, asp_single, c, e, n);
     for (int a = 0; a < 3; ++a) ext_full[a] = e[a];
   }
   const float elow[3] = {-(ext_full[0] / 2.0f), -(ext_full[1] / 2.0f), -(ext_full[2] / 2.0f)};

@@ -46,6 +46,13 @@ class VolumeInfo(C.Structure):
                 ("max_gradient", C.c_double), ("device_bytes", C.c_uint64)]
 
 
+class SubframeInfo(C.Structure):
+    _fields_ = [("lod", C.c_uint32), ("decreased_screen_res", C.c_int),
+                ("decreased_sampling_rate", C.c_int), ("render_width", C.c_uint32),
+                ("render_height", C.c_uint32), ("min_lod", C.c_uint32), ("start_lod", C.c_uint32),
+                ("ms", C.c_float), ("frame_complete", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
                 ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
@@ -97,6 +104,14 @@ PROTOTYPES = {
     "tvk_resize": [_vp, C.c_uint32, C.c_uint32],
     "tvk_set_frame_termination": [_vp, C.c_float],
     "tvk_paint": [_vp],
+    "tvk_set_lod": [_vp, C.c_uint32],
+    "tvk_set_reduced_quality": [_vp, C.c_int, C.c_int],
+    "tvk_set_perf_measures": [_vp, C.c_uint32, C.c_int, C.c_float, C.c_float],
+    "tvk_set_lod_limits": [_vp, C.c_uint32, C.c_uint32],
+    "tvk_set_capture_mode": [_vp, C.c_int],
+    "tvk_compute_min_lod": [_vp, _u32p],
+    "tvk_paint_progressive": [_vp, C.c_int, C.POINTER(SubframeInfo)],
+    "tvk_get_render_size": [_vp, _u32p, _u32p],
     "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
     "tvk_read_image": [_vp, _f32p, C.c_size_t],
     "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],

@@ -267,33 +267,7 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   // pass 3: maximum gradient magnitude over inner voxels
   launch_max_gradient(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                       V->n_bricks, V->overlap, max_bz, sc.max_grad_bits, s, &launches);
-  // pass 4: macro-cell min/max for empty-space skipping inside bricks
-  V->cell_offsets.resize(V->n_bricks);
-  V->cell_counts.resize(V->n_bricks);
-  V->cell_dims.resize(V->n_bricks);
-  uint32_t max_cells = 0;
-  V->total_cells = 0;
-  for (uint64_t k = 0; k < V->n_bricks; ++k) {
-    const uint32_t cx = cells_per_axis(V->sizes[3 * k]), cy = cells_per_axis(V->sizes[3 * k + 1]),
-                   cz = cells_per_axis(V->sizes[3 * k + 2]);
-    V->cell_dims[k] = cx | (cy << 10) | (cz << 20);
-    V->cell_counts[k] = cx * cy * cz;
-    V->cell_offsets[k] = V->total_cells;
-    V->total_cells += V->cell_counts[k];
-    max_cells = std::max(max_cells, V->cell_counts[k]);
-  }
-  TVK_CUDA(cudaMalloc(&V->d_cells, V->total_cells * sizeof(uint32_t)));
-  TVK_CUDA(cudaMalloc(&V->d_cell_meta, V->n_bricks * (sizeof(uint64_t) + sizeof(uint32_t))));
-  uint64_t* d_cell_off = static_cast<uint64_t*>(V->d_cell_meta);
-  uint32_t* d_cell_cnt = reinterpret_cast<uint32_t*>(d_cell_off + V->n_bricks);
-  TVK_CUDA(cudaMemcpyAsync(d_cell_off, V->cell_offsets.data(), V->n_bricks * sizeof(uint64_t),
-                           cudaMemcpyHostToDevice, s));
-  TVK_CUDA(cudaMemcpyAsync(d_cell_cnt, V->cell_counts.data(), V->n_bricks * sizeof(uint32_t),
-                           cudaMemcpyHostToDevice, s));
-  launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
-                     d_cell_off, V->n_bricks, max_cells, static_cast<uint32_t*>(V->d_cells), s,
-                     &launches);
-  // pass 5: the coarser LODs (ComputeHierarchy + FillOverlap) and their min/max
+  // pass 4: the coarser LODs (ComputeHierarchy + FillOverlap) and their min/max
   DevBuf d_lmm, d_wave;
   std::vector<uint32_t> lmin, lmax;
   if (V->total_bricks > V->n_bricks) {
@@ -313,6 +287,34 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     TVK_CUDA(cudaMemcpyAsync(lmax.data(), d_lmm.as<uint32_t>() + V->total_bricks,
                              V->total_bricks * 4, cudaMemcpyDeviceToHost, s));
   }
+  // pass 5: macro-cell min/max for empty-space skipping inside the bricks of
+  // every built LOD (after the coarser LODs exist)
+  const uint64_t nb_all = V->total_bricks;
+  V->cell_offsets.resize(nb_all);
+  V->cell_counts.resize(nb_all);
+  V->cell_dims.resize(nb_all);
+  uint32_t max_cells = 0;
+  V->total_cells = 0;
+  for (uint64_t k = 0; k < nb_all; ++k) {
+    const uint32_t cx = cells_per_axis(V->sizes[3 * k]), cy = cells_per_axis(V->sizes[3 * k + 1]),
+                   cz = cells_per_axis(V->sizes[3 * k + 2]);
+    V->cell_dims[k] = cx | (cy << 10) | (cz << 20);
+    V->cell_counts[k] = cx * cy * cz;
+    V->cell_offsets[k] = V->total_cells;
+    V->total_cells += V->cell_counts[k];
+    max_cells = std::max(max_cells, V->cell_counts[k]);
+  }
+  TVK_CUDA(cudaMalloc(&V->d_cells, V->total_cells * sizeof(uint32_t)));
+  TVK_CUDA(cudaMalloc(&V->d_cell_meta, nb_all * (sizeof(uint64_t) + sizeof(uint32_t))));
+  uint64_t* d_cell_off = static_cast<uint64_t*>(V->d_cell_meta);
+  uint32_t* d_cell_cnt = reinterpret_cast<uint32_t*>(d_cell_off + nb_all);
+  TVK_CUDA(cudaMemcpyAsync(d_cell_off, V->cell_offsets.data(), nb_all * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_cell_cnt, V->cell_counts.data(), nb_all * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, s));
+  launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                     d_cell_off, nb_all, max_cells, static_cast<uint32_t*>(V->d_cells), s,
+                     &launches);
 
   std::vector<uint32_t> bmin(V->n_bricks), bmax(V->n_bricks);
   V->hist.resize(gbins);
@@ -556,6 +558,29 @@ struct tvk_renderer {
   tvk_stats stats{};
   uint64_t launches = 0;
   bool painted = false;
+  // level of detail and reduced-quality rendering (AbstrRenderer m_iCurrentLOD,
+  // decreaseScreenResNow / decreaseSamplingRateNow, SetPerfMeasures factors)
+  uint32_t lod = 0;
+  bool dec_screen = false, dec_sampling = false;
+  float screen_dec = 2.0f, sample_dec = 2.0f;
+  uint32_t render_w = 0, render_h = 0;  // size of the last ray-marched image
+  tvk::DevBuf d_lowimg;
+  // progressive frames (AbstrRenderer::PlanFrame, ComputeMin/MaxLODForCurrentView,
+  // CompletedASubframe); names follow the reference's members
+  float max_ms_per_frame = 10000.0f;    // SetPerfMeasures, 0 fps -> 10 s
+  bool low_res_intermediate = false;    // m_bRenderLowResIntermediateResults
+  uint32_t lod_limits[2] = {0, 0};      // m_iLODLimits
+  bool capture = false;                 // m_eRendererTarget == RT_CAPTURE
+  bool decrease_screen_res = false, decrease_sampling_rate = false;
+  bool decrease_screen_res_now = false, decrease_sampling_rate_now = false;
+  bool another_redraw_low_res = false;  // doAnotherRedrawDueToLowResOutput
+  float msec_passed[2] = {-1.0f, -1.0f};
+  float msec_current_frame = -1.0f;
+  uint32_t lod_not_ok = 0;
+  uint64_t perf_lod_skip = 0;
+  uint64_t max_lod_index = 0, min_lod_view = 0, start_lod_offset = 0, current_lod_offset = 0;
+  uint64_t current_lod = 0;
+  bool frame_started = false;
 };
 
 namespace tvk {
@@ -595,31 +620,33 @@ void upload_tf(tvk_renderer* R, float step_scale) {
   R->empty_valid = false;
 }
 
-// Empty-cell bits of every LOD-0 brick for the current TF (re-run when the TF,
-// the sample rate or the volume changes).
+// Empty-cell bits of every brick of every built LOD for the current TF (re-run
+// when the TF, the opacity correction or the volume changes).
 void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale, bool iso_mode,
                         float iso_norm) {
   if (R->empty_valid && R->empty_iso == iso_mode && (!iso_mode || R->empty_iso_norm == iso_norm))
     return;
-  R->empty_word_off.resize(V->n_bricks);
+  // every built LOD's bricks, indexed by TOC position
+  const uint64_t nb = V->total_bricks;
+  R->empty_word_off.resize(nb);
   uint64_t words = 0;
   uint32_t max_words = 0;
-  for (uint64_t k = 0; k < V->n_bricks; ++k) {
+  for (uint64_t k = 0; k < nb; ++k) {
     R->empty_word_off[k] = words;
     const uint32_t w = (V->cell_counts[k] + 31) / 32;
     words += w;
     max_words = std::max(max_words, w);
   }
   R->d_empty.ensure(std::max<uint64_t>(1, words) * sizeof(uint32_t));
-  R->d_empty_meta.ensure(V->n_bricks * sizeof(uint64_t));
-  TVK_CUDA(cudaMemcpyAsync(R->d_empty_meta.p, R->empty_word_off.data(),
-                           V->n_bricks * sizeof(uint64_t), cudaMemcpyHostToDevice, R->stream));
+  R->d_empty_meta.ensure(nb * sizeof(uint64_t));
+  TVK_CUDA(cudaMemcpyAsync(R->d_empty_meta.p, R->empty_word_off.data(), nb * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, R->stream));
   EmptyCellParams p;
   p.cell_minmax = static_cast<const uint32_t*>(V->d_cells);
   p.cell_offsets = static_cast<const uint64_t*>(V->d_cell_meta);
-  p.cell_counts = reinterpret_cast<const uint32_t*>(p.cell_offsets + V->n_bricks);
+  p.cell_counts = reinterpret_cast<const uint32_t*>(p.cell_offsets + nb);
   p.word_offsets = R->d_empty_meta.as<uint64_t>();
-  p.n_bricks = V->n_bricks;
+  p.n_bricks = nb;
   p.nz_prefix = R->d_tfpfx.as<uint32_t>();
   p.tf_w = R->tf_w;
   p.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
@@ -650,7 +677,13 @@ void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgb
   R->tf_dirty = true;
 }
 
-void paint(tvk_renderer* R) {
+// What one (sub)frame renders: the LOD and the two reduced-quality switches.
+struct Subframe {
+  uint32_t lod;
+  bool dec_screen, dec_sampling;
+};
+
+void paint(tvk_renderer* R, const Subframe& sf) {
   const tvk_volume* V = R->vol;
   if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
   const bool iso_mode = R->mode == TVK_RM_ISOSURFACE;
@@ -658,12 +691,28 @@ void paint(tvk_renderer* R) {
   if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
   if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
   if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
+  const uint32_t L = sf.lod;
+  if (L >= V->lods.size()) fail(TVK_ERR_INVALID_ARG, "LOD out of range");
+  if (L + 1 >= V->lod_first.size())
+    fail(TVK_ERR_UNSUPPORTED, "the volume was created with LOD 0 only");
   TVK_CUDA(cudaSetDevice(R->device));
   const uint64_t launches0 = R->launches;
 
-  // GLRaycaster.cpp:253-257: fStepScale at LOD 0
-  const float srm = R->srm;
-  const float step_scale = 1.0f / srm * 1.0f;
+  // GLRaycaster.cpp:253-257: the sample rate divided by m_fSampleDecFactor while
+  // decreasing the sampling rate; fStepScale grows with the LOD's voxel size
+  const float srm = R->srm / (sf.dec_sampling ? R->sample_dec : 1.0f);
+  float dom = 0.0f;
+  for (int a = 0; a < 3; ++a)
+    dom = std::max(dom, float(V->lods[0].size[a]) / float(V->lods[L].size[a]));
+  const float step_scale = 1.0f / srm * dom;
+  // GLRenderer.cpp:864-889 SetViewPort: 1/m_fScreenResDecFactor of the viewport,
+  // rounded to the nearest pixel
+  uint32_t rw = R->width, rh = R->height;
+  if (sf.dec_screen) {
+    const float rescale = 1.0f / R->screen_dec;
+    rw = std::max(1u, uint32_t(float(R->width) * rescale + 0.5f));
+    rh = std::max(1u, uint32_t(float(R->height) * rescale + 0.5f));
+  }
   if (!R->tf.empty()) upload_tf(R, step_scale);
   // GLRenderer.cpp:1813-1819 CalculateScaling
   const uint32_t imax = (1u << (8 * V->bytes)) - 1;
@@ -672,7 +721,7 @@ void paint(tvk_renderer* R) {
   const float iso_norm = float(double(R->isovalue) / double(1u << (8 * V->bytes)));
   if (R->cell_skip) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
 
-  const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
+  const View view = make_view(R->eye, R->at, R->up, R->fovy, rw, rh, R->model);
 
   // AbstrRenderer.cpp:1003-1012: scale of the brick boxes
   const double user_scale[3] = {1, 1, 1};
@@ -697,9 +746,10 @@ void paint(tvk_renderer* R) {
   const double rescale = rmax / double(R->tf_w - 1);
   const double lo = double(nz_lo) * rescale, hi = double(nz_hi) * rescale;
 
-  // per-brick records of the visible LOD-0 bricks (BuildSubFrameBrickList)
+  // per-brick records of the visible bricks of LOD L (BuildSubFrameBrickList)
+  const uint64_t first = V->lod_first[L], nbl = V->lod_first[L + 1] - first;
   TVK_CUDA(cudaEventSynchronize(R->ev_staged));
-  R->h_bricks.ensure(V->n_bricks * sizeof(DevBrick));
+  R->h_bricks.ensure(nbl * sizeof(DevBrick));
   DevBrick* hb = R->h_bricks.as<DevBrick>();
   uint32_t nvis = 0;
   // Front-to-back order valid for every ray: bricks sorted by L1 distance of
@@ -707,14 +757,14 @@ void paint(tvk_renderer* R) {
   // distance grows at every crossing into the next brick, so this order
   // restates the per-ray entry-distance order of the brick loop
   // (AbstrRenderer.cpp:1097 sorts by corner distance instead).
-  const LodInfo& l0 = V->lods[0];
+  const LodInfo& ll = V->lods[L];
   int64_t eye_cell[3];
   for (int a = 0; a < 3; ++a) {
     const double o = view.inv[a][3];
-    const uint64_t stride = a == 0 ? 1 : (a == 1 ? l0.bricks[0] : l0.bricks[0] * l0.bricks[1]);
-    int64_t e = int64_t(l0.bricks[a]);
-    for (uint64_t i = 0; i < l0.bricks[a]; ++i) {
-      const tvk_brick_md& m = V->md[i * stride];
+    const uint64_t stride = a == 0 ? 1 : (a == 1 ? ll.bricks[0] : ll.bricks[0] * ll.bricks[1]);
+    int64_t e = int64_t(ll.bricks[a]);
+    for (uint64_t i = 0; i < ll.bricks[a]; ++i) {
+      const tvk_brick_md& m = V->md[first + i * stride];
       const double lo_b = double(m.center[a] * vs[a] - m.extents[a] * vs[a] / 2.0f);
       const double hi_b = double(m.center[a] * vs[a] + m.extents[a] * vs[a] / 2.0f);
       if (i == 0 && o < lo_b) { e = -1; break; }
@@ -723,13 +773,14 @@ void paint(tvk_renderer* R) {
     eye_cell[a] = e;
   }
   std::vector<std::pair<uint64_t, uint64_t>> order;  // (L1 distance, brick)
-  order.reserve(V->n_bricks);
-  for (uint64_t k = 0; k < V->n_bricks; ++k) {
+  order.reserve(nbl);
+  for (uint64_t j = 0; j < nbl; ++j) {
+    const uint64_t k = first + j;
     // ContainsData (uvfDataset.cpp:1201-1215): TF value limits, or the isovalue
     if (iso_mode ? !(double(R->isovalue) <= V->bmax[k]) : !(hi >= V->bmin[k] && lo <= V->bmax[k]))
       continue;
-    const int64_t c[3] = {int64_t(k % l0.bricks[0]), int64_t((k / l0.bricks[0]) % l0.bricks[1]),
-                          int64_t(k / (l0.bricks[0] * l0.bricks[1]))};
+    const int64_t c[3] = {int64_t(j % ll.bricks[0]), int64_t((j / ll.bricks[0]) % ll.bricks[1]),
+                          int64_t(j / (ll.bricks[0] * ll.bricks[1]))};
     uint64_t d = 0;
     for (int a = 0; a < 3; ++a) d += uint64_t(std::llabs(c[a] - eye_cell[a]));
     order.emplace_back(d, k);
@@ -747,9 +798,10 @@ void paint(tvk_renderer* R) {
       c[a] = m.center[a] * vs[a];
       b.pmin[a] = c[a] - e[a] / 2.0f;
       b.pmax[a] = c[a] + e[a] / 2.0f;
-      // UVFDataset::GetTextCoords (uvfDataset.cpp:1766-1767)
+      // UVFDataset::GetTextCoords (uvfDataset.cpp:1747-1774): the upper corner
+      // is scaled by the LOD's brick aspect (ExtendedOctree::GetBrickAspect)
       tmin[a] = float(V->overlap) / float(b.n[a]);
-      tmax[a] = 1.0f - tmin[a];
+      tmax[a] = (1.0f - tmin[a]) * float(ll.aspect[a]);
     }
     // GLRaycaster.cpp:589-612 ComputeEyeToTextureMatrix
     for (int a = 0; a < 3; ++a) {
@@ -768,7 +820,7 @@ void paint(tvk_renderer* R) {
     b.cells = V->cell_dims[k];
     b.empty_off = R->cell_skip ? R->empty_word_off[k] : 0;
   }
-  R->d_bricks.ensure(std::max<size_t>(1, V->n_bricks) * sizeof(DevBrick));
+  R->d_bricks.ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
   if (nvis)
     TVK_CUDA(cudaMemcpyAsync(R->d_bricks.p, hb, nvis * sizeof(DevBrick), cudaMemcpyHostToDevice,
                              R->stream));
@@ -821,26 +873,168 @@ void paint(tvk_renderer* R) {
   for (int a = 0; a < 3; ++a)  // GLRenderer.cpp:2807-2808
     P.iso_diffuse[a] = (R->diffuse[a] * R->diffuse[3]) * R->iso_color[a];
   P.max_q = 1.0e6f;
-  P.width = R->width;
-  P.height = R->height;
+  P.width = rw;
+  P.height = rh;
   const size_t npix = size_t(R->width) * R->height;
   R->d_img.ensure(npix * sizeof(float4));
-  R->d_spp.ensure(npix * sizeof(uint32_t));
+  R->d_spp.ensure(size_t(rw) * rh * sizeof(uint32_t));
   R->d_counters.ensure(4 * sizeof(unsigned long long));
-  P.out = R->d_img.as<float4>();
+  const bool upscale = rw != R->width || rh != R->height;
+  if (upscale) R->d_lowimg.ensure(size_t(rw) * rh * sizeof(float4));
+  P.out = upscale ? R->d_lowimg.as<float4>() : R->d_img.as<float4>();
   P.spp = R->d_spp.as<uint32_t>();
   P.counters = R->d_counters.as<unsigned long long>();
   TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
   TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
   launch_raycast(P, R->stream, &R->launches);
+  // GLRenderer.cpp:717-747 CopyOverCompletedRegion: the reduced image is
+  // stretched over the viewport with GL_LINEAR
+  if (upscale)
+    launch_upscale(R->d_lowimg.as<float4>(), rw, rh, R->d_img.as<float4>(), R->width, R->height,
+                   1.0f / R->screen_dec, R->stream, &R->launches);
   TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
+  R->render_w = rw;
+  R->render_h = rh;
   R->h_counters.ensure(4 * sizeof(unsigned long long));
   TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, R->stream));
   R->stats.bricks_visible = nvis;
-  R->stats.bricks_total = V->n_bricks;
+  R->stats.bricks_total = nbl;
   R->stats.kernel_launches = R->launches - launches0;
   R->painted = true;
+}
+
+// CullingLOD::GetLODLevel (CullingLOD.cpp:126-138) with the screen parameters of
+// SetScreenParams (:57-67, screen-space error 1) as ComputeMinLODForCurrentView
+// (AbstrRenderer.cpp:789-803) calls it: the volume centre at the origin, the
+// normalised domain extent and the LOD-0 voxel count, clamped to the LOD limits.
+uint64_t min_lod_for_view(const tvk_renderer* R, const tvk_volume* V) {
+  const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
+  float ext[3];
+  for (int a = 0; a < 3; ++a) ext[a] = float(V->dims[a]);  // times GetScale() = 1
+  const float emax = std::max(ext[0], std::max(ext[1], ext[2]));
+  float err = 0.0f;
+  for (int a = 0; a < 3; ++a) err = std::max(err, (ext[a] / emax) / float(V->dims[a]));
+  const float lod_factor = 2.0f * std::tan(R->fovy * ((3.1416f / 180.0f) / 2.0f)) * 1.0f /
+                           float(R->height);
+  const float z_center = float(view.mv[2][3]);
+  const float fz = std::max(R->znear, -z_center);
+  const int level = int(std::floor(std::log(lod_factor * fz / err) / std::log(2.0f)));
+  const int hi = int(V->lods.size()) - 1;
+  return uint64_t(std::min(std::max(level, int(R->lod_limits[1])), hi));
+}
+
+// AbstrRenderer::ComputeMaxLODForCurrentView (AbstrRenderer.cpp:681-787).
+void compute_start_lod(tvk_renderer* R) {
+  if (!R->capture && R->msec_passed[0] >= 0.0f) {
+    if (R->msec_passed[0] > R->max_ms_per_frame) {
+      if (R->lod_not_ok < 3) {
+        R->lod_not_ok++;
+      } else {
+        R->lod_not_ok = 0;
+        const uint64_t skip = std::max<uint64_t>(1, R->perf_lod_skip) - 1;
+        if (R->perf_lod_skip != skip) {
+          R->msec_passed[0] = R->msec_passed[1];
+          R->perf_lod_skip = skip;
+        } else if (R->low_res_intermediate) {
+          if (!(R->decrease_sampling_rate && R->decrease_screen_res)) {
+            if (!R->decrease_screen_res)
+              R->decrease_screen_res = true;
+            else
+              R->decrease_sampling_rate = true;
+          }
+        }
+      }
+    } else if (R->msec_passed[1] >= 0.0f && R->msec_passed[1] <= R->max_ms_per_frame) {
+      // the last frame finished (our subframes always render every brick)
+      R->lod_not_ok = 0;
+      if (R->decrease_sampling_rate || R->decrease_screen_res) {
+        if (R->decrease_sampling_rate)
+          R->decrease_sampling_rate = false;
+        else
+          R->decrease_screen_res = false;
+      } else {
+        R->perf_lod_skip =
+            std::min<uint64_t>(R->max_lod_index - R->min_lod_view, R->perf_lod_skip + 1);
+      }
+    }
+    // unsigned arithmetic as in the reference (wraps where it does)
+    R->start_lod_offset = std::max<uint64_t>(R->min_lod_view, R->max_lod_index - R->perf_lod_skip);
+  } else if (R->capture) {
+    R->start_lod_offset = R->min_lod_view;
+  } else {
+    R->start_lod_offset = R->max_lod_index;  // the very first frame
+  }
+  R->start_lod_offset =
+      std::min<uint64_t>(R->start_lod_offset, R->max_lod_index - uint64_t(R->lod_limits[0]));
+  R->current_lod_offset = R->start_lod_offset;
+  R->msec_passed[0] = R->msec_passed[1] = -1.0f;  // RestartTimers
+}
+
+// One subframe of a progressive frame: AbstrRenderer::PlanFrame
+// (AbstrRenderer.cpp:1125-1212), the paint, and CompletedASubframe (:651-670).
+void paint_progressive(tvk_renderer* R, bool new_frame, tvk_subframe_info* info) {
+  const tvk_volume* V = R->vol;
+  if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
+  if (!new_frame && !R->frame_started) new_frame = true;
+  bool build = false;
+  if (new_frame) {
+    R->min_lod_view = min_lod_for_view(R, V);
+    compute_start_lod(R);
+    R->decrease_sampling_rate_now = R->decrease_sampling_rate;
+    R->decrease_screen_res_now = R->decrease_screen_res;
+    build = true;
+    if (R->decrease_sampling_rate_now || R->decrease_screen_res_now)
+      R->another_redraw_low_res = true;
+  } else if (R->decrease_sampling_rate_now || R->decrease_screen_res_now) {
+    R->decrease_screen_res_now = false;
+    R->decrease_sampling_rate_now = false;
+    R->another_redraw_low_res = false;
+  } else if (R->current_lod_offset > R->min_lod_view) {
+    build = true;
+    R->current_lod_offset--;
+  } else {
+    // the frame is complete: the reference's CheckForRedraw asks for nothing more
+    std::memset(info, 0, sizeof(*info));
+    info->lod = uint32_t(R->current_lod);
+    info->frame_complete = 1;
+    return;
+  }
+  if (build)
+    R->current_lod = R->capture ? 0
+                                : std::min<uint64_t>(R->current_lod_offset, V->lods.size() - 1);
+  // LODs the volume does not hold fall back to the coarsest built one
+  const uint64_t built = V->lod_first.size() - 2;
+  const uint32_t lod = uint32_t(std::min<uint64_t>(R->current_lod, built));
+  R->frame_started = true;
+  paint(R, Subframe{lod, R->decrease_screen_res_now, R->decrease_sampling_rate_now});
+  TVK_CUDA(cudaEventSynchronize(R->ev_stop));
+  float ms = 0.0f;
+  TVK_CUDA(cudaEventElapsedTime(&ms, R->ev_start, R->ev_stop));
+  R->msec_current_frame += ms;
+  // CompletedASubframe
+  const bool first_sub = R->current_lod_offset == R->start_lod_offset &&
+                         (!R->decrease_screen_res || R->decrease_screen_res_now) &&
+                         (!R->decrease_sampling_rate || R->decrease_sampling_rate_now);
+  const bool second_sub = !first_sub && (R->current_lod_offset == R->start_lod_offset ||
+                                         (R->current_lod_offset + 1 == R->start_lod_offset &&
+                                          !(R->decrease_screen_res || R->decrease_sampling_rate)));
+  if (first_sub)
+    R->msec_passed[0] = R->msec_current_frame;
+  else if (second_sub)
+    R->msec_passed[1] = R->msec_current_frame;
+  R->msec_current_frame = 0.0f;
+  info->lod = lod;
+  info->decreased_screen_res = R->decrease_screen_res_now ? 1 : 0;
+  info->decreased_sampling_rate = R->decrease_sampling_rate_now ? 1 : 0;
+  info->render_width = R->render_w;
+  info->render_height = R->render_h;
+  info->min_lod = uint32_t(R->min_lod_view);
+  info->start_lod = uint32_t(R->start_lod_offset);
+  info->ms = ms;
+  // AbstrRenderer::CheckForRedraw (AbstrRenderer.cpp:440-470)
+  info->frame_complete =
+      (R->current_lod_offset > R->min_lod_view || R->another_redraw_low_res) ? 0 : 1;
 }
 
 }  // namespace
@@ -1098,6 +1292,16 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
       tvk::fail(TVK_ERR_UNSUPPORTED, "rendering runs on bricked source volumes, not rebricked ones");
     r->vol = v;
     r->empty_valid = false;
+    r->frame_started = false;
+    // AbstrRenderer.cpp:247: m_iMaxLODIndex = GetLargestSingleBrickLOD(0)
+    r->max_lod_index = 0;
+    if (v) {
+      for (size_t l = 0; l < v->lods.size(); ++l)
+        if (v->lods[l].bricks[0] * v->lods[l].bricks[1] * v->lods[l].bricks[2] == 1) {
+          r->max_lod_index = l;
+          break;
+        }
+    }
     // AbstrRenderer.cpp:252-259: the isovalue starts at half the data range
     if (v) r->isovalue = float(v->range_max - v->range_min) / 2.0f;
   });
@@ -1278,7 +1482,87 @@ tvk_status tvk_set_frame_termination(tvk_renderer* r, float threshold) {
 tvk_status tvk_paint(tvk_renderer* r) {
   return guarded([&] {
     REQUIRE(r, "null renderer");
-    tvk::paint(r);
+    tvk::paint(r, tvk::Subframe{r->lod, r->dec_screen, r->dec_sampling});
+  });
+}
+
+tvk_status tvk_set_lod(tvk_renderer* r, uint32_t lod) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->lod = lod;
+  });
+}
+
+tvk_status tvk_set_reduced_quality(tvk_renderer* r, int decrease_screen_res,
+                                   int decrease_sampling_rate) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->dec_screen = decrease_screen_res != 0;
+    r->dec_sampling = decrease_sampling_rate != 0;
+  });
+}
+
+tvk_status tvk_set_perf_measures(tvk_renderer* r, uint32_t min_framerate,
+                                 int low_res_intermediate, float screen_res_dec_factor,
+                                 float sample_dec_factor) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    REQUIRE(screen_res_dec_factor >= 1.0f && screen_res_dec_factor <= 64.0f,
+            "screen resolution decrease factor must be in [1, 64]");
+    REQUIRE(sample_dec_factor > 0.0f, "sample rate decrease factor must be > 0");
+    // AbstrRenderer::SetPerfMeasures (AbstrRenderer.cpp:1435-1454)
+    r->max_ms_per_frame = (min_framerate == 0) ? 10000.0f : 1000.0f / float(min_framerate);
+    r->screen_dec = screen_res_dec_factor;
+    r->sample_dec = sample_dec_factor;
+    r->low_res_intermediate = low_res_intermediate != 0;
+    if (!r->low_res_intermediate) {
+      r->decrease_screen_res = r->decrease_screen_res_now = false;
+      r->decrease_sampling_rate = r->decrease_sampling_rate_now = false;
+      r->another_redraw_low_res = false;
+    }
+    r->frame_started = false;
+  });
+}
+
+tvk_status tvk_set_lod_limits(tvk_renderer* r, uint32_t coarsest_skip, uint32_t finest) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->lod_limits[0] = coarsest_skip;
+    r->lod_limits[1] = finest;
+    r->frame_started = false;
+  });
+}
+
+tvk_status tvk_set_capture_mode(tvk_renderer* r, int capture) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    r->capture = capture != 0;
+    r->frame_started = false;
+  });
+}
+
+tvk_status tvk_compute_min_lod(tvk_renderer* r, uint32_t* lod) {
+  return guarded([&] {
+    REQUIRE(r && lod, "null argument");
+    if (!r->vol) tvk::fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
+    if (r->width == 0 || r->height == 0) tvk::fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
+    *lod = uint32_t(tvk::min_lod_for_view(r, r->vol));
+  });
+}
+
+tvk_status tvk_paint_progressive(tvk_renderer* r, int new_frame, tvk_subframe_info* info) {
+  return guarded([&] {
+    REQUIRE(r && info, "null argument");
+    tvk::paint_progressive(r, new_frame != 0, info);
+  });
+}
+
+tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* height) {
+  return guarded([&] {
+    REQUIRE(r && width && height, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    *width = r->render_w;
+    *height = r->render_h;
   });
 }
 
@@ -1309,7 +1593,9 @@ tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t
   return guarded([&] {
     REQUIRE(r && host_counts, "null argument");
     if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
-    const size_t np = size_t(r->width) * r->height;
+    // counts of the ray-marched image (render size; smaller than the viewport
+    // while the screen resolution is decreased)
+    const size_t np = size_t(r->render_w) * r->render_h;
     REQUIRE(n >= np, "output buffer smaller than the image");
     TVK_CUDA(cudaMemcpyAsync(host_counts, r->d_spp.p, np * sizeof(uint32_t),
                              cudaMemcpyDeviceToHost, r->stream));

@@ -730,6 +730,44 @@ void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, 
   ++*launches;
 }
 
+namespace {
+
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float w) {
+  return make_float4(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y), fmaf(w, b.z - a.z, a.z),
+                     fmaf(w, b.w - a.w, a.w));
+}
+
+__global__ void __launch_bounds__(256)
+upscale_kernel(const float4* __restrict__ low, uint32_t lw, uint32_t lh, float4* __restrict__ out,
+               uint32_t w, uint32_t h, float rescale) {
+  // GLRenderer::FullscreenQuadRegion (GLRenderer.cpp:688-713): pixel x of the
+  // viewport reads texture coordinate (x + 0.5) / w * rescale of the w-wide
+  // target, i.e. texel position (x + 0.5) * rescale - 0.5, filtered with
+  // GL_LINEAR and clamped to the reduced image's edge.
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y;
+  if (x >= w) return;
+  const float u = (float(x) + 0.5f) * rescale - 0.5f;
+  const float v = (float(y) + 0.5f) * rescale - 0.5f;
+  const float fu = floorf(u), fv = floorf(v);
+  const float wx = u - fu, wy = v - fv;
+  const int x0 = min(max(int(fu), 0), int(lw) - 1), x1 = min(max(int(fu) + 1, 0), int(lw) - 1);
+  const int y0 = min(max(int(fv), 0), int(lh) - 1), y1 = min(max(int(fv) + 1, 0), int(lh) - 1);
+  const float4 c0 = lerp4(low[size_t(y0) * lw + x0], low[size_t(y0) * lw + x1], wx);
+  const float4 c1 = lerp4(low[size_t(y1) * lw + x0], low[size_t(y1) * lw + x1], wx);
+  out[size_t(y) * w + x] = lerp4(c0, c1, wy);
+}
+
+}  // namespace
+
+void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, uint32_t w,
+                    uint32_t h, float rescale, cudaStream_t s, uint64_t* launches) {
+  const dim3 grid((w + 255) / 256, h);
+  upscale_kernel<<<grid, 256, 0, s>>>(low, lw, lh, out, w, h, rescale);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 block(128);
   const dim3 grid((p.width + 15) / 16, (p.height + 7) / 8);

@@ -186,6 +186,10 @@ struct RenderParams {
 };
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
+// Bilinear stretch of a reduced-resolution image over the viewport
+// (GLRenderer::CopyOverCompletedRegion with GL_LINEAR).
+void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, uint32_t w,
+                    uint32_t h, float rescale, cudaStream_t s, uint64_t* launches);
 
 }  // namespace tvk
 

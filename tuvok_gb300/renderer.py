@@ -275,8 +275,47 @@ class Renderer:
         check(lib().tvk_read_image(self._h, out.ctypes.data_as(N._f32p), out.size))
         return out
 
+    def SetLOD(self, lod):
+        """m_iCurrentLOD for Paint()."""
+        check(lib().tvk_set_lod(self._h, int(lod)))
+
+    def SetReducedQuality(self, decrease_screen_res=False, decrease_sampling_rate=False):
+        """decreaseScreenResNow / decreaseSamplingRateNow for Paint()."""
+        check(lib().tvk_set_reduced_quality(self._h, int(bool(decrease_screen_res)),
+                                            int(bool(decrease_sampling_rate))))
+
+    def SetPerfMeasures(self, min_framerate=0, render_low_res_intermediate=False,
+                        screen_res_dec_factor=2.0, sample_dec_factor=2.0):
+        check(lib().tvk_set_perf_measures(self._h, int(min_framerate),
+                                          int(bool(render_low_res_intermediate)),
+                                          float(screen_res_dec_factor), float(sample_dec_factor)))
+
+    def SetLODLimits(self, coarsest_skip, finest):
+        check(lib().tvk_set_lod_limits(self._h, int(coarsest_skip), int(finest)))
+
+    def SetCaptureMode(self, on):
+        check(lib().tvk_set_capture_mode(self._h, int(bool(on))))
+
+    def ComputeMinLODForCurrentView(self):
+        out = C.c_uint32()
+        check(lib().tvk_compute_min_lod(self._h, C.byref(out)))
+        return out.value
+
+    def PaintProgressive(self, new_frame=False):
+        """One subframe of a progressive frame; returns its SubframeInfo."""
+        info = N.SubframeInfo()
+        check(lib().tvk_paint_progressive(self._h, int(bool(new_frame)), C.byref(info)))
+        return info
+
+    def GetRenderSize(self):
+        w, h = C.c_uint32(), C.c_uint32()
+        check(lib().tvk_get_render_size(self._h, C.byref(w), C.byref(h)))
+        return w.value, h.value
+
     def ReadSampleCounts(self):
-        out = np.empty((self._h_px, self._w), dtype=np.uint32)
+        """Per-pixel sample counts of the ray-marched image (GetRenderSize)."""
+        w, h = self.GetRenderSize()
+        out = np.empty((h, w), dtype=np.uint32)
         check(lib().tvk_read_sample_counts(self._h, out.ctypes.data_as(N._u32p), out.size))
         return out
 
