@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batching", action="store_true",
+                   help="skip the 64-view batched-paint measurement")
+    p.add_argument("--batch-steps", type=int, default=10)
     p.add_argument("--frame-ert", type=float, default=1.0)
     return p.parse_args()
 
@@ -268,6 +271,73 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batching(args, torch, steps):
+    """64 mixed views over four volumes: one tvk_paint_batch per step (one
+    persistent launch replayed from a CUDA graph) against the same 64 frames
+    painted with tvk_paint one renderer after another."""
+    from tuvok_gb300 import Batch, Renderer
+    from tuvok_gb300.workloads import BATCH_VOLUMES, batch_views, orbit_poses, tf2d_lobes
+    vols = [make_volume(w, torch) for w in BATCH_VOLUMES]
+    tf = tf2d_lobes()
+    views = batch_views()
+    rs = []
+    for vi, (w, h), srm, lit in views:
+        r = Renderer()
+        r.RegisterDataset(vols[vi][0])
+        r.Set2DTransFloat(tf)
+        r.SetRendermode(1)
+        r.SetUseLighting(lit)
+        r.SetSampleRateModifier(srm)
+        r.Resize(w, h)
+        rs.append(r)
+    poses = orbit_poses(len(rs) * (steps + 4), 4242)
+
+    def set_cams(step):
+        for k, r in enumerate(rs):
+            eye, at, up = poses[step * len(rs) + k]
+            r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+
+    b = Batch()
+    for i in range(3):
+        set_cams(i)
+        b.Paint(rs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gpu_ms = []
+    for i in range(steps):
+        set_cams(3 + i)
+        b.Paint(rs)
+        gpu_ms.append(b.GetInfo().ms)
+    torch.cuda.synchronize()
+    batched_s = time.perf_counter() - t0
+    info = b.GetInfo()
+    for i in range(3):
+        set_cams(i)
+        for r in rs:
+            r.Paint()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        set_cams(3 + i)
+        for r in rs:
+            r.Paint()
+    torch.cuda.synchronize()
+    single_s = time.perf_counter() - t0
+    pixels = sum(w * h for _, (w, h), _, _ in views)
+    return {"workload": "batch_mixed_64", "views": len(rs), "steps": steps,
+            "volumes": [f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} "
+                        f"{'u8' if w.dtype == np.uint8 else 'u16'}" for w in BATCH_VOLUMES],
+            "pixels_per_step": pixels,
+            "batched_views_per_s": len(rs) * steps / batched_s,
+            "independent_views_per_s": len(rs) * steps / single_s,
+            "speedup": single_s / batched_s,
+            "gpu_ms_per_batch": float(np.median(gpu_ms)),
+            "ctas_per_sm": info.ctas_per_sm, "graph_reused": info.graph_reused,
+            "gpu_launches_per_batch": 1,
+            "note": "wall-clock over the steps incl. host planning of 64 brick lists; "
+                    "independent = tvk_paint per renderer, each on its own stream"}
+
+
 def run_ours(args):
     import torch
     from tuvok_gb300 import Renderer
@@ -355,6 +425,12 @@ def run_ours(args):
     h2d = int(np.mean(vis)) * dev_brick_bytes
     d2h = w.width * w.height * 16 + 32
 
+    batching = None
+    if not args.no_batching:
+        del r
+        torch.cuda.empty_cache()
+        batching = run_batching(args, torch, args.batch_steps)
+
     cpu = None
     if raw_host is not None:
         threads = os.cpu_count() or 1
@@ -402,6 +478,7 @@ def run_ours(args):
             "gpu_launches": K,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
+            "batching": batching,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -344,6 +344,45 @@ typedef struct tvk_subframe_info {
  * render nothing until the next new frame. */
 tvk_status tvk_paint_progressive(tvk_renderer* r, int new_frame, tvk_subframe_info* info);
 
+/* ---- Batched frames (no counterpart in the reference, which paints render
+ * regions and renderers one after another: GLRenderer.cpp:622-660,
+ * MasterController::RequestNewVolumeRenderer MasterController.cpp:145-200) ---- */
+
+typedef struct tvk_batch tvk_batch;
+
+typedef struct tvk_batch_info {
+  uint32_t frames;        /* renderers in the last batch */
+  uint32_t tiles;         /* 16x8-pixel work items of the persistent launch */
+  uint32_t ctas;          /* persistent CTAs launched */
+  uint32_t ctas_per_sm;   /* chosen by the autotuner or fixed */
+  uint32_t launches;      /* persistent launches: one per kernel variant (voxel
+                             type x iso/compositing) and per 64 frames */
+  int graph_reused;       /* 1: the captured CUDA graph was replayed */
+  int autotuned;          /* 1: this call timed the candidate grid sizes */
+  float ms;               /* GPU time of the batch */
+} tvk_batch_info;
+
+/* A batch context (its own stream, CUDA graph and autotuning cache) on the
+ * current device. */
+tvk_status tvk_batch_create(tvk_batch** out);
+tvk_status tvk_batch_destroy(tvk_batch* b);
+
+/* Paints the current frame of every renderer (each with its own volume, TF,
+ * mode, lighting, sample rate, view, viewport, LOD and reduced-quality
+ * switches) in persistent kernel launches -- one per kernel variant present
+ * (u8/u16 x iso/compositing) and per 64 frames -- replayed from a CUDA graph
+ * while the batch's shape is unchanged.  Every renderer's image, sample counts and
+ * statistics are bit-identical to its own tvk_paint.  Results are ordered
+ * before later work on each renderer's stream.  The first call for a new
+ * shape may render the batch a few extra times to time candidate grid sizes
+ * (autotuning, on by default). */
+tvk_status tvk_paint_batch(tvk_batch* b, tvk_renderer* const* renderers, uint32_t n);
+
+/* autotune = 0 with ctas_per_sm = 0 uses the occupancy maximum; ctas_per_sm
+ * > 0 fixes the persistent grid at that many CTAs per SM. */
+tvk_status tvk_batch_set_autotune(tvk_batch* b, int autotune, uint32_t ctas_per_sm);
+tvk_status tvk_batch_get_info(tvk_batch* b, tvk_batch_info* out);
+
 /* Size of the last ray-marched image (the viewport, or the reduced one). */
 tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* height);
 

@@ -53,6 +53,12 @@ class SubframeInfo(C.Structure):
                 ("ms", C.c_float), ("frame_complete", C.c_int)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("frames", C.c_uint32), ("tiles", C.c_uint32), ("ctas", C.c_uint32),
+                ("ctas_per_sm", C.c_uint32), ("launches", C.c_uint32),
+                ("graph_reused", C.c_int), ("autotuned", C.c_int), ("ms", C.c_float)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
                 ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
@@ -112,6 +118,11 @@ PROTOTYPES = {
     "tvk_compute_min_lod": [_vp, _u32p],
     "tvk_paint_progressive": [_vp, C.c_int, C.POINTER(SubframeInfo)],
     "tvk_get_render_size": [_vp, _u32p, _u32p],
+    "tvk_batch_create": [C.POINTER(_vp)],
+    "tvk_batch_destroy": [_vp],
+    "tvk_paint_batch": [_vp, C.POINTER(_vp), C.c_uint32],
+    "tvk_batch_set_autotune": [_vp, C.c_int, C.c_uint32],
+    "tvk_batch_get_info": [_vp, C.POINTER(BatchInfo)],
     "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
     "tvk_read_image": [_vp, _f32p, C.c_size_t],
     "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -521,6 +522,7 @@ struct tvk_renderer {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_staged = nullptr;
+  cudaEvent_t ev_ready = nullptr;  // a planned frame's uploads are queued (batch paints)
   const tvk_volume* vol = nullptr;
   // transfer function (effective RGBA as the GPU samples it)
   std::vector<float> tf;
@@ -581,6 +583,25 @@ struct tvk_renderer {
   uint64_t max_lod_index = 0, min_lod_view = 0, start_lod_offset = 0, current_lod_offset = 0;
   uint64_t current_lod = 0;
   bool frame_started = false;
+};
+
+// Several renderers' frames in one persistent launch (replaces the reference's
+// sequential per-region / per-renderer paints, GLRenderer.cpp:622-660).
+struct tvk_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_done = nullptr;
+  tvk::DevBuf d_next;                        // one work counter per launch
+  std::vector<tvk::BatchLaunch> launch;      // frame tables of the launches
+  std::vector<int> variant;                  // kernel variant of each launch
+  bool autotune = true;
+  uint32_t fixed_ctas_per_sm = 0;           // 0: tuned or the occupancy maximum
+  std::map<std::vector<uint64_t>, uint32_t> tuned;  // launch shapes -> CTAs per SM
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> graph_sig;
+  std::vector<cudaGraphNode_t> kernel_nodes;  // graph node of each launch
+  tvk_batch_info info{};
 };
 
 namespace tvk {
@@ -683,7 +704,18 @@ struct Subframe {
   bool dec_screen, dec_sampling;
 };
 
-void paint(tvk_renderer* R, const Subframe& sf) {
+// A frame planned on the host and ready to launch.
+struct PlannedFrame {
+  RenderParams P;
+  uint32_t rw, rh;   // ray-marched size (smaller than the viewport when reduced)
+  bool upscale;
+  uint64_t launches0;
+};
+
+// Everything of a paint up to the kernel launch: TF table and empty-cell bits,
+// the brick list of the LOD (uploaded on the renderer's stream), the counters
+// cleared, and the frame's parameters.
+PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
   const tvk_volume* V = R->vol;
   if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
   const bool iso_mode = R->mode == TVK_RM_ISOSURFACE;
@@ -885,23 +917,39 @@ void paint(tvk_renderer* R, const Subframe& sf) {
   P.spp = R->d_spp.as<uint32_t>();
   P.counters = R->d_counters.as<unsigned long long>();
   TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
-  TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
-  launch_raycast(P, R->stream, &R->launches);
-  // GLRenderer.cpp:717-747 CopyOverCompletedRegion: the reduced image is
-  // stretched over the viewport with GL_LINEAR
-  if (upscale)
-    launch_upscale(R->d_lowimg.as<float4>(), rw, rh, R->d_img.as<float4>(), R->width, R->height,
-                   1.0f / R->screen_dec, R->stream, &R->launches);
-  TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
-  R->render_w = rw;
-  R->render_h = rh;
+  R->stats.bricks_visible = nvis;
+  R->stats.bricks_total = nbl;
+  return PlannedFrame{P, rw, rh, upscale, launches0};
+}
+
+// GLRenderer.cpp:717-747 CopyOverCompletedRegion: the reduced image is
+// stretched over the viewport with GL_LINEAR
+void launch_upscale_of(tvk_renderer* R, const PlannedFrame& F, cudaStream_t s,
+                       uint64_t* launches) {
+  if (F.upscale)
+    launch_upscale(R->d_lowimg.as<float4>(), F.rw, F.rh, R->d_img.as<float4>(), R->width,
+                   R->height, 1.0f / R->screen_dec, s, launches);
+}
+
+// After the frame's kernels are ordered on the renderer's stream: the counters'
+// read-back and the bookkeeping of a finished paint.
+void finish_frame(tvk_renderer* R, const PlannedFrame& F) {
+  R->render_w = F.rw;
+  R->render_h = F.rh;
   R->h_counters.ensure(4 * sizeof(unsigned long long));
   TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, R->stream));
-  R->stats.bricks_visible = nvis;
-  R->stats.bricks_total = nbl;
-  R->stats.kernel_launches = R->launches - launches0;
+  R->stats.kernel_launches = R->launches - F.launches0;
   R->painted = true;
+}
+
+void paint(tvk_renderer* R, const Subframe& sf) {
+  const PlannedFrame F = plan_frame(R, sf);
+  TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
+  launch_raycast(F.P, R->stream, &R->launches);
+  launch_upscale_of(R, F, R->stream, &R->launches);
+  TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
+  finish_frame(R, F);
 }
 
 // CullingLOD::GetLODLevel (CullingLOD.cpp:126-138) with the screen parameters of
@@ -1035,6 +1083,197 @@ void paint_progressive(tvk_renderer* R, bool new_frame, tvk_subframe_info* info)
   // AbstrRenderer::CheckForRedraw (AbstrRenderer.cpp:440-470)
   info->frame_complete =
       (R->current_lod_offset > R->min_lod_view || R->another_redraw_low_res) ? 0 : 1;
+}
+
+// The launches of one batch on the batch stream: the work counters cleared,
+// one persistent kernel per launch (frame tables travel as kernel parameters),
+// the reduced frames' upscales.
+void enqueue_batch(tvk_batch* B, tvk_renderer* const* rs, const std::vector<PlannedFrame>& F,
+                   uint32_t ctas) {
+  const size_t nl = B->launch.size();
+  TVK_CUDA(cudaMemsetAsync(B->d_next.p, 0, nl * sizeof(uint32_t), B->stream));
+  uint64_t dummy = 0;
+  for (size_t k = 0; k < nl; ++k)
+    launch_raycast_batch(B->launch[k], B->variant[k], B->d_next.as<uint32_t>() + k, ctas,
+                         B->stream, &dummy);
+  for (size_t i = 0; i < F.size(); ++i) launch_upscale_of(rs[i], F[i], B->stream, &dummy);
+}
+
+void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
+  TVK_CUDA(cudaSetDevice(B->device));
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!rs[i]) fail(TVK_ERR_INVALID_ARG, "null renderer in the batch");
+    if (rs[i]->device != B->device)
+      fail(TVK_ERR_INVALID_ARG, "every renderer of a batch must be on the batch's device");
+    for (uint32_t j = 0; j < i; ++j)
+      if (rs[j] == rs[i]) fail(TVK_ERR_INVALID_ARG, "a renderer appears twice in the batch");
+  }
+  // plan every frame on its renderer's stream, then order the batch stream after them
+  std::vector<PlannedFrame> F;
+  F.reserve(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    tvk_renderer* R = rs[i];
+    F.push_back(plan_frame(R, Subframe{R->lod, R->dec_screen, R->dec_sampling}));
+    TVK_CUDA(cudaEventRecord(R->ev_ready, R->stream));
+    TVK_CUDA(cudaStreamWaitEvent(B->stream, R->ev_ready, 0));
+  }
+  // group the frames by kernel variant, at most kBatchFrames per launch
+  B->launch.clear();
+  B->variant.clear();
+  for (int v = 0; v < 4; ++v) {
+    for (uint32_t i = 0; i < n; ++i) {
+      const int fv = (F[i].P.bytes == 2 ? 2 : 0) + (F[i].P.mode == TVK_RM_ISOSURFACE ? 1 : 0);
+      if (fv != v) continue;
+      if (B->launch.empty() || B->variant.back() != v ||
+          B->launch.back().n_frames == kBatchFrames) {
+        B->launch.emplace_back();
+        B->launch.back().n_frames = 0;
+        B->launch.back().tile_first[0] = 0;
+        B->variant.push_back(v);
+      }
+      BatchLaunch& L = B->launch.back();
+      L.frames[L.n_frames] = F[i].P;
+      L.tile_first[L.n_frames + 1] =
+          L.tile_first[L.n_frames] + ((F[i].rw + 15) / 16) * ((F[i].rh + 7) / 8);
+      L.n_frames++;
+    }
+  }
+  const size_t nl = B->launch.size();
+  B->d_next.ensure(nl * sizeof(uint32_t));
+  // The shape of the launch sequence (what a captured graph bakes in): the
+  // launches' variants and frame counts, and per frame the renderer, sizes and
+  // upscale buffers.
+  std::vector<uint64_t> shape = {nl, uint64_t(uintptr_t(B->d_next.p))};
+  for (size_t k = 0; k < nl; ++k) {
+    shape.push_back(uint64_t(B->variant[k]));
+    shape.push_back(B->launch[k].n_frames);
+  }
+  for (uint32_t i = 0; i < n; ++i) {
+    tvk_renderer* R = rs[i];
+    for (uint64_t v : {uint64_t(uintptr_t(R)), uint64_t(F[i].rw), uint64_t(F[i].rh),
+                       uint64_t(R->width), uint64_t(R->height), uint64_t(F[i].upscale),
+                       uint64_t(uintptr_t(R->d_lowimg.p)), uint64_t(uintptr_t(R->d_img.p))})
+      shape.push_back(v);
+  }
+  int sms = 0;
+  TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device));
+  uint32_t max_per_sm = 1u << 30;
+  for (int v : B->variant)
+    max_per_sm = std::min(max_per_sm, uint32_t(std::max(1, batch_ctas_per_sm_max(v))));
+  uint32_t per_sm = B->fixed_ctas_per_sm ? std::min(B->fixed_ctas_per_sm, max_per_sm) : max_per_sm;
+  bool tuned_now = false;
+  if (!B->fixed_ctas_per_sm) {
+    auto it = B->tuned.find(shape);
+    if (it != B->tuned.end()) {
+      per_sm = it->second;
+    } else if (B->autotune) {
+      // time each persistent-grid size on this batch; the frames are
+      // re-rendered identically, only the counters are cleared in between
+      float best = std::numeric_limits<float>::infinity();
+      std::vector<uint32_t> cands;
+      for (uint32_t c : {max_per_sm, (max_per_sm * 3) / 4, max_per_sm / 2, 2u, 1u})
+        if (c >= 1 && c <= max_per_sm && std::find(cands.begin(), cands.end(), c) == cands.end())
+          cands.push_back(c);
+      for (uint32_t c : cands) {
+        TVK_CUDA(cudaEventRecord(B->ev_start, B->stream));
+        enqueue_batch(B, rs, F, c * uint32_t(sms));
+        TVK_CUDA(cudaEventRecord(B->ev_stop, B->stream));
+        for (uint32_t i = 0; i < n; ++i)
+          TVK_CUDA(cudaMemsetAsync(rs[i]->d_counters.p, 0, 4 * sizeof(unsigned long long),
+                                   B->stream));
+        TVK_CUDA(cudaEventSynchronize(B->ev_stop));
+        float ms = 0;
+        TVK_CUDA(cudaEventElapsedTime(&ms, B->ev_start, B->ev_stop));
+        if (ms < best) {
+          best = ms;
+          per_sm = c;
+        }
+      }
+      B->tuned[shape] = per_sm;
+      tuned_now = true;
+    }
+  }
+  const uint32_t ctas = per_sm * uint32_t(sms);
+  shape.push_back(ctas);
+  // one CUDA graph per launch shape; replays update the kernel nodes' frame
+  // tables (new cameras, TFs, brick lists) in place
+  const bool reused = B->exec && shape == B->graph_sig;
+  if (!reused) {
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    B->exec = nullptr;
+    B->graph = nullptr;
+    B->graph_sig.clear();
+    B->kernel_nodes.clear();
+    TVK_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue_batch(B, rs, F, ctas);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(B->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    TVK_CUDA(cudaStreamEndCapture(B->stream, &B->graph));
+    size_t nn = 0;
+    TVK_CUDA(cudaGraphGetNodes(B->graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    TVK_CUDA(cudaGraphGetNodes(B->graph, nodes.data(), &nn));
+    B->kernel_nodes.assign(nl, nullptr);
+    const uint32_t* base = B->d_next.as<uint32_t>();
+    for (cudaGraphNode_t node : nodes) {
+      cudaGraphNodeType t;
+      TVK_CUDA(cudaGraphNodeGetType(node, &t));
+      if (t != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      TVK_CUDA(cudaGraphKernelNodeGetParams(node, &kp));
+      bool batch = false;
+      for (int v = 0; v < 4; ++v) batch |= kp.func == batch_kernel_function(v);
+      if (!batch) continue;
+      // the launch is identified by its work counter, the second argument
+      const uint32_t* counter = *static_cast<uint32_t* const*>(kp.kernelParams[1]);
+      const size_t k = size_t(counter - base);
+      if (k >= nl) fail(TVK_ERR_INTERNAL, "unrecognised batch kernel node");
+      B->kernel_nodes[k] = node;
+    }
+    for (cudaGraphNode_t node : B->kernel_nodes)
+      if (!node) fail(TVK_ERR_INTERNAL, "batch kernel node missing from the graph");
+    TVK_CUDA(cudaGraphInstantiate(&B->exec, B->graph, 0));
+    B->graph_sig = shape;
+  } else {
+    for (size_t k = 0; k < nl; ++k) {
+      uint32_t* counter = B->d_next.as<uint32_t>() + k;
+      void* args[2] = {&B->launch[k], &counter};
+      cudaKernelNodeParams kp{};
+      kp.func = const_cast<void*>(batch_kernel_function(B->variant[k]));
+      kp.gridDim = dim3(ctas);
+      kp.blockDim = dim3(128);
+      kp.sharedMemBytes = 0;
+      kp.kernelParams = args;
+      TVK_CUDA(cudaGraphExecKernelNodeSetParams(B->exec, B->kernel_nodes[k], &kp));
+    }
+  }
+  for (uint32_t i = 0; i < n; ++i) TVK_CUDA(cudaEventRecord(rs[i]->ev_start, B->stream));
+  TVK_CUDA(cudaEventRecord(B->ev_start, B->stream));
+  TVK_CUDA(cudaGraphLaunch(B->exec, B->stream));
+  TVK_CUDA(cudaEventRecord(B->ev_stop, B->stream));
+  for (uint32_t i = 0; i < n; ++i) TVK_CUDA(cudaEventRecord(rs[i]->ev_stop, B->stream));
+  TVK_CUDA(cudaEventRecord(B->ev_done, B->stream));
+  uint32_t tiles = 0;
+  for (const BatchLaunch& L : B->launch) tiles += L.tile_first[L.n_frames];
+  for (uint32_t i = 0; i < n; ++i) {
+    tvk_renderer* R = rs[i];
+    TVK_CUDA(cudaStreamWaitEvent(R->stream, B->ev_done, 0));
+    R->launches += 1 + (F[i].upscale ? 1 : 0);  // its batch kernel (+ upscale)
+    finish_frame(R, F[i]);
+  }
+  B->info.frames = n;
+  B->info.tiles = tiles;
+  B->info.ctas = ctas;
+  B->info.ctas_per_sm = per_sm;
+  B->info.launches = uint32_t(nl);
+  B->info.graph_reused = reused ? 1 : 0;
+  B->info.autotuned = tuned_now ? 1 : 0;
 }
 
 }  // namespace
@@ -1268,6 +1507,7 @@ tvk_status tvk_renderer_create(tvk_renderer** out) {
     TVK_CUDA(cudaEventCreate(&R->ev_start));
     TVK_CUDA(cudaEventCreate(&R->ev_stop));
     TVK_CUDA(cudaEventCreateWithFlags(&R->ev_staged, cudaEventDisableTiming));
+    TVK_CUDA(cudaEventCreateWithFlags(&R->ev_ready, cudaEventDisableTiming));
     TVK_CUDA(cudaEventRecord(R->ev_staged, R->stream));
     *out = R.release();
   });
@@ -1280,6 +1520,7 @@ tvk_status tvk_renderer_destroy(tvk_renderer* r) {
     if (r->ev_start) cudaEventDestroy(r->ev_start);
     if (r->ev_stop) cudaEventDestroy(r->ev_stop);
     if (r->ev_staged) cudaEventDestroy(r->ev_staged);
+    if (r->ev_ready) cudaEventDestroy(r->ev_ready);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
   });
@@ -1554,6 +1795,58 @@ tvk_status tvk_paint_progressive(tvk_renderer* r, int new_frame, tvk_subframe_in
   return guarded([&] {
     REQUIRE(r && info, "null argument");
     tvk::paint_progressive(r, new_frame != 0, info);
+  });
+}
+
+tvk_status tvk_batch_create(tvk_batch** out) {
+  return guarded([&] {
+    REQUIRE(out, "null output handle");
+    std::unique_ptr<tvk_batch> B(new tvk_batch());
+    TVK_CUDA(cudaGetDevice(&B->device));
+    TVK_CUDA(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+    TVK_CUDA(cudaEventCreate(&B->ev_start));
+    TVK_CUDA(cudaEventCreate(&B->ev_stop));
+    TVK_CUDA(cudaEventCreateWithFlags(&B->ev_done, cudaEventDisableTiming));
+    *out = B.release();
+  });
+}
+
+tvk_status tvk_batch_destroy(tvk_batch* b) {
+  return guarded([&] {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaEvent_t e : {b->ev_start, b->ev_stop, b->ev_done})
+      if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+  });
+}
+
+tvk_status tvk_batch_set_autotune(tvk_batch* b, int autotune, uint32_t ctas_per_sm) {
+  return guarded([&] {
+    REQUIRE(b, "null batch");
+    b->autotune = autotune != 0;
+    b->fixed_ctas_per_sm = ctas_per_sm;
+    b->tuned.clear();
+  });
+}
+
+tvk_status tvk_paint_batch(tvk_batch* b, tvk_renderer* const* renderers, uint32_t n) {
+  return guarded([&] {
+    REQUIRE(b && renderers && n >= 1, "need a batch and at least one renderer");
+    tvk::paint_batch(b, renderers, n);
+  });
+}
+
+tvk_status tvk_batch_get_info(tvk_batch* b, tvk_batch_info* out) {
+  return guarded([&] {
+    REQUIRE(b && out, "null argument");
+    if (b->info.frames == 0) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    TVK_CUDA(cudaEventSynchronize(b->ev_stop));
+    TVK_CUDA(cudaEventElapsedTime(&b->info.ms, b->ev_start, b->ev_stop));
+    *out = b->info;
   });
 }
 

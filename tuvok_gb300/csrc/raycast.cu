@@ -576,13 +576,22 @@ __device__ __forceinline__ bool footprint_touches_tile(const RenderParams& P, co
   return xmax >= tx0 - 2.0f && xmin <= tx0 + 17.0f && ymax >= ty0 - 2.0f && ymin <= ty0 + 9.0f;
 }
 
-// kIso: isosurface mode (nearest refined hit + compose); otherwise the
-// compositing modes (1D/2D TF, lit or unlit)
+// Shared-memory state of one 16x8-pixel tile: the candidate brick list.
+struct TileShared {
+  uint16_t cand[kCandChunk];
+  uint32_t warp_cnt[4];
+  uint32_t n_cand;
+};
+
+// One 16x8-pixel tile (tile coordinates bx, by) of the frame P describes; all
+// 128 threads of the CTA take part.  kIso: isosurface mode (nearest refined hit
+// + compose); otherwise the compositing modes (1D/2D TF, lit or unlit).
 template <class T, bool kIso>
-__global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
+__device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, uint32_t by,
+                                            TileShared& sh) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-  const uint32_t py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  const uint32_t px = bx * 16 + (warp & 1) * 8 + (lane & 7);
+  const uint32_t py = by * 8 + (warp >> 1) * 4 + (lane >> 3);
   const bool active = px < P.width && py < P.height;
 
   const float nx = (float(px) + 0.5f) * P.inv_w2 - 1.0f;
@@ -601,10 +610,7 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
   // strictly grows whenever a ray crosses into the next brick).  Each CTA
   // keeps, in that order, the bricks whose screen footprint can touch its
   // 16x8-pixel tile; each ray then marches those its own slab test hits.
-  __shared__ uint16_t cand[kCandChunk];
-  __shared__ uint32_t warp_cnt[4];
-  __shared__ uint32_t n_cand;
-  const float tx0 = float(blockIdx.x * 16), ty0 = float(blockIdx.y * 8);
+  const float tx0 = float(bx * 16), ty0 = float(by * 8);
 
   float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t samples = 0, shaded = 0, graded = 0;
@@ -615,26 +621,27 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
   for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
     const uint32_t end = min(P.n_bricks, base + kCandChunk);
     __syncthreads();  // the previous chunk's list is no longer read
-    if (tid == 0) n_cand = 0;
+    if (tid == 0) sh.n_cand = 0;
     for (uint32_t s = base; s < end; s += blockDim.x) {
       const uint32_t i = s + tid;
       const bool keep = i < end && footprint_touches_tile(P, P.bricks[i], tx0, ty0);
       const uint32_t m = __ballot_sync(0xffffffffu, keep);
       __syncthreads();
-      if (lane == 0) warp_cnt[warp] = __popc(m);
+      if (lane == 0) sh.warp_cnt[warp] = __popc(m);
       __syncthreads();
-      uint32_t off = n_cand;
-      for (uint32_t w2 = 0; w2 < warp; ++w2) off += warp_cnt[w2];
-      if (keep) cand[off + __popc(m & ((1u << lane) - 1u))] = uint16_t(i - base);
+      uint32_t off = sh.n_cand;
+      for (uint32_t w2 = 0; w2 < warp; ++w2) off += sh.warp_cnt[w2];
+      if (keep) sh.cand[off + __popc(m & ((1u << lane) - 1u))] = uint16_t(i - base);
       __syncthreads();
-      if (tid == 0) n_cand += warp_cnt[0] + warp_cnt[1] + warp_cnt[2] + warp_cnt[3];
+      if (tid == 0)
+        sh.n_cand += sh.warp_cnt[0] + sh.warp_cnt[1] + sh.warp_cnt[2] + sh.warp_cnt[3];
     }
     __syncthreads();
     if (!active) continue;
-    const uint32_t nc = n_cand;
+    const uint32_t nc = sh.n_cand;
     for (uint32_t c = 0; c < nc; ++c) {
       if (frame.w >= P.frame_ert) break;
-      const DevBrick& bg = P.bricks[base + cand[c]];
+      const DevBrick& bg = P.bricks[base + sh.cand[c]];
       float tn = -INFINITY, tf = INFINITY;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
@@ -677,12 +684,55 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
   }
   // frame totals: one atomic per warp
   const uint32_t s = __reduce_add_sync(0xffffffffu, samples);
-  const uint32_t sh = __reduce_add_sync(0xffffffffu, shaded);
+  const uint32_t shd = __reduce_add_sync(0xffffffffu, shaded);
   const uint32_t gr = __reduce_add_sync(0xffffffffu, graded);
   if (lane == 0) {
     atomicAdd(&P.counters[0], (unsigned long long)s);
-    atomicAdd(&P.counters[1], (unsigned long long)sh);
+    atomicAdd(&P.counters[1], (unsigned long long)shd);
     atomicAdd(&P.counters[3], (unsigned long long)gr);
+  }
+}
+
+template <class T, bool kIso>
+__global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
+  __shared__ TileShared sh;
+  render_tile<T, kIso>(P, blockIdx.x, blockIdx.y, sh);
+}
+
+// Many frames in one persistent launch (the reference renders render regions
+// and renderers one after another, GLRenderer.cpp:622-660).  Work items are
+// (frame, tile) pairs numbered frame by frame (L.tile_first is the prefix sum
+// of tiles per frame); each CTA takes the next item from a global counter and
+// renders the tile with the same code as raycast_kernel, reading the frame's
+// parameters from the launch's parameter block, so every pixel is bit-for-bit
+// the single-frame result.
+template <class T, bool kIso>
+__global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS)
+raycast_batch_kernel(const __grid_constant__ BatchLaunch L, uint32_t* __restrict__ next_item) {
+  __shared__ TileShared sh;
+  __shared__ uint32_t item, frame_idx;
+  const uint32_t n_items = L.tile_first[L.n_frames];
+  for (;;) {
+    __syncthreads();  // the previous item's shared state is no longer read
+    if (threadIdx.x == 0) {
+      const uint32_t it = atomicAdd(next_item, 1u);
+      // frame whose tile range holds the item (binary search of the prefix)
+      uint32_t lo = 0, hi = L.n_frames;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (L.tile_first[mid] <= it) lo = mid; else hi = mid;
+      }
+      item = it;
+      frame_idx = lo;
+    }
+    __syncthreads();
+    const uint32_t it = item;
+    if (it >= n_items) return;
+    const uint32_t f = frame_idx;
+    const RenderParams& P = L.frames[f];
+    const uint32_t local = it - L.tile_first[f];
+    const uint32_t tiles_x = (P.width + 15) / 16;
+    render_tile<T, kIso>(P, local % tiles_x, local / tiles_x, sh);
   }
 }
 
@@ -764,6 +814,34 @@ void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, ui
                     uint32_t h, float rescale, cudaStream_t s, uint64_t* launches) {
   const dim3 grid((w + 255) / 256, h);
   upscale_kernel<<<grid, 256, 0, s>>>(low, lw, lh, out, w, h, rescale);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+const void* batch_kernel_function(int variant) {
+  switch (variant) {
+    case 0: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, false>);
+    case 1: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, true>);
+    case 2: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, false>);
+    default: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, true>);
+  }
+}
+
+int batch_ctas_per_sm_max(int variant) {
+  int n = 0;
+  TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel_function(variant), 128,
+                                                         0));
+  return n;
+}
+
+void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_item,
+                          uint32_t ctas, cudaStream_t s, uint64_t* launches) {
+  switch (variant) {
+    case 0: raycast_batch_kernel<uint8_t, false><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 1: raycast_batch_kernel<uint8_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 2: raycast_batch_kernel<uint16_t, false><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    default: raycast_batch_kernel<uint16_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+  }
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }

@@ -186,6 +186,21 @@ struct RenderParams {
 };
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
+// Frames of one persistent batched launch, passed whole as a kernel parameter
+// (it lives in the constant bank; no staging copy).  All frames of a launch
+// share the kernel variant: voxel type and iso or compositing mode.
+constexpr uint32_t kBatchFrames = 64;
+struct BatchLaunch {
+  uint32_t n_frames;
+  uint32_t tile_first[kBatchFrames + 1];  // prefix sum of 16x8 tiles per frame
+  RenderParams frames[kBatchFrames];
+};
+static_assert(sizeof(BatchLaunch) <= 32000, "kernel parameters are limited to 32 KB");
+// variant = (bytes == 2 ? 2 : 0) + (iso ? 1 : 0); *d_next_item must start at 0
+void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_item,
+                          uint32_t ctas, cudaStream_t s, uint64_t* launches);
+int batch_ctas_per_sm_max(int variant);
+const void* batch_kernel_function(int variant);
 // Bilinear stretch of a reduced-resolution image over the viewport
 // (GLRenderer::CopyOverCompletedRegion with GL_LINEAR).
 void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, uint32_t w,

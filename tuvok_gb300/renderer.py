@@ -336,6 +336,38 @@ class Renderer:
         return p.value, w.value, h.value
 
 
+class Batch:
+    """Paints several renderers' frames in one persistent launch (tvk_paint_batch)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().tvk_batch_create(C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            check(lib().tvk_batch_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def SetAutotune(self, on=True, ctas_per_sm=0):
+        check(lib().tvk_batch_set_autotune(self._h, int(bool(on)), int(ctas_per_sm)))
+
+    def Paint(self, renderers):
+        arr = (C.c_void_p * len(renderers))(*[r._h.value for r in renderers])
+        check(lib().tvk_paint_batch(self._h, arr, len(renderers)))
+
+    def GetInfo(self):
+        info = N.BatchInfo()
+        check(lib().tvk_batch_get_info(self._h, C.byref(info)))
+        return info
+
+
 def generate_volume_device(ptr, dims, dtype, blobs, noise_amp, octaves, cell, seed, int_noise,
                            vmax):
     """Fills device memory at ``ptr`` with a seeded blob volume (see tvk.h)."""

@@ -132,6 +132,56 @@ PLAIN_MEDIUM_LIT = Workload(
 WORKLOADS = {w.name: w for w in (PLAIN_SMALL, PLAIN_LARGE_LIT, PLAIN_MEDIUM_LIT)}
 
 
+# Batching: 64 views of mixed sizes over four volumes made with the plain_small
+# blob rules (values scaled to the type's range), a 256x256 float 2D TF of
+# three Gaussian lobes over (value, |gradient| * gradient scale), sample-rate
+# modifier in {0.5, 1, 2}, lit and unlit mixed; bricks 64^3 core + 1 ghost.
+BATCH_VOLUMES = [
+    Workload(name="batch_a", dims=(128, 128, 128), dtype=np.uint8, vmax=255, n_blobs=32,
+             sigma=(4, 20), peak=(64, 255), noise_amp=4, noise_octaves=0, noise_cell=0,
+             int_noise=True, brick_core=64, overlap=1, width=0, height=0, srm=1.0,
+             lighting=False, light_model=0, tf_kind="", seed=501),
+    Workload(name="batch_b", dims=(256, 256, 256), dtype=np.uint16, vmax=4095, n_blobs=32,
+             sigma=(8, 40), peak=(1024, 4095), noise_amp=64, noise_octaves=0, noise_cell=0,
+             int_noise=True, brick_core=64, overlap=1, width=0, height=0, srm=1.0,
+             lighting=False, light_model=0, tf_kind="", seed=502),
+    Workload(name="batch_c", dims=(384, 384, 256), dtype=np.uint8, vmax=255, n_blobs=32,
+             sigma=(10, 50), peak=(64, 255), noise_amp=4, noise_octaves=0, noise_cell=0,
+             int_noise=True, brick_core=64, overlap=1, width=0, height=0, srm=1.0,
+             lighting=False, light_model=0, tf_kind="", seed=503),
+    Workload(name="batch_d", dims=(512, 512, 512), dtype=np.uint16, vmax=4095, n_blobs=32,
+             sigma=(16, 80), peak=(1024, 4095), noise_amp=64, noise_octaves=0, noise_cell=0,
+             int_noise=True, brick_core=64, overlap=1, width=0, height=0, srm=1.0,
+             lighting=False, light_model=0, tf_kind="", seed=504),
+]
+BATCH_SIZES = [(256, 256), (512, 512), (768, 768), (1024, 1024), (1280, 720)]
+
+
+def tf2d_lobes(w=256, h=256, seed=77):
+    """2D TF of three Gaussian lobes (RGBA float, [h][w]; x = value, y = gradient)."""
+    rng = np.random.default_rng(seed)
+    v, g = np.meshgrid(np.linspace(0, 1, w), np.linspace(0, 1, h))
+    t = np.zeros((h, w, 4), dtype=np.float32)
+    for _ in range(3):
+        cv, cg, sv, sg = (rng.uniform(0.3, 0.9), rng.uniform(0.0, 0.6), rng.uniform(0.04, 0.12),
+                          rng.uniform(0.1, 0.3))
+        a = np.exp(-((v - cv) ** 2 / (2 * sv * sv) + (g - cg) ** 2 / (2 * sg * sg)))
+        col = rng.uniform(0.2, 1.0, 3)
+        for c in range(3):
+            t[..., c] = np.maximum(t[..., c], (a * col[c]).astype(np.float32))
+        t[..., 3] = np.maximum(t[..., 3], (0.6 * a).astype(np.float32))
+    t[..., 3] = np.where(t[..., 3] < 0.02, 0.0, t[..., 3])
+    return t
+
+
+def batch_views(n=64, seed=900):
+    """(volume index, (width, height), srm, lit) per view, seeded."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(0, len(BATCH_VOLUMES))),
+             BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))],
+             float(rng.choice([0.5, 1.0, 2.0])), bool(rng.integers(0, 2))) for _ in range(n)]
+
+
 def numpy_blob_volume(dims, dtype, n_blobs, sigma, peak, vmax, seed, noise=0):
     """Small CPU-made volume for tests (input creation only): [z, y, x] array."""
     rng = np.random.default_rng(seed)
