@@ -50,6 +50,12 @@ def parse():
     p.add_argument("--no-batching", action="store_true",
                    help="skip the 64-view batched-paint measurement")
     p.add_argument("--batch-steps", type=int, default=10)
+    p.add_argument("--no-learned", action="store_true",
+                   help="skip the learned-reconstruction measurement")
+    p.add_argument("--judge-db", type=float, default=38.0,
+                   help="probe-ray judge: fall back below this probe PSNR")
+    p.add_argument("--learned-quality-poses", type=int, default=24)
+    p.add_argument("--learned-ssim-poses", type=int, default=6)
     p.add_argument("--frame-ert", type=float, default=1.0)
     return p.parse_args()
 
@@ -338,6 +344,92 @@ def run_batching(args, torch, steps):
                     "independent = tvk_paint per renderer, each on its own stream"}
 
 
+def ssim_rgb(a, b):
+    """Mean SSIM over the RGB channels (Gaussian window sigma 1.5, data range 1)."""
+    from scipy.ndimage import gaussian_filter
+    c1, c2 = 0.01 ** 2, 0.03 ** 2
+    vals = []
+    for ch in range(3):
+        x, y = a[..., ch].astype(np.float64), b[..., ch].astype(np.float64)
+        mx, my = gaussian_filter(x, 1.5), gaussian_filter(y, 1.5)
+        sxx = gaussian_filter(x * x, 1.5) - mx * mx
+        syy = gaussian_filter(y * y, 1.5) - my * my
+        sxy = gaussian_filter(x * y, 1.5) - mx * my
+        vals.append(np.mean(((2 * mx * my + c1) * (2 * sxy + c2)) /
+                            ((mx * mx + my * my + c1) * (sxx + syy + c2))))
+    return float(np.mean(vals))
+
+
+def run_learned(args, torch, r, w, poses, plain_fps):
+    """tvk_paint_learned on the same volume, TF and poses as the plain frames:
+    frame rate (blocking, judge included), quality against the plain render and
+    the method without the network (bilinear upscale of the half-resolution,
+    half-rate frame), and the probe judge's fallback rate."""
+    from tuvok_gb300.learned import WEIGHTS, LearnedRenderer, UNet, psnr
+    if not WEIGHTS.exists():
+        return {"unavailable": "no trained weights in tuvok_gb300/weights"}
+    net = LearnedRenderer(UNet.load_params())
+    thr = args.judge_db
+
+    def frame(i):
+        eye, at, up = poses[i % len(poses)]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        return net.Paint(r, thr)
+
+    for i in range(args.warmup):
+        frame(i)
+    torch.cuda.synchronize()
+    K = args.steps
+    infos = []
+    t0 = time.perf_counter()
+    for i in range(K):
+        infos.append(frame(args.warmup + i))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    fps = K / wall
+    # quality on a subset of the timed poses (untimed)
+    n_q = min(K, args.learned_quality_poses)
+    ps_l, ps_b, ss_l, ss_b, probe = [], [], [], [], []
+    for i in range(n_q):
+        eye, at, up = poses[(args.warmup + i) % len(poses)]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        info = net.Paint(r, -1.0)  # the network's frame, never replaced
+        learned = r.ReadBackPixels().copy()
+        probe.append(info.probe_psnr_db)
+        r.SetReducedQuality(True, True)
+        r.Paint()
+        bilinear = r.ReadBackPixels().copy()
+        r.SetReducedQuality(False, False)
+        r.Paint()
+        plain = r.ReadBackPixels().copy()
+        ps_l.append(psnr(float(np.mean((learned - plain) ** 2))))
+        ps_b.append(psnr(float(np.mean((bilinear - plain) ** 2))))
+        if i < args.learned_ssim_poses:
+            ss_l.append(ssim_rgb(learned, plain))
+            ss_b.append(ssim_rgb(bilinear, plain))
+    fell = sum(x.fell_back for x in infos)
+    return {
+        "value": fps, "unit": "frames/s", "vs_plain": fps / plain_fps,
+        "ms_per_frame": 1000.0 * wall / K,
+        "gpu_ms": {k: float(np.median([getattr(x, k) for x in infos]))
+                   for k in ("ms_reduced", "ms_network", "ms_probe", "ms_fallback")},
+        "reduced": [int(infos[0].reduced_width), int(infos[0].reduced_height)],
+        "judge_threshold_db": thr, "fallback_rate": fell / K,
+        "psnr_db": {"learned_mean": float(np.mean(ps_l)), "learned_min": float(np.min(ps_l)),
+                    "bilinear_mean": float(np.mean(ps_b)), "probe_mean": float(np.mean(probe)),
+                    "poses": n_q},
+        "ssim": {"learned_mean": float(np.mean(ss_l)), "bilinear_mean": float(np.mean(ss_b)),
+                 "poses": len(ss_l)},
+        "network": {"params": 300032, "dtype": "bf16 weights/activations, fp32 accumulate",
+                    "weights": "tuvok_gb300/weights/recon_unet.npz (trained on the GPU by "
+                               "tuvok_gb300.learned on 8 seeded volumes 256^3..1024^3, random "
+                               "cameras, perturbed TFs; none is this volume)"},
+        "note": "quality = whole 1920x1080 RGBA frame vs the plain render of the same pose "
+                "(network frame, before any fallback); frame rate with the probe judge "
+                "(1 full-quality ray per 8x8 block) and its fallbacks included",
+    }
+
+
 def run_ours(args):
     import torch
     from tuvok_gb300 import Renderer
@@ -425,6 +517,10 @@ def run_ours(args):
     h2d = int(np.mean(vis)) * dev_brick_bytes
     d2h = w.width * w.height * 16 + 32
 
+    learned = None
+    if not args.no_learned:
+        learned = run_learned(args, torch, r, w, poses, value)
+
     batching = None
     if not args.no_batching:
         del r
@@ -478,6 +574,7 @@ def run_ours(args):
             "gpu_launches": K,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
+            "learned": learned,
             "batching": batching,
         }
         print(json.dumps(line), flush=True)

@@ -383,6 +383,119 @@ tvk_status tvk_paint_batch(tvk_batch* b, tvk_renderer* const* renderers, uint32_
 tvk_status tvk_batch_set_autotune(tvk_batch* b, int autotune, uint32_t ctas_per_sm);
 tvk_status tvk_batch_get_info(tvk_batch* b, tvk_batch_info* out);
 
+/* ---- Learned reconstruction primitives (no counterpart in the reference; the
+ * network replaces its progressive reduced-quality frames, a25 above) ----
+ *
+ * Device pointers throughout; `stream` is a cudaStream_t (NULL = default).
+ * Activations are NHWC BF16; a layer's weights are [tap = ky*3+kx][cout][cin]
+ * (FP32 masters, BF16 copies for the kernels).  Convolutions run on the tensor
+ * cores with FP32 accumulation. */
+
+typedef struct tvk_cnn_conv {
+  const void* x1;        /* BF16 input [n][h][w][c1] */
+  const void* x2;        /* optional second input concatenated after x1 [n][h][w][c2] */
+  int c1, c2;            /* c1 + c2 a multiple of 16, at most 128 */
+  int n, h, w;           /* output size equals input size (padding 1) */
+  const void* weights;   /* BF16 [9][cout][c1 + c2] */
+  const float* bias;     /* [cout] or NULL */
+  int cout;              /* a multiple of 8 in 8..128, 8 | 16 | 32 | 48 | ... */
+  float slope;           /* LeakyReLU slope; negative: no activation */
+  void* y_bf16;          /* BF16 output [n][h][w][cout] or NULL */
+  float* y_f32;          /* FP32 output (channels < split) or NULL */
+  float* y2_f32;         /* FP32 output of channels >= split, or NULL (no split) */
+  int split;
+  int accumulate;        /* FP32 outputs: add to the values there */
+} tvk_cnn_conv;
+
+typedef struct tvk_cnn_wgrad {
+  const void* x1;        /* forward input(s), BF16 */
+  const void* x2;
+  int c1, c2;
+  const void* gy;        /* BF16 gradient at the pre-activation output [n][h][w][cout] */
+  int n, h, w, cout;
+  float* dw;             /* FP32 [9][cout][c1 + c2], accumulated */
+  float* db;             /* FP32 [cout], accumulated, or NULL */
+} tvk_cnn_wgrad;
+
+/* y = act(conv3x3(concat(x1, x2), W) + b), zero padding (forward); with the
+ * flipped-transposed weights of tvk_cnn_weights_bf16 it is the data gradient. */
+tvk_status tvk_cnn_conv3x3(const tvk_cnn_conv* args, void* stream);
+/* dW += sum_p G[p] (x) X[p + tap], db += sum_p G[p]. */
+tvk_status tvk_cnn_conv3x3_wgrad(const tvk_cnn_wgrad* args, void* stream);
+/* G = dY * LeakyReLU'(Y) as BF16 (y = NULL or slope < 0: G = dY). */
+tvk_status tvk_cnn_act_grad(const float* dy, const void* y, float slope, void* g_bf16, size_t n,
+                            void* stream);
+tvk_status tvk_cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, void* stream);
+tvk_status tvk_cnn_avgpool2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                                     int accumulate, void* stream);
+tvk_status tvk_cnn_upsample2(const void* x, int n, int h, int w, int c, void* y, void* stream);
+tvk_status tvk_cnn_upsample2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                                      void* stream);
+/* out [n][2h][2w][4] = base + pixel-shuffled head [n][h][w][16] (FP32). */
+tvk_status tvk_cnn_head(const float* head, const float* base, int n, int h, int w, float* out,
+                        void* stream);
+tvk_status tvk_cnn_head_backward(const float* dout, int n, int h, int w, float* dhead,
+                                 void* stream);
+/* *loss += mean((out - target)^2); dout = 2 (out - target) / n (dout may be NULL). */
+tvk_status tvk_cnn_mse(const float* out, const float* target, size_t n, float* dout, float* loss,
+                       void* stream);
+/* Adam step `step` (1-based) on FP32 weights. */
+tvk_status tvk_cnn_adam(float* w, const float* g, float* m, float* v, size_t n, float lr, float b1,
+                        float b2, float eps, int step, void* stream);
+/* BF16 copies of a layer's FP32 weights: forward [9][cout][cin] and (if bwd is
+ * not NULL) backward-data [9][cin][cout] with flipped taps. */
+tvk_status tvk_cnn_weights_bf16(const float* w, int cout, int cin, void* fwd, void* bwd,
+                                void* stream);
+tvk_status tvk_cnn_to_bf16(const float* x, size_t n, void* y, void* stream);
+
+/* Network input of a reduced frame: RGBA of the w x h image (FP32 [h][w][4]) in
+ * channels 0..3, zero elsewhere and in the padding up to wp x hp, as BF16
+ * [hp][wp][16]. */
+tvk_status tvk_cnn_prepare_input(const float* image_rgba, int h, int w, int hp, int wp, void* out,
+                                 void* stream);
+
+/* ---- Learned reconstruction (replaces the reference's progressive reduced-
+ * quality frames, AbstrRenderer.cpp:681-787 and GLRenderer.cpp:717-747) ----
+ *
+ * The network: a fixed 4-level U-Net of 11 3x3 convolutions (LeakyReLU 0.1):
+ * e0a 16->32, e0b 32->32 | pool | e1a 32->48, e1b 48->48 | pool | e2a 48->64,
+ * e2b 64->64 | pool | b 64->64 | up, d2 (64+64)->64 | up, d1 (64+48)->48 | up,
+ * d0 (48+32)->32 | head 32->16 (no activation), whose 16 channels are RGBA x
+ * 2x2 sub-pixels added to the bilinear upscale of the reduced frame. */
+
+typedef struct tvk_learned tvk_learned;
+
+typedef struct tvk_learned_info {
+  float probe_psnr_db;           /* PSNR of the frame at the probe pixels */
+  int fell_back;                 /* 1: the plain full-quality frame was rendered */
+  float ms_reduced;              /* reduced frame + bilinear upscale */
+  float ms_network;              /* input preparation + U-Net */
+  float ms_probe;                /* probe rays + their comparison */
+  float ms_fallback;             /* the plain frame when falling back, else ~0 */
+  uint32_t reduced_width, reduced_height;
+} tvk_learned_info;
+
+/* Number of FP32 parameters: per layer in the order above, the weights
+ * [9][cout][cin] followed by the bias [cout]. */
+tvk_status tvk_learned_param_count(size_t* n);
+tvk_status tvk_learned_create(const float* host_params, size_t n, tvk_learned** out);
+tvk_status tvk_learned_destroy(tvk_learned* net);
+
+/* One learned frame on the renderer (its volume, TF, lighting, view and
+ * viewport): the frame at half resolution and half sample rate (as
+ * tvk_set_reduced_quality), its bilinear upscale plus the network's residual
+ * as the image, then the probe-ray judge: one pixel of every 8x8 block is ray
+ * marched at full quality and compared; below threshold_db of probe PSNR the
+ * plain full-quality frame replaces the result.  Blocking (the judge reads its
+ * error back). */
+tvk_status tvk_paint_learned(tvk_renderer* r, tvk_learned* net, float threshold_db,
+                             tvk_learned_info* info);
+
+/* Copies the last final image (reduced = 0, width*height*4 floats) or the last
+ * ray-marched reduced image (reduced = 1, render size) to device memory, on the
+ * renderer's stream. */
+tvk_status tvk_copy_image_device(tvk_renderer* r, int reduced, void* dst, size_t bytes);
+
 /* Size of the last ray-marched image (the viewport, or the reduced one). */
 tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* height);
 

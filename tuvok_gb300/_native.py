@@ -59,6 +59,26 @@ class BatchInfo(C.Structure):
                 ("graph_reused", C.c_int), ("autotuned", C.c_int), ("ms", C.c_float)]
 
 
+class CnnConv(C.Structure):
+    _fields_ = [("x1", C.c_void_p), ("x2", C.c_void_p), ("c1", C.c_int), ("c2", C.c_int),
+                ("n", C.c_int), ("h", C.c_int), ("w", C.c_int), ("weights", C.c_void_p),
+                ("bias", C.c_void_p), ("cout", C.c_int), ("slope", C.c_float),
+                ("y_bf16", C.c_void_p), ("y_f32", C.c_void_p), ("y2_f32", C.c_void_p),
+                ("split", C.c_int), ("accumulate", C.c_int)]
+
+
+class CnnWgrad(C.Structure):
+    _fields_ = [("x1", C.c_void_p), ("x2", C.c_void_p), ("c1", C.c_int), ("c2", C.c_int),
+                ("gy", C.c_void_p), ("n", C.c_int), ("h", C.c_int), ("w", C.c_int),
+                ("cout", C.c_int), ("dw", C.c_void_p), ("db", C.c_void_p)]
+
+
+class LearnedInfo(C.Structure):
+    _fields_ = [("probe_psnr_db", C.c_float), ("fell_back", C.c_int), ("ms_reduced", C.c_float),
+                ("ms_network", C.c_float), ("ms_probe", C.c_float), ("ms_fallback", C.c_float),
+                ("reduced_width", C.c_uint32), ("reduced_height", C.c_uint32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
                 ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
@@ -118,6 +138,26 @@ PROTOTYPES = {
     "tvk_compute_min_lod": [_vp, _u32p],
     "tvk_paint_progressive": [_vp, C.c_int, C.POINTER(SubframeInfo)],
     "tvk_get_render_size": [_vp, _u32p, _u32p],
+    "tvk_cnn_conv3x3": [C.POINTER(CnnConv), _vp],
+    "tvk_cnn_conv3x3_wgrad": [C.POINTER(CnnWgrad), _vp],
+    "tvk_cnn_act_grad": [_vp, _vp, C.c_float, _vp, C.c_size_t, _vp],
+    "tvk_cnn_avgpool2": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_avgpool2_backward": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp],
+    "tvk_cnn_upsample2": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_upsample2_backward": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_head": [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_head_backward": [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_mse": [_vp, _vp, C.c_size_t, _vp, _vp, _vp],
+    "tvk_cnn_adam": [_vp, _vp, _vp, _vp, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float,
+                     C.c_int, _vp],
+    "tvk_cnn_weights_bf16": [_vp, C.c_int, C.c_int, _vp, _vp, _vp],
+    "tvk_cnn_to_bf16": [_vp, C.c_size_t, _vp, _vp],
+    "tvk_cnn_prepare_input": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_learned_param_count": [C.POINTER(C.c_size_t)],
+    "tvk_learned_create": [_f32p, C.c_size_t, C.POINTER(_vp)],
+    "tvk_learned_destroy": [_vp],
+    "tvk_paint_learned": [_vp, _vp, C.c_float, C.POINTER(LearnedInfo)],
+    "tvk_copy_image_device": [_vp, C.c_int, _vp, C.c_size_t],
     "tvk_batch_create": [C.POINTER(_vp)],
     "tvk_batch_destroy": [_vp],
     "tvk_paint_batch": [_vp, C.POINTER(_vp), C.c_uint32],

@@ -545,16 +545,26 @@ struct tvk_renderer {
   double model[3][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}};
   uint32_t width = 0, height = 0;
   // device buffers
-  tvk::DevBuf d_img, d_spp, d_bricks, d_tf, d_tfcol, d_counters;
+  tvk::DevBuf d_img, d_spp, d_bricks, d_counters;
   tvk::PinnedBuf h_bricks, h_counters;
   tvk::PinnedBuf h_tf;
-  float tf_step_scale = -1.0f;  // step scale the device table was built for
   // empty-cell bits for the current TF and volume
-  tvk::DevBuf d_empty, d_empty_meta, d_tfpfx;
-  std::vector<uint64_t> empty_word_off;
-  bool empty_valid = false;
-  bool empty_iso = false;
-  float empty_iso_norm = 0.0f;
+  // Device TF tables (opacity-corrected for one step scale) and the empty-cell
+  // bits made from them; two slots, so frames that alternate sample rates
+  // (reduced and full quality) rebuild nothing
+  struct TfSlot {
+    float step_scale = -1.0f;
+    bool valid = false;
+    uint64_t used = 0;
+    tvk::DevBuf d_tf, d_tfcol, d_tfpfx, d_empty, d_empty_meta;
+    std::vector<uint64_t> empty_word_off;
+    bool empty_valid = false;
+    bool empty_iso = false;
+    float empty_iso_norm = 0.0f;
+  };
+  TfSlot slots[2];
+  int slot = 0;
+  uint64_t slot_clock = 0;
   float iso_color[3] = {0.5f, 0.5f, 0.5f};  // AbstrRenderer.cpp:86 m_vIsoColor
   bool cell_skip = true;
   tvk_stats stats{};
@@ -604,11 +614,60 @@ struct tvk_batch {
   tvk_batch_info info{};
 };
 
+// The reconstruction network: a fixed 4-level U-Net over the reduced frame.
+namespace tvk {
+struct UNetLayer {
+  const char* name;
+  int c1, c2, cout;
+  float slope;  // LeakyReLU slope, < 0: none
+};
+// e*: encoder (two convolutions per level, 2x2 average pooling between levels),
+// b: bottleneck, d*: decoder (2x nearest upsampling, then one convolution over
+// the upsampled tensor concatenated with the encoder's skip tensor), head: 16
+// channels = RGBA x 2x2 sub-pixels added to the bilinear upscale.
+constexpr UNetLayer kUNet[] = {
+    {"e0a", 16, 0, 32, 0.1f}, {"e0b", 32, 0, 32, 0.1f}, {"e1a", 32, 0, 48, 0.1f},
+    {"e1b", 48, 0, 48, 0.1f}, {"e2a", 48, 0, 64, 0.1f}, {"e2b", 64, 0, 64, 0.1f},
+    {"b", 64, 0, 64, 0.1f},   {"d2", 64, 64, 64, 0.1f}, {"d1", 64, 48, 48, 0.1f},
+    {"d0", 48, 32, 32, 0.1f}, {"head", 32, 0, 16, -1.0f}};
+constexpr int kUNetLayers = int(sizeof(kUNet) / sizeof(kUNet[0]));
+inline size_t unet_param_count() {
+  size_t n = 0;
+  for (const UNetLayer& l : kUNet) n += size_t(9) * l.cout * (l.c1 + l.c2) + l.cout;
+  return n;
+}
+}  // namespace tvk
+
+struct tvk_learned {
+  int device = 0;
+  tvk::DevBuf d_w, d_b;                    // BF16 weights, FP32 biases (all layers)
+  size_t w_off[tvk::kUNetLayers] = {}, b_off[tvk::kUNetLayers] = {};
+  tvk::DevBuf d_act, d_head, d_input, d_sum;
+  int hp = 0, wp = 0;
+  tvk::PinnedBuf h_sum;
+  cudaEvent_t ev[5] = {};
+  uint32_t frame = 0;
+};
+
 namespace tvk {
 namespace {
 
 void upload_tf(tvk_renderer* R, float step_scale) {
-  if (!R->tf_dirty && R->tf_step_scale == step_scale) return;
+  if (R->tf_dirty) {
+    for (auto& sl : R->slots) sl.valid = false;
+    R->tf_dirty = false;
+  }
+  for (int i = 0; i < 2; ++i)
+    if (R->slots[i].valid && R->slots[i].step_scale == step_scale) {
+      R->slot = i;
+      R->slots[i].used = ++R->slot_clock;
+      return;
+    }
+  // rebuild the least recently used slot
+  const int si = (!R->slots[0].valid || (R->slots[1].valid && R->slots[0].used <= R->slots[1].used))
+                     ? 0 : 1;
+  R->slot = si;
+  tvk_renderer::TfSlot& S = R->slots[si];
   const size_t n = size_t(R->tf_w) * R->tf_h;
   // the previous upload may still be reading the staging buffer
   TVK_CUDA(cudaStreamSynchronize(R->stream));
@@ -626,61 +685,63 @@ void upload_tf(tvk_renderer* R, float step_scale) {
     // a sample whose corrected alpha is exactly 0 adds exactly nothing
     if (t[4 * i + 3] != 0.0f) col[i % R->tf_w] = 1;
   }
-  R->d_tf.ensure(n * sizeof(float4));
-  R->d_tfcol.ensure(R->tf_w);
-  TVK_CUDA(cudaMemcpyAsync(R->d_tf.p, t, n * sizeof(float4), cudaMemcpyHostToDevice, R->stream));
-  TVK_CUDA(cudaMemcpyAsync(R->d_tfcol.p, col, R->tf_w, cudaMemcpyHostToDevice, R->stream));
+  S.d_tf.ensure(n * sizeof(float4));
+  S.d_tfcol.ensure(R->tf_w);
+  TVK_CUDA(cudaMemcpyAsync(S.d_tf.p, t, n * sizeof(float4), cudaMemcpyHostToDevice, R->stream));
+  TVK_CUDA(cudaMemcpyAsync(S.d_tfcol.p, col, R->tf_w, cudaMemcpyHostToDevice, R->stream));
   // prefix counts of value columns with any non-zero corrected alpha
   std::vector<uint32_t> pfx(R->tf_w + 1, 0);
   for (uint32_t x = 0; x < R->tf_w; ++x) pfx[x + 1] = pfx[x] + (col[x] ? 1u : 0u);
-  R->d_tfpfx.ensure(pfx.size() * sizeof(uint32_t));
-  TVK_CUDA(cudaMemcpy(R->d_tfpfx.p, pfx.data(), pfx.size() * sizeof(uint32_t),
+  S.d_tfpfx.ensure(pfx.size() * sizeof(uint32_t));
+  TVK_CUDA(cudaMemcpy(S.d_tfpfx.p, pfx.data(), pfx.size() * sizeof(uint32_t),
                       cudaMemcpyHostToDevice));
-  R->tf_dirty = false;
-  R->tf_step_scale = step_scale;
-  R->empty_valid = false;
+  S.valid = true;
+  S.step_scale = step_scale;
+  S.used = ++R->slot_clock;
+  S.empty_valid = false;
 }
 
 // Empty-cell bits of every brick of every built LOD for the current TF (re-run
 // when the TF, the opacity correction or the volume changes).
 void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale, bool iso_mode,
                         float iso_norm) {
-  if (R->empty_valid && R->empty_iso == iso_mode && (!iso_mode || R->empty_iso_norm == iso_norm))
+  tvk_renderer::TfSlot& S = R->slots[R->slot];
+  if (S.empty_valid && S.empty_iso == iso_mode && (!iso_mode || S.empty_iso_norm == iso_norm))
     return;
   // every built LOD's bricks, indexed by TOC position
   const uint64_t nb = V->total_bricks;
-  R->empty_word_off.resize(nb);
+  S.empty_word_off.resize(nb);
   uint64_t words = 0;
   uint32_t max_words = 0;
   for (uint64_t k = 0; k < nb; ++k) {
-    R->empty_word_off[k] = words;
+    S.empty_word_off[k] = words;
     const uint32_t w = (V->cell_counts[k] + 31) / 32;
     words += w;
     max_words = std::max(max_words, w);
   }
-  R->d_empty.ensure(std::max<uint64_t>(1, words) * sizeof(uint32_t));
-  R->d_empty_meta.ensure(nb * sizeof(uint64_t));
-  TVK_CUDA(cudaMemcpyAsync(R->d_empty_meta.p, R->empty_word_off.data(), nb * sizeof(uint64_t),
+  S.d_empty.ensure(std::max<uint64_t>(1, words) * sizeof(uint32_t));
+  S.d_empty_meta.ensure(nb * sizeof(uint64_t));
+  TVK_CUDA(cudaMemcpyAsync(S.d_empty_meta.p, S.empty_word_off.data(), nb * sizeof(uint64_t),
                            cudaMemcpyHostToDevice, R->stream));
   EmptyCellParams p;
   p.cell_minmax = static_cast<const uint32_t*>(V->d_cells);
   p.cell_offsets = static_cast<const uint64_t*>(V->d_cell_meta);
   p.cell_counts = reinterpret_cast<const uint32_t*>(p.cell_offsets + nb);
-  p.word_offsets = R->d_empty_meta.as<uint64_t>();
+  p.word_offsets = S.d_empty_meta.as<uint64_t>();
   p.n_bricks = nb;
-  p.nz_prefix = R->d_tfpfx.as<uint32_t>();
+  p.nz_prefix = S.d_tfpfx.as<uint32_t>();
   p.tf_w = R->tf_w;
   p.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
   p.trans_scale = trans_scale;
   p.iso_mode = iso_mode ? 1 : 0;
   p.iso_norm = iso_norm;
-  p.bits = R->d_empty.as<uint32_t>();
+  p.bits = S.d_empty.as<uint32_t>();
   launch_empty_cells(p, max_words, R->stream, &R->launches);
   // the word offsets above were copied from pageable memory; keep them alive
   TVK_CUDA(cudaStreamSynchronize(R->stream));
-  R->empty_valid = true;
-  R->empty_iso = iso_mode;
-  R->empty_iso_norm = iso_norm;
+  S.empty_valid = true;
+  S.empty_iso = iso_mode;
+  S.empty_iso_norm = iso_norm;
 }
 
 void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgba8) {
@@ -850,7 +911,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
     b.step = stp;
     b.off = V->offsets[k];
     b.cells = V->cell_dims[k];
-    b.empty_off = R->cell_skip ? R->empty_word_off[k] : 0;
+    b.empty_off = R->cell_skip ? R->slots[R->slot].empty_word_off[k] : 0;
   }
   R->d_bricks.ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
   if (nvis)
@@ -864,14 +925,14 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
   P.bytes = V->bytes;
   P.bricks = R->d_bricks.as<DevBrick>();
   P.n_bricks = nvis;
-  P.tf = R->d_tf.as<float4>();
-  P.tf_col_nonzero = R->d_tfcol.as<uint8_t>();
+  P.tf = R->slots[R->slot].d_tf.as<float4>();
+  P.tf_col_nonzero = R->slots[R->slot].d_tfcol.as<uint8_t>();
   P.tf_w = R->tf_w;
   P.tf_h = R->tf_h;
   P.mode = R->mode;
   P.lighting = R->lighting ? 1 : 0;
   P.light_model = R->light_model;
-  P.empty_bits = R->cell_skip ? R->d_empty.as<uint32_t>() : nullptr;
+  P.empty_bits = R->cell_skip ? R->slots[R->slot].d_empty.as<uint32_t>() : nullptr;
   P.trans_scale = trans_scale;
   const float mg = float(V->max_grad);
   P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;  // GLRenderer.cpp:1840-1841
@@ -907,6 +968,10 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
   P.max_q = 1.0e6f;
   P.width = rw;
   P.height = rh;
+  P.out_w = rw;
+  P.out_h = rh;
+  P.stride = 1;
+  P.off_x = P.off_y = 0;
   const size_t npix = size_t(R->width) * R->height;
   R->d_img.ensure(npix * sizeof(float4));
   R->d_spp.ensure(size_t(rw) * rh * sizeof(uint32_t));
@@ -1134,7 +1199,7 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
       BatchLaunch& L = B->launch.back();
       L.frames[L.n_frames] = F[i].P;
       L.tile_first[L.n_frames + 1] =
-          L.tile_first[L.n_frames] + ((F[i].rw + 15) / 16) * ((F[i].rh + 7) / 8);
+          L.tile_first[L.n_frames] + ((F[i].P.out_w + 15) / 16) * ((F[i].P.out_h + 7) / 8);
       L.n_frames++;
     }
   }
@@ -1274,6 +1339,145 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
   B->info.launches = uint32_t(nl);
   B->info.graph_reused = reused ? 1 : 0;
   B->info.autotuned = tuned_now ? 1 : 0;
+}
+
+// The U-Net over the reduced frame's 16-channel input (BF16 [hp][wp][16]); the
+// head's residual is added to the full-resolution base image in place.
+void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int out_w,
+              cudaStream_t s) {
+  const int h0 = N->hp, w0 = N->wp;
+  const size_t px0 = size_t(h0) * w0, px1 = px0 / 4, px2 = px0 / 16, px3 = px0 / 64;
+  // activation buffers (BF16 elements), carved from one allocation
+  const size_t sizes[] = {px0 * 32, px0 * 32, px1 * 32, px1 * 48, px1 * 48, px2 * 48, px2 * 64,
+                          px2 * 64, px3 * 64, px3 * 64, px2 * 64, px2 * 64, px1 * 64, px1 * 48,
+                          px0 * 48, px0 * 32};
+  size_t total = 0;
+  for (size_t z : sizes) total += (z + 127) / 128 * 128;
+  N->d_act.ensure(total * 2);
+  N->d_head.ensure(px0 * 16 * sizeof(float));
+  void* buf[16];
+  size_t off = 0;
+  for (int i = 0; i < 16; ++i) {
+    buf[i] = static_cast<uint8_t*>(N->d_act.p) + off * 2;
+    off += (sizes[i] + 127) / 128 * 128;
+  }
+  void *a0 = buf[0], *s0 = buf[1], *p0 = buf[2], *a1 = buf[3], *s1 = buf[4], *p1 = buf[5];
+  void *a2 = buf[6], *s2 = buf[7], *p2 = buf[8], *bt = buf[9], *u2 = buf[10], *d2 = buf[11];
+  void *u1 = buf[12], *d1 = buf[13], *u0 = buf[14], *d0 = buf[15];
+  auto conv = [&](int li, const void* x1, const void* x2, int h, int w, void* ybf, float* yf) {
+    const UNetLayer& L = kUNet[li];
+    CnnConv c{};
+    c.x1 = x1;
+    c.x2 = x2;
+    c.c1 = L.c1;
+    c.c2 = L.c2;
+    c.n = 1;
+    c.h = h;
+    c.w = w;
+    c.weights = static_cast<const uint16_t*>(N->d_w.p) + N->w_off[li];
+    c.bias = N->d_b.as<float>() + N->b_off[li];
+    c.cout = L.cout;
+    c.slope = L.slope;
+    c.y_bf16 = ybf;
+    c.y_f32 = yf;
+    c.split = L.cout;
+    cnn_conv3x3(c, s);
+  };
+  conv(0, x16, nullptr, h0, w0, a0, nullptr);
+  conv(1, a0, nullptr, h0, w0, s0, nullptr);
+  cnn_avgpool2(s0, 1, h0, w0, 32, p0, s);
+  conv(2, p0, nullptr, h0 / 2, w0 / 2, a1, nullptr);
+  conv(3, a1, nullptr, h0 / 2, w0 / 2, s1, nullptr);
+  cnn_avgpool2(s1, 1, h0 / 2, w0 / 2, 48, p1, s);
+  conv(4, p1, nullptr, h0 / 4, w0 / 4, a2, nullptr);
+  conv(5, a2, nullptr, h0 / 4, w0 / 4, s2, nullptr);
+  cnn_avgpool2(s2, 1, h0 / 4, w0 / 4, 64, p2, s);
+  conv(6, p2, nullptr, h0 / 8, w0 / 8, bt, nullptr);
+  cnn_upsample2(bt, 1, h0 / 8, w0 / 8, 64, u2, s);
+  conv(7, u2, s2, h0 / 4, w0 / 4, d2, nullptr);
+  cnn_upsample2(d2, 1, h0 / 4, w0 / 4, 64, u1, s);
+  conv(8, u1, s1, h0 / 2, w0 / 2, d1, nullptr);
+  cnn_upsample2(d1, 1, h0 / 2, w0 / 2, 48, u0, s);
+  conv(9, u0, s0, h0, w0, d0, nullptr);
+  conv(10, d0, nullptr, h0, w0, nullptr, N->d_head.as<float>());
+  cnn_head(N->d_head.as<float>(), base_out, 1, h0, w0, out_h, out_w, base_out, s);
+}
+
+// One learned frame: the reduced frame (half resolution, half sample rate) and
+// its bilinear upscale, the network's residual added to it, then 1/64 of the
+// pixels marched at full quality as probes; below threshold_db of probe PSNR
+// the frame falls back to the plain full-quality render.
+void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_learned_info* info) {
+  if (R->device != N->device) fail(TVK_ERR_INVALID_ARG, "renderer and network on other devices");
+  TVK_CUDA(cudaSetDevice(R->device));
+  const float saved_dec = R->screen_dec, saved_sdec = R->sample_dec;
+  R->screen_dec = 2.0f;
+  R->sample_dec = 2.0f;
+  cudaStream_t s = R->stream;
+  TVK_CUDA(cudaEventRecord(N->ev[0], s));
+  PlannedFrame low;
+  try {
+    low = plan_frame(R, Subframe{0, true, true});
+  } catch (...) {
+    R->screen_dec = saved_dec;
+    R->sample_dec = saved_sdec;
+    throw;
+  }
+  launch_raycast(low.P, s, &R->launches);
+  launch_upscale_of(R, low, s, &R->launches);
+  R->screen_dec = saved_dec;
+  R->sample_dec = saved_sdec;
+  TVK_CUDA(cudaEventRecord(N->ev[1], s));
+  const float* lowimg = low.upscale ? R->d_lowimg.as<float>() : R->d_img.as<float>();
+  N->hp = int((low.rh + 7) / 8 * 8);
+  N->wp = int((low.rw + 7) / 8 * 8);
+  if (2 * N->hp < int(R->height) || 2 * N->wp < int(R->width))
+    fail(TVK_ERR_INTERNAL, "reduced frame smaller than half the viewport");
+  DevBuf& x16 = N->d_input;
+  x16.ensure(size_t(N->hp) * N->wp * 16 * 2);
+  cnn_prepare_input(lowimg, int(low.rh), int(low.rw), N->hp, N->wp, x16.p, s);
+  run_unet(N, x16.p, R->d_img.as<float>(), int(R->height), int(R->width), s);
+  R->launches += kUNetLayers + 8;
+  TVK_CUDA(cudaEventRecord(N->ev[2], s));
+  // probes: one pixel of every 8x8 block at full quality, offset per frame
+  const PlannedFrame full = plan_frame(R, Subframe{0, false, false});
+  const int stride = 8, ox = int((N->frame * 5u + 3u) % 8u), oy = int((N->frame * 3u + 1u) % 8u);
+  ++N->frame;
+  RenderParams P = full.P;
+  P.stride = stride;
+  P.off_x = ox;
+  P.off_y = oy;
+  P.out_w = (R->width - ox + stride - 1) / stride;
+  P.out_h = (R->height - oy + stride - 1) / stride;
+  N->d_sum.ensure(4 * P.out_w * P.out_h * sizeof(float) + 256);
+  float4* probe = reinterpret_cast<float4*>(static_cast<uint8_t*>(N->d_sum.p) + 256);
+  float* sum = N->d_sum.as<float>();
+  P.out = probe;
+  TVK_CUDA(cudaMemsetAsync(sum, 0, sizeof(float), s));
+  launch_raycast(P, s, &R->launches);
+  cnn_probe_mse(R->d_img.as<float>(), int(R->width), reinterpret_cast<const float*>(probe),
+                int(P.out_w), int(P.out_h), stride, ox, oy, sum, s);
+  N->h_sum.ensure(sizeof(float));
+  TVK_CUDA(cudaMemcpyAsync(N->h_sum.p, sum, sizeof(float), cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaEventRecord(N->ev[3], s));
+  TVK_CUDA(cudaEventSynchronize(N->ev[3]));
+  const double mse = double(*N->h_sum.as<float>()) / (4.0 * P.out_w * P.out_h);
+  const float psnr = mse > 0 ? float(10.0 * std::log10(1.0 / mse)) : 1000.0f;
+  const bool fall_back = psnr < threshold_db;
+  if (fall_back) launch_raycast(full.P, s, &R->launches);
+  TVK_CUDA(cudaEventRecord(N->ev[4], s));
+  finish_frame(R, full);
+  TVK_CUDA(cudaEventSynchronize(N->ev[4]));
+  float t[4];
+  for (int i = 0; i < 4; ++i) TVK_CUDA(cudaEventElapsedTime(&t[i], N->ev[i], N->ev[i + 1]));
+  info->probe_psnr_db = psnr;
+  info->fell_back = fall_back ? 1 : 0;
+  info->ms_reduced = t[0];
+  info->ms_network = t[1];
+  info->ms_probe = t[2];
+  info->ms_fallback = t[3];
+  info->reduced_width = low.rw;
+  info->reduced_height = low.rh;
 }
 
 }  // namespace
@@ -1532,7 +1736,7 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
     if (v && v->rebricked)
       tvk::fail(TVK_ERR_UNSUPPORTED, "rendering runs on bricked source volumes, not rebricked ones");
     r->vol = v;
-    r->empty_valid = false;
+    for (auto& sl : r->slots) sl.empty_valid = false;
     r->frame_started = false;
     // AbstrRenderer.cpp:247: m_iMaxLODIndex = GetLargestSingleBrickLOD(0)
     r->max_lod_index = 0;
@@ -1847,6 +2051,205 @@ tvk_status tvk_batch_get_info(tvk_batch* b, tvk_batch_info* out) {
     TVK_CUDA(cudaEventSynchronize(b->ev_stop));
     TVK_CUDA(cudaEventElapsedTime(&b->info.ms, b->ev_start, b->ev_stop));
     *out = b->info;
+  });
+}
+
+// ---- learned reconstruction
+
+static cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+tvk_status tvk_learned_param_count(size_t* n) {
+  return guarded([&] {
+    REQUIRE(n, "null argument");
+    *n = tvk::unet_param_count();
+  });
+}
+
+tvk_status tvk_learned_create(const float* host_params, size_t n, tvk_learned** out) {
+  return guarded([&] {
+    REQUIRE(host_params && out, "null argument");
+    REQUIRE(n == tvk::unet_param_count(), "parameter count does not match the network");
+    std::unique_ptr<tvk_learned> N(new tvk_learned());
+    TVK_CUDA(cudaGetDevice(&N->device));
+    size_t nw = 0, nb = 0;
+    for (int i = 0; i < tvk::kUNetLayers; ++i) {
+      const tvk::UNetLayer& L = tvk::kUNet[i];
+      N->w_off[i] = nw;
+      N->b_off[i] = nb;
+      nw += size_t(9) * L.cout * (L.c1 + L.c2);
+      nb += L.cout;
+    }
+    // host layout: per layer the FP32 weights [9][cout][cin] then the bias
+    std::vector<float> w(nw), b(nb);
+    size_t src = 0;
+    for (int i = 0; i < tvk::kUNetLayers; ++i) {
+      const tvk::UNetLayer& L = tvk::kUNet[i];
+      const size_t lw = size_t(9) * L.cout * (L.c1 + L.c2);
+      std::copy(host_params + src, host_params + src + lw, w.begin() + N->w_off[i]);
+      src += lw;
+      std::copy(host_params + src, host_params + src + L.cout, b.begin() + N->b_off[i]);
+      src += L.cout;
+    }
+    tvk::DevBuf d_w32;
+    d_w32.ensure(nw * sizeof(float));
+    N->d_w.ensure(nw * 2);
+    N->d_b.ensure(nb * sizeof(float));
+    TVK_CUDA(cudaMemcpy(d_w32.p, w.data(), nw * sizeof(float), cudaMemcpyHostToDevice));
+    TVK_CUDA(cudaMemcpy(N->d_b.p, b.data(), nb * sizeof(float), cudaMemcpyHostToDevice));
+    tvk::cnn_to_bf16(d_w32.as<float>(), nw, N->d_w.p, nullptr);
+    TVK_CUDA(cudaDeviceSynchronize());
+    for (cudaEvent_t& e : N->ev) TVK_CUDA(cudaEventCreate(&e));
+    *out = N.release();
+  });
+}
+
+tvk_status tvk_learned_destroy(tvk_learned* n) {
+  return guarded([&] {
+    if (!n) return;
+    for (cudaEvent_t e : n->ev)
+      if (e) cudaEventDestroy(e);
+    delete n;
+  });
+}
+
+tvk_status tvk_paint_learned(tvk_renderer* r, tvk_learned* net, float threshold_db,
+                             tvk_learned_info* info) {
+  return guarded([&] {
+    REQUIRE(r && net && info, "null argument");
+    tvk::paint_learned(r, net, threshold_db, info);
+  });
+}
+
+tvk_status tvk_cnn_prepare_input(const float* image_rgba, int h, int w, int hp, int wp, void* out,
+                                 void* stream) {
+  return guarded([&] {
+    REQUIRE(image_rgba && out && hp >= h && wp >= w, "null argument or padding too small");
+    tvk::cnn_prepare_input(image_rgba, h, w, hp, wp, out, as_stream(stream));
+  });
+}
+
+tvk_status tvk_copy_image_device(tvk_renderer* r, int reduced, void* dst, size_t bytes) {
+  return guarded([&] {
+    REQUIRE(r && dst, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    const size_t n = reduced ? size_t(r->render_w) * r->render_h * 16
+                             : size_t(r->width) * r->height * 16;
+    REQUIRE(bytes >= n, "destination smaller than the image");
+    const void* src = (reduced && (r->render_w != r->width || r->render_h != r->height))
+                          ? r->d_lowimg.p : r->d_img.p;
+    TVK_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, r->stream));
+  });
+}
+
+// ---- learned reconstruction primitives
+
+tvk_status tvk_cnn_conv3x3(const tvk_cnn_conv* a, void* stream) {
+  return guarded([&] {
+    REQUIRE(a && a->x1 && a->weights, "null argument");
+    REQUIRE(a->c2 == 0 || a->x2, "second input missing");
+    REQUIRE((a->c1 + a->c2) % 16 == 0 && a->c1 % 2 == 0 && a->c1 + a->c2 <= 128,
+            "input channels must be a multiple of 16, at most 128");
+    REQUIRE(a->cout % 8 == 0 && a->cout >= 8 && a->cout <= 128, "cout must be 8 .. 128");
+    REQUIRE(a->n >= 1 && a->h >= 1 && a->w >= 1, "empty tensor");
+    REQUIRE(a->y_bf16 || a->y_f32, "no output");
+    REQUIRE(!a->y2_f32 || (a->split > 0 && a->split < a->cout && a->y_f32), "bad split");
+    tvk::cnn_conv3x3(*a, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_conv3x3_wgrad(const tvk_cnn_wgrad* a, void* stream) {
+  return guarded([&] {
+    REQUIRE(a && a->x1 && a->gy && a->dw, "null argument");
+    REQUIRE(a->c2 == 0 || a->x2, "second input missing");
+    REQUIRE((a->c1 + a->c2) % 16 == 0 && a->c1 + a->c2 <= 128,
+            "input channels must be a multiple of 16, at most 128");
+    REQUIRE(a->cout % 8 == 0 && a->cout >= 8 && a->cout <= 64, "cout must be 8 .. 64");
+    tvk::cnn_conv3x3_wgrad(*a, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_act_grad(const float* dy, const void* y, float slope, void* g, size_t n,
+                            void* stream) {
+  return guarded([&] {
+    REQUIRE(dy && g, "null argument");
+    tvk::cnn_act_grad(dy, y, slope, g, n, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, void* stream) {
+  return guarded([&] {
+    REQUIRE(x && y && h % 2 == 0 && w % 2 == 0, "even sizes and buffers needed");
+    tvk::cnn_avgpool2(x, n, h, w, c, y, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_avgpool2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                                     int accumulate, void* stream) {
+  return guarded([&] {
+    REQUIRE(dy && dx && h % 2 == 0 && w % 2 == 0, "even sizes and buffers needed");
+    tvk::cnn_avgpool2_backward(dy, n, h, w, c, dx, accumulate, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_upsample2(const void* x, int n, int h, int w, int c, void* y, void* stream) {
+  return guarded([&] {
+    REQUIRE(x && y, "null argument");
+    tvk::cnn_upsample2(x, n, h, w, c, y, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_upsample2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                                      void* stream) {
+  return guarded([&] {
+    REQUIRE(dy && dx, "null argument");
+    tvk::cnn_upsample2_backward(dy, n, h, w, c, dx, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_head(const float* head, const float* base, int n, int h, int w, float* out,
+                        void* stream) {
+  return guarded([&] {
+    REQUIRE(head && base && out, "null argument");
+    tvk::cnn_head(head, base, n, h, w, 2 * h, 2 * w, out, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_head_backward(const float* dout, int n, int h, int w, float* dhead,
+                                 void* stream) {
+  return guarded([&] {
+    REQUIRE(dout && dhead, "null argument");
+    tvk::cnn_head_backward(dout, n, h, w, dhead, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_mse(const float* out, const float* target, size_t n, float* dout, float* loss,
+                       void* stream) {
+  return guarded([&] {
+    REQUIRE(out && target && loss && n > 0, "null argument");
+    tvk::cnn_mse(out, target, n, dout, loss, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_adam(float* w, const float* g, float* m, float* v, size_t n, float lr,
+                        float b1, float b2, float eps, int step, void* stream) {
+  return guarded([&] {
+    REQUIRE(w && g && m && v && step >= 1, "null argument or step < 1");
+    tvk::cnn_adam(w, g, m, v, n, lr, b1, b2, eps, step, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_weights_bf16(const float* w, int cout, int cin, void* fwd, void* bwd,
+                                void* stream) {
+  return guarded([&] {
+    REQUIRE(w && fwd, "null argument");
+    tvk::cnn_weights_bf16(w, cout, cin, fwd, bwd, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_to_bf16(const float* x, size_t n, void* y, void* stream) {
+  return guarded([&] {
+    REQUIRE(x && y, "null argument");
+    tvk::cnn_to_bf16(x, n, y, as_stream(stream));
   });
 }
 

@@ -1,0 +1,615 @@
+// cnn.cu -- kernels of the learned reconstruction network: 3x3 convolutions on
+// the tensor cores (BF16 operands, FP32 accumulation) forward, backward-data
+// and backward-weights, 2x2 average pooling, 2x nearest upsampling, the
+// pixel-shuffle head that adds the network's residual to the bilinear upscale
+// of the reduced frame, the loss and Adam.
+//
+// Layout: activations NHWC (channels innermost), BF16; weights of a layer as
+// [tap = ky * 3 + kx][cout][cin] (cin innermost), FP32 masters and BF16 copies.
+// A convolution is an implicit GEMM: M = output pixels, N = output channels,
+// K = 9 taps x input channels.  One CTA (4 warps) computes an 8x8 pixel patch
+// for every output channel: the 10x10 input halo and the current tap's weights
+// are staged in shared memory and each warp issues mma.sync.m16n8k16 over its
+// 16 pixels.  The skip connections of the U-Net concatenate two tensors along
+// channels; the convolution reads them in place (x1: c1 channels, x2: c2).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "tvk_internal.h"
+
+namespace tvk {
+namespace {
+
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return uint32_t(__bfloat16_as_ushort(lo)) | (uint32_t(__bfloat16_as_ushort(hi)) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// ------------------------------------------------------------- convolution
+
+// Output of a convolution: BF16 (with bias and LeakyReLU) or FP32 (optionally
+// added to what is there, for gradients that sum over several consumers), and
+// optionally split by channel into two tensors (gradients of a concatenation).
+struct ConvArgs {
+  const __nv_bfloat16* x1;
+  const __nv_bfloat16* x2;
+  int c1, c2;                 // input channels of x1, x2 (c2 may be 0)
+  int n, h, w;                // batch and spatial size (same in and out)
+  const __nv_bfloat16* wt;    // [9][cout][c1 + c2]
+  const float* bias;          // [cout] or null
+  int cout;
+  float slope;                // LeakyReLU negative slope; < 0: no activation
+  __nv_bfloat16* y_bf16;      // BF16 output [n][h][w][cout] or null
+  float* y_f32;               // FP32 output (first split) or null
+  float* y2_f32;              // FP32 output of channels >= split or null
+  int split;                  // channel where y2 starts (== cout: no split)
+  int accumulate;             // FP32 outputs: add to the existing values
+};
+
+template <int kNT>  // n-tiles of 8 output channels
+__global__ void __launch_bounds__(kThreads) conv3x3_kernel(const ConvArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int cin = a.c1 + a.c2;
+  const int cpad = cin + 8;  // row pitch of the halo (breaks bank conflicts)
+  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem_raw);       // [100][cpad]
+  __nv_bfloat16* wsm = halo + 100 * cpad;                                // [cout][cpad]
+  const int tiles_x = (a.w + 7) / 8, tiles_y = (a.h + 7) / 8;
+  const int t = blockIdx.x;
+  const int img = t / (tiles_x * tiles_y);
+  const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
+  const int y0 = ty * 8 - 1, x0 = tx * 8 - 1;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, q = lane & 3;
+
+  // 10x10 halo of the input, zero outside the image; two channels per thread step
+  const int halo_words = 100 * (cin / 2);
+  for (int i = tid; i < halo_words; i += kThreads) {
+    const int pix = i / (cin / 2), c = (i % (cin / 2)) * 2;
+    const int yy = y0 + pix / 10, xx = x0 + pix % 10;
+    uint32_t v = 0;
+    if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
+      const size_t p = (size_t(img) * a.h + yy) * a.w + xx;
+      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + p * a.c1 + c)
+                   : *reinterpret_cast<const uint32_t*>(a.x2 + p * a.c2 + (c - a.c1));
+    }
+    *reinterpret_cast<uint32_t*>(halo + pix * cpad + c) = v;
+  }
+
+  float acc[kNT][4];
+#pragma unroll
+  for (int j = 0; j < kNT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+  // this thread's two pixel rows of the warp's 16 pixels (patch rows 2w, 2w+1)
+  const int pr0 = 2 * warp, pr1 = 2 * warp + 1, pc = g;
+  const int cout_pad = kNT * 8;
+  for (int tap = 0; tap < 9; ++tap) {
+    __syncthreads();  // halo written / previous tap's weights no longer read
+    const __nv_bfloat16* wtap = a.wt + size_t(tap) * a.cout * cin;
+    for (int i = tid; i < cout_pad * (cin / 2); i += kThreads) {
+      const int co = i / (cin / 2), c = (i % (cin / 2)) * 2;
+      const uint32_t v = co < a.cout ? *reinterpret_cast<const uint32_t*>(wtap + co * cin + c) : 0u;
+      *reinterpret_cast<uint32_t*>(wsm + co * cpad + c) = v;
+    }
+    __syncthreads();
+    const int ky = tap / 3, kx = tap % 3;
+    const __nv_bfloat16* r0 = halo + ((pr0 + ky) * 10 + pc + kx) * cpad;
+    const __nv_bfloat16* r1 = halo + ((pr1 + ky) * 10 + pc + kx) * cpad;
+    for (int k0 = 0; k0 < cin; k0 += 16) {
+      uint32_t af[4];
+      af[0] = *reinterpret_cast<const uint32_t*>(r0 + k0 + 2 * q);
+      af[1] = *reinterpret_cast<const uint32_t*>(r1 + k0 + 2 * q);
+      af[2] = *reinterpret_cast<const uint32_t*>(r0 + k0 + 8 + 2 * q);
+      af[3] = *reinterpret_cast<const uint32_t*>(r1 + k0 + 8 + 2 * q);
+#pragma unroll
+      for (int j = 0; j < kNT; ++j) {
+        const __nv_bfloat16* wr = wsm + (j * 8 + g) * cpad + k0 + 2 * q;
+        mma_bf16(acc[j], af, *reinterpret_cast<const uint32_t*>(wr),
+                 *reinterpret_cast<const uint32_t*>(wr + 8));
+      }
+    }
+  }
+
+  // epilogue: rows g (pixel row pr0) and g + 8 (pixel row pr1), columns 2q, 2q+1
+  const int oy0 = ty * 8 + pr0, oy1 = ty * 8 + pr1, ox = tx * 8 + pc;
+#pragma unroll
+  for (int j = 0; j < kNT; ++j) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int oy = half ? oy1 : oy0;
+      if (oy >= a.h || ox >= a.w) continue;
+      const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = j * 8 + 2 * q + e;
+        if (co >= a.cout) continue;
+        float v = acc[j][half * 2 + e];
+        if (a.bias) v += a.bias[co];
+        if (a.slope >= 0.0f && v < 0.0f) v *= a.slope;
+        if (a.y_bf16) a.y_bf16[p * a.cout + co] = __float2bfloat16_rn(v);
+        if (co < a.split) {
+          if (a.y_f32) {
+            float* o = a.y_f32 + p * a.split + co;
+            *o = a.accumulate ? *o + v : v;
+          }
+        } else if (a.y2_f32) {
+          const int c2n = a.cout - a.split;
+          float* o = a.y2_f32 + p * c2n + (co - a.split);
+          *o = a.accumulate ? *o + v : v;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- weight gradient
+
+struct WgradArgs {
+  const __nv_bfloat16* x1;  // forward input (concatenation of x1, x2)
+  const __nv_bfloat16* x2;
+  int c1, c2;
+  const __nv_bfloat16* gy;  // gradient at the pre-activation output [n][h][w][cout]
+  int n, h, w, cout;
+  float* dw;                // [9][cout][cin], accumulated
+  float* db;                // [cout], accumulated (tap-0 CTAs only), or null
+  int patches_per_cta;
+};
+
+// dW[tap][co][ci] = sum over pixels p of G[p][co] * X[p + tap][ci]: a GEMM with
+// M = output channels, N = input channels and K = pixels.  CTA (tap, chunk)
+// walks its chunk of 8x8 patches, staging G and the tap-shifted X in shared
+// memory; warp w owns output channels 16w .. 16w+15 and all input channels.
+template <int kNT>  // n-tiles of 8 input channels
+__global__ void __launch_bounds__(kThreads) wgrad_kernel(const WgradArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int cin = a.c1 + a.c2;
+  const int gpad = a.cout + 8, xpad = cin + 8;
+  __nv_bfloat16* gs = reinterpret_cast<__nv_bfloat16*>(smem_raw);   // [64][gpad]
+  __nv_bfloat16* xs = gs + 64 * gpad;                               // [64][xpad]
+  const int tap = blockIdx.y, ky = tap / 3 - 1, kx = tap % 3 - 1;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, q = lane & 3;
+  const int tiles_x = (a.w + 7) / 8, tiles_y = (a.h + 7) / 8;
+  const int n_patches = a.n * tiles_x * tiles_y;
+  const int p_begin = blockIdx.x * a.patches_per_cta;
+  const int p_end = min(n_patches, p_begin + a.patches_per_cta);
+  const int m0 = warp * 16;
+  const bool warp_active = m0 < a.cout;
+  float acc[kNT][4];
+#pragma unroll
+  for (int j = 0; j < kNT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+  float bacc = 0.0f;  // bias gradient of channel tid (tap-0 CTAs)
+  for (int pt = p_begin; pt < p_end; ++pt) {
+    const int img = pt / (tiles_x * tiles_y);
+    const int tyy = (pt / tiles_x) % tiles_y, txx = pt % tiles_x;
+    __syncthreads();
+    for (int i = tid; i < 64 * a.cout; i += kThreads) {
+      const int pix = i / a.cout, co = i % a.cout;
+      const int yy = tyy * 8 + pix / 8, xx = txx * 8 + pix % 8;
+      __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+      if (yy < a.h && xx < a.w) v = a.gy[((size_t(img) * a.h + yy) * a.w + xx) * a.cout + co];
+      gs[pix * gpad + co] = v;
+    }
+    for (int i = tid; i < 64 * cin; i += kThreads) {
+      const int pix = i / cin, c = i % cin;
+      const int yy = tyy * 8 + pix / 8 + ky, xx = txx * 8 + pix % 8 + kx;
+      const int oy = tyy * 8 + pix / 8, ox = txx * 8 + pix % 8;
+      __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+      if (oy < a.h && ox < a.w && yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
+        const size_t p = (size_t(img) * a.h + yy) * a.w + xx;
+        v = c < a.c1 ? a.x1[p * a.c1 + c] : a.x2[p * a.c2 + (c - a.c1)];
+      }
+      xs[pix * xpad + c] = v;
+    }
+    __syncthreads();
+    if (a.db && tap == 4 && tid < a.cout)
+      for (int pix = 0; pix < 64; ++pix) bacc += __bfloat162float(gs[pix * gpad + tid]);
+    if (!warp_active) continue;
+    for (int k0 = 0; k0 < 64; k0 += 16) {
+      // A (16 x 16, m = output channel, k = pixel) from G^T
+      uint32_t af[4];
+      const int ma = m0 + g, mb = m0 + g + 8;
+      const int ka = k0 + 2 * q, kb = k0 + 8 + 2 * q;
+      auto gat = [&](int pix, int co) {
+        return co < a.cout ? gs[pix * gpad + co] : __float2bfloat16_rn(0.0f);
+      };
+      af[0] = pack_bf16(gat(ka, ma), gat(ka + 1, ma));
+      af[1] = pack_bf16(gat(ka, mb), gat(ka + 1, mb));
+      af[2] = pack_bf16(gat(kb, ma), gat(kb + 1, ma));
+      af[3] = pack_bf16(gat(kb, mb), gat(kb + 1, mb));
+#pragma unroll
+      for (int j = 0; j < kNT; ++j) {
+        const int ci = j * 8 + g;
+        const uint32_t b0 = pack_bf16(xs[ka * xpad + ci], xs[(ka + 1) * xpad + ci]);
+        const uint32_t b1 = pack_bf16(xs[kb * xpad + ci], xs[(kb + 1) * xpad + ci]);
+        mma_bf16(acc[j], af, b0, b1);
+      }
+    }
+  }
+  if (a.db && tap == 4 && tid < a.cout) atomicAdd(&a.db[tid], bacc);
+  if (!warp_active) return;
+#pragma unroll
+  for (int j = 0; j < kNT; ++j) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int co = m0 + g + (e >= 2 ? 8 : 0);
+      const int ci = j * 8 + 2 * q + (e & 1);
+      if (co < a.cout && ci < cin)
+        atomicAdd(&a.dw[(size_t(tap) * a.cout + co) * cin + ci], acc[j][e]);
+    }
+  }
+}
+
+// ------------------------------------------------------------- elementwise
+
+// G = dY * LeakyReLU'(Y) (Y > 0 exactly when the pre-activation is), as BF16
+__global__ void act_grad_kernel(const float* __restrict__ dy, const __nv_bfloat16* __restrict__ y,
+                                float slope, __nv_bfloat16* __restrict__ gout, size_t n) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const float d = dy[i];
+    const float v = (!y || slope < 0.0f || __bfloat162float(y[i]) > 0.0f) ? d : d * slope;
+    gout[i] = __float2bfloat16_rn(v);
+  }
+}
+
+__global__ void avgpool2_kernel(const __nv_bfloat16* __restrict__ x, int n, int h, int w, int c,
+                                __nv_bfloat16* __restrict__ y) {
+  const int ho = h / 2, wo = w / 2;
+  const size_t total = size_t(n) * ho * wo * c;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i % c);
+    const size_t p = i / c;
+    const int xo = int(p % wo), yo = int((p / wo) % ho), img = int(p / (size_t(wo) * ho));
+    const size_t b = ((size_t(img) * h + 2 * yo) * w + 2 * xo) * c + ch;
+    const float s = (__bfloat162float(x[b]) + __bfloat162float(x[b + c])) +
+                    (__bfloat162float(x[b + size_t(w) * c]) +
+                     __bfloat162float(x[b + size_t(w) * c + c]));
+    y[i] = __float2bfloat16_rn(s * 0.25f);
+  }
+}
+
+__global__ void avgpool2_backward_kernel(const float* __restrict__ dy, int n, int h, int w, int c,
+                                         float* __restrict__ dx, int accumulate) {
+  const size_t total = size_t(n) * h * w * c;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i % c);
+    const size_t p = i / c;
+    const int xx = int(p % w), yy = int((p / w) % h), img = int(p / (size_t(w) * h));
+    const size_t o = ((size_t(img) * (h / 2) + yy / 2) * (w / 2) + xx / 2) * c + ch;
+    const float v = dy[o] * 0.25f;
+    dx[i] = accumulate ? dx[i] + v : v;
+  }
+}
+
+__global__ void upsample2_kernel(const __nv_bfloat16* __restrict__ x, int n, int h, int w, int c,
+                                 __nv_bfloat16* __restrict__ y) {
+  const size_t total = size_t(n) * (2 * h) * (2 * w) * c;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i % c);
+    const size_t p = i / c;
+    const int xx = int(p % (2 * w)), yy = int((p / (2 * w)) % (2 * h));
+    const int img = int(p / (size_t(4) * w * h));
+    y[i] = x[((size_t(img) * h + yy / 2) * w + xx / 2) * c + ch];
+  }
+}
+
+__global__ void upsample2_backward_kernel(const float* __restrict__ dy, int n, int h, int w, int c,
+                                          float* __restrict__ dx) {
+  const size_t total = size_t(n) * h * w * c;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i % c);
+    const size_t p = i / c;
+    const int xx = int(p % w), yy = int((p / w) % h), img = int(p / (size_t(w) * h));
+    const size_t b = ((size_t(img) * 2 * h + 2 * yy) * 2 * w + 2 * xx) * c + ch;
+    const size_t r = size_t(2 * w) * c;
+    dx[i] = (dy[b] + dy[b + c]) + (dy[b + r] + dy[b + r + c]);
+  }
+}
+
+// out[Y][X][ch] = base[Y][X][ch] + head[Y/2][X/2][ch*4 + (Y%2)*2 + X%2] (pixel
+// shuffle) for the oh x ow output (at most 2h x 2w); base and out may alias
+__global__ void head_kernel(const float* __restrict__ head, const float* base, int n, int h, int w,
+                            int oh, int ow, float* out) {
+  const size_t total = size_t(n) * oh * ow * 4;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i & 3);
+    const size_t p = i >> 2;
+    const int xx = int(p % ow), yy = int((p / ow) % oh);
+    const int img = int(p / (size_t(ow) * oh));
+    const int sub = ch * 4 + (yy & 1) * 2 + (xx & 1);
+    out[i] = base[i] + head[((size_t(img) * h + yy / 2) * w + xx / 2) * 16 + sub];
+  }
+}
+
+// Network input of a reduced frame: RGBA of the w x h image in channels 0..3,
+// zero elsewhere and in the padding up to wp x hp, as BF16 [hp][wp][16]
+__global__ void prepare_input_kernel(const float4* __restrict__ img, int h, int w, int hp, int wp,
+                                     uint32_t* __restrict__ out) {
+  const size_t total = size_t(hp) * wp * 8;  // 8 words (16 BF16) per pixel
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int word = int(i & 7);
+    const size_t p = i >> 3;
+    const int xx = int(p % wp), yy = int(p / wp);
+    uint32_t v = 0;
+    if (word < 2 && xx < w && yy < h) {
+      const float4 c = img[size_t(yy) * w + xx];
+      v = word == 0 ? pack_bf16(__float2bfloat16_rn(c.x), __float2bfloat16_rn(c.y))
+                    : pack_bf16(__float2bfloat16_rn(c.z), __float2bfloat16_rn(c.w));
+    }
+    out[i] = v;
+  }
+}
+
+// Mean squared RGBA difference between the probe rays and the same pixels of a
+// frame: probe pixel (x, y) is frame pixel (x * stride + ox, y * stride + oy).
+__global__ void probe_mse_kernel(const float4* __restrict__ frame, int w,
+                                 const float4* __restrict__ probe, int pw, int ph, int stride,
+                                 int ox, int oy, float* __restrict__ sum) {
+  float s = 0.0f;
+  const int n = pw * ph;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int x = i % pw, y = i / pw;
+    const float4 a = frame[size_t(y * stride + oy) * w + x * stride + ox];
+    const float4 b = probe[i];
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+    s += (dx * dx + dy * dy) + (dz * dz + dw * dw);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sum, s);
+}
+
+__global__ void head_backward_kernel(const float* __restrict__ dout, int n, int h, int w,
+                                     float* __restrict__ dhead) {
+  const size_t total = size_t(n) * h * w * 16;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int sub = int(i & 15);
+    const size_t p = i >> 4;
+    const int xx = int(p % w), yy = int((p / w) % h), img = int(p / (size_t(w) * h));
+    const int ch = sub >> 2, dyy = (sub >> 1) & 1, dxx = sub & 1;
+    dhead[i] = dout[((size_t(img) * 2 * h + 2 * yy + dyy) * 2 * w + 2 * xx + dxx) * 4 + ch];
+  }
+}
+
+// mean squared error over all elements: loss accumulated into *loss (sum of
+// squares / n), gradient 2 (out - target) / n
+__global__ void mse_kernel(const float* __restrict__ out, const float* __restrict__ target,
+                           size_t n, float* __restrict__ dout, float* __restrict__ loss) {
+  float s = 0.0f;
+  const float inv = 1.0f / float(n);
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const float d = out[i] - target[i];
+    if (dout) dout[i] = 2.0f * d * inv;
+    s += d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv);
+}
+
+// Adam on the FP32 masters, then the BF16 copies: forward [tap][cout][cin]
+// and backward-data [8 - tap][cin][cout] (flipped taps, swapped channels)
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, size_t n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+__global__ void weights_bf16_kernel(const float* __restrict__ w, int cout, int cin,
+                                    __nv_bfloat16* __restrict__ fwd,
+                                    __nv_bfloat16* __restrict__ bwd) {
+  const size_t total = size_t(9) * cout * cin;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ci = int(i % cin), co = int((i / cin) % cout), tap = int(i / (size_t(cin) * cout));
+    const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
+    fwd[i] = b;
+    if (bwd) bwd[(size_t(8 - tap) * cin + ci) * cout + co] = b;
+  }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ x, size_t n, __nv_bfloat16* __restrict__ y) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += size_t(gridDim.x) * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+uint32_t grid_for(size_t n) {
+  const size_t b = (n + 255) / 256;
+  return uint32_t(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
+}
+
+}  // namespace
+
+void cnn_conv3x3(const CnnConv& c, cudaStream_t s) {
+  ConvArgs a{};
+  a.x1 = static_cast<const __nv_bfloat16*>(c.x1);
+  a.x2 = static_cast<const __nv_bfloat16*>(c.x2);
+  a.c1 = c.c1;
+  a.c2 = c.c2;
+  a.n = c.n;
+  a.h = c.h;
+  a.w = c.w;
+  a.wt = static_cast<const __nv_bfloat16*>(c.weights);
+  a.bias = c.bias;
+  a.cout = c.cout;
+  a.slope = c.slope;
+  a.y_bf16 = static_cast<__nv_bfloat16*>(c.y_bf16);
+  a.y_f32 = c.y_f32;
+  a.y2_f32 = c.y2_f32;
+  a.split = c.y2_f32 ? c.split : c.cout;
+  a.accumulate = c.accumulate;
+  const int cin = c.c1 + c.c2;
+  const int nt = (c.cout + 7) / 8;
+  const size_t smem = (size_t(100) + size_t(nt) * 8) * (cin + 8) * sizeof(__nv_bfloat16);
+  const unsigned blocks = unsigned(c.n) * ((c.w + 7) / 8) * ((c.h + 7) / 8);
+#define TVK_CONV_CASE(NT)                                                                 \
+  case NT:                                                                                \
+    TVK_CUDA(cudaFuncSetAttribute(conv3x3_kernel<NT>,                                     \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))); \
+    conv3x3_kernel<NT><<<blocks, kThreads, smem, s>>>(a);                                 \
+    break;
+  switch (nt) {
+    TVK_CONV_CASE(1)
+    TVK_CONV_CASE(2)
+    TVK_CONV_CASE(4)
+    TVK_CONV_CASE(6)
+    TVK_CONV_CASE(8)
+    TVK_CONV_CASE(10)
+    TVK_CONV_CASE(12)
+    TVK_CONV_CASE(14)
+    TVK_CONV_CASE(16)
+    default: fail(TVK_ERR_UNSUPPORTED, "output channels must be 8, 16, 32, ..., 128");
+  }
+#undef TVK_CONV_CASE
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_conv3x3_wgrad(const CnnWgrad& c, cudaStream_t s) {
+  WgradArgs a{};
+  a.x1 = static_cast<const __nv_bfloat16*>(c.x1);
+  a.x2 = static_cast<const __nv_bfloat16*>(c.x2);
+  a.c1 = c.c1;
+  a.c2 = c.c2;
+  a.gy = static_cast<const __nv_bfloat16*>(c.gy);
+  a.n = c.n;
+  a.h = c.h;
+  a.w = c.w;
+  a.cout = c.cout;
+  a.dw = c.dw;
+  a.db = c.db;
+  const int cin = c.c1 + c.c2;
+  const int patches = c.n * ((c.w + 7) / 8) * ((c.h + 7) / 8);
+  // about 4 CTAs per SM over the 9 taps
+  const int chunks = std::max(1, std::min(patches, (152 * 4 + 8) / 9));
+  a.patches_per_cta = (patches + chunks - 1) / chunks;
+  const dim3 grid((patches + a.patches_per_cta - 1) / a.patches_per_cta, 9);
+  const size_t smem = (size_t(64) * (c.cout + 8) + size_t(64) * (cin + 8)) * sizeof(__nv_bfloat16);
+  const int nt = cin / 8;
+#define TVK_WG_CASE(NT)                                                                   \
+  case NT:                                                                                \
+    TVK_CUDA(cudaFuncSetAttribute(wgrad_kernel<NT>,                                       \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))); \
+    wgrad_kernel<NT><<<grid, kThreads, smem, s>>>(a);                                     \
+    break;
+  switch (nt) {
+    TVK_WG_CASE(2)
+    TVK_WG_CASE(4)
+    TVK_WG_CASE(6)
+    TVK_WG_CASE(8)
+    TVK_WG_CASE(10)
+    TVK_WG_CASE(12)
+    TVK_WG_CASE(14)
+    TVK_WG_CASE(16)
+    default: fail(TVK_ERR_UNSUPPORTED, "input channels must be 16, 32, ..., 128");
+  }
+#undef TVK_WG_CASE
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_act_grad(const float* dy, const void* y, float slope, void* g, size_t n, cudaStream_t s) {
+  act_grad_kernel<<<grid_for(n), 256, 0, s>>>(dy, static_cast<const __nv_bfloat16*>(y), slope,
+                                              static_cast<__nv_bfloat16*>(g), n);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s) {
+  avgpool2_kernel<<<grid_for(size_t(n) * (h / 2) * (w / 2) * c), 256, 0, s>>>(
+      static_cast<const __nv_bfloat16*>(x), n, h, w, c, static_cast<__nv_bfloat16*>(y));
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_avgpool2_backward(const float* dy, int n, int h, int w, int c, float* dx, int accumulate,
+                           cudaStream_t s) {
+  avgpool2_backward_kernel<<<grid_for(size_t(n) * h * w * c), 256, 0, s>>>(dy, n, h, w, c, dx,
+                                                                          accumulate);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_upsample2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s) {
+  upsample2_kernel<<<grid_for(size_t(n) * 4 * h * w * c), 256, 0, s>>>(
+      static_cast<const __nv_bfloat16*>(x), n, h, w, c, static_cast<__nv_bfloat16*>(y));
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_upsample2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                            cudaStream_t s) {
+  upsample2_backward_kernel<<<grid_for(size_t(n) * h * w * c), 256, 0, s>>>(dy, n, h, w, c, dx);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_head(const float* head, const float* base, int n, int h, int w, int oh, int ow,
+              float* out, cudaStream_t s) {
+  head_kernel<<<grid_for(size_t(n) * 4 * oh * ow), 256, 0, s>>>(head, base, n, h, w, oh, ow, out);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_prepare_input(const float* img, int h, int w, int hp, int wp, void* out, cudaStream_t s) {
+  prepare_input_kernel<<<grid_for(size_t(hp) * wp * 8), 256, 0, s>>>(
+      reinterpret_cast<const float4*>(img), h, w, hp, wp, static_cast<uint32_t*>(out));
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_probe_mse(const float* frame, int w, const float* probe, int pw, int ph, int stride,
+                   int ox, int oy, float* sum, cudaStream_t s) {
+  probe_mse_kernel<<<std::max(1, std::min(152 * 4, (pw * ph + 255) / 256)), 256, 0, s>>>(
+      reinterpret_cast<const float4*>(frame), w, reinterpret_cast<const float4*>(probe), pw, ph,
+      stride, ox, oy, sum);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_head_backward(const float* dout, int n, int h, int w, float* dhead, cudaStream_t s) {
+  head_backward_kernel<<<grid_for(size_t(n) * 16 * h * w), 256, 0, s>>>(dout, n, h, w, dhead);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_mse(const float* out, const float* target, size_t n, float* dout, float* loss,
+             cudaStream_t s) {
+  mse_kernel<<<std::min<uint32_t>(grid_for(n), 152 * 8), 256, 0, s>>>(out, target, n, dout, loss);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_adam(float* w, const float* g, float* m, float* v, size_t n, float lr, float b1, float b2,
+              float eps, int step, cudaStream_t s) {
+  const float c1 = 1.0f - powf(b1, float(step)), c2 = 1.0f - powf(b2, float(step));
+  adam_kernel<<<grid_for(n), 256, 0, s>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_weights_bf16(const float* w, int cout, int cin, void* fwd, void* bwd, cudaStream_t s) {
+  weights_bf16_kernel<<<grid_for(size_t(9) * cout * cin), 256, 0, s>>>(
+      w, cout, cin, static_cast<__nv_bfloat16*>(fwd), static_cast<__nv_bfloat16*>(bwd));
+  TVK_CUDA(cudaGetLastError());
+}
+
+void cnn_to_bf16(const float* x, size_t n, void* y, cudaStream_t s) {
+  to_bf16_kernel<<<grid_for(n), 256, 0, s>>>(x, n, static_cast<__nv_bfloat16*>(y));
+  TVK_CUDA(cudaGetLastError());
+}
+
+}  // namespace tvk

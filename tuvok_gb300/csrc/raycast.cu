@@ -555,7 +555,8 @@ constexpr uint32_t kCandChunk = 1024;
 // a 2-pixel margin covers rounding.  Bricks reaching behind the near plane
 // are always kept (the per-ray slab test decides).
 __device__ __forceinline__ bool footprint_touches_tile(const RenderParams& P, const DevBrick& b,
-                                                       float tx0, float ty0) {
+                                                       float tx0, float ty0, float span_x,
+                                                       float span_y) {
   float xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
   const float hw = 0.5f * float(P.width), hh = 0.5f * float(P.height);
 #pragma unroll
@@ -573,7 +574,8 @@ __device__ __forceinline__ bool footprint_touches_tile(const RenderParams& P, co
     xmin = fminf(xmin, sx); xmax = fmaxf(xmax, sx);
     ymin = fminf(ymin, sy); ymax = fmaxf(ymax, sy);
   }
-  return xmax >= tx0 - 2.0f && xmin <= tx0 + 17.0f && ymax >= ty0 - 2.0f && ymin <= ty0 + 9.0f;
+  return xmax >= tx0 - 2.0f && xmin <= tx0 + span_x + 2.0f && ymax >= ty0 - 2.0f &&
+         ymin <= ty0 + span_y + 2.0f;
 }
 
 // Shared-memory state of one 16x8-pixel tile: the candidate brick list.
@@ -592,10 +594,12 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t px = bx * 16 + (warp & 1) * 8 + (lane & 7);
   const uint32_t py = by * 8 + (warp >> 1) * 4 + (lane >> 3);
-  const bool active = px < P.width && py < P.height;
+  // the frame pixel this thread marches (stride 1, offset 0 for whole frames)
+  const uint32_t fx = px * P.stride + P.off_x, fy = py * P.stride + P.off_y;
+  const bool active = px < P.out_w && py < P.out_h && fx < P.width && fy < P.height;
 
-  const float nx = (float(px) + 0.5f) * P.inv_w2 - 1.0f;
-  const float ny = (float(py) + 0.5f) * P.inv_h2 - 1.0f;
+  const float nx = (float(fx) + 0.5f) * P.inv_w2 - 1.0f;
+  const float ny = (float(fy) + 0.5f) * P.inv_h2 - 1.0f;
   const float dir[3] = {nx * P.kx, ny * P.ky, -1.0f};
   float o[3], inv[3];
 #pragma unroll
@@ -610,7 +614,8 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   // strictly grows whenever a ray crosses into the next brick).  Each CTA
   // keeps, in that order, the bricks whose screen footprint can touch its
   // 16x8-pixel tile; each ray then marches those its own slab test hits.
-  const float tx0 = float(bx * 16), ty0 = float(by * 8);
+  const float tx0 = float(bx * 16 * P.stride + P.off_x), ty0 = float(by * 8 * P.stride + P.off_y);
+  const float span_x = float(15 * P.stride), span_y = float(7 * P.stride);
 
   float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
   uint32_t samples = 0, shaded = 0, graded = 0;
@@ -624,7 +629,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
     if (tid == 0) sh.n_cand = 0;
     for (uint32_t s = base; s < end; s += blockDim.x) {
       const uint32_t i = s + tid;
-      const bool keep = i < end && footprint_touches_tile(P, P.bricks[i], tx0, ty0);
+      const bool keep = i < end && footprint_touches_tile(P, P.bricks[i], tx0, ty0, span_x, span_y);
       const uint32_t m = __ballot_sync(0xffffffffu, keep);
       __syncthreads();
       if (lane == 0) sh.warp_cnt[warp] = __popc(m);
@@ -678,7 +683,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   // leaves the pixel empty
   if (iso_mode && have_hit && best.f != 0.0f) frame = iso_compose(P, best);
   if (active) {
-    const size_t pix = size_t(py) * P.width + px;
+    const size_t pix = size_t(py) * P.out_w + px;
     P.out[pix] = frame;
     if (P.spp) P.spp[pix] = samples;
   }
@@ -731,7 +736,7 @@ raycast_batch_kernel(const __grid_constant__ BatchLaunch L, uint32_t* __restrict
     const uint32_t f = frame_idx;
     const RenderParams& P = L.frames[f];
     const uint32_t local = it - L.tile_first[f];
-    const uint32_t tiles_x = (P.width + 15) / 16;
+    const uint32_t tiles_x = (P.out_w + 15) / 16;
     render_tile<T, kIso>(P, local % tiles_x, local / tiles_x, sh);
   }
 }
@@ -848,7 +853,7 @@ void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_it
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 block(128);
-  const dim3 grid((p.width + 15) / 16, (p.height + 7) / 8);
+  const dim3 grid((p.out_w + 15) / 16, (p.out_h + 7) / 8);
   const bool iso = p.mode == TVK_RM_ISOSURFACE;
   if (p.bytes == 1) {
     if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);

@@ -179,7 +179,10 @@ struct RenderParams {
   float proj_x, proj_y;      // vProjParam
   float iso_diffuse[3];      // diffuse colour * iso colour
   float max_q;               // guard on len/step
-  uint32_t width, height;
+  uint32_t width, height;     // the frame the camera projects to
+  // pixels actually marched: (x * stride + off_x, y * stride + off_y) for x <
+  // out_w, y < out_h, written densely to out (stride 1, offset 0: every pixel)
+  uint32_t out_w, out_h, stride, off_x, off_y;
   float4* out;
   uint32_t* spp;             // per-pixel sample counts (may be null)
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
@@ -205,6 +208,32 @@ const void* batch_kernel_function(int variant);
 // (GLRenderer::CopyOverCompletedRegion with GL_LINEAR).
 void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, uint32_t w,
                     uint32_t h, float rescale, cudaStream_t s, uint64_t* launches);
+
+// ------------------------------------------------------------------ CNN (cnn.cu)
+
+using CnnConv = tvk_cnn_conv;
+using CnnWgrad = tvk_cnn_wgrad;
+void cnn_conv3x3(const CnnConv& c, cudaStream_t s);
+void cnn_conv3x3_wgrad(const CnnWgrad& c, cudaStream_t s);
+void cnn_act_grad(const float* dy, const void* y, float slope, void* g, size_t n, cudaStream_t s);
+void cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s);
+void cnn_avgpool2_backward(const float* dy, int n, int h, int w, int c, float* dx, int accumulate,
+                           cudaStream_t s);
+void cnn_upsample2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s);
+void cnn_upsample2_backward(const float* dy, int n, int h, int w, int c, float* dx,
+                            cudaStream_t s);
+void cnn_head(const float* head, const float* base, int n, int h, int w, int oh, int ow,
+              float* out, cudaStream_t s);
+void cnn_prepare_input(const float* img, int h, int w, int hp, int wp, void* out, cudaStream_t s);
+void cnn_probe_mse(const float* frame, int w, const float* probe, int pw, int ph, int stride,
+                   int ox, int oy, float* sum, cudaStream_t s);
+void cnn_head_backward(const float* dout, int n, int h, int w, float* dhead, cudaStream_t s);
+void cnn_mse(const float* out, const float* target, size_t n, float* dout, float* loss,
+             cudaStream_t s);
+void cnn_adam(float* w, const float* g, float* m, float* v, size_t n, float lr, float b1, float b2,
+              float eps, int step, cudaStream_t s);
+void cnn_weights_bf16(const float* w, int cout, int cin, void* fwd, void* bwd, cudaStream_t s);
+void cnn_to_bf16(const float* x, size_t n, void* y, cudaStream_t s);
 
 }  // namespace tvk
 

@@ -200,6 +200,10 @@ class Renderer:
         self._w = self._h_px = 0
         self._vol = None
 
+    @property
+    def handle(self):
+        return self._h
+
     def close(self):
         if self._h:
             check(lib().tvk_renderer_destroy(self._h))
