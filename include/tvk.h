@@ -182,6 +182,15 @@ tvk_status tvk_volume_get_max_used_brick_size(const tvk_volume* v, uint32_t out[
 tvk_status tvk_volume_get_brick(const tvk_volume* v, uint64_t timestep, uint64_t lod,
                                 uint64_t index, void* host_out, size_t bytes);
 
+/* Frees the volume's device brick pool, keeping its metadata: the out-of-core
+ * set-up, where a GridLeaper pool created with host_source = 1 (which holds a
+ * pinned host copy of the bricks) is the only renderer of the volume, as
+ * GPUMemMan::GetVolumePool keeps only the cache on the GPU (GPUMemMan.cpp:
+ * 766-844).  Everything that reads the device bricks afterwards (tvk_paint,
+ * tvk_volume_get_brick, rebricking, device-sourced pools) fails with
+ * TVK_ERR_STATE.  Blocks until the device is idle. */
+tvk_status tvk_volume_release_bricks(tvk_volume* v);
+
 /* BrickedDataset::MaxMinForKey (IO/BrickedDataset.h:73). */
 tvk_status tvk_volume_get_minmax(const tvk_volume* v, uint64_t timestep, uint64_t lod,
                                  uint64_t index, tvk_minmax* out);
@@ -495,6 +504,61 @@ tvk_status tvk_paint_learned(tvk_renderer* r, tvk_learned* net, float threshold_
  * ray-marched reduced image (reduced = 1, render size) to device memory, on the
  * renderer's stream. */
 tvk_status tvk_copy_image_device(tvk_renderer* r, int reduced, void* dst, size_t bytes);
+
+/* ---- GridLeaper: single-pass LOD traversal over a paged brick cache ----
+ *
+ * A pool is the GLVolumePool of a volume (GLVolumePool.cpp:119-259): a brick
+ * cache of slots in HBM (as many maximum-size bricks as `budget_bytes` holds),
+ * a page table over the bricks of every LOD (MISSING / CHILD_EMPTY / EMPTY /
+ * slot), the visibility flags for the current TF or isovalue
+ * (RecomputeVisibilityForOctree, :1020-1359) and the missing-brick hash table
+ * (GLHashTable, size max(15, 509 / (brick voxels / 32768)), 10 probes).  The
+ * single brick of the coarsest LOD is pinned in the last slot.  With
+ * host_source the volume's bricks are copied once to pinned host memory and
+ * paged from there to the device on a side stream, else they are copied from
+ * the volume's device pool. */
+
+typedef struct tvk_pool tvk_pool;
+
+typedef struct tvk_pool_info {
+  uint32_t slots;
+  uint64_t slot_bytes;
+  uint64_t bricks;        /* bricks of every LOD (page-table entries) */
+  uint32_t hash_size;
+  int host_source;
+  uint64_t paged_total;   /* bricks paged in so far */
+} tvk_pool_info;
+
+typedef struct tvk_leaper_info {
+  uint32_t passes;        /* traversal passes run */
+  uint32_t paged;         /* bricks paged in during this frame */
+  uint32_t missing_last;  /* bricks the last pass reported missing */
+  int converged;          /* 1: the last pass found every brick it wanted */
+  uint32_t resident;      /* bricks in the cache after the frame */
+  float ms;               /* GPU time of the frame, paging included */
+} tvk_leaper_info;
+
+tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_source,
+                           tvk_pool** out);
+tvk_status tvk_pool_destroy(tvk_pool* p);
+tvk_status tvk_pool_get_info(const tvk_pool* p, tvk_pool_info* out);
+/* The host copy of the page table (one entry per brick in TOC order: 0
+ * MISSING, 1 CHILD_EMPTY, 2 EMPTY, else slot + 3). */
+tvk_status tvk_pool_get_page_table(const tvk_pool* p, uint32_t* out, size_t n);
+/* The bricks (TOC indices, ascending) the last traversal pass reported missing
+ * through the hash table (GLHashTable::GetData, GLHashTable.cpp:90-105): the
+ * first min(n, *count) are written, *count is the total. */
+tvk_status tvk_pool_get_requests(const tvk_pool* p, uint64_t* out, size_t n, size_t* count);
+
+/* One GridLeaper frame with the renderer's TF, mode (1D, 2D, iso), lighting,
+ * sample rate and view (GLGridLeaper::Render3DRegion, GLGridLeaper.cpp:914-1154):
+ * traversal passes (GLGridLeaper-blend.glsl / -iso.glsl) that resume each ray
+ * where it first met a brick coarser than its screen-space error asked for;
+ * between passes the reported bricks are paged in, oldest slots first.  Stops
+ * when a pass reports nothing missing or after max_passes.  The image is the
+ * last pass's (tvk_read_image).  Blocking. */
+tvk_status tvk_leaper_paint(tvk_renderer* r, tvk_pool* pool, uint32_t max_passes,
+                            tvk_leaper_info* info);
 
 /* Size of the last ray-marched image (the viewport, or the reduced one). */
 tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* height);

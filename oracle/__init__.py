@@ -98,6 +98,9 @@ def lib():
         L.orc_build_octree.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
                                        C.c_int, C.c_void_p, C.c_uint64, _u64p, C.c_uint64]
         L.orc_build_octree.restype = C.c_int64
+        L.orc_leaper_render.argtypes = [C.POINTER(Scene), _u32p, C.c_uint64,
+                                        C.POINTER(C.c_float), _u32p, _u64p, C.c_uint64, _u64p]
+        L.orc_leaper_render.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -332,6 +335,83 @@ class Prepared:
 
     def __del__(self):
         self.close()
+
+
+def leaper_render(raw, bsize, overlap, tf, page, *, width, height, **kw):
+    """One GridLeaper pass over the page table `page` (one entry per brick of
+    every LOD in TOC order: 0 MISSING, 1 CHILD_EMPTY, 2 EMPTY, >= 3 resident).
+    Returns (image [h, w, 4], samples, counts [h, w], missing TOC indices)."""
+    raw = np.ascontiguousarray(raw)
+    _, cnt = lod_table((raw.shape[2], raw.shape[1], raw.shape[0]), bsize, overlap)
+    page = np.ascontiguousarray(page, dtype=np.uint32)
+    if page.size != sum(c[0] * c[1] * c[2] for c in cnt):
+        raise ValueError("the page table needs one entry per brick of every LOD")
+    s, keep = make_scene(raw, bsize, overlap, tf, width=width, height=height, **kw)
+    img = np.zeros((height, width, 4), dtype=np.float32)
+    counts = np.zeros((height, width), dtype=np.uint32)
+    missing = np.zeros(page.size, dtype=np.uint64)
+    nm = C.c_uint64()
+    n = lib().orc_leaper_render(C.byref(s), page.ctypes.data_as(_u32p), page.size,
+                                img.ctypes.data_as(C.POINTER(C.c_float)),
+                                counts.ctypes.data_as(_u32p), missing.ctypes.data_as(_u64p),
+                                page.size, C.byref(nm))
+    del keep
+    return img, int(n), counts, missing[:nm.value].astype(np.int64)
+
+
+def tf_value_limits(tf, range_max):
+    """The value range the TF reaches (AbstrRenderer::ContainsData's limits):
+    the first and last TF column with a non-zero alpha, times
+    range_max / (width - 1) (GLGridLeaper.cpp:650-670)."""
+    tf = np.asarray(tf, dtype=np.float32)
+    a = tf[..., 3].reshape(-1, tf.shape[-2]) if tf.ndim == 3 else tf[:, 3][None, :]
+    cols = np.nonzero((a != 0).any(axis=0))[0]
+    w = a.shape[1]
+    lo, hi = (int(cols[0]), int(cols[-1])) if cols.size else (w, 0)
+    rescale = float(range_max) / float(max(w, 2) - 1)
+    return lo * rescale, hi * rescale
+
+
+def leaper_visibility(raw, bsize, overlap, cached, *, lo=0.0, hi=0.0, isovalue=None,
+                      median=False, clamp=False):
+    """GLVolumePool::RecomputeVisibility (GLVolumePool.cpp:1580-1700) restated:
+    every entry MISSING; the bricks in `cached` (TOC index -> slot entry, the
+    cached bricks that hold visible data) keep their entry; every other brick
+    that holds nothing visible (ContainsData, :962-989: value range [lo, hi], or
+    the isovalue) becomes CHILD_EMPTY when every existing child is CHILD_EMPTY
+    (the finest LOD always), else EMPTY (RecomputeVisibilityForOctree,
+    :1020-1359).  Returns the page table (uint32)."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    bricks = build_octree(raw, bsize, overlap, clamp=clamp, median=median)
+    _, counts = lod_table(dims, bsize, overlap)
+    first = np.concatenate([[0], np.cumsum([c[0] * c[1] * c[2] for c in counts])]).astype(int)
+    page = np.zeros(first[-1], dtype=np.uint32)
+    for i, e in cached.items():
+        page[i] = e
+    for l, c in enumerate(counts):
+        for k in range(c[0] * c[1] * c[2]):
+            i = first[l] + k
+            if page[i] >= 3:
+                continue
+            mn, mx = brick_stats(bricks[i])
+            has = (isovalue >= mn and isovalue <= mx) if isovalue is not None else \
+                (hi >= mn and lo <= mx)
+            if has:
+                continue
+            child_empty = True
+            if l > 0:
+                cc = counts[l - 1]
+                x, y, z = k % c[0], (k // c[0]) % c[1], k // (c[0] * c[1])
+                for dz in (0, 1):
+                    for dy in (0, 1):
+                        for dx in (0, 1):
+                            cx, cy, cz = 2 * x + dx, 2 * y + dy, 2 * z + dz
+                            if cx < cc[0] and cy < cc[1] and cz < cc[2]:
+                                ci = first[l - 1] + cx + cy * cc[0] + cz * cc[0] * cc[1]
+                                child_empty &= page[ci] == 1
+            page[i] = 1 if child_empty else 2
+    return page
 
 
 class RebrickError(ValueError):

@@ -185,6 +185,16 @@ uint64_t orc_render_prepared(void* prepared, const orc_scene* cam, float* out_rg
                              uint32_t* samples_per_pixel, double* march_s);
 void orc_release(void* prepared);
 
+/* One GridLeaper pass (GLGridLeaper-blend.glsl / -iso.glsl) of the scene over a
+ * page table with one entry per brick of every LOD in TOC order (0 MISSING,
+ * 1 CHILD_EMPTY, 2 EMPTY, >= 3 resident), the bricks built by
+ * orc_build_octree.  Writes the image and per-pixel samples; the bricks the
+ * rays reported missing go to `missing` (ascending TOC index).  Returns the
+ * number of samples. */
+uint64_t orc_leaper_render(const orc_scene* scene, const uint32_t* page, uint64_t n_page,
+                           float* out_rgba, uint32_t* samples_per_pixel, uint64_t* missing,
+                           uint64_t max_missing, uint64_t* n_missing);
+
 /* IEEE binary16 round-to-nearest-even of a float, returned as float (the
  * RGBA16F ray-entry buffer of GLRaycaster.cpp:97). */
 float orc_round_half(float x);

@@ -28,10 +28,12 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cfenv>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #ifdef _OPENMP
@@ -834,6 +836,419 @@ extern "C" uint64_t orc_render_prepared(void* h, const orc_scene* cam, float* ou
 }
 
 extern "C" void orc_release(void* h) { delete static_cast<Prepared*>(h); }
+
+// ---------------------------------------------------------------- GridLeaper
+//
+// One pass of GLGridLeaper-blend.glsl:65-228 / GLGridLeaper-iso.glsl:68-200 over
+// a page table (GetBrick and friends, GLVolumePool.cpp:484-656), restated per
+// pixel.  Bricks are addressed in their local texel coordinates (the pool
+// texture coordinates of a slot, scaled by the pool size), so only the page
+// table's states matter, not which slot holds a brick.
+
+namespace {
+
+struct LeaperBrick {
+  const uint8_t* data;
+  uint32_t n[3];
+};
+
+// texel-centre trilinear at local texel coordinates, clamp to the brick's edge
+float leaper_sample(const LeaperBrick& b, int dtype, float l0, float l1, float l2, float im) {
+  const float u[3] = {std::fmin(std::fmax(l0 - 0.5f, 0.0f), float(b.n[0]) - 1.0f),
+                      std::fmin(std::fmax(l1 - 0.5f, 0.0f), float(b.n[1]) - 1.0f),
+                      std::fmin(std::fmax(l2 - 0.5f, 0.0f), float(b.n[2]) - 1.0f)};
+  int i0[3], i1[3];
+  float f[3];
+  for (int a = 0; a < 3; ++a) {
+    i0[a] = int(u[a]);
+    f[a] = u[a] - float(i0[a]);
+    i1[a] = std::min(i0[a] + 1, int(b.n[a]) - 1);
+  }
+  auto fetch = [&](int x, int y, int z) -> float {
+    const size_t i = size_t(x) + size_t(y) * b.n[0] + size_t(z) * b.n[0] * b.n[1];
+    return dtype == 0 ? float(b.data[i]) : float(reinterpret_cast<const uint16_t*>(b.data)[i]);
+  };
+  auto lerp = [](float a, float c, float w) { return std::fma(w, c - a, a); };
+  const float c00 = lerp(fetch(i0[0], i0[1], i0[2]), fetch(i1[0], i0[1], i0[2]), f[0]);
+  const float c10 = lerp(fetch(i0[0], i1[1], i0[2]), fetch(i1[0], i1[1], i0[2]), f[0]);
+  const float c01 = lerp(fetch(i0[0], i0[1], i1[2]), fetch(i1[0], i0[1], i1[2]), f[0]);
+  const float c11 = lerp(fetch(i0[0], i1[1], i1[2]), fetch(i1[0], i1[1], i1[2]), f[0]);
+  const float c0 = lerp(c00, c10, f[1]);
+  const float c1 = lerp(c01, c11, f[1]);
+  return lerp(c0, c1, f[2]) * im;
+}
+
+inline float len3f(float x, float y, float z) { return std::sqrt((x * x + y * y) + z * z); }
+
+}  // namespace
+
+extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page, uint64_t n_page,
+                                      float* out, uint32_t* spp, uint64_t* missing,
+                                      uint64_t max_missing, uint64_t* n_missing) {
+  const orc_scene& s = *sc;
+  const int bytes = s.dtype == 0 ? 1 : 2;
+  uint64_t lsz[3 * 64], lcnt[3 * 64];
+  const int n_lods = orc_lod_table(s.dims, s.brick_size, s.overlap, lsz, lcnt, 64);
+  std::vector<uint64_t> first(n_lods + 1, 0), shapes;
+  uint64_t total_vox = 0;
+  std::vector<std::array<uint32_t, 3>> nv;
+  for (int l = 0; l < n_lods; ++l) {
+    first[l + 1] = first[l] + lcnt[3 * l] * lcnt[3 * l + 1] * lcnt[3 * l + 2];
+    for (uint64_t k = 0; k < first[l + 1] - first[l]; ++k) {
+      const uint64_t c3[3] = {k % lcnt[3 * l], (k / lcnt[3 * l]) % lcnt[3 * l + 1],
+                              k / (lcnt[3 * l] * lcnt[3 * l + 1])};
+      uint64_t bs[3];
+      orc_brick_size(&lsz[3 * l], &lcnt[3 * l], s.brick_size, s.overlap, c3, bs);
+      nv.push_back({uint32_t(bs[0]), uint32_t(bs[1]), uint32_t(bs[2])});
+      total_vox += bs[0] * bs[1] * bs[2];
+    }
+  }
+  if (n_page < first[n_lods]) return 0;
+  std::vector<uint8_t> pool(total_vox * bytes);
+  std::vector<uint64_t> off(first[n_lods]);
+  orc_build_octree(s.raw, s.dtype, s.dims, s.brick_size, s.overlap, s.clamp_to_edge, s.median,
+                   pool.data(), total_vox, off.data(), first[n_lods]);
+  // TF with the opacity correction of ocFactor = 1 / srm (host table, as the GPU)
+  const size_t ntf = size_t(s.tf_w) * s.tf_h;
+  std::vector<float> tf(4 * ntf, 0.0f);
+  const float oc = 1.0f / s.sample_rate_modifier;
+  for (size_t i = 0; i < ntf && s.render_mode != ORC_RM_ISO; ++i) {
+    float e[4];
+    for (int c = 0; c < 4; ++c) {
+      e[c] = s.tf[4 * i + c];
+      if (s.tf_rgba8) {
+        const unsigned char b = (unsigned char)(std::max(0.0f, std::min(e[c], 1.0f)) * 255);
+        e[c] = float(b) / 255.0f;
+      }
+    }
+    tf[4 * i] = e[0];
+    tf[4 * i + 1] = e[1];
+    tf[4 * i + 2] = e[2];
+    tf[4 * i + 3] = 1.0f - std::pow(1.0f - e[3], oc);
+  }
+  double rmax = 0;
+  for (uint64_t i = 0; i < s.dims[0] * s.dims[1] * s.dims[2]; ++i)
+    rmax = std::max(rmax, bytes == 1 ? double(static_cast<const uint8_t*>(s.raw)[i])
+                                     : double(static_cast<const uint16_t*>(s.raw)[i]));
+  const uint32_t imax = (1u << (8 * bytes)) - 1;
+  const float trans_scale = float(double(imax) / rmax);
+  float grad_scale = 1.0f;
+  if (s.render_mode == ORC_RM_2D) {
+    const float mg = float(orc_max_gradient(s.raw, s.dtype, s.dims, s.brick_size, s.overlap,
+                                            s.clamp_to_edge));
+    grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
+  }
+  const float im = bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  const float iso_norm = float(double(s.isovalue) / double(1u << (8 * bytes)));
+  Setup st;  // the fields iso_compose reads
+  st.s = &s;
+  for (int a = 0; a < 3; ++a) {
+    st.light_a[a] = s.ambient[a] * s.ambient[3];
+    st.light_d[a] = s.diffuse[a] * s.diffuse[3];
+    st.light_s[a] = s.specular[a] * s.specular[3];
+    st.iso_diffuse[a] = st.light_d[a] * s.iso_color[a];
+  }
+  const View v = make_view(s);
+  // layouts (GetFloatBrickLayout) and geometry
+  float layout[64][3];
+  for (int l = 0; l < n_lods; ++l)
+    for (int a = 0; a < 3; ++a) {
+      float c = float(s.dims[a]) / float(s.brick_size[a] - 2 * s.overlap);
+      c /= float(uint64_t(1) << l);
+      if (float(uint32_t(c)) == c) c -= c * std::numeric_limits<float>::epsilon();
+      layout[l][a] = c;
+    }
+  const uint32_t max_lod = uint32_t(n_lods - 1);
+  float ext[3], vol_size[3], max_inner[3];
+  const float dmax = float(std::max(s.dims[0], std::max(s.dims[1], s.dims[2])));
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = float(s.dims[a]) / dmax;
+    vol_size[a] = float(s.dims[a]);
+    max_inner[a] = float(s.brick_size[a] - 2 * s.overlap);
+  }
+  const float ghost = float(s.overlap);
+  const float lod_factor =
+      2.0f * std::tan(s.fovy_deg * ((3.1416f / 180.0f) / 2.0f)) * 1.0f / float(s.height);
+  const float lod0_err = std::max(ext[0] / vol_size[0], std::max(ext[1] / vol_size[1], ext[2] / vol_size[2]));
+  double e2n[3][4];
+  float eye2norm[3][4], norm2eye[3][4], nte[3][3];
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 4; ++c) e2n[r][c] = v.inv[r][c] / double(ext[r]);
+    e2n[r][3] += 0.5;
+  }
+  for (int r = 0; r < 3; ++r) {
+    double acc = v.mv[r][3];
+    for (int c = 0; c < 4; ++c) eye2norm[r][c] = float(e2n[r][c]);
+    for (int c = 0; c < 3; ++c) {
+      norm2eye[r][c] = float(v.mv[r][c] * double(ext[c]));
+      acc -= v.mv[r][c] * double(ext[c]) * 0.5;
+      nte[r][c] = float(v.mv[r][c]);
+    }
+    norm2eye[r][3] = float(acc);
+  }
+  double ld[3], em[3];
+  for (int r = 0; r < 3; ++r) {
+    ld[r] = e2n[r][0] * s.light_dir[0] + e2n[r][1] * s.light_dir[1] + e2n[r][2] * s.light_dir[2];
+    em[r] = e2n[r][0] * s.eye[0] + e2n[r][1] * s.eye[1] + e2n[r][2] * s.eye[2] + e2n[r][3];
+  }
+  const double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+  float Lm[3], Em[3];
+  for (int a = 0; a < 3; ++a) {
+    Lm[a] = float(ld[a] / ll);
+    Em[a] = float(em[a]);
+  }
+  const float srm = s.sample_rate_modifier;
+  const float W = float(s.tf_w), H = float(s.tf_h);
+  const bool lit = s.lighting != 0, two_d = s.render_mode == ORC_RM_2D,
+             iso = s.render_mode == ORC_RM_ISO;
+  std::vector<char> wanted(first[n_lods], 0);
+  uint64_t total = 0;
+
+  for (uint32_t py = 0; py < s.height; ++py)
+    for (uint32_t px = 0; px < s.width; ++px) {
+      const size_t pix = size_t(py) * s.width + px;
+      float* o4 = out + 4 * pix;
+      o4[0] = o4[1] = o4[2] = o4[3] = 0.0f;
+      if (spp) spp[pix] = 0;
+      const float nx = (float(px) + 0.5f) * v.inv_w2 - 1.0f;
+      const float ny = (float(py) + 0.5f) * v.inv_h2 - 1.0f;
+      const float de[3] = {nx * v.kx, ny * v.ky, -1.0f};
+      float o[3], d[3];
+      for (int a = 0; a < 3; ++a) {
+        o[a] = eye2norm[a][3];
+        d[a] = std::fma(eye2norm[a][2], de[2], std::fma(eye2norm[a][1], de[1], eye2norm[a][0] * de[0]));
+      }
+      float s0 = -INFINITY, s1 = INFINITY;
+      for (int a = 0; a < 3; ++a) {
+        const float inv = 1.0f / d[a];
+        const float ta = (0.0f - o[a]) * inv, tb = (1.0f - o[a]) * inv;
+        s0 = std::fmax(s0, std::fmin(ta, tb));
+        s1 = std::fmin(s1, std::fmax(ta, tb));
+      }
+      const float s_in = std::fmax(s0, s.znear);
+      if (!(s1 > s_in) || s1 > s.zfar) continue;
+      float ent[3], exi[3];
+      for (int a = 0; a < 3; ++a) {
+        exi[a] = std::fma(s1, d[a], o[a]);
+        ent[a] = std::fma(s_in, d[a], o[a]);
+      }
+      const float exit_depth = -s1, entry_depth = -s_in;
+      const float dir[3] = {exi[0] - ent[0], exi[1] - ent[1], exi[2] - ent[2]};
+      const float ray_len = len3f(dir[0], dir[1], dir[2]);
+      float sv[3] = {dir[0] * vol_size[0], dir[1] * vol_size[1], dir[2] * vol_size[2]};
+      {
+        const float l = len3f(sv[0], sv[1], sv[2]);
+        for (int a = 0; a < 3; ++a) sv[a] = (sv[a] / l) / (2.0f * srm);
+      }
+      const float step_len = len3f(sv[0], sv[1], sv[2]);
+      const float voxel_eps = 0.125f / 2000.0f;
+      float acc[4] = {0, 0, 0, 0};
+      float cur[3] = {ent[0], ent[1], ent[2]};
+      float t = 0.0f;
+      uint32_t last[4] = {0, 0, 0, 9999};
+      uint32_t samples = 0;
+      float hitc[4] = {0, 0, 0, 0};
+      auto info_at = [&](const float p[3], uint32_t lod, uint32_t bc[3]) {
+        for (int a = 0; a < 3; ++a) bc[a] = uint32_t(p[a] * layout[lod][a]);
+        const uint64_t id = first[lod] + bc[0] + bc[1] * lcnt[3 * lod] +
+                            bc[2] * lcnt[3 * lod] * lcnt[3 * lod + 1];
+        return std::make_pair(page[id], id);
+      };
+      if (ray_len > voxel_eps) {
+        for (uint32_t j = 0; j < 100; ++j) {
+          const float depth = entry_depth * (1.0f - t) + exit_depth * t;
+          const float lv = std::log2(lod_factor * (-depth) / lod0_err);
+          uint32_t lod = lv > 0.0f ? std::min(max_lod, uint32_t(lv)) : 0u;
+          float p[3];
+          for (int a = 0; a < 3; ++a) p[a] = std::fmin(std::fmax(cur[a], 0.0f), 1.0f);
+          uint32_t bc[3];
+          auto r = info_at(p, lod, bc);
+          uint32_t info = r.first;
+          uint64_t id = r.second;
+          if (info == 0) {
+            wanted[id] = 1;
+            while (info == 0 && lod < max_lod) {
+              ++lod;
+              r = info_at(p, lod, bc);
+              info = r.first;
+              id = r.second;
+            }
+            if (info == 0) info = 2;
+          }
+          const bool empty = info <= 2;
+          if (empty) {
+            for (uint32_t l = lod + 1; l < max_lod; ++l) {
+              uint32_t lbc[3];
+              const auto rr = info_at(p, l, lbc);
+              if (rr.first != 1) break;
+              bc[0] = lbc[0]; bc[1] = lbc[1]; bc[2] = lbc[2];
+              info = rr.first;
+              id = rr.second;
+              lod = l;
+            }
+          }
+          float c0[3], c1[3], bexit[3];
+          float tmin = INFINITY;
+          for (int a = 0; a < 3; ++a) {
+            c0[a] = float(bc[a]) / layout[lod][a];
+            c1[a] = float(bc[a] + 1u) / layout[lod][a];
+            const float div = 1.0f / dir[a];
+            const float corner = div >= 0.0f ? c1[a] : c0[a];
+            tmin = std::fmin(tmin, (corner - p[a]) * div);
+          }
+          for (int a = 0; a < 3; ++a) bexit[a] = std::fma(tmin, dir[a], p[a]);
+          const bool same = last[0] == bc[0] && last[1] == bc[1] && last[2] == bc[2] && last[3] == lod;
+          bool done = false;
+          if (!empty && !same) {
+            LeaperBrick b;
+            b.data = pool.data() + off[id] * bytes;
+            b.n[0] = nv[id][0]; b.n[1] = nv[id][1]; b.n[2] = nv[id][2];
+            float sc[3], tr[3], pc[3], pe[3], pxx[3];
+            for (int a = 0; a < 3; ++a) {
+              sc[a] = max_inner[a] * layout[lod][a];
+              tr[a] = ghost - c0[a] * sc[a];
+              pe[a] = std::fma(p[a], sc[a], tr[a]);
+              pxx[a] = std::fma(bexit[a], sc[a], tr[a]);
+              pc[a] = pe[a];
+            }
+            int steps = int(std::ceil(len3f(pxx[0] - pe[0], pxx[1] - pe[1], pxx[2] - pe[2]) / step_len));
+            steps = std::min(steps, int(std::ceil(len3f((exi[0] - cur[0]) * sc[0], (exi[1] - cur[1]) * sc[1],
+                                                        (exi[2] - cur[2]) * sc[2]) / step_len)));
+            auto smp = [&](float a0, float a1, float a2) { return leaper_sample(b, s.dtype, a0, a1, a2, im); };
+            for (int i = 0; i < steps; ++i) {
+              ++samples;
+              const float val = smp(pc[0], pc[1], pc[2]);
+              if (iso) {
+                if (val >= iso_norm) {
+                  float rr2[3] = {sv[0] / 2.0f, sv[1] / 2.0f, sv[2] / 2.0f};
+                  float q[3] = {pc[0] - rr2[0], pc[1] - rr2[1], pc[2] - rr2[2]};
+                  for (int k = 0; k < 5; ++k) {
+                    for (int a = 0; a < 3; ++a) rr2[a] = rr2[a] / 2.0f;
+                    const float vv = smp(q[0], q[1], q[2]);
+                    for (int a = 0; a < 3; ++a) q[a] = vv >= iso_norm ? q[a] - rr2[a] : q[a] + rr2[a];
+                  }
+                  const float xp = smp(q[0] + 1.0f, q[1], q[2]), xm = smp(q[0] - 1.0f, q[1], q[2]);
+                  const float yp = smp(q[0], q[1] - 1.0f, q[2]), ym = smp(q[0], q[1] + 1.0f, q[2]);
+                  const float zp = smp(q[0], q[1], q[2] + 1.0f), zm = smp(q[0], q[1], q[2] - 1.0f);
+                  float g[3] = {(xm - xp) / 2.0f, (yp - ym) / 2.0f, (zm - zp) / 2.0f};
+                  const float gl = len3f(g[0], g[1], g[2]);
+                  if (gl > 0.0f) { g[0] = g[0] / gl; g[1] = g[1] / gl; g[2] = g[2] / gl; }
+                  float hp[3], he[3], hn[3];
+                  for (int a = 0; a < 3; ++a) hp[a] = (q[a] - tr[a]) / sc[a];
+                  for (int r2 = 0; r2 < 3; ++r2) {
+                    he[r2] = std::fma(norm2eye[r2][0], hp[0],
+                                      std::fma(norm2eye[r2][1], hp[1],
+                                               std::fma(norm2eye[r2][2], hp[2], norm2eye[r2][3])));
+                    hn[r2] = std::fma(nte[r2][2], g[2], std::fma(nte[r2][1], g[1], nte[r2][0] * g[0]));
+                  }
+                  float c3[3];
+                  iso_compose<float>(st, he, hn, c3);
+                  hitc[0] = c3[0]; hitc[1] = c3[1]; hitc[2] = c3[2]; hitc[3] = 1.0f;
+                  done = true;
+                  break;
+                }
+              } else {
+                float src[4];
+                const float u = val * trans_scale;
+                float fx = std::floor(u * W);
+                fx = std::fmin(std::fmax(fx, 0.0f), W - 1.0f);
+                float g0 = 0, g1 = 0, g2 = 0;
+                bool need = lit;
+                bool col_any = true;
+                if (two_d) {
+                  col_any = false;
+                  for (uint32_t y = 0; y < s.tf_h; ++y)
+                    if (tf[4 * (size_t(y) * s.tf_w + size_t(fx)) + 3] != 0.0f) col_any = true;
+                  need = col_any;
+                } else {
+                  for (int c = 0; c < 4; ++c) src[c] = tf[4 * size_t(fx) + c];
+                  need = lit && src[3] != 0.0f;
+                }
+                if (need) {
+                  const float xp = smp(pc[0] + 1.0f, pc[1], pc[2]), xm = smp(pc[0] - 1.0f, pc[1], pc[2]);
+                  const float yp = smp(pc[0], pc[1] - 1.0f, pc[2]), ym = smp(pc[0], pc[1] + 1.0f, pc[2]);
+                  const float zp = smp(pc[0], pc[1], pc[2] + 1.0f), zm = smp(pc[0], pc[1], pc[2] - 1.0f);
+                  g0 = (xm - xp) / 2.0f;
+                  g1 = (yp - ym) / 2.0f;
+                  g2 = (zm - zp) / 2.0f;
+                }
+                float mag = 0.0f;
+                if (two_d) {
+                  if (need) {
+                    mag = len3f(g0, g1, g2);
+                    const float w = 1.0f - mag * grad_scale;
+                    float fy = std::floor(w * H);
+                    fy = std::fmin(std::fmax(fy, 0.0f), H - 1.0f);
+                    for (int c = 0; c < 4; ++c) src[c] = tf[4 * (size_t(fy) * s.tf_w + size_t(fx)) + c];
+                  } else {
+                    src[0] = src[1] = src[2] = src[3] = 0.0f;
+                  }
+                  need = need && lit && src[3] != 0.0f;
+                }
+                if (lit && need) {
+                  float N[3];
+                  if (two_d) {
+                    N[0] = mag > 0.0f ? g0 / mag : g0;
+                    N[1] = mag > 0.0f ? g1 / mag : g1;
+                    N[2] = mag > 0.0f ? g2 / mag : g2;
+                  } else {
+                    N[0] = g0; N[1] = g1; N[2] = g2;
+                    const float l = len3f(N[0], N[1], N[2]);
+                    if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+                  }
+                  float mp[3];
+                  for (int a = 0; a < 3; ++a) mp[a] = (pc[a] - tr[a]) / sc[a];
+                  // lighting.glsl:33-43 with the model-space eye
+                  const float q0 = Em[0] - mp[0], q1 = Em[1] - mp[1], q2 = Em[2] - mp[2];
+                  const float lq = len3f(q0, q1, q2);
+                  const float V0 = q0 / lq, V1 = q1 / lq, V2 = q2 / lq;
+                  const float dd = (N[0] * V0 + N[1] * V1) + N[2] * V2;
+                  float R0 = V0 - (2.0f * dd) * N[0], R1 = V1 - (2.0f * dd) * N[1],
+                        R2 = V2 - (2.0f * dd) * N[2];
+                  const float lr = len3f(R0, R1, R2);
+                  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+                  const float diff = std::fmax(std::fabs((N[0] * Lm[0] + N[1] * Lm[1]) + N[2] * Lm[2]), 0.0f);
+                  const float spec = pow_int_or_real(std::fmax((R0 * Lm[0] + R1 * Lm[1]) + R2 * Lm[2], 0.0f), 8.0f);
+                  for (int c = 0; c < 3; ++c) {
+                    const float dcol = st.light_d[c] * src[c];
+                    float x = st.light_a[c] + dcol * diff;
+                    x = x + st.light_s[c] * spec;
+                    src[c] = std::fmin(std::fmax(x, 0.0f), 1.0f);
+                  }
+                }
+                const float w = 1.0f - acc[3];
+                acc[0] = std::fma(src[0] * w, src[3], acc[0]);
+                acc[1] = std::fma(src[1] * w, src[3], acc[1]);
+                acc[2] = std::fma(src[2] * w, src[3], acc[2]);
+                acc[3] = std::fma(src[3], w, acc[3]);
+                if (acc[3] > 0.99f) { done = true; break; }
+              }
+              for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
+            }
+            if (done) break;
+            for (int a = 0; a < 3; ++a) cur[a] = (pc[a] - tr[a]) / sc[a];
+          } else {
+            for (int a = 0; a < 3; ++a) cur[a] = std::fma(voxel_eps, dir[a] / ray_len, bexit[a]);
+          }
+          last[0] = bc[0]; last[1] = bc[1]; last[2] = bc[2]; last[3] = lod;
+          t = len3f(ent[0] - bexit[0], ent[1] - bexit[1], ent[2] - bexit[2]) / ray_len;
+          if (t > 0.9999f) break;
+        }
+      }
+      const float* res = iso ? hitc : acc;
+      for (int c = 0; c < 4; ++c) o4[c] = res[c];
+      if (spp) spp[pix] = samples;
+      total += samples;
+    }
+  uint64_t nm = 0;
+  for (uint64_t i = 0; i < first[n_lods]; ++i)
+    if (wanted[i]) {
+      if (nm < max_missing && missing) missing[nm] = i;
+      ++nm;
+    }
+  if (n_missing) *n_missing = nm;
+  return total;
+}
 
 extern "C" void orc_render_size(const orc_scene* sc, uint32_t* w, uint32_t* h) {
   render_size(*sc, w, h);

@@ -79,6 +79,17 @@ class LearnedInfo(C.Structure):
                 ("reduced_width", C.c_uint32), ("reduced_height", C.c_uint32)]
 
 
+class PoolInfo(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("slot_bytes", C.c_uint64), ("bricks", C.c_uint64),
+                ("hash_size", C.c_uint32), ("host_source", C.c_int),
+                ("paged_total", C.c_uint64)]
+
+
+class LeaperInfo(C.Structure):
+    _fields_ = [("passes", C.c_uint32), ("paged", C.c_uint32), ("missing_last", C.c_uint32),
+                ("converged", C.c_int), ("resident", C.c_uint32), ("ms", C.c_float)]
+
+
 class Stats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64),
                 ("bricks_visible", C.c_uint64), ("bricks_total", C.c_uint64),
@@ -163,6 +174,13 @@ PROTOTYPES = {
     "tvk_paint_batch": [_vp, C.POINTER(_vp), C.c_uint32],
     "tvk_batch_set_autotune": [_vp, C.c_int, C.c_uint32],
     "tvk_batch_get_info": [_vp, C.POINTER(BatchInfo)],
+    "tvk_volume_release_bricks": [_vp],
+    "tvk_pool_create": [_vp, C.c_uint64, C.c_int, C.POINTER(_vp)],
+    "tvk_pool_destroy": [_vp],
+    "tvk_pool_get_info": [_vp, C.POINTER(PoolInfo)],
+    "tvk_pool_get_page_table": [_vp, _u32p, C.c_size_t],
+    "tvk_pool_get_requests": [_vp, _u64p, C.c_size_t, C.POINTER(C.c_size_t)],
+    "tvk_leaper_paint": [_vp, _vp, C.c_uint32, C.POINTER(LeaperInfo)],
     "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
     "tvk_read_image": [_vp, _f32p, C.c_size_t],
     "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],

@@ -375,7 +375,7 @@ void compute_histogram2d(const tvk_volume* V, uint64_t bins, uint64_t* host_out)
                            cudaMemcpyHostToDevice, s));
   TVK_CUDA(cudaMemsetAsync(d_hist.p, 0, out_bytes, s));
   uint64_t launches = 0;
-  launch_histogram2d(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+  launch_histogram2d(device_bricks(V), V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                      V->n_bricks, max_bz, hp, d_hist.as<unsigned long long>(), s, &launches);
   TVK_CUDA(cudaMemcpyAsync(host_out, d_hist.p, out_bytes, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaStreamSynchronize(s));
@@ -647,6 +647,41 @@ struct tvk_learned {
   tvk::PinnedBuf h_sum;
   cudaEvent_t ev[5] = {};
   uint32_t frame = 0;
+};
+
+// LOD-octree brick cache for the GridLeaper (GLVolumePool + GLHashTable).
+struct tvk_pool {
+  const tvk_volume* vol = nullptr;
+  int device = 0;
+  uint32_t n_slots = 0;
+  uint64_t slot_voxels = 0;
+  tvk::DevBuf d_slots;
+  bool host_source = false;          // bricks paged from pinned host memory
+  tvk::PinnedBuf h_bricks;           // host brick store (the volume's pool layout)
+  std::vector<uint32_t> page;        // page table per brick (all LODs)
+  tvk::PinnedBuf h_page;
+  tvk::DevBuf d_page, d_dims;
+  struct Slot {                      // PoolSlotData (GLVolumePool.h:24-60)
+    int64_t brick = -1;
+    uint64_t time = 0;                 // 0 never used, 1 flagged empty, else creation time
+    uint64_t orig_time = 0;
+  };
+  std::vector<Slot> slots;           // the coarsest brick starts in the last slot
+  uint64_t clock = 2;
+  uint32_t coarsest = 0;
+  tvk::DevBuf d_hash;
+  tvk::PinnedBuf h_hash;
+  uint32_t hash_size = 0, rehash = 10;
+  tvk::DevBuf d_resume_pos, d_resume_col;
+  cudaStream_t page_stream = nullptr;
+  cudaEvent_t ev_paged = nullptr;
+  // visibility flags were computed for this state
+  bool vis_valid = false;
+  int vis_mode = -1;
+  double vis_lo = 0, vis_hi = 0;
+  float vis_iso = 0;
+  uint64_t paged_total = 0;
+  std::vector<uint64_t> requests;    // bricks the last pass reported missing
 };
 
 namespace tvk {
@@ -921,7 +956,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
 
   RenderParams P;
   std::memset(&P, 0, sizeof(P));
-  P.pool = V->d_pool;
+  P.pool = device_bricks(V);
   P.bytes = V->bytes;
   P.bricks = R->d_bricks.as<DevBrick>();
   P.n_bricks = nvis;
@@ -1480,6 +1515,337 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   info->reduced_height = low.rh;
 }
 
+// GLVolumePool.cpp:89-107 GetFloatBrickLayout
+void float_brick_layout(const tvk_volume* V, uint32_t lod, float out[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const uint32_t inner = V->brick_size[a] - 2 * V->overlap;
+    float c = float(V->dims[a]) / float(inner);
+    c /= float(uint64_t(1) << lod);
+    if (float(uint32_t(c)) == c) c -= c * std::numeric_limits<float>::epsilon();
+    out[a] = c;
+  }
+}
+
+// GLVolumePool::RecomputeVisibility (GLVolumePool.cpp:1580-1700) with the
+// ContainsData tests of :962-989 (the 2D mode's gradient test always passes:
+// bricks of an ExtendedOctree carry the gradient range [-DBL_MAX, DBL_MAX],
+// MaxMinDataBlock.cpp:175-195).  Every entry is reset to MISSING; cached
+// bricks keep their slot when visible, else become EMPTY and their slot is
+// flagged for early eviction (RecomputeVisibilityForBrickPool, :991-1018);
+// then every brick not cached-and-visible that holds nothing visible becomes
+// CHILD_EMPTY when all its children are CHILD_EMPTY (finest bricks by
+// definition), else EMPTY (RecomputeVisibilityForOctree, :1020-1359).
+void pool_visibility(tvk_pool* pool, int mode, double lo, double hi, float iso) {
+  const tvk_volume* V = pool->vol;
+  auto contains = [&](uint64_t id) {
+    const double mn = V->bmin[id], mx = V->bmax[id];
+    return mode == TVK_RM_ISOSURFACE ? (double(iso) >= mn && double(iso) <= mx)
+                                     : (hi >= mn && lo <= mx);
+  };
+  std::fill(pool->page.begin(), pool->page.end(), kBiMissing);
+  for (uint32_t i = 0; i < pool->n_slots; ++i) {
+    tvk_pool::Slot& S = pool->slots[i];
+    if (S.brick < 0) continue;
+    const bool now = contains(uint64_t(S.brick)), before = S.time > 1;
+    if (now) {
+      if (!before) S.time = S.orig_time;  // Restore
+      pool->page[uint64_t(S.brick)] = i + kBiFlagCount;
+    } else {
+      if (before) {  // FlagEmpty
+        S.orig_time = S.time;
+        S.time = 1;
+      }
+      pool->page[uint64_t(S.brick)] = kBiEmpty;
+    }
+  }
+  const size_t n_lods = V->lod_first.size() - 1;
+  for (size_t l = 0; l < n_lods; ++l) {
+    const LodInfo& li = V->lods[l];
+    for (uint64_t k = 0; k < V->lod_first[l + 1] - V->lod_first[l]; ++k) {
+      const uint64_t id = V->lod_first[l] + k;
+      if (pool->page[id] >= kBiFlagCount || contains(id)) continue;
+      bool child_empty = true;
+      if (l > 0) {
+        const LodInfo& lc = V->lods[l - 1];
+        const uint64_t x = k % li.bricks[0], y = (k / li.bricks[0]) % li.bricks[1],
+                       z = k / (li.bricks[0] * li.bricks[1]);
+        for (int c = 0; c < 8 && child_empty; ++c) {
+          const uint64_t cx = 2 * x + (c & 1), cy = 2 * y + ((c >> 1) & 1), cz = 2 * z + (c >> 2);
+          if (cx >= lc.bricks[0] || cy >= lc.bricks[1] || cz >= lc.bricks[2]) continue;
+          const uint64_t cid = V->lod_first[l - 1] + cx + cy * lc.bricks[0] +
+                               cz * lc.bricks[0] * lc.bricks[1];
+          child_empty = pool->page[cid] == kBiChildEmpty;
+        }
+      }
+      pool->page[id] = child_empty ? kBiChildEmpty : kBiEmpty;
+    }
+  }
+}
+
+// Copies brick `id` into slot `slot` on the paging stream (UploadBrick,
+// GLVolumePool.cpp:673-717): a visible brick evicted from the slot becomes
+// MISSING (one flagged empty keeps its EMPTY / CHILD_EMPTY entry).
+void pool_upload(tvk_pool* pool, uint32_t slot, uint64_t id, uint64_t time) {
+  const tvk_volume* V = pool->vol;
+  tvk_pool::Slot& S = pool->slots[slot];
+  if (S.brick >= 0 && S.time > 1) pool->page[uint64_t(S.brick)] = kBiMissing;
+  S.brick = int64_t(id);
+  S.time = time;
+  pool->page[id] = slot + kBiFlagCount;
+  const size_t bytes = size_t(V->sizes[3 * id]) * V->sizes[3 * id + 1] * V->sizes[3 * id + 2] *
+                       V->bytes;
+  void* dst = static_cast<uint8_t*>(pool->d_slots.p) + size_t(slot) * pool->slot_voxels * V->bytes;
+  const void* src = pool->host_source
+                        ? static_cast<const void*>(pool->h_bricks.as<uint8_t>() +
+                                                   V->offsets[id] * V->bytes)
+                        : static_cast<const void*>(static_cast<const uint8_t*>(device_bricks(V)) +
+                                                   V->offsets[id] * V->bytes);
+  TVK_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                           pool->host_source ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                           pool->page_stream));
+}
+
+void pool_upload_page_table(tvk_pool* pool) {
+  const size_t n = pool->page.size();
+  // the staging copy of the previous upload may still be in flight
+  TVK_CUDA(cudaEventSynchronize(pool->ev_paged));
+  std::memcpy(pool->h_page.p, pool->page.data(), n * sizeof(uint32_t));
+  TVK_CUDA(cudaMemcpyAsync(pool->d_page.p, pool->h_page.p, n * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, pool->page_stream));
+  TVK_CUDA(cudaEventRecord(pool->ev_paged, pool->page_stream));
+}
+
+// One GridLeaper frame (GLGridLeaper::Render3DRegion, GLGridLeaper.cpp:914-1154):
+// passes of the traversal, each followed by paging in the bricks its rays
+// reported missing, until a pass reports none or max_passes is reached.
+void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leaper_info* info) {
+  const tvk_volume* V = R->vol;
+  if (!V || V != pool->vol) fail(TVK_ERR_STATE, "the renderer's volume is not the pool's volume");
+  const bool iso_mode = R->mode == TVK_RM_ISOSURFACE;
+  if (!iso_mode && R->tf.empty()) fail(TVK_ERR_STATE, "no transfer function set");
+  if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
+  if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
+  if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
+  TVK_CUDA(cudaSetDevice(R->device));
+  const uint64_t launches0 = R->launches;
+  const float srm = R->srm;
+  // GLGridLeaper-blend.glsl OpacityCorrectColor with ocFactor = 1 / srm
+  if (!R->tf.empty()) upload_tf(R, 1.0f / srm);
+  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
+  const float trans_scale = float(double(imax) / V->range_max);
+  const float iso_norm = float(double(R->isovalue) / double(1u << (8 * V->bytes)));
+  // the visible range of the TF (AbstrRenderer::ContainsData's limits)
+  uint64_t nz_lo = R->tf_w, nz_hi = 0;
+  for (uint32_t y = 0; y < R->tf_h; ++y)
+    for (uint32_t x = 0; x < R->tf_w; ++x)
+      if (R->tf[4 * (size_t(y) * R->tf_w + x) + 3] != 0) {
+        nz_lo = std::min<uint64_t>(nz_lo, x);
+        nz_hi = std::max<uint64_t>(nz_hi, x);
+      }
+  const double rescale = V->range_max / double(std::max<uint32_t>(R->tf_w, 2) - 1);
+  const double lo = double(nz_lo) * rescale, hi = double(nz_hi) * rescale;
+  if (!pool->vis_valid || pool->vis_mode != R->mode || pool->vis_lo != lo ||
+      pool->vis_hi != hi || pool->vis_iso != R->isovalue) {
+    pool_visibility(pool, R->mode, lo, hi, R->isovalue);
+    if (pool->page[pool->coarsest] == kBiMissing) {
+      // The coarsest brick was evicted while it held nothing visible and now
+      // does: a ray whose every coarser fallback is MISSING would never find
+      // a brick (GLVolumePool.cpp:553-590 loops until one is found), so the
+      // single brick of the coarsest LOD is brought back first.
+      uint32_t oldest = 0;
+      for (uint32_t i = 1; i < pool->n_slots; ++i)
+        if (pool->slots[i].time < pool->slots[oldest].time) oldest = i;
+      pool_upload(pool, oldest, pool->coarsest, ~uint64_t(0));
+    }
+    pool->vis_valid = true;
+    pool->vis_mode = R->mode;
+    pool->vis_lo = lo;
+    pool->vis_hi = hi;
+    pool->vis_iso = R->isovalue;
+    pool_upload_page_table(pool);
+  }
+
+  const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
+  LeaperParams L;
+  std::memset(&L, 0, sizeof(L));
+  RenderParams& P = L.R;
+  P.bytes = V->bytes;
+  P.tf = R->slots[R->slot].d_tf.as<float4>();
+  P.tf_col_nonzero = R->slots[R->slot].d_tfcol.as<uint8_t>();
+  P.tf_w = R->tf_w;
+  P.tf_h = R->tf_h;
+  P.mode = R->mode;
+  P.lighting = R->lighting ? 1 : 0;
+  P.light_model = R->light_model;
+  P.trans_scale = trans_scale;
+  const float mg = float(V->max_grad);
+  P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
+  P.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  for (int a = 0; a < 3; ++a) {
+    P.light_a[a] = R->ambient[a] * R->ambient[3];
+    P.light_d[a] = R->diffuse[a] * R->diffuse[3];
+    P.light_s[a] = R->specular[a] * R->specular[3];
+    P.light_dir[a] = R->light_dir[a];
+    P.domain_scale[a] = 1.0f;
+    P.iso_diffuse[a] = (R->diffuse[a] * R->diffuse[3]) * R->iso_color[a];
+  }
+  P.kx = view.kx;
+  P.ky = view.ky;
+  P.inv_w2 = view.inv_w2;
+  P.inv_h2 = view.inv_h2;
+  P.znear = R->znear;
+  P.zfar = R->zfar;
+  P.iso_norm = iso_norm;
+  P.width = P.out_w = R->width;
+  P.height = P.out_h = R->height;
+  P.stride = 1;
+  const size_t npix = size_t(R->width) * R->height;
+  R->d_img.ensure(npix * sizeof(float4));
+  R->d_spp.ensure(npix * sizeof(uint32_t));
+  R->d_counters.ensure(4 * sizeof(unsigned long long));
+  P.out = R->d_img.as<float4>();
+  P.spp = R->d_spp.as<uint32_t>();
+  P.counters = R->d_counters.as<unsigned long long>();
+  // pool geometry
+  L.slots = pool->d_slots.p;
+  L.slot_voxels = pool->slot_voxels;
+  L.page = pool->d_page.as<uint32_t>();
+  L.brick_dims = pool->d_dims.as<uint32_t>();
+  const uint32_t n_lods = uint32_t(V->lod_first.size() - 1);
+  L.max_lod = n_lods - 1;
+  for (uint32_t l = 0; l < n_lods; ++l) {
+    float_brick_layout(V, l, L.layout[l]);
+    const LodInfo& li = V->lods[l];
+    for (int a = 0; a < 3; ++a)
+      if (uint64_t(L.layout[l][a]) >= li.bricks[a])
+        fail(TVK_ERR_UNSUPPORTED, "the pool's float brick layout exceeds the LOD's bricks");
+    L.lod_offset[l] = uint32_t(V->lod_first[l]);
+    L.lod_lx[l] = uint32_t(li.bricks[0]);
+    L.lod_lxy[l] = uint32_t(li.bricks[0] * li.bricks[1]);
+  }
+  float ext[3];
+  const float dmax = float(std::max(V->dims[0], std::max(V->dims[1], V->dims[2])));
+  for (int a = 0; a < 3; ++a) {
+    L.vol_size[a] = float(V->dims[a]);
+    L.max_inner[a] = float(V->brick_size[a] - 2 * V->overlap);
+    ext[a] = float(V->dims[a]) / dmax;  // GetVolumeAABB extent (scale 1)
+  }
+  L.ghost = float(V->overlap);
+  // CullingLOD::SetScreenParams (CullingLOD.cpp:57-67), GLVolumePool::Enable (:790-803)
+  L.lod_factor = 2.0f * std::tan(R->fovy * ((3.1416f / 180.0f) / 2.0f)) * 1.0f / float(R->height);
+  L.lod0_err = std::max(ext[0] / L.vol_size[0], std::max(ext[1] / L.vol_size[1], ext[2] / L.vol_size[2]));
+  // ComputeEyeToModelMatrix (GLGridLeaper.cpp:558-571): eye -> model -> [0, 1]^3
+  double e2n[3][4];
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 4; ++c) e2n[r][c] = view.inv[r][c] / double(ext[r]);
+    e2n[r][3] += 0.5;
+  }
+  for (int r = 0; r < 3; ++r) {
+    double acc = view.mv[r][3];
+    for (int c = 0; c < 4; ++c) L.eye2norm[r][c] = float(e2n[r][c]);
+    for (int c = 0; c < 3; ++c) {
+      L.norm2eye[r][c] = float(view.mv[r][c] * double(ext[c]));
+      acc -= view.mv[r][c] * double(ext[c]) * 0.5;
+      L.norm_to_eye_n[r][c] = float(view.mv[r][c]);
+    }
+    L.norm2eye[r][3] = float(acc);
+  }
+  // GLGridLeaper.cpp:739-742: the light direction through the eye -> norm
+  // matrix (normalised), and the camera's eye point taken through the same
+  // matrix as if it were an eye-space point
+  double ld[3], em[3];
+  for (int r = 0; r < 3; ++r) {
+    ld[r] = e2n[r][0] * R->light_dir[0] + e2n[r][1] * R->light_dir[1] + e2n[r][2] * R->light_dir[2];
+    em[r] = e2n[r][0] * R->eye[0] + e2n[r][1] * R->eye[1] + e2n[r][2] * R->eye[2] + e2n[r][3];
+  }
+  const double ll = std::sqrt(ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2]);
+  for (int a = 0; a < 3; ++a) {
+    L.light_dir_model[a] = float(ld[a] / ll);
+    L.eye_model[a] = float(em[a]);
+  }
+  L.srm = srm;
+  L.hash = pool->d_hash.as<uint32_t>();
+  L.hash_size = pool->hash_size;
+  L.rehash = pool->rehash;
+  const LodInfo& l0 = V->lods[0];
+  L.ser_x = uint32_t(l0.bricks[0]);
+  L.ser_xy = uint32_t(l0.bricks[0] * l0.bricks[1]);
+  L.ser_xyz = uint32_t(l0.bricks[0] * l0.bricks[1] * l0.bricks[2]);
+  pool->d_resume_pos.ensure(npix * sizeof(float4));
+  pool->d_resume_col.ensure(npix * sizeof(float4));
+  L.resume_pos = pool->d_resume_pos.as<float4>();
+  L.resume_col = pool->d_resume_col.as<float4>();
+
+  std::memset(info, 0, sizeof(*info));
+  const uint64_t l0n = L.ser_xyz;
+  TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
+  for (uint32_t pass = 0; pass < std::max(1u, max_passes); ++pass) {
+    L.first_pass = pass == 0 ? 1u : 0u;
+    TVK_CUDA(cudaStreamWaitEvent(R->stream, pool->ev_paged, 0));
+    TVK_CUDA(cudaMemsetAsync(pool->d_hash.p, 0, pool->hash_size * sizeof(uint32_t), R->stream));
+    TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
+    launch_leaper(L, R->stream, &R->launches);
+    TVK_CUDA(cudaMemcpyAsync(pool->h_hash.p, pool->d_hash.p, pool->hash_size * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, R->stream));
+    TVK_CUDA(cudaStreamSynchronize(R->stream));
+    ++info->passes;
+    // the missing bricks this pass reported (GLHashTable::GetData)
+    std::vector<uint64_t> want;
+    const uint32_t* h = pool->h_hash.as<uint32_t>();
+    for (uint32_t i = 0; i < pool->hash_size; ++i) {
+      if (!h[i]) continue;
+      const uint64_t key = h[i] - 1u;
+      const uint64_t lod = key / l0n, rem = key % l0n;
+      const uint64_t x = rem % L.ser_x, y = (rem / L.ser_x) % (L.ser_xy / L.ser_x),
+                     z = rem / L.ser_xy;
+      if (lod >= n_lods) continue;
+      const LodInfo& li = V->lods[lod];
+      if (x >= li.bricks[0] || y >= li.bricks[1] || z >= li.bricks[2]) continue;
+      want.push_back(V->lod_first[lod] + x + y * li.bricks[0] + z * li.bricks[0] * li.bricks[1]);
+    }
+    info->missing_last = uint32_t(want.size());
+    pool->requests = want;
+    std::sort(pool->requests.begin(), pool->requests.end());
+    if (want.empty()) {
+      info->converged = 1;
+      break;
+    }
+    if (pass + 1 >= std::max(1u, max_passes)) break;
+    // PrepareForPaging (:955-959): slots by creation time (never used 0,
+    // flagged empty 1, the coarsest brick the maximum); the bricks go into the
+    // first n - 1 of that order (UploadBrick, :768-778)
+    std::vector<uint32_t> order(pool->n_slots);
+    for (uint32_t i = 0; i < pool->n_slots; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+      return pool->slots[a].time < pool->slots[b].time;
+    });
+    uint32_t ins = 0;
+    for (uint64_t id : want) {
+      if (ins + 1 >= pool->n_slots) break;  // every slot replaced this round
+      if (pool->page[id] >= kBiFlagCount) continue;
+      pool_upload(pool, order[ins++], id, pool->clock++);
+      ++info->paged;
+      ++pool->paged_total;
+    }
+    pool_upload_page_table(pool);
+  }
+  TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
+  R->h_counters.ensure(4 * sizeof(unsigned long long));
+  TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, R->stream));
+  TVK_CUDA(cudaEventSynchronize(R->ev_stop));
+  TVK_CUDA(cudaEventElapsedTime(&info->ms, R->ev_start, R->ev_stop));
+  uint32_t resident = 0;
+  for (const tvk_pool::Slot& sl : pool->slots) resident += sl.brick >= 0 ? 1u : 0u;
+  info->resident = resident;
+  R->render_w = R->width;
+  R->render_h = R->height;
+  R->stats.bricks_visible = resident;
+  R->stats.bricks_total = V->total_bricks;
+  R->stats.kernel_launches = R->launches - launches0;
+  R->painted = true;
+}
+
 }  // namespace
 }  // namespace tvk
 
@@ -1596,8 +1962,19 @@ tvk_status tvk_volume_get_brick(const tvk_volume* v, uint64_t ts, uint64_t lod, 
     const size_t n = size_t(v->sizes[3 * k]) * v->sizes[3 * k + 1] * v->sizes[3 * k + 2] * v->bytes;
     REQUIRE(bytes >= n, "output buffer smaller than the brick");
     TVK_CUDA(cudaSetDevice(v->device));
-    TVK_CUDA(cudaMemcpy(host_out, static_cast<const uint8_t*>(v->d_pool) + v->offsets[k] * v->bytes,
+    TVK_CUDA(cudaMemcpy(host_out,
+                        static_cast<const uint8_t*>(tvk::device_bricks(v)) + v->offsets[k] * v->bytes,
                         n, cudaMemcpyDeviceToHost));
+  });
+}
+
+tvk_status tvk_volume_release_bricks(tvk_volume* v) {
+  return guarded([&] {
+    REQUIRE(v, "null argument");
+    TVK_CUDA(cudaSetDevice(v->device));
+    TVK_CUDA(cudaDeviceSynchronize());  // no launch may still read the pool
+    if (v->d_pool) TVK_CUDA(cudaFree(v->d_pool));
+    v->d_pool = nullptr;
   });
 }
 
@@ -2250,6 +2627,109 @@ tvk_status tvk_cnn_to_bf16(const float* x, size_t n, void* y, void* stream) {
   return guarded([&] {
     REQUIRE(x && y, "null argument");
     tvk::cnn_to_bf16(x, n, y, as_stream(stream));
+  });
+}
+
+// ---- GridLeaper brick cache
+
+tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_source,
+                           tvk_pool** out) {
+  return guarded([&] {
+    REQUIRE(v && out, "null argument");
+    if (v->rebricked) tvk::fail(TVK_ERR_UNSUPPORTED, "pools are built over bricked volumes");
+    const size_t n_lods = v->lod_first.size() - 1;
+    if (n_lods != v->lods.size())
+      tvk::fail(TVK_ERR_UNSUPPORTED, "the GridLeaper needs every LOD (volume built with LODs)");
+    REQUIRE(n_lods <= tvk::kLeaperMaxLods, "too many LODs");
+    std::unique_ptr<tvk_pool> P(new tvk_pool());
+    P->vol = v;
+    P->device = v->device;
+    TVK_CUDA(cudaSetDevice(v->device));
+    for (uint64_t k = 0; k < v->total_bricks; ++k)
+      P->slot_voxels = std::max<uint64_t>(P->slot_voxels, uint64_t(v->sizes[3 * k]) *
+                                                              v->sizes[3 * k + 1] * v->sizes[3 * k + 2]);
+    const uint64_t slot_bytes = P->slot_voxels * v->bytes;
+    P->n_slots = uint32_t(std::min<uint64_t>(v->total_bricks, budget_bytes / slot_bytes));
+    REQUIRE(P->n_slots >= 2, "the budget holds fewer than two bricks");
+    P->d_slots.ensure(size_t(P->n_slots) * slot_bytes);
+    P->host_source = host_source != 0;
+    tvk::device_bricks(v);  // the bricks are copied or paged from the device pool
+    if (P->host_source) {
+      P->h_bricks.ensure(v->pool_bytes);
+      TVK_CUDA(cudaMemcpy(P->h_bricks.p, tvk::device_bricks(v), v->pool_bytes,
+                          cudaMemcpyDeviceToHost));
+    }
+    P->page.assign(v->total_bricks, tvk::kBiMissing);
+    P->h_page.ensure(v->total_bricks * sizeof(uint32_t));
+    P->d_page.ensure(v->total_bricks * sizeof(uint32_t));
+    std::vector<uint32_t> dims(v->total_bricks);
+    for (uint64_t k = 0; k < v->total_bricks; ++k)
+      dims[k] = v->sizes[3 * k] | (v->sizes[3 * k + 1] << 10) | (v->sizes[3 * k + 2] << 20);
+    P->d_dims.ensure(v->total_bricks * sizeof(uint32_t));
+    TVK_CUDA(cudaMemcpy(P->d_dims.p, dims.data(), dims.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice));
+    // GLGridLeaper.cpp:266-273: hash table size from the brick volume
+    const double rmax = double(v->brick_size[0]) * v->brick_size[1] * v->brick_size[2] / 32768.0;
+    P->hash_size = std::max<uint32_t>(15, uint32_t(509 / rmax));
+    P->d_hash.ensure(P->hash_size * sizeof(uint32_t));
+    P->h_hash.ensure(P->hash_size * sizeof(uint32_t));
+    TVK_CUDA(cudaStreamCreateWithFlags(&P->page_stream, cudaStreamNonBlocking));
+    TVK_CUDA(cudaEventCreateWithFlags(&P->ev_paged, cudaEventDisableTiming));
+    P->slots.assign(P->n_slots, tvk_pool::Slot{});
+    // the single brick of the coarsest LOD stays in the last slot
+    P->coarsest = uint32_t(v->total_bricks - 1);
+    tvk::pool_upload(P.get(), P->n_slots - 1, P->coarsest, ~uint64_t(0));
+    tvk::pool_upload_page_table(P.get());
+    TVK_CUDA(cudaStreamSynchronize(P->page_stream));
+    *out = P.release();
+  });
+}
+
+tvk_status tvk_pool_destroy(tvk_pool* p) {
+  return guarded([&] {
+    if (!p) return;
+    if (p->page_stream) cudaStreamSynchronize(p->page_stream);
+    if (p->ev_paged) cudaEventDestroy(p->ev_paged);
+    if (p->page_stream) cudaStreamDestroy(p->page_stream);
+    delete p;
+  });
+}
+
+tvk_status tvk_pool_get_page_table(const tvk_pool* p, uint32_t* out, size_t n) {
+  return guarded([&] {
+    REQUIRE(p && out, "null argument");
+    REQUIRE(n >= p->page.size(), "output smaller than the page table");
+    std::memcpy(out, p->page.data(), p->page.size() * sizeof(uint32_t));
+  });
+}
+
+tvk_status tvk_pool_get_requests(const tvk_pool* p, uint64_t* out, size_t n, size_t* count) {
+  return guarded([&] {
+    REQUIRE(p && count, "null argument");
+    REQUIRE(out || n == 0, "null output");
+    const size_t k = std::min(n, p->requests.size());
+    std::copy(p->requests.begin(), p->requests.begin() + k, out);
+    *count = p->requests.size();
+  });
+}
+
+tvk_status tvk_pool_get_info(const tvk_pool* p, tvk_pool_info* out) {
+  return guarded([&] {
+    REQUIRE(p && out, "null argument");
+    out->slots = p->n_slots;
+    out->slot_bytes = p->slot_voxels * p->vol->bytes;
+    out->bricks = p->vol->total_bricks;
+    out->hash_size = p->hash_size;
+    out->host_source = p->host_source ? 1 : 0;
+    out->paged_total = p->paged_total;
+  });
+}
+
+tvk_status tvk_leaper_paint(tvk_renderer* r, tvk_pool* pool, uint32_t max_passes,
+                            tvk_leaper_info* info) {
+  return guarded([&] {
+    REQUIRE(r && pool && info, "null argument");
+    tvk::leaper_paint(r, pool, max_passes, info);
   });
 }
 

@@ -787,6 +787,361 @@ void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, 
 
 namespace {
 
+// ================================================================= GridLeaper
+//
+// One GLGridLeaper pass per pixel (GLGridLeaper-blend.glsl:65-228 and
+// GLGridLeaper-iso.glsl:68-200): along the ray in normalised volume
+// coordinates, pick a LOD from the eye-space depth, look the brick up in the
+// page table (falling back to coarser LODs and reporting the miss to the hash
+// table), leap over EMPTY / CHILD_EMPTY bricks, and march resident bricks in
+// steps of 0.5/srm voxel of their LOD.  Positions inside a brick are its local
+// texel coordinates (the pool texture coordinates of GLVolumePool.cpp:529-545
+// scaled by the pool size and shifted to the slot), so the result does not
+// depend on which cache slot holds the brick.
+
+// lighting.glsl:33-43 with a model-space eye (GLGridLeaper-Method-1D-L.glsl)
+__device__ __forceinline__ void lighting_eye(const LeaperParams& L, const float pos[3],
+                                             const float N[3], const float tfc[3], float out[3]) {
+  const RenderParams& P = L.R;
+  const float p0 = L.eye_model[0] - pos[0], p1 = L.eye_model[1] - pos[1],
+              p2 = L.eye_model[2] - pos[2];
+  const float lp = len3(p0, p1, p2);
+  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  const float d = (N[0] * V0 + N[1] * V1) + N[2] * V2;
+  float R0 = V0 - (2.0f * d) * N[0];
+  float R1 = V1 - (2.0f * d) * N[1];
+  float R2 = V2 - (2.0f * d) * N[2];
+  const float lr = len3(R0, R1, R2);
+  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+  const float* Ld = L.light_dir_model;
+  const float diff = fmaxf(fabsf((N[0] * Ld[0] + N[1] * Ld[1]) + N[2] * Ld[2]), 0.0f);
+  const float spec = pow_int_or_real(fmaxf((R0 * Ld[0] + R1 * Ld[1]) + R2 * Ld[2], 0.0f), 8.0f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float dcol = P.light_d[i] * tfc[i];
+    float c = P.light_a[i] + dcol * diff;
+    c = c + P.light_s[i] * spec;
+    out[i] = fminf(fmaxf(c, 0.0f), 1.0f);
+  }
+}
+
+// GLHashTable.cpp:150-185: key = Serialize(brick), linear probing with
+// atomicCompSwap from 0, at most `rehash` probes
+__device__ __forceinline__ void report_missing(const LeaperParams& L, const uint32_t bc[3],
+                                               uint32_t lod) {
+  const uint32_t key = 1u + bc[0] + bc[1] * L.ser_x + bc[2] * L.ser_xy + lod * L.ser_xyz;
+  for (uint32_t r = 0; r < L.rehash; ++r) {
+    const uint32_t old = atomicCAS(&L.hash[(key + r) % L.hash_size], 0u, key);
+    if (old == 0u || old == key) return;
+  }
+}
+
+// ComputeBrickCoords + GetBrickInfo
+__device__ __forceinline__ uint32_t brick_info(const LeaperParams& L, const float p[3],
+                                               uint32_t lod, uint32_t bc[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) bc[a] = uint32_t(p[a] * L.layout[lod][a]);
+  return __ldg(&L.page[L.lod_offset[lod] + bc[0] + bc[1] * L.lod_lx[lod] + bc[2] * L.lod_lxy[lod]]);
+}
+
+template <class T, bool kIso>
+__global__ void __launch_bounds__(128, 4) leaper_kernel(const LeaperParams L) {
+  const RenderParams& P = L.R;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  const uint32_t py = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  if (px >= P.width || py >= P.height) return;
+  const size_t pix = size_t(py) * P.width + px;
+
+  // eye-space ray through the pixel centre (z = -1) and its normalised-volume
+  // counterpart; the eye point at parameter s has depth (eye z) -s
+  const float nx = (float(px) + 0.5f) * P.inv_w2 - 1.0f;
+  const float ny = (float(py) + 0.5f) * P.inv_h2 - 1.0f;
+  const float de[3] = {nx * P.kx, ny * P.ky, -1.0f};
+  float o[3], d[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = L.eye2norm[a][3];
+    d[a] = fmaf(L.eye2norm[a][2], de[2], fmaf(L.eye2norm[a][1], de[1], L.eye2norm[a][0] * de[0]));
+  }
+  // the volume box [0,1]^3: entry (front faces or the near plane), exit (back faces)
+  float s0 = -INFINITY, s1 = INFINITY;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float inv = 1.0f / d[a];
+    const float ta = (0.0f - o[a]) * inv, tb = (1.0f - o[a]) * inv;
+    s0 = fmaxf(s0, fminf(ta, tb));
+    s1 = fminf(s1, fmaxf(ta, tb));
+  }
+  const float s_in = fmaxf(s0, P.znear);
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!(s1 > s_in) || s1 > P.zfar) {
+    P.out[pix] = acc;
+    L.resume_pos[pix] = make_float4(0.f, 0.f, 0.f, 1000.f);
+    L.resume_col[pix] = acc;
+    if (P.spp) P.spp[pix] = 0;
+    return;
+  }
+  float ent[3], ext[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) ext[a] = fmaf(s1, d[a], o[a]);
+  const float exit_depth = -s1;
+  float entry_depth;
+  if (L.first_pass) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ent[a] = fmaf(s_in, d[a], o[a]);
+    entry_depth = -s_in;
+  } else {
+    const float4 rp = L.resume_pos[pix];
+    if (rp.w == 1000.0f) {  // finished in an earlier pass
+      P.out[pix] = L.resume_col[pix];
+      if (P.spp) P.spp[pix] = 0;
+      return;
+    }
+    ent[0] = rp.x; ent[1] = rp.y; ent[2] = rp.z;
+    entry_depth = rp.w;
+    acc = L.resume_col[pix];
+  }
+  float4 res_pos = make_float4(ent[0], ent[1], ent[2], entry_depth);
+  float4 res_col = acc;
+  const float dir[3] = {ext[0] - ent[0], ext[1] - ent[1], ext[2] - ent[2]};
+  const float ray_len = len3(dir[0], dir[1], dir[2]);
+  // TransformToPoolSpace: 0.5 / srm texel of the brick's LOD per step
+  float sv[3] = {dir[0] * L.vol_size[0], dir[1] * L.vol_size[1], dir[2] * L.vol_size[2]};
+  {
+    const float l = len3(sv[0], sv[1], sv[2]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) sv[a] = (sv[a] / l) / (2.0f * L.srm);
+  }
+  const float step_len = len3(sv[0], sv[1], sv[2]);
+  const float voxel_eps = 0.125f / 2000.0f;
+  const float im = P.inv_max_raw;
+  const float W = float(P.tf_w), H = float(P.tf_h);
+  const bool lit = P.lighting != 0;
+  const bool two_d = P.mode == TVK_RM_2DTRANS;
+  float cur[3] = {ent[0], ent[1], ent[2]};
+  float t = 0.0f;
+  bool optimal = true;
+  uint32_t last[4] = {0u, 0u, 0u, 9999u};
+  uint32_t samples = 0;
+  bool hit = false;
+  float4 hit_col = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  if (ray_len > voxel_eps) {
+    for (uint32_t j = 0; j < 100; ++j) {
+      const float depth = entry_depth * (1.0f - t) + exit_depth * t;
+      // ComputeLOD (GLVolumePool.cpp:650-653); a negative level is level 0
+      const float lv = log2f(L.lod_factor * (-depth) / L.lod0_err);
+      uint32_t lod = lv > 0.0f ? min(L.max_lod, uint32_t(lv)) : 0u;
+      // GetBrick (GLVolumePool.cpp:553-612)
+      float p[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) p[a] = fminf(fmaxf(cur[a], 0.0f), 1.0f);
+      bool found = true;
+      uint32_t bc[3];
+      uint32_t info = brick_info(L, p, lod, bc);
+      if (info == kBiMissing) {
+        report_missing(L, bc, lod);
+        found = false;
+        while (info == kBiMissing && lod < L.max_lod) {
+          ++lod;
+          info = brick_info(L, p, lod, bc);
+        }
+        if (info == kBiMissing) info = kBiEmpty;  // the coarsest brick is always resident
+      }
+      const bool empty = info <= kBiEmpty;
+      if (empty) {
+        for (uint32_t l = lod + 1; l < L.max_lod; ++l) {
+          uint32_t lbc[3];
+          const uint32_t linfo = brick_info(L, p, l, lbc);
+          if (linfo != kBiChildEmpty) break;
+          bc[0] = lbc[0]; bc[1] = lbc[1]; bc[2] = lbc[2];
+          info = linfo;
+          lod = l;
+        }
+      }
+      float c0[3], c1[3], bexit[3];
+      float tmin = INFINITY;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        c0[a] = float(bc[a]) / L.layout[lod][a];
+        c1[a] = float(bc[a] + 1u) / L.layout[lod][a];
+        const float div = 1.0f / dir[a];
+        const float corner = div >= 0.0f ? c1[a] : c0[a];
+        tmin = fminf(tmin, (corner - p[a]) * div);
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) bexit[a] = fmaf(tmin, dir[a], p[a]);
+      if (!found && optimal) {
+        optimal = false;
+        res_pos = make_float4(cur[0], cur[1], cur[2], depth);
+        res_col = acc;
+      }
+      const bool same = last[0] == bc[0] && last[1] == bc[1] && last[2] == bc[2] && last[3] == lod;
+      if (!empty && !same) {
+        const uint32_t gid = L.lod_offset[lod] + bc[0] + bc[1] * L.lod_lx[lod] +
+                             bc[2] * L.lod_lxy[lod];
+        const uint32_t dims = __ldg(&L.brick_dims[gid]);
+        BrickView<T> vol;
+        vol.p = static_cast<const T*>(L.slots) + size_t(info - kBiFlagCount) * L.slot_voxels;
+        vol.n0 = int(dims & 1023u); vol.n1 = int((dims >> 10) & 1023u); vol.n2 = int(dims >> 20);
+        vol.fn0 = float(vol.n0); vol.fn1 = float(vol.n1); vol.fn2 = float(vol.n2);
+        vol.sx = uint32_t(vol.n0); vol.sxy = uint32_t(vol.n0 * vol.n1);
+        float sc[3], tr[3], pc[3], pe[3], pxx[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          sc[a] = L.max_inner[a] * L.layout[lod][a];
+          tr[a] = L.ghost - c0[a] * sc[a];
+          pe[a] = fmaf(p[a], sc[a], tr[a]);
+          pxx[a] = fmaf(bexit[a], sc[a], tr[a]);
+          pc[a] = pe[a];
+        }
+        int steps = int(ceilf(len3(pxx[0] - pe[0], pxx[1] - pe[1], pxx[2] - pe[2]) / step_len));
+        steps = min(steps, int(ceilf(len3((ext[0] - cur[0]) * sc[0], (ext[1] - cur[1]) * sc[1],
+                                          (ext[2] - cur[2]) * sc[2]) / step_len)));
+        auto sample = [&](float l0, float l1, float l2) -> float {
+          const float u0 = fminf(fmaxf(l0 - 0.5f, 0.0f), vol.fn0 - 1.0f);
+          const float u1 = fminf(fmaxf(l1 - 0.5f, 0.0f), vol.fn1 - 1.0f);
+          const float u2 = fminf(fmaxf(l2 - 0.5f, 0.0f), vol.fn2 - 1.0f);
+          return vol.sample_u(u0, u1, u2) * im;
+        };
+        bool done = false;
+        for (int i = 0; i < steps; ++i) {
+          ++samples;
+          const float v = sample(pc[0], pc[1], pc[2]);
+          if (kIso) {
+            // GLGridLeaper-Method-iso.glsl: first sample >= fIsoval, 5 bisections
+            if (v >= P.iso_norm) {
+              float r[3] = {sv[0] / 2.0f, sv[1] / 2.0f, sv[2] / 2.0f};
+              float q[3] = {pc[0] - r[0], pc[1] - r[1], pc[2] - r[2]};
+              for (int k = 0; k < 5; ++k) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) r[a] = r[a] / 2.0f;
+                const float vv = sample(q[0], q[1], q[2]);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) q[a] = vv >= P.iso_norm ? q[a] - r[a] : q[a] + r[a];
+              }
+              // hit position (eye space) and normal (ComputeNormal, to eye space)
+              float hn[3], he[3], g[3];
+              const float xp = sample(q[0] + 1.0f, q[1], q[2]), xm = sample(q[0] - 1.0f, q[1], q[2]);
+              const float yp = sample(q[0], q[1] - 1.0f, q[2]), ym = sample(q[0], q[1] + 1.0f, q[2]);
+              const float zp = sample(q[0], q[1], q[2] + 1.0f), zm = sample(q[0], q[1], q[2] - 1.0f);
+              g[0] = ((xm - xp) / 2.0f) * P.domain_scale[0];
+              g[1] = ((yp - ym) / 2.0f) * P.domain_scale[1];
+              g[2] = ((zm - zp) / 2.0f) * P.domain_scale[2];
+              const float gl = len3(g[0], g[1], g[2]);
+              if (gl > 0.0f) { g[0] = g[0] / gl; g[1] = g[1] / gl; g[2] = g[2] / gl; }
+              float hp[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) hp[a] = (q[a] - tr[a]) / sc[a];
+#pragma unroll
+              for (int r2 = 0; r2 < 3; ++r2) {
+                he[r2] = affine_row(L.norm2eye[r2], hp[0], hp[1], hp[2]);
+                hn[r2] = fmaf(L.norm_to_eye_n[r2][2], g[2],
+                              fmaf(L.norm_to_eye_n[r2][1], g[1], L.norm_to_eye_n[r2][0] * g[0]));
+              }
+              IsoHit h;
+              h.pos[0] = he[0]; h.pos[1] = he[1]; h.pos[2] = he[2];
+              h.n[0] = hn[0]; h.n[1] = hn[1]; h.n[2] = hn[2];
+              h.f = 1.0f;
+              h.depth = 0.0f;
+              hit_col = iso_compose(P, h);
+              hit = true;
+              done = true;
+              break;
+            }
+          } else {
+            float4 src;
+            const float u = v * P.trans_scale;
+            float fx = floorf(u * W);
+            fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
+            float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+            bool need_grad = lit;
+            if (two_d) need_grad = P.tf_col_nonzero[int(fx)] != 0;
+            if (!two_d) {
+              src = __ldg(&P.tf[int(fx)]);
+              need_grad = lit && src.w != 0.0f;
+            }
+            if (need_grad) {
+              // GLGridLeaper-GradientTools.glsl:6-19 (Yp sampled at -delta.y)
+              const float xp = sample(pc[0] + 1.0f, pc[1], pc[2]), xm = sample(pc[0] - 1.0f, pc[1], pc[2]);
+              const float yp = sample(pc[0], pc[1] - 1.0f, pc[2]), ym = sample(pc[0], pc[1] + 1.0f, pc[2]);
+              const float zp = sample(pc[0], pc[1], pc[2] + 1.0f), zm = sample(pc[0], pc[1], pc[2] - 1.0f);
+              g0 = (xm - xp) / 2.0f;
+              g1 = (yp - ym) / 2.0f;
+              g2 = (zm - zp) / 2.0f;
+            }
+            float mag = 0.0f;
+            if (two_d) {
+              if (need_grad) {
+                mag = len3(g0, g1, g2);
+                const float w = 1.0f - mag * P.grad_scale;
+                float fy = floorf(w * H);
+                fy = fminf(fmaxf(fy, 0.0f), H - 1.0f);
+                src = __ldg(&P.tf[int(fy) * P.tf_w + int(fx)]);
+              } else {
+                src = make_float4(0.f, 0.f, 0.f, 0.f);
+              }
+              need_grad = need_grad && lit && src.w != 0.0f;
+            }
+            if (lit && need_grad) {
+              float N[3];
+              if (two_d) {  // GLGridLeaper-Method-2D-L.glsl: domain scale * g / |g|
+                const float q0 = mag > 0.0f ? g0 / mag : g0, q1 = mag > 0.0f ? g1 / mag : g1,
+                            q2 = mag > 0.0f ? g2 / mag : g2;
+                N[0] = P.domain_scale[0] * q0; N[1] = P.domain_scale[1] * q1;
+                N[2] = P.domain_scale[2] * q2;
+              } else {      // ComputeNormal: g * domain scale, safely normalised
+                N[0] = g0 * P.domain_scale[0]; N[1] = g1 * P.domain_scale[1];
+                N[2] = g2 * P.domain_scale[2];
+                const float l = len3(N[0], N[1], N[2]);
+                if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+              }
+              float mp[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) mp[a] = (pc[a] - tr[a]) / sc[a];
+              const float tfc[3] = {src.x, src.y, src.z};
+              float lc[3];
+              lighting_eye(L, mp, N, tfc, lc);
+              src.x = lc[0]; src.y = lc[1]; src.z = lc[2];
+            }
+            // Compositing.glsl UnderCompositing
+            const float w = 1.0f - acc.w;
+            acc.x = fmaf(src.x * w, src.w, acc.x);
+            acc.y = fmaf(src.y * w, src.w, acc.y);
+            acc.z = fmaf(src.z * w, src.w, acc.z);
+            acc.w = fmaf(src.w, w, acc.w);
+            if (acc.w > 0.99f) { done = true; break; }
+          }
+#pragma unroll
+          for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
+        }
+        if (done) break;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) cur[a] = (pc[a] - tr[a]) / sc[a];
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) cur[a] = fmaf(voxel_eps, dir[a] / ray_len, bexit[a]);
+      }
+      last[0] = bc[0]; last[1] = bc[1]; last[2] = bc[2]; last[3] = lod;
+      t = len3(ent[0] - bexit[0], ent[1] - bexit[1], ent[2] - bexit[2]) / ray_len;
+      if (t > 0.9999f) break;
+    }
+  }
+  // TerminateRay: a ray that met only bricks of the wanted resolution is done
+  const float4 out = kIso ? hit_col : acc;
+  if (optimal) {
+    res_pos.w = 1000.0f;
+    res_col = out;
+  }
+  P.out[pix] = out;
+  L.resume_pos[pix] = res_pos;
+  L.resume_col[pix] = res_col;
+  if (P.spp) P.spp[pix] = samples;
+  const uint32_t wsum = __reduce_add_sync(__activemask(), samples);
+  if ((lane == __ffs(__activemask()) - 1)) atomicAdd(&P.counters[0], (unsigned long long)wsum);
+}
+
 __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float w) {
   return make_float4(fmaf(w, b.x - a.x, a.x), fmaf(w, b.y - a.y, a.y), fmaf(w, b.z - a.z, a.z),
                      fmaf(w, b.w - a.w, a.w));
@@ -846,6 +1201,20 @@ void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_it
     case 1: raycast_batch_kernel<uint8_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
     case 2: raycast_batch_kernel<uint16_t, false><<<ctas, 128, 0, s>>>(L, d_next_item); break;
     default: raycast_batch_kernel<uint16_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+  }
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_leaper(const LeaperParams& p, cudaStream_t s, uint64_t* launches) {
+  const dim3 grid((p.R.width + 15) / 16, (p.R.height + 7) / 8);
+  const bool iso = p.R.mode == TVK_RM_ISOSURFACE;
+  if (p.R.bytes == 1) {
+    if (iso) leaper_kernel<uint8_t, true><<<grid, 128, 0, s>>>(p);
+    else leaper_kernel<uint8_t, false><<<grid, 128, 0, s>>>(p);
+  } else {
+    if (iso) leaper_kernel<uint16_t, true><<<grid, 128, 0, s>>>(p);
+    else leaper_kernel<uint16_t, false><<<grid, 128, 0, s>>>(p);
   }
   TVK_CUDA(cudaGetLastError());
   ++*launches;

@@ -276,11 +276,11 @@ tvk_volume* rebrick_volume(const tvk_volume* S, const uint32_t Bt[3], int mm_mod
   const dim3 grid(uint32_t(n), (max_tz + kZChunk - 1) / kZChunk);
   if (V->bytes == 1)
     rebrick_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
-        static_cast<const uint8_t*>(S->d_pool), static_cast<uint8_t*>(V->d_pool),
+        static_cast<const uint8_t*>(device_bricks(S)), static_cast<uint8_t*>(V->d_pool),
         static_cast<const RebrickEntry*>(d_table.p), bmin, bmax);
   else
     rebrick_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
-        static_cast<const uint16_t*>(S->d_pool), static_cast<uint16_t*>(V->d_pool),
+        static_cast<const uint16_t*>(device_bricks(S)), static_cast<uint16_t*>(V->d_pool),
         static_cast<const RebrickEntry*>(d_table.p), bmin, bmax);
   TVK_CUDA(cudaGetLastError());
   std::vector<uint32_t> mn(n), mx(n);

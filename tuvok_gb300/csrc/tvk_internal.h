@@ -204,6 +204,42 @@ void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_it
                           uint32_t ctas, cudaStream_t s, uint64_t* launches);
 int batch_ctas_per_sm_max(int variant);
 const void* batch_kernel_function(int variant);
+// ------------------------------------------------------------------ GridLeaper
+
+// Page-table entries (GLVolumePool.cpp:25-30): flags, or the slot + kBiFlagCount
+constexpr uint32_t kBiMissing = 0, kBiChildEmpty = 1, kBiEmpty = 2, kBiFlagCount = 3;
+constexpr uint32_t kLeaperMaxLods = 20;
+
+// One GridLeaper pass (GLGridLeaper-blend.glsl / -iso.glsl over the functions
+// GLVolumePool.cpp:484-656 generates).  Shading, TF and camera fields come from
+// the renderer's RenderParams.
+struct LeaperParams {
+  RenderParams R;
+  const void* slots;           // brick cache: slot s at slots + s * slot_voxels
+  uint64_t slot_voxels;
+  const uint32_t* page;        // page table over the bricks of every LOD
+  const uint32_t* brick_dims;  // per brick n_voxels x | y << 10 | z << 20
+  uint32_t max_lod;            // iMaxLOD
+  float layout[kLeaperMaxLods][3];  // GetFloatBrickLayout per LOD
+  uint32_t lod_offset[kLeaperMaxLods], lod_lx[kLeaperMaxLods], lod_lxy[kLeaperMaxLods];
+  float vol_size[3];           // LOD-0 voxels (volumeSize)
+  float max_inner[3];          // inner brick size (maxInnerBrickSize)
+  float ghost;                 // overlap voxels per side
+  float lod_factor, lod0_err;  // fLoDFactor, fLevelZeroWorldSpaceError
+  float eye2norm[3][4];        // eye space -> normalised volume coordinates
+  float norm2eye[3][4];
+  float norm_to_eye_n[3][3];   // normals (mModelViewIT)
+  float light_dir_model[3], eye_model[3];
+  float srm;
+  uint32_t* hash;              // missing-brick hash table (GLHashTable)
+  uint32_t hash_size, rehash;
+  uint32_t ser_x, ser_xy, ser_xyz;  // Serialize: LOD-0 layout x, x*y, x*y*z
+  float4* resume_pos;          // xyz = normalised position, w = depth (1000: done)
+  float4* resume_col;
+  uint32_t first_pass;
+};
+void launch_leaper(const LeaperParams& p, cudaStream_t s, uint64_t* launches);
+
 // Bilinear stretch of a reduced-resolution image over the viewport
 // (GLRenderer::CopyOverCompletedRegion with GL_LINEAR).
 void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, uint32_t w,
@@ -278,5 +314,16 @@ struct tvk_volume {
 };
 
 struct tvk_renderer;
+
+namespace tvk {
+// The volume's device brick pool; an error once tvk_volume_release_bricks
+// moved the bricks to host memory (only a GridLeaper pool paging from its
+// pinned host copy renders such a volume).
+inline const void* device_bricks(const tvk_volume* V) {
+  if (!V->d_pool)
+    fail(TVK_ERR_STATE, "the volume's bricks were released from device memory");
+  return V->d_pool;
+}
+}  // namespace tvk
 
 static_assert(sizeof(tvk::DevBrick) == 112, "DevBrick layout is part of the per-frame upload size");

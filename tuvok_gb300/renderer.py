@@ -171,6 +171,11 @@ class Volume:
     def GetMaxBrickSize(self):
         return tuple(self.info.brick_size)
 
+    def ReleaseBricks(self):
+        """Frees the device brick pool (tvk_volume_release_bricks): afterwards
+        only a host-sourced Pool renders the volume."""
+        check(lib().tvk_volume_release_bricks(self._h))
+
     def GetMaxUsedBrickSizes(self):
         out = _u32((0, 0, 0))
         check(lib().tvk_volume_get_max_used_brick_size(self._h, out))
@@ -369,6 +374,60 @@ class Batch:
     def GetInfo(self):
         info = N.BatchInfo()
         check(lib().tvk_batch_get_info(self._h, C.byref(info)))
+        return info
+
+
+class Pool:
+    """The GridLeaper's brick cache over a bricked volume (GLVolumePool): a
+    device pool of brick slots holding at most ``budget_bytes``, a page table of
+    every brick of every LOD, and the missing-brick hash table.  With
+    ``host_source`` the bricks are paged from a pinned host copy (the
+    out-of-core path); otherwise from the volume's device pool."""
+
+    def __init__(self, volume, budget_bytes, host_source=False):
+        h = C.c_void_p()
+        check(lib().tvk_pool_create(volume.handle, int(budget_bytes), int(bool(host_source)),
+                                    C.byref(h)))
+        self._h = h
+        self._vol = volume  # the pool reads the volume's bricks
+
+    def close(self):
+        if self._h:
+            check(lib().tvk_pool_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def GetInfo(self):
+        info = N.PoolInfo()
+        check(lib().tvk_pool_get_info(self._h, C.byref(info)))
+        return info
+
+    def GetPageTable(self):
+        """Entry per brick in TOC order: 0 MISSING, 1 CHILD_EMPTY, 2 EMPTY, else slot + 3."""
+        n = self.GetInfo().bricks
+        out = np.empty(n, dtype=np.uint32)
+        check(lib().tvk_pool_get_page_table(self._h, out.ctypes.data_as(N._u32p), n))
+        return out
+
+    def GetRequests(self):
+        """TOC indices of the bricks the last pass reported missing (ascending)."""
+        n = C.c_size_t()
+        check(lib().tvk_pool_get_requests(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint64)
+        if n.value:
+            check(lib().tvk_pool_get_requests(self._h, out.ctypes.data_as(N._u64p), n.value,
+                                              C.byref(n)))
+        return out.astype(np.int64)
+
+    def Paint(self, renderer, max_passes=32):
+        """One GridLeaper frame of ``renderer`` (tvk_leaper_paint); returns LeaperInfo."""
+        info = N.LeaperInfo()
+        check(lib().tvk_leaper_paint(renderer._h, self._h, int(max_passes), C.byref(info)))
         return info
 
 
