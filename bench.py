@@ -57,6 +57,16 @@ def parse():
     p.add_argument("--learned-quality-poses", type=int, default=24)
     p.add_argument("--learned-ssim-poses", type=int, default=6)
     p.add_argument("--frame-ert", type=float, default=1.0)
+    p.add_argument("--no-ooc", action="store_true",
+                   help="skip the out-of-core GridLeaper fly-through")
+    p.add_argument("--ooc-dim", type=int, default=2048,
+                   help="edge of the out-of-core volume (the 4096^3 case needs ~150 GB of HBM "
+                        "while bricking and ~82 GB of pinned host memory)")
+    p.add_argument("--ooc-frames", type=int, default=0, help="timed frames (0: all 300)")
+    p.add_argument("--ooc-warmup", type=int, default=3)
+    p.add_argument("--ooc-passes", type=int, default=64)
+    p.add_argument("--ooc-request-table", type=int, default=1024,
+                   help="hash-table entries of the second fly-through")
     return p.parse_args()
 
 
@@ -430,6 +440,111 @@ def run_learned(args, torch, r, w, poses, plain_fps):
     }
 
 
+def h2d_peak_gbs(torch, nbytes=1 << 30):
+    """Pinned host -> device copy bandwidth (best of 5 single 1 GiB copies)."""
+    src = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    best = 0.0
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        dst.copy_(src, non_blocking=True)
+        b.record()
+        b.synchronize()
+        best = max(best, nbytes / (a.elapsed_time(b) / 1000.0) / 1e9)
+    del src, dst
+    return best
+
+
+def run_ooc(args, torch):
+    """Out-of-core LOD rendering with the GridLeaper: the bricks live in pinned
+    host memory (the device pool is released), a bounded brick cache is paged
+    over the host link between traversal passes, isosurface 128 lit at 1080p
+    along a seeded fly-through.  One step = one frame: passes until nothing is
+    missing or --ooc-passes."""
+    from tuvok_gb300 import Pool, Renderer
+    from tuvok_gb300.workloads import flythrough_poses, ooc_lod
+    w = ooc_lod(args.ooc_dim)
+    peak_h2d = h2d_peak_gbs(torch)
+    vol, raw, brick_s = make_volume(w, torch)
+    del raw
+    torch.cuda.empty_cache()
+    pool_bytes = vol.info.device_bytes
+    t0 = time.perf_counter()
+    pool = Pool(vol, w.extra["cache_bytes"], host_source=True)
+    host_copy_s = time.perf_counter() - t0
+    vol.ReleaseBricks()
+    torch.cuda.empty_cache()
+    pinfo = pool.GetInfo()
+    r = Renderer()
+    r.RegisterDataset(vol)
+    r.SetRendermode(2)
+    r.SetIsoValue(w.extra["iso"])
+    r.SetUseLighting(True)
+    r.SetSampleRateModifier(w.srm)
+    r.Resize(w.width, w.height)
+    poses = flythrough_poses(w.n_poses, w.seed + 77)
+
+    def frame(i):
+        eye, at, up = poses[i % len(poses)]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        return pool.Paint(r, max_passes=args.ooc_passes)
+
+    def flythrough():
+        for i in range(args.ooc_warmup):
+            frame(i)
+        torch.cuda.synchronize()
+        K = args.ooc_frames or len(poses)
+        infos = []
+        t0 = time.perf_counter()
+        for i in range(K):
+            infos.append(frame(args.ooc_warmup + i))
+        wall = time.perf_counter() - t0
+        f = {k: np.array([getattr(x, k) for x in infos], dtype=np.float64)
+             for k in ("passes", "paged", "bytes_paged", "ms", "ms_traversal", "converged",
+                       "samples")}
+        page_s = max(float(np.sum(f["ms"] - f["ms_traversal"])) / 1000.0, 1e-9)
+        return {
+            "hash_size": int(pool.GetInfo().hash_size),
+            "frames": K, "frames_per_s": K / wall, "ms_per_frame_wall": wall * 1000.0 / K,
+            "gpu_ms_per_frame": float(np.mean(f["ms"])),
+            "traversal_ms_per_frame": float(np.mean(f["ms_traversal"])),
+            "passes_per_frame": float(np.mean(f["passes"])),
+            "converged_fraction": float(np.mean(f["converged"])),
+            "bricks_paged_per_frame": float(np.mean(f["paged"])),
+            "paged_bytes_per_frame": float(np.mean(f["bytes_paged"])),
+            "paging_gb_per_s_outside_traversal": float(np.sum(f["bytes_paged"])) / page_s / 1e9,
+            "msamples_per_s_traversal": float(np.sum(f["samples"])) /
+                                        max(float(np.sum(f["ms_traversal"])), 1e-9) / 1e3,
+            "gpu_launches_per_frame": float(np.mean(f["passes"])),
+        }
+
+    ref_table = flythrough()
+    pool.Reset()
+    pool.SetRequestTable(args.ooc_request_table, 10)
+    big_table = flythrough()
+    return {
+        "workload": w.name, "dims": list(w.dims), "voxel": "u8", "brick": list(w.brick_size),
+        "lods": int(vol.GetLODLevelCount()),
+        "bricks": int(pinfo.bricks), "brick_bytes_total": pool_bytes,
+        "cache": {"slots": int(pinfo.slots), "bytes": int(pinfo.slots) * int(pinfo.slot_bytes),
+                  "budget": w.extra["cache_bytes"]},
+        "mode": "iso 128 lit (5 bisection steps)", "width": w.width, "height": w.height,
+        "warmup_frames": args.ooc_warmup, "max_passes": args.ooc_passes,
+        "reference_request_table": ref_table,
+        "enlarged_request_table": big_table,
+        "h2d_peak_gbs": peak_h2d,
+        "bricking_s": brick_s, "host_copy_s": host_copy_s,
+        "note": "the bricks are built on the GPU, copied to pinned host memory, and the "
+                "device copy is freed (tvk_volume_release_bricks): only the cache is on the "
+                "GPU. Frames page the bricks a pass reports through the hash table; the "
+                "reference's table holds 15 entries for 130^3 bricks, the enlarged one "
+                "lets a pass request more. The cache is emptied (PH_Reset) between the runs. "
+                "GPU time outside the traversal holds the hash read-back, the host's page "
+                "table update and the pinned-host copies",
+    }
+
+
 def run_ours(args):
     import torch
     from tuvok_gb300 import Renderer
@@ -527,6 +642,14 @@ def run_ours(args):
         torch.cuda.empty_cache()
         batching = run_batching(args, torch, args.batch_steps)
 
+    ooc = None
+    if not args.no_ooc:
+        import gc
+        r = vol = None
+        gc.collect()
+        torch.cuda.empty_cache()
+        ooc = run_ooc(args, torch)
+
     cpu = None
     if raw_host is not None:
         threads = os.cpu_count() or 1
@@ -576,6 +699,7 @@ def run_ours(args):
             "clocks": clocks.summary(),
             "learned": learned,
             "batching": batching,
+            "out_of_core": ooc,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -536,6 +536,9 @@ typedef struct tvk_leaper_info {
   int converged;          /* 1: the last pass found every brick it wanted */
   uint32_t resident;      /* bricks in the cache after the frame */
   float ms;               /* GPU time of the frame, paging included */
+  float ms_traversal;     /* of which in the traversal kernels */
+  uint64_t bytes_paged;   /* brick bytes copied into the cache this frame */
+  uint64_t samples;       /* samples over all passes */
 } tvk_leaper_info;
 
 tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_source,
@@ -549,6 +552,18 @@ tvk_status tvk_pool_get_page_table(const tvk_pool* p, uint32_t* out, size_t n);
  * through the hash table (GLHashTable::GetData, GLHashTable.cpp:90-105): the
  * first min(n, *count) are written, *count is the total. */
 tvk_status tvk_pool_get_requests(const tvk_pool* p, uint64_t* out, size_t n, size_t* count);
+
+/* GLVolumePool::PH_Reset (GLVolumePool.cpp:261-282): empties the cache except
+ * the slot holding the coarsest brick; visibility is recomputed on the next
+ * tvk_leaper_paint. */
+tvk_status tvk_pool_reset(tvk_pool* p);
+
+/* Size of the missing-brick hash table (GLHashTable, GLGridLeaper.cpp:266-273):
+ * 0 restores the reference's max(15, 509 / (brick voxels / 32768)) with 10
+ * probes; otherwise `size` entries and `rehash` probes.  A pass reports at
+ * most `size` bricks, so with 128^3 bricks the reference's 15 entries bound
+ * the bricks paged per pass. */
+tvk_status tvk_pool_set_request_table(tvk_pool* p, uint32_t size, uint32_t rehash);
 
 /* One GridLeaper frame with the renderer's TF, mode (1D, 2D, iso), lighting,
  * sample rate and view (GLGridLeaper::Render3DRegion, GLGridLeaper.cpp:914-1154):

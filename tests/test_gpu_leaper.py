@@ -303,3 +303,36 @@ def test_gpu_leaper_released_device_bricks(cuda_ok, vols):
     np.testing.assert_array_equal(imgs[0][0], imgs[1][0])
     np.testing.assert_array_equal(imgs[0][1], imgs[1][1])
     assert imgs[0][2] == imgs[1][2] > 0
+
+
+def test_gpu_leaper_request_table_and_reset(cuda_ok, vols):
+    """A 4-entry request table reports at most 4 bricks per pass, so the frame
+    needs more passes to converge; PH_Reset empties the cache and the next
+    pass equals a cold pass."""
+    raw = vols["u8"]
+    tf = tf_for("u8", 0)
+    eye = (0.3, 0.4, 1.5)
+    out = {}
+    for size in (0, 4):
+        vol, r = setup(raw, tf, 0, False)
+        pool = Pool(vol, 1 << 30)
+        pool.SetRequestTable(size, 10)
+        assert pool.GetInfo().hash_size == (4 if size else 2859)
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+        info = pool.Paint(r, max_passes=200)
+        assert info.converged == 1
+        out[size] = (info.passes, info.paged, pool.GetPageTable())
+        if size == 4:
+            assert info.passes >= 1 + (info.paged + 3) // 4
+            cold_vol, cold_r = setup(raw, tf, 0, False)
+            cold = Pool(cold_vol, 1 << 30)
+            cold_r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+            cold.Paint(cold_r, max_passes=1)
+            pool.Reset()
+            page = pool.GetPageTable()
+            assert (page >= 3).sum() <= 1
+            one = pool.Paint(r, max_passes=1)
+            assert one.resident <= 1 and one.paged == 0
+            np.testing.assert_array_equal(pool.GetPageTable(), cold.GetPageTable())
+            np.testing.assert_array_equal(r.ReadBackPixels(), cold_r.ReadBackPixels())
+    assert out[4][0] > out[0][0]

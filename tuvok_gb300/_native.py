@@ -87,7 +87,9 @@ class PoolInfo(C.Structure):
 
 class LeaperInfo(C.Structure):
     _fields_ = [("passes", C.c_uint32), ("paged", C.c_uint32), ("missing_last", C.c_uint32),
-                ("converged", C.c_int), ("resident", C.c_uint32), ("ms", C.c_float)]
+                ("converged", C.c_int), ("resident", C.c_uint32), ("ms", C.c_float),
+                ("ms_traversal", C.c_float), ("bytes_paged", C.c_uint64),
+                ("samples", C.c_uint64)]
 
 
 class Stats(C.Structure):
@@ -180,6 +182,8 @@ PROTOTYPES = {
     "tvk_pool_get_info": [_vp, C.POINTER(PoolInfo)],
     "tvk_pool_get_page_table": [_vp, _u32p, C.c_size_t],
     "tvk_pool_get_requests": [_vp, _u64p, C.c_size_t, C.POINTER(C.c_size_t)],
+    "tvk_pool_set_request_table": [_vp, C.c_uint32, C.c_uint32],
+    "tvk_pool_reset": [_vp],
     "tvk_leaper_paint": [_vp, _vp, C.c_uint32, C.POINTER(LeaperInfo)],
     "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
     "tvk_read_image": [_vp, _f32p, C.c_size_t],

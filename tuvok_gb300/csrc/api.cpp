@@ -675,6 +675,7 @@ struct tvk_pool {
   tvk::DevBuf d_resume_pos, d_resume_col;
   cudaStream_t page_stream = nullptr;
   cudaEvent_t ev_paged = nullptr;
+  cudaEvent_t ev_pass[2] = {nullptr, nullptr};  // brackets each traversal launch
   // visibility flags were computed for this state
   bool vis_valid = false;
   int vis_mode = -1;
@@ -1515,6 +1516,12 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   info->reduced_height = low.rh;
 }
 
+// GLGridLeaper.cpp:266-273: hash table size from the brick volume
+uint32_t reference_hash_size(const tvk_volume* v) {
+  const double rmax = double(v->brick_size[0]) * v->brick_size[1] * v->brick_size[2] / 32768.0;
+  return std::max<uint32_t>(15, uint32_t(509 / rmax));
+}
+
 // GLVolumePool.cpp:89-107 GetFloatBrickLayout
 void float_brick_layout(const tvk_volume* V, uint32_t lod, float out[3]) {
   for (int a = 0; a < 3; ++a) {
@@ -1585,7 +1592,7 @@ void pool_visibility(tvk_pool* pool, int mode, double lo, double hi, float iso) 
 // Copies brick `id` into slot `slot` on the paging stream (UploadBrick,
 // GLVolumePool.cpp:673-717): a visible brick evicted from the slot becomes
 // MISSING (one flagged empty keeps its EMPTY / CHILD_EMPTY entry).
-void pool_upload(tvk_pool* pool, uint32_t slot, uint64_t id, uint64_t time) {
+uint64_t pool_upload(tvk_pool* pool, uint32_t slot, uint64_t id, uint64_t time) {
   const tvk_volume* V = pool->vol;
   tvk_pool::Slot& S = pool->slots[slot];
   if (S.brick >= 0 && S.time > 1) pool->page[uint64_t(S.brick)] = kBiMissing;
@@ -1603,6 +1610,7 @@ void pool_upload(tvk_pool* pool, uint32_t slot, uint64_t id, uint64_t time) {
   TVK_CUDA(cudaMemcpyAsync(dst, src, bytes,
                            pool->host_source ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
                            pool->page_stream));
+  return bytes;
 }
 
 void pool_upload_page_table(tvk_pool* pool) {
@@ -1784,10 +1792,19 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
     TVK_CUDA(cudaStreamWaitEvent(R->stream, pool->ev_paged, 0));
     TVK_CUDA(cudaMemsetAsync(pool->d_hash.p, 0, pool->hash_size * sizeof(uint32_t), R->stream));
     TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
+    TVK_CUDA(cudaEventRecord(pool->ev_pass[0], R->stream));
     launch_leaper(L, R->stream, &R->launches);
+    TVK_CUDA(cudaEventRecord(pool->ev_pass[1], R->stream));
     TVK_CUDA(cudaMemcpyAsync(pool->h_hash.p, pool->d_hash.p, pool->hash_size * sizeof(uint32_t),
                              cudaMemcpyDeviceToHost, R->stream));
+    R->h_counters.ensure(4 * sizeof(unsigned long long));
+    TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, R->stream));
     TVK_CUDA(cudaStreamSynchronize(R->stream));
+    float pass_ms = 0.0f;
+    TVK_CUDA(cudaEventElapsedTime(&pass_ms, pool->ev_pass[0], pool->ev_pass[1]));
+    info->ms_traversal += pass_ms;
+    info->samples += R->h_counters.as<unsigned long long>()[0];
     ++info->passes;
     // the missing bricks this pass reported (GLHashTable::GetData)
     std::vector<uint64_t> want;
@@ -1823,16 +1840,13 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
     for (uint64_t id : want) {
       if (ins + 1 >= pool->n_slots) break;  // every slot replaced this round
       if (pool->page[id] >= kBiFlagCount) continue;
-      pool_upload(pool, order[ins++], id, pool->clock++);
+      info->bytes_paged += pool_upload(pool, order[ins++], id, pool->clock++);
       ++info->paged;
       ++pool->paged_total;
     }
     pool_upload_page_table(pool);
   }
   TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
-  R->h_counters.ensure(4 * sizeof(unsigned long long));
-  TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost, R->stream));
   TVK_CUDA(cudaEventSynchronize(R->ev_stop));
   TVK_CUDA(cudaEventElapsedTime(&info->ms, R->ev_start, R->ev_stop));
   uint32_t resident = 0;
@@ -2641,6 +2655,8 @@ tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_
     if (n_lods != v->lods.size())
       tvk::fail(TVK_ERR_UNSUPPORTED, "the GridLeaper needs every LOD (volume built with LODs)");
     REQUIRE(n_lods <= tvk::kLeaperMaxLods, "too many LODs");
+    for (int a = 0; a < 3; ++a)
+      REQUIRE(v->brick_size[a] <= 1023, "pool bricks are at most 1023 voxels per axis");
     std::unique_ptr<tvk_pool> P(new tvk_pool());
     P->vol = v;
     P->device = v->device;
@@ -2668,13 +2684,13 @@ tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_
     P->d_dims.ensure(v->total_bricks * sizeof(uint32_t));
     TVK_CUDA(cudaMemcpy(P->d_dims.p, dims.data(), dims.size() * sizeof(uint32_t),
                         cudaMemcpyHostToDevice));
-    // GLGridLeaper.cpp:266-273: hash table size from the brick volume
-    const double rmax = double(v->brick_size[0]) * v->brick_size[1] * v->brick_size[2] / 32768.0;
-    P->hash_size = std::max<uint32_t>(15, uint32_t(509 / rmax));
+    P->hash_size = tvk::reference_hash_size(v);
     P->d_hash.ensure(P->hash_size * sizeof(uint32_t));
     P->h_hash.ensure(P->hash_size * sizeof(uint32_t));
     TVK_CUDA(cudaStreamCreateWithFlags(&P->page_stream, cudaStreamNonBlocking));
     TVK_CUDA(cudaEventCreateWithFlags(&P->ev_paged, cudaEventDisableTiming));
+    TVK_CUDA(cudaEventCreate(&P->ev_pass[0]));
+    TVK_CUDA(cudaEventCreate(&P->ev_pass[1]));
     P->slots.assign(P->n_slots, tvk_pool::Slot{});
     // the single brick of the coarsest LOD stays in the last slot
     P->coarsest = uint32_t(v->total_bricks - 1);
@@ -2690,6 +2706,8 @@ tvk_status tvk_pool_destroy(tvk_pool* p) {
     if (!p) return;
     if (p->page_stream) cudaStreamSynchronize(p->page_stream);
     if (p->ev_paged) cudaEventDestroy(p->ev_paged);
+    for (cudaEvent_t e : p->ev_pass)
+      if (e) cudaEventDestroy(e);
     if (p->page_stream) cudaStreamDestroy(p->page_stream);
     delete p;
   });
@@ -2710,6 +2728,40 @@ tvk_status tvk_pool_get_requests(const tvk_pool* p, uint64_t* out, size_t n, siz
     const size_t k = std::min(n, p->requests.size());
     std::copy(p->requests.begin(), p->requests.begin() + k, out);
     *count = p->requests.size();
+  });
+}
+
+tvk_status tvk_pool_reset(tvk_pool* p) {
+  return guarded([&] {
+    REQUIRE(p, "null argument");
+    TVK_CUDA(cudaSetDevice(p->device));
+    TVK_CUDA(cudaStreamSynchronize(p->page_stream));
+    // GLVolumePool::PH_Reset (GLVolumePool.cpp:261-282): every slot but the
+    // one holding the coarsest brick is emptied, every entry but that brick's
+    // becomes MISSING, and visibility is recomputed before the next pass
+    const uint32_t keep = p->page[p->coarsest];
+    for (tvk_pool::Slot& sl : p->slots)
+      if (sl.brick != int64_t(p->coarsest)) sl = tvk_pool::Slot{};
+    std::fill(p->page.begin(), p->page.end(), tvk::kBiMissing);
+    p->page[p->coarsest] = keep;
+    p->vis_valid = false;
+    tvk::pool_upload_page_table(p);
+    TVK_CUDA(cudaStreamSynchronize(p->page_stream));
+  });
+}
+
+tvk_status tvk_pool_set_request_table(tvk_pool* p, uint32_t size, uint32_t rehash) {
+  return guarded([&] {
+    REQUIRE(p, "null argument");
+    REQUIRE(size <= (1u << 24), "request table above 2^24 entries");
+    REQUIRE(rehash >= 1 || size == 0, "rehash must be at least 1");
+    TVK_CUDA(cudaSetDevice(p->device));
+    TVK_CUDA(cudaStreamSynchronize(p->page_stream));
+    const uint32_t n = size ? size : tvk::reference_hash_size(p->vol);
+    p->d_hash.ensure(size_t(n) * sizeof(uint32_t));
+    p->h_hash.ensure(size_t(n) * sizeof(uint32_t));
+    p->hash_size = n;
+    p->rehash = size ? rehash : 10u;
   });
 }
 

@@ -414,6 +414,14 @@ class Pool:
         check(lib().tvk_pool_get_page_table(self._h, out.ctypes.data_as(N._u32p), n))
         return out
 
+    def Reset(self):
+        """Empties the cache but for the coarsest brick (GLVolumePool::PH_Reset)."""
+        check(lib().tvk_pool_reset(self._h))
+
+    def SetRequestTable(self, size=0, rehash=10):
+        """Missing-brick hash table size (0: the reference's) and probe count."""
+        check(lib().tvk_pool_set_request_table(self._h, int(size), int(rehash)))
+
     def GetRequests(self):
         """TOC indices of the bricks the last pass reported missing (ascending)."""
         n = C.c_size_t()

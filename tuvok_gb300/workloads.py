@@ -132,6 +132,43 @@ PLAIN_MEDIUM_LIT = Workload(
 WORKLOADS = {w.name: w for w in (PLAIN_SMALL, PLAIN_LARGE_LIT, PLAIN_MEDIUM_LIT)}
 
 
+# Out-of-core LOD rendering (GridLeaper): a logical N^3 uint8 volume of 1024
+# blobs (sigma and noise cell scaled with N / 4096) + 4-octave value noise of
+# amplitude 25.5 (10% of range); bricks of 128^3 core + 1 ghost voxel with
+# every coarser LOD down to one brick; isosurface 128, lit, 1920x1080, 300
+# seeded fly-through frames; a brick cache of (N / 4096)^3 * 24 GB paged from
+# pinned host memory.
+def ooc_lod(n=2048):
+    f = n / 4096.0
+    return Workload(
+        name=f"ooc_lod_iso_{n}", dims=(n, n, n), dtype=np.uint8, vmax=255, n_blobs=1024,
+        sigma=(32 * f, 160 * f), peak=(96, 255), noise_amp=25.5, noise_octaves=4,
+        noise_cell=256.0 * f, int_noise=False, brick_core=128, overlap=1, width=1920,
+        height=1080, srm=1.0, lighting=True, light_model=0, tf_kind="", seed=4096, n_poses=300,
+        extra={"iso": 128.0, "cache_bytes": int(24e9 * f ** 3)})
+
+
+def flythrough_poses(n: int, seed: int):
+    """Seeded fly-through around and into the unit volume: the eye follows a
+    smooth closed curve (distance 0.55..1.45 from the centre, elevation within
+    +-35 degrees) and looks at a point that wanders near the centre; the
+    camera moves a little each frame, as in an interactive session."""
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 2 * math.pi, 6)
+    out = []
+    for i in range(n):
+        t = i / n
+        az = 2 * math.pi * t + ph[0]
+        r = 1.0 + 0.45 * math.sin(2 * math.pi * 2 * t + ph[1])
+        el = math.radians(35) * math.sin(2 * math.pi * 3 * t + ph[2])
+        eye = (r * math.cos(el) * math.sin(az), r * math.sin(el), r * math.cos(el) * math.cos(az))
+        at = (0.15 * math.sin(2 * math.pi * 5 * t + ph[3]),
+              0.15 * math.sin(2 * math.pi * 4 * t + ph[4]),
+              0.15 * math.sin(2 * math.pi * 3 * t + ph[5]))
+        out.append((eye, at, (0.0, 1.0, 0.0)))
+    return out
+
+
 # Batching: 64 views of mixed sizes over four volumes made with the plain_small
 # blob rules (values scaled to the type's range), a 256x256 float 2D TF of
 # three Gaussian lobes over (value, |gradient| * gradient scale), sample-rate
