@@ -422,7 +422,8 @@ def run_learned(args, torch, r, w, poses, plain_fps):
         "value": fps, "unit": "frames/s", "vs_plain": fps / plain_fps,
         "ms_per_frame": 1000.0 * wall / K,
         "gpu_ms": {k: float(np.median([getattr(x, k) for x in infos]))
-                   for k in ("ms_reduced", "ms_network", "ms_probe", "ms_fallback")},
+                   for k in ("ms_reduced", "ms_network", "ms_probe", "ms_judge", "ms_fallback",
+                             "ms_frame")},
         "reduced": [int(infos[0].reduced_width), int(infos[0].reduced_height)],
         "judge_threshold_db": thr, "fallback_rate": fell / K,
         "psnr_db": {"learned_mean": float(np.mean(ps_l)), "learned_min": float(np.min(ps_l)),

@@ -479,9 +479,13 @@ typedef struct tvk_learned_info {
   int fell_back;                 /* 1: the plain full-quality frame was rendered */
   float ms_reduced;              /* reduced frame + bilinear upscale */
   float ms_network;              /* input preparation + U-Net */
-  float ms_probe;                /* probe rays + their comparison */
+  float ms_probe;                /* the probe rays (on their own stream, overlapping
+                                    the reduced frame and the network) */
   float ms_fallback;             /* the plain frame when falling back, else ~0 */
   uint32_t reduced_width, reduced_height;
+  float ms_judge;                /* after the network: waiting for the probes and
+                                    comparing them */
+  float ms_frame;                /* the whole frame on the renderer's stream */
 } tvk_learned_info;
 
 /* Number of FP32 parameters: per layer in the order above, the weights

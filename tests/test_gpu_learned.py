@@ -43,10 +43,22 @@ def test_gpu_learned_equals_training_forward(cuda_ok):
     lr = LearnedRenderer(net.params())
     info = lr.Paint(r, threshold_db=0.0)
     assert info.fell_back == 0 and (info.reduced_width, info.reduced_height) == (100, 60)
-    img = r.ReadBackPixels()
+    img = r.ReadBackPixels().copy()
     np.testing.assert_array_equal(img, ref)
-    # the judge's probe PSNR is that of the probe pixels
-    assert math.isfinite(info.probe_psnr_db) or info.probe_psnr_db == 1000.0
+    # the judge's probe PSNR is that of the probe pixels: one full-quality ray
+    # per 8x8 block at offset (3, 1) on a network's first frame, marched on the
+    # probe stream while the reduced frame and the network ran
+    r.Paint()
+    plain = r.ReadBackPixels()
+    d = (img[1::8, 3::8].astype(np.float64) - plain[1::8, 3::8]) ** 2
+    want = 10.0 * math.log10(1.0 / d.mean())
+    assert abs(info.probe_psnr_db - want) < 1e-3, (info.probe_psnr_db, want)
+    assert info.ms_probe > 0 and info.ms_frame >= info.ms_reduced + info.ms_network
+    # the next frame moves the probes (offset (0, 4))
+    info2 = lr.Paint(r, threshold_db=0.0)
+    img2 = r.ReadBackPixels().copy()
+    d2 = (img2[4::8, 0::8].astype(np.float64) - plain[4::8, 0::8]) ** 2
+    assert abs(info2.probe_psnr_db - 10.0 * math.log10(1.0 / d2.mean())) < 1e-3
 
 
 def test_gpu_learned_fallback_is_the_plain_frame(cuda_ok):

@@ -76,7 +76,8 @@ class CnnWgrad(C.Structure):
 class LearnedInfo(C.Structure):
     _fields_ = [("probe_psnr_db", C.c_float), ("fell_back", C.c_int), ("ms_reduced", C.c_float),
                 ("ms_network", C.c_float), ("ms_probe", C.c_float), ("ms_fallback", C.c_float),
-                ("reduced_width", C.c_uint32), ("reduced_height", C.c_uint32)]
+                ("reduced_width", C.c_uint32), ("reduced_height", C.c_uint32),
+                ("ms_judge", C.c_float), ("ms_frame", C.c_float)]
 
 
 class PoolInfo(C.Structure):

@@ -647,6 +647,12 @@ struct tvk_learned {
   tvk::PinnedBuf h_sum;
   cudaEvent_t ev[5] = {};
   uint32_t frame = 0;
+  // the probe rays run on their own stream with their own brick list
+  cudaStream_t probe_stream = nullptr;
+  tvk::DevBuf p_bricks, p_counters;
+  tvk::PinnedBuf p_hbricks;
+  cudaEvent_t ev_pstaged = nullptr, ev_planned = nullptr, ev_pstart = nullptr,
+              ev_pdone = nullptr;
 };
 
 // LOD-octree brick cache for the GridLeaper (GLVolumePool + GLHashTable).
@@ -809,10 +815,26 @@ struct PlannedFrame {
   uint64_t launches0;
 };
 
-// Everything of a paint up to the kernel launch: TF table and empty-cell bits,
-// the brick list of the LOD (uploaded on the renderer's stream), the counters
-// cleared, and the frame's parameters.
-PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
+// Where a planned frame's brick list and counters go: the renderer's own
+// buffers and stream, or a second set so that two frames of one renderer can
+// be in flight on two streams (the learned frame's probe rays).
+struct Stage {
+  DevBuf* d_bricks;
+  PinnedBuf* h_bricks;
+  cudaEvent_t ev_staged;   // the last brick-list upload from h_bricks
+  DevBuf* d_counters;
+  cudaStream_t stream;     // brick-list upload and counter clear
+};
+
+Stage renderer_stage(tvk_renderer* R) {
+  return Stage{&R->d_bricks, &R->h_bricks, R->ev_staged, &R->d_counters, R->stream};
+}
+
+// Everything of a paint up to the kernel launch: TF table and empty-cell bits
+// (on the renderer's stream), the brick list of the LOD (uploaded on the
+// stage's stream), the counters cleared, and the frame's parameters.
+PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage = nullptr) {
+  const Stage st = stage ? *stage : renderer_stage(R);
   const tvk_volume* V = R->vol;
   if (!V) fail(TVK_ERR_STATE, "no volume attached (tvk_renderer_set_volume)");
   const bool iso_mode = R->mode == TVK_RM_ISOSURFACE;
@@ -877,9 +899,9 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
 
   // per-brick records of the visible bricks of LOD L (BuildSubFrameBrickList)
   const uint64_t first = V->lod_first[L], nbl = V->lod_first[L + 1] - first;
-  TVK_CUDA(cudaEventSynchronize(R->ev_staged));
-  R->h_bricks.ensure(nbl * sizeof(DevBrick));
-  DevBrick* hb = R->h_bricks.as<DevBrick>();
+  TVK_CUDA(cudaEventSynchronize(st.ev_staged));
+  st.h_bricks->ensure(nbl * sizeof(DevBrick));
+  DevBrick* hb = st.h_bricks->as<DevBrick>();
   uint32_t nvis = 0;
   // Front-to-back order valid for every ray: bricks sorted by L1 distance of
   // their grid coordinates from the eye's brick cell.  Along a ray that
@@ -949,17 +971,17 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
     b.cells = V->cell_dims[k];
     b.empty_off = R->cell_skip ? R->slots[R->slot].empty_word_off[k] : 0;
   }
-  R->d_bricks.ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
+  st.d_bricks->ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
   if (nvis)
-    TVK_CUDA(cudaMemcpyAsync(R->d_bricks.p, hb, nvis * sizeof(DevBrick), cudaMemcpyHostToDevice,
-                             R->stream));
-  TVK_CUDA(cudaEventRecord(R->ev_staged, R->stream));
+    TVK_CUDA(cudaMemcpyAsync(st.d_bricks->p, hb, nvis * sizeof(DevBrick), cudaMemcpyHostToDevice,
+                             st.stream));
+  TVK_CUDA(cudaEventRecord(st.ev_staged, st.stream));
 
   RenderParams P;
   std::memset(&P, 0, sizeof(P));
   P.pool = device_bricks(V);
   P.bytes = V->bytes;
-  P.bricks = R->d_bricks.as<DevBrick>();
+  P.bricks = st.d_bricks->as<DevBrick>();
   P.n_bricks = nvis;
   P.tf = R->slots[R->slot].d_tf.as<float4>();
   P.tf_col_nonzero = R->slots[R->slot].d_tfcol.as<uint8_t>();
@@ -1011,13 +1033,13 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf) {
   const size_t npix = size_t(R->width) * R->height;
   R->d_img.ensure(npix * sizeof(float4));
   R->d_spp.ensure(size_t(rw) * rh * sizeof(uint32_t));
-  R->d_counters.ensure(4 * sizeof(unsigned long long));
+  st.d_counters->ensure(4 * sizeof(unsigned long long));
   const bool upscale = rw != R->width || rh != R->height;
   if (upscale) R->d_lowimg.ensure(size_t(rw) * rh * sizeof(float4));
   P.out = upscale ? R->d_lowimg.as<float4>() : R->d_img.as<float4>();
   P.spp = R->d_spp.as<uint32_t>();
-  P.counters = R->d_counters.as<unsigned long long>();
-  TVK_CUDA(cudaMemsetAsync(R->d_counters.p, 0, 4 * sizeof(unsigned long long), R->stream));
+  P.counters = st.d_counters->as<unsigned long long>();
+  TVK_CUDA(cudaMemsetAsync(st.d_counters->p, 0, 4 * sizeof(unsigned long long), st.stream));
   R->stats.bricks_visible = nvis;
   R->stats.bricks_total = nbl;
   return PlannedFrame{P, rw, rh, upscale, launches0};
@@ -1446,11 +1468,17 @@ void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int o
 void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_learned_info* info) {
   if (R->device != N->device) fail(TVK_ERR_INVALID_ARG, "renderer and network on other devices");
   TVK_CUDA(cudaSetDevice(R->device));
+  cudaStream_t s = R->stream;
+  TVK_CUDA(cudaEventRecord(N->ev[0], s));
+  // Both frames are planned before either launches: the full-rate plan (the
+  // probe rays and the fallback) first, so that the viewport-sized buffers
+  // are allocated before the reduced frame's parameters point into them.
+  const Stage probe_stage{&N->p_bricks, &N->p_hbricks, N->ev_pstaged, &N->p_counters,
+                          N->probe_stream};
+  const PlannedFrame full = plan_frame(R, Subframe{0, false, false}, &probe_stage);
   const float saved_dec = R->screen_dec, saved_sdec = R->sample_dec;
   R->screen_dec = 2.0f;
   R->sample_dec = 2.0f;
-  cudaStream_t s = R->stream;
-  TVK_CUDA(cudaEventRecord(N->ev[0], s));
   PlannedFrame low;
   try {
     low = plan_frame(R, Subframe{0, true, true});
@@ -1459,10 +1487,35 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
     R->sample_dec = saved_sdec;
     throw;
   }
-  launch_raycast(low.P, s, &R->launches);
-  launch_upscale_of(R, low, s, &R->launches);
   R->screen_dec = saved_dec;
   R->sample_dec = saved_sdec;
+  // TF tables and empty-cell bits of both plans were written on the
+  // renderer's stream: the probe stream starts after them
+  TVK_CUDA(cudaEventRecord(N->ev_planned, s));
+  TVK_CUDA(cudaStreamWaitEvent(N->probe_stream, N->ev_planned, 0));
+
+  // probes: one pixel of every 8x8 block at full quality, offset per frame,
+  // marched on the probe stream while the reduced frame and the network run
+  const int stride = 8, ox = int((N->frame * 5u + 3u) % 8u), oy = int((N->frame * 3u + 1u) % 8u);
+  ++N->frame;
+  RenderParams P = full.P;
+  P.stride = stride;
+  P.off_x = ox;
+  P.off_y = oy;
+  P.out_w = (R->width - ox + stride - 1) / stride;
+  P.out_h = (R->height - oy + stride - 1) / stride;
+  P.spp = nullptr;
+  N->d_sum.ensure(4 * P.out_w * P.out_h * sizeof(float) + 256);
+  float4* probe = reinterpret_cast<float4*>(static_cast<uint8_t*>(N->d_sum.p) + 256);
+  float* sum = N->d_sum.as<float>();
+  P.out = probe;
+  TVK_CUDA(cudaEventRecord(N->ev_pstart, N->probe_stream));
+  launch_raycast(P, N->probe_stream, &R->launches);
+  TVK_CUDA(cudaEventRecord(N->ev_pdone, N->probe_stream));
+
+  // the reduced frame, upscaled into the viewport image, and the network
+  launch_raycast(low.P, s, &R->launches);
+  launch_upscale_of(R, low, s, &R->launches);
   TVK_CUDA(cudaEventRecord(N->ev[1], s));
   const float* lowimg = low.upscale ? R->d_lowimg.as<float>() : R->d_img.as<float>();
   N->hp = int((low.rh + 7) / 8 * 8);
@@ -1475,22 +1528,10 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   run_unet(N, x16.p, R->d_img.as<float>(), int(R->height), int(R->width), s);
   R->launches += kUNetLayers + 8;
   TVK_CUDA(cudaEventRecord(N->ev[2], s));
-  // probes: one pixel of every 8x8 block at full quality, offset per frame
-  const PlannedFrame full = plan_frame(R, Subframe{0, false, false});
-  const int stride = 8, ox = int((N->frame * 5u + 3u) % 8u), oy = int((N->frame * 3u + 1u) % 8u);
-  ++N->frame;
-  RenderParams P = full.P;
-  P.stride = stride;
-  P.off_x = ox;
-  P.off_y = oy;
-  P.out_w = (R->width - ox + stride - 1) / stride;
-  P.out_h = (R->height - oy + stride - 1) / stride;
-  N->d_sum.ensure(4 * P.out_w * P.out_h * sizeof(float) + 256);
-  float4* probe = reinterpret_cast<float4*>(static_cast<uint8_t*>(N->d_sum.p) + 256);
-  float* sum = N->d_sum.as<float>();
-  P.out = probe;
+
+  // the judge: probe error against the network's frame
+  TVK_CUDA(cudaStreamWaitEvent(s, N->ev_pdone, 0));
   TVK_CUDA(cudaMemsetAsync(sum, 0, sizeof(float), s));
-  launch_raycast(P, s, &R->launches);
   cnn_probe_mse(R->d_img.as<float>(), int(R->width), reinterpret_cast<const float*>(probe),
                 int(P.out_w), int(P.out_h), stride, ox, oy, sum, s);
   N->h_sum.ensure(sizeof(float));
@@ -1500,18 +1541,27 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   const double mse = double(*N->h_sum.as<float>()) / (4.0 * P.out_w * P.out_h);
   const float psnr = mse > 0 ? float(10.0 * std::log10(1.0 / mse)) : 1000.0f;
   const bool fall_back = psnr < threshold_db;
-  if (fall_back) launch_raycast(full.P, s, &R->launches);
+  if (fall_back) {
+    TVK_CUDA(cudaMemsetAsync(N->p_counters.p, 0, 4 * sizeof(unsigned long long), s));
+    launch_raycast(full.P, s, &R->launches);
+    // the frame's stats are the plain frame's
+    TVK_CUDA(cudaMemcpyAsync(R->d_counters.p, N->p_counters.p, 4 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToDevice, s));
+  }
   TVK_CUDA(cudaEventRecord(N->ev[4], s));
-  finish_frame(R, full);
+  finish_frame(R, fall_back ? full : low);
   TVK_CUDA(cudaEventSynchronize(N->ev[4]));
-  float t[4];
+  float t[4], tp = 0.0f;
   for (int i = 0; i < 4; ++i) TVK_CUDA(cudaEventElapsedTime(&t[i], N->ev[i], N->ev[i + 1]));
+  TVK_CUDA(cudaEventElapsedTime(&tp, N->ev_pstart, N->ev_pdone));
   info->probe_psnr_db = psnr;
   info->fell_back = fall_back ? 1 : 0;
   info->ms_reduced = t[0];
   info->ms_network = t[1];
-  info->ms_probe = t[2];
+  info->ms_probe = tp;
   info->ms_fallback = t[3];
+  info->ms_judge = t[2];
+  TVK_CUDA(cudaEventElapsedTime(&info->ms_frame, N->ev[0], N->ev[4]));
   info->reduced_width = low.rw;
   info->reduced_height = low.rh;
 }
@@ -2490,6 +2540,12 @@ tvk_status tvk_learned_create(const float* host_params, size_t n, tvk_learned** 
     tvk::cnn_to_bf16(d_w32.as<float>(), nw, N->d_w.p, nullptr);
     TVK_CUDA(cudaDeviceSynchronize());
     for (cudaEvent_t& e : N->ev) TVK_CUDA(cudaEventCreate(&e));
+    TVK_CUDA(cudaStreamCreateWithFlags(&N->probe_stream, cudaStreamNonBlocking));
+    TVK_CUDA(cudaEventCreateWithFlags(&N->ev_pstaged, cudaEventDisableTiming));
+    TVK_CUDA(cudaEventRecord(N->ev_pstaged, N->probe_stream));
+    TVK_CUDA(cudaEventCreateWithFlags(&N->ev_planned, cudaEventDisableTiming));
+    TVK_CUDA(cudaEventCreate(&N->ev_pstart));
+    TVK_CUDA(cudaEventCreate(&N->ev_pdone));
     *out = N.release();
   });
 }
@@ -2497,8 +2553,12 @@ tvk_status tvk_learned_create(const float* host_params, size_t n, tvk_learned** 
 tvk_status tvk_learned_destroy(tvk_learned* n) {
   return guarded([&] {
     if (!n) return;
+    if (n->probe_stream) cudaStreamSynchronize(n->probe_stream);
     for (cudaEvent_t e : n->ev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {n->ev_pstaged, n->ev_planned, n->ev_pstart, n->ev_pdone})
+      if (e) cudaEventDestroy(e);
+    if (n->probe_stream) cudaStreamDestroy(n->probe_stream);
     delete n;
   });
 }
