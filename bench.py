@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--learned-quality-poses", type=int, default=24)
     p.add_argument("--learned-ssim-poses", type=int, default=6)
     p.add_argument("--frame-ert", type=float, default=1.0)
+    p.add_argument("--only", choices=["learned", "batching", "ooc"], default=None,
+                   help="run one secondary measurement alone (profiling cases)")
     p.add_argument("--no-ooc", action="store_true",
                    help="skip the out-of-core GridLeaper fly-through")
     p.add_argument("--ooc-dim", type=int, default=2048,
@@ -419,7 +421,7 @@ def run_learned(args, torch, r, w, poses, plain_fps):
             ss_b.append(ssim_rgb(bilinear, plain))
     fell = sum(x.fell_back for x in infos)
     return {
-        "value": fps, "unit": "frames/s", "vs_plain": fps / plain_fps,
+        "value": fps, "unit": "frames/s", "vs_plain": fps / plain_fps if plain_fps else None,
         "ms_per_frame": 1000.0 * wall / K,
         "gpu_ms": {k: float(np.median([getattr(x, k) for x in infos]))
                    for k in ("ms_reduced", "ms_network", "ms_probe", "ms_judge", "ms_fallback",
@@ -544,6 +546,28 @@ def run_ooc(args, torch):
                 "GPU time outside the traversal holds the hash read-back, the host's page "
                 "table update and the pinned-host copies",
     }
+
+
+def run_only(args):
+    """--only LEG: one secondary measurement alone (the small cases the ncu
+    captures run); prints {"only": LEG, LEG: {...}} instead of the contract line."""
+    import torch
+    from tuvok_gb300 import Renderer
+    from tuvok_gb300.workloads import WORKLOADS
+    torch.cuda.set_device(0)
+    if args.only == "ooc":
+        out = run_ooc(args, torch)
+    elif args.only == "batching":
+        out = run_batching(args, torch, args.batch_steps)
+    else:
+        w = WORKLOADS[args.workload]
+        vol, raw, _ = make_volume(w, torch)
+        del raw
+        torch.cuda.empty_cache()
+        r = Renderer()
+        configure(r, w, vol, args.frame_ert)
+        out = run_learned(args, torch, r, w, w.poses(), None)
+    print(json.dumps({"only": args.only, args.only: out}), flush=True)
 
 
 def run_ours(args):
@@ -712,6 +736,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        run_only(args)
     else:
         run_ours(args)
 

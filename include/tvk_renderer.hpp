@@ -9,6 +9,7 @@
 
 #include <array>
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -41,6 +42,33 @@ class BrickedVolume {
                             clamp_to_edge ? 1 : 0, &v_));
   }
   ~BrickedVolume() { tvk_volume_destroy(v_); }
+  // tvk_volume_create_ex: TVK_VOLUME_* flags (device input, median LODs, LOD 0 only)
+  static std::unique_ptr<BrickedVolume> Create(const void* voxels, tvk_dtype dtype,
+                                               std::array<uint64_t, 3> dims,
+                                               std::array<uint32_t, 3> brick_size,
+                                               uint32_t overlap, uint32_t flags) {
+    std::unique_ptr<BrickedVolume> v(new BrickedVolume());
+    check(tvk_volume_create_ex(voxels, dtype, dims.data(), brick_size.data(), overlap, flags,
+                               &v->v_));
+    return v;
+  }
+  // DynamicBrickingDS over this volume (tvk_volume_rebrick)
+  static std::unique_ptr<BrickedVolume> Rebrick(const BrickedVolume& src,
+                                                std::array<uint32_t, 3> brick_size,
+                                                tvk_minmax_mode mode) {
+    std::unique_ptr<BrickedVolume> v(new BrickedVolume());
+    check(tvk_volume_rebrick(src.v_, brick_size.data(), mode, &v->v_));
+    return v;
+  }
+  std::vector<uint64_t> GetHistogram(size_t bins) const {
+    std::vector<uint64_t> h(bins);
+    uint64_t used = 0;
+    check(tvk_volume_get_histogram(v_, h.data(), bins, &used));
+    h.resize(used);
+    return h;
+  }
+  // Out-of-core: frees the device bricks (a host-sourced VolumePool keeps rendering)
+  void ReleaseBricks() { check(tvk_volume_release_bricks(v_)); }
   BrickedVolume(const BrickedVolume&) = delete;
   BrickedVolume& operator=(const BrickedVolume&) = delete;
 
@@ -94,6 +122,7 @@ class BrickedVolume {
   }
 
  private:
+  BrickedVolume() = default;
   tvk_volume* v_ = nullptr;
 };
 
@@ -154,11 +183,123 @@ class Renderer {
     check(tvk_get_stats(r_, &s));
     return s;
   }
+  // m_iCurrentLOD, decreaseScreenResNow / decreaseSamplingRateNow
+  void SetLOD(uint32_t lod) { check(tvk_set_lod(r_, lod)); }
+  void SetReducedQuality(bool screen, bool sampling) {
+    check(tvk_set_reduced_quality(r_, screen ? 1 : 0, sampling ? 1 : 0));
+  }
+  // AbstrRenderer::SetPerfMeasures / SetLODLimits / ComputeMinLODForCurrentView
+  void SetPerfMeasures(uint32_t min_framerate, bool low_res_intermediate,
+                       float screen_res_dec_factor = 2.0f, float sample_dec_factor = 2.0f) {
+    check(tvk_set_perf_measures(r_, min_framerate, low_res_intermediate ? 1 : 0,
+                                screen_res_dec_factor, sample_dec_factor));
+  }
+  void SetLODLimits(uint32_t coarsest_skip, uint32_t finest) {
+    check(tvk_set_lod_limits(r_, coarsest_skip, finest));
+  }
+  uint32_t ComputeMinLODForCurrentView() {
+    uint32_t l = 0;
+    check(tvk_compute_min_lod(r_, &l));
+    return l;
+  }
+  // One subframe of the progressive frame (PlanFrame)
+  tvk_subframe_info PaintProgressive(bool new_frame) {
+    tvk_subframe_info i;
+    check(tvk_paint_progressive(r_, new_frame ? 1 : 0, &i));
+    return i;
+  }
   tvk_renderer* handle() const { return r_; }
 
  private:
   tvk_renderer* r_ = nullptr;
   uint32_t w_ = 0, h_ = 0;
+};
+
+// Several renderers' frames in one persistent launch replayed from a CUDA
+// graph (the reference paints render regions one after another,
+// GLRenderer.cpp:622-660).
+class BatchPainter {
+ public:
+  BatchPainter() { check(tvk_batch_create(&b_)); }
+  ~BatchPainter() { tvk_batch_destroy(b_); }
+  BatchPainter(const BatchPainter&) = delete;
+  BatchPainter& operator=(const BatchPainter&) = delete;
+  void SetAutotune(bool on, uint32_t ctas_per_sm = 0) {
+    check(tvk_batch_set_autotune(b_, on ? 1 : 0, ctas_per_sm));
+  }
+  void Paint(const std::vector<Renderer*>& rs) {
+    std::vector<tvk_renderer*> h;
+    for (Renderer* r : rs) h.push_back(r->handle());
+    check(tvk_paint_batch(b_, h.data(), uint32_t(h.size())));
+  }
+  tvk_batch_info Info() {
+    tvk_batch_info i;
+    check(tvk_batch_get_info(b_, &i));
+    return i;
+  }
+
+ private:
+  tvk_batch* b_ = nullptr;
+};
+
+// The learned reconstruction: reduced frame + tensor-core U-Net + probe judge
+// with fallback to the plain frame.
+class LearnedReconstruction {
+ public:
+  explicit LearnedReconstruction(const std::vector<float>& params) {
+    check(tvk_learned_create(params.data(), params.size(), &n_));
+  }
+  ~LearnedReconstruction() { tvk_learned_destroy(n_); }
+  LearnedReconstruction(const LearnedReconstruction&) = delete;
+  LearnedReconstruction& operator=(const LearnedReconstruction&) = delete;
+  static size_t ParamCount() {
+    size_t n = 0;
+    check(tvk_learned_param_count(&n));
+    return n;
+  }
+  tvk_learned_info Paint(Renderer& r, float threshold_db) {
+    tvk_learned_info i;
+    check(tvk_paint_learned(r.handle(), n_, threshold_db, &i));
+    return i;
+  }
+
+ private:
+  tvk_learned* n_ = nullptr;
+};
+
+// GLVolumePool + GLHashTable + GLGridLeaper::Render3DRegion: the LOD brick
+// cache of a volume and the GridLeaper frame over it.
+class VolumePool {
+ public:
+  VolumePool(const BrickedVolume& v, uint64_t budget_bytes, bool host_source) {
+    check(tvk_pool_create(v.handle(), budget_bytes, host_source ? 1 : 0, &p_));
+  }
+  ~VolumePool() { tvk_pool_destroy(p_); }
+  VolumePool(const VolumePool&) = delete;
+  VolumePool& operator=(const VolumePool&) = delete;
+  tvk_pool_info Info() const {
+    tvk_pool_info i;
+    check(tvk_pool_get_info(p_, &i));
+    return i;
+  }
+  std::vector<uint32_t> PageTable() const {
+    std::vector<uint32_t> t(Info().bricks);
+    check(tvk_pool_get_page_table(p_, t.data(), t.size()));
+    return t;
+  }
+  void Reset() { check(tvk_pool_reset(p_)); }  // PH_Reset
+  void SetRequestTable(uint32_t size, uint32_t rehash) {
+    check(tvk_pool_set_request_table(p_, size, rehash));
+  }
+  // Render3DRegion's subframes until converged or max_passes
+  tvk_leaper_info Paint(Renderer& r, uint32_t max_passes) {
+    tvk_leaper_info i;
+    check(tvk_leaper_paint(r.handle(), p_, max_passes, &i));
+    return i;
+  }
+
+ private:
+  tvk_pool* p_ = nullptr;
 };
 
 }  // namespace tvk

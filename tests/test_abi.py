@@ -62,3 +62,17 @@ def test_check_raises_with_message():
     with pytest.raises(N.TvkError) as e:
         N.check(N.lib().tvk_paint(None))
     assert "TVK_ERR_INVALID_ARG" in str(e.value)
+
+
+def test_cpp_shim_compiles():
+    """include/tvk_renderer.hpp (the C++ mirror of AbstrRenderer, BrickedDataset,
+    GLVolumePool) and the C++ host example compile against include/tvk.h."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = HEADER.parent.parent
+    subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                    f"-I{root / 'include'}", str(root / "tests" / "cpp" / "shim_demo.cpp")],
+                   check=True)
