@@ -140,8 +140,10 @@ max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ off
                     unsigned long long* out_bits) {
   // Every inner voxel: Q = dx^2 + dy^2 + dz^2 of the central differences.  Distinct
   // integer Q values give |grad| values whose relative gap (>= 1/(2Q)) far exceeds
-  // double rounding, so the maximum |grad| sits at a voxel of maximum Q; only those
-  // lanes evaluate the reference's double expression and publish its bits.
+  // double rounding, so the maximum |grad| sits at a voxel of maximum Q.  Each
+  // thread keeps its largest Q and evaluates the reference's double expression
+  // only when a voxel reaches it with another (|dx|, |dy|, |dz|); the largest
+  // of the threads' values is the maximum.  A warp walks x-rows (coalesced).
   const uint32_t b = blockIdx.x;
   const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
   const T* p = pool + offsets[b];
@@ -150,43 +152,42 @@ max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ off
   const uint32_t z1 = min(bs[2] - ov, z0 + z_chunk);
   const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
   const double nf2 = double(T(~T(0))) * 2.0;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   long long best_q = -1;
   double best_f = 0.0;
-  const uint32_t n = (z1 > z0) ? (z1 - z0) * ix * iy : 0;
-  // iterate in whole warps so the warp-wide reduction below is uniform
-  const uint32_t n_pad = (n + 31u) & ~31u;
-  for (uint32_t t = threadIdx.x; t < n_pad; t += blockDim.x) {
-    long long q = -1;
-    int dx = 0, dy = 0, dz = 0;
-    if (t < n) {
-      const uint32_t k = z0 + t / (ix * iy);
-      const uint32_t r = t % (ix * iy);
-      const uint32_t j = ov + r / ix;
-      const uint32_t i = ov + r % ix;
-      const uint64_t c = uint64_t(i) + uint64_t(j) * sx + uint64_t(k) * sxy;
-      dx = int(p[c - 1]) - int(p[c + 1]);
-      dy = int(p[c - sx]) - int(p[c + sx]);
-      dz = int(p[c - sxy]) - int(p[c + sxy]);
-      q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
-    }
-    long long wq = q;
-    for (int o = 16; o > 0; o >>= 1) wq = max(wq, (long long)__shfl_xor_sync(0xffffffffu, wq, o));
-    if (q >= 0 && q == wq) {
+  int ba = -1, bb = -1, bc = -1;  // |dx|, |dy|, |dz| of the best value
+  const uint32_t rows = (z1 > z0) ? (z1 - z0) * iy : 0;
+  for (uint32_t row = warp; row < rows; row += kThreads / 32) {
+    const uint32_t k = z0 + row / iy, j = ov + row % iy;
+    const T* line = p + uint64_t(j) * sx + uint64_t(k) * sxy;
+    for (uint32_t i = ov + lane; i < ov + ix; i += 32) {
+      const T* c = line + i;
+      const int dx = int(c[-1]) - int(c[1]);
+      const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
+      const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
+      const long long q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
+      if (q < best_q) continue;
+      const int ax = abs(dx), ay = abs(dy), az = abs(dz);
+      if (q == best_q && ax == ba && ay == bb && az == bc) continue;
       const double gx = __ddiv_rn(double(dx), nf2);
       const double gy = __ddiv_rn(double(dy), nf2);
       const double gz = __ddiv_rn(double(dz), nf2);
-      const double s = __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz));
-      const double f = __dsqrt_rn(s);
-      if (q > best_q || (q == best_q && f > best_f)) {
+      const double sq = __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz));
+      const double f = __dsqrt_rn(sq);
+      if (q > best_q || f > best_f) {
         best_q = q;
         best_f = f;
+        ba = ax; bb = ay; bc = az;
       }
     }
   }
-  if (best_q >= 0) {
-    // positive doubles order like their bit patterns
-    atomicMax(out_bits, (unsigned long long)__double_as_longlong(best_f));
+  // positive doubles order like their bit patterns
+  unsigned long long bits = best_q >= 0 ? (unsigned long long)__double_as_longlong(best_f) : 0ull;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = ob > bits ? ob : bits;
   }
+  if (lane == 0 && bits) atomicMax(out_bits, bits);
 }
 
 template <class T>

@@ -149,11 +149,67 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
   }
 }
 
+// The ghost shell of an n0 x n1 x n2 brick (voxels within ov of a face),
+// enumerated without visiting the inner voxels: the ghost planes along z,
+// then the ghost rows of the other planes, then the ghost x ends of the
+// remaining rows.
+struct Shell {
+  uint32_t n[3], ov, gk, gj, gi, mk, mj;
+  uint32_t a, b, total;  // segment ends
+};
+
+__device__ __forceinline__ Shell make_shell(const uint32_t n[3], uint32_t ov) {
+  Shell s;
+  s.n[0] = n[0]; s.n[1] = n[1]; s.n[2] = n[2];
+  s.ov = ov;
+  s.gk = min(n[2], 2 * ov);
+  s.gj = min(n[1], 2 * ov);
+  s.gi = min(n[0], 2 * ov);
+  s.mk = n[2] - s.gk;
+  s.mj = n[1] - s.gj;
+  s.a = s.gk * n[1] * n[0];
+  s.b = s.a + s.mk * s.gj * n[0];
+  s.total = s.b + s.mk * s.mj * s.gi;
+  return s;
+}
+
+// p-th ghost index of an axis of extent n with g = min(n, 2 ov) ghost layers
+__device__ __forceinline__ uint32_t ghost_index(uint32_t p, uint32_t n, uint32_t g, uint32_t ov) {
+  return p < min(ov, n) ? p : n - g + p;
+}
+
+__device__ __forceinline__ void shell_voxel(const Shell& s, uint32_t t, uint32_t& i, uint32_t& j,
+                                            uint32_t& k) {
+  if (t < s.a) {
+    const uint32_t plane = s.n[1] * s.n[0];
+    k = ghost_index(t / plane, s.n[2], s.gk, s.ov);
+    const uint32_t r = t % plane;
+    j = r / s.n[0];
+    i = r % s.n[0];
+  } else if (t < s.b) {
+    t -= s.a;
+    const uint32_t slab = s.gj * s.n[0];
+    k = s.ov + t / slab;
+    const uint32_t r = t % slab;
+    j = ghost_index(r / s.n[0], s.n[1], s.gj, s.ov);
+    i = r % s.n[0];
+  } else {
+    t -= s.b;
+    const uint32_t slab = s.mj * s.gi;
+    k = s.ov + t / slab;
+    const uint32_t r = t % slab;
+    j = s.ov + r / s.gi;
+    i = ghost_index(r % s.gi, s.n[0], s.gi, s.ov);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 fill_overlap_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, LodGeom g,
                     const uint32_t* __restrict__ wave, uint32_t B0, uint32_t B1, uint32_t B2,
                     uint32_t ov, int clamp) {
+  // Brick wave[blockIdx.x]; its ghost shell is split over gridDim.y CTAs
+  // (one CTA when clamping: the clamp steps are ordered by __syncthreads).
   const uint32_t B[3] = {B0, B1, B2};
   const uint32_t b = wave[blockIdx.x];
   const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
@@ -167,9 +223,11 @@ fill_overlap_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, 
     return pool + offsets[g.first + (c[0] + dx) + (c[1] + dy) * g.cnt[0] +
                           (c[2] + dz) * g.cnt[0] * g.cnt[1]];
   };
-  const uint32_t total = n[0] * n[1] * n[2];
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-    const uint32_t i = t % n[0], j = (t / n[0]) % n[1], k = t / (n[0] * n[1]);
+  const Shell sh = make_shell(n, ov);
+  const uint32_t t0 = blockIdx.y * blockDim.x + threadIdx.x, dt = gridDim.y * blockDim.x;
+  for (uint32_t t = t0; t < sh.total; t += dt) {
+    uint32_t i, j, k;
+    shell_voxel(sh, t, i, j, k);
     const bool xh = i >= n[0] - ov, yh = j >= n[1] - ov, zh = k >= n[2] - ov;
     const bool xl = i < ov, yl = j < ov, zl = k < ov;
     // the last copy of FillOverlap whose target region holds (i, j, k)
@@ -199,7 +257,8 @@ fill_overlap_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, 
       else if (d[a] < 0) s[a] = s[a] + ns[a] - 2 * ov;
     }
     const T* src = brick_ptr(dx, dy, dz);
-    dst[t] = src[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * ns[1]) * ns[0]];
+    dst[i + (uint64_t(j) + uint64_t(k) * n[1]) * n[0]] =
+        src[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * ns[1]) * ns[0]];
   }
   if (!clamp) return;
   // ClampToEdge (ExtendedOctreeConverter.cpp:376-462) on sides without a
@@ -207,15 +266,17 @@ fill_overlap_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, 
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     __syncthreads();
-    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-      const uint32_t v[3] = {t % n[0], (t / n[0]) % n[1], t / (n[0] * n[1])};
+    for (uint32_t t = t0; t < sh.total; t += dt) {
+      uint32_t v[3];
+      shell_voxel(sh, t, v[0], v[1], v[2]);
       uint32_t from = v[a];
       if (!has_lo[a] && v[a] < ov) from = ov;
       else if (!has_hi[a] && v[a] >= n[a] - ov) from = n[a] - 1 - ov;
       else continue;
       uint32_t s[3] = {v[0], v[1], v[2]};
       s[a] = from;
-      dst[t] = dst[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * n[1]) * n[0]];
+      dst[v[0] + (uint64_t(v[1]) + uint64_t(v[2]) * n[1]) * n[0]] =
+          dst[s[0] + (uint64_t(s[1]) + uint64_t(s[2]) * n[1]) * n[0]];
     }
   }
 }
@@ -225,16 +286,42 @@ __global__ void __launch_bounds__(kThreads)
 brick_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
                     const uint64_t* __restrict__ voxels, uint64_t first, uint32_t* out_min,
                     uint32_t* out_max) {
-  // ComputeBrickStats<T> (.inc:408-444): every voxel of the brick
+  // ComputeBrickStats<T> (.inc:408-444): every voxel of the brick, the brick
+  // split over gridDim.y CTAs; 16-byte loads (bricks start 256-byte aligned)
   const uint64_t b = first + blockIdx.x;
   const T* p = pool + offsets[b];
   const uint64_t nv = voxels[b];
+  constexpr uint32_t kPer = 16 / sizeof(T);
+  const uint64_t nvec = nv / kPer;
+  const uint64_t per_cta = (nvec + gridDim.y - 1) / gridDim.y;
+  const uint64_t v0 = blockIdx.y * per_cta, v1 = min(nvec, v0 + per_cta);
+  const uint4* pv = reinterpret_cast<const uint4*>(p);
   uint32_t lo = 0xffffffffu, hi = 0;
-  for (uint64_t t = threadIdx.x; t < nv; t += blockDim.x) {
-    const uint32_t v = p[t];
-    lo = min(lo, v);
-    hi = max(hi, v);
+  for (uint64_t t = v0 + threadIdx.x; t < v1; t += blockDim.x) {
+    const uint4 w = pv[t];
+    const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (sizeof(T) == 1) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const uint32_t v = (words[q] >> (8 * e)) & 0xffu;
+          lo = min(lo, v);
+          hi = max(hi, v);
+        }
+      } else {
+        const uint32_t a = words[q] & 0xffffu, c = words[q] >> 16;
+        lo = min(lo, min(a, c));
+        hi = max(hi, max(a, c));
+      }
+    }
   }
+  if (blockIdx.y == gridDim.y - 1)  // the tail after the last full 16 bytes
+    for (uint64_t t = nvec * kPer + threadIdx.x; t < nv; t += blockDim.x) {
+      const uint32_t v = p[t];
+      lo = min(lo, v);
+      hi = max(hi, v);
+    }
   for (int o = 16; o > 0; o >>= 1) {
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
@@ -244,8 +331,8 @@ brick_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ off
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int w = 1; w < kThreads / 32; ++w) { lo = min(lo, slo[w]); hi = max(hi, shi[w]); }
-    out_min[blockIdx.x] = lo;
-    out_max[blockIdx.x] = hi;
+    atomicMin(&out_min[blockIdx.x], lo);
+    atomicMax(&out_max[blockIdx.x], hi);
   }
 }
 
@@ -300,12 +387,16 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
     for (uint32_t w = 0; w < nw; ++w) {
       const uint32_t cnt = starts[w + 1] - starts[w];
       if (!cnt) continue;
+      // the shell of a full brick split over enough CTAs to fill the GPU
+      // (one CTA per brick when clamping orders its steps with barriers)
+      const uint32_t split = clamp ? 1u : std::max(1u, std::min(32u, 1216u / cnt));
+      const dim3 fgrid(cnt, split);
       if (bytes == 1)
-        fill_overlap_kernel<uint8_t><<<cnt, kThreads, 0, s>>>(
+        fill_overlap_kernel<uint8_t><<<fgrid, kThreads, 0, s>>>(
             static_cast<uint8_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
             clamp ? 1 : 0);
       else
-        fill_overlap_kernel<uint16_t><<<cnt, kThreads, 0, s>>>(
+        fill_overlap_kernel<uint16_t><<<fgrid, kThreads, 0, s>>>(
             static_cast<uint16_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
             clamp ? 1 : 0);
       TVK_CUDA(cudaGetLastError());
@@ -313,12 +404,15 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
     }
     // the wave list is pageable host memory reused by the next level
     TVK_CUDA(cudaStreamSynchronize(s));
+    TVK_CUDA(cudaMemsetAsync(d_min + hi.first, 0xff, nb * sizeof(uint32_t), s));
+    TVK_CUDA(cudaMemsetAsync(d_max + hi.first, 0, nb * sizeof(uint32_t), s));
+    const dim3 mgrid(uint32_t(nb), std::max(1u, std::min(64u, 2432u / uint32_t(nb))));
     if (bytes == 1)
-      brick_minmax_kernel<uint8_t><<<uint32_t(nb), kThreads, 0, s>>>(
+      brick_minmax_kernel<uint8_t><<<mgrid, kThreads, 0, s>>>(
           static_cast<const uint8_t*>(pool), d_offsets, d_voxels, hi.first, d_min + hi.first,
           d_max + hi.first);
     else
-      brick_minmax_kernel<uint16_t><<<uint32_t(nb), kThreads, 0, s>>>(
+      brick_minmax_kernel<uint16_t><<<mgrid, kThreads, 0, s>>>(
           static_cast<const uint16_t*>(pool), d_offsets, d_voxels, hi.first, d_min + hi.first,
           d_max + hi.first);
     TVK_CUDA(cudaGetLastError());
