@@ -76,3 +76,4 @@ def test_cpp_shim_compiles():
     subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
                     f"-I{root / 'include'}", str(root / "tests" / "cpp" / "shim_demo.cpp")],
                    check=True)
+

@@ -299,6 +299,8 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   for (uint64_t k = 0; k < nb_all; ++k) {
     const uint32_t cx = cells_per_axis(V->sizes[3 * k]), cy = cells_per_axis(V->sizes[3 * k + 1]),
                    cz = cells_per_axis(V->sizes[3 * k + 2]);
+    if (cx > 1023 || cy > 1023 || cz > 1023)
+      fail(TVK_ERR_UNSUPPORTED, "bricks above 2046 voxels per axis (macro-cell table limit)");
     V->cell_dims[k] = cx | (cy << 10) | (cz << 20);
     V->cell_counts[k] = cx * cy * cz;
     V->cell_offsets[k] = V->total_cells;
@@ -557,6 +559,7 @@ struct tvk_renderer {
     bool valid = false;
     uint64_t used = 0;
     tvk::DevBuf d_tf, d_tfcol, d_tfpfx, d_empty, d_empty_meta;
+    tvk::DevBuf d_dist, d_dist_tmp, d_cell_dims;  // macro-cell distances (+ scratch)
     std::vector<uint64_t> empty_word_off;
     bool empty_valid = false;
     bool empty_iso = false;
@@ -779,6 +782,32 @@ void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale,
   p.iso_norm = iso_norm;
   p.bits = S.d_empty.as<uint32_t>();
   launch_empty_cells(p, max_words, R->stream, &R->launches);
+  // Chebyshev distances of the cells to the nearest non-empty cell
+  const uint64_t ncells = std::max<uint64_t>(1, V->total_cells);
+  S.d_dist.ensure(ncells);
+  S.d_dist_tmp.ensure(2 * ncells);
+  S.d_cell_dims.ensure(nb * sizeof(uint32_t));
+  TVK_CUDA(cudaMemcpyAsync(S.d_cell_dims.p, V->cell_dims.data(), nb * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, R->stream));
+  uint32_t max_lines[3] = {0, 0, 0};
+  for (uint64_t k = 0; k < nb; ++k) {
+    const uint32_t d = V->cell_dims[k];
+    const uint32_t cx = d & 1023u, cy = (d >> 10) & 1023u, cz = d >> 20;
+    max_lines[0] = std::max(max_lines[0], cy * cz);
+    max_lines[1] = std::max(max_lines[1], cx * cz);
+    max_lines[2] = std::max(max_lines[2], cx * cy);
+  }
+  CellDistParams cd;
+  cd.bits = S.d_empty.as<uint32_t>();
+  cd.word_offsets = S.d_empty_meta.as<uint64_t>();
+  cd.cell_offsets = static_cast<const uint64_t*>(V->d_cell_meta);
+  cd.cell_dims = S.d_cell_dims.as<uint32_t>();
+  cd.in = nullptr;
+  cd.out = nullptr;
+  cd.n_bricks = nb;
+  uint8_t* tmp = S.d_dist_tmp.as<uint8_t>();
+  launch_cell_dist(cd, max_lines, tmp, tmp + ncells, S.d_dist.as<uint8_t>(), R->stream,
+                   &R->launches);
   // the word offsets above were copied from pageable memory; keep them alive
   TVK_CUDA(cudaStreamSynchronize(R->stream));
   S.empty_valid = true;
@@ -969,7 +998,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     b.step = stp;
     b.off = V->offsets[k];
     b.cells = V->cell_dims[k];
-    b.empty_off = R->cell_skip ? R->slots[R->slot].empty_word_off[k] : 0;
+    b.cell_off = V->cell_offsets[k];
   }
   st.d_bricks->ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
   if (nvis)
@@ -990,7 +1019,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   P.mode = R->mode;
   P.lighting = R->lighting ? 1 : 0;
   P.light_model = R->light_model;
-  P.empty_bits = R->cell_skip ? R->slots[R->slot].d_empty.as<uint32_t>() : nullptr;
+  P.cell_dist = R->cell_skip ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
   P.trans_scale = trans_scale;
   const float mg = float(V->max_grad);
   P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;  // GLRenderer.cpp:1840-1841
