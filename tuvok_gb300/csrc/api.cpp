@@ -1752,6 +1752,8 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
     pool_upload_page_table(pool);
   }
 
+  // empty-cell distances of every brick for this TF / isovalue
+  if (R->cell_skip) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
   const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
   LeaperParams L;
   std::memset(&L, 0, sizeof(L));
@@ -1862,6 +1864,8 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
   pool->d_resume_col.ensure(npix * sizeof(float4));
   L.resume_pos = pool->d_resume_pos.as<float4>();
   L.resume_col = pool->d_resume_col.as<float4>();
+  L.cell_dist = R->cell_skip ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
+  L.cell_off = static_cast<const uint64_t*>(V->d_cell_meta);
 
   std::memset(info, 0, sizeof(*info));
   const uint64_t l0n = L.ser_xyz;

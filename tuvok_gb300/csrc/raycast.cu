@@ -1097,8 +1097,51 @@ __global__ void __launch_bounds__(128, 4) leaper_kernel(const LeaperParams L) {
           const float u2 = fminf(fmaxf(l2 - 0.5f, 0.0f), vol.fn2 - 1.0f);
           return vol.sample_u(u0, u1, u2) * im;
         };
+        // macro cells of the brick (as in the brick-by-brick march): steps in
+        // an empty cube add nothing and cannot hit, so they are leapt over,
+        // the position keeping the chain of additions
+        const uint8_t* __restrict__ dist = L.cell_dist ? L.cell_dist + L.cell_off[gid] : nullptr;
+        const int ncx = int(cells_per_axis(uint32_t(vol.n0))),
+                  ncy = int(cells_per_axis(uint32_t(vol.n1))),
+                  ncz = int(cells_per_axis(uint32_t(vol.n2)));
+        const float idu0 = 1.0f / fabsf(sv[0]), idu1 = 1.0f / fabsf(sv[1]),
+                    idu2 = 1.0f / fabsf(sv[2]);
         bool done = false;
         for (int i = 0; i < steps; ++i) {
+          if (dist) {
+            const float uu0 = pc[0] - 0.5f, uu1 = pc[1] - 0.5f, uu2 = pc[2] - 0.5f;
+            const float u0 = fminf(fmaxf(uu0, 0.0f), vol.fn0 - 1.0f);
+            const float u1 = fminf(fmaxf(uu1, 0.0f), vol.fn1 - 1.0f);
+            const float u2 = fminf(fmaxf(uu2, 0.0f), vol.fn2 - 1.0f);
+            const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
+                      cz = int(u2) >> kCellShift;
+            const int dd = __ldg(&dist[(cz * ncy + cy) * ncx + cx]);
+            if (dd != 0) {
+              int k = 0;
+              if (uu0 == u0 && uu1 == u1 && uu2 == u2) {
+                const int r = dd - 1;
+                const float lo0 = float(max(cx - r, 0) << kCellShift),
+                            lo1 = float(max(cy - r, 0) << kCellShift),
+                            lo2 = float(max(cz - r, 0) << kCellShift);
+                const float hi0 = float(min(cx + r + 1, ncx) << kCellShift),
+                            hi1 = float(min(cy + r + 1, ncy) << kCellShift),
+                            hi2 = float(min(cz + r + 1, ncz) << kCellShift);
+                const float d0 = sv[0] > 0.0f ? hi0 - uu0 : uu0 - lo0;
+                const float d1 = sv[1] > 0.0f ? hi1 - uu1 : uu1 - lo1;
+                const float d2 = sv[2] > 0.0f ? hi2 - uu2 : uu2 - lo2;
+                const float m = fminf(fminf((d0 - 0.015625f) * idu0, (d1 - 0.015625f) * idu1),
+                                      (d2 - 0.015625f) * idu2);
+                k = m > 0.0f ? int(fminf(m, float(steps - 1 - i))) : 0;
+              }
+              samples += uint32_t(k + 1);
+              for (int j = 0; j <= k; ++j) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
+              }
+              i += k;
+              continue;
+            }
+          }
           ++samples;
           const float v = sample(pc[0], pc[1], pc[2]);
           if (kIso) {

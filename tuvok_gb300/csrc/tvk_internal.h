@@ -260,6 +260,8 @@ struct LeaperParams {
   float4* resume_pos;          // xyz = normalised position, w = depth (1000: done)
   float4* resume_col;
   uint32_t first_pass;
+  const uint8_t* cell_dist;    // macro-cell distances of every brick (null: none)
+  const uint64_t* cell_off;    // per brick, first macro cell
 };
 void launch_leaper(const LeaperParams& p, cudaStream_t s, uint64_t* launches);
 
