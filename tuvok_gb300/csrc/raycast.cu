@@ -918,12 +918,19 @@ __device__ __forceinline__ void lighting_eye(const LeaperParams& L, const float 
 }
 
 // GLHashTable.cpp:150-185: key = Serialize(brick), linear probing with
-// atomicCompSwap from 0, at most `rehash` probes
+// atomicCompSwap from 0, at most `rehash` probes.  An entry only ever goes
+// from 0 to a key, so two shortcuts leave the table as the plain probing
+// would: one lane reports for all lanes of its warp with the same key, and a
+// probe that already reads a non-zero entry needs no atomic.
 __device__ __forceinline__ void report_missing(const LeaperParams& L, const uint32_t bc[3],
                                                uint32_t lod) {
   const uint32_t key = 1u + bc[0] + bc[1] * L.ser_x + bc[2] * L.ser_xy + lod * L.ser_xyz;
+  const uint32_t peers = __match_any_sync(__activemask(), key);
+  if (uint32_t(__ffs(peers) - 1) != (threadIdx.x & 31u)) return;
   for (uint32_t r = 0; r < L.rehash; ++r) {
-    const uint32_t old = atomicCAS(&L.hash[(key + r) % L.hash_size], 0u, key);
+    uint32_t* slot = &L.hash[(key + r) % L.hash_size];
+    uint32_t old = *reinterpret_cast<volatile uint32_t*>(slot);
+    if (old == 0u) old = atomicCAS(slot, 0u, key);
     if (old == 0u || old == key) return;
   }
 }
@@ -936,8 +943,12 @@ __device__ __forceinline__ uint32_t brick_info(const LeaperParams& L, const floa
   return __ldg(&L.page[L.lod_offset[lod] + bc[0] + bc[1] * L.lod_lx[lod] + bc[2] * L.lod_lxy[lod]]);
 }
 
+#ifndef TVK_LEAPER_MIN_BLOCKS
+#define TVK_LEAPER_MIN_BLOCKS 4
+#endif
+
 template <class T, bool kIso>
-__global__ void __launch_bounds__(128, 4) leaper_kernel(const LeaperParams L) {
+__global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(const LeaperParams L) {
   const RenderParams& P = L.R;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
