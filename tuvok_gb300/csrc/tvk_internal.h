@@ -160,7 +160,7 @@ void launch_empty_cells(const EmptyCellParams& p, uint32_t max_words_per_brick, 
 // may leap over that whole cube.  Three separable passes (x from the empty
 // bits, then y, then z) over all bricks.
 #ifndef TVK_CELL_DIST_CAP
-#define TVK_CELL_DIST_CAP 31  // 15, 31 and 63 measure the same with 2^3 cells
+#define TVK_CELL_DIST_CAP 15  // 15, 31 and 63 measure the same with 2^3 cells; 15 halves the passes
 #endif
 constexpr int kCellDistCap = TVK_CELL_DIST_CAP;
 struct CellDistParams {
