@@ -290,14 +290,23 @@ def run_reference(args):
 
 
 def run_batching(args, torch, steps):
-    """64 mixed views over four volumes: one tvk_paint_batch per step (one
-    persistent launch replayed from a CUDA graph) against the same 64 frames
-    painted with tvk_paint one renderer after another."""
-    from tuvok_gb300 import Batch, Renderer
-    from tuvok_gb300.workloads import BATCH_VOLUMES, batch_views, orbit_poses, tf2d_lobes
+    """64 mixed views over four volumes (the batching configuration), and 256
+    small views over the same volumes: one tvk_paint_batch per step (persistent
+    launches replayed from a CUDA graph) against the same frames painted with
+    tvk_paint one renderer after another."""
+    from tuvok_gb300.workloads import BATCH_VOLUMES, SMALL_BATCH_SIZES, batch_views
     vols = [make_volume(w, torch) for w in BATCH_VOLUMES]
+    out = run_batch_views(torch, steps, vols, batch_views())
+    small = run_batch_views(torch, steps, vols, batch_views(256, 901, SMALL_BATCH_SIZES))
+    small["workload"] = "batch_small_256"
+    out["small_views"] = small
+    return out
+
+
+def run_batch_views(torch, steps, vols, views):
+    from tuvok_gb300 import Batch, Renderer
+    from tuvok_gb300.workloads import BATCH_VOLUMES, orbit_poses, tf2d_lobes
     tf = tf2d_lobes()
-    views = batch_views()
     rs = []
     for vi, (w, h), srm, lit in views:
         r = Renderer()
@@ -341,19 +350,31 @@ def run_batching(args, torch, steps):
             r.Paint()
     torch.cuda.synchronize()
     single_s = time.perf_counter() - t0
+    # the reference's order: one view after the other, each finished before the next
+    t0 = time.perf_counter()
+    for i in range(steps):
+        set_cams(3 + i)
+        for r in rs:
+            r.Paint()
+            r.GetStats()  # waits for the renderer's stream
+    seq_s = time.perf_counter() - t0
     pixels = sum(w * h for _, (w, h), _, _ in views)
-    return {"workload": "batch_mixed_64", "views": len(rs), "steps": steps,
+    return {"workload": f"batch_mixed_{len(rs)}", "views": len(rs), "steps": steps,
             "volumes": [f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} "
                         f"{'u8' if w.dtype == np.uint8 else 'u16'}" for w in BATCH_VOLUMES],
             "pixels_per_step": pixels,
             "batched_views_per_s": len(rs) * steps / batched_s,
             "independent_views_per_s": len(rs) * steps / single_s,
             "speedup": single_s / batched_s,
+            "sequential_views_per_s": len(rs) * steps / seq_s,
+            "speedup_vs_sequential": seq_s / batched_s,
             "gpu_ms_per_batch": float(np.median(gpu_ms)),
             "ctas_per_sm": info.ctas_per_sm, "graph_reused": info.graph_reused,
-            "gpu_launches_per_batch": 1,
-            "note": "wall-clock over the steps incl. host planning of 64 brick lists; "
-                    "independent = tvk_paint per renderer, each on its own stream"}
+            "gpu_launches_per_batch": int(info.launches),
+            "note": f"wall-clock over the steps incl. host planning of {len(rs)} brick lists; "
+                    "independent = tvk_paint per renderer, each on its own stream (they "
+                    "overlap on the GPU); sequential = each paint finished before the next, "
+                    "the reference's region-after-region order"}
 
 
 def ssim_rgb(a, b):

@@ -211,11 +211,17 @@ def tf2d_lobes(w=256, h=256, seed=77):
     return t
 
 
-def batch_views(n=64, seed=900):
+# Many small views (thumbnails, multi-view displays): where one launch for all
+# of them matters most.
+SMALL_BATCH_SIZES = [(96, 96), (128, 128), (160, 120), (192, 192), (256, 256)]
+
+
+def batch_views(n=64, seed=900, sizes=None):
     """(volume index, (width, height), srm, lit) per view, seeded."""
+    sizes = sizes or BATCH_SIZES
     rng = np.random.default_rng(seed)
     return [(int(rng.integers(0, len(BATCH_VOLUMES))),
-             BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))],
+             sizes[int(rng.integers(0, len(sizes)))],
              float(rng.choice([0.5, 1.0, 2.0])), bool(rng.integers(0, 2))) for _ in range(n)]
 
 
