@@ -61,9 +61,9 @@ def parse():
                    help="run one secondary measurement alone (profiling cases)")
     p.add_argument("--no-ooc", action="store_true",
                    help="skip the out-of-core GridLeaper fly-through")
-    p.add_argument("--ooc-dim", type=int, default=2048,
-                   help="edge of the out-of-core volume (the 4096^3 case needs ~150 GB of HBM "
-                        "while bricking and ~82 GB of pinned host memory)")
+    p.add_argument("--ooc-dim", type=int, default=0,
+                   help="edge of the out-of-core volume; 0: 4096 (the configuration's size) "
+                        "when the GPU has 220 GB and the host 120 GB free, else 2048")
     p.add_argument("--ooc-frames", type=int, default=0, help="timed frames (0: all 300)")
     p.add_argument("--ooc-warmup", type=int, default=3)
     p.add_argument("--ooc-passes", type=int, default=64)
@@ -480,6 +480,21 @@ def h2d_peak_gbs(torch, nbytes=1 << 30):
     return best
 
 
+def ooc_default_dim(torch):
+    """4096 (the out-of-core configuration: 82 GB of bricks in pinned host
+    memory, ~190 GB of HBM at the peak of bricking) when this box has room,
+    else 2048."""
+    free_dev, _ = torch.cuda.mem_get_info()
+    avail_host = 0
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                avail_host = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 4096 if free_dev > 220e9 and avail_host > 120e9 else 2048
+
+
 def run_ooc(args, torch):
     """Out-of-core LOD rendering with the GridLeaper: the bricks live in pinned
     host memory (the device pool is released), a bounded brick cache is paged
@@ -488,7 +503,8 @@ def run_ooc(args, torch):
     missing or --ooc-passes."""
     from tuvok_gb300 import Pool, Renderer
     from tuvok_gb300.workloads import flythrough_poses, ooc_lod
-    w = ooc_lod(args.ooc_dim)
+    dim = args.ooc_dim or ooc_default_dim(torch)
+    w = ooc_lod(dim)
     peak_h2d = h2d_peak_gbs(torch)
     vol, raw, brick_s = make_volume(w, torch)
     del raw
@@ -678,23 +694,32 @@ def run_ours(args):
     h2d = int(np.mean(vis)) * dev_brick_bytes
     d2h = w.width * w.height * 16 + 32
 
+    def guarded_leg(fn, *a):
+        # a secondary measurement that fails is reported, not allowed to take
+        # the headline line with it
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"}
+
     learned = None
     if not args.no_learned:
-        learned = run_learned(args, torch, r, w, poses, value)
+        learned = guarded_leg(run_learned, args, torch, r, w, poses, value)
 
+    import gc
     batching = None
     if not args.no_batching:
-        del r
+        r = None
+        gc.collect()
         torch.cuda.empty_cache()
-        batching = run_batching(args, torch, args.batch_steps)
+        batching = guarded_leg(run_batching, args, torch, args.batch_steps)
 
     ooc = None
     if not args.no_ooc:
-        import gc
         r = vol = None
         gc.collect()
         torch.cuda.empty_cache()
-        ooc = run_ooc(args, torch)
+        ooc = guarded_leg(run_ooc, args, torch)
 
     cpu = None
     if raw_host is not None:
