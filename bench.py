@@ -422,7 +422,7 @@ def run_learned(args, torch, r, w, poses, plain_fps):
     fps = K / wall
     # quality on a subset of the timed poses (untimed)
     n_q = min(K, args.learned_quality_poses)
-    ps_l, ps_b, ss_l, ss_b, probe = [], [], [], [], []
+    ps_l, ps_b, ss_l, ss_b, probe, ps_res, ps_rate = [], [], [], [], [], [], []
     for i in range(n_q):
         eye, at, up = poses[(args.warmup + i) % len(poses)]
         r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
@@ -432,11 +432,19 @@ def run_learned(args, torch, r, w, poses, plain_fps):
         r.SetReducedQuality(True, True)
         r.Paint()
         bilinear = r.ReadBackPixels().copy()
+        r.SetReducedQuality(True, False)
+        r.Paint()
+        half_res = r.ReadBackPixels().copy()
+        r.SetReducedQuality(False, True)
+        r.Paint()
+        half_rate = r.ReadBackPixels().copy()
         r.SetReducedQuality(False, False)
         r.Paint()
         plain = r.ReadBackPixels().copy()
         ps_l.append(psnr(float(np.mean((learned - plain) ** 2))))
         ps_b.append(psnr(float(np.mean((bilinear - plain) ** 2))))
+        ps_res.append(psnr(float(np.mean((half_res - plain) ** 2))))
+        ps_rate.append(psnr(float(np.mean((half_rate - plain) ** 2))))
         if i < args.learned_ssim_poses:
             ss_l.append(ssim_rgb(learned, plain))
             ss_b.append(ssim_rgb(bilinear, plain))
@@ -451,6 +459,8 @@ def run_learned(args, torch, r, w, poses, plain_fps):
         "judge_threshold_db": thr, "fallback_rate": fell / K,
         "psnr_db": {"learned_mean": float(np.mean(ps_l)), "learned_min": float(np.min(ps_l)),
                     "bilinear_mean": float(np.mean(ps_b)), "probe_mean": float(np.mean(probe)),
+                    "half_resolution_only_mean": float(np.mean(ps_res)),
+                    "half_sample_rate_only_mean": float(np.mean(ps_rate)),
                     "poses": n_q},
         "ssim": {"learned_mean": float(np.mean(ss_l)), "bilinear_mean": float(np.mean(ss_b)),
                  "poses": len(ss_l)},
