@@ -48,6 +48,12 @@ CASES = [  # n, h, w, c1, c2, cout, slope
     (1, 12, 20, 64, 64, 64, 0.1),
     (1, 8, 24, 48, 32, 32, 0.1),
     (2, 10, 10, 32, 0, 16, -1.0),
+    # large images take the 16x16-patch kernel: all taps' weights staged at
+    # once, and (128 input channels) one tap at a time
+    (1, 290, 300, 32, 0, 32, 0.1),
+    (1, 300, 288, 64, 64, 64, 0.1),
+    (2, 200, 248, 48, 32, 32, 0.1),
+    (1, 300, 300, 32, 16, 32, 0.1),   # data gradient split over the concatenation
 ]
 
 
@@ -85,7 +91,9 @@ def test_gpu_conv3x3_forward_and_gradients(cuda_ok, case):
     g = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
     check(lib().tvk_cnn_act_grad(p(dy_t), p(y) if slope >= 0 else None, slope, p(g), dy.size,
                                  stream()))
-    gref = K.bf16(np.where(host(y) > 0, dy, dy * slope) if slope >= 0 else dy)
+    # the GPU multiplies the FP32 gradient by the FP32 slope, then rounds to BF16
+    dy32 = dy.astype(np.float32)
+    gref = K.bf16(np.where(host(y) > 0, dy32, dy32 * np.float32(slope)) if slope >= 0 else dy32)
     np.testing.assert_array_equal(host(g), gref)
     dx1 = torch.zeros((n, h, w, c1), dtype=torch.float32, device="cuda")
     dx2 = torch.zeros((n, h, w, c2), dtype=torch.float32, device="cuda") if c2 else None

@@ -152,6 +152,128 @@ __global__ void __launch_bounds__(kThreads) conv3x3_kernel(const ConvArgs a) {
   }
 }
 
+// The same convolution for large images: a CTA of 8 warps computes a 16x16
+// pixel patch (each warp two pixel rows of 16 = two m16 tiles that share every
+// B fragment), and with kAllTaps the weights of all 9 taps are staged once, so
+// the tap loop runs without barriers.
+constexpr int kWideThreads = 256;
+constexpr int kWideTile = 16, kWideHalo = kWideTile + 2;
+
+template <int kNT, bool kAllTaps>
+__global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int cin = a.c1 + a.c2;
+  const int cpad = cin + 8;
+  const int cw = cin / 2;  // 32-bit words per pixel
+  __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem_raw);   // [18 * 18][cpad]
+  __nv_bfloat16* wsm = halo + kWideHalo * kWideHalo * cpad;           // [taps][cout_pad][cpad]
+  const int tiles_x = (a.w + kWideTile - 1) / kWideTile;
+  const int tiles_y = (a.h + kWideTile - 1) / kWideTile;
+  const int t = blockIdx.x;
+  const int img = t / (tiles_x * tiles_y);
+  const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
+  const int y0 = ty * kWideTile - 1, x0 = tx * kWideTile - 1;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, q = lane & 3;
+  constexpr int cout_pad = kNT * 8;
+
+  for (int i = tid; i < kWideHalo * kWideHalo * cw; i += kWideThreads) {
+    const int pix = i / cw, c = (i % cw) * 2;
+    const int yy = y0 + pix / kWideHalo, xx = x0 + pix % kWideHalo;
+    uint32_t v = 0;
+    if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
+      const size_t p = (size_t(img) * a.h + yy) * a.w + xx;
+      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + p * a.c1 + c)
+                   : *reinterpret_cast<const uint32_t*>(a.x2 + p * a.c2 + (c - a.c1));
+    }
+    *reinterpret_cast<uint32_t*>(halo + pix * cpad + c) = v;
+  }
+  auto load_tap = [&](int tap, __nv_bfloat16* dst) {
+    const __nv_bfloat16* wtap = a.wt + size_t(tap) * a.cout * cin;
+    for (int i = tid; i < cout_pad * cw; i += kWideThreads) {
+      const int co = i / cw, c = (i % cw) * 2;
+      const uint32_t v = co < a.cout ? *reinterpret_cast<const uint32_t*>(wtap + co * cin + c) : 0u;
+      *reinterpret_cast<uint32_t*>(dst + co * cpad + c) = v;
+    }
+  };
+  if (kAllTaps) {
+    for (int tap = 0; tap < 9; ++tap) load_tap(tap, wsm + tap * cout_pad * cpad);
+    __syncthreads();
+  }
+
+  float acc[2][kNT][4];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int j = 0; j < kNT; ++j) acc[m][j][0] = acc[m][j][1] = acc[m][j][2] = acc[m][j][3] = 0.0f;
+  const int pr0 = 2 * warp, pr1 = 2 * warp + 1;
+  for (int tap = 0; tap < 9; ++tap) {
+    const __nv_bfloat16* wt_s = wsm;
+    if (kAllTaps) {
+      wt_s = wsm + tap * cout_pad * cpad;
+    } else {
+      __syncthreads();  // halo written / previous tap's weights no longer read
+      load_tap(tap, wsm);
+      __syncthreads();
+    }
+    const int ky = tap / 3, kx = tap % 3;
+    for (int k0 = 0; k0 < cin; k0 += 16) {
+      uint32_t af[2][4];
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const __nv_bfloat16* r0 = halo + ((pr0 + ky) * kWideHalo + m * 8 + g + kx) * cpad;
+        const __nv_bfloat16* r1 = halo + ((pr1 + ky) * kWideHalo + m * 8 + g + kx) * cpad;
+        af[m][0] = *reinterpret_cast<const uint32_t*>(r0 + k0 + 2 * q);
+        af[m][1] = *reinterpret_cast<const uint32_t*>(r1 + k0 + 2 * q);
+        af[m][2] = *reinterpret_cast<const uint32_t*>(r0 + k0 + 8 + 2 * q);
+        af[m][3] = *reinterpret_cast<const uint32_t*>(r1 + k0 + 8 + 2 * q);
+      }
+#pragma unroll
+      for (int j = 0; j < kNT; ++j) {
+        const __nv_bfloat16* wr = wt_s + (j * 8 + g) * cpad + k0 + 2 * q;
+        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(wr);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(wr + 8);
+        mma_bf16(acc[0][j], af[0], b0, b1);
+        mma_bf16(acc[1][j], af[1], b0, b1);
+      }
+    }
+  }
+
+  // epilogue: m-tile m covers pixel columns 8m .. 8m+7; rows g (pr0), g + 8 (pr1)
+#pragma unroll
+  for (int m = 0; m < 2; ++m) {
+    const int ox = tx * kWideTile + m * 8 + g;
+#pragma unroll
+    for (int j = 0; j < kNT; ++j) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int oy = ty * kWideTile + (half ? pr1 : pr0);
+        if (oy >= a.h || ox >= a.w) continue;
+        const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int co = j * 8 + 2 * q + e;
+          if (co >= a.cout) continue;
+          float v = acc[m][j][half * 2 + e];
+          if (a.bias) v += a.bias[co];
+          if (a.slope >= 0.0f && v < 0.0f) v *= a.slope;
+          if (a.y_bf16) a.y_bf16[p * a.cout + co] = __float2bfloat16_rn(v);
+          if (co < a.split) {
+            if (a.y_f32) {
+              float* o = a.y_f32 + p * a.split + co;
+              *o = a.accumulate ? *o + v : v;
+            }
+          } else if (a.y2_f32) {
+            const int c2n = a.cout - a.split;
+            float* o = a.y2_f32 + p * c2n + (co - a.split);
+            *o = a.accumulate ? *o + v : v;
+          }
+        }
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------- weight gradient
 
 struct WgradArgs {
@@ -466,6 +588,40 @@ void cnn_conv3x3(const CnnConv& c, cudaStream_t s) {
   a.accumulate = c.accumulate;
   const int cin = c.c1 + c.c2;
   const int nt = (c.cout + 7) / 8;
+  // large images: 16x16 patches (all taps' weights staged when they fit in
+  // 64 KB with the halo), while there are at least two waves of them
+  const unsigned wide_blocks =
+      unsigned(c.n) * ((c.w + kWideTile - 1) / kWideTile) * ((c.h + kWideTile - 1) / kWideTile);
+  if (wide_blocks >= 2 * 152 && nt <= 8) {
+    const size_t pitch = size_t(cin + 8) * sizeof(__nv_bfloat16);
+    const size_t halo = size_t(kWideHalo) * kWideHalo * pitch;
+    const size_t all = halo + size_t(9) * nt * 8 * pitch, one = halo + size_t(nt) * 8 * pitch;
+    const bool all_taps = all <= 64 * 1024;
+    const size_t smem = all_taps ? all : one;
+#define TVK_WIDE_CASE(NT)                                                                   \
+  case NT:                                                                                  \
+    if (all_taps) {                                                                         \
+      TVK_CUDA(cudaFuncSetAttribute(conv3x3_wide_kernel<NT, true>,                          \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))); \
+      conv3x3_wide_kernel<NT, true><<<wide_blocks, kWideThreads, smem, s>>>(a);             \
+    } else {                                                                                \
+      TVK_CUDA(cudaFuncSetAttribute(conv3x3_wide_kernel<NT, false>,                         \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))); \
+      conv3x3_wide_kernel<NT, false><<<wide_blocks, kWideThreads, smem, s>>>(a);            \
+    }                                                                                       \
+    break;
+    switch (nt) {
+      TVK_WIDE_CASE(1)
+      TVK_WIDE_CASE(2)
+      TVK_WIDE_CASE(4)
+      TVK_WIDE_CASE(6)
+      TVK_WIDE_CASE(8)
+      default: fail(TVK_ERR_UNSUPPORTED, "output channels must be 8, 16, 32, ..., 128");
+    }
+#undef TVK_WIDE_CASE
+    TVK_CUDA(cudaGetLastError());
+    return;
+  }
   const size_t smem = (size_t(100) + size_t(nt) * 8) * (cin + 8) * sizeof(__nv_bfloat16);
   const unsigned blocks = unsigned(c.n) * ((c.w + 7) / 8) * ((c.h + 7) / 8);
 #define TVK_CONV_CASE(NT)                                                                 \
