@@ -554,13 +554,14 @@ def run_ooc(args, torch):
         wall = time.perf_counter() - t0
         f = {k: np.array([getattr(x, k) for x in infos], dtype=np.float64)
              for k in ("passes", "paged", "bytes_paged", "ms", "ms_traversal", "converged",
-                       "samples")}
+                       "samples", "ms_host")}
         page_s = max(float(np.sum(f["ms"] - f["ms_traversal"])) / 1000.0, 1e-9)
         return {
             "hash_size": int(pool.GetInfo().hash_size),
             "frames": K, "frames_per_s": K / wall, "ms_per_frame_wall": wall * 1000.0 / K,
             "gpu_ms_per_frame": float(np.mean(f["ms"])),
             "traversal_ms_per_frame": float(np.mean(f["ms_traversal"])),
+            "host_paging_ms_per_frame": float(np.mean(f["ms_host"])),
             "passes_per_frame": float(np.mean(f["passes"])),
             "converged_fraction": float(np.mean(f["converged"])),
             "bricks_paged_per_frame": float(np.mean(f["paged"])),

@@ -543,6 +543,7 @@ typedef struct tvk_leaper_info {
   float ms_traversal;     /* of which in the traversal kernels */
   uint64_t bytes_paged;   /* brick bytes copied into the cache this frame */
   uint64_t samples;       /* samples over all passes */
+  float ms_host;          /* host time choosing slots and issuing the copies */
 } tvk_leaper_info;
 
 tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_source,

@@ -90,7 +90,7 @@ class LeaperInfo(C.Structure):
     _fields_ = [("passes", C.c_uint32), ("paged", C.c_uint32), ("missing_last", C.c_uint32),
                 ("converged", C.c_int), ("resident", C.c_uint32), ("ms", C.c_float),
                 ("ms_traversal", C.c_float), ("bytes_paged", C.c_uint64),
-                ("samples", C.c_uint64)]
+                ("samples", C.c_uint64), ("ms_host", C.c_float)]
 
 
 class Stats(C.Structure):

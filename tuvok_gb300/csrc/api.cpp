@@ -6,6 +6,7 @@
 // and is compiled with -ffp-contract=off, so the values handed to the GPU do not
 // depend on the host compiler or CPU.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1913,21 +1914,25 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
     if (pass + 1 >= std::max(1u, max_passes)) break;
     // PrepareForPaging (:955-959): slots by creation time (never used 0,
     // flagged empty 1, the coarsest brick the maximum); the bricks go into the
-    // first n - 1 of that order (UploadBrick, :768-778)
-    std::vector<uint32_t> order(pool->n_slots);
-    for (uint32_t i = 0; i < pool->n_slots; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-      return pool->slots[a].time < pool->slots[b].time;
-    });
+    // first n - 1 of that order (UploadBrick, :768-778).  Only as many slots
+    // as there are requests are needed, so only those are ordered (ties by
+    // slot index, as a stable sort would leave them).
+    const auto t_host0 = std::chrono::steady_clock::now();
+    std::vector<std::pair<uint64_t, uint32_t>> order(pool->n_slots);
+    for (uint32_t i = 0; i < pool->n_slots; ++i) order[i] = {pool->slots[i].time, i};
+    const size_t need = std::min<size_t>(want.size(), order.size());
+    std::partial_sort(order.begin(), order.begin() + need, order.end());
     uint32_t ins = 0;
     for (uint64_t id : want) {
-      if (ins + 1 >= pool->n_slots) break;  // every slot replaced this round
+      if (ins + 1 >= pool->n_slots || ins >= need) break;  // every slot replaced this round
       if (pool->page[id] >= kBiFlagCount) continue;
-      info->bytes_paged += pool_upload(pool, order[ins++], id, pool->clock++);
+      info->bytes_paged += pool_upload(pool, order[ins++].second, id, pool->clock++);
       ++info->paged;
       ++pool->paged_total;
     }
     pool_upload_page_table(pool);
+    info->ms_host += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() -
+                                                              t_host0).count();
   }
   TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
   TVK_CUDA(cudaEventSynchronize(R->ev_stop));
