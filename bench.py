@@ -371,7 +371,8 @@ def run_batch_views(torch, steps, vols, views):
             "sequential_views_per_s": len(rs) * steps / seq_s,
             "speedup_vs_sequential": seq_s / batched_s,
             "gpu_ms_per_batch": float(np.median(gpu_ms)),
-            "ctas_per_sm": info.ctas_per_sm, "graph_reused": info.graph_reused,
+            "ctas_per_sm": info.ctas_per_sm, "rays_per_thread": info.rays_per_thread,
+            "graph_reused": info.graph_reused,
             "gpu_launches_per_batch": int(info.launches),
             "note": f"wall-clock over the steps incl. host planning of {len(rs)} brick lists; "
                     "independent = tvk_paint per renderer, each on its own stream (they "

@@ -361,7 +361,7 @@ typedef struct tvk_batch tvk_batch;
 
 typedef struct tvk_batch_info {
   uint32_t frames;        /* renderers in the last batch */
-  uint32_t tiles;         /* 16x8-pixel work items of the persistent launch */
+  uint32_t tiles;         /* work items (tiles) of the persistent launches */
   uint32_t ctas;          /* persistent CTAs launched */
   uint32_t ctas_per_sm;   /* chosen by the autotuner or fixed */
   uint32_t launches;      /* persistent launches: one per kernel variant (voxel
@@ -369,6 +369,7 @@ typedef struct tvk_batch_info {
   int graph_reused;       /* 1: the captured CUDA graph was replayed */
   int autotuned;          /* 1: this call timed the candidate grid sizes */
   float ms;               /* GPU time of the batch */
+  uint32_t rays_per_thread; /* 1: 16x8-pixel tiles; 2: 32x8 tiles, two rays per thread */
 } tvk_batch_info;
 
 /* A batch context (its own stream, CUDA graph and autotuning cache) on the
@@ -390,6 +391,9 @@ tvk_status tvk_paint_batch(tvk_batch* b, tvk_renderer* const* renderers, uint32_
 /* autotune = 0 with ctas_per_sm = 0 uses the occupancy maximum; ctas_per_sm
  * > 0 fixes the persistent grid at that many CTAs per SM. */
 tvk_status tvk_batch_set_autotune(tvk_batch* b, int autotune, uint32_t ctas_per_sm);
+/* Rays each thread marches (tile width 16 x rays): 0 lets the autotuner pick
+ * 1 or 2 per launch shape, together with the grid size. */
+tvk_status tvk_batch_set_rays_per_thread(tvk_batch* b, uint32_t rays_per_thread);
 tvk_status tvk_batch_get_info(tvk_batch* b, tvk_batch_info* out);
 
 /* ---- Learned reconstruction primitives (no counterpart in the reference; the

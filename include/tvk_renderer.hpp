@@ -227,6 +227,7 @@ class BatchPainter {
   void SetAutotune(bool on, uint32_t ctas_per_sm = 0) {
     check(tvk_batch_set_autotune(b_, on ? 1 : 0, ctas_per_sm));
   }
+  void SetRaysPerThread(uint32_t rays) { check(tvk_batch_set_rays_per_thread(b_, rays)); }
   void Paint(const std::vector<Renderer*>& rs) {
     std::vector<tvk_renderer*> h;
     for (Renderer* r : rs) h.push_back(r->handle());

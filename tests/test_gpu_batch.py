@@ -128,8 +128,29 @@ def test_gpu_batch_many_views(cuda_ok, volumes):
     b = Batch()
     b.Paint(rs)
     check_equal(rs, ref)
-    assert b.GetInfo().tiles == sum(((w + 15) // 16) * ((h + 7) // 8)
-                                    for (_, _, _, _, _, w, h, _, _, _) in views)
+    info = b.GetInfo()
+    tw = 16 * info.rays_per_thread
+    assert info.rays_per_thread in (1, 2)
+    assert info.tiles == sum(((w + tw - 1) // tw) * ((h + 7) // 8)
+                             for (_, _, _, _, _, w, h, _, _, _) in views)
+
+
+@pytest.mark.parametrize("rays", [1, 2])
+def test_gpu_batch_rays_per_thread(cuda_ok, volumes, rays):
+    """Tiles of 16x8 pixels with one ray per thread, or 32x8 with two: every
+    frame and sample count equals its own tvk_paint either way."""
+    rs = make_renderers(volumes, VIEWS)
+    set_poses(rs, 31)
+    ref = singles(rs)
+    b = Batch()
+    b.SetRaysPerThread(rays)
+    b.Paint(rs)
+    check_equal(rs, ref)
+    info = b.GetInfo()
+    assert info.rays_per_thread == rays
+    tw = 16 * rays
+    assert info.tiles == sum(((r.GetRenderSize()[0] + tw - 1) // tw) *
+                             ((r.GetRenderSize()[1] + 7) // 8) for r in rs)
 
 
 def test_gpu_batch_errors(cuda_ok, volumes):

@@ -56,7 +56,8 @@ class SubframeInfo(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [("frames", C.c_uint32), ("tiles", C.c_uint32), ("ctas", C.c_uint32),
                 ("ctas_per_sm", C.c_uint32), ("launches", C.c_uint32),
-                ("graph_reused", C.c_int), ("autotuned", C.c_int), ("ms", C.c_float)]
+                ("graph_reused", C.c_int), ("autotuned", C.c_int), ("ms", C.c_float),
+                ("rays_per_thread", C.c_uint32)]
 
 
 class CnnConv(C.Structure):
@@ -176,6 +177,7 @@ PROTOTYPES = {
     "tvk_batch_destroy": [_vp],
     "tvk_paint_batch": [_vp, C.POINTER(_vp), C.c_uint32],
     "tvk_batch_set_autotune": [_vp, C.c_int, C.c_uint32],
+    "tvk_batch_set_rays_per_thread": [_vp, C.c_uint32],
     "tvk_batch_get_info": [_vp, C.POINTER(BatchInfo)],
     "tvk_volume_release_bricks": [_vp],
     "tvk_pool_create": [_vp, C.c_uint64, C.c_int, C.POINTER(_vp)],

@@ -610,7 +610,10 @@ struct tvk_batch {
   std::vector<int> variant;                  // kernel variant of each launch
   bool autotune = true;
   uint32_t fixed_ctas_per_sm = 0;           // 0: tuned or the occupancy maximum
-  std::map<std::vector<uint64_t>, uint32_t> tuned;  // launch shapes -> CTAs per SM
+  uint32_t fixed_rays_per_thread = 0;       // 0: tuned (1 or 2), else fixed
+  // launch shapes -> (CTAs per SM, rays per thread)
+  std::map<std::vector<uint64_t>, std::pair<uint32_t, uint32_t>> tuned;
+  uint32_t rpt = 1;                         // rays per thread of the current launches
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> graph_sig;
@@ -1241,6 +1244,21 @@ void paint_progressive(tvk_renderer* R, bool new_frame, tvk_subframe_info* info)
 // The launches of one batch on the batch stream: the work counters cleared,
 // one persistent kernel per launch (frame tables travel as kernel parameters),
 // the reduced frames' upscales.
+// Work items of the launches for `rpt` rays per thread: tiles of (16 rpt) x 8
+// pixels, and the kernel variants that march them.
+void set_batch_tiles(tvk_batch* B, uint32_t rpt) {
+  B->rpt = rpt;
+  for (size_t k = 0; k < B->launch.size(); ++k) {
+    BatchLaunch& L = B->launch[k];
+    const uint32_t tw = 16 * rpt;
+    L.tile_first[0] = 0;
+    for (uint32_t f = 0; f < L.n_frames; ++f)
+      L.tile_first[f + 1] = L.tile_first[f] + ((L.frames[f].out_w + tw - 1) / tw) *
+                                                  ((L.frames[f].out_h + 7) / 8);
+    B->variant[k] = (B->variant[k] & 3) + (rpt == 2 ? 4 : 0);
+  }
+}
+
 void enqueue_batch(tvk_batch* B, tvk_renderer* const* rs, const std::vector<PlannedFrame>& F,
                    uint32_t ctas) {
   const size_t nl = B->launch.size();
@@ -1286,8 +1304,6 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
       }
       BatchLaunch& L = B->launch.back();
       L.frames[L.n_frames] = F[i].P;
-      L.tile_first[L.n_frames + 1] =
-          L.tile_first[L.n_frames] + ((F[i].P.out_w + 15) / 16) * ((F[i].P.out_h + 7) / 8);
       L.n_frames++;
     }
   }
@@ -1310,44 +1326,64 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
   }
   int sms = 0;
   TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device));
-  uint32_t max_per_sm = 1u << 30;
-  for (int v : B->variant)
-    max_per_sm = std::min(max_per_sm, uint32_t(std::max(1, batch_ctas_per_sm_max(v))));
-  uint32_t per_sm = B->fixed_ctas_per_sm ? std::min(B->fixed_ctas_per_sm, max_per_sm) : max_per_sm;
+  auto max_per_sm_for = [&](uint32_t rpt) {
+    uint32_t m = 1u << 30;
+    for (int v : B->variant)
+      m = std::min(m, uint32_t(std::max(1, batch_ctas_per_sm_max((v & 3) + (rpt == 2 ? 4 : 0)))));
+    return m;
+  };
+  uint32_t rpt = B->fixed_rays_per_thread ? B->fixed_rays_per_thread : 1;
+  uint32_t per_sm = B->fixed_ctas_per_sm ? std::min(B->fixed_ctas_per_sm, max_per_sm_for(rpt))
+                                         : max_per_sm_for(rpt);
   bool tuned_now = false;
-  if (!B->fixed_ctas_per_sm) {
+  const bool tune_grid = !B->fixed_ctas_per_sm, tune_rpt = !B->fixed_rays_per_thread;
+  if (tune_grid || tune_rpt) {
     auto it = B->tuned.find(shape);
     if (it != B->tuned.end()) {
-      per_sm = it->second;
+      if (tune_grid) per_sm = it->second.first;
+      if (tune_rpt) rpt = it->second.second;
     } else if (B->autotune) {
-      // time each persistent-grid size on this batch; the frames are
-      // re-rendered identically, only the counters are cleared in between
+      // time each candidate (rays per thread x persistent-grid size) on this
+      // batch; the frames are re-rendered identically, only the counters are
+      // cleared in between
       float best = std::numeric_limits<float>::infinity();
-      std::vector<uint32_t> cands;
-      for (uint32_t c : {max_per_sm, (max_per_sm * 3) / 4, max_per_sm / 2, 2u, 1u})
-        if (c >= 1 && c <= max_per_sm && std::find(cands.begin(), cands.end(), c) == cands.end())
-          cands.push_back(c);
-      for (uint32_t c : cands) {
-        TVK_CUDA(cudaEventRecord(B->ev_start, B->stream));
-        enqueue_batch(B, rs, F, c * uint32_t(sms));
-        TVK_CUDA(cudaEventRecord(B->ev_stop, B->stream));
-        for (uint32_t i = 0; i < n; ++i)
-          TVK_CUDA(cudaMemsetAsync(rs[i]->d_counters.p, 0, 4 * sizeof(unsigned long long),
-                                   B->stream));
-        TVK_CUDA(cudaEventSynchronize(B->ev_stop));
-        float ms = 0;
-        TVK_CUDA(cudaEventElapsedTime(&ms, B->ev_start, B->ev_stop));
-        if (ms < best) {
-          best = ms;
-          per_sm = c;
+      for (uint32_t r : {1u, 2u}) {
+        if (!tune_rpt && r != rpt) continue;
+        const uint32_t mx = max_per_sm_for(r);
+        std::vector<uint32_t> cands;
+        if (!tune_grid) {
+          cands.push_back(std::min(B->fixed_ctas_per_sm, mx));
+        } else {
+          for (uint32_t c : {mx, (mx * 3) / 4, mx / 2, 2u, 1u})
+            if (c >= 1 && c <= mx && std::find(cands.begin(), cands.end(), c) == cands.end())
+              cands.push_back(c);
+        }
+        set_batch_tiles(B, r);
+        for (uint32_t c : cands) {
+          TVK_CUDA(cudaEventRecord(B->ev_start, B->stream));
+          enqueue_batch(B, rs, F, c * uint32_t(sms));
+          TVK_CUDA(cudaEventRecord(B->ev_stop, B->stream));
+          for (uint32_t i = 0; i < n; ++i)
+            TVK_CUDA(cudaMemsetAsync(rs[i]->d_counters.p, 0, 4 * sizeof(unsigned long long),
+                                     B->stream));
+          TVK_CUDA(cudaEventSynchronize(B->ev_stop));
+          float ms = 0;
+          TVK_CUDA(cudaEventElapsedTime(&ms, B->ev_start, B->ev_stop));
+          if (ms < best) {
+            best = ms;
+            per_sm = c;
+            rpt = r;
+          }
         }
       }
-      B->tuned[shape] = per_sm;
+      B->tuned[shape] = {per_sm, rpt};
       tuned_now = true;
     }
   }
+  set_batch_tiles(B, rpt);
   const uint32_t ctas = per_sm * uint32_t(sms);
   shape.push_back(ctas);
+  shape.push_back(rpt);
   // one CUDA graph per launch shape; replays update the kernel nodes' frame
   // tables (new cameras, TFs, brick lists) in place
   const bool reused = B->exec && shape == B->graph_sig;
@@ -1381,7 +1417,7 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
       cudaKernelNodeParams kp{};
       TVK_CUDA(cudaGraphKernelNodeGetParams(node, &kp));
       bool batch = false;
-      for (int v = 0; v < 4; ++v) batch |= kp.func == batch_kernel_function(v);
+      for (int v = 0; v < 8; ++v) batch |= kp.func == batch_kernel_function(v);
       if (!batch) continue;
       // the launch is identified by its work counter, the second argument
       const uint32_t* counter = *static_cast<uint32_t* const*>(kp.kernelParams[1]);
@@ -1424,6 +1460,7 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
   B->info.tiles = tiles;
   B->info.ctas = ctas;
   B->info.ctas_per_sm = per_sm;
+  B->info.rays_per_thread = rpt;
   B->info.launches = uint32_t(nl);
   B->info.graph_reused = reused ? 1 : 0;
   B->info.autotuned = tuned_now ? 1 : 0;
@@ -2520,6 +2557,14 @@ tvk_status tvk_paint_batch(tvk_batch* b, tvk_renderer* const* renderers, uint32_
   return guarded([&] {
     REQUIRE(b && renderers && n >= 1, "need a batch and at least one renderer");
     tvk::paint_batch(b, renderers, n);
+  });
+}
+
+tvk_status tvk_batch_set_rays_per_thread(tvk_batch* b, uint32_t rays_per_thread) {
+  return guarded([&] {
+    REQUIRE(b, "null argument");
+    REQUIRE(rays_per_thread <= 2, "rays per thread must be 0 (tuned), 1 or 2");
+    b->fixed_rays_per_thread = rays_per_thread;
   });
 }
 

@@ -599,44 +599,39 @@ struct TileShared {
   uint32_t n_cand;
 };
 
-// One 16x8-pixel tile (tile coordinates bx, by) of the frame P describes; all
-// 128 threads of the CTA take part.  kIso: isosurface mode (nearest refined hit
-// + compose); otherwise the compositing modes (1D/2D TF, lit or unlit).
-template <class T, bool kIso>
+// One tile of (16 * kRPT) x 8 pixels (tile coordinates bx, by) of the frame P
+// describes; all 128 threads of the CTA take part, each marching kRPT rays
+// one after the other (pixel columns 16 r + ...).  kIso: isosurface mode
+// (nearest refined hit + compose); otherwise the compositing modes (1D/2D TF,
+// lit or unlit).  Every pixel's value does not depend on kRPT.
+template <class T, bool kIso, int kRPT>
 __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, uint32_t by,
                                             TileShared& sh) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t px = bx * 16 + (warp & 1) * 8 + (lane & 7);
-  const uint32_t py = by * 8 + (warp >> 1) * 4 + (lane >> 3);
-  // the frame pixel this thread marches (stride 1, offset 0 for whole frames)
-  const uint32_t fx = px * P.stride + P.off_x, fy = py * P.stride + P.off_y;
-  const bool active = px < P.out_w && py < P.out_h && fx < P.width && fy < P.height;
-
-  const float nx = (float(fx) + 0.5f) * P.inv_w2 - 1.0f;
-  const float ny = (float(fy) + 0.5f) * P.inv_h2 - 1.0f;
-  const float dir[3] = {nx * P.kx, ny * P.ky, -1.0f};
-  float o[3], inv[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    o[a] = P.inv[a][3];
-    const float d = fmaf(P.inv[a][2], dir[2], fmaf(P.inv[a][1], dir[1], P.inv[a][0] * dir[0]));
-    inv[a] = 1.0f / d;
-  }
+  constexpr uint32_t kW = 16 * kRPT;
 
   // The host lists the visible bricks in a front-to-back order that holds for
   // every ray (increasing L1 grid distance from the eye's brick cell, which
   // strictly grows whenever a ray crosses into the next brick).  Each CTA
   // keeps, in that order, the bricks whose screen footprint can touch its
-  // 16x8-pixel tile; each ray then marches those its own slab test hits.
-  const float tx0 = float(bx * 16 * P.stride + P.off_x), ty0 = float(by * 8 * P.stride + P.off_y);
-  const float span_x = float(15 * P.stride), span_y = float(7 * P.stride);
+  // tile; each ray then marches those its own slab test hits.
+  const float tx0 = float(bx * kW * P.stride + P.off_x), ty0 = float(by * 8 * P.stride + P.off_y);
+  const float span_x = float((kW - 1) * P.stride), span_y = float(7 * P.stride);
 
-  float4 frame = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t samples = 0, shaded = 0, graded = 0;
+  float4 frame[kRPT];
+  uint32_t ray_samples[kRPT];
+  uint32_t shaded = 0, graded = 0;
   constexpr bool iso_mode = kIso;
-  IsoHit best;
-  float best_depth = 1.0f;  // depth buffer cleared to 1, test DF_LESS
-  bool have_hit = false;
+  IsoHit best[kRPT];
+  float best_depth[kRPT];  // depth buffer cleared to 1, test DF_LESS
+  bool have_hit[kRPT];
+#pragma unroll
+  for (int r = 0; r < kRPT; ++r) {
+    frame[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ray_samples[r] = 0;
+    best_depth[r] = 1.0f;
+    have_hit[r] = false;
+  }
   for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
     const uint32_t end = min(P.n_bricks, base + kCandChunk);
     __syncthreads();  // the previous chunk's list is no longer read
@@ -656,50 +651,80 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
         sh.n_cand += sh.warp_cnt[0] + sh.warp_cnt[1] + sh.warp_cnt[2] + sh.warp_cnt[3];
     }
     __syncthreads();
-    if (!active) continue;
     const uint32_t nc = sh.n_cand;
-    for (uint32_t c = 0; c < nc; ++c) {
-      if (frame.w >= P.frame_ert) break;
-      const DevBrick& bg = P.bricks[base + sh.cand[c]];
-      float tn = -INFINITY, tf = INFINITY;
+#pragma unroll 1
+    for (int r = 0; r < kRPT; ++r) {
+      const uint32_t px = bx * kW + uint32_t(r) * 16 + (warp & 1) * 8 + (lane & 7);
+      const uint32_t py = by * 8 + (warp >> 1) * 4 + (lane >> 3);
+      // the frame pixel this ray marches (stride 1, offset 0 for whole frames)
+      const uint32_t fx = px * P.stride + P.off_x, fy = py * P.stride + P.off_y;
+      const bool active = px < P.out_w && py < P.out_h && fx < P.width && fy < P.height;
+      if (!active) continue;
+      const float nx = (float(fx) + 0.5f) * P.inv_w2 - 1.0f;
+      const float ny = (float(fy) + 0.5f) * P.inv_h2 - 1.0f;
+      const float dir[3] = {nx * P.kx, ny * P.ky, -1.0f};
+      float o[3], inv[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        const float t0 = (__ldg(&bg.pmin[a]) - o[a]) * inv[a];
-        const float t1 = (__ldg(&bg.pmax[a]) - o[a]) * inv[a];
-        tn = fmaxf(tn, fminf(t0, t1));
-        tf = fminf(tf, fmaxf(t0, t1));
+        o[a] = P.inv[a][3];
+        const float d = fmaf(P.inv[a][2], dir[2], fmaf(P.inv[a][1], dir[1], P.inv[a][0] * dir[0]));
+        inv[a] = 1.0f / d;
       }
-      const float ti = fmaxf(tn, P.znear);
-      if (!(tf > ti) || tf > P.zfar) continue;
-      const DevBrick b = bg;
-      if (iso_mode) {
-        // A later brick's hit lies beyond its (RGBA16F-rounded) entry, so
-        // once that entry is behind the nearest hit it cannot pass the
-        // depth test; bricks come in increasing entry order along the ray.
-        if (have_hit && ti * (1.0f - 2e-3f) - 1e-4f > -best.pos[2]) break;
-        IsoHit h;
-        if (iso_brick<T>(P, b, dir, ti, tf, h, samples, shaded) && h.depth < best_depth) {
-          best = h;
-          best_depth = h.depth;
-          have_hit = true;
+      uint32_t samples = ray_samples[r];
+      for (uint32_t c = 0; c < nc; ++c) {
+        if (frame[r].w >= P.frame_ert) break;
+        const DevBrick& bg = P.bricks[base + sh.cand[c]];
+        float tn = -INFINITY, tf = INFINITY;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float t0 = (__ldg(&bg.pmin[a]) - o[a]) * inv[a];
+          const float t1 = (__ldg(&bg.pmax[a]) - o[a]) * inv[a];
+          tn = fmaxf(tn, fminf(t0, t1));
+          tf = fminf(tf, fmaxf(t0, t1));
         }
-        continue;
+        const float ti = fmaxf(tn, P.znear);
+        if (!(tf > ti) || tf > P.zfar) continue;
+        const DevBrick b = bg;
+        if (iso_mode) {
+          // A later brick's hit lies beyond its (RGBA16F-rounded) entry, so
+          // once that entry is behind the nearest hit it cannot pass the
+          // depth test; bricks come in increasing entry order along the ray.
+          if (have_hit[r] && ti * (1.0f - 2e-3f) - 1e-4f > -best[r].pos[2]) break;
+          IsoHit h;
+          if (iso_brick<T>(P, b, dir, ti, tf, h, samples, shaded) && h.depth < best_depth[r]) {
+            best[r] = h;
+            best_depth[r] = h.depth;
+            have_hit[r] = true;
+          }
+          continue;
+        }
+        const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded);
+        const float w = 1.0f - frame[r].w;
+        frame[r].x = fmaf(col.x, w, frame[r].x);
+        frame[r].y = fmaf(col.y, w, frame[r].y);
+        frame[r].z = fmaf(col.z, w, frame[r].z);
+        frame[r].w = fmaf(col.w, w, frame[r].w);
       }
-      const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded);
-      const float w = 1.0f - frame.w;
-      frame.x = fmaf(col.x, w, frame.x);
-      frame.y = fmaf(col.y, w, frame.y);
-      frame.z = fmaf(col.z, w, frame.z);
-      frame.w = fmaf(col.w, w, frame.w);
+      ray_samples[r] = samples;
     }
   }
-  // Compose-FS.glsl:58-61: no hit, or an interpolation parameter of exactly 0,
-  // leaves the pixel empty
-  if (iso_mode && have_hit && best.f != 0.0f) frame = iso_compose(P, best);
-  if (active) {
-    const size_t pix = size_t(py) * P.out_w + px;
-    P.out[pix] = frame;
-    if (P.spp) P.spp[pix] = samples;
+  uint32_t samples = 0;
+#pragma unroll
+  for (int r = 0; r < kRPT; ++r) {
+    const uint32_t px = bx * kW + uint32_t(r) * 16 + (warp & 1) * 8 + (lane & 7);
+    const uint32_t py = by * 8 + (warp >> 1) * 4 + (lane >> 3);
+    const uint32_t fx = px * P.stride + P.off_x, fy = py * P.stride + P.off_y;
+    const bool active = px < P.out_w && py < P.out_h && fx < P.width && fy < P.height;
+    // Compose-FS.glsl:58-61: no hit, or an interpolation parameter of exactly
+    // 0, leaves the pixel empty
+    float4 out = frame[r];
+    if (iso_mode && have_hit[r] && best[r].f != 0.0f) out = iso_compose(P, best[r]);
+    if (active) {
+      const size_t pix = size_t(py) * P.out_w + px;
+      P.out[pix] = out;
+      if (P.spp) P.spp[pix] = ray_samples[r];
+    }
+    samples += ray_samples[r];
   }
   // frame totals: one atomic per warp
   const uint32_t s = __reduce_add_sync(0xffffffffu, samples);
@@ -715,7 +740,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
 template <class T, bool kIso>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
   __shared__ TileShared sh;
-  render_tile<T, kIso>(P, blockIdx.x, blockIdx.y, sh);
+  render_tile<T, kIso, 1>(P, blockIdx.x, blockIdx.y, sh);
 }
 
 // Many frames in one persistent launch (the reference renders render regions
@@ -725,7 +750,7 @@ __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(co
 // renders the tile with the same code as raycast_kernel, reading the frame's
 // parameters from the launch's parameter block, so every pixel is bit-for-bit
 // the single-frame result.
-template <class T, bool kIso>
+template <class T, bool kIso, int kRPT>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS)
 raycast_batch_kernel(const __grid_constant__ BatchLaunch L, uint32_t* __restrict__ next_item) {
   __shared__ TileShared sh;
@@ -750,8 +775,8 @@ raycast_batch_kernel(const __grid_constant__ BatchLaunch L, uint32_t* __restrict
     const uint32_t f = frame_idx;
     const RenderParams& P = L.frames[f];
     const uint32_t local = it - L.tile_first[f];
-    const uint32_t tiles_x = (P.out_w + 15) / 16;
-    render_tile<T, kIso>(P, local % tiles_x, local / tiles_x, sh);
+    const uint32_t tiles_x = (P.out_w + 16 * kRPT - 1) / (16 * kRPT);
+    render_tile<T, kIso, kRPT>(P, local % tiles_x, local / tiles_x, sh);
   }
 }
 
@@ -1326,10 +1351,14 @@ void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, ui
 
 const void* batch_kernel_function(int variant) {
   switch (variant) {
-    case 0: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, false>);
-    case 1: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, true>);
-    case 2: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, false>);
-    default: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, true>);
+    case 0: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, false, 1>);
+    case 1: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, true, 1>);
+    case 2: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, false, 1>);
+    case 3: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, true, 1>);
+    case 4: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, false, 2>);
+    case 5: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint8_t, true, 2>);
+    case 6: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, false, 2>);
+    default: return reinterpret_cast<const void*>(&raycast_batch_kernel<uint16_t, true, 2>);
   }
 }
 
@@ -1343,10 +1372,14 @@ int batch_ctas_per_sm_max(int variant) {
 void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_item,
                           uint32_t ctas, cudaStream_t s, uint64_t* launches) {
   switch (variant) {
-    case 0: raycast_batch_kernel<uint8_t, false><<<ctas, 128, 0, s>>>(L, d_next_item); break;
-    case 1: raycast_batch_kernel<uint8_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
-    case 2: raycast_batch_kernel<uint16_t, false><<<ctas, 128, 0, s>>>(L, d_next_item); break;
-    default: raycast_batch_kernel<uint16_t, true><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 0: raycast_batch_kernel<uint8_t, false, 1><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 1: raycast_batch_kernel<uint8_t, true, 1><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 2: raycast_batch_kernel<uint16_t, false, 1><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 3: raycast_batch_kernel<uint16_t, true, 1><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 4: raycast_batch_kernel<uint8_t, false, 2><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 5: raycast_batch_kernel<uint8_t, true, 2><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    case 6: raycast_batch_kernel<uint16_t, false, 2><<<ctas, 128, 0, s>>>(L, d_next_item); break;
+    default: raycast_batch_kernel<uint16_t, true, 2><<<ctas, 128, 0, s>>>(L, d_next_item); break;
   }
   TVK_CUDA(cudaGetLastError());
   ++*launches;

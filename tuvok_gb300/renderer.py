@@ -367,6 +367,10 @@ class Batch:
     def SetAutotune(self, on=True, ctas_per_sm=0):
         check(lib().tvk_batch_set_autotune(self._h, int(bool(on)), int(ctas_per_sm)))
 
+    def SetRaysPerThread(self, rays=0):
+        """1 or 2 rays per thread (16x8 or 32x8 tiles); 0 lets the autotuner pick."""
+        check(lib().tvk_batch_set_rays_per_thread(self._h, int(rays)))
+
     def Paint(self, renderers):
         arr = (C.c_void_p * len(renderers))(*[r._h.value for r in renderers])
         check(lib().tvk_paint_batch(self._h, arr, len(renderers)))
