@@ -462,10 +462,19 @@ tvk_status tvk_cnn_weights_bf16(const float* w, int cout, int cin, void* fwd, vo
 tvk_status tvk_cnn_to_bf16(const float* x, size_t n, void* y, void* stream);
 
 /* Network input of a reduced frame: RGBA of the w x h image (FP32 [h][w][4]) in
- * channels 0..3, zero elsewhere and in the padding up to wp x hp, as BF16
- * [hp][wp][16]. */
-tvk_status tvk_cnn_prepare_input(const float* image_rgba, int h, int w, int hp, int wp, void* out,
-                                 void* stream);
+ * channels 0..3, the first-hit depth (FP32 [h][w], as tvk_copy_depth_device
+ * gives it; may be null) in channel 4, zero elsewhere and in the padding up to
+ * wp x hp, as BF16 [hp][wp][16]. */
+tvk_status tvk_cnn_prepare_input(const float* image_rgba, const float* depth, int h, int w, int hp,
+                                 int wp, void* out, void* stream);
+
+/* First-hit depth of the ray-marched pixels: with `on`, every paint also
+ * writes 1 / (1 + t) per pixel of the ray-marched image (render size), t the
+ * eye-space distance of the first sample that adds anything (the iso hit in
+ * iso mode), 0 where nothing is hit.  tvk_paint_learned writes it for its
+ * reduced frame regardless. */
+tvk_status tvk_set_depth_output(tvk_renderer* r, int on);
+tvk_status tvk_copy_depth_device(tvk_renderer* r, void* dst, size_t bytes);
 
 /* ---- Learned reconstruction (replaces the reference's progressive reduced-
  * quality frames, AbstrRenderer.cpp:681-787 and GLRenderer.cpp:717-747) ----

@@ -36,8 +36,8 @@ def test_gpu_learned_equals_training_forward(cuda_ok):
     # a non-zero head so the residual matters
     net.layers["head"]["w"].normal_(0, 0.05)
     net.refresh()
-    low, base, full = render_pair(torch, r, (0.4, 0.5, 1.4))
-    x = prepare_input(torch, low)
+    low, depth, base, full = render_pair(torch, r, (0.4, 0.5, 1.4))
+    x = prepare_input(torch, low, depth)
     out = net.forward(x, base.new_zeros((1, 2 * x.shape[1], 2 * x.shape[2], 4)))
     ref = (out[0, :120, :200] + base).cpu().numpy()
     lr = LearnedRenderer(net.params())
@@ -84,10 +84,29 @@ def test_gpu_learned_beats_bilinear_on_held_out_poses(cuda_ok):
     lr = LearnedRenderer(UNet.load_params())
     gains = []
     for eye, at, up in orbit_poses(6, 777):
-        low, base, full = render_pair(torch, r, eye, at)
+        low, depth, base, full = render_pair(torch, r, eye, at)
         info = lr.Paint(r, threshold_db=0.0)
         img = torch.tensor(r.ReadBackPixels(), device="cuda")
         m_learned = float(((img - full) ** 2).mean())
         m_bilinear = float(((base - full) ** 2).mean())
         gains.append(psnr(m_learned) - psnr(m_bilinear))
     assert np.mean(gains) > 0.5, gains
+
+
+def test_gpu_first_hit_depth(cuda_ok):
+    """The first-hit depth of the reduced frame (a network input): non-zero
+    exactly where the frame has opacity, 1 / (1 + t) with t the eye distance of
+    the first contributing sample, so a camera farther away sees smaller
+    values."""
+    from tuvok_gb300.learned import render_pair
+    vol, r = small_scene()
+    means = []
+    for dist in (1.3, 2.6):
+        low, depth, base, full = render_pair(torch, r, (0.0, 0.0, dist))
+        a = low[..., 3].cpu().numpy()
+        d = depth.cpu().numpy()
+        assert ((d > 0) == (a > 0)).all()
+        hit = d[d > 0]
+        assert hit.size > 0 and (hit < 1.0 / (1.0 + (dist - 0.9))).all() and (hit > 0.0).all()
+        means.append(float(hit.mean()))
+    assert means[1] < means[0]

@@ -167,7 +167,9 @@ PROTOTYPES = {
                      C.c_int, _vp],
     "tvk_cnn_weights_bf16": [_vp, C.c_int, C.c_int, _vp, _vp, _vp],
     "tvk_cnn_to_bf16": [_vp, C.c_size_t, _vp, _vp],
-    "tvk_cnn_prepare_input": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_cnn_prepare_input": [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_set_depth_output": [_vp, C.c_int],
+    "tvk_copy_depth_device": [_vp, _vp, C.c_size_t],
     "tvk_learned_param_count": [C.POINTER(C.c_size_t)],
     "tvk_learned_create": [_f32p, C.c_size_t, C.POINTER(_vp)],
     "tvk_learned_destroy": [_vp],

@@ -571,6 +571,8 @@ struct tvk_renderer {
   uint64_t slot_clock = 0;
   float iso_color[3] = {0.5f, 0.5f, 0.5f};  // AbstrRenderer.cpp:86 m_vIsoColor
   bool cell_skip = true;
+  bool depth_out = false;            // write the first-hit depth of ray-marched pixels
+  tvk::DevBuf d_depth;
   tvk_stats stats{};
   uint64_t launches = 0;
   bool painted = false;
@@ -1071,6 +1073,10 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   if (upscale) R->d_lowimg.ensure(size_t(rw) * rh * sizeof(float4));
   P.out = upscale ? R->d_lowimg.as<float4>() : R->d_img.as<float4>();
   P.spp = R->d_spp.as<uint32_t>();
+  if (R->depth_out) {
+    R->d_depth.ensure(size_t(rw) * rh * sizeof(float));
+    P.depth = R->d_depth.as<float>();
+  }
   P.counters = st.d_counters->as<unsigned long long>();
   TVK_CUDA(cudaMemsetAsync(st.d_counters->p, 0, 4 * sizeof(unsigned long long), st.stream));
   R->stats.bricks_visible = nvis;
@@ -1544,18 +1550,22 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
                           N->probe_stream};
   const PlannedFrame full = plan_frame(R, Subframe{0, false, false}, &probe_stage);
   const float saved_dec = R->screen_dec, saved_sdec = R->sample_dec;
+  const bool saved_depth = R->depth_out;
   R->screen_dec = 2.0f;
   R->sample_dec = 2.0f;
+  R->depth_out = true;  // the network reads the reduced frame's first-hit depth
   PlannedFrame low;
   try {
     low = plan_frame(R, Subframe{0, true, true});
   } catch (...) {
     R->screen_dec = saved_dec;
     R->sample_dec = saved_sdec;
+    R->depth_out = saved_depth;
     throw;
   }
   R->screen_dec = saved_dec;
   R->sample_dec = saved_sdec;
+  R->depth_out = saved_depth;
   // TF tables and empty-cell bits of both plans were written on the
   // renderer's stream: the probe stream starts after them
   TVK_CUDA(cudaEventRecord(N->ev_planned, s));
@@ -1591,7 +1601,8 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
     fail(TVK_ERR_INTERNAL, "reduced frame smaller than half the viewport");
   DevBuf& x16 = N->d_input;
   x16.ensure(size_t(N->hp) * N->wp * 16 * 2);
-  cnn_prepare_input(lowimg, int(low.rh), int(low.rw), N->hp, N->wp, x16.p, s);
+  cnn_prepare_input(lowimg, R->d_depth.as<float>(), int(low.rh), int(low.rw), N->hp, N->wp,
+                    x16.p, s);
   run_unet(N, x16.p, R->d_img.as<float>(), int(R->height), int(R->width), s);
   R->launches += kUNetLayers + 8;
   TVK_CUDA(cudaEventRecord(N->ev[2], s));
@@ -2654,11 +2665,29 @@ tvk_status tvk_paint_learned(tvk_renderer* r, tvk_learned* net, float threshold_
   });
 }
 
-tvk_status tvk_cnn_prepare_input(const float* image_rgba, int h, int w, int hp, int wp, void* out,
-                                 void* stream) {
+tvk_status tvk_cnn_prepare_input(const float* image_rgba, const float* depth, int h, int w, int hp,
+                                 int wp, void* out, void* stream) {
   return guarded([&] {
     REQUIRE(image_rgba && out && hp >= h && wp >= w, "null argument or padding too small");
-    tvk::cnn_prepare_input(image_rgba, h, w, hp, wp, out, as_stream(stream));
+    tvk::cnn_prepare_input(image_rgba, depth, h, w, hp, wp, out, as_stream(stream));
+  });
+}
+
+tvk_status tvk_set_depth_output(tvk_renderer* r, int on) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    r->depth_out = on != 0;
+  });
+}
+
+tvk_status tvk_copy_depth_device(tvk_renderer* r, void* dst, size_t bytes) {
+  return guarded([&] {
+    REQUIRE(r && dst, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    if (!r->depth_out || !r->d_depth.p) tvk::fail(TVK_ERR_STATE, "depth output is off");
+    const size_t n = size_t(r->render_w) * r->render_h * sizeof(float);
+    REQUIRE(bytes >= n, "destination smaller than the depth image");
+    TVK_CUDA(cudaMemcpyAsync(dst, r->d_depth.p, n, cudaMemcpyDeviceToDevice, r->stream));
   });
 }
 

@@ -461,7 +461,8 @@ __global__ void head_kernel(const float* __restrict__ head, const float* base, i
 
 // Network input of a reduced frame: RGBA of the w x h image in channels 0..3,
 // zero elsewhere and in the padding up to wp x hp, as BF16 [hp][wp][16]
-__global__ void prepare_input_kernel(const float4* __restrict__ img, int h, int w, int hp, int wp,
+__global__ void prepare_input_kernel(const float4* __restrict__ img,
+                                     const float* __restrict__ depth, int h, int w, int hp, int wp,
                                      uint32_t* __restrict__ out) {
   const size_t total = size_t(hp) * wp * 8;  // 8 words (16 BF16) per pixel
   for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
@@ -474,6 +475,8 @@ __global__ void prepare_input_kernel(const float4* __restrict__ img, int h, int 
       const float4 c = img[size_t(yy) * w + xx];
       v = word == 0 ? pack_bf16(__float2bfloat16_rn(c.x), __float2bfloat16_rn(c.y))
                     : pack_bf16(__float2bfloat16_rn(c.z), __float2bfloat16_rn(c.w));
+    } else if (word == 2 && depth && xx < w && yy < h) {
+      v = pack_bf16(__float2bfloat16_rn(depth[size_t(yy) * w + xx]), __float2bfloat16_rn(0.0f));
     }
     out[i] = v;
   }
@@ -725,9 +728,10 @@ void cnn_head(const float* head, const float* base, int n, int h, int w, int oh,
   TVK_CUDA(cudaGetLastError());
 }
 
-void cnn_prepare_input(const float* img, int h, int w, int hp, int wp, void* out, cudaStream_t s) {
+void cnn_prepare_input(const float* img, const float* depth, int h, int w, int hp, int wp,
+                       void* out, cudaStream_t s) {
   prepare_input_kernel<<<grid_for(size_t(hp) * wp * 8), 256, 0, s>>>(
-      reinterpret_cast<const float4*>(img), h, w, hp, wp, static_cast<uint32_t*>(out));
+      reinterpret_cast<const float4*>(img), depth, h, w, hp, wp, static_cast<uint32_t*>(out));
   TVK_CUDA(cudaGetLastError());
 }
 

@@ -224,7 +224,7 @@ template <class T>
 __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBrick& b,
                                               const float dir[3], float t_in, float t_out,
                                               uint32_t& samples, uint32_t& shaded,
-                                              uint32_t& graded) {
+                                              uint32_t& graded, float& first_t) {
   float en[3], ex[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -386,6 +386,8 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       src.x = lc[0]; src.y = lc[1]; src.z = lc[2];
       if (two_d) src.w = fminf(fmaxf(src.w, 0.0f), 1.0f);
     }
+    // the first sample that adds anything (the ray's first hit, a network input)
+    if (src.w != 0.0f && first_t == INFINITY) first_t = t_in + float(i) * ((t_out - t_in) / q);
     // Compositing.glsl:33-38 UnderCompositing
     const float w = 1.0f - c.w;
     c.x = fmaf(src.x * w, src.w, c.x);
@@ -619,6 +621,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   const float span_x = float((kW - 1) * P.stride), span_y = float(7 * P.stride);
 
   float4 frame[kRPT];
+  float first_t[kRPT];
   uint32_t ray_samples[kRPT];
   uint32_t shaded = 0, graded = 0;
   constexpr bool iso_mode = kIso;
@@ -628,6 +631,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
 #pragma unroll
   for (int r = 0; r < kRPT; ++r) {
     frame[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    first_t[r] = INFINITY;
     ray_samples[r] = 0;
     best_depth[r] = 1.0f;
     have_hit[r] = false;
@@ -698,7 +702,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           }
           continue;
         }
-        const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded);
+        const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded, first_t[r]);
         const float w = 1.0f - frame[r].w;
         frame[r].x = fmaf(col.x, w, frame[r].x);
         frame[r].y = fmaf(col.y, w, frame[r].y);
@@ -718,11 +722,15 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
     // Compose-FS.glsl:58-61: no hit, or an interpolation parameter of exactly
     // 0, leaves the pixel empty
     float4 out = frame[r];
-    if (iso_mode && have_hit[r] && best[r].f != 0.0f) out = iso_compose(P, best[r]);
+    if (iso_mode && have_hit[r] && best[r].f != 0.0f) {
+      out = iso_compose(P, best[r]);
+      first_t[r] = -best[r].pos[2];
+    }
     if (active) {
       const size_t pix = size_t(py) * P.out_w + px;
       P.out[pix] = out;
       if (P.spp) P.spp[pix] = ray_samples[r];
+      if (P.depth) P.depth[pix] = first_t[r] == INFINITY ? 0.0f : 1.0f / (1.0f + first_t[r]);
     }
     samples += ray_samples[r];
   }

@@ -208,6 +208,7 @@ struct RenderParams {
   uint32_t out_w, out_h, stride, off_x, off_y;
   float4* out;
   uint32_t* spp;             // per-pixel sample counts (may be null)
+  float* depth;              // per pixel 1 / (1 + first-hit distance), 0: no hit (may be null)
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
 };
 
@@ -285,7 +286,8 @@ void cnn_upsample2_backward(const float* dy, int n, int h, int w, int c, float* 
                             cudaStream_t s);
 void cnn_head(const float* head, const float* base, int n, int h, int w, int oh, int ow,
               float* out, cudaStream_t s);
-void cnn_prepare_input(const float* img, int h, int w, int hp, int wp, void* out, cudaStream_t s);
+void cnn_prepare_input(const float* img, const float* depth, int h, int w, int hp, int wp,
+                       void* out, cudaStream_t s);
 void cnn_probe_mse(const float* frame, int w, const float* probe, int pw, int ph, int stride,
                    int ox, int oy, float* sum, cudaStream_t s);
 void cnn_head_backward(const float* dout, int n, int h, int w, float* dhead, cudaStream_t s);

@@ -236,12 +236,14 @@ class UNet:
         return acc, dout
 
 
-def prepare_input(torch, low):
-    """Reduced RGBA frame [h][w][4] (FP32, device) -> BF16 input [1][hp][wp][16]."""
+def prepare_input(torch, low, depth=None):
+    """Reduced RGBA frame [h][w][4] and its first-hit depth [h][w] (FP32,
+    device) -> BF16 input [1][hp][wp][16]."""
     h, w = low.shape[0], low.shape[1]
     hp, wp = (h + 7) // 8 * 8, (w + 7) // 8 * 8
     x = torch.empty((1, hp, wp, 16), dtype=torch.bfloat16, device="cuda")
-    check(lib().tvk_cnn_prepare_input(_p(low), h, w, hp, wp, _p(x),
+    check(lib().tvk_cnn_prepare_input(_p(low), _p(depth) if depth is not None else None, h, w,
+                                      hp, wp, _p(x),
                                       C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return x
 
@@ -312,23 +314,28 @@ def configure_lit(r, vol, tf, width=1920, height=1080, srm=1.5):
 
 
 def render_pair(torch, r, eye, at=(0, 0, 0)):
-    """(reduced RGBA [540][960][4], bilinear upscale [1080][1920][4], plain [1080][1920][4])."""
+    """(reduced RGBA [540][960][4], its first-hit depth [540][960], bilinear
+    upscale [1080][1920][4], plain [1080][1920][4])."""
     r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at)
     r.SetReducedQuality(True, True)
+    check(lib().tvk_set_depth_output(r.handle, 1))
     r.Paint()
     rw, rh = r.GetRenderSize()
     W, H = r._w, r._h_px
     low = torch.empty((rh, rw, 4), dtype=torch.float32, device="cuda")
+    depth = torch.empty((rh, rw), dtype=torch.float32, device="cuda")
     base = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     full = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     check(lib().tvk_copy_image_device(r.handle, 1, _p(low), low.numel() * 4))
+    check(lib().tvk_copy_depth_device(r.handle, _p(depth), depth.numel() * 4))
     check(lib().tvk_copy_image_device(r.handle, 0, _p(base), base.numel() * 4))
+    check(lib().tvk_set_depth_output(r.handle, 0))
     r.SetReducedQuality(False, False)
     r.Paint()
     check(lib().tvk_copy_image_device(r.handle, 0, _p(full), full.numel() * 4))
     torch.cuda.current_stream().wait_stream(torch.cuda.ExternalStream(r.GetStream()))
     torch.cuda.synchronize()
-    return low, base, full
+    return low, depth, base, full
 
 
 def psnr(mse):
@@ -357,8 +364,8 @@ def train(torch, steps=4000, crops=8, crop=128, lr=1e-3, seed=7, log=print, net=
             vol = vols[int(rng.integers(0, len(vols)))]
             configure_lit(r, vol, random_bands_tf(rng))
             eye, at = random_camera(rng)
-            low, base, full = render_pair(torch, r, eye, at)
-            x = prepare_input(torch, low)
+            low, depth, base, full = render_pair(torch, r, eye, at)
+            x = prepare_input(torch, low, depth)
             pair = (x, base, full)
         x, base, full = pair
         ys = rng.integers(0, (low.shape[0] - crop) // 2 + 1, crops) * 2
@@ -435,9 +442,11 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--minutes", type=float, default=None, help="stop after this wall time")
     ap.add_argument("--out", default=str(WEIGHTS))
-    ap.add_argument("--resume", action="store_true")
+    ap.add_argument("--resume", action="store_true", help="continue from the weights at --out")
+    ap.add_argument("--init", default=None, help="start from these weights (fine-tuning)")
     a = ap.parse_args()
-    net = UNet(torch, params=UNet.load_params(a.out), seed=a.seed) if a.resume else None
+    start = a.init or (a.out if a.resume else None)
+    net = UNet(torch, params=UNet.load_params(start), seed=a.seed) if start else None
     net, hist = train(torch, steps=a.steps, crops=a.crops, crop=a.crop, lr=a.lr, seed=a.seed,
                       net=net, time_budget_s=a.minutes * 60 if a.minutes else None)
     net.save(a.out, steps=len(hist) and hist[-1][0] + 1, crops=a.crops, crop=a.crop, lr=a.lr,
