@@ -837,8 +837,8 @@ namespace {
 // One pass of the separable Chebyshev distance transform: one thread per line
 // of cells along `axis` of brick brick_base + blockIdx.y.  Pass x measures the
 // 1D distance to the nearest non-empty cell of the line (forward and backward
-// sweeps); passes y and z take min over j of max(|i - j|, previous(j)) in a
-// window of kCellDistCap.  Cells outside the brick count as empty.
+// sweeps); passes y and z take min over j of max(|i - j|, previous(j)) for
+// |i - j| < kCellDistCap.  Cells outside the brick count as empty.
 __global__ void cell_dist_kernel(const CellDistParams P, int axis, uint32_t brick_base) {
   const uint32_t b = brick_base + blockIdx.y;
   if (b >= P.n_bricks) return;
@@ -879,12 +879,13 @@ __global__ void cell_dist_kernel(const CellDistParams P, int axis, uint32_t bric
     return;
   }
   const uint8_t* in = P.in + co;
-  for (uint32_t i = 0; i < len; ++i) {
-    int best = kCellDistCap;
-    const int j0 = max(0, int(i) - kCellDistCap), j1 = min(int(len) - 1, int(i) + kCellDistCap);
-    for (int j = j0; j <= j1 && best > 0; ++j) {
-      const int v = max(abs(int(i) - j), int(in[base + uint64_t(j) * stride]));
-      best = min(best, v);
+  for (int i = 0; i < int(len); ++i) {
+    // grow the window outward from i: a cell r away gives at least r, so the
+    // search ends once r reaches the best value found
+    int best = min(kCellDistCap, int(in[base + uint64_t(i) * stride]));
+    for (int r = 1; r < best; ++r) {
+      if (i - r >= 0) best = min(best, max(r, int(in[base + uint64_t(i - r) * stride])));
+      if (i + r < int(len)) best = min(best, max(r, int(in[base + uint64_t(i + r) * stride])));
     }
     out[base + uint64_t(i) * stride] = uint8_t(best);
   }
