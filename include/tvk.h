@@ -468,6 +468,16 @@ tvk_status tvk_cnn_to_bf16(const float* x, size_t n, void* y, void* stream);
 tvk_status tvk_cnn_prepare_input(const float* image_rgba, const float* depth, int h, int w, int hp,
                                  int wp, void* out, void* stream);
 
+/* AbstrRenderer::SetClipPlane / EnableClipPlane / DisableClipPlane
+ * (AbstrRenderer.h:215-219) for the brick-by-brick ray march: plane (a, b, c, d)
+ * in world space; points with n . x + d >= 0, n = normalize(a, b, c) in model
+ * space, are cut away (PLANE::clip, Basics/Vectors.h:1455-1457).  Each brick's
+ * ray segment is cut at the plane (GLRaycaster.cpp:328-337 caps the brick box)
+ * and bricks wholly on the cut side are skipped (AbstrRenderer::Clipped,
+ * AbstrRenderer.cpp:923-948).  tvk_leaper_paint refuses a clipping renderer. */
+tvk_status tvk_set_clip_plane(tvk_renderer* r, const float plane[4]);
+tvk_status tvk_enable_clip_plane(tvk_renderer* r, int on);
+
 /* First-hit depth of the ray-marched pixels: with `on`, every paint also
  * writes 1 / (1 + t) per pixel of the ray-marched image (render size), t the
  * eye-space distance of the first sample that adds anything (the iso hit in

@@ -183,6 +183,10 @@ class Renderer {
     check(tvk_get_stats(r_, &s));
     return s;
   }
+  // AbstrRenderer::SetClipPlane / EnableClipPlane / DisableClipPlane (world space)
+  void SetClipPlane(const float plane[4]) { check(tvk_set_clip_plane(r_, plane)); }
+  void EnableClipPlane() { check(tvk_enable_clip_plane(r_, 1)); }
+  void DisableClipPlane() { check(tvk_enable_clip_plane(r_, 0)); }
   // m_iCurrentLOD, decreaseScreenResNow / decreaseSamplingRateNow
   void SetLOD(uint32_t lod) { check(tvk_set_lod(r_, lod)); }
   void SetReducedQuality(bool screen, bool sampling) {

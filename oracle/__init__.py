@@ -35,7 +35,7 @@ class Scene(C.Structure):
         ("row_phase", C.c_uint32), ("threads", C.c_int), ("iso_color", C.c_float * 3),
         ("lod", C.c_uint32), ("median", C.c_int), ("decrease_screen_res", C.c_int),
         ("decrease_sampling_rate", C.c_int), ("screen_res_dec_factor", C.c_float),
-        ("sample_dec_factor", C.c_float),
+        ("sample_dec_factor", C.c_float), ("clip_on", C.c_int), ("clip_plane", C.c_float * 4),
     ]
 
 
@@ -241,7 +241,7 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
                light_dir=(0, 0, -1), bp=(0.2, 0.6, 0.2, 32.0), frame_ert=1.0,
                use_double=False, row_stride=1, row_phase=0, threads=0, isovalue=None,
                iso_color=(0.5, 0.5, 0.5), lod=0, median=False, dec_screen=False,
-               dec_sampling=False, screen_dec=2.0, sample_dec=2.0):
+               dec_sampling=False, screen_dec=2.0, sample_dec=2.0, clip_plane=None):
     """Scene struct for the oracle; returns (scene, arrays that must stay alive)."""
     raw = np.ascontiguousarray(raw)
     tf = np.ascontiguousarray(np.asarray(tf, dtype=np.float32))
@@ -285,6 +285,9 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
         isovalue = float(np.float32(float(raw.max()) - float(raw.min())) / np.float32(2.0))
     s.isovalue = isovalue
     s.iso_color[:] = iso_color
+    if clip_plane is not None:
+        s.clip_on = 1
+        s.clip_plane[:] = [float(x) for x in clip_plane]
     return s, (raw, tf)
 
 

@@ -160,6 +160,11 @@ typedef struct orc_scene {
   int median;               /* ComputeHierarchy filter of those LODs */
   int decrease_screen_res, decrease_sampling_rate;
   float screen_res_dec_factor, sample_dec_factor;
+  /* AbstrRenderer's clip plane (SetClipPlane / EnableClipPlane): a, b, c, d
+   * in world (= model) space; points with n.x + d >= 0, n = normalize(a, b, c),
+   * are cut away (PLANE::clip, Basics/Vectors.h:1455-1457) */
+  int clip_on;
+  float clip_plane[4];
 } orc_scene;
 
 /* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row

@@ -188,7 +188,41 @@ struct Setup {
   float light_a[3], light_d[3], light_s[3];
   float domain_scale[3];
   double norm_mat[3][3];
+  // clip plane: model-space plane and its eye-space form, bricks wholly cut away
+  float clip_model[4], clip_eye[4];
+  std::vector<char> clipped;
 };
+
+// The clip plane in model space: the normal normalised, d kept
+// (GLRaycaster.cpp:328-337 with an identity model transform).
+void clip_model_plane(const float plane[4], float out[4]) {
+  const float len = std::sqrt((plane[0] * plane[0] + plane[1] * plane[1]) + plane[2] * plane[2]);
+  for (int a = 0; a < 3; ++a) out[a] = plane[a] / len;
+  out[3] = plane[3];
+}
+
+// AbstrRenderer::Clipped (AbstrRenderer.cpp:923-948): every corner of the
+// brick box on the cut side
+bool brick_clipped(const float pl[4], const float pmin[3], const float pmax[3]) {
+  for (int c = 0; c < 8; ++c) {
+    const float x = (c & 4) ? pmax[0] : pmin[0];
+    const float y = (c & 2) ? pmax[1] : pmin[1];
+    const float z = (c & 1) ? pmax[2] : pmin[2];
+    if (!(((pl[0] * x + pl[1] * y) + pl[2] * z) + pl[3] >= 0.0f)) return false;
+  }
+  return true;
+}
+
+// Ray parameters [lo, hi] kept by the clip plane along the eye-space ray
+// dir * t: the cut is where the plane's eye-space form changes sign.
+inline void clip_range(const float ce[4], const float dir[3], float& lo, float& hi) {
+  const float s = std::fma(ce[2], dir[2], std::fma(ce[1], dir[1], ce[0] * dir[0]));
+  lo = -INFINITY;
+  hi = INFINITY;
+  if (s > 0.0f) hi = -ce[3] / s;
+  else if (s < 0.0f) lo = -ce[3] / s;
+  else if (ce[3] > 0.0f) { lo = INFINITY; hi = -INFINITY; }
+}
 
 template <class T>
 void lighting_ref(const Setup& st, const T pos[3], const T N[3], const T tfc[3], T out[3]) {
@@ -463,7 +497,10 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
   for (int a = 0; a < 3; ++a) inv[a] = 1.0f / d[a];
   struct Hit { float t0, t1; int b; };
   std::vector<Hit> hits;
+  float clip_lo = -INFINITY, clip_hi = INFINITY;
+  if (s.clip_on) clip_range(st.clip_eye, dir, clip_lo, clip_hi);
   for (int bi : st.visible) {
+    if (s.clip_on && st.clipped[bi]) continue;
     const BrickR& b = st.bricks[bi];
     float tn = -INFINITY, tf = INFINITY;
     for (int a = 0; a < 3; ++a) {
@@ -476,7 +513,10 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
     // front faces are clipped; a back face behind the far plane is clipped.
     const float ti = std::fmax(tn, s.znear);
     if (!(tf > ti) || tf > s.zfar) continue;
-    hits.push_back({ti, tf, bi});
+    // the clipped box's front faces (its cap included) and back faces
+    const float ci = std::fmax(ti, clip_lo), cf = std::fmin(tf, clip_hi);
+    if (!(cf > ci)) continue;
+    hits.push_back({ci, cf, bi});
   }
   std::sort(hits.begin(), hits.end(), [](const Hit& a, const Hit& b) {
     return a.t0 < b.t0 || (a.t0 == b.t0 && a.b < b.b);
@@ -687,6 +727,20 @@ void apply_view(Setup& st) {
   st.view = make_view(*st.s);
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) st.norm_mat[r][c] = st.view.mv[r][c];
+  st.clipped.assign(st.bricks.size(), 0);
+  if (st.s->clip_on) {
+    clip_model_plane(st.s->clip_plane, st.clip_model);
+    double d = double(st.clip_model[3]);
+    for (int j = 0; j < 3; ++j) {
+      double n = 0;
+      for (int i = 0; i < 3; ++i) n += double(st.clip_model[i]) * st.view.inv[i][j];
+      st.clip_eye[j] = float(n);
+    }
+    for (int i = 0; i < 3; ++i) d += double(st.clip_model[i]) * st.view.inv[i][3];
+    st.clip_eye[3] = float(d);
+    for (size_t k = 0; k < st.bricks.size(); ++k)
+      st.clipped[k] = brick_clipped(st.clip_model, st.bricks[k].pmin, st.bricks[k].pmax) ? 1 : 0;
+  }
   for (BrickR& b : st.bricks) {
     for (int a = 0; a < 3; ++a) {
       const double sc = double((b.tmin[a] - b.tmax[a]) / (b.pmin[a] - b.pmax[a]));

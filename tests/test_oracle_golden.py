@@ -202,3 +202,21 @@ def test_round_half_is_ieee_rne():
                          [1e-8, 3e-8, 6e-5, 65504.0, 65519.99, 65520.0, 0.0, -0.0]])
     for x in xs.astype(np.float32):
         assert O.round_half(x) == float(np.float32(np.float16(x))), x
+
+
+def test_oracle_clip_plane_properties():
+    """The oracle's clip plane: a plane beyond the volume changes nothing, one
+    that cuts everything leaves an empty frame, and a half cut removes samples."""
+    import numpy as np
+    from tuvok_gb300.workloads import numpy_blob_volume
+    raw = numpy_blob_volume((24, 20, 18), np.uint8, 4, (3, 7), (80, 255), 255, 5, 0)
+    tf = np.zeros((256, 4), dtype=np.float32)
+    tf[:, 0] = tf[:, 3] = np.linspace(0, 0.5, 256)
+    kw = dict(width=24, height=20, eye=(0.3, 0.4, 1.5), want_counts=True)
+    base, n, _ = O.render(raw, (10, 10, 10), 1, tf, **kw)
+    same, n2, _ = O.render(raw, (10, 10, 10), 1, tf, clip_plane=(1, 0, 0, -10), **kw)
+    assert np.array_equal(base, same) and n == n2
+    none, n3, _ = O.render(raw, (10, 10, 10), 1, tf, clip_plane=(1, 0, 0, 10), **kw)
+    assert not none.any() and n3 == 0
+    half, n4, _ = O.render(raw, (10, 10, 10), 1, tf, clip_plane=(1, 0, 0, 0), **kw)
+    assert 0 < n4 < n

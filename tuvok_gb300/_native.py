@@ -168,6 +168,8 @@ PROTOTYPES = {
     "tvk_cnn_weights_bf16": [_vp, C.c_int, C.c_int, _vp, _vp, _vp],
     "tvk_cnn_to_bf16": [_vp, C.c_size_t, _vp, _vp],
     "tvk_cnn_prepare_input": [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
+    "tvk_set_clip_plane": [_vp, _f32p],
+    "tvk_enable_clip_plane": [_vp, C.c_int],
     "tvk_set_depth_output": [_vp, C.c_int],
     "tvk_copy_depth_device": [_vp, _vp, C.c_size_t],
     "tvk_learned_param_count": [C.POINTER(C.c_size_t)],

@@ -572,6 +572,8 @@ struct tvk_renderer {
   float iso_color[3] = {0.5f, 0.5f, 0.5f};  // AbstrRenderer.cpp:86 m_vIsoColor
   bool cell_skip = true;
   bool depth_out = false;            // write the first-hit depth of ray-marched pixels
+  bool clip_on = false;              // AbstrRenderer m_bClipPlaneOn
+  float clip_plane[4] = {0, 0, 1, 0};  // m_ClipPlane, world space
   tvk::DevBuf d_depth;
   tvk_stats stats{};
   uint64_t launches = 0;
@@ -958,6 +960,42 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     }
     eye_cell[a] = e;
   }
+  // The clip plane in model space (GLRaycaster.cpp:328-337: the world plane
+  // through the inverse model transform, the normal normalised, d kept) and
+  // in eye space for the rays
+  float clip_m[4] = {0, 0, 0, 0}, clip_e[4] = {0, 0, 0, 0};
+  if (R->clip_on) {
+    double nm[3], dm = double(R->clip_plane[3]);
+    for (int j = 0; j < 3; ++j) {
+      nm[j] = 0;
+      for (int i = 0; i < 3; ++i) nm[j] += double(R->clip_plane[i]) * R->model[i][j];
+    }
+    for (int i = 0; i < 3; ++i) dm += double(R->clip_plane[i]) * R->model[i][3];
+    const float n0 = float(nm[0]), n1 = float(nm[1]), n2 = float(nm[2]);
+    const float len = std::sqrt((n0 * n0 + n1 * n1) + n2 * n2);
+    clip_m[0] = n0 / len;
+    clip_m[1] = n1 / len;
+    clip_m[2] = n2 / len;
+    clip_m[3] = float(dm);
+    double de = double(clip_m[3]);
+    for (int j = 0; j < 3; ++j) {
+      double ne = 0;
+      for (int i = 0; i < 3; ++i) ne += double(clip_m[i]) * view.inv[i][j];
+      clip_e[j] = float(ne);
+    }
+    for (int i = 0; i < 3; ++i) de += double(clip_m[i]) * view.inv[i][3];
+    clip_e[3] = float(de);
+  }
+  // AbstrRenderer::Clipped (AbstrRenderer.cpp:923-948): every corner cut away
+  auto clipped = [&](const float pmin[3], const float pmax[3]) {
+    for (int c = 0; c < 8; ++c) {
+      const float x = (c & 4) ? pmax[0] : pmin[0];
+      const float y = (c & 2) ? pmax[1] : pmin[1];
+      const float z = (c & 1) ? pmax[2] : pmin[2];
+      if (!(((clip_m[0] * x + clip_m[1] * y) + clip_m[2] * z) + clip_m[3] >= 0.0f)) return false;
+    }
+    return true;
+  };
   std::vector<std::pair<uint64_t, uint64_t>> order;  // (L1 distance, brick)
   order.reserve(nbl);
   for (uint64_t j = 0; j < nbl; ++j) {
@@ -975,7 +1013,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   for (const auto& ok : order) {
     const uint64_t k = ok.second;
     const tvk_brick_md& m = V->md[k];
-    DevBrick& b = hb[nvis++];
+    DevBrick& b = hb[nvis];
     std::memset(&b, 0, sizeof(b));
     float e[3], c[3], tmin[3], tmax[3];
     for (int a = 0; a < 3; ++a) {
@@ -1005,6 +1043,8 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     b.off = V->offsets[k];
     b.cells = V->cell_dims[k];
     b.cell_off = V->cell_offsets[k];
+    if (R->clip_on && clipped(b.pmin, b.pmax)) continue;  // the slot is reused
+    ++nvis;
   }
   st.d_bricks->ensure(std::max<size_t>(1, nbl) * sizeof(DevBrick));
   if (nvis)
@@ -1041,6 +1081,8 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     for (int j = 0; j < 4; ++j) P.inv[a][j] = float(view.inv[a][j]);
     for (int j = 0; j < 4; ++j) P.mv[a][j] = float(view.mv[a][j]);
   }
+  P.clip_on = R->clip_on ? 1 : 0;
+  for (int a = 0; a < 4; ++a) P.clip_eye[a] = clip_e[a];
   P.bp_ka = R->bp[0];
   P.bp_kd = R->bp[1];
   P.bp_ks = R->bp[2];
@@ -1762,6 +1804,7 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
   if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
   if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
   if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
+  if (R->clip_on) fail(TVK_ERR_UNSUPPORTED, "the GridLeaper does not clip (disable the clip plane)");
   TVK_CUDA(cudaSetDevice(R->device));
   const uint64_t launches0 = R->launches;
   const float srm = R->srm;
@@ -2670,6 +2713,25 @@ tvk_status tvk_cnn_prepare_input(const float* image_rgba, const float* depth, in
   return guarded([&] {
     REQUIRE(image_rgba && out && hp >= h && wp >= w, "null argument or padding too small");
     tvk::cnn_prepare_input(image_rgba, depth, h, w, hp, wp, out, as_stream(stream));
+  });
+}
+
+tvk_status tvk_set_clip_plane(tvk_renderer* r, const float plane[4]) {
+  return guarded([&] {
+    REQUIRE(r && plane, "null argument");
+    REQUIRE(std::isfinite(plane[0]) && std::isfinite(plane[1]) && std::isfinite(plane[2]) &&
+                std::isfinite(plane[3]),
+            "clip plane must be finite");
+    REQUIRE(plane[0] != 0.0f || plane[1] != 0.0f || plane[2] != 0.0f,
+            "clip plane normal must not be zero");
+    for (int a = 0; a < 4; ++a) r->clip_plane[a] = plane[a];
+  });
+}
+
+tvk_status tvk_enable_clip_plane(tvk_renderer* r, int on) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    r->clip_on = on != 0;
   });
 }
 

@@ -674,6 +674,16 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
         const float d = fmaf(P.inv[a][2], dir[2], fmaf(P.inv[a][1], dir[1], P.inv[a][0] * dir[0]));
         inv[a] = 1.0f / d;
       }
+      // the clip plane keeps the ray parameters [clip_lo, clip_hi]
+      // (GLRaycaster.cpp:328-337 caps each brick box with the plane)
+      float clip_lo = -INFINITY, clip_hi = INFINITY;
+      if (P.clip_on) {
+        const float cs = fmaf(P.clip_eye[2], dir[2], fmaf(P.clip_eye[1], dir[1],
+                                                          P.clip_eye[0] * dir[0]));
+        if (cs > 0.0f) clip_hi = -P.clip_eye[3] / cs;
+        else if (cs < 0.0f) clip_lo = -P.clip_eye[3] / cs;
+        else if (P.clip_eye[3] > 0.0f) { clip_lo = INFINITY; clip_hi = -INFINITY; }
+      }
       uint32_t samples = ray_samples[r];
       for (uint32_t c = 0; c < nc; ++c) {
         if (frame[r].w >= P.frame_ert) break;
@@ -686,8 +696,10 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           tn = fmaxf(tn, fminf(t0, t1));
           tf = fminf(tf, fmaxf(t0, t1));
         }
-        const float ti = fmaxf(tn, P.znear);
-        if (!(tf > ti) || tf > P.zfar) continue;
+        const float t_near = fmaxf(tn, P.znear);
+        if (!(tf > t_near) || tf > P.zfar) continue;
+        const float ti = fmaxf(t_near, clip_lo), tc = fminf(tf, clip_hi);
+        if (!(tc > ti)) continue;
         const DevBrick b = bg;
         if (iso_mode) {
           // A later brick's hit lies beyond its (RGBA16F-rounded) entry, so
@@ -695,14 +707,14 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           // depth test; bricks come in increasing entry order along the ray.
           if (have_hit[r] && ti * (1.0f - 2e-3f) - 1e-4f > -best[r].pos[2]) break;
           IsoHit h;
-          if (iso_brick<T>(P, b, dir, ti, tf, h, samples, shaded) && h.depth < best_depth[r]) {
+          if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
             best[r] = h;
             best_depth[r] = h.depth;
             have_hit[r] = true;
           }
           continue;
         }
-        const float4 col = march_brick<T>(P, b, dir, ti, tf, samples, shaded, graded, first_t[r]);
+        const float4 col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
         const float w = 1.0f - frame[r].w;
         frame[r].x = fmaf(col.x, w, frame[r].x);
         frame[r].y = fmaf(col.y, w, frame[r].y);

@@ -209,6 +209,8 @@ struct RenderParams {
   float4* out;
   uint32_t* spp;             // per-pixel sample counts (may be null)
   float* depth;              // per pixel 1 / (1 + first-hit distance), 0: no hit (may be null)
+  int clip_on;               // clip plane: keep eye-space points p with
+  float clip_eye[4];         //   clip_eye . (p, 1) <= 0
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
 };
 

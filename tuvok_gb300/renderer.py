@@ -284,6 +284,17 @@ class Renderer:
         check(lib().tvk_read_image(self._h, out.ctypes.data_as(N._f32p), out.size))
         return out
 
+    def SetClipPlane(self, plane):
+        """AbstrRenderer::SetClipPlane: (a, b, c, d) in world space; n.x + d >= 0 is cut."""
+        pl = (C.c_float * 4)(*[float(v) for v in plane])
+        check(lib().tvk_set_clip_plane(self._h, pl))
+
+    def EnableClipPlane(self, on=True):
+        check(lib().tvk_enable_clip_plane(self._h, int(bool(on))))
+
+    def DisableClipPlane(self):
+        self.EnableClipPlane(False)
+
     def SetLOD(self, lod):
         """m_iCurrentLOD for Paint()."""
         check(lib().tvk_set_lod(self._h, int(lod)))
