@@ -757,10 +757,15 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   }
 }
 
+// Rays per thread of the single-frame kernel (tiles of 16 x TVK_RAYCAST_RPT by 8 pixels).
+#ifndef TVK_RAYCAST_RPT
+#define TVK_RAYCAST_RPT 1
+#endif
+
 template <class T, bool kIso>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
   __shared__ TileShared sh;
-  render_tile<T, kIso, 1>(P, blockIdx.x, blockIdx.y, sh);
+  render_tile<T, kIso, TVK_RAYCAST_RPT>(P, blockIdx.x, blockIdx.y, sh);
 }
 
 // Many frames in one persistent launch (the reference renders render regions
@@ -1422,7 +1427,8 @@ void launch_leaper(const LeaperParams& p, cudaStream_t s, uint64_t* launches) {
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 block(128);
-  const dim3 grid((p.out_w + 15) / 16, (p.out_h + 7) / 8);
+  const uint32_t tw = 16 * TVK_RAYCAST_RPT;
+  const dim3 grid((p.out_w + tw - 1) / tw, (p.out_h + 7) / 8);
   const bool iso = p.mode == TVK_RM_ISOSURFACE;
   if (p.bytes == 1) {
     if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);
