@@ -478,6 +478,34 @@ tvk_status tvk_cnn_prepare_input(const float* image_rgba, const float* depth, in
 tvk_status tvk_set_clip_plane(tvk_renderer* r, const float plane[4]);
 tvk_status tvk_enable_clip_plane(tvk_renderer* r, int on);
 
+/* ClearView (AbstrRenderer::SetCV, AbstrRenderer.cpp:1247-1256; its state
+ * :130-136, 171).  In iso mode with ClearView on, tvk_paint marches a second,
+ * "focus" isosurface at the ClearView isovalue behind the "context" surface
+ * (GLRaycaster-ISO-CV-FS.glsl, driven by GLRaycaster.cpp:421-436) and shades
+ * both with Compose-CV-FS.glsl: the context surface fades out near the focus
+ * point and where its normals vary little, revealing the focus surface.
+ * The isovalue is in data units like tvk_set_isovalue (normalised as
+ * GetNormalizedCVIsovalue, AbstrRenderer.cpp:426-438); it starts at 1.5x the
+ * isovalue when a volume is set (AbstrRenderer.cpp:261).  Colour, size,
+ * context scale and border scale are SetCVColor / SetCVSize /
+ * SetCVContextScale / SetCVBorderScale (AbstrRenderer.cpp:1316-1347; defaults
+ * (1,0,0), 5.5, 1, 60).  The focus position is model space, w = 1
+ * (SetCVFocusPosFVec, :1349-1352; default (0, 0, 0.5, 1));
+ * tvk_set_cv_focus_pixel picks it from the context hit of the last ClearView
+ * frame at a pixel of the ray-marched image (row 0 at the bottom), or moves it
+ * far away (w = 0) where that pixel has no hit (GLRenderer::CVFocusHasChanged,
+ * GLRenderer.cpp:2833-2854).  Batches and tvk_paint_learned refuse a ClearView
+ * renderer in iso mode; tvk_leaper_paint renders without ClearView
+ * (GLGridLeaper::SupportsClearView is false). */
+tvk_status tvk_set_clearview(tvk_renderer* r, int on);
+tvk_status tvk_set_cv_isovalue(tvk_renderer* r, float isovalue);
+tvk_status tvk_set_cv_color(tvk_renderer* r, const float rgb[3]);
+tvk_status tvk_set_cv_params(tvk_renderer* r, float size, float context_scale,
+                             float border_scale);
+tvk_status tvk_set_cv_focus_pos(tvk_renderer* r, const float pos[4]);
+tvk_status tvk_get_cv_focus_pos(const tvk_renderer* r, float pos[4]);
+tvk_status tvk_set_cv_focus_pixel(tvk_renderer* r, uint32_t x, uint32_t y);
+
 /* First-hit depth of the ray-marched pixels: with `on`, every paint also
  * writes 1 / (1 + t) per pixel of the ray-marched image (render size), t the
  * eye-space distance of the first sample that adds anything (the iso hit in

@@ -187,6 +187,16 @@ class Renderer {
   void SetClipPlane(const float plane[4]) { check(tvk_set_clip_plane(r_, plane)); }
   void EnableClipPlane() { check(tvk_enable_clip_plane(r_, 1)); }
   void DisableClipPlane() { check(tvk_enable_clip_plane(r_, 0)); }
+  // AbstrRenderer::SetCV, SetCVIsoValue, SetCVColor, SetCVSize /
+  // SetCVContextScale / SetCVBorderScale, SetCVFocusPosFVec, SetCVFocusPos
+  void SetCV(bool enable) { check(tvk_set_clearview(r_, enable ? 1 : 0)); }
+  void SetCVIsoValue(float isovalue) { check(tvk_set_cv_isovalue(r_, isovalue)); }
+  void SetCVColor(const float rgb[3]) { check(tvk_set_cv_color(r_, rgb)); }
+  void SetCVParams(float size, float context_scale, float border_scale) {
+    check(tvk_set_cv_params(r_, size, context_scale, border_scale));
+  }
+  void SetCVFocusPosFVec(const float pos[4]) { check(tvk_set_cv_focus_pos(r_, pos)); }
+  void SetCVFocusPos(uint32_t x, uint32_t y) { check(tvk_set_cv_focus_pixel(r_, x, y)); }
   // m_iCurrentLOD, decreaseScreenResNow / decreaseSamplingRateNow
   void SetLOD(uint32_t lod) { check(tvk_set_lod(r_, lod)); }
   void SetReducedQuality(bool screen, bool sampling) {

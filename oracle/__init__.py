@@ -36,6 +36,9 @@ class Scene(C.Structure):
         ("lod", C.c_uint32), ("median", C.c_int), ("decrease_screen_res", C.c_int),
         ("decrease_sampling_rate", C.c_int), ("screen_res_dec_factor", C.c_float),
         ("sample_dec_factor", C.c_float), ("clip_on", C.c_int), ("clip_plane", C.c_float * 4),
+        ("cv_on", C.c_int), ("cv_isovalue", C.c_float), ("cv_color", C.c_float * 3),
+        ("cv_size", C.c_float), ("cv_context_scale", C.c_float), ("cv_border_scale", C.c_float),
+        ("cv_pos", C.c_float * 4),
     ]
 
 
@@ -241,8 +244,13 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
                light_dir=(0, 0, -1), bp=(0.2, 0.6, 0.2, 32.0), frame_ert=1.0,
                use_double=False, row_stride=1, row_phase=0, threads=0, isovalue=None,
                iso_color=(0.5, 0.5, 0.5), lod=0, median=False, dec_screen=False,
-               dec_sampling=False, screen_dec=2.0, sample_dec=2.0, clip_plane=None):
-    """Scene struct for the oracle; returns (scene, arrays that must stay alive)."""
+               dec_sampling=False, screen_dec=2.0, sample_dec=2.0, clip_plane=None,
+               clearview=None):
+    """Scene struct for the oracle; returns (scene, arrays that must stay alive).
+
+    clearview: None, or a dict with any of isovalue (default 1.5 x the
+    isovalue), color, size, context_scale, border_scale, pos (model space,
+    4 components) -- the AbstrRenderer ClearView state."""
     raw = np.ascontiguousarray(raw)
     tf = np.ascontiguousarray(np.asarray(tf, dtype=np.float32))
     s = Scene()
@@ -280,14 +288,26 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
     s.decrease_screen_res, s.decrease_sampling_rate = int(dec_screen), int(dec_sampling)
     s.screen_res_dec_factor, s.sample_dec_factor = screen_dec, sample_dec
     s.threads = threads
+    # AbstrRenderer.cpp:252-261: half the data range once a dataset is loaded,
+    # the ClearView isovalue half as much again above that
+    default_iso = np.float32(float(raw.max()) - float(raw.min())) / np.float32(2.0)
     if isovalue is None:
-        # AbstrRenderer.cpp:252-259: half the data range once a dataset is loaded
-        isovalue = float(np.float32(float(raw.max()) - float(raw.min())) / np.float32(2.0))
+        isovalue = float(default_iso)
     s.isovalue = isovalue
     s.iso_color[:] = iso_color
     if clip_plane is not None:
         s.clip_on = 1
         s.clip_plane[:] = [float(x) for x in clip_plane]
+    if clearview is not None:
+        cv = dict(clearview)
+        s.cv_on = 1
+        s.cv_isovalue = cv.get("isovalue",
+                               float(default_iso + default_iso / np.float32(2.0)))
+        s.cv_color[:] = cv.get("color", (1.0, 0.0, 0.0))
+        s.cv_size = cv.get("size", 5.5)
+        s.cv_context_scale = cv.get("context_scale", 1.0)
+        s.cv_border_scale = cv.get("border_scale", 60.0)
+        s.cv_pos[:] = cv.get("pos", (0.0, 0.0, 0.5, 1.0))
     return s, (raw, tf)
 
 

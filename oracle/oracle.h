@@ -165,6 +165,15 @@ typedef struct orc_scene {
    * are cut away (PLANE::clip, Basics/Vectors.h:1455-1457) */
   int clip_on;
   float clip_plane[4];
+  /* ClearView in iso mode (AbstrRenderer SetCV and its m_fCVIsovalue,
+   * m_vCVColor, m_fCVSize, m_fCVContextScale, m_fCVBorderScale, m_vCVPos):
+   * the focus isosurface behind the context surface, composed by
+   * Compose-CV-FS.glsl.  cv_pos is model space (w = 0: a direction) */
+  int cv_on;
+  float cv_isovalue;        /* data units */
+  float cv_color[3];
+  float cv_size, cv_context_scale, cv_border_scale;
+  float cv_pos[4];
 } orc_scene;
 
 /* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row

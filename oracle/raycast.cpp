@@ -188,6 +188,12 @@ struct Setup {
   float light_a[3], light_d[3], light_s[3];
   float domain_scale[3];
   double norm_mat[3][3];
+  // ClearView: focus isovalue, diffuse colour and the focus point in eye
+  // space; per-pixel hit records (context pos + parameter, normal, focus pos +
+  // parameter, normal) and the size of the target the frame is drawn into
+  float cv_iso_norm = 0.0f, cv_diffuse[3] = {0, 0, 0}, cv_pick[3] = {0, 0, 0};
+  double* cv_rec = nullptr;
+  uint32_t fbo_w = 0, fbo_h = 0;
   // clip plane: model-space plane and its eye-space form, bricks wholly cut away
   float clip_model[4], clip_eye[4];
   std::vector<char> clipped;
@@ -387,9 +393,16 @@ void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_i
 // RefineIsosurface.glsl:37-52 (5 bisection steps from half a step back), the
 // eye-space hit interpolated by |hit - entry| / |exit - entry| in texture
 // space, its non-linear depth and the normal (Volume3D.glsl:56-60).
-template <class T>
+// kCV: GLRaycaster-ISO-CV-FS.glsl:56-115, the ClearView focus pass at
+// isovalue iso_cv: the texture-space entry moves to parameter p_start
+// (GLSL: entryTex * (1 - p) + exitTex * p) while the eye-space entry stays
+// (the shader blends vRayEntry with itself), so the step count and the
+// eye-space interpolation use the whole brick; the depth written is the ray
+// exit's (gl_FragDepth from vEyePos).
+template <class T, bool kCV = false>
 bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in, float t_out,
-               T hit_eye[3], T& fpar, T nrm[3], T& depth, uint64_t& samples) {
+               T hit_eye[3], T& fpar, T nrm[3], T& depth, uint64_t& samples,
+               float iso_cv = 0.0f, T p_start = T(0)) {
   const orc_scene& s = *st.s;
   Vol<T> vol{&b, s.dtype, T(s.dtype == 0 ? 1.0f / 255.0f : 1.0f / 65535.0f)};
   float en[3], ex[3];
@@ -404,6 +417,9 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
     tin[a] = affine_row<float>(b.tex[a], en[0], en[1], en[2]);
     tout[a] = affine_row<float>(b.tex[a], ex[0], ex[1], ex[2]);
   }
+  if (kCV)
+    for (int a = 0; a < 3; ++a)
+      tin[a] = float(T(tin[a]) * (T(1) - p_start) + T(tout[a]) * p_start);
   const T len_tex = len3(T(tout[0] - tin[0]), T(tout[1] - tin[1]), T(tout[2] - tin[2]));
   const float q = len / b.step;
   if (!(q < 1.0e6f)) return false;
@@ -413,7 +429,7 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
     inc[a] = T(tout[a] - tin[a]) / T(q);
     pos[a] = T(tin[a]);
   }
-  const T iso = T(st.iso_norm);
+  const T iso = T(kCV ? iso_cv : st.iso_norm);
   bool hit = false;
   for (int i = 0; i < n; ++i) {
     ++samples;
@@ -433,7 +449,7 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
   }
   fpar = len3(cur[0] - T(tin[0]), cur[1] - T(tin[1]), cur[2] - T(tin[2])) / len_tex;
   for (int a = 0; a < 3; ++a) hit_eye[a] = T(en[a]) * (T(1) - fpar) + T(ex[a]) * fpar;
-  depth = T(st.proj_x) + (T(st.proj_y) / -hit_eye[2]);
+  depth = T(st.proj_x) + (T(st.proj_y) / -(kCV ? T(ex[2]) : hit_eye[2]));
   // normal at the refined position
   const T vs[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
   const T xp = vol.sample(cur[0] + vs[0], cur[1], cur[2]);
@@ -455,9 +471,20 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
 }
 
 // Compose-FS.glsl:40-63 Lighting of the nearest hit (N.z made non-negative;
-// diffuse from |N . -L|, specular exponent 8).
+// diffuse from |N . -L|, specular exponent 8), with the diffuse colour
+// `diffuse` (Compose-CV-FS.glsl:48-56 is the same function).
+template <class T>
+void surface_lighting(const Setup& st, const T pos[3], const T nin[3], const float diffuse[3],
+                      T out[3]);
+
 template <class T>
 void iso_compose(const Setup& st, const T pos[3], const T nin[3], T out[3]) {
+  surface_lighting<T>(st, pos, nin, st.iso_diffuse, out);
+}
+
+template <class T>
+void surface_lighting(const Setup& st, const T pos[3], const T nin[3], const float diffuse[3],
+                      T out[3]) {
   const T N[3] = {nin[0], nin[1], std::fabs(nin[2])};
   T p[3] = {T(0) - pos[0], T(0) - pos[1], T(0) - pos[2]};
   const T lp = len3(p[0], p[1], p[2]);
@@ -472,7 +499,7 @@ void iso_compose(const Setup& st, const T pos[3], const T nin[3], T out[3]) {
   const T diff = std::fmax(std::fabs(dot3(N, nL)), T(0));
   const T spec = pow_int_or_real(std::fmax(dot3(R, L), T(0)), 8.0f);
   for (int i = 0; i < 3; ++i) {
-    T c = T(st.light_a[i]) + T(st.iso_diffuse[i]) * diff;
+    T c = T(st.light_a[i]) + T(diffuse[i]) * diff;
     c = c + T(st.light_s[i]) * spec;
     out[i] = std::fmin(std::fmax(c, T(0)), T(1));
   }
@@ -523,7 +550,47 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
   });
   T frame[4] = {0, 0, 0, 0};
   const uint64_t before = samples;
-  if (s.render_mode == ORC_RM_ISO) {
+  if (s.render_mode == ORC_RM_ISO && s.cv_on) {
+    // ClearView (GLRaycaster.cpp:421-436): per brick, in list order, the
+    // context pass into m_pFBOIsoHit (depth test on the hit depth; normal.w =
+    // the brick's tile ID), then the focus pass into m_pFBOCVHit, which starts
+    // at the context hit when the hit buffer's tile ID is this brick's (the
+    // cleared buffer reads tile 0 with parameter 0, a start at the entry).
+    T best_depth = T(1), pos[3] = {0, 0, 0}, nrm[3] = {0, 0, 0}, fpar = 0;
+    T cv_depth = T(1), pos2[3] = {0, 0, 0}, nrm2[3] = {0, 0, 0}, fpar2 = 0;
+    bool any = false, any2 = false;
+    int last_tile = 0;
+    for (const Hit& h : hits) {
+      T hp[3], hn[3], f, depth;
+      if (iso_brick<T>(st, st.bricks[h.b], dir, h.t0, h.t1, hp, f, hn, depth, samples) &&
+          depth < best_depth) {
+        best_depth = depth;
+        for (int a = 0; a < 3; ++a) { pos[a] = hp[a]; nrm[a] = hn[a]; }
+        fpar = f;
+        any = true;
+        last_tile = h.b;
+      }
+      const T p_start = (last_tile == h.b) ? fpar : T(0);
+      if (iso_brick<T, true>(st, st.bricks[h.b], dir, h.t0, h.t1, hp, f, hn, depth, samples,
+                             st.cv_iso_norm, p_start) &&
+          depth < cv_depth) {
+        cv_depth = depth;
+        for (int a = 0; a < 3; ++a) { pos2[a] = hp[a]; nrm2[a] = hn[a]; }
+        fpar2 = f;
+        any2 = true;
+      }
+    }
+    double* rec = st.cv_rec + 16 * (size_t(py) * s.width + px);
+    for (int k = 0; k < 16; ++k) rec[k] = 0.0;
+    if (any) {
+      for (int a = 0; a < 3; ++a) { rec[a] = double(pos[a]); rec[4 + a] = double(nrm[a]); }
+      rec[3] = double(fpar);
+    }
+    if (any2) {
+      for (int a = 0; a < 3; ++a) { rec[8 + a] = double(pos2[a]); rec[12 + a] = double(nrm2[a]); }
+      rec[11] = double(fpar2);
+    }
+  } else if (s.render_mode == ORC_RM_ISO) {
     // every brick writes its refined hit through a depth test (DF_LESS on a
     // buffer cleared to 1, GLRenderer.cpp:140-141, GLRaycaster.cpp:423-433)
     T best_depth = T(1), pos[3] = {0, 0, 0}, nrm[3] = {0, 0, 0}, fpar = 0;
@@ -668,6 +735,9 @@ Setup build_setup(const orc_scene& s) {
   }
   // AbstrRenderer.cpp:412-424: fIsoval = isovalue / 2^bits (not 2^bits - 1)
   st.iso_norm = float(double(s.isovalue) / double(1u << (8 * bytes)));
+  // AbstrRenderer.cpp:426-438 GetNormalizedCVIsovalue; GLRenderer.cpp:2784
+  st.cv_iso_norm = float(double(s.cv_isovalue) / double(1u << (8 * bytes)));
+  for (int a = 0; a < 3; ++a) st.cv_diffuse[a] = st.light_d[a] * s.cv_color[a];
   // CullingLOD.cpp:69-72
   st.proj_x = s.zfar / (s.zfar - s.znear);
   st.proj_y = (s.zfar * s.znear / (s.znear - s.zfar));
@@ -727,6 +797,12 @@ void apply_view(Setup& st) {
   st.view = make_view(*st.s);
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) st.norm_mat[r][c] = st.view.mv[r][c];
+  // GLRenderer.cpp:2789: vCVPickPos = m_vCVPos * modelView
+  for (int r = 0; r < 3; ++r) {
+    double e = 0;
+    for (int j = 0; j < 4; ++j) e += st.view.mv[r][j] * double(st.s->cv_pos[j]);
+    st.cv_pick[r] = float(e);
+  }
   st.clipped.assign(st.bricks.size(), 0);
   if (st.s->clip_on) {
     clip_model_plane(st.s->clip_plane, st.clip_model);
@@ -795,9 +871,78 @@ void upscale(const float* low, uint32_t lw, uint32_t lh, float* out, uint32_t w,
 
 uint64_t march_rows(Setup& st, float* out, uint32_t* spp, double* march_s);
 
+// Compose-CV-FS.glsl:49-108 over the hit records of a w x h frame drawn at the
+// lower left of an fbo_w x fbo_h target.  The neighbour normals are GL_NEAREST
+// lookups one texel away with GL_CLAMP (GLRenderer.cpp:1793): clamped at the
+// target's edges; beyond a reduced frame's right or top edge the target holds
+// the cleared (zero) normal.
+template <class T>
+void cv_compose(const Setup& st, float* out) {
+  const orc_scene& s = *st.s;
+  const int w = int(s.width), h = int(s.height);
+  const int fw = int(st.fbo_w), fh = int(st.fbo_h);
+  auto normal_at = [&](int x, int y, T n[3]) {
+    x = std::min(std::max(x, 0), fw - 1);
+    y = std::min(std::max(y, 0), fh - 1);
+    for (int a = 0; a < 3; ++a)
+      n[a] = (x >= w || y >= h) ? T(0) : T(st.cv_rec[16 * (size_t(y) * w + x) + 4 + a]);
+  };
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const double* rec = st.cv_rec + 16 * (size_t(y) * w + x);
+      float* o = out + 4 * (size_t(y) * w + x);
+      if (T(rec[3]) == T(0)) {  // no context hit: discard (the frame stays cleared)
+        for (int c = 0; c < 4; ++c) o[c] = 0.0f;
+        continue;
+      }
+      const T pos[3] = {T(rec[0]), T(rec[1]), T(rec[2])};
+      const T n[3] = {T(rec[4]), T(rec[5]), T(rec[6])};
+      T ctx[4];
+      surface_lighting<T>(st, pos, n, st.iso_diffuse, ctx);
+      ctx[3] = T(1);
+      // curvature estimate: |n(+x) - n| + |n(-x) - n| + |n(+y) - n| + |n(-y) - n|
+      T nb[4][3];
+      normal_at(x + 1, y, nb[0]);
+      normal_at(x - 1, y, nb[1]);
+      normal_at(x, y + 1, nb[2]);
+      normal_at(x, y - 1, nb[3]);
+      T acc[3];
+      for (int a = 0; a < 3; ++a) {
+        acc[a] = std::fabs(nb[0][a] - n[a]);
+        for (int k = 1; k < 4; ++k) acc[a] = acc[a] + std::fabs(nb[k][a] - n[a]);
+      }
+      const T curvature = len3(acc[0], acc[1], acc[2]);
+      const T dist_w = len3(pos[0] - T(st.cv_pick[0]), pos[1] - T(st.cv_pick[1]),
+                            pos[2] - T(st.cv_pick[2])) * T(s.cv_size);
+      const T blend = std::fmin(
+          std::fmax(std::fmax(curvature * T(s.cv_context_scale),
+                              std::fmin(std::fmax(dist_w, T(0)), T(1))),
+                    T(0)),
+          T(1));
+      T foc[4] = {0, 0, 0, 0};
+      if (T(rec[11]) != T(0)) {
+        const T p2[3] = {T(rec[8]), T(rec[9]), T(rec[10])};
+        const T n2[3] = {T(rec[12]), T(rec[13]), T(rec[14])};
+        surface_lighting<T>(st, p2, n2, st.cv_diffuse, foc);
+        foc[3] = T(1);
+      }
+      T col[4];
+      for (int c = 0; c < 4; ++c)
+        col[c] = std::fmin(std::fmax(ctx[c] * blend + foc[c] * (T(1) - blend), T(0)), T(1));
+      const T dark = T(0.5) * (T(1) - std::fmin(std::fmax(std::fabs(dist_w - T(1)) *
+                                                              T(s.cv_border_scale),
+                                                          T(0)),
+                                                T(1)));
+      for (int c = 0; c < 3; ++c) o[c] = float(col[c] - dark);
+      o[3] = float(col[3]);
+    }
+}
+
 uint64_t march_all(Setup& st, float* out, uint32_t* spp, double* march_s) {
   uint32_t rw, rh;
   render_size(*st.s, &rw, &rh);
+  st.fbo_w = st.s->width;
+  st.fbo_h = st.s->height;
   if (rw == st.s->width && rh == st.s->height) return march_rows(st, out, spp, march_s);
   // reduced viewport: march the smaller image with its own projection, then stretch it
   const orc_scene* full = st.s;
@@ -821,6 +966,9 @@ uint64_t march_rows(Setup& st, float* out, uint32_t* spp, double* march_s) {
   const auto t1 = std::chrono::steady_clock::now();
   const uint32_t stride = s.row_stride ? s.row_stride : 1;
   uint64_t total = 0;
+  const bool cv = s.render_mode == ORC_RM_ISO && s.cv_on;
+  std::vector<double> cv_rec(cv ? size_t(s.width) * s.height * 16 : 0, 0.0);
+  st.cv_rec = cv ? cv_rec.data() : nullptr;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
   for (int64_t py = 0; py < int64_t(s.height); ++py) {
     if (uint32_t(py) % stride != s.row_phase % stride) continue;
@@ -833,6 +981,11 @@ uint64_t march_rows(Setup& st, float* out, uint32_t* spp, double* march_s) {
         render_pixel<float>(st, px, uint32_t(py), out + 4 * i, spp ? spp + i : nullptr, local);
     }
     total += local;
+  }
+  if (cv) {
+    if (s.use_double) cv_compose<double>(st, out);
+    else cv_compose<float>(st, out);
+    st.cv_rec = nullptr;
   }
   const auto t2 = std::chrono::steady_clock::now();
   if (march_s) *march_s = std::chrono::duration<double>(t2 - t1).count();

@@ -220,3 +220,28 @@ def test_oracle_clip_plane_properties():
     assert not none.any() and n3 == 0
     half, n4, _ = O.render(raw, (10, 10, 10), 1, tf, clip_plane=(1, 0, 0, 0), **kw)
     assert 0 < n4 < n
+
+
+def test_oracle_clearview_properties():
+    """The oracle's ClearView (Compose-CV-FS.glsl): with the focus point far
+    away (the picking miss, GLRenderer.cpp:2848-2850) the blend factor is 1 and
+    the border term 0, so the frame is the plain isosurface frame bit for bit;
+    the focus pass adds samples; a focus point on the surface with no
+    curvature weight reveals the focus surface (red) around it."""
+    from tuvok_gb300.workloads import numpy_blob_volume
+    raw = numpy_blob_volume((26, 22, 20), np.uint8, 5, (3, 7), (80, 255), 255, 7, 0)
+    tf = np.zeros((16, 4), dtype=np.float32)
+    kw = dict(width=40, height=32, eye=(0.4, 0.3, 1.4), mode=2, isovalue=90.0,
+              want_counts=True)
+    iso, n_iso, c_iso = O.render(raw, (10, 10, 10), 1, tf, **kw)
+    assert (iso[..., 3] > 0).mean() > 0.05
+    far = dict(isovalue=160.0, pos=(1e7, 1e7, 1e7, 0.0))
+    cv, n_cv, c_cv = O.render(raw, (10, 10, 10), 1, tf, clearview=far, **kw)
+    assert np.array_equal(cv, iso)
+    assert n_cv > n_iso and (c_cv >= c_iso).all()
+    near = dict(isovalue=160.0, pos=(0.0, 0.0, 0.0, 1.0), context_scale=0.0, size=3.0,
+                color=(1.0, 0.0, 0.0))
+    cv2, _, _ = O.render(raw, (10, 10, 10), 1, tf, clearview=near, **kw)
+    changed = np.abs(cv2 - iso).max(axis=-1) > 1e-3
+    assert changed.any() and not changed.all()
+    assert ((cv2[..., 3] == 0) == (iso[..., 3] == 0)).all()

@@ -170,6 +170,13 @@ PROTOTYPES = {
     "tvk_cnn_prepare_input": [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
     "tvk_set_clip_plane": [_vp, _f32p],
     "tvk_enable_clip_plane": [_vp, C.c_int],
+    "tvk_set_clearview": [_vp, C.c_int],
+    "tvk_set_cv_isovalue": [_vp, C.c_float],
+    "tvk_set_cv_color": [_vp, _f32p],
+    "tvk_set_cv_params": [_vp, C.c_float, C.c_float, C.c_float],
+    "tvk_set_cv_focus_pos": [_vp, _f32p],
+    "tvk_get_cv_focus_pos": [_vp, _f32p],
+    "tvk_set_cv_focus_pixel": [_vp, C.c_uint32, C.c_uint32],
     "tvk_set_depth_output": [_vp, C.c_int],
     "tvk_copy_depth_device": [_vp, _vp, C.c_size_t],
     "tvk_learned_param_count": [C.POINTER(C.c_size_t)],

@@ -574,6 +574,16 @@ struct tvk_renderer {
   bool depth_out = false;            // write the first-hit depth of ray-marched pixels
   bool clip_on = false;              // AbstrRenderer m_bClipPlaneOn
   float clip_plane[4] = {0, 0, 1, 0};  // m_ClipPlane, world space
+  // ClearView (AbstrRenderer.cpp:130-136, 171 defaults; m_fCVIsovalue follows
+  // the isovalue when a dataset is set, AbstrRenderer.cpp:261)
+  bool cv_on = false;
+  float cv_iso = 0.8f;
+  float cv_color[3] = {1, 0, 0};
+  float cv_size = 5.5f, cv_context_scale = 1.0f, cv_border_scale = 60.0f;
+  float cv_pos[4] = {0, 0, 0.5f, 1};   // m_vCVPos, model space
+  tvk::DevBuf d_cvhits;                // the last ClearView frame's hit records
+  double cv_last_inv[3][4] = {};       // its eye -> model transform (picking)
+  bool cv_painted = false;
   tvk::DevBuf d_depth;
   tvk_stats stats{};
   uint64_t launches = 0;
@@ -850,6 +860,7 @@ struct PlannedFrame {
   uint32_t rw, rh;   // ray-marched size (smaller than the viewport when reduced)
   bool upscale;
   uint64_t launches0;
+  CvComposeParams cv;  // ClearView frames (P.cv_on): the compose pass
 };
 
 // Where a planned frame's brick list and counters go: the renderer's own
@@ -1123,7 +1134,39 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   TVK_CUDA(cudaMemsetAsync(st.d_counters->p, 0, 4 * sizeof(unsigned long long), st.stream));
   R->stats.bricks_visible = nvis;
   R->stats.bricks_total = nbl;
-  return PlannedFrame{P, rw, rh, upscale, launches0};
+  CvComposeParams cv;
+  std::memset(&cv, 0, sizeof(cv));
+  if (iso_mode && R->cv_on) {
+    // GLRaycaster.cpp:571-575 (GetNormalizedCVIsovalue: isovalue / 2^bits)
+    P.cv_on = 1;
+    P.cv_iso = float(double(R->cv_iso) / double(1u << (8 * V->bytes)));
+    P.cv_cell_skip = P.cv_iso >= iso_norm ? 1 : 0;
+    R->d_cvhits.ensure(size_t(rw) * rh * 4 * sizeof(float4));
+    P.cv_hits = R->d_cvhits.as<float4>();
+    // GLRenderer.cpp:2777-2794 ComposeSurfaceImage uniforms
+    cv.hits = P.cv_hits;
+    cv.out = P.out;
+    cv.w = rw;
+    cv.h = rh;
+    cv.fbo_w = R->width;
+    cv.fbo_h = R->height;
+    for (int a = 0; a < 3; ++a) {
+      cv.light_a[a] = P.light_a[a];
+      cv.diffuse_context[a] = P.iso_diffuse[a];
+      cv.diffuse_focus[a] = (R->diffuse[a] * R->diffuse[3]) * R->cv_color[a];
+      cv.light_s[a] = P.light_s[a];
+      cv.light_dir[a] = P.light_dir[a];
+      // vCVPickPos = m_vCVPos * modelView
+      double e = 0;
+      for (int j = 0; j < 4; ++j) e += view.mv[a][j] * double(R->cv_pos[j]);
+      cv.pick[a] = float(e);
+    }
+    cv.size = R->cv_size;
+    cv.context_scale = R->cv_context_scale;
+    cv.border_scale = R->cv_border_scale;
+    std::memcpy(R->cv_last_inv, view.inv, sizeof(R->cv_last_inv));
+  }
+  return PlannedFrame{P, rw, rh, upscale, launches0, cv};
 }
 
 // GLRenderer.cpp:717-747 CopyOverCompletedRegion: the reduced image is
@@ -1151,6 +1194,8 @@ void paint(tvk_renderer* R, const Subframe& sf) {
   const PlannedFrame F = plan_frame(R, sf);
   TVK_CUDA(cudaEventRecord(R->ev_start, R->stream));
   launch_raycast(F.P, R->stream, &R->launches);
+  if (F.P.cv_on) launch_cv_compose(F.cv, R->stream, &R->launches);
+  R->cv_painted = F.P.cv_on != 0;
   launch_upscale_of(R, F, R->stream, &R->launches);
   TVK_CUDA(cudaEventRecord(R->ev_stop, R->stream));
   finish_frame(R, F);
@@ -1326,6 +1371,8 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
       fail(TVK_ERR_INVALID_ARG, "every renderer of a batch must be on the batch's device");
     for (uint32_t j = 0; j < i; ++j)
       if (rs[j] == rs[i]) fail(TVK_ERR_INVALID_ARG, "a renderer appears twice in the batch");
+    if (rs[i]->cv_on && rs[i]->mode == TVK_RM_ISOSURFACE)
+      fail(TVK_ERR_UNSUPPORTED, "ClearView frames are painted one at a time (tvk_paint)");
   }
   // plan every frame on its renderer's stream, then order the batch stream after them
   std::vector<PlannedFrame> F;
@@ -1582,6 +1629,8 @@ void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int o
 // the frame falls back to the plain full-quality render.
 void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_learned_info* info) {
   if (R->device != N->device) fail(TVK_ERR_INVALID_ARG, "renderer and network on other devices");
+  if (R->cv_on && R->mode == TVK_RM_ISOSURFACE)
+    fail(TVK_ERR_UNSUPPORTED, "the learned reconstruction does not take ClearView frames");
   TVK_CUDA(cudaSetDevice(R->device));
   cudaStream_t s = R->stream;
   TVK_CUDA(cudaEventRecord(N->ev[0], s));
@@ -2317,8 +2366,12 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
           break;
         }
     }
-    // AbstrRenderer.cpp:252-259: the isovalue starts at half the data range
-    if (v) r->isovalue = float(v->range_max - v->range_min) / 2.0f;
+    // AbstrRenderer.cpp:252-261: the isovalue starts at half the data range,
+    // the ClearView isovalue half as much again above it
+    if (v) {
+      r->isovalue = float(v->range_max - v->range_min) / 2.0f;
+      r->cv_iso = r->isovalue + (r->isovalue / 2.0f);
+    }
   });
 }
 
@@ -2732,6 +2785,83 @@ tvk_status tvk_enable_clip_plane(tvk_renderer* r, int on) {
   return guarded([&] {
     REQUIRE(r, "null argument");
     r->clip_on = on != 0;
+  });
+}
+
+tvk_status tvk_set_clearview(tvk_renderer* r, int on) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    r->cv_on = on != 0;
+  });
+}
+
+tvk_status tvk_set_cv_isovalue(tvk_renderer* r, float isovalue) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    REQUIRE(std::isfinite(isovalue), "isovalue must be finite");
+    r->cv_iso = isovalue;
+  });
+}
+
+tvk_status tvk_set_cv_color(tvk_renderer* r, const float rgb[3]) {
+  return guarded([&] {
+    REQUIRE(r && rgb, "null argument");
+    for (int a = 0; a < 3; ++a) r->cv_color[a] = rgb[a];
+  });
+}
+
+tvk_status tvk_set_cv_params(tvk_renderer* r, float size, float context_scale,
+                             float border_scale) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    REQUIRE(std::isfinite(size) && std::isfinite(context_scale) && std::isfinite(border_scale),
+            "ClearView parameters must be finite");
+    r->cv_size = size;
+    r->cv_context_scale = context_scale;
+    r->cv_border_scale = border_scale;
+  });
+}
+
+tvk_status tvk_set_cv_focus_pos(tvk_renderer* r, const float pos[4]) {
+  return guarded([&] {
+    REQUIRE(r && pos, "null argument");
+    for (int a = 0; a < 4; ++a) r->cv_pos[a] = pos[a];
+  });
+}
+
+tvk_status tvk_get_cv_focus_pos(const tvk_renderer* r, float pos[4]) {
+  return guarded([&] {
+    REQUIRE(r && pos, "null argument");
+    for (int a = 0; a < 4; ++a) pos[a] = r->cv_pos[a];
+  });
+}
+
+// GLRenderer::CVFocusHasChanged (GLRenderer.cpp:2833-2854): the context hit
+// of the last ClearView frame at pixel (x, y) (row 0 at the bottom), moved to
+// model space; a pixel without a hit moves the focus far away (w = 0).
+tvk_status tvk_set_cv_focus_pixel(tvk_renderer* r, uint32_t x, uint32_t y) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    if (!r->cv_painted) tvk::fail(TVK_ERR_STATE, "no ClearView frame painted yet");
+    TVK_CUDA(cudaSetDevice(r->device));
+    float hit[4] = {0, 0, 0, 0};
+    if (x < r->render_w && y < r->render_h) {
+      TVK_CUDA(cudaStreamSynchronize(r->stream));
+      const size_t pix = size_t(y) * r->render_w + x;
+      TVK_CUDA(cudaMemcpy(hit, r->d_cvhits.as<float4>() + 4 * pix, sizeof(hit),
+                          cudaMemcpyDeviceToHost));
+    }
+    if (hit[3] != 0.0f) {
+      for (int a = 0; a < 3; ++a) {
+        double m = r->cv_last_inv[a][3];
+        for (int j = 0; j < 3; ++j) m += r->cv_last_inv[a][j] * double(hit[j]);
+        r->cv_pos[a] = float(m);
+      }
+      r->cv_pos[3] = 1.0f;
+    } else {
+      r->cv_pos[0] = r->cv_pos[1] = r->cv_pos[2] = 10000000.0f;
+      r->cv_pos[3] = 0.0f;
+    }
   });
 }
 

@@ -416,10 +416,19 @@ struct IsoHit {
   float depth;
 };
 
-template <class T>
+//
+// kCV: the focus-surface pass of GLRaycaster-ISO-CV-FS.glsl:56-115 with
+// isovalue `iso_cv`.  Its texture-space entry moves to the parameter p_start of
+// the brick (the context hit, when that hit lies in this brick); the eye-space
+// entry does not move (the shader blends vRayEntry with itself), so the step
+// count and the eye-space hit interpolation keep the whole brick's entry.  The
+// hit's depth (of the brick's exit) is not computed: along a ray the first
+// brick with a focus hit wins the depth test.
+template <class T, bool kCV = false>
 __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick& b,
                                           const float dir[3], float t_in, float t_out,
-                                          IsoHit& h, uint32_t& samples, uint32_t& shaded) {
+                                          IsoHit& h, uint32_t& samples, uint32_t& shaded,
+                                          float iso_cv = 0.0f, float p_start = 0.0f) {
   float en[3], ex[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -433,6 +442,10 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
   for (int a = 0; a < 3; ++a) {
     tin[a] = affine_row(b.tex[a], en[0], en[1], en[2]);
     tout[a] = affine_row(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  if (kCV) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) tin[a] = tin[a] * (1.0f - p_start) + tout[a] * p_start;
   }
   const float len_tex = len3(tout[0] - tin[0], tout[1] - tin[1], tout[2] - tin[2]);
   const float q = len / b.step;
@@ -450,9 +463,10 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
   vol.fn0 = float(b.n[0]); vol.fn1 = float(b.n[1]); vol.fn2 = float(b.n[2]);
   vol.sx = b.n[0]; vol.sxy = b.n[0] * b.n[1];
   const float im = P.inv_max_raw;
-  const float iso = P.iso_norm;
+  const float iso = kCV ? iso_cv : P.iso_norm;
   // cells whose maximum stays below the isovalue cannot produce a hit
-  const uint8_t* __restrict__ dist = P.cell_dist ? P.cell_dist + b.cell_off : nullptr;
+  const uint8_t* __restrict__ dist =
+      (P.cell_dist && (!kCV || P.cv_cell_skip)) ? P.cell_dist + b.cell_off : nullptr;
   const int ncx = int(b.cells & 1023u), ncy = int((b.cells >> 10) & 1023u),
             ncz = int(b.cells >> 20);
   const float du0 = inc[0] * vol.fn0, du1 = inc[1] * vol.fn1, du2 = inc[2] * vol.fn2;
@@ -520,7 +534,7 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
   h.f = len3(cur[0] - tin[0], cur[1] - tin[1], cur[2] - tin[2]) / len_tex;
 #pragma unroll
   for (int a = 0; a < 3; ++a) h.pos[a] = en[a] * (1.0f - h.f) + ex[a] * h.f;
-  h.depth = P.proj_x + (P.proj_y / -h.pos[2]);
+  h.depth = kCV ? 0.0f : P.proj_x + (P.proj_y / -h.pos[2]);
   const float vs0 = 1.0f / float(b.n[0]), vs1 = 1.0f / float(b.n[1]), vs2 = 1.0f / float(b.n[2]);
   const float xp = vol.sample_raw(cur[0] + vs0, cur[1], cur[2]) * im;
   const float xm = vol.sample_raw(cur[0] + (-vs0), cur[1], cur[2]) * im;
@@ -537,6 +551,32 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
   const float l = len3(h.n[0], h.n[1], h.n[2]);
   if (l > 0.0f) { h.n[0] = h.n[0] / l; h.n[1] = h.n[1] / l; h.n[2] = h.n[2] / l; }
   return true;
+}
+
+// Lighting of Compose-FS.glsl:40-48 (and Compose-CV-FS.glsl:48-56) at the
+// eye-space position pos with normal n: N.z made non-negative, diffuse from
+// |N . -L|, specular exponent 8, clamped to [0, 1].
+__device__ __forceinline__ void surface_lighting(const float pos[3], const float n[3],
+                                                 const float* light_a, const float* diffuse,
+                                                 const float* light_s, const float* L,
+                                                 float c[3]) {
+  const float N0 = n[0], N1 = n[1], N2 = fabsf(n[2]);
+  const float p0 = 0.0f - pos[0], p1 = 0.0f - pos[1], p2 = 0.0f - pos[2];
+  const float lp = len3(p0, p1, p2);
+  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  const float d = (N0 * V0 + N1 * V1) + N2 * V2;
+  float R0 = V0 - (2.0f * d) * N0, R1 = V1 - (2.0f * d) * N1, R2 = V2 - (2.0f * d) * N2;
+  const float lr = len3(R0, R1, R2);
+  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+  const float nl0 = -L[0], nl1 = -L[1], nl2 = -L[2];
+  const float diff = fmaxf(fabsf((N0 * nl0 + N1 * nl1) + N2 * nl2), 0.0f);
+  const float spec = pow_int_or_real(fmaxf((R0 * L[0] + R1 * L[1]) + R2 * L[2], 0.0f), 8.0f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float x = light_a[i] + diffuse[i] * diff;
+    x = x + light_s[i] * spec;
+    c[i] = fminf(fmaxf(x, 0.0f), 1.0f);
+  }
 }
 
 // Compose-FS.glsl:40-63: lighting of the nearest hit.
@@ -605,8 +645,9 @@ struct TileShared {
 // describes; all 128 threads of the CTA take part, each marching kRPT rays
 // one after the other (pixel columns 16 r + ...).  kIso: isosurface mode
 // (nearest refined hit + compose); otherwise the compositing modes (1D/2D TF,
-// lit or unlit).  Every pixel's value does not depend on kRPT.
-template <class T, bool kIso, int kRPT>
+// lit or unlit).  Every pixel's value does not depend on kRPT.  kCV (with
+// kIso): ClearView, both surfaces' hits go to P.cv_hits for cv_compose.
+template <class T, bool kIso, int kRPT, bool kCV = false>
 __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, uint32_t by,
                                             TileShared& sh) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -628,6 +669,8 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
   IsoHit best[kRPT];
   float best_depth[kRPT];  // depth buffer cleared to 1, test DF_LESS
   bool have_hit[kRPT];
+  IsoHit focus[kRPT];      // ClearView: the focus surface's hit
+  bool have_focus[kRPT];
 #pragma unroll
   for (int r = 0; r < kRPT; ++r) {
     frame[r] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -635,6 +678,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
     ray_samples[r] = 0;
     best_depth[r] = 1.0f;
     have_hit[r] = false;
+    have_focus[r] = false;
   }
   for (uint32_t base = 0; base < P.n_bricks; base += kCandChunk) {
     const uint32_t end = min(P.n_bricks, base + kCandChunk);
@@ -705,13 +749,37 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           // A later brick's hit lies beyond its (RGBA16F-rounded) entry, so
           // once that entry is behind the nearest hit it cannot pass the
           // depth test; bricks come in increasing entry order along the ray.
-          if (have_hit[r] && ti * (1.0f - 2e-3f) - 1e-4f > -best[r].pos[2]) break;
-          IsoHit h;
-          if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
-            best[r] = h;
-            best_depth[r] = h.depth;
-            have_hit[r] = true;
+          const bool settled = have_hit[r] && ti * (1.0f - 2e-3f) - 1e-4f > -best[r].pos[2];
+          if (!kCV) {
+            if (settled) break;
+            IsoHit h;
+            if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
+              best[r] = h;
+              best_depth[r] = h.depth;
+              have_hit[r] = true;
+            }
+            continue;
           }
+          // ClearView (GLRaycaster.cpp:421-436): per brick the context pass,
+          // then the focus pass, which starts at the context hit when the
+          // nearest context hit so far is this brick's (its tile ID).  The
+          // focus pass writes the brick's exit depth, so the first brick
+          // along the ray with a focus hit keeps it.
+          if (settled && have_focus[r]) break;
+          bool here = false;
+          if (!settled) {
+            IsoHit h;
+            if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
+              best[r] = h;
+              best_depth[r] = h.depth;
+              have_hit[r] = true;
+              here = true;
+            }
+          }
+          if (!have_focus[r] &&
+              iso_brick<T, true>(P, b, dir, ti, tc, focus[r], samples, shaded, P.cv_iso,
+                                 here ? best[r].f : 0.0f))
+            have_focus[r] = true;
           continue;
         }
         const float4 col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
@@ -735,12 +803,24 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
     // 0, leaves the pixel empty
     float4 out = frame[r];
     if (iso_mode && have_hit[r] && best[r].f != 0.0f) {
-      out = iso_compose(P, best[r]);
+      if (!kCV) out = iso_compose(P, best[r]);
       first_t[r] = -best[r].pos[2];
     }
     if (active) {
       const size_t pix = size_t(py) * P.out_w + px;
-      P.out[pix] = out;
+      if (kCV) {
+        // the two hit buffers of GLRenderer (m_pFBOIsoHit, m_pFBOCVHit):
+        // position + interpolation parameter, normal; cleared to zero
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4* H = P.cv_hits + 4 * pix;
+        H[0] = have_hit[r] ? make_float4(best[r].pos[0], best[r].pos[1], best[r].pos[2], best[r].f) : z;
+        H[1] = have_hit[r] ? make_float4(best[r].n[0], best[r].n[1], best[r].n[2], 0.f) : z;
+        H[2] = have_focus[r] ? make_float4(focus[r].pos[0], focus[r].pos[1], focus[r].pos[2],
+                                           focus[r].f) : z;
+        H[3] = have_focus[r] ? make_float4(focus[r].n[0], focus[r].n[1], focus[r].n[2], 0.f) : z;
+      } else {
+        P.out[pix] = out;
+      }
       if (P.spp) P.spp[pix] = ray_samples[r];
       if (P.depth) P.depth[pix] = first_t[r] == INFINITY ? 0.0f : 1.0f / (1.0f + first_t[r]);
     }
@@ -762,10 +842,65 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
 #define TVK_RAYCAST_RPT 1
 #endif
 
-template <class T, bool kIso>
+template <class T, bool kIso, bool kCV = false>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
   __shared__ TileShared sh;
-  render_tile<T, kIso, TVK_RAYCAST_RPT>(P, blockIdx.x, blockIdx.y, sh);
+  render_tile<T, kIso, TVK_RAYCAST_RPT, kCV>(P, blockIdx.x, blockIdx.y, sh);
+}
+
+// Compose-CV-FS.glsl:49-108, one thread per pixel.  Neighbour normals are
+// read as the shader's GL_NEAREST / GL_CLAMP lookups one texel away in a
+// target of fbo_w x fbo_h: clamped at the target's edges, zero (the cleared
+// buffer) beyond a reduced frame's right and top edges inside the target.
+__global__ void cv_compose_kernel(const CvComposeParams C) {
+  const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= C.w || y >= C.h) return;
+  const size_t pix = size_t(y) * C.w + x;
+  const float4 hp = C.hits[4 * pix];
+  if (hp.w == 0.0f) {
+    C.out[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float4 hn = C.hits[4 * pix + 1];
+  const float pos[3] = {hp.x, hp.y, hp.z}, n[3] = {hn.x, hn.y, hn.z};
+  float ctx[3];
+  surface_lighting(pos, n, C.light_a, C.diffuse_context, C.light_s, C.light_dir, ctx);
+  auto normal_at = [&](int nx, int ny) {
+    nx = min(max(nx, 0), int(C.fbo_w) - 1);
+    ny = min(max(ny, 0), int(C.fbo_h) - 1);
+    if (nx >= int(C.w) || ny >= int(C.h)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return C.hits[4 * (size_t(ny) * C.w + nx) + 1];
+  };
+  const float4 n_r = normal_at(int(x) + 1, int(y)), n_l = normal_at(int(x) - 1, int(y));
+  const float4 n_u = normal_at(int(x), int(y) + 1), n_d = normal_at(int(x), int(y) - 1);
+  const float c0 = ((fabsf(n_r.x - n[0]) + fabsf(n_l.x - n[0])) + fabsf(n_u.x - n[0])) +
+                   fabsf(n_d.x - n[0]);
+  const float c1 = ((fabsf(n_r.y - n[1]) + fabsf(n_l.y - n[1])) + fabsf(n_u.y - n[1])) +
+                   fabsf(n_d.y - n[1]);
+  const float c2 = ((fabsf(n_r.z - n[2]) + fabsf(n_l.z - n[2])) + fabsf(n_u.z - n[2])) +
+                   fabsf(n_d.z - n[2]);
+  const float curvature = len3(c0, c1, c2);
+  const float dist_w = len3(pos[0] - C.pick[0], pos[1] - C.pick[1], pos[2] - C.pick[2]) * C.size;
+  const float blend =
+      fminf(fmaxf(fmaxf(curvature * C.context_scale, fminf(fmaxf(dist_w, 0.0f), 1.0f)), 0.0f),
+            1.0f);
+  float foc[4] = {0.f, 0.f, 0.f, 0.f};
+  const float4 fp = C.hits[4 * pix + 2];
+  if (fp.w != 0.0f) {
+    const float4 fn = C.hits[4 * pix + 3];
+    const float fpos[3] = {fp.x, fp.y, fp.z}, fnrm[3] = {fn.x, fn.y, fn.z};
+    surface_lighting(fpos, fnrm, C.light_a, C.diffuse_focus, C.light_s, C.light_dir, foc);
+    foc[3] = 1.0f;
+  }
+  const float ctx4[4] = {ctx[0], ctx[1], ctx[2], 1.0f};
+  float col[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    col[i] = fminf(fmaxf(ctx4[i] * blend + foc[i] * (1.0f - blend), 0.0f), 1.0f);
+  const float dark =
+      0.5f * (1.0f - fminf(fmaxf(fabsf(dist_w - 1.0f) * C.border_scale, 0.0f), 1.0f));
+  C.out[pix] = make_float4(col[0] - dark, col[1] - dark, col[2] - dark, col[3]);
 }
 
 // Many frames in one persistent launch (the reference renders render regions
@@ -1430,13 +1565,24 @@ void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const uint32_t tw = 16 * TVK_RAYCAST_RPT;
   const dim3 grid((p.out_w + tw - 1) / tw, (p.out_h + 7) / 8);
   const bool iso = p.mode == TVK_RM_ISOSURFACE;
+  const bool cv = iso && p.cv_on;
   if (p.bytes == 1) {
-    if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);
+    if (cv) raycast_kernel<uint8_t, true, true><<<grid, block, 0, s>>>(p);
+    else if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);
     else raycast_kernel<uint8_t, false><<<grid, block, 0, s>>>(p);
   } else {
-    if (iso) raycast_kernel<uint16_t, true><<<grid, block, 0, s>>>(p);
+    if (cv) raycast_kernel<uint16_t, true, true><<<grid, block, 0, s>>>(p);
+    else if (iso) raycast_kernel<uint16_t, true><<<grid, block, 0, s>>>(p);
     else raycast_kernel<uint16_t, false><<<grid, block, 0, s>>>(p);
   }
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_cv_compose(const CvComposeParams& p, cudaStream_t s, uint64_t* launches) {
+  const dim3 block(32, 4);
+  const dim3 grid((p.w + 31) / 32, (p.h + 3) / 4);
+  cv_compose_kernel<<<grid, block, 0, s>>>(p);
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }

@@ -211,10 +211,31 @@ struct RenderParams {
   float* depth;              // per pixel 1 / (1 + first-hit distance), 0: no hit (may be null)
   int clip_on;               // clip plane: keep eye-space points p with
   float clip_eye[4];         //   clip_eye . (p, 1) <= 0
+  // ClearView (iso mode): the march writes, per pixel, the context surface's
+  // hit and normal and the focus surface's hit and normal to cv_hits (four
+  // float4 per pixel) instead of shading; cv_compose shades them.
+  int cv_on;
+  float cv_iso;              // the focus surface's fIsoval (GetNormalizedCVIsovalue)
+  int cv_cell_skip;          // cell distances hold for cv_iso too (cv_iso >= iso_norm)
+  float4* cv_hits;
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
 };
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
+
+// Compose-CV-FS.glsl:49-108 over the hit records of a ClearView frame of
+// w x h pixels drawn at the lower left of a fbo_w x fbo_h target: context
+// lighting, curvature from the four neighbours' normals, distance to the focus
+// point, focus lighting, blend and border darkening.
+struct CvComposeParams {
+  const float4* hits;        // four float4 per pixel (see RenderParams::cv_hits)
+  float4* out;
+  uint32_t w, h, fbo_w, fbo_h;
+  float light_a[3], diffuse_context[3], diffuse_focus[3], light_s[3], light_dir[3];
+  float size, context_scale, border_scale;  // vCVParam
+  float pick[3];                             // vCVPickPos (eye space)
+};
+void launch_cv_compose(const CvComposeParams& p, cudaStream_t s, uint64_t* launches);
 // Frames of one persistent batched launch, passed whole as a kernel parameter
 // (it lives in the constant bank; no staging copy).  All frames of a launch
 // share the kernel variant: voxel type and iso or compositing mode.

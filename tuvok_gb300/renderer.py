@@ -295,6 +295,37 @@ class Renderer:
     def DisableClipPlane(self):
         self.EnableClipPlane(False)
 
+    # ClearView (AbstrRenderer::SetCV and its parameters): in iso mode a focus
+    # isosurface is revealed behind the context surface around a focus point.
+    def SetCV(self, on=True):
+        check(lib().tvk_set_clearview(self._h, int(bool(on))))
+
+    def SetCVIsoValue(self, isovalue):
+        """Focus isovalue in data units (default 1.5x the initial isovalue)."""
+        check(lib().tvk_set_cv_isovalue(self._h, float(isovalue)))
+
+    def SetCVColor(self, rgb):
+        check(lib().tvk_set_cv_color(self._h, (C.c_float * 3)(*[float(v) for v in rgb])))
+
+    def SetCVParams(self, size=5.5, context_scale=1.0, border_scale=60.0):
+        """SetCVSize / SetCVContextScale / SetCVBorderScale."""
+        check(lib().tvk_set_cv_params(self._h, float(size), float(context_scale),
+                                      float(border_scale)))
+
+    def SetCVFocusPosFVec(self, pos):
+        """Focus point in model space, (x, y, z, w) with w = 1."""
+        check(lib().tvk_set_cv_focus_pos(self._h, (C.c_float * 4)(*[float(v) for v in pos])))
+
+    def GetCVFocusPos(self):
+        out = (C.c_float * 4)()
+        check(lib().tvk_get_cv_focus_pos(self._h, out))
+        return tuple(out)
+
+    def SetCVFocusPos(self, x, y):
+        """Picks the focus point from the last ClearView frame's context hit at
+        pixel (x, y) of the ray-marched image, row 0 at the bottom."""
+        check(lib().tvk_set_cv_focus_pixel(self._h, int(x), int(y)))
+
     def SetLOD(self, lod):
         """m_iCurrentLOD for Paint()."""
         check(lib().tvk_set_lod(self._h, int(lod)))
