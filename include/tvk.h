@@ -41,7 +41,16 @@ typedef enum tvk_status {
   TVK_ERR_INTERNAL = 6
 } tvk_status;
 
-typedef enum tvk_dtype { TVK_U8 = 0, TVK_U16 = 1 } tvk_dtype;
+/* Voxel types.  TVK_RGBA8: colour volumes, four unsigned 8-bit channels per
+ * voxel, x fastest (Dataset::GetComponentCount() == 4, AbstrRenderer::
+ * ColorData).  Colour volumes are bricked at LOD 0 only, with no statistics
+ * (AbstrRenderer::ContainsData never skips colour bricks); they render in 1D
+ * mode (the voxel's colour times the TF entry at (r + g + b) / 3,
+ * VRender1D-Color.glsl / VRender1DLit-Color.glsl) and iso mode (the alpha
+ * channel's isosurface with its colour, GLRaycaster-Color-FS.glsl and
+ * Compose-Color-FS.glsl); 2D mode, ClearView, batches, the GridLeaper pool,
+ * rebricking and the histograms refuse them. */
+typedef enum tvk_dtype { TVK_U8 = 0, TVK_U16 = 1, TVK_RGBA8 = 2 } tvk_dtype;
 
 /* AbstrRenderer::ERenderMode (Renderer/AbstrRenderer.h:120-126) */
 typedef enum tvk_render_mode {
@@ -56,6 +65,21 @@ typedef enum tvk_light_model {
   TVK_LIGHT_REFERENCE = 0,
   TVK_LIGHT_BLINN_PHONG = 1
 } tvk_light_model;
+
+/* AbstrRenderer::ScalingMethod (Renderer/AbstrRenderer.h:156-159): how a
+ * 1D-mode sample maps to a TF coordinate.  SMETH_BIT_WIDTH: value * fTransScale
+ * with CalculateScaling (GLRenderer.cpp:1813-1819).  SMETH_BIAS_AND_SCALE
+ * (MasterController::RequestNewVolumeRenderer's bBiasAndScaleTF): GLRaycaster
+ * uploads TFuncBias = -min and fTransScale = |min| + |max| of the data range
+ * (TFScaling.cpp scale_bias_and_scale, GLRaycaster.cpp:577-584), but its 1D
+ * shaders never receive a ScaleMethod other than 0 (the setter is commented
+ * out, GLRenderer.cpp:1820-1833), so the bias goes unused and the coordinate is
+ * value * (|min| + |max|).  That is what this renderer computes; 2D and iso
+ * modes and the GridLeaper are unaffected. */
+typedef enum tvk_scaling_method {
+  TVK_SCALE_BIT_WIDTH = 0,
+  TVK_SCALE_BIAS_AND_SCALE = 1
+} tvk_scaling_method;
 
 typedef struct tvk_volume tvk_volume;
 typedef struct tvk_renderer tvk_renderer;
@@ -269,6 +293,8 @@ tvk_status tvk_set_iso_color(tvk_renderer* r, const float rgb[3]);
  * RGBA (colour * w is used) and light direction in eye space. */
 tvk_status tvk_set_colors(tvk_renderer* r, const float ambient[4], const float diffuse[4],
                           const float specular[4], const float light_dir[3]);
+/* AbstrRenderer::SetScalingMethod (AbstrRenderer.h:263-265). */
+tvk_status tvk_set_scaling_method(tvk_renderer* r, tvk_scaling_method method);
 /* Selects the lighting model; ka/kd/ks/shininess are used by Blinn-Phong. */
 tvk_status tvk_set_light_model(tvk_renderer* r, tvk_light_model model, float ka, float kd,
                                float ks, float shininess);

@@ -187,6 +187,8 @@ class Renderer {
   void SetClipPlane(const float plane[4]) { check(tvk_set_clip_plane(r_, plane)); }
   void EnableClipPlane() { check(tvk_enable_clip_plane(r_, 1)); }
   void DisableClipPlane() { check(tvk_enable_clip_plane(r_, 0)); }
+  // AbstrRenderer::SetScalingMethod
+  void SetScalingMethod(tvk_scaling_method m) { check(tvk_set_scaling_method(r_, m)); }
   // AbstrRenderer::SetCV, SetCVIsoValue, SetCVColor, SetCVSize /
   // SetCVContextScale / SetCVBorderScale, SetCVFocusPosFVec, SetCVFocusPos
   void SetCV(bool enable) { check(tvk_set_clearview(r_, enable ? 1 : 0)); }

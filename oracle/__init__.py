@@ -38,7 +38,7 @@ class Scene(C.Structure):
         ("sample_dec_factor", C.c_float), ("clip_on", C.c_int), ("clip_plane", C.c_float * 4),
         ("cv_on", C.c_int), ("cv_isovalue", C.c_float), ("cv_color", C.c_float * 3),
         ("cv_size", C.c_float), ("cv_context_scale", C.c_float), ("cv_border_scale", C.c_float),
-        ("cv_pos", C.c_float * 4),
+        ("cv_pos", C.c_float * 4), ("tf_bias_scale", C.c_int),
     ]
 
 
@@ -117,6 +117,9 @@ def _u32(v):
 
 
 def _dt(arr):
+    """0 = u8, 1 = u16 ([z, y, x]); 2 = RGBA8 colour ([z, y, x, 4] uint8)."""
+    if arr.dtype == np.uint8 and arr.ndim == 4:
+        return 2
     return 0 if arr.dtype == np.uint8 else 1
 
 
@@ -141,7 +144,7 @@ def lod0_brick(raw, bsize, overlap, clamp, coords):
     dims = (raw.shape[2], raw.shape[1], raw.shape[0])
     sizes, counts = lod_table(dims, bsize, overlap)
     bs = brick_size(sizes[0], counts[0], bsize, overlap, coords)
-    out = np.zeros((bs[2], bs[1], bs[0]), dtype=raw.dtype)
+    out = np.zeros((bs[2], bs[1], bs[0]) + raw.shape[3:], dtype=raw.dtype)
     lib().orc_lod0_brick(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims), _u32(bsize),
                          overlap, int(clamp), _u64(coords), out.ctypes.data_as(C.c_void_p))
     return out
@@ -245,7 +248,7 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
                use_double=False, row_stride=1, row_phase=0, threads=0, isovalue=None,
                iso_color=(0.5, 0.5, 0.5), lod=0, median=False, dec_screen=False,
                dec_sampling=False, screen_dec=2.0, sample_dec=2.0, clip_plane=None,
-               clearview=None):
+               clearview=None, bias_scale=False):
     """Scene struct for the oracle; returns (scene, arrays that must stay alive).
 
     clearview: None, or a dict with any of isovalue (default 1.5 x the
@@ -290,7 +293,9 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
     s.threads = threads
     # AbstrRenderer.cpp:252-261: half the data range once a dataset is loaded,
     # the ClearView isovalue half as much again above that
-    default_iso = np.float32(float(raw.max()) - float(raw.min())) / np.float32(2.0)
+    # colour volumes: the 8-bit channel range
+    rng = (0.0, 255.0) if raw.ndim == 4 else (float(raw.min()), float(raw.max()))
+    default_iso = np.float32(rng[1] - rng[0]) / np.float32(2.0)
     if isovalue is None:
         isovalue = float(default_iso)
     s.isovalue = isovalue
@@ -298,6 +303,7 @@ def make_scene(raw, bsize, overlap, tf, *, width=1, height=1, eye=(0, 0, 1.6), a
     if clip_plane is not None:
         s.clip_on = 1
         s.clip_plane[:] = [float(x) for x in clip_plane]
+    s.tf_bias_scale = int(bool(bias_scale))
     if clearview is not None:
         cv = dict(clearview)
         s.cv_on = 1

@@ -206,7 +206,10 @@ void hist256(const T* p, const uint64_t n[3], uint32_t ov, uint32_t shift, uint3
 extern "C" void orc_lod0_brick(const void* raw, int dtype, const uint64_t dims[3],
                                const uint32_t brick_size[3], uint32_t overlap,
                                int clamp_to_edge, const uint64_t coords[3], void* out) {
-  if (dtype == 0)
+  if (dtype == 2)  // RGBA8: the same copy of 4-byte voxels
+    lod0_brick<uint32_t>(as<uint32_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
+                         coords, static_cast<uint32_t*>(out));
+  else if (dtype == 0)
     lod0_brick<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
                         coords, static_cast<uint8_t*>(out));
   else

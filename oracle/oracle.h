@@ -126,7 +126,7 @@ enum { ORC_LIGHT_REFERENCE = 0, ORC_LIGHT_BLINN_PHONG = 1 };
 typedef struct orc_scene {
   /* volume, bricked by the oracle itself */
   const void* raw;
-  int dtype;                /* 0 = u8, 1 = u16 */
+  int dtype;                /* 0 = u8, 1 = u16, 2 = RGBA8 colour (LOD 0 only) */
   uint64_t dims[3];
   uint32_t brick_size[3];   /* including overlap, as Tuvok counts it */
   uint32_t overlap;
@@ -174,6 +174,9 @@ typedef struct orc_scene {
   float cv_color[3];
   float cv_size, cv_context_scale, cv_border_scale;
   float cv_pos[4];
+  /* AbstrRenderer SMETH_BIAS_AND_SCALE in 1D mode: fTransScale = |min| + |max|
+   * of the data range (GLRaycaster.cpp:577-584; the bias is never applied) */
+  int tf_bias_scale;
 } orc_scene;
 
 /* Renders the scene; out_rgba is width*height*4 floats, row 0 = bottom row

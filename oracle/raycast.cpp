@@ -133,8 +133,10 @@ struct Vol {
   const BrickR* b;
   int dtype;
   T inv_max;
+  int ch = 0;  // RGBA8: the channel sampled (0 = red ... 3 = alpha)
   T fetch(int x, int y, int z) const {
     const size_t i = size_t(x) + size_t(y) * b->n[0] + size_t(z) * b->n[0] * b->n[1];
+    if (dtype == 2) return T(b->data[4 * i + size_t(ch)]);
     if (dtype == 0) return T(b->data[i]);
     return T(reinterpret_cast<const uint16_t*>(b->data.data())[i]);
   }
@@ -279,7 +281,7 @@ template <class T>
 void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_in,
                  float t_out, T col[4], uint64_t& samples) {
   const orc_scene& s = *st.s;
-  Vol<T> vol{&b, s.dtype, T(s.dtype == 0 ? 1.0f / 255.0f : 1.0f / 65535.0f)};
+  Vol<T> vol{&b, s.dtype, T(s.dtype == 1 ? 1.0f / 65535.0f : 1.0f / 255.0f)};
   // GLRaycaster.cpp:93-99: entry eye position passes through an RGBA16F target
   float en[3], ex[3];
   for (int a = 0; a < 3; ++a) {
@@ -404,7 +406,7 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
                T hit_eye[3], T& fpar, T nrm[3], T& depth, uint64_t& samples,
                float iso_cv = 0.0f, T p_start = T(0)) {
   const orc_scene& s = *st.s;
-  Vol<T> vol{&b, s.dtype, T(s.dtype == 0 ? 1.0f / 255.0f : 1.0f / 65535.0f)};
+  Vol<T> vol{&b, s.dtype, T(s.dtype == 1 ? 1.0f / 65535.0f : 1.0f / 255.0f)};
   float en[3], ex[3];
   for (int a = 0; a < 3; ++a) {
     en[a] = orc_round_half(dir[a] * t_in);
@@ -505,6 +507,168 @@ void surface_lighting(const Setup& st, const T pos[3], const T nin[3], const flo
   }
 }
 
+// Normal of a colour volume from its red channel (Volume3D.glsl:43-60 reads
+// sampleVolume(...).x).
+template <class T>
+void color_normal(const Setup& st, Vol<T> red, const T pos[3], const T vstep[3], T N[3]) {
+  red.ch = 0;
+  const T xp = red.sample(pos[0] + vstep[0], pos[1], pos[2]);
+  const T xm = red.sample(pos[0] + (-vstep[0]), pos[1], pos[2]);
+  const T yp = red.sample(pos[0], pos[1] + (-vstep[1]), pos[2]);
+  const T ym = red.sample(pos[0], pos[1] + vstep[1], pos[2]);
+  const T zp = red.sample(pos[0], pos[1], pos[2] + vstep[2]);
+  const T zm = red.sample(pos[0], pos[1], pos[2] + (-vstep[2]));
+  const T gs[3] = {((xm - xp) / T(2)) * T(st.domain_scale[0]),
+                   ((yp - ym) / T(2)) * T(st.domain_scale[1]),
+                   ((zm - zp) / T(2)) * T(st.domain_scale[2])};
+  for (int r = 0; r < 3; ++r)
+    N[r] = std::fma(T(float(st.norm_mat[r][2])), gs[2],
+                    std::fma(T(float(st.norm_mat[r][1])), gs[1], T(float(st.norm_mat[r][0])) * gs[0]));
+  const T l = len3(N[0], N[1], N[2]);
+  if (l > T(0)) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+}
+
+// A brick of a colour volume in 1D mode: GLRaycaster-1D-FS.glsl /
+// -1D-light-FS.glsl with VRender1D-Color.glsl:44-53 and VRender1DLit-Color.glsl:
+// 44-62 -- the filtered RGBA times the TF entry at (r + g + b) / 3, opacity
+// correction of the product's alpha, lit with the product's colour.
+template <class T>
+void brick_march_color(const Setup& st, const BrickR& b, const float dir[3], float t_in,
+                       float t_out, T col[4], uint64_t& samples) {
+  const orc_scene& s = *st.s;
+  Vol<T> vol{&b, 2, T(1.0f / 255.0f)};
+  float en[3], ex[3];
+  for (int a = 0; a < 3; ++a) {
+    en[a] = orc_round_half(dir[a] * t_in);
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = std::sqrt((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row<float>(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row<float>(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float q = len / b.step;
+  const int n = int(q) + 1;
+  T inc[3], pos[3], epos[3], einc[3];
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = T(tout[a] - tin[a]) / T(q);
+    pos[a] = T(tin[a]);
+    epos[a] = T(en[a]);
+  }
+  {
+    const T ddx = T(ex[0]) - T(en[0]), ddy = T(ex[1]) - T(en[1]), ddz = T(ex[2]) - T(en[2]);
+    const T l = len3(ddx, ddy, ddz);
+    einc[0] = (ddx / l) * T(b.step);
+    einc[1] = (ddy / l) * T(b.step);
+    einc[2] = (ddz / l) * T(b.step);
+  }
+  const T vstep[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
+  const uint32_t W = s.tf_w;
+  T c[4] = {0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    T v[4];
+    for (int k = 0; k < 4; ++k) {
+      vol.ch = k;
+      v[k] = vol.sample(pos[0], pos[1], pos[2]);
+    }
+    const T u = ((v[0] + v[1]) + v[2]) / T(3);
+    T fi = std::floor(u * T(W));
+    fi = std::fmin(std::fmax(fi, T(0)), T(W - 1));
+    const float* e = &st.tf[4 * size_t(fi)];
+    T src[4] = {v[0] * T(e[0]), v[1] * T(e[1]), v[2] * T(e[2]), v[3] * T(e[3])};
+    src[3] = T(1) - std::pow(T(1) - src[3], T(st.step_scale));
+    if (s.lighting && src[3] != T(0)) {
+      T N[3], lc[3];
+      color_normal<T>(st, vol, pos, vstep, N);
+      const T tfc[3] = {src[0], src[1], src[2]};
+      if (s.light_model == ORC_LIGHT_BLINN_PHONG)
+        lighting_bp<T>(st, epos, N, tfc, lc);
+      else
+        lighting_ref<T>(st, epos, N, tfc, lc);
+      src[0] = lc[0]; src[1] = lc[1]; src[2] = lc[2];
+    }
+    const T w = T(1) - c[3];
+    c[0] = std::fma(src[0] * w, src[3], c[0]);
+    c[1] = std::fma(src[1] * w, src[3], c[1]);
+    c[2] = std::fma(src[2] * w, src[3], c[2]);
+    c[3] = std::fma(src[3], w, c[3]);
+    for (int a = 0; a < 3; ++a) {
+      pos[a] = pos[a] + inc[a];
+      epos[a] = epos[a] + einc[a];
+    }
+    if (c[3] >= T(0.99f)) break;
+  }
+  for (int a = 0; a < 4; ++a) col[a] = c[a];
+}
+
+// GLRaycaster-Color-FS.glsl for one brick: the first step whose alpha is >=
+// fIsoval, RefineIsosurface on the red channel, the red channel's normal, and
+// the colour at the unrefined step packed into the two hit buffers' alphas
+// (red + 1; floor(green * 512) + blue).
+template <class T>
+bool iso_brick_color(const Setup& st, const BrickR& b, const float dir[3], float t_in,
+                     float t_out, T hit_eye[3], T nrm[3], T& depth, T& enc_r, T& enc_gb,
+                     uint64_t& samples) {
+  Vol<T> vol{&b, 2, T(1.0f / 255.0f)};
+  float en[3], ex[3];
+  for (int a = 0; a < 3; ++a) {
+    en[a] = orc_round_half(dir[a] * t_in);
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = std::sqrt((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row<float>(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row<float>(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const T len_tex = len3(T(tout[0] - tin[0]), T(tout[1] - tin[1]), T(tout[2] - tin[2]));
+  const float q = len / b.step;
+  if (!(q < 1.0e6f)) return false;
+  const int n = int(q) + 1;
+  T inc[3], pos[3];
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = T(tout[a] - tin[a]) / T(q);
+    pos[a] = T(tin[a]);
+  }
+  const T iso = T(st.iso_norm);
+  bool hit = false;
+  vol.ch = 3;
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    if (vol.sample(pos[0], pos[1], pos[2]) >= iso) { hit = true; break; }
+    for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+  }
+  if (!hit) return false;
+  T d[3], cur[3];
+  for (int a = 0; a < 3; ++a) {
+    d[a] = inc[a] / T(2);
+    cur[a] = pos[a] - d[a];
+  }
+  vol.ch = 0;
+  for (int k = 0; k < 5; ++k) {
+    for (int a = 0; a < 3; ++a) d[a] = d[a] / T(2);
+    const bool above = vol.sample(cur[0], cur[1], cur[2]) >= iso;
+    for (int a = 0; a < 3; ++a) cur[a] = above ? cur[a] - d[a] : cur[a] + d[a];
+  }
+  T rgb[3];
+  for (int k = 0; k < 3; ++k) {
+    vol.ch = k;
+    rgb[k] = vol.sample(pos[0], pos[1], pos[2]);
+  }
+  const T fpar = len3(cur[0] - T(tin[0]), cur[1] - T(tin[1]), cur[2] - T(tin[2])) / len_tex;
+  for (int a = 0; a < 3; ++a) hit_eye[a] = T(en[a]) * (T(1) - fpar) + T(ex[a]) * fpar;
+  depth = T(st.proj_x) + (T(st.proj_y) / -hit_eye[2]);
+  const T vs[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
+  color_normal<T>(st, vol, cur, vs, nrm);
+  enc_r = rgb[0] + T(1);
+  enc_gb = std::floor(rgb[1] * T(512)) + rgb[2];
+  return true;
+}
+
 template <class T>
 void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_t* spp,
                   uint64_t& samples) {
@@ -550,7 +714,33 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
   });
   T frame[4] = {0, 0, 0, 0};
   const uint64_t before = samples;
-  if (s.render_mode == ORC_RM_ISO && s.cv_on) {
+  if (s.dtype == 2 && s.render_mode == ORC_RM_ISO) {
+    // colour: nearest hit by the depth test, Compose-Color-FS.glsl:60-88 (the
+    // hit buffer's alpha is red + 1, never 0)
+    T best_depth = T(1), pos[3] = {0, 0, 0}, nrm[3] = {0, 0, 0}, er = 0, egb = 0;
+    bool any = false;
+    for (const Hit& h : hits) {
+      T hp[3], hn[3], depth, r1, gb;
+      if (!iso_brick_color<T>(st, st.bricks[h.b], dir, h.t0, h.t1, hp, hn, depth, r1, gb,
+                              samples))
+        continue;
+      if (!(depth < best_depth)) continue;
+      best_depth = depth;
+      for (int a = 0; a < 3; ++a) { pos[a] = hp[a]; nrm[a] = hn[a]; }
+      er = r1;
+      egb = gb;
+      any = true;
+    }
+    if (any) {
+      const T rgb[3] = {er - T(1), std::floor(egb / T(2)) / T(256), egb - std::floor(egb)};
+      const T n[3] = {nrm[0], nrm[1], std::fabs(nrm[2])};
+      float dcol[3];  // vColor.rgb * vLightDiffuse
+      T c[3];
+      for (int a = 0; a < 3; ++a) dcol[a] = float(rgb[a] * T(st.light_d[a]));
+      surface_lighting<T>(st, pos, n, dcol, c);
+      frame[0] = c[0]; frame[1] = c[1]; frame[2] = c[2]; frame[3] = T(1);
+    }
+  } else if (s.render_mode == ORC_RM_ISO && s.cv_on) {
     // ClearView (GLRaycaster.cpp:421-436): per brick, in list order, the
     // context pass into m_pFBOIsoHit (depth test on the hit depth; normal.w =
     // the brick's tile ID), then the focus pass into m_pFBOCVHit, which starts
@@ -614,7 +804,10 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
     for (const Hit& h : hits) {
       if (frame[3] >= T(s.frame_ert)) break;
       T c[4];
-      brick_march<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
+      if (s.dtype == 2)
+        brick_march_color<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
+      else
+        brick_march<T>(st, st.bricks[h.b], dir, h.t0, h.t1, c, samples);
       // GLRenderer.cpp:151-153 blend (ONE_MINUS_DST_ALPHA, ONE) into RGBA32F
       const T w = T(1) - frame[3];
       for (int a = 0; a < 4; ++a) frame[a] = std::fma(c[a], w, frame[a]);
@@ -627,11 +820,13 @@ void render_pixel(const Setup& st, uint32_t px, uint32_t py, float* out, uint32_
 Setup build_setup(const orc_scene& s) {
   Setup st;
   st.s = &s;
-  const int bytes = s.dtype == 0 ? 1 : 2;
+  const bool color = s.dtype == 2;  // RGBA8: LOD 0, no statistics, every brick drawn
+  const int bytes = color ? 4 : (s.dtype == 0 ? 1 : 2);
+  const int bits = color ? 8 : 8 * bytes;  // Dataset::GetBitWidth (per channel)
   uint64_t lod_all[3 * 64], cnt_all[3 * 64];
   const int n_lods = orc_lod_table(s.dims, s.brick_size, s.overlap, lod_all, cnt_all, 64);
   // the rendered LOD (AbstrRenderer m_iCurrentLOD); its bricks, metadata and aspect
-  const uint32_t L = std::min<uint32_t>(s.lod, uint32_t(n_lods - 1));
+  const uint32_t L = color ? 0u : std::min<uint32_t>(s.lod, uint32_t(n_lods - 1));
   const uint64_t* lod = &lod_all[3 * L];
   const uint64_t* cnt = &cnt_all[3 * L];
   const uint64_t nb = cnt[0] * cnt[1] * cnt[2];
@@ -675,17 +870,23 @@ Setup build_setup(const orc_scene& s) {
 
   // data range (dataset GetRange) and TF non-zero limits
   const uint64_t nvox = s.dims[0] * s.dims[1] * s.dims[2];
-  double rmax = 0;
-#pragma omp parallel for reduction(max : rmax)
-  for (int64_t ii = 0; ii < int64_t(nvox); ++ii) {
+  double rmax = 0, rmin = 1e300;
+  if (color) { rmin = 0; rmax = 255; }
+#pragma omp parallel for reduction(max : rmax) reduction(min : rmin)
+  for (int64_t ii = 0; ii < int64_t(color ? 0 : nvox); ++ii) {
     const uint64_t i = uint64_t(ii);
     const double x = bytes == 1 ? double(static_cast<const uint8_t*>(s.raw)[i])
                                 : double(static_cast<const uint16_t*>(s.raw)[i]);
     rmax = std::max(rmax, x);
+    rmin = std::min(rmin, x);
   }
-  // GLRenderer.cpp:1813-1819 CalculateScaling: (2^bits-1)/MaxValue
-  const uint32_t imax = (1u << (8 * bytes)) - 1;
-  st.trans_scale = float(double(imax) / rmax);
+  // GLRenderer.cpp:1813-1819 CalculateScaling: (2^bits-1)/MaxValue; with bias
+  // and scale in 1D mode GLRaycaster.cpp:577-584 sets fTransScale to
+  // scale_bias_and_scale's |min| + |max| (TFScaling.cpp)
+  const uint32_t imax = (1u << bits) - 1;
+  st.trans_scale = (s.render_mode == ORC_RM_1D && s.tf_bias_scale)
+                       ? std::fabs(float(rmin)) + std::fabs(float(rmax))
+                       : float(double(imax) / rmax);
   // GLRenderer.cpp:1840-1841: fGradientScale = 1 / MaxGradientMagnitude
   st.grad_scale = 1.0f;
   if (s.render_mode == ORC_RM_2D) {
@@ -734,9 +935,9 @@ Setup build_setup(const orc_scene& s) {
     st.iso_diffuse[a] = st.light_d[a] * s.iso_color[a];
   }
   // AbstrRenderer.cpp:412-424: fIsoval = isovalue / 2^bits (not 2^bits - 1)
-  st.iso_norm = float(double(s.isovalue) / double(1u << (8 * bytes)));
+  st.iso_norm = float(double(s.isovalue) / double(1u << bits));
   // AbstrRenderer.cpp:426-438 GetNormalizedCVIsovalue; GLRenderer.cpp:2784
-  st.cv_iso_norm = float(double(s.cv_isovalue) / double(1u << (8 * bytes)));
+  st.cv_iso_norm = float(double(s.cv_isovalue) / double(1u << bits));
   for (int a = 0; a < 3; ++a) st.cv_diffuse[a] = st.light_d[a] * s.cv_color[a];
   // CullingLOD.cpp:69-72
   st.proj_x = s.zfar / (s.zfar - s.znear);
@@ -778,10 +979,14 @@ Setup build_setup(const orc_scene& s) {
                          b.data.data());
         else
           std::memcpy(b.data.data(), octree.data() + octree_off[lod_first + k] * bytes, nbytes);
-        double mn, mx;
-        orc_brick_stats(b.data.data(), s.dtype, uint64_t(b.n[0]) * b.n[1] * b.n[2], &mn, &mx);
-        // ContainsData: value range vs TF limits, or the isovalue (uvfDataset.cpp:1201-1215)
-        if (iso_mode)
+        double mn = 0, mx = 255;
+        if (!color)
+          orc_brick_stats(b.data.data(), s.dtype, uint64_t(b.n[0]) * b.n[1] * b.n[2], &mn, &mx);
+        // ContainsData: value range vs TF limits, or the isovalue
+        // (uvfDataset.cpp:1201-1215); colour bricks always (AbstrRenderer.cpp:955-959)
+        if (color)
+          contains_flag[k] = 1;
+        else if (iso_mode)
           contains_flag[k] = (double(s.isovalue) <= mx) ? 1 : 0;
         else
           contains_flag[k] = (hi >= mn && lo <= mx) ? 1 : 0;

@@ -1,0 +1,138 @@
+"""Colour (RGBA8) volumes against the oracle: LOD-0 bricks with their ghost
+layer bit for bit; 1D mode (VRender1D-Color / VRender1DLit-Color: the voxel's
+colour times the TF entry at (r + g + b) / 3) and iso mode (the alpha
+channel's surface, GLRaycaster-Color-FS + Compose-Color-FS) with the usual
+image tolerance.  The opacity correction of a colour sample depends on the
+voxel's alpha, so it runs per sample on the GPU (powf) and in libm on the CPU;
+a last-bit difference can move early ray termination by one step, so sample
+counts are compared per pixel with that allowance."""
+import numpy as np
+import pytest
+
+import oracle as O
+from tuvok_gb300 import Batch, Pool, Renderer, TvkError, Volume
+from tuvok_gb300.workloads import numpy_blob_volume
+from test_gpu_render import compare
+
+pytestmark = pytest.mark.gpu
+
+BS = 18
+W, H = 80, 64
+
+
+@pytest.fixture(scope="module")
+def rgba():
+    dims = (45, 38, 33)
+    ch = [numpy_blob_volume(dims, np.uint8, 7, (3, 9), (60, 255), 255, 70 + k, 3)
+          for k in range(4)]
+    return np.stack(ch, axis=-1)
+
+
+def color_tf(n=64):
+    t = np.zeros((n, 4), dtype=np.float32)
+    i = np.arange(n) / (n - 1)
+    t[:, 0], t[:, 1], t[:, 2] = 0.4 + 0.6 * i, 1.0 - 0.5 * i, 0.7
+    t[:, 3] = np.clip((i - 0.2) / 0.8, 0, 1) * 0.5
+    return t
+
+
+def renderer(vol, mode, lit, tf=None):
+    r = Renderer()
+    r.RegisterDataset(vol)
+    if tf is not None:
+        r.Set1DTransFloat(tf)
+    r.SetRendermode(mode)
+    r.SetUseLighting(lit)
+    return r
+
+
+@pytest.mark.parametrize("clamp", [False, True])
+def test_gpu_color_bricks_match_oracle(cuda_ok, rgba, clamp):
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1, clamp_to_edge=clamp)
+    assert vol.GetLODLevelCount() >= 1
+    for k in range(vol.GetBrickCount(0)):
+        x, y, z, _ = vol.IndexTo4D(0, k)
+        np.testing.assert_array_equal(vol.GetBrick((0, 0, k)),
+                                      O.lod0_brick(rgba, (BS,) * 3, 1, clamp, (x, y, z)))
+
+
+CASES = [
+    # id, mode, lighting, light model, eye
+    ("1d", 0, False, 0, (0.3, 0.4, 1.5)),
+    ("1d_lit", 0, True, 0, (-1.1, 0.2, -0.7)),
+    ("1d_lit_bp", 0, True, 1, (0.9, -0.6, 1.0)),
+    ("iso", 2, False, 0, (0.3, 0.4, 1.5)),
+    ("iso_inside", 2, False, 0, (0.05, 0.02, 0.1)),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_gpu_color_render_matches_oracle(cuda_ok, rgba, case):
+    name, mode, lit, model, eye = case
+    tf = color_tf()
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1)
+    r = renderer(vol, mode, lit, tf)
+    if model == 1:
+        r.SetLightModel(1, 0.2, 0.6, 0.2, 32.0)
+    iso = 130.0
+    if mode == 2:
+        r.SetIsoValue(iso)
+    r.SetSampleRateModifier(1.5)
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+    r.Resize(W, H)
+    r.Paint()
+    img, cnt, st = r.ReadBackPixels(), r.ReadSampleCounts(), r.GetStats()
+    kw = dict(width=W, height=H, eye=eye, mode=mode, lighting=lit, light_model=model,
+              srm=1.5, want_counts=True)
+    if mode == 2:
+        kw["isovalue"] = iso
+    ref, n, rc = O.render(rgba, (BS,) * 3, 1, tf, **kw)
+    compare(img, ref, name)
+    assert st.bricks_visible == st.bricks_total  # colour bricks are never skipped
+    if mode == 2:
+        assert (cnt <= rc).all()
+        assert (img[..., 3] > 0).mean() > 0.05
+    else:
+        assert (cnt != rc).mean() < 2e-3, name
+        assert (img[..., 3] > 0).mean() > 0.05
+
+
+def test_gpu_color_clip_and_reduced(cuda_ok, rgba):
+    tf = color_tf()
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1)
+    r = renderer(vol, 0, True, tf)
+    eye = (0.5, 0.35, 1.3)
+    r.SetClipPlane((0.3, -0.5, 0.8, 0.05))
+    r.EnableClipPlane()
+    r.SetReducedQuality(True, True)
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+    r.Resize(W, H)
+    r.Paint()
+    ref, _, _ = O.render(rgba, (BS,) * 3, 1, tf, width=W, height=H, eye=eye, lighting=True,
+                         clip_plane=(0.3, -0.5, 0.8, 0.05), dec_screen=True, dec_sampling=True)
+    compare(r.ReadBackPixels(), ref, "clip + reduced")
+
+
+def test_gpu_color_refusals(cuda_ok, rgba):
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1)
+    r = renderer(vol, 1, False)
+    r.Set2DTransFloat(np.ones((8, 16, 4), np.float32))
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=(0.3, 0.4, 1.5))
+    r.Resize(W, H)
+    with pytest.raises(TvkError):
+        r.Paint()  # 2D mode
+    r.SetRendermode(0)
+    r.Set1DTransFloat(color_tf())
+    r.SetLOD(1)
+    with pytest.raises(TvkError):
+        r.Paint()  # LOD 0 only
+    r.SetLOD(0)
+    r.Paint()
+    with pytest.raises(TvkError):
+        Batch().Paint([r])
+    with pytest.raises(TvkError):
+        Pool(vol, 1 << 26)
+    with pytest.raises(TvkError):
+        vol.GetHistogram()
+    with pytest.raises(TvkError):
+        vol.Rebrick((9, 9, 9))

@@ -245,3 +245,32 @@ def test_oracle_clearview_properties():
     changed = np.abs(cv2 - iso).max(axis=-1) > 1e-3
     assert changed.any() and not changed.all()
     assert ((cv2[..., 3] == 0) == (iso[..., 3] == 0)).all()
+
+
+def test_oracle_color_volume_properties():
+    """The oracle's colour (RGBA8) volumes: bricks copy the 4-byte voxels with
+    their ghost layer; zero alpha draws nothing; the alpha channel's isosurface
+    covers the pixels a scalar volume of the same alpha bytes covers."""
+    from tuvok_gb300.workloads import numpy_blob_volume
+    dims = (22, 18, 16)
+    ch = [numpy_blob_volume(dims, np.uint8, 4, (3, 7), (80, 255), 255, 40 + k, 2)
+          for k in range(4)]
+    rgba = np.stack(ch, axis=-1)
+    for clamp in (False, True):
+        for c in [(0, 0, 0), (1, 1, 1), (2, 1, 0)]:
+            b = O.lod0_brick(rgba, (10, 10, 10), 1, clamp, c)
+            for k in range(4):
+                np.testing.assert_array_equal(b[..., k], O.lod0_brick(ch[k], (10, 10, 10), 1,
+                                                                      clamp, c))
+    tf = np.ones((64, 4), dtype=np.float32)
+    kw = dict(width=30, height=24, eye=(0.4, 0.3, 1.4), want_counts=True)
+    clear = rgba.copy()
+    clear[..., 3] = 0
+    img, n, _ = O.render(clear, (10, 10, 10), 1, tf, **kw)
+    assert n > 0 and not img.any()
+    img, n, _ = O.render(rgba, (10, 10, 10), 1, tf, lighting=True, **kw)
+    assert (img[..., 3] > 0).mean() > 0.05 and np.isfinite(img).all()
+    ciso, _, _ = O.render(rgba, (10, 10, 10), 1, tf, mode=2, isovalue=120.0, **kw)
+    siso, _, _ = O.render(ch[3], (10, 10, 10), 1, tf, mode=2, isovalue=120.0, **kw)
+    cov_c, cov_s = ciso[..., 3] > 0, siso[..., 3] > 0
+    assert (cov_c | ~cov_s).all() and (cov_c != cov_s).mean() < 0.01 and cov_c.mean() > 0.05

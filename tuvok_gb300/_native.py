@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libtvk.so"
 
 TVK_OK = 0
-TVK_U8, TVK_U16 = 0, 1
+TVK_U8, TVK_U16, TVK_RGBA8 = 0, 1, 2
 TVK_RM_1DTRANS, TVK_RM_2DTRANS, TVK_RM_ISOSURFACE = 0, 1, 2
 TVK_LIGHT_REFERENCE, TVK_LIGHT_BLINN_PHONG = 0, 1
 TVK_MM_SOURCE, TVK_MM_PRECOMPUTE, TVK_MM_DYNAMIC = 0, 1, 2
@@ -170,6 +170,7 @@ PROTOTYPES = {
     "tvk_cnn_prepare_input": [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],
     "tvk_set_clip_plane": [_vp, _f32p],
     "tvk_enable_clip_plane": [_vp, C.c_int],
+    "tvk_set_scaling_method": [_vp, C.c_int],
     "tvk_set_clearview": [_vp, C.c_int],
     "tvk_set_cv_isovalue": [_vp, C.c_float],
     "tvk_set_cv_color": [_vp, _f32p],

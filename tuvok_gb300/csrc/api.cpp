@@ -224,6 +224,35 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
                            cudaMemcpyHostToDevice, s));
   TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
                            cudaMemcpyHostToDevice, s));
+  if (V->dtype == TVK_RGBA8) {
+    // colour volumes: the bricks only.  Channel range of 8-bit data; no
+    // histograms, gradients or macro cells (colour bricks are never empty).
+    BrickGrid g;
+    for (int a = 0; a < 3; ++a) {
+      g.dims[a] = V->dims[a];
+      g.B[a] = V->brick_size[a];
+      g.cnt[a] = uint32_t(l0.bricks[a]);
+    }
+    g.ov = V->overlap;
+    g.clamp = V->clamp ? 1 : 0;
+    g.total = nvox;
+    launch_brick_copy4(d_raw, g, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(), V->n_bricks,
+                       V->d_pool, s, &launches);
+    TVK_CUDA(cudaStreamSynchronize(s));
+    V->range_min = 0;
+    V->range_max = 255;
+    V->bmin.assign(V->total_bricks, 0.0);
+    V->bmax.assign(V->total_bricks, 255.0);
+    V->hist.clear();
+    V->bhist.clear();
+    V->hist_trimmed = 0;
+    V->max_grad = 0;
+    V->cell_offsets.assign(V->total_bricks, 0);
+    V->cell_counts.assign(V->total_bricks, 0);
+    V->cell_dims.assign(V->total_bricks, 0);
+    V->total_cells = 0;
+    return;
+  }
   TVK_CUDA(cudaMemcpyAsync(d_vox.p, voxels.data(), V->total_bricks * sizeof(uint64_t),
                            cudaMemcpyHostToDevice, s));
   // scratch: bmin, bmax, bhist, hist, max_grad bits, raw min/max
@@ -384,6 +413,12 @@ void compute_histogram2d(const tvk_volume* V, uint64_t bins, uint64_t* host_out)
   TVK_CUDA(cudaStreamSynchronize(s));
 }
 
+// Paths built for scalar (one-component) volumes only.
+void require_scalar(const tvk_volume* V, const char* what) {
+  if (V->dtype == TVK_RGBA8)
+    fail(TVK_ERR_UNSUPPORTED, std::string(what) + " take scalar volumes, not colour volumes");
+}
+
 void free_volume_device(tvk_volume* V) {
   for (void** p : {&V->d_pool, &V->d_cells, &V->d_cell_meta}) {
     if (*p) cudaFree(*p);
@@ -395,7 +430,12 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
                           const uint32_t bsz[3], uint32_t ov, int clamp, bool median = false,
                           bool build_lods = true) {
   REQUIRE(src && dims && bsz, "null argument");
-  REQUIRE(dtype == TVK_U8 || dtype == TVK_U16, "dtype must be TVK_U8 or TVK_U16");
+  REQUIRE(dtype == TVK_U8 || dtype == TVK_U16 || dtype == TVK_RGBA8,
+          "dtype must be TVK_U8, TVK_U16 or TVK_RGBA8");
+  if (dtype == TVK_RGBA8) {
+    REQUIRE(!median, "colour volumes have no coarser LODs to filter");
+    build_lods = false;  // colour volumes are bricked at LOD 0 only
+  }
   for (int a = 0; a < 3; ++a) {
     REQUIRE(dims[a] >= 1, "volume dimensions must be >= 1");
     REQUIRE(bsz[a] > 2 * ov, "brick size must exceed twice the overlap (ExtendedOctree.cpp:196)");
@@ -405,7 +445,7 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
   std::unique_ptr<tvk_volume> V(new tvk_volume());
   TVK_CUDA(cudaGetDevice(&V->device));
   V->dtype = dtype;
-  V->bytes = dtype == TVK_U8 ? 1 : 2;
+  V->bytes = dtype == TVK_U8 ? 1 : (dtype == TVK_U16 ? 2 : 4);
   for (int a = 0; a < 3; ++a) {
     V->dims[a] = dims[a];
     V->brick_size[a] = bsz[a];
@@ -557,6 +597,7 @@ struct tvk_renderer {
   // (reduced and full quality) rebuild nothing
   struct TfSlot {
     float step_scale = -1.0f;
+    bool raw_alpha = false;
     bool valid = false;
     uint64_t used = 0;
     tvk::DevBuf d_tf, d_tfcol, d_tfpfx, d_empty, d_empty_meta;
@@ -565,6 +606,7 @@ struct tvk_renderer {
     bool empty_valid = false;
     bool empty_iso = false;
     float empty_iso_norm = 0.0f;
+    float empty_trans_scale = 0.0f;
   };
   TfSlot slots[2];
   int slot = 0;
@@ -576,6 +618,7 @@ struct tvk_renderer {
   float clip_plane[4] = {0, 0, 1, 0};  // m_ClipPlane, world space
   // ClearView (AbstrRenderer.cpp:130-136, 171 defaults; m_fCVIsovalue follows
   // the isovalue when a dataset is set, AbstrRenderer.cpp:261)
+  tvk_scaling_method tf_scaling = TVK_SCALE_BIT_WIDTH;  // m_TFScalingMethod
   bool cv_on = false;
   float cv_iso = 0.8f;
   float cv_color[3] = {1, 0, 0};
@@ -715,13 +758,16 @@ struct tvk_pool {
 namespace tvk {
 namespace {
 
-void upload_tf(tvk_renderer* R, float step_scale) {
+// raw_alpha: the entries keep their alpha (colour volumes correct the opacity
+// of each sample's product with the voxel alpha instead).
+void upload_tf(tvk_renderer* R, float step_scale, bool raw_alpha = false) {
   if (R->tf_dirty) {
     for (auto& sl : R->slots) sl.valid = false;
     R->tf_dirty = false;
   }
   for (int i = 0; i < 2; ++i)
-    if (R->slots[i].valid && R->slots[i].step_scale == step_scale) {
+    if (R->slots[i].valid && R->slots[i].step_scale == step_scale &&
+        R->slots[i].raw_alpha == raw_alpha) {
       R->slot = i;
       R->slots[i].used = ++R->slot_clock;
       return;
@@ -744,7 +790,7 @@ void upload_tf(tvk_renderer* R, float step_scale) {
     t[4 * i + 2] = R->tf[4 * i + 2];
     // VRender1D.glsl:53 opacity correction, evaluated per table entry
     const float a = R->tf[4 * i + 3];
-    t[4 * i + 3] = 1.0f - std::pow(1.0f - a, step_scale);
+    t[4 * i + 3] = raw_alpha ? a : 1.0f - std::pow(1.0f - a, step_scale);
     // a sample whose corrected alpha is exactly 0 adds exactly nothing
     if (t[4 * i + 3] != 0.0f) col[i % R->tf_w] = 1;
   }
@@ -760,6 +806,7 @@ void upload_tf(tvk_renderer* R, float step_scale) {
                       cudaMemcpyHostToDevice));
   S.valid = true;
   S.step_scale = step_scale;
+  S.raw_alpha = raw_alpha;
   S.used = ++R->slot_clock;
   S.empty_valid = false;
 }
@@ -769,7 +816,8 @@ void upload_tf(tvk_renderer* R, float step_scale) {
 void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale, bool iso_mode,
                         float iso_norm) {
   tvk_renderer::TfSlot& S = R->slots[R->slot];
-  if (S.empty_valid && S.empty_iso == iso_mode && (!iso_mode || S.empty_iso_norm == iso_norm))
+  if (S.empty_valid && S.empty_iso == iso_mode &&
+      (iso_mode ? S.empty_iso_norm == iso_norm : S.empty_trans_scale == trans_scale))
     return;
   // every built LOD's bricks, indexed by TOC position
   const uint64_t nb = V->total_bricks;
@@ -831,6 +879,7 @@ void update_empty_cells(tvk_renderer* R, const tvk_volume* V, float trans_scale,
   S.empty_valid = true;
   S.empty_iso = iso_mode;
   S.empty_iso_norm = iso_norm;
+  S.empty_trans_scale = trans_scale;
 }
 
 void set_tf(tvk_renderer* R, const float* rgba, uint32_t w, uint32_t h, bool rgba8) {
@@ -890,6 +939,8 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   if (R->width == 0 || R->height == 0) fail(TVK_ERR_STATE, "no viewport (tvk_resize)");
   if (R->mode == TVK_RM_2DTRANS && !R->tf_2d) fail(TVK_ERR_STATE, "2D mode needs a 2D TF");
   if (R->mode == TVK_RM_1DTRANS && R->tf_2d) fail(TVK_ERR_STATE, "1D mode needs a 1D TF");
+  if (V->dtype == TVK_RGBA8 && R->mode == TVK_RM_2DTRANS)
+    fail(TVK_ERR_UNSUPPORTED, "colour volumes render in 1D or iso mode only");
   const uint32_t L = sf.lod;
   if (L >= V->lods.size()) fail(TVK_ERR_INVALID_ARG, "LOD out of range");
   if (L + 1 >= V->lod_first.size())
@@ -912,13 +963,19 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     rw = std::max(1u, uint32_t(float(R->width) * rescale + 0.5f));
     rh = std::max(1u, uint32_t(float(R->height) * rescale + 0.5f));
   }
-  if (!R->tf.empty()) upload_tf(R, step_scale);
-  // GLRenderer.cpp:1813-1819 CalculateScaling
-  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
-  const float trans_scale = float(double(imax) / V->range_max);
+  if (!R->tf.empty()) upload_tf(R, step_scale, V->dtype == TVK_RGBA8);
+  // GLRenderer.cpp:1813-1819 CalculateScaling, or in 1D mode with bias and
+  // scale the fTransScale of GLRaycaster.cpp:577-584 (|min| + |max|)
+  const bool color = V->dtype == TVK_RGBA8;
+  const uint32_t cbits = color ? 8 : 8 * V->bytes;  // Dataset::GetBitWidth
+  const uint32_t imax = (1u << cbits) - 1;
+  const float trans_scale =
+      (R->mode == TVK_RM_1DTRANS && R->tf_scaling == TVK_SCALE_BIAS_AND_SCALE)
+          ? std::fabs(float(V->range_min)) + std::fabs(float(V->range_max))
+          : float(double(imax) / V->range_max);
   // AbstrRenderer.cpp:412-424 GetNormalizedIsovalue: isovalue / 2^bits
-  const float iso_norm = float(double(R->isovalue) / double(1u << (8 * V->bytes)));
-  if (R->cell_skip) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
+  const float iso_norm = float(double(R->isovalue) / double(1u << cbits));
+  if (R->cell_skip && !color) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
 
   const View view = make_view(R->eye, R->at, R->up, R->fovy, rw, rh, R->model);
 
@@ -1011,8 +1068,10 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   order.reserve(nbl);
   for (uint64_t j = 0; j < nbl; ++j) {
     const uint64_t k = first + j;
-    // ContainsData (uvfDataset.cpp:1201-1215): TF value limits, or the isovalue
-    if (iso_mode ? !(double(R->isovalue) <= V->bmax[k]) : !(hi >= V->bmin[k] && lo <= V->bmax[k]))
+    // ContainsData (uvfDataset.cpp:1201-1215): TF value limits, or the
+    // isovalue; colour bricks always (AbstrRenderer.cpp:955-959)
+    if (!color &&
+        (iso_mode ? !(double(R->isovalue) <= V->bmax[k]) : !(hi >= V->bmin[k] && lo <= V->bmax[k])))
       continue;
     const int64_t c[3] = {int64_t(j % ll.bricks[0]), int64_t((j / ll.bricks[0]) % ll.bricks[1]),
                           int64_t(j / (ll.bricks[0] * ll.bricks[1]))};
@@ -1076,11 +1135,12 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   P.mode = R->mode;
   P.lighting = R->lighting ? 1 : 0;
   P.light_model = R->light_model;
-  P.cell_dist = R->cell_skip ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
+  P.cell_dist = (R->cell_skip && !color) ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
   P.trans_scale = trans_scale;
+  P.step_scale = step_scale;
   const float mg = float(V->max_grad);
   P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;  // GLRenderer.cpp:1840-1841
-  P.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  P.inv_max_raw = V->bytes == 2 ? 1.0f / 65535.0f : 1.0f / 255.0f;
   for (int a = 0; a < 3; ++a) {
     // GLRenderer.cpp:2890-2893: colour.xyz * colour.w
     P.light_a[a] = R->ambient[a] * R->ambient[3];
@@ -1136,10 +1196,10 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   R->stats.bricks_total = nbl;
   CvComposeParams cv;
   std::memset(&cv, 0, sizeof(cv));
-  if (iso_mode && R->cv_on) {
+  if (iso_mode && R->cv_on && !color) {  // GLRaycaster::SupportsClearView: scalar data
     // GLRaycaster.cpp:571-575 (GetNormalizedCVIsovalue: isovalue / 2^bits)
     P.cv_on = 1;
-    P.cv_iso = float(double(R->cv_iso) / double(1u << (8 * V->bytes)));
+    P.cv_iso = float(double(R->cv_iso) / double(1u << cbits));
     P.cv_cell_skip = P.cv_iso >= iso_norm ? 1 : 0;
     R->d_cvhits.ensure(size_t(rw) * rh * 4 * sizeof(float4));
     P.cv_hits = R->d_cvhits.as<float4>();
@@ -1373,6 +1433,7 @@ void paint_batch(tvk_batch* B, tvk_renderer* const* rs, uint32_t n) {
       if (rs[j] == rs[i]) fail(TVK_ERR_INVALID_ARG, "a renderer appears twice in the batch");
     if (rs[i]->cv_on && rs[i]->mode == TVK_RM_ISOSURFACE)
       fail(TVK_ERR_UNSUPPORTED, "ClearView frames are painted one at a time (tvk_paint)");
+    if (rs[i]->vol) require_scalar(rs[i]->vol, "batches");
   }
   // plan every frame on its renderer's stream, then order the batch stream after them
   std::vector<PlannedFrame> F;
@@ -1631,6 +1692,7 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   if (R->device != N->device) fail(TVK_ERR_INVALID_ARG, "renderer and network on other devices");
   if (R->cv_on && R->mode == TVK_RM_ISOSURFACE)
     fail(TVK_ERR_UNSUPPORTED, "the learned reconstruction does not take ClearView frames");
+  if (R->vol) require_scalar(R->vol, "the learned reconstruction");
   TVK_CUDA(cudaSetDevice(R->device));
   cudaStream_t s = R->stream;
   TVK_CUDA(cudaEventRecord(N->ev[0], s));
@@ -2165,7 +2227,7 @@ tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out) {
       out->brick_size[a] = v->brick_size[a];
     }
     out->dtype = v->dtype;
-    out->bit_width = 8u * v->bytes;
+    out->bit_width = v->dtype == TVK_RGBA8 ? 8u : 8u * v->bytes;  // per channel
     out->overlap = v->overlap;
     out->lod_count = uint32_t(v->lods.size());
     out->lod0_bricks = v->n_bricks;
@@ -2237,6 +2299,7 @@ tvk_status tvk_volume_get_histogram(const tvk_volume* v, uint64_t* host_out, siz
                                     uint64_t* trimmed_len) {
   return guarded([&] {
     REQUIRE(v && host_out, "null argument");
+    tvk::require_scalar(v, "histograms");
     std::memset(host_out, 0, bins * sizeof(uint64_t));
     const size_t n = std::min(bins, v->hist.size());
     for (size_t i = 0; i < n; ++i) host_out[i] = v->hist[i];
@@ -2249,6 +2312,7 @@ tvk_status tvk_volume_get_histogram2d(const tvk_volume* v, uint64_t* host_out, s
                                       float* max_gradient) {
   return guarded([&] {
     REQUIRE(v && host_out, "null argument");
+    tvk::require_scalar(v, "histograms");
     if (v->rebricked)
       tvk::fail(TVK_ERR_UNSUPPORTED,
                 "a rebricked volume forwards its histograms to the source volume; query that");
@@ -2269,6 +2333,7 @@ tvk_status tvk_volume_get_brick_histograms(const tvk_volume* v, uint32_t* host_o
                                            size_t n_bricks, uint32_t* shift) {
   return guarded([&] {
     REQUIRE(v && host_out, "null argument");
+    tvk::require_scalar(v, "histograms");
     if (v->rebricked)
       tvk::fail(TVK_ERR_UNSUPPORTED, "per-brick histograms exist for bricked source volumes only");
     REQUIRE(n_bricks >= v->n_bricks, "output holds fewer bricks than the volume");
@@ -2282,6 +2347,7 @@ tvk_status tvk_volume_rebrick(const tvk_volume* src, const uint32_t brick_size[3
   return guarded([&] {
     REQUIRE(src && brick_size && out, "null argument");
     *out = nullptr;
+    tvk::require_scalar(src, "rebricking");
     *out = tvk::rebrick_volume(src, brick_size, minmax_mode);
   });
 }
@@ -2466,6 +2532,15 @@ tvk_status tvk_set_colors(tvk_renderer* r, const float ambient[4], const float d
       r->specular[a] = specular[a];
     }
     for (int a = 0; a < 3; ++a) r->light_dir[a] = light_dir[a];
+  });
+}
+
+tvk_status tvk_set_scaling_method(tvk_renderer* r, tvk_scaling_method method) {
+  return guarded([&] {
+    REQUIRE(r, "null argument");
+    REQUIRE(method == TVK_SCALE_BIT_WIDTH || method == TVK_SCALE_BIAS_AND_SCALE,
+            "unknown scaling method");
+    r->tf_scaling = method;
   });
 }
 
@@ -3014,6 +3089,7 @@ tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_
                            tvk_pool** out) {
   return guarded([&] {
     REQUIRE(v && out, "null argument");
+    tvk::require_scalar(v, "the GridLeaper pool");
     if (v->rebricked) tvk::fail(TVK_ERR_UNSUPPORTED, "pools are built over bricked volumes");
     const size_t n_lods = v->lod_first.size() - 1;
     if (n_lods != v->lods.size())

@@ -133,6 +133,30 @@ brick_lod0_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
     if (gh[i]) atomicAdd(&sc.hist[i], (unsigned long long)gh[i]);
 }
 
+// Colour (RGBA8) volumes: the LOD-0 bricks with their ghost voxels (zero or
+// clamp-to-edge), one 4-byte RGBA voxel per texel, no statistics.
+__global__ void __launch_bounds__(kThreads)
+brick_copy4_kernel(const uint32_t* __restrict__ raw, BrickGrid g,
+                   const uint64_t* __restrict__ offsets, const uint32_t* __restrict__ sizes,
+                   uint32_t* __restrict__ pool, uint32_t z_chunk) {
+  const uint32_t b = blockIdx.x;
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
+  const uint32_t z0 = blockIdx.y * z_chunk;
+  const uint32_t z1 = min(bs[2], z0 + z_chunk);
+  if (z0 >= z1) return;
+  uint32_t* out = pool + offsets[b];
+  const uint32_t sxy = bs[0] * bs[1];
+  const uint32_t n = (z1 - z0) * sxy;
+  for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+    const uint32_t k = z0 + t / sxy;
+    const uint32_t r = t - (k - z0) * sxy;
+    const uint32_t j = r / bs[0];
+    const uint32_t i = r - j * bs[0];
+    out[uint64_t(k) * sxy + r] = source_voxel<uint32_t>(raw, g, c, bs, i, j, k);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
@@ -291,6 +315,17 @@ void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g, const uin
     brick_lod0_kernel<uint16_t><<<grid, kThreads, smem, s>>>(
         static_cast<const uint16_t*>(raw), g, d_offsets, d_sizes, static_cast<uint16_t*>(pool),
         sc, hist_shift, smem_bins, z_chunk);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_brick_copy4(const void* raw, const BrickGrid& g, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, void* pool, cudaStream_t s,
+                        uint64_t* launches) {
+  const uint32_t z_chunk = 8;
+  const dim3 grid(uint32_t(n_bricks), (g.B[2] + z_chunk - 1) / z_chunk);
+  brick_copy4_kernel<<<grid, kThreads, 0, s>>>(static_cast<const uint32_t*>(raw), g, d_offsets,
+                                               d_sizes, static_cast<uint32_t*>(pool), z_chunk);
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }

@@ -16,6 +16,7 @@
 // but that cannot change the pixel is skipped: gradients and lighting of samples
 // whose corrected alpha is 0 (their compositing adds exactly zero).
 #include <cuda_fp16.h>
+#include <type_traits>
 
 #include "tvk_internal.h"
 
@@ -74,6 +75,62 @@ struct BrickView {
     return fmaf(fz, c1 - c0, c0);
   }
 };
+
+// RGBA8 bricks (colour volumes, four unsigned-normalised channels): every
+// channel filtered exactly like the scalar lookup.
+struct ColorView {
+  const uchar4* __restrict__ p;
+  int n0, n1, n2;
+  float fn0, fn1, fn2;
+  uint32_t sx, sxy;
+
+  __device__ __forceinline__ uchar4 fetch(int x, int y, int z) const {
+    return __ldg(p + (size_t(x) + size_t(y) * sx + size_t(z) * sxy));
+  }
+  __device__ __forceinline__ static float tri(float fx, float fy, float fz, float v000,
+                                              float v100, float v010, float v110, float v001,
+                                              float v101, float v011, float v111) {
+    const float c00 = fmaf(fx, v100 - v000, v000);
+    const float c10 = fmaf(fx, v110 - v010, v010);
+    const float c01 = fmaf(fx, v101 - v001, v001);
+    const float c11 = fmaf(fx, v111 - v011, v011);
+    const float c0 = fmaf(fy, c10 - c00, c00);
+    const float c1 = fmaf(fy, c11 - c01, c01);
+    return fmaf(fz, c1 - c0, c0);
+  }
+  // channel mask: bit c set = filter channel c (others returned as 0); raw units
+  template <int kMask>
+  __device__ __forceinline__ float4 sample_raw(float tx, float ty, float tz) const {
+    const float u0 = fminf(fmaxf(fmaf(tx, fn0, -0.5f), 0.0f), float(n0 - 1));
+    const float u1 = fminf(fmaxf(fmaf(ty, fn1, -0.5f), 0.0f), float(n1 - 1));
+    const float u2 = fminf(fmaxf(fmaf(tz, fn2, -0.5f), 0.0f), float(n2 - 1));
+    const int x0 = int(u0), y0 = int(u1), z0 = int(u2);
+    const float fx = u0 - float(x0), fy = u1 - float(y0), fz = u2 - float(z0);
+    const int x1 = min(x0 + 1, n0 - 1), y1 = min(y0 + 1, n1 - 1), z1 = min(z0 + 1, n2 - 1);
+    const uchar4 a = fetch(x0, y0, z0), b = fetch(x1, y0, z0), c = fetch(x0, y1, z0),
+                 d = fetch(x1, y1, z0), e = fetch(x0, y0, z1), f = fetch(x1, y0, z1),
+                 g = fetch(x0, y1, z1), h = fetch(x1, y1, z1);
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (kMask & 1)
+      r.x = tri(fx, fy, fz, a.x, b.x, c.x, d.x, e.x, f.x, g.x, h.x);
+    if (kMask & 2)
+      r.y = tri(fx, fy, fz, a.y, b.y, c.y, d.y, e.y, f.y, g.y, h.y);
+    if (kMask & 4)
+      r.z = tri(fx, fy, fz, a.z, b.z, c.z, d.z, e.z, f.z, g.z, h.z);
+    if (kMask & 8)
+      r.w = tri(fx, fy, fz, a.w, b.w, c.w, d.w, e.w, f.w, g.w, h.w);
+    return r;
+  }
+};
+
+__device__ __forceinline__ ColorView color_view(const RenderParams& P, const DevBrick& b) {
+  ColorView v;
+  v.p = static_cast<const uchar4*>(P.pool) + b.off;
+  v.n0 = int(b.n[0]); v.n1 = int(b.n[1]); v.n2 = int(b.n[2]);
+  v.fn0 = float(b.n[0]); v.fn1 = float(b.n[1]); v.fn2 = float(b.n[2]);
+  v.sx = b.n[0]; v.sxy = b.n[0] * b.n[1];
+  return v;
+}
 
 // Footprint of a centre sample, kept so the six central-difference lookups
 // (each one voxel away along one axis) reuse its index math and its voxels.
@@ -414,6 +471,7 @@ struct IsoHit {
   float f;       // interpolation parameter (alpha of the hit buffer)
   float n[3];
   float depth;
+  float enc_r, enc_gb;  // colour volumes: the packed hit colour
 };
 
 //
@@ -603,6 +661,194 @@ __device__ __forceinline__ float4 iso_compose(const RenderParams& P, const IsoHi
   return make_float4(c[0], c[1], c[2], 1.0f);
 }
 
+// Normal from the red channel's central differences (Volume3D.glsl:43-60:
+// sampleVolume(...).x of a colour volume), in eye space, safely normalised.
+__device__ __forceinline__ void color_normal(const RenderParams& P, const ColorView& vol,
+                                             const float pos[3], float N[3]) {
+  const float vs0 = 1.0f / vol.fn0, vs1 = 1.0f / vol.fn1, vs2 = 1.0f / vol.fn2;
+  const float im = P.inv_max_raw;
+  const float xp = vol.sample_raw<1>(pos[0] + vs0, pos[1], pos[2]).x * im;
+  const float xm = vol.sample_raw<1>(pos[0] + (-vs0), pos[1], pos[2]).x * im;
+  const float yp = vol.sample_raw<1>(pos[0], pos[1] + (-vs1), pos[2]).x * im;
+  const float ym = vol.sample_raw<1>(pos[0], pos[1] + vs1, pos[2]).x * im;
+  const float zp = vol.sample_raw<1>(pos[0], pos[1], pos[2] + vs2).x * im;
+  const float zm = vol.sample_raw<1>(pos[0], pos[1], pos[2] + (-vs2)).x * im;
+  const float gs0 = ((xm - xp) / 2.0f) * P.domain_scale[0];
+  const float gs1 = ((yp - ym) / 2.0f) * P.domain_scale[1];
+  const float gs2 = ((zm - zp) / 2.0f) * P.domain_scale[2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    N[r] = fmaf(P.norm_mat[r][2], gs2, fmaf(P.norm_mat[r][1], gs1, P.norm_mat[r][0] * gs0));
+  const float l = len3(N[0], N[1], N[2]);
+  if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+}
+
+// One brick of a colour volume in 1D mode (GLRaycaster-1D-FS /
+// -1D-light-FS with VRender1D-Color.glsl:44-53 / VRender1DLit-Color.glsl:
+// 44-62): the filtered RGBA times the TF entry at (r + g + b) / 3, opacity
+// correction of the product's alpha (P.tf holds uncorrected entries), lit
+// with the product's colour as the diffuse colour.  No macro-cell leaps:
+// colour bricks are never empty (AbstrRenderer::ContainsData).
+__device__ __forceinline__ float4 march_brick_color(const RenderParams& P, const DevBrick& b,
+                                                    const float dir[3], float t_in, float t_out,
+                                                    uint32_t& samples, uint32_t& shaded,
+                                                    uint32_t& graded, float& first_t) {
+  float en[3], ex[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    en[a] = __half2float(__float2half_rn(dir[a] * t_in));
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float q = len / b.step;
+  float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!(q < P.max_q)) {
+    atomicAdd(&P.counters[2], 1ull);
+    return c;
+  }
+  const int n = int(q) + 1;
+  float pos[3], inc[3], epos[3], einc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = (tout[a] - tin[a]) / q;
+    pos[a] = tin[a];
+    epos[a] = en[a];
+  }
+  einc[0] = (dx / len) * b.step;
+  einc[1] = (dy / len) * b.step;
+  einc[2] = (dz / len) * b.step;
+  const ColorView vol = color_view(P, b);
+  const float im = P.inv_max_raw;
+  const float W = float(P.tf_w);
+  const bool lit = P.lighting != 0;
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    ++shaded;
+    const float4 raw = vol.sample_raw<15>(pos[0], pos[1], pos[2]);
+    const float v0 = raw.x * im, v1 = raw.y * im, v2 = raw.z * im, v3 = raw.w * im;
+    const float u = ((v0 + v1) + v2) / 3.0f;
+    float fx = floorf(u * W);
+    fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
+    const float4 t = __ldg(&P.tf[int(fx)]);
+    float4 src = make_float4(v0 * t.x, v1 * t.y, v2 * t.z, v3 * t.w);
+    src.w = 1.0f - powf(1.0f - src.w, P.step_scale);
+    if (lit && src.w != 0.0f) {
+      ++graded;
+      float N[3];
+      color_normal(P, vol, pos, N);
+      const float tfc[3] = {src.x, src.y, src.z};
+      float lc[3];
+      if (P.light_model == TVK_LIGHT_BLINN_PHONG)
+        lighting_bp(P, epos, N, tfc, lc);
+      else
+        lighting_ref(P, epos, N, tfc, lc);
+      src.x = lc[0]; src.y = lc[1]; src.z = lc[2];
+    }
+    if (src.w != 0.0f && first_t == INFINITY) first_t = t_in + float(i) * ((t_out - t_in) / q);
+    const float w = 1.0f - c.w;
+    c.x = fmaf(src.x * w, src.w, c.x);
+    c.y = fmaf(src.y * w, src.w, c.y);
+    c.z = fmaf(src.z * w, src.w, c.z);
+    c.w = fmaf(src.w, w, c.w);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      pos[a] = pos[a] + inc[a];
+      epos[a] = epos[a] + einc[a];
+    }
+    if (c.w >= 0.99f) break;
+  }
+  return c;
+}
+
+// GLRaycaster-Color-FS.glsl for one brick: the first step whose alpha is >=
+// fIsoval, RefineIsosurface.glsl on the red channel (its sampleVolume(...).x),
+// the normal from the red channel, and the colour at the unrefined step,
+// packed as the shader packs it: red + 1 in the hit's alpha, floor(green *
+// 512) + blue in the normal's alpha.
+__device__ __forceinline__ bool iso_brick_color(const RenderParams& P, const DevBrick& b,
+                                                const float dir[3], float t_in, float t_out,
+                                                IsoHit& h, uint32_t& samples,
+                                                uint32_t& shaded) {
+  float en[3], ex[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    en[a] = __half2float(__float2half_rn(dir[a] * t_in));
+    ex[a] = dir[a] * t_out;
+  }
+  const float dx = ex[0] - en[0], dy = ex[1] - en[1], dz = ex[2] - en[2];
+  const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+  float tin[3], tout[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    tin[a] = affine_row(b.tex[a], en[0], en[1], en[2]);
+    tout[a] = affine_row(b.tex[a], ex[0], ex[1], ex[2]);
+  }
+  const float len_tex = len3(tout[0] - tin[0], tout[1] - tin[1], tout[2] - tin[2]);
+  const float q = len / b.step;
+  if (!(q < P.max_q)) return false;
+  const int n = int(q) + 1;
+  float pos[3], inc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    inc[a] = (tout[a] - tin[a]) / q;
+    pos[a] = tin[a];
+  }
+  const ColorView vol = color_view(P, b);
+  const float im = P.inv_max_raw;
+  const float iso = P.iso_norm;
+  bool hit = false;
+  for (int i = 0; i < n; ++i) {
+    ++samples;
+    ++shaded;
+    if (vol.sample_raw<8>(pos[0], pos[1], pos[2]).w * im >= iso) { hit = true; break; }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+  }
+  if (!hit) return false;
+  float d[3], cur[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    d[a] = inc[a] / 2.0f;
+    cur[a] = pos[a] - d[a];
+  }
+  for (int k = 0; k < 5; ++k) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) d[a] = d[a] / 2.0f;
+    const bool above = vol.sample_raw<1>(cur[0], cur[1], cur[2]).x * im >= iso;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cur[a] = above ? cur[a] - d[a] : cur[a] + d[a];
+  }
+  const float4 col = vol.sample_raw<7>(pos[0], pos[1], pos[2]);
+  h.f = len3(cur[0] - tin[0], cur[1] - tin[1], cur[2] - tin[2]) / len_tex;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) h.pos[a] = en[a] * (1.0f - h.f) + ex[a] * h.f;
+  h.depth = P.proj_x + (P.proj_y / -h.pos[2]);
+  color_normal(P, vol, cur, h.n);
+  h.enc_r = col.x * im + 1.0f;
+  h.enc_gb = floorf((col.y * im) * 512.0f) + col.z * im;
+  return true;
+}
+
+// Compose-Color-FS.glsl:60-88: the colour recovered from the two packed
+// channels lights the hit (diffuse = colour * the diffuse light).
+__device__ __forceinline__ float4 iso_compose_color(const RenderParams& P, const IsoHit& h) {
+  const float rgb[3] = {h.enc_r - 1.0f, floorf(h.enc_gb / 2.0f) / 256.0f,
+                        h.enc_gb - floorf(h.enc_gb)};
+  const float n[3] = {h.n[0], h.n[1], fabsf(h.n[2])};
+  float dcol[3], c[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dcol[i] = rgb[i] * P.light_d[i];
+  surface_lighting(h.pos, n, P.light_a, dcol, P.light_s, P.light_dir, c);
+  return make_float4(c[0], c[1], c[2], 1.0f);
+}
+
 constexpr uint32_t kCandChunk = 1024;
 
 // Conservative: can any pixel ray of the 16x8 tile at (tx0, ty0) meet brick b?
@@ -652,6 +898,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
                                             TileShared& sh) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr uint32_t kW = 16 * kRPT;
+  constexpr bool kColor = std::is_same<T, uchar4>::value;  // RGBA8 colour volume
 
   // The host lists the visible bricks in a front-to-back order that holds for
   // every ray (increasing L1 grid distance from the eye's brick cell, which
@@ -750,6 +997,17 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           // once that entry is behind the nearest hit it cannot pass the
           // depth test; bricks come in increasing entry order along the ray.
           const bool settled = have_hit[r] && ti * (1.0f - 2e-3f) - 1e-4f > -best[r].pos[2];
+          if constexpr (kColor) {
+            if (settled) break;
+            IsoHit h;
+            if (iso_brick_color(P, b, dir, ti, tc, h, samples, shaded) &&
+                h.depth < best_depth[r]) {
+              best[r] = h;
+              best_depth[r] = h.depth;
+              have_hit[r] = true;
+            }
+            continue;
+          } else {
           if (!kCV) {
             if (settled) break;
             IsoHit h;
@@ -781,8 +1039,13 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
                                  here ? best[r].f : 0.0f))
             have_focus[r] = true;
           continue;
+          }
         }
-        const float4 col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
+        float4 col;
+        if constexpr (kColor)
+          col = march_brick_color(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
+        else
+          col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
         const float w = 1.0f - frame[r].w;
         frame[r].x = fmaf(col.x, w, frame[r].x);
         frame[r].y = fmaf(col.y, w, frame[r].y);
@@ -802,7 +1065,13 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
     // Compose-FS.glsl:58-61: no hit, or an interpolation parameter of exactly
     // 0, leaves the pixel empty
     float4 out = frame[r];
-    if (iso_mode && have_hit[r] && best[r].f != 0.0f) {
+    if constexpr (kColor) {
+      if (iso_mode && have_hit[r]) {
+        // the packed red + 1 is the hit buffer's alpha: never 0
+        out = iso_compose_color(P, best[r]);
+        first_t[r] = -best[r].pos[2];
+      }
+    } else if (iso_mode && have_hit[r] && best[r].f != 0.0f) {
       if (!kCV) out = iso_compose(P, best[r]);
       first_t[r] = -best[r].pos[2];
     }
@@ -1566,7 +1835,10 @@ void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 grid((p.out_w + tw - 1) / tw, (p.out_h + 7) / 8);
   const bool iso = p.mode == TVK_RM_ISOSURFACE;
   const bool cv = iso && p.cv_on;
-  if (p.bytes == 1) {
+  if (p.bytes == 4) {
+    if (iso) raycast_kernel<uchar4, true><<<grid, block, 0, s>>>(p);
+    else raycast_kernel<uchar4, false><<<grid, block, 0, s>>>(p);
+  } else if (p.bytes == 1) {
     if (cv) raycast_kernel<uint8_t, true, true><<<grid, block, 0, s>>>(p);
     else if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);
     else raycast_kernel<uint8_t, false><<<grid, block, 0, s>>>(p);

@@ -55,6 +55,10 @@ struct BrickGrid {
 
 void launch_raw_minmax(const void* raw, int bytes, uint64_t n, uint32_t* minmax,
                        cudaStream_t s, uint64_t* launches);
+// RGBA8 colour volumes: LOD-0 bricks with ghost voxels only
+void launch_brick_copy4(const void* raw, const BrickGrid& g, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, void* pool, cudaStream_t s,
+                        uint64_t* launches);
 void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g,
                        const uint64_t* d_offsets, const uint32_t* d_sizes, uint64_t n_bricks,
                        void* pool, const BrickScratch& sc, uint32_t hist_shift,
@@ -177,7 +181,7 @@ void launch_cell_dist(const CellDistParams& p, const uint32_t max_lines[3], uint
 
 struct RenderParams {
   const void* pool;
-  int bytes;                 // 1 or 2
+  int bytes;                 // 1 or 2 (scalar), 4 (RGBA8 colour volume)
   const DevBrick* bricks;    // visible bricks only, compact
   uint32_t n_bricks;
   const uint8_t* cell_dist;    // macro-cell distances (null: no skipping inside bricks)
@@ -218,6 +222,7 @@ struct RenderParams {
   float cv_iso;              // the focus surface's fIsoval (GetNormalizedCVIsovalue)
   int cv_cell_skip;          // cell distances hold for cv_iso too (cv_iso >= iso_norm)
   float4* cv_hits;
+  float step_scale;          // fStepScale (colour volumes correct opacity per sample)
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
 };
 

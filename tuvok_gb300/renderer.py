@@ -50,13 +50,15 @@ class Volume:
                  (self.LOD0_ONLY if lod0_only else 0))
         if isinstance(data, np.ndarray):
             arr = np.ascontiguousarray(data)
-            if arr.dtype == np.uint8:
+            if arr.dtype == np.uint8 and arr.ndim == 4 and arr.shape[3] == 4:
+                dt = N.TVK_RGBA8  # colour volume [z, y, x, rgba]
+            elif arr.dtype == np.uint8 and arr.ndim == 3:
                 dt = N.TVK_U8
-            elif arr.dtype == np.uint16:
+            elif arr.dtype == np.uint16 and arr.ndim == 3:
                 dt = N.TVK_U16
             else:
-                raise TypeError("volumes are uint8 or uint16")
-            z, y, x = arr.shape
+                raise TypeError("volumes are uint8 or uint16 [z, y, x], or uint8 [z, y, x, 4] RGBA")
+            z, y, x = arr.shape[:3]
             check(lib().tvk_volume_create_ex(arr.ctypes.data_as(C.c_void_p), dt,
                                              _u64((x, y, z)), bs, overlap, flags, C.byref(h)))
         else:
@@ -87,7 +89,7 @@ class Volume:
     # ---- dataset interface (IO/Dataset.h, IO/BrickedDataset.h)
     @property
     def np_dtype(self):
-        return np.uint8 if self.info.dtype == N.TVK_U8 else np.uint16
+        return np.uint16 if self.info.dtype == N.TVK_U16 else np.uint8
 
     def GetDomainSize(self, lod=0):
         s, b = _u64((0, 0, 0)), _u64((0, 0, 0))
@@ -119,10 +121,12 @@ class Volume:
         return md
 
     def GetBrick(self, key):
-        """Brick voxels (ghost included) as a numpy array [z, y, x]."""
+        """Brick voxels (ghost included) as a numpy array [z, y, x] ([z, y, x, 4]
+        for a colour volume)."""
         md = self.GetBrickMetadata(key)
         nx, ny, nz = md.n_voxels
-        out = np.empty((nz, ny, nx), dtype=self.np_dtype)
+        shape = (nz, ny, nx, 4) if self.info.dtype == N.TVK_RGBA8 else (nz, ny, nx)
+        out = np.empty(shape, dtype=self.np_dtype)
         ts, lod, idx = key
         check(lib().tvk_volume_get_brick(self._h, ts, lod, idx, out.ctypes.data_as(C.c_void_p),
                                          out.nbytes))
@@ -294,6 +298,13 @@ class Renderer:
 
     def DisableClipPlane(self):
         self.EnableClipPlane(False)
+
+    SMETH_BIT_WIDTH, SMETH_BIAS_AND_SCALE = 0, 1
+
+    def SetScalingMethod(self, method):
+        """AbstrRenderer::SetScalingMethod: the 1D TF coordinate scale
+        (SMETH_BIAS_AND_SCALE: value * (|min| + |max|), as GLRaycaster computes it)."""
+        check(lib().tvk_set_scaling_method(self._h, int(method)))
 
     # ClearView (AbstrRenderer::SetCV and its parameters): in iso mode a focus
     # isosurface is revealed behind the context surface around a focus point.
