@@ -162,6 +162,23 @@ enum {
 tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint64_t dims[3],
                                 const uint32_t brick_size[3], uint32_t overlap, uint32_t flags,
                                 tvk_volume** out);
+/* Opens the ExtendedOctree brick container that Tuvok's converter writes
+ * (ExtendedOctreeConverter::Convert) and a UVF file's TOC block holds, at byte
+ * `offset` of `path` (ExtendedOctree::Open, IO/UVF/ExtendedOctree/
+ * ExtendedOctree.cpp:67-172; headers of UVF version >= 5).  Bricks are read at
+ * their table-of-contents offsets in any on-disk layout (scanline, Morton,
+ * Hilbert, random) and expanded from LZ4 where stored so (GetBrickData,
+ * :313-361); zlib, LZMA and bzip2 bricks return TVK_ERR_UNSUPPORTED.
+ * 1-component uint8 / uint16 and 4-component uint8 (TVK_RGBA8) volumes with a
+ * 1:1:1 aspect.  The volume is rebuilt on the GPU from the LOD-0 bricks' inner
+ * voxels (statistics, histograms, coarser LODs) and every brick the file holds
+ * must equal the rebuild byte for byte: the rebuild starts from `flags`
+ * (TVK_VOLUME_CLAMP_TO_EDGE, TVK_VOLUME_MEDIAN, TVK_VOLUME_LOD0_ONLY) and tries
+ * the other border and filter settings, which the header does not record;
+ * a file that matches none returns TVK_ERR_INVALID_ARG. */
+tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
+                                           uint32_t uvf_version, uint32_t flags,
+                                           tvk_volume** out);
 tvk_status tvk_volume_destroy(tvk_volume* v);
 tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out);
 

@@ -52,6 +52,16 @@ class BrickedVolume {
                                &v->v_));
     return v;
   }
+  // ExtendedOctree::Open over a converter-written brick file (uncompressed or
+  // LZ4 bricks; tvk_volume_open_extended_octree)
+  static std::unique_ptr<BrickedVolume> OpenExtendedOctree(const std::string& path,
+                                                           uint64_t offset = 0,
+                                                           uint32_t uvf_version = 5,
+                                                           uint32_t flags = 0) {
+    std::unique_ptr<BrickedVolume> v(new BrickedVolume());
+    check(tvk_volume_open_extended_octree(path.c_str(), offset, uvf_version, flags, &v->v_));
+    return v;
+  }
   // DynamicBrickingDS over this volume (tvk_volume_rebrick)
   static std::unique_ptr<BrickedVolume> Rebrick(const BrickedVolume& src,
                                                 std::array<uint32_t, 3> brick_size,

@@ -67,6 +67,37 @@ void* ref_convert(const void* raw, int dtype, const uint64_t dims[3], const uint
   return t;
 }
 
+// Writes the converter's ExtendedOctree file for a flat volume: dtype 0 =
+// uint8, 1 = uint16; `components` per voxel; compression 0 = none, 3 = LZ4
+// (level 1 = LZ4_compress, > 1 = LZ4 HC); layout 0..3 = scanline, Morton,
+// Hilbert, random.  Returns 1 on success.
+int ref_write_eo(const void* raw, int dtype, uint64_t components, const uint64_t dims[3],
+                 const uint32_t brick_size[3], uint32_t overlap, int clamp_to_edge, int median,
+                 int compression, uint32_t level, int layout, const char* out_path,
+                 const char* scratch_dir) {
+  const size_t bytes = (dtype == 0 ? 1 : 2) * components;
+  const uint64_t n = dims[0] * dims[1] * dims[2];
+  const std::string in_path = std::string(scratch_dir) + "/tvk_ref_eo_in.raw";
+  {
+    FILE* f = std::fopen(in_path.c_str(), "wb");
+    if (!f) return 0;
+    std::fwrite(raw, bytes, n, f);
+    std::fclose(f);
+  }
+  tuvok::QuietOut quiet;
+  BrickStatVec stats;  // Convert requires somewhere to put them
+  ExtendedOctreeConverter conv(UINT64VECTOR3(brick_size[0], brick_size[1], brick_size[2]),
+                               overlap, 256ull << 20, quiet);
+  const bool ok = conv.Convert(in_path, 0,
+                               dtype == 0 ? ExtendedOctree::CT_UINT8 : ExtendedOctree::CT_UINT16,
+                               components, UINT64VECTOR3(dims[0], dims[1], dims[2]),
+                               DOUBLEVECTOR3(1, 1, 1), out_path, 0, &stats,
+                               COMPRESSION_TYPE(compression), level, median != 0,
+                               clamp_to_edge != 0, LAYOUT_TYPE(layout));
+  std::remove(in_path.c_str());
+  return ok ? 1 : 0;
+}
+
 uint64_t ref_brick_count(void* h) { return static_cast<RefTree*>(h)->coords.size(); }
 
 uint64_t ref_lod_count(void* h) { return static_cast<RefTree*>(h)->tree.GetLODCount(); }

@@ -1,0 +1,91 @@
+"""tvk_volume_open_extended_octree over the converter-written fixtures
+(tests/golden/eo, made by the reference's ExtendedOctreeConverter): the
+loaded volume equals the one bricked from the same voxels -- every brick of
+every LOD, the statistics and a rendered frame -- whatever flags the caller
+guesses; malformed files are refused without touching the GPU state."""
+import json
+import shutil
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tuvok_gb300 import Renderer, TvkError, Volume
+from test_gpu_render import ramp_tf
+
+pytestmark = pytest.mark.gpu
+
+EO = Path(__file__).resolve().parent / "golden" / "eo"
+CASES = json.loads((EO / "cases.json").read_text())
+
+
+def direct(case):
+    raw = np.load(EO / f"{case['name']}.npy")
+    return raw, Volume(raw, brick_size=case["brick_size"], overlap=case["overlap"],
+                       clamp_to_edge=case["clamp"], median=case["median"])
+
+
+def all_keys(v):
+    return [(0, lod, k) for lod in range(v.GetLODLevelCount())
+            for k in range(v.GetBrickCount(lod))]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+@pytest.mark.parametrize("guess", ["right", "wrong"])
+def test_gpu_eo_matches_direct_bricking(cuda_ok, case, guess):
+    raw, ref = direct(case)
+    flip = guess == "wrong"
+    v = Volume.FromExtendedOctree(EO / f"{case['name']}.eo",
+                                  clamp_to_edge=case["clamp"] ^ flip,
+                                  median=case["median"] ^ flip)
+    color = case["components"] == 4
+    keys = [(0, 0, k) for k in range(ref.GetBrickCount(0))] if color else all_keys(ref)
+    for key in keys:
+        np.testing.assert_array_equal(v.GetBrick(key), ref.GetBrick(key), err_msg=str(key))
+        mm, mr = v.MaxMinForKey(key), ref.MaxMinForKey(key)
+        assert (mm.min_scalar, mm.max_scalar) == (mr.min_scalar, mr.max_scalar)
+    assert v.GetRange() == ref.GetRange()
+    assert v.MaxGradientMagnitude() == ref.MaxGradientMagnitude()
+    imgs = []
+    for vol in (v, ref):
+        r = Renderer()
+        r.RegisterDataset(vol)
+        r.Set1DTransFloat(ramp_tf(256 if case["dtype"] == "u8" else 1024))
+        r.SetUseLighting(True)
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=(0.4, 0.3, 1.4))
+        r.Resize(48, 40)
+        r.Paint()
+        imgs.append(r.ReadBackPixels().copy())
+    np.testing.assert_array_equal(imgs[0], imgs[1])
+
+
+def test_gpu_eo_refuses_malformed_files(cuda_ok, tmp_path):
+    with pytest.raises(TvkError):
+        Volume.FromExtendedOctree(tmp_path / "missing.eo")
+    src = EO / "u8_none_scanline.eo"
+    with pytest.raises(TvkError):
+        Volume.FromExtendedOctree(src, uvf_version=4)
+    data = src.read_bytes()
+    short = tmp_path / "short.eo"
+    short.write_bytes(data[: len(data) // 2])
+    with pytest.raises(TvkError):
+        Volume.FromExtendedOctree(short)
+    # a flipped voxel: no rebuild matches
+    bad = bytearray(data)
+    bad[-100] ^= 0x5A
+    (tmp_path / "bad.eo").write_bytes(bytes(bad))
+    with pytest.raises(TvkError):
+        Volume.FromExtendedOctree(tmp_path / "bad.eo")
+    # a corrupt LZ4 stream: the bounded decoder refuses it
+    lz = bytearray((EO / "u8_lz4hc_hilbert.eo").read_bytes())
+    for i in range(len(lz) - 4000, len(lz), 7):
+        lz[i] = 0xFF
+    (tmp_path / "lz.eo").write_bytes(bytes(lz))
+    with pytest.raises(TvkError):
+        Volume.FromExtendedOctree(tmp_path / "lz.eo")
+    # the same file at an offset inside a larger file (a UVF TOC block)
+    wrapped = tmp_path / "wrapped.bin"
+    wrapped.write_bytes(b"\0" * 123 + data)
+    v = Volume.FromExtendedOctree(wrapped, offset=123)
+    assert v.GetBrickCount(0) > 1
+    shutil.rmtree(tmp_path, ignore_errors=True)

@@ -171,6 +171,8 @@ PROTOTYPES = {
     "tvk_set_clip_plane": [_vp, _f32p],
     "tvk_enable_clip_plane": [_vp, C.c_int],
     "tvk_set_scaling_method": [_vp, C.c_int],
+    "tvk_volume_open_extended_octree": [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32,
+                                        C.POINTER(_vp)],
     "tvk_set_clearview": [_vp, C.c_int],
     "tvk_set_cv_isovalue": [_vp, C.c_float],
     "tvk_set_cv_color": [_vp, _f32p],

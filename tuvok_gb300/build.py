@@ -29,7 +29,8 @@ HOST_FLAGS = "-fPIC,-ffp-contract=off,-O3,-Wall"
 # per-file extra flags: the ray march keeps every multiply and add separate
 # unless the source writes fmaf, so it matches the oracle bit for bit
 EXTRA = {"raycast.cu": ["-fmad=false"]}
-SOURCES = ["api.cpp", "bricking.cu", "cnn.cu", "lod.cu", "raycast.cu", "rebrick.cu", "volgen.cu"]
+SOURCES = ["api.cpp", "bricking.cu", "cnn.cu", "eo.cpp", "lod.cu", "raycast.cu", "rebrick.cu",
+           "volgen.cu"]
 HEADERS = [CSRC / "tvk_internal.h", ROOT / "include" / "tvk.h"]
 ORACLE_SOURCES = [ROOT / "oracle" / "bricking.cpp", ROOT / "oracle" / "raycast.cpp",
                   ROOT / "oracle" / "rebrick.cpp"]

@@ -2210,6 +2210,86 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
   });
 }
 
+tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
+                                           uint32_t uvf_version, uint32_t flags,
+                                           tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(path && out, "null argument");
+    *out = nullptr;
+    tvk::EoFile e;
+    tvk::eo_open(path, offset, uvf_version, e);
+    tvk_dtype dt;
+    if (e.component_type == 0 && e.components == 1) dt = TVK_U8;
+    else if (e.component_type == 1 && e.components == 1) dt = TVK_U16;
+    else if (e.component_type == 0 && e.components == 4) dt = TVK_RGBA8;
+    else
+      tvk::fail(TVK_ERR_UNSUPPORTED,
+                "ExtendedOctree: 1-component uint8 / uint16 and 4-component uint8 volumes only");
+    if (e.normals) tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: precomputed normals");
+    if (e.aspect[0] != 1.0 || e.aspect[1] != 1.0 || e.aspect[2] != 1.0)
+      tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: volume aspect other than 1:1:1");
+    const uint32_t bs[3] = {uint32_t(e.brick_size[0]), uint32_t(e.brick_size[1]),
+                            uint32_t(e.brick_size[2])};
+    const uint32_t ov = e.overlap;
+    const size_t vb = size_t(dt == TVK_U16 ? 2 : 1) * e.components;  // bytes per voxel
+    // the flat volume from the LOD-0 bricks' inner voxels
+    const std::vector<tvk::LodInfo> lods = tvk::lod_table(e.dims, bs, ov);
+    std::vector<tvk_brick_md> md0;
+    tvk::brick_metadata(lods[0], bs, ov, md0);
+    std::vector<uint8_t> raw(size_t(e.dims[0] * e.dims[1] * e.dims[2]) * vb), brick;
+    const uint64_t core[3] = {bs[0] - 2ull * ov, bs[1] - 2ull * ov, bs[2] - 2ull * ov};
+    for (uint64_t k = 0; k < md0.size(); ++k) {
+      const uint32_t* n = md0[k].n_voxels;
+      tvk::eo_read_brick(e, k, size_t(n[0]) * n[1] * n[2] * vb, brick);
+      const uint64_t c[3] = {k % lods[0].bricks[0], (k / lods[0].bricks[0]) % lods[0].bricks[1],
+                             k / (lods[0].bricks[0] * lods[0].bricks[1])};
+      for (uint32_t z = ov; z + ov < n[2]; ++z)
+        for (uint32_t y = ov; y + ov < n[1]; ++y) {
+          const uint64_t gx = c[0] * core[0], gy = c[1] * core[1] + (y - ov),
+                         gz = c[2] * core[2] + (z - ov);
+          std::memcpy(raw.data() + ((gz * e.dims[1] + gy) * e.dims[0] + gx) * vb,
+                      brick.data() + ((size_t(z) * n[1] + y) * n[0] + ov) * vb,
+                      size_t(n[0] - 2 * ov) * vb);
+        }
+    }
+    // Rebuild with the given border and filter settings first, then the other
+    // three; keep the first rebuild whose every brick equals the file's (the
+    // header records neither setting).
+    const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0 || dt == TVK_RGBA8;
+    const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
+               median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && dt != TVK_RGBA8;
+    std::vector<uint8_t> dev;
+    auto drop = [](tvk_volume* v) {
+      tvk::free_volume_device(v);
+      delete v;
+    };
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      const bool clamp = clamp0 ^ ((attempt & 1) != 0), median = median0 ^ ((attempt & 2) != 0);
+      if (median && (lod0_only || dt == TVK_RGBA8)) continue;
+      std::unique_ptr<tvk_volume, decltype(drop)> V(
+          tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
+                             !lod0_only),
+          drop);
+      bool same = true;
+      for (uint64_t k = 0; k < V->total_bricks && same; ++k) {
+        const size_t nb = size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
+        tvk::eo_read_brick(e, k, nb, brick);
+        dev.resize(nb);
+        TVK_CUDA(cudaMemcpy(dev.data(), static_cast<const uint8_t*>(V->d_pool) + V->offsets[k] * vb,
+                            nb, cudaMemcpyDeviceToHost));
+        same = std::memcmp(dev.data(), brick.data(), nb) == 0;
+      }
+      if (same) {
+        *out = V.release();
+        return;
+      }
+    }
+    tvk::fail(TVK_ERR_INVALID_ARG,
+              "ExtendedOctree: the file's bricks differ from every rebuild of its LOD-0 data "
+              "(mean or median LODs, zero or clamped borders)");
+  });
+}
+
 tvk_status tvk_volume_destroy(tvk_volume* v) {
   return guarded([&] {
     if (!v) return;

@@ -1,0 +1,155 @@
+// ExtendedOctree files: the brick container Tuvok's converter writes and its
+// UVF TOC block holds (IO/UVF/ExtendedOctree/ExtendedOctree.cpp:67-172 Open,
+// :313-361 GetBrickData).  Host code: the header and brick table of contents
+// are parsed, bricks are read at their TOC offsets and expanded when they are
+// LZ4 blocks; the ABI entry in api.cpp rebuilds the volume from the LOD-0
+// bricks and checks every stored brick against the rebuild.
+
+#include <cstdio>
+#include <cstring>
+
+#include "tvk_internal.h"
+
+namespace tvk {
+
+namespace {
+
+struct File {
+  std::FILE* f = nullptr;
+  explicit File(const char* path) : f(std::fopen(path, "rb")) {}
+  ~File() {
+    if (f) std::fclose(f);
+  }
+};
+
+void seek(std::FILE* f, uint64_t pos) {
+  if (fseeko(f, off_t(pos), SEEK_SET) != 0) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: seek failed");
+}
+
+template <class T>
+T read_value(std::FILE* f) {
+  T v;
+  if (std::fread(&v, sizeof(T), 1, f) != 1)
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: file ends inside the header");
+  return v;
+}
+
+}  // namespace
+
+// LZ4 block format (the public format LZ4_compress / LZ4_compressHC2 write and
+// LZ4_decompress_fast reads, Lz4Compression.cpp:13-69): sequences of a token
+// (literal count in the high nibble, match length - 4 in the low nibble, 15
+// meaning "more length bytes follow, each 255 continuing"), the literals, and
+// a 2-byte little-endian back offset; the last sequence ends with literals.
+// Every read and write is bounds-checked; returns the input bytes consumed.
+size_t lz4_decode_block(const uint8_t* src, size_t src_len, uint8_t* dst, size_t dst_len) {
+  size_t i = 0, o = 0;
+  auto bad = [] { fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: corrupt LZ4 brick"); };
+  auto more = [&](size_t n) {
+    for (;;) {
+      if (i >= src_len) bad();
+      const uint8_t b = src[i++];
+      n += b;
+      if (b != 255) return n;
+    }
+  };
+  for (;;) {
+    if (i >= src_len) bad();
+    const uint8_t token = src[i++];
+    size_t lit = token >> 4;
+    if (lit == 15) lit = more(lit);
+    if (lit > src_len - i || lit > dst_len - o) bad();
+    std::memcpy(dst + o, src + i, lit);
+    i += lit;
+    o += lit;
+    if (o == dst_len) return i;
+    if (src_len - i < 2) bad();
+    const size_t off = size_t(src[i]) | (size_t(src[i + 1]) << 8);
+    i += 2;
+    if (off == 0 || off > o) bad();
+    size_t ml = token & 15u;
+    if (ml == 15) ml = more(ml);
+    ml += 4;
+    if (ml > dst_len - o) bad();
+    for (size_t k = 0; k < ml; ++k, ++o) dst[o] = dst[o - off];  // may overlap
+    if (o == dst_len) return i;
+  }
+}
+
+void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e) {
+  File fh(path);
+  if (!fh.f) fail(TVK_ERR_INVALID_ARG, std::string("cannot open ") + path);
+  std::FILE* f = fh.f;
+  e.path = path;
+  e.base = offset;
+  seek(f, offset);
+  // ExtendedOctree.cpp:91-118: the global header, in the writer's byte order
+  // (both are little-endian here)
+  e.component_type = read_value<uint32_t>(f);
+  e.components = read_value<uint64_t>(f);
+  e.normals = read_value<uint8_t>(f) != 0;
+  for (int a = 0; a < 3; ++a) e.dims[a] = read_value<uint64_t>(f);
+  for (int a = 0; a < 3; ++a) e.aspect[a] = read_value<double>(f);
+  for (int a = 0; a < 3; ++a) e.brick_size[a] = read_value<uint64_t>(f);
+  e.overlap = read_value<uint32_t>(f);
+  // UVF files up to version 4 hold an older header (no version field, 32-bit
+  // brick sizes by ExtendedOctree::ComputeHeaderSize) that Open itself does
+  // not parse consistently; those are refused
+  if (uvf_version <= 4)
+    fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: headers of UVF versions <= 4 are not read");
+  e.version = read_value<uint32_t>(f);
+  if (e.version == 0) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: version 0");
+  e.size = read_value<uint64_t>(f);
+  e.compression_level = e.version > 1 ? read_value<uint32_t>(f) : 0;
+  const double asp = e.aspect[0] * e.aspect[1] * e.aspect[2];
+  if (e.components == 0 || e.dims[0] * e.dims[1] * e.dims[2] == 0 || asp == 0 ||
+      e.brick_size[0] * e.brick_size[1] * e.brick_size[2] == 0)
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: empty volume, aspect or brick size");
+  for (int a = 0; a < 3; ++a)
+    if (e.brick_size[a] <= 2ull * e.overlap || e.brick_size[a] > 4096)
+      fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: brick size out of range");
+  // ExtendedOctree.cpp:127-160: the table of contents, one entry per brick of
+  // every LOD in TOC order
+  uint32_t bs32[3] = {uint32_t(e.brick_size[0]), uint32_t(e.brick_size[1]),
+                      uint32_t(e.brick_size[2])};
+  const std::vector<LodInfo> lods = lod_table(e.dims, bs32, e.overlap);
+  uint64_t n = 0;
+  for (const LodInfo& l : lods) n += l.bricks[0] * l.bricks[1] * l.bricks[2];
+  e.toc.resize(n);
+  for (uint64_t k = 0; k < n; ++k) {
+    EoFile::Entry& t = e.toc[k];
+    t.offset = read_value<uint64_t>(f);
+    t.length = read_value<uint64_t>(f);
+    t.compression = read_value<uint32_t>(f);
+    t.valid_length = read_value<uint64_t>(f);
+    t.atlas[0] = read_value<uint32_t>(f);
+    t.atlas[1] = read_value<uint32_t>(f);
+  }
+}
+
+// GetBrickData (ExtendedOctree.cpp:313-361): `bytes` is the brick's size
+// expanded (voxels incl. overlap x components x component size).
+void eo_read_brick(const EoFile& e, uint64_t index, size_t bytes, std::vector<uint8_t>& out) {
+  if (index >= e.toc.size()) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: brick index");
+  const EoFile::Entry& t = e.toc[index];
+  File fh(e.path.c_str());
+  if (!fh.f) fail(TVK_ERR_INVALID_ARG, "cannot reopen " + e.path);
+  seek(fh.f, e.base + t.offset);
+  out.resize(bytes);
+  if (t.compression == 0) {  // CT_NONE
+    if (t.length != bytes) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: brick length mismatch");
+    if (std::fread(out.data(), 1, bytes, fh.f) != bytes)
+      fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: file ends inside a brick");
+    return;
+  }
+  if (t.compression != 3)  // CT_LZ4
+    fail(TVK_ERR_UNSUPPORTED,
+         "ExtendedOctree: only uncompressed and LZ4 bricks are read (zlib, LZMA and bzip2 "
+         "decoders are not built)");
+  std::vector<uint8_t> buf(size_t(t.length));
+  if (std::fread(buf.data(), 1, buf.size(), fh.f) != buf.size())
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: file ends inside a brick");
+  lz4_decode_block(buf.data(), buf.size(), out.data(), bytes);
+}
+
+}  // namespace tvk

@@ -69,6 +69,30 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
                          uint64_t* launches);
 // ExtendedOctree tables and UVF metadata (api.cpp)
 std::vector<LodInfo> lod_table(const uint64_t dims[3], const uint32_t B[3], uint32_t ov);
+
+// ExtendedOctree file (eo.cpp): header and table of contents
+struct EoFile {
+  std::string path;
+  uint64_t base = 0;               // offset of the header in the file
+  uint32_t component_type = 0;     // ExtendedOctree::COMPONENT_TYPE (0 = UINT8, 1 = UINT16)
+  uint64_t components = 0;
+  bool normals = false;
+  uint64_t dims[3] = {0, 0, 0};
+  double aspect[3] = {1, 1, 1};
+  uint64_t brick_size[3] = {0, 0, 0};
+  uint32_t overlap = 0, version = 0, compression_level = 0;
+  uint64_t size = 0;
+  struct Entry {
+    uint64_t offset, length;       // from the header's start
+    uint32_t compression;          // COMPRESSION_TYPE: 0 none, 3 LZ4
+    uint64_t valid_length;
+    uint32_t atlas[2];
+  };
+  std::vector<Entry> toc;          // every LOD's bricks in TOC order
+};
+void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e);
+void eo_read_brick(const EoFile& e, uint64_t index, size_t bytes, std::vector<uint8_t>& out);
+size_t lz4_decode_block(const uint8_t* src, size_t src_len, uint8_t* dst, size_t dst_len);
 void brick_size(const LodInfo& l, const uint32_t B[3], uint32_t ov, const uint64_t c[3],
                 uint32_t out[3]);
 void brick_metadata(const LodInfo& l, const uint32_t B[3], uint32_t ov,

@@ -71,6 +71,18 @@ class Volume:
         self.info = N.VolumeInfo()
         check(lib().tvk_volume_get_info(self._h, C.byref(self.info)))
 
+    @classmethod
+    def FromExtendedOctree(cls, path, offset=0, uvf_version=5, clamp_to_edge=False,
+                           median=False, lod0_only=False):
+        """ExtendedOctree::Open + GetBrickData: a converter-written brick file
+        (uncompressed or LZ4 bricks), rebuilt on the GPU and checked brick by brick."""
+        flags = ((cls.CLAMP_TO_EDGE if clamp_to_edge else 0) | (cls.MEDIAN if median else 0) |
+                 (cls.LOD0_ONLY if lod0_only else 0))
+        h = C.c_void_p()
+        check(lib().tvk_volume_open_extended_octree(str(path).encode(), int(offset),
+                                                    int(uvf_version), flags, C.byref(h)))
+        return cls(None, _handle=h)
+
     @property
     def handle(self):
         return self._h
