@@ -171,11 +171,14 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
  * :313-361); zlib, LZMA and bzip2 bricks return TVK_ERR_UNSUPPORTED.
  * 1-component uint8 / uint16 and 4-component uint8 (TVK_RGBA8) volumes with a
  * 1:1:1 aspect.  The volume is rebuilt on the GPU from the LOD-0 bricks' inner
- * voxels (statistics, histograms, coarser LODs) and every brick the file holds
- * must equal the rebuild byte for byte: the rebuild starts from `flags`
+ * voxels (statistics, histograms, coarser LODs).  The header records neither
+ * the border fill nor the LOD filter, so the rebuild starts from `flags`
  * (TVK_VOLUME_CLAMP_TO_EDGE, TVK_VOLUME_MEDIAN, TVK_VOLUME_LOD0_ONLY) and tries
- * the other border and filter settings, which the header does not record;
- * a file that matches none returns TVK_ERR_INVALID_ARG. */
+ * the others: the LOD-0 bricks must equal the file's byte for byte (else
+ * TVK_ERR_INVALID_ARG), and coarser bricks that no filter reproduces are taken
+ * from the file with their min/max recomputed (the converter leaves stale
+ * buffer data in some ghost corners of coarser bricks under clamp-to-edge with
+ * an overlap of 2 or more). */
 tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                                            uint32_t uvf_version, uint32_t flags,
                                            tvk_volume** out);

@@ -2252,41 +2252,98 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                       size_t(n[0] - 2 * ov) * vb);
         }
     }
-    // Rebuild with the given border and filter settings first, then the other
-    // three; keep the first rebuild whose every brick equals the file's (the
-    // header records neither setting).
+    // Rebuild from the LOD-0 data: the border setting (not recorded in the
+    // header) is the one whose LOD-0 bricks equal the file's, trying `flags`
+    // first; then the filter whose coarser bricks equal the file's.  Where no
+    // filter reproduces a coarser brick the file's bytes are kept: with
+    // clamp-to-edge and an overlap of 2 or more, the converter's coarser
+    // bricks carry stale buffer contents in some ghost corners
+    // (DownsampleBrick skips its memset under clamp, ExtendedOctreeConverter.
+    // inc:261-262, and FillOverlap copies corners from neighbours not yet
+    // filled), which no rebuild reproduces.
     const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0 || dt == TVK_RGBA8;
     const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
-               median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && dt != TVK_RGBA8;
+               median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && !lod0_only;
     std::vector<uint8_t> dev;
     auto drop = [](tvk_volume* v) {
       tvk::free_volume_device(v);
       delete v;
     };
-    for (int attempt = 0; attempt < 4; ++attempt) {
-      const bool clamp = clamp0 ^ ((attempt & 1) != 0), median = median0 ^ ((attempt & 2) != 0);
-      if (median && (lod0_only || dt == TVK_RGBA8)) continue;
-      std::unique_ptr<tvk_volume, decltype(drop)> V(
-          tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
-                             !lod0_only),
-          drop);
-      bool same = true;
-      for (uint64_t k = 0; k < V->total_bricks && same; ++k) {
-        const size_t nb = size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
+    using VolPtr = std::unique_ptr<tvk_volume, decltype(drop)>;
+    auto brick_bytes = [&](const tvk_volume* V, uint64_t k) {
+      return size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
+    };
+    auto same_as_file = [&](const tvk_volume* V, uint64_t k) {
+      const size_t nb = brick_bytes(V, k);
+      tvk::eo_read_brick(e, k, nb, brick);
+      dev.resize(nb);
+      TVK_CUDA(cudaMemcpy(dev.data(), static_cast<const uint8_t*>(V->d_pool) + V->offsets[k] * vb,
+                          nb, cudaMemcpyDeviceToHost));
+      return std::memcmp(dev.data(), brick.data(), nb) == 0;
+    };
+    for (int ci = 0; ci < 2; ++ci) {
+      const bool clamp = clamp0 ^ (ci == 1);
+      VolPtr best(nullptr, drop);
+      std::vector<uint64_t> best_bad;
+      for (int mi = 0; mi < (lod0_only ? 1 : 2); ++mi) {
+        const bool median = median0 ^ (mi == 1);
+        VolPtr V(tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
+                                    !lod0_only),
+                 drop);
+        bool lod0 = true;
+        for (uint64_t k = 0; k < V->n_bricks && lod0; ++k) lod0 = same_as_file(V.get(), k);
+        if (!lod0) break;  // LOD 0 does not depend on the filter
+        std::vector<uint64_t> bad;
+        for (uint64_t k = V->n_bricks; k < V->total_bricks; ++k)
+          if (!same_as_file(V.get(), k)) bad.push_back(k);
+        if (bad.empty()) {
+          *out = V.release();
+          return;
+        }
+        if (!best || bad.size() < best_bad.size()) {
+          best = std::move(V);
+          best_bad = std::move(bad);
+        }
+      }
+      if (!best) continue;
+      // keep the file's coarser bricks that no filter reproduced, with their
+      // statistics (min/max over the whole brick, ComputeBrickStats) and macro cells
+      tvk_volume* V = best.get();
+      for (uint64_t k : best_bad) {
+        const size_t nb = brick_bytes(V, k);
         tvk::eo_read_brick(e, k, nb, brick);
-        dev.resize(nb);
-        TVK_CUDA(cudaMemcpy(dev.data(), static_cast<const uint8_t*>(V->d_pool) + V->offsets[k] * vb,
-                            nb, cudaMemcpyDeviceToHost));
-        same = std::memcmp(dev.data(), brick.data(), nb) == 0;
+        TVK_CUDA(cudaMemcpy(static_cast<uint8_t*>(V->d_pool) + V->offsets[k] * vb, brick.data(), nb,
+                            cudaMemcpyHostToDevice));
+        double lo = 1e300, hi = -1e300;
+        for (size_t i = 0; i < nb / vb; ++i) {
+          const double x = vb == 1 ? double(brick[i])
+                                   : double(reinterpret_cast<const uint16_t*>(brick.data())[i]);
+          lo = std::min(lo, x);
+          hi = std::max(hi, x);
+        }
+        V->bmin[k] = lo;
+        V->bmax[k] = hi;
       }
-      if (same) {
-        *out = V.release();
-        return;
-      }
+      tvk::DevBuf d_off, d_sizes;
+      d_off.ensure(V->total_bricks * sizeof(uint64_t));
+      d_sizes.ensure(V->total_bricks * 3 * sizeof(uint32_t));
+      TVK_CUDA(cudaMemcpy(d_off.p, V->offsets.data(), V->total_bricks * sizeof(uint64_t),
+                          cudaMemcpyHostToDevice));
+      TVK_CUDA(cudaMemcpy(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice));
+      uint32_t max_cells = 0;
+      for (uint32_t c : V->cell_counts) max_cells = std::max(max_cells, c);
+      uint64_t launches = 0;
+      tvk::launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                              static_cast<const uint64_t*>(V->d_cell_meta), V->total_bricks,
+                              max_cells, static_cast<uint32_t*>(V->d_cells), nullptr, &launches);
+      TVK_CUDA(cudaDeviceSynchronize());
+      *out = best.release();
+      return;
     }
     tvk::fail(TVK_ERR_INVALID_ARG,
-              "ExtendedOctree: the file's bricks differ from every rebuild of its LOD-0 data "
-              "(mean or median LODs, zero or clamped borders)");
+              "ExtendedOctree: the file's LOD-0 bricks differ from a rebricking of their own "
+              "inner voxels with zero or clamped borders");
   });
 }
 
