@@ -2265,11 +2265,13 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
     const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
                median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && !lod0_only;
     std::vector<uint8_t> dev;
-    auto drop = [](tvk_volume* v) {
-      tvk::free_volume_device(v);
-      delete v;
+    struct Drop {
+      void operator()(tvk_volume* v) const {
+        tvk::free_volume_device(v);
+        delete v;
+      }
     };
-    using VolPtr = std::unique_ptr<tvk_volume, decltype(drop)>;
+    using VolPtr = std::unique_ptr<tvk_volume, Drop>;
     auto brick_bytes = [&](const tvk_volume* V, uint64_t k) {
       return size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
     };
@@ -2283,13 +2285,12 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
     };
     for (int ci = 0; ci < 2; ++ci) {
       const bool clamp = clamp0 ^ (ci == 1);
-      VolPtr best(nullptr, drop);
+      VolPtr best;
       std::vector<uint64_t> best_bad;
       for (int mi = 0; mi < (lod0_only ? 1 : 2); ++mi) {
         const bool median = median0 ^ (mi == 1);
         VolPtr V(tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
-                                    !lod0_only),
-                 drop);
+                                    !lod0_only));
         bool lod0 = true;
         for (uint64_t k = 0; k < V->n_bricks && lod0; ++k) lod0 = same_as_file(V.get(), k);
         if (!lod0) break;  // LOD 0 does not depend on the filter
