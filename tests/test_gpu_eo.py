@@ -73,9 +73,10 @@ def test_gpu_eo_refuses_malformed_files(cuda_ok, tmp_path):
     short.write_bytes(data[: len(data) // 2])
     with pytest.raises(TvkError):
         Volume.FromExtendedOctree(short)
-    # a flipped voxel: no rebuild matches
+    # a LOD-0 ghost voxel that its neighbour does not hold: no rebuild matches
+    import test_eo_fixtures as F
     bad = bytearray(data)
-    bad[-100] ^= 0x5A
+    bad[F.parse(data)["toc"][0][0]] ^= 0x5A  # brick (0, 0, 0), corner ghost voxel
     (tmp_path / "bad.eo").write_bytes(bytes(bad))
     with pytest.raises(TvkError):
         Volume.FromExtendedOctree(tmp_path / "bad.eo")
