@@ -235,14 +235,15 @@ inline void clip_range(const float ce[4], const float dir[3], float& lo, float& 
 template <class T>
 void lighting_ref(const Setup& st, const T pos[3], const T N[3], const T tfc[3], T out[3]) {
   // lighting.glsl:33-43 via VRender1DLit.glsl:67-68 (diffuse colour * TF colour)
+  // normalize() as a multiply by the correctly rounded reciprocal length
   T p[3] = {-pos[0], -pos[1], -pos[2]};
-  const T lp = len3(p[0], p[1], p[2]);
-  T V[3] = {p[0] / lp, p[1] / lp, p[2] / lp};
+  const T ilp = T(1) / len3(p[0], p[1], p[2]);
+  T V[3] = {p[0] * ilp, p[1] * ilp, p[2] * ilp};
   const T d = dot3(N, V);
   T R[3];
   for (int i = 0; i < 3; ++i) R[i] = V[i] - (T(2) * d) * N[i];
-  const T lr = len3(R[0], R[1], R[2]);
-  for (int i = 0; i < 3; ++i) R[i] = R[i] / lr;
+  const T ilr = T(1) / len3(R[0], R[1], R[2]);
+  for (int i = 0; i < 3; ++i) R[i] = R[i] * ilr;
   const T L[3] = {T(st.s->light_dir[0]), T(st.s->light_dir[1]), T(st.s->light_dir[2])};
   const T diff = std::fmax(std::fabs(dot3(N, L)), T(0));
   const T spec = pow_int_or_real(std::fmax(dot3(R, L), T(0)), 8.0f);
@@ -259,14 +260,14 @@ void lighting_bp(const Setup& st, const T pos[3], const T Nin[3], const T tfc[3]
   // Blinn-Phong (selectable model): two-sided, half vector, ka/kd/ks/shininess.
   const orc_scene& s = *st.s;
   T p[3] = {-pos[0], -pos[1], -pos[2]};
-  const T lp = len3(p[0], p[1], p[2]);
-  T V[3] = {p[0] / lp, p[1] / lp, p[2] / lp};
+  const T ilp = T(1) / len3(p[0], p[1], p[2]);
+  T V[3] = {p[0] * ilp, p[1] * ilp, p[2] * ilp};
   T N[3] = {Nin[0], Nin[1], Nin[2]};
   if (dot3(N, V) < T(0)) { N[0] = -N[0]; N[1] = -N[1]; N[2] = -N[2]; }
   const T Lt[3] = {-T(s.light_dir[0]), -T(s.light_dir[1]), -T(s.light_dir[2])};
   T H[3] = {Lt[0] + V[0], Lt[1] + V[1], Lt[2] + V[2]};
-  const T lh = len3(H[0], H[1], H[2]);
-  for (int i = 0; i < 3; ++i) H[i] = H[i] / lh;
+  const T ilh = T(1) / len3(H[0], H[1], H[2]);
+  for (int i = 0; i < 3; ++i) H[i] = H[i] * ilh;
   const T diff = std::fmax(dot3(N, Lt), T(0));
   const T spec = pow_int_or_real(std::fmax(dot3(N, H), T(0)), s.bp_shininess);
   for (int i = 0; i < 3; ++i) {
@@ -364,7 +365,10 @@ void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_i
                         std::fma(T(float(st.norm_mat[r][1])), gs[1],
                                  T(float(st.norm_mat[r][0])) * gs[0]));
       const T l = len3(N[0], N[1], N[2]);
-      if (l > T(0)) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+      if (l > T(0)) {
+        const T il = T(1) / l;
+        N[0] = N[0] * il; N[1] = N[1] * il; N[2] = N[2] * il;
+      }
       T lc[3];
       const T tfc[3] = {src[0], src[1], src[2]};
       if (s.light_model == ORC_LIGHT_BLINN_PHONG)

@@ -234,14 +234,15 @@ __device__ __forceinline__ void lighting_ref(const RenderParams& P, const float 
                                              const float N[3], const float tfc[3], float out[3]) {
   // Shaders/lighting.glsl:33-43
   const float p0 = -pos[0], p1 = -pos[1], p2 = -pos[2];
-  const float lp = len3(p0, p1, p2);
-  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  // normalize() as a multiply by the correctly rounded reciprocal length
+  const float ilp = 1.0f / len3(p0, p1, p2);
+  const float V0 = p0 * ilp, V1 = p1 * ilp, V2 = p2 * ilp;
   const float d = (N[0] * V0 + N[1] * V1) + N[2] * V2;
   float R0 = V0 - (2.0f * d) * N[0];
   float R1 = V1 - (2.0f * d) * N[1];
   float R2 = V2 - (2.0f * d) * N[2];
-  const float lr = len3(R0, R1, R2);
-  R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+  const float ilr = 1.0f / len3(R0, R1, R2);
+  R0 = R0 * ilr; R1 = R1 * ilr; R2 = R2 * ilr;
   const float* L = P.light_dir;
   const float diff = fmaxf(fabsf((N[0] * L[0] + N[1] * L[1]) + N[2] * L[2]), 0.0f);
   const float spec = pow_int_or_real(fmaxf((R0 * L[0] + R1 * L[1]) + R2 * L[2], 0.0f), 8.0f);
@@ -257,14 +258,14 @@ __device__ __forceinline__ void lighting_ref(const RenderParams& P, const float 
 __device__ __forceinline__ void lighting_bp(const RenderParams& P, const float pos[3],
                                             const float Nin[3], const float tfc[3], float out[3]) {
   const float p0 = -pos[0], p1 = -pos[1], p2 = -pos[2];
-  const float lp = len3(p0, p1, p2);
-  const float V0 = p0 / lp, V1 = p1 / lp, V2 = p2 / lp;
+  const float ilp = 1.0f / len3(p0, p1, p2);
+  const float V0 = p0 * ilp, V1 = p1 * ilp, V2 = p2 * ilp;
   float N0 = Nin[0], N1 = Nin[1], N2 = Nin[2];
   if ((N0 * V0 + N1 * V1) + N2 * V2 < 0.0f) { N0 = -N0; N1 = -N1; N2 = -N2; }
   const float L0 = -P.light_dir[0], L1 = -P.light_dir[1], L2 = -P.light_dir[2];
   float H0 = L0 + V0, H1 = L1 + V1, H2 = L2 + V2;
-  const float lh = len3(H0, H1, H2);
-  H0 = H0 / lh; H1 = H1 / lh; H2 = H2 / lh;
+  const float ilh = 1.0f / len3(H0, H1, H2);
+  H0 = H0 * ilh; H1 = H1 * ilh; H2 = H2 * ilh;
   const float diff = fmaxf((N0 * L0 + N1 * L1) + N2 * L2, 0.0f);
   const float spec = pow_int_or_real(fmaxf((N0 * H0 + N1 * H1) + N2 * H2, 0.0f), P.bp_shininess);
 #pragma unroll
@@ -433,7 +434,10 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       for (int r = 0; r < 3; ++r)
         N[r] = fmaf(P.norm_mat[r][2], gs2, fmaf(P.norm_mat[r][1], gs1, P.norm_mat[r][0] * gs0));
       const float l = len3(N[0], N[1], N[2]);
-      if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+      if (l > 0.0f) {
+        const float il = 1.0f / l;
+        N[0] = N[0] * il; N[1] = N[1] * il; N[2] = N[2] * il;
+      }
       const float tfc[3] = {src.x, src.y, src.z};
       float lc[3];
       if (P.light_model == TVK_LIGHT_BLINN_PHONG)
