@@ -300,8 +300,9 @@ void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_i
   const float q = len / b.step;
   const int n = int(q) + 1;
   T inc[3], pos[3], epos[3], einc[3];
+  const T iq = T(1) / T(q);  // the increment: a multiply by the step count's reciprocal
   for (int a = 0; a < 3; ++a) {
-    inc[a] = T(tout[a] - tin[a]) / T(q);
+    inc[a] = T(tout[a] - tin[a]) * iq;
     pos[a] = T(tin[a]);
     epos[a] = T(en[a]);
   }
@@ -309,9 +310,10 @@ void brick_march(const Setup& st, const BrickR& b, const float dir[3], float t_i
   {
     const T ddx = T(ex[0]) - T(en[0]), ddy = T(ex[1]) - T(en[1]), ddz = T(ex[2]) - T(en[2]);
     const T l = len3(ddx, ddy, ddz);
-    einc[0] = (ddx / l) * T(b.step);
-    einc[1] = (ddy / l) * T(b.step);
-    einc[2] = (ddz / l) * T(b.step);
+    const T il = T(1) / l;
+    einc[0] = (ddx * il) * T(b.step);
+    einc[1] = (ddy * il) * T(b.step);
+    einc[2] = (ddz * il) * T(b.step);
   }
   const T vstep[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
   const bool lit = s.lighting != 0;
@@ -431,8 +433,9 @@ bool iso_brick(const Setup& st, const BrickR& b, const float dir[3], float t_in,
   if (!(q < 1.0e6f)) return false;
   const int n = int(q) + 1;
   T inc[3], pos[3];
+  const T iq = T(1) / T(q);  // the increment: a multiply by the step count's reciprocal
   for (int a = 0; a < 3; ++a) {
-    inc[a] = T(tout[a] - tin[a]) / T(q);
+    inc[a] = T(tout[a] - tin[a]) * iq;
     pos[a] = T(tin[a]);
   }
   const T iso = T(kCV ? iso_cv : st.iso_norm);
@@ -556,17 +559,19 @@ void brick_march_color(const Setup& st, const BrickR& b, const float dir[3], flo
   const float q = len / b.step;
   const int n = int(q) + 1;
   T inc[3], pos[3], epos[3], einc[3];
+  const T iq = T(1) / T(q);  // the increment: a multiply by the step count's reciprocal
   for (int a = 0; a < 3; ++a) {
-    inc[a] = T(tout[a] - tin[a]) / T(q);
+    inc[a] = T(tout[a] - tin[a]) * iq;
     pos[a] = T(tin[a]);
     epos[a] = T(en[a]);
   }
   {
     const T ddx = T(ex[0]) - T(en[0]), ddy = T(ex[1]) - T(en[1]), ddz = T(ex[2]) - T(en[2]);
     const T l = len3(ddx, ddy, ddz);
-    einc[0] = (ddx / l) * T(b.step);
-    einc[1] = (ddy / l) * T(b.step);
-    einc[2] = (ddz / l) * T(b.step);
+    const T il = T(1) / l;
+    einc[0] = (ddx * il) * T(b.step);
+    einc[1] = (ddy * il) * T(b.step);
+    einc[2] = (ddz * il) * T(b.step);
   }
   const T vstep[3] = {T(1.0f / float(b.n[0])), T(1.0f / float(b.n[1])), T(1.0f / float(b.n[2]))};
   const uint32_t W = s.tf_w;
@@ -634,8 +639,9 @@ bool iso_brick_color(const Setup& st, const BrickR& b, const float dir[3], float
   if (!(q < 1.0e6f)) return false;
   const int n = int(q) + 1;
   T inc[3], pos[3];
+  const T iq = T(1) / T(q);  // the increment: a multiply by the step count's reciprocal
   for (int a = 0; a < 3; ++a) {
-    inc[a] = T(tout[a] - tin[a]) / T(q);
+    inc[a] = T(tout[a] - tin[a]) * iq;
     pos[a] = T(tin[a]);
   }
   const T iso = T(st.iso_norm);

@@ -305,15 +305,18 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   }
   const int n = int(q) + 1;
   float pos[3], inc[3], epos[3], einc[3];
+  // the increment divides by the step count: a multiply by its reciprocal
+  const float iq = 1.0f / q;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    inc[a] = (tout[a] - tin[a]) / q;
+    inc[a] = (tout[a] - tin[a]) * iq;
     pos[a] = tin[a];
     epos[a] = en[a];
   }
-  einc[0] = (dx / len) * b.step;
-  einc[1] = (dy / len) * b.step;
-  einc[2] = (dz / len) * b.step;
+  const float ilen = 1.0f / len;
+  einc[0] = (dx * ilen) * b.step;
+  einc[1] = (dy * ilen) * b.step;
+  einc[2] = (dz * ilen) * b.step;
 
   BrickView<T> vol;
   vol.p = static_cast<const T*>(P.pool) + b.off;
@@ -514,9 +517,11 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
   if (!(q < P.max_q)) return false;
   const int n = int(q) + 1;
   float pos[3], inc[3];
+  // the increment divides by the step count: a multiply by its reciprocal
+  const float iq = 1.0f / q;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    inc[a] = (tout[a] - tin[a]) / q;
+    inc[a] = (tout[a] - tin[a]) * iq;
     pos[a] = tin[a];
   }
   BrickView<T> vol;
@@ -719,15 +724,18 @@ __device__ __forceinline__ float4 march_brick_color(const RenderParams& P, const
   }
   const int n = int(q) + 1;
   float pos[3], inc[3], epos[3], einc[3];
+  // the increment divides by the step count: a multiply by its reciprocal
+  const float iq = 1.0f / q;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    inc[a] = (tout[a] - tin[a]) / q;
+    inc[a] = (tout[a] - tin[a]) * iq;
     pos[a] = tin[a];
     epos[a] = en[a];
   }
-  einc[0] = (dx / len) * b.step;
-  einc[1] = (dy / len) * b.step;
-  einc[2] = (dz / len) * b.step;
+  const float ilen = 1.0f / len;
+  einc[0] = (dx * ilen) * b.step;
+  einc[1] = (dy * ilen) * b.step;
+  einc[2] = (dz * ilen) * b.step;
   const ColorView vol = color_view(P, b);
   const float im = P.inv_max_raw;
   const float W = float(P.tf_w);
@@ -799,9 +807,11 @@ __device__ __forceinline__ bool iso_brick_color(const RenderParams& P, const Dev
   if (!(q < P.max_q)) return false;
   const int n = int(q) + 1;
   float pos[3], inc[3];
+  // the increment divides by the step count: a multiply by its reciprocal
+  const float iq = 1.0f / q;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    inc[a] = (tout[a] - tin[a]) / q;
+    inc[a] = (tout[a] - tin[a]) * iq;
     pos[a] = tin[a];
   }
   const ColorView vol = color_view(P, b);
