@@ -43,7 +43,8 @@ typedef enum tvk_status {
 
 /* Voxel types.  TVK_RGBA8: colour volumes, four unsigned 8-bit channels per
  * voxel, x fastest (Dataset::GetComponentCount() == 4, AbstrRenderer::
- * ColorData).  Colour volumes are bricked at LOD 0 only, with no statistics
+ * ColorData).  Colour volumes get every LOD, each channel filtered on its own
+ * (ExtendedOctreeConverter.inc:39-44), and no statistics
  * (AbstrRenderer::ContainsData never skips colour bricks); they render in 1D
  * mode (the voxel's colour times the TF entry at (r + g + b) / 3,
  * VRender1D-Color.glsl / VRender1DLit-Color.glsl) and iso mode (the alpha

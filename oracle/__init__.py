@@ -223,7 +223,8 @@ def build_octree(raw, bsize, overlap, clamp=False, median=False):
                 for x in range(lc[0]):
                     shapes.append(brick_size(ls, lc, bsize, overlap, (x, y, z)))
     total = sum(s[0] * s[1] * s[2] for s in shapes)
-    pool = np.zeros(total, dtype=raw.dtype)
+    comps = raw.shape[3:]  # (4,) for RGBA8 colour volumes
+    pool = np.zeros((total,) + comps, dtype=raw.dtype)
     offs = np.zeros(len(shapes), dtype=np.uint64)
     n = lib().orc_build_octree(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
                                _u32(bsize), overlap, int(clamp), int(median),
@@ -232,7 +233,7 @@ def build_octree(raw, bsize, overlap, clamp=False, median=False):
     assert n == len(shapes), n
     out = []
     for s, o in zip(shapes, offs):
-        out.append(pool[int(o):int(o) + s[0] * s[1] * s[2]].reshape(s[2], s[1], s[0]))
+        out.append(pool[int(o):int(o) + s[0] * s[1] * s[2]].reshape((s[2], s[1], s[0]) + comps))
     return out
 
 

@@ -658,6 +658,24 @@ extern "C" int64_t orc_build_octree(const void* raw, int dtype, const uint64_t d
                                     int clamp_to_edge, int median, void* pool,
                                     uint64_t pool_voxels, uint64_t* brick_offsets,
                                     uint64_t max_bricks) {
+  if (dtype == 2) {
+    // RGBA8: every step filters or copies each component on its own
+    // (ExtendedOctreeConverter.inc:39-44), so the octree is the four
+    // single-channel octrees interleaved
+    const uint64_t n = dims[0] * dims[1] * dims[2];
+    std::vector<uint8_t> chan(n), part(pool_voxels);
+    uint8_t* out = static_cast<uint8_t*>(pool);
+    int64_t bricks = -1;
+    for (int c = 0; c < 4; ++c) {
+      for (uint64_t i = 0; i < n; ++i) chan[i] = as<uint8_t>(raw)[4 * i + uint64_t(c)];
+      bricks = build_octree<uint8_t>(chan.data(), dims, brick_size, overlap, clamp_to_edge != 0,
+                                     median != 0, part.data(), pool_voxels, brick_offsets,
+                                     max_bricks);
+      if (bricks < 0) return bricks;
+      for (uint64_t i = 0; i < pool_voxels; ++i) out[4 * i + uint64_t(c)] = part[i];
+    }
+    return bricks;
+  }
   if (dtype == 0)
     return build_octree<uint8_t>(as<uint8_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
                                  median != 0, static_cast<uint8_t*>(pool), pool_voxels,

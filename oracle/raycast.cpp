@@ -836,7 +836,7 @@ Setup build_setup(const orc_scene& s) {
   uint64_t lod_all[3 * 64], cnt_all[3 * 64];
   const int n_lods = orc_lod_table(s.dims, s.brick_size, s.overlap, lod_all, cnt_all, 64);
   // the rendered LOD (AbstrRenderer m_iCurrentLOD); its bricks, metadata and aspect
-  const uint32_t L = color ? 0u : std::min<uint32_t>(s.lod, uint32_t(n_lods - 1));
+  const uint32_t L = std::min<uint32_t>(s.lod, uint32_t(n_lods - 1));
   const uint64_t* lod = &lod_all[3 * L];
   const uint64_t* cnt = &cnt_all[3 * L];
   const uint64_t nb = cnt[0] * cnt[1] * cnt[2];

@@ -1,5 +1,5 @@
-"""Colour (RGBA8) volumes against the oracle: LOD-0 bricks with their ghost
-layer bit for bit; 1D mode (VRender1D-Color / VRender1DLit-Color: the voxel's
+"""Colour (RGBA8) volumes against the oracle: the bricks of every LOD with
+their ghost layers bit for bit; 1D mode (VRender1D-Color / VRender1DLit-Color: the voxel's
 colour times the TF entry at (r + g + b) / 3) and iso mode (the alpha
 channel's surface, GLRaycaster-Color-FS + Compose-Color-FS) with the usual
 image tolerance.  The opacity correction of a colour sample depends on the
@@ -46,29 +46,35 @@ def renderer(vol, mode, lit, tf=None):
     return r
 
 
-@pytest.mark.parametrize("clamp", [False, True])
-def test_gpu_color_bricks_match_oracle(cuda_ok, rgba, clamp):
-    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1, clamp_to_edge=clamp)
-    assert vol.GetLODLevelCount() >= 1
-    for k in range(vol.GetBrickCount(0)):
-        x, y, z, _ = vol.IndexTo4D(0, k)
-        np.testing.assert_array_equal(vol.GetBrick((0, 0, k)),
-                                      O.lod0_brick(rgba, (BS,) * 3, 1, clamp, (x, y, z)))
+@pytest.mark.parametrize("clamp,median", [(False, False), (True, False), (False, True)])
+def test_gpu_color_bricks_match_oracle(cuda_ok, rgba, clamp, median):
+    """Every LOD: each channel filtered on its own (the oracle's octree is the
+    four channel octrees interleaved, pinned to the converter's RGBA files)."""
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1, clamp_to_edge=clamp, median=median)
+    ref = O.build_octree(rgba, (BS,) * 3, 1, clamp=clamp, median=median)
+    k = 0
+    for lod in range(vol.GetLODLevelCount()):
+        for i in range(vol.GetBrickCount(lod)):
+            np.testing.assert_array_equal(vol.GetBrick((0, lod, i)), ref[k], err_msg=f"{lod} {i}")
+            k += 1
+    assert k == len(ref)
 
 
 CASES = [
-    # id, mode, lighting, light model, eye
-    ("1d", 0, False, 0, (0.3, 0.4, 1.5)),
-    ("1d_lit", 0, True, 0, (-1.1, 0.2, -0.7)),
-    ("1d_lit_bp", 0, True, 1, (0.9, -0.6, 1.0)),
-    ("iso", 2, False, 0, (0.3, 0.4, 1.5)),
-    ("iso_inside", 2, False, 0, (0.05, 0.02, 0.1)),
+    # id, mode, lighting, light model, eye, LOD
+    ("1d", 0, False, 0, (0.3, 0.4, 1.5), 0),
+    ("1d_lit", 0, True, 0, (-1.1, 0.2, -0.7), 0),
+    ("1d_lit_bp", 0, True, 1, (0.9, -0.6, 1.0), 0),
+    ("iso", 2, False, 0, (0.3, 0.4, 1.5), 0),
+    ("iso_inside", 2, False, 0, (0.05, 0.02, 0.1), 0),
+    ("1d_lit_lod1", 0, True, 0, (0.7, 0.5, 1.2), 1),
+    ("iso_lod1", 2, False, 0, (-0.8, 0.6, 1.0), 1),
 ]
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
 def test_gpu_color_render_matches_oracle(cuda_ok, rgba, case):
-    name, mode, lit, model, eye = case
+    name, mode, lit, model, eye, lod = case
     tf = color_tf()
     vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1)
     r = renderer(vol, mode, lit, tf)
@@ -78,12 +84,13 @@ def test_gpu_color_render_matches_oracle(cuda_ok, rgba, case):
     if mode == 2:
         r.SetIsoValue(iso)
     r.SetSampleRateModifier(1.5)
+    r.SetLOD(lod)
     r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
     r.Resize(W, H)
     r.Paint()
     img, cnt, st = r.ReadBackPixels(), r.ReadSampleCounts(), r.GetStats()
     kw = dict(width=W, height=H, eye=eye, mode=mode, lighting=lit, light_model=model,
-              srm=1.5, want_counts=True)
+              srm=1.5, want_counts=True, lod=lod)
     if mode == 2:
         kw["isovalue"] = iso
     ref, n, rc = O.render(rgba, (BS,) * 3, 1, tf, **kw)
@@ -123,10 +130,6 @@ def test_gpu_color_refusals(cuda_ok, rgba):
         r.Paint()  # 2D mode
     r.SetRendermode(0)
     r.Set1DTransFloat(color_tf())
-    r.SetLOD(1)
-    with pytest.raises(TvkError):
-        r.Paint()  # LOD 0 only
-    r.SetLOD(0)
     r.Paint()
     with pytest.raises(TvkError):
         Batch().Paint([r])

@@ -41,7 +41,7 @@ def test_gpu_eo_matches_direct_bricking(cuda_ok, case, guess):
     color = case["components"] == 4
     # LOD 0 always; coarser LODs where the converter's bricks are reproducible
     # (not under clamp-to-edge with an overlap of 2 or more)
-    lod0 = color or (case["clamp"] and case["overlap"] >= 2)
+    lod0 = case["clamp"] and case["overlap"] >= 2
     keys = [(0, 0, k) for k in range(ref.GetBrickCount(0))] if lod0 else all_keys(ref)
     for key in keys:
         np.testing.assert_array_equal(v.GetBrick(key), ref.GetBrick(key), err_msg=str(key))

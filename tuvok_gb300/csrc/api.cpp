@@ -224,9 +224,12 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
                            cudaMemcpyHostToDevice, s));
   TVK_CUDA(cudaMemcpyAsync(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
                            cudaMemcpyHostToDevice, s));
+  TVK_CUDA(cudaMemcpyAsync(d_vox.p, voxels.data(), V->total_bricks * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
   if (V->dtype == TVK_RGBA8) {
-    // colour volumes: the bricks only.  Channel range of 8-bit data; no
-    // histograms, gradients or macro cells (colour bricks are never empty).
+    // colour volumes: the bricks of every LOD, each channel filtered on its
+    // own.  Channel range of 8-bit data; no histograms, gradients or macro
+    // cells (colour bricks are never empty).
     BrickGrid g;
     for (int a = 0; a < 3; ++a) {
       g.dims[a] = V->dims[a];
@@ -238,6 +241,17 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     g.total = nvox;
     launch_brick_copy4(d_raw, g, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(), V->n_bricks,
                        V->d_pool, s, &launches);
+    if (V->total_bricks > V->n_bricks) {
+      DevBuf d_wave;
+      uint64_t max_lod_bricks = 0;
+      for (size_t l = 1; l < n_lods; ++l)
+        max_lod_bricks = std::max<uint64_t>(max_lod_bricks, V->lod_first[l + 1] - V->lod_first[l]);
+      d_wave.ensure(max_lod_bricks * sizeof(uint32_t));
+      std::vector<LodInfo> built(V->lods.begin(), V->lods.begin() + n_lods);
+      build_lod_levels(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_vox.as<uint64_t>(), built,
+                       V->lod_first, V->brick_size, V->overlap, V->clamp, V->median, nullptr,
+                       nullptr, d_wave.as<uint32_t>(), s, &launches);
+    }
     TVK_CUDA(cudaStreamSynchronize(s));
     V->range_min = 0;
     V->range_max = 255;
@@ -253,8 +267,6 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     V->total_cells = 0;
     return;
   }
-  TVK_CUDA(cudaMemcpyAsync(d_vox.p, voxels.data(), V->total_bricks * sizeof(uint64_t),
-                           cudaMemcpyHostToDevice, s));
   // scratch: bmin, bmax, bhist, hist, max_grad bits, raw min/max
   const uint64_t gbins = uint64_t(1) << (8 * V->bytes);
   const size_t sz_bmin = V->n_bricks * 4, sz_bh = V->n_bricks * 256 * 4, sz_h = gbins * 8;
@@ -432,10 +444,7 @@ tvk_volume* create_volume(const void* src, bool on_device, tvk_dtype dtype, cons
   REQUIRE(src && dims && bsz, "null argument");
   REQUIRE(dtype == TVK_U8 || dtype == TVK_U16 || dtype == TVK_RGBA8,
           "dtype must be TVK_U8, TVK_U16 or TVK_RGBA8");
-  if (dtype == TVK_RGBA8) {
-    REQUIRE(!median, "colour volumes have no coarser LODs to filter");
-    build_lods = false;  // colour volumes are bricked at LOD 0 only
-  }
+
   for (int a = 0; a < 3; ++a) {
     REQUIRE(dims[a] >= 1, "volume dimensions must be >= 1");
     REQUIRE(bsz[a] > 2 * ov, "brick size must exceed twice the overlap (ExtendedOctree.cpp:196)");
@@ -2261,7 +2270,7 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
     // (DownsampleBrick skips its memset under clamp, ExtendedOctreeConverter.
     // inc:261-262, and FillOverlap copies corners from neighbours not yet
     // filled), which no rebuild reproduces.
-    const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0 || dt == TVK_RGBA8;
+    const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0;
     const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
                median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && !lod0_only;
     std::vector<uint8_t> dev;
@@ -2315,6 +2324,7 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
         tvk::eo_read_brick(e, k, nb, brick);
         TVK_CUDA(cudaMemcpy(static_cast<uint8_t*>(V->d_pool) + V->offsets[k] * vb, brick.data(), nb,
                             cudaMemcpyHostToDevice));
+        if (dt == TVK_RGBA8) continue;  // colour bricks carry no statistics
         double lo = 1e300, hi = -1e300;
         for (size_t i = 0; i < nb / vb; ++i) {
           const double x = vb == 1 ? double(brick[i])
@@ -2324,6 +2334,10 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
         }
         V->bmin[k] = lo;
         V->bmax[k] = hi;
+      }
+      if (dt == TVK_RGBA8) {  // no macro cells to refresh
+        *out = best.release();
+        return;
       }
       tvk::DevBuf d_off, d_sizes;
       d_off.ensure(V->total_bricks * sizeof(uint64_t));

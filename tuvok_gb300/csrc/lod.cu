@@ -57,6 +57,27 @@ __device__ __forceinline__ T median4(T a, T b, T c) {
   return max(a, b);
 }
 
+// Voxel components: scalar voxels have one; RGBA8 colour voxels (packed in a
+// 32-bit word, red in the low byte) four, each filtered on its own like the
+// reference's per-component loop (ExtendedOctreeConverter.inc:39-44).
+template <class T>
+struct Comp {
+  static constexpr int n = 1;
+  __device__ static uint32_t get(T v, int) { return uint32_t(v); }
+  __device__ static void set(T& v, int, uint32_t x) { v = T(x); }
+};
+struct Rgba8 {
+  uint32_t w;
+};
+template <>
+struct Comp<Rgba8> {
+  static constexpr int n = 4;
+  __device__ static uint32_t get(Rgba8 v, int c) { return (v.w >> (8 * c)) & 0xffu; }
+  __device__ static void set(Rgba8& v, int c, uint32_t x) {
+    v.w = (v.w & ~(0xffu << (8 * c))) | ((x & 0xffu) << (8 * c));
+  }
+};
+
 // Geometry of one LOD for the kernels.
 struct LodGeom {
   uint32_t cnt[3];        // bricks per axis
@@ -91,7 +112,7 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
   for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
     const uint32_t k = z0 + t / sxy, r = t % sxy, j = r / n[0], i = r % n[0];
     const uint32_t v[3] = {i, j, k};
-    T out = T(0);
+    T out{};
     bool covered = true;
     uint32_t child[3], l[3], cs[3];
     int pair[3];  // 1: two samples along the axis, 0: the odd boundary sample
@@ -123,8 +144,15 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
         const T a0 = S(X, Y, Z), a1 = S(X, Y, Z + 1), a2 = S(X, Y + 1, Z), a3 = S(X, Y + 1, Z + 1);
         const T a4 = S(X + 1, Y, Z), a5 = S(X + 1, Y, Z + 1), a6 = S(X + 1, Y + 1, Z),
                 a7 = S(X + 1, Y + 1, Z + 1);
-        out = median ? median8<T>(a0, a1, a2, a3, a4, a5, a6)
-                     : T((uint32_t(a0) + a1 + a2 + a3 + a4 + a5 + a6 + a7) >> 3);
+#pragma unroll
+        for (int q = 0; q < Comp<T>::n; ++q) {
+          const uint32_t b0 = Comp<T>::get(a0, q), b1 = Comp<T>::get(a1, q),
+                         b2 = Comp<T>::get(a2, q), b3 = Comp<T>::get(a3, q),
+                         b4 = Comp<T>::get(a4, q), b5 = Comp<T>::get(a5, q),
+                         b6 = Comp<T>::get(a6, q), b7 = Comp<T>::get(a7, q);
+          Comp<T>::set(out, q, median ? median8<uint32_t>(b0, b1, b2, b3, b4, b5, b6)
+                                      : (b0 + b1 + b2 + b3 + b4 + b5 + b6 + b7) >> 3);
+        }
       } else if (np == 2) {
         T a0, a1, a2, a3;
         if (!pair[0]) {  // plane at the end of x: p0, p1, p2, p3
@@ -134,13 +162,22 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
         } else {  // end of z: p0, p2, p4, p6
           a0 = S(X, Y, Z); a1 = S(X, Y + 1, Z); a2 = S(X + 1, Y, Z); a3 = S(X + 1, Y + 1, Z);
         }
-        out = median ? median4<T>(a0, a1, a2) : T((uint32_t(a0) + a1 + a2 + a3) >> 2);
+#pragma unroll
+        for (int q = 0; q < Comp<T>::n; ++q) {
+          const uint32_t b0 = Comp<T>::get(a0, q), b1 = Comp<T>::get(a1, q),
+                         b2 = Comp<T>::get(a2, q), b3 = Comp<T>::get(a3, q);
+          Comp<T>::set(out, q, median ? median4<uint32_t>(b0, b1, b2) : (b0 + b1 + b2 + b3) >> 2);
+        }
       } else if (np == 1) {
         T a0 = S(X, Y, Z), a1;
         if (pair[2]) a1 = S(X, Y, Z + 1);       // x/y line: p0, p1
         else if (pair[0]) a1 = S(X + 1, Y, Z);  // y/z line: p0, p4
         else a1 = S(X, Y + 1, Z);               // x/z line: p0, p2
-        out = median ? a0 : T((uint32_t(a0) + a1) >> 1);
+#pragma unroll
+        for (int q = 0; q < Comp<T>::n; ++q) {
+          const uint32_t b0 = Comp<T>::get(a0, q), b1 = Comp<T>::get(a1, q);
+          Comp<T>::set(out, q, median ? b0 : (b0 + b1) >> 1);
+        }
       } else {
         out = S(X, Y, Z);  // odd corner copies *p0 (.inc:244-246)
       }
@@ -358,7 +395,11 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
     const uint64_t nb = uint64_t(hi.cnt[0]) * hi.cnt[1] * hi.cnt[2];
     const uint32_t z_chunk = 8;
     const dim3 grid(uint32_t(nb), (B[2] + z_chunk - 1) / z_chunk);
-    if (bytes == 1)
+    if (bytes == 4)
+      downsample_kernel<Rgba8><<<grid, kThreads, 0, s>>>(static_cast<Rgba8*>(pool), d_offsets,
+                                                         lo, hi, B[0], B[1], B[2], ov,
+                                                         median ? 1 : 0, z_chunk);
+    else if (bytes == 1)
       downsample_kernel<uint8_t><<<grid, kThreads, 0, s>>>(static_cast<uint8_t*>(pool), d_offsets,
                                                            lo, hi, B[0], B[1], B[2], ov,
                                                            median ? 1 : 0, z_chunk);
@@ -391,7 +432,11 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
       // (one CTA per brick when clamping orders its steps with barriers)
       const uint32_t split = clamp ? 1u : std::max(1u, std::min(32u, 1216u / cnt));
       const dim3 fgrid(cnt, split);
-      if (bytes == 1)
+      if (bytes == 4)
+        fill_overlap_kernel<uint32_t><<<fgrid, kThreads, 0, s>>>(
+            static_cast<uint32_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
+            clamp ? 1 : 0);
+      else if (bytes == 1)
         fill_overlap_kernel<uint8_t><<<fgrid, kThreads, 0, s>>>(
             static_cast<uint8_t*>(pool), d_offsets, hi, d_wave + starts[w], B[0], B[1], B[2], ov,
             clamp ? 1 : 0);
@@ -404,6 +449,7 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
     }
     // the wave list is pageable host memory reused by the next level
     TVK_CUDA(cudaStreamSynchronize(s));
+    if (bytes == 4) continue;  // colour bricks carry no statistics
     TVK_CUDA(cudaMemsetAsync(d_min + hi.first, 0xff, nb * sizeof(uint32_t), s));
     TVK_CUDA(cudaMemsetAsync(d_max + hi.first, 0, nb * sizeof(uint32_t), s));
     const dim3 mgrid(uint32_t(nb), std::max(1u, std::min(64u, 2432u / uint32_t(nb))));
