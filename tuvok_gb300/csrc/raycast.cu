@@ -22,17 +22,23 @@
 
 // 1: the lit march batches the gradient and lighting of pending samples
 // across the warp (same per-ray arithmetic, other interleaving); measured
-// 11 % faster on the 1024^3 lit frame (4.26 -> 3.83 ms), 19 % on 512^3.
+// 12 % faster on the 1024^3 lit frame (4.26 -> 3.76 ms), 20 % on 512^3.
 // TVK_DEFER_NUM / TVK_DEFER_DEN: the pending share of the marching lanes that
-// starts a batch.
+// starts a batch (1/3: 3.93, 1/2: 3.84, 2/3: 3.77, 3/4: 3.77, 7/8: 3.79 ms).
 #ifndef TVK_DEFER_LIGHT
 #define TVK_DEFER_LIGHT 1
 #endif
 #ifndef TVK_DEFER_NUM
-#define TVK_DEFER_NUM 1
+#define TVK_DEFER_NUM 3
 #endif
 #ifndef TVK_DEFER_DEN
-#define TVK_DEFER_DEN 2
+#define TVK_DEFER_DEN 4
+#endif
+// 1: the centre samples are batched the same way (a lane that reached a
+// non-empty cell waits while the others leap); measured slower (4.59 against
+// 3.76 ms on the 1024^3 lit frame), so off
+#ifndef TVK_DEFER_SAMPLE
+#define TVK_DEFER_SAMPLE 0
 #endif
 
 namespace tvk {
@@ -363,16 +369,19 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   Foot foot;
   float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
   float fx = 0.0f;
+  bool ready = false;  // at a non-empty step, its sample not taken yet
+  float u0 = 0.f, u1 = 0.f, u2 = 0.f;
   for (;;) {
-    bool fin = false;  // a sample is complete: composite it and advance
-    if (!pend) {
+    bool fin = false;     // a sample is complete: composite it and advance
+    bool leaped = false;  // this lane leapt over empty cells in this round
+    if (!pend && !ready) {
       if (i >= n) break;
       const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
       const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
       const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
-      const float u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
-      const float u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
-      const float u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+      u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
+      u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
+      u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
       int dd = 0;
       int cx = 0, cy = 0, cz = 0;
       if (dist) {
@@ -406,7 +415,26 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
           }
         }
         i += k + 1;
+        leaped = true;
       } else {
+        ready = true;
+      }
+    }
+    // Progress: leaping lanes advance; when no lane leapt in a round, every
+    // waiting lane goes ahead, so no round passes without progress.
+    bool take = ready;
+    bool stalled = false;
+#if TVK_DEFER_SAMPLE
+    {
+      const unsigned am = __activemask();
+      const unsigned rm = __ballot_sync(am, ready);
+      stalled = __ballot_sync(am, leaped) == 0u;
+      take = ready && (stalled || TVK_DEFER_DEN * __popc(rm) >= TVK_DEFER_NUM * __popc(am));
+    }
+#endif
+    if (take) {
+      {
+        ready = false;
         ++samples;
         ++shaded;
         const float v = centre_sample(vol, u0, u1, u2, foot) * im;
@@ -427,7 +455,7 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
     }
     const unsigned am = __activemask();
     const unsigned pm = __ballot_sync(am, pend);
-    if (pend && (TVK_DEFER_DEN * __popc(pm) >= TVK_DEFER_NUM * __popc(am))) {
+    if (pend && (stalled || TVK_DEFER_DEN * __popc(pm) >= TVK_DEFER_NUM * __popc(am))) {
       ++graded;
       // Volume3D.glsl:43-54 (Yp sampled at -step.y)
       const float xp = shifted_x(vol, foot, clamp_u(pos[0] + vs0, vol.fn0, vol.n0)) * im;
