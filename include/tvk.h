@@ -292,6 +292,48 @@ tvk_status tvk_set_tf1d_rgba8(tvk_renderer* r, const uint8_t* rgba, uint32_t n);
 /* Float RGBA table.  rgba8_upload != 0 reproduces the GL_RGBA8 upload
  * (clamp, x255, truncate); 0 keeps FP32 entries. */
 tvk_status tvk_set_tf1d_float(tvk_renderer* r, const float* rgba, uint32_t n, int rgba8_upload);
+
+/* ---- TransferFunction1D (IO/TransferFunction1D.h:53-101) on a caller-held
+ * table of n entries of 4 floats (RGBA), host only.  Each function gives the
+ * reference method's table bit for bit; none touches the GPU.  The renderer
+ * takes the table through tvk_set_tf1d_float. */
+
+/* TransferFunction1D::SetStdFunction (TransferFunction1D.cpp:74-113): a
+ * smoothstep ramp centred on center * (n - 1) entries, inv_gradient * (n - 1)
+ * entries wide (both clamped to [0, 1]), 0 before and 1 after (reversed when
+ * inverted).  component 0..3 sets one channel (the 4-argument overload);
+ * -1 sets all four, not inverted (the 2-argument overload, defaults 0.5 and
+ * 0.5). */
+tvk_status tvk_tf1d_set_std_function(float* rgba, uint64_t n, float center, float inv_gradient,
+                                     int component, int inverted);
+/* TransferFunction1D::Set (TransferFunction1D.cpp:146-177): n RGBA bytes to
+ * floats, colour channels stretched by the per-channel min/max that
+ * minmax_component4 finds (:115-144: every channel's range starts from the
+ * table's first byte), alpha = byte / 255. */
+tvk_status tvk_tf1d_from_bytes(const uint8_t* rgba8, uint64_t n, float* rgba);
+/* TransferFunction1D::Resample (TransferFunction1D.cpp:198-238): box average
+ * down, linear interpolation up.  dst may equal src only when n_dst == n_src. */
+tvk_status tvk_tf1d_resample(const float* src, uint64_t n_src, float* dst, uint64_t n_dst);
+/* TransferFunction1D::FillOrTruncate (TransferFunction1D.cpp:188-197). */
+tvk_status tvk_tf1d_fill_or_truncate(const float* src, uint64_t n_src, float* dst,
+                                     uint64_t n_dst);
+/* TransferFunction1D::ComputeNonZeroLimits / GetNonZeroLimits
+ * (TransferFunction1D.cpp:362-371): limits = {first, last} entry with a
+ * non-zero alpha, {n, 0} when every alpha is 0. */
+tvk_status tvk_tf1d_nonzero_limits(const float* rgba, uint64_t n, uint64_t limits[2]);
+/* TransferFunction1D::GetByteArray / GetShortArray (TransferFunction1D.cpp:
+ * 311-351): each channel clamped to [0, 1], times used_range, truncated;
+ * out holds 4 * n values. */
+tvk_status tvk_tf1d_byte_array(const float* rgba, uint64_t n, uint8_t used_range, uint8_t* out);
+tvk_status tvk_tf1d_short_array(const float* rgba, uint64_t n, uint16_t used_range,
+                                uint16_t* out);
+/* TransferFunction1D::Load / Save (TransferFunction1D.cpp:240-306): the text
+ * format (entry count, then 4 numbers per entry).  Load with rgba == NULL
+ * stores the entry count in *n_out only; otherwise capacity must hold it.  A
+ * file whose stream is not good after the last number is refused, as
+ * Load(istream) refuses it. */
+tvk_status tvk_tf1d_load(const char* path, float* rgba, uint64_t capacity, uint64_t* n_out);
+tvk_status tvk_tf1d_save(const char* path, const float* rgba, uint64_t n);
 /* 2D TF (TransferFunction2D, IO/TransferFunction2D.cpp:222-264) as a float
  * table of h rows (gradient axis, row 0 at t = 0) by w columns (value axis). */
 tvk_status tvk_set_tf2d_float(tvk_renderer* r, const float* rgba, uint32_t w, uint32_t h,

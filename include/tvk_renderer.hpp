@@ -7,6 +7,7 @@
 #ifndef TVK_RENDERER_HPP
 #define TVK_RENDERER_HPP
 
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <memory>
@@ -137,6 +138,87 @@ class BrickedVolume {
 };
 
 // The renderer, named after AbstrRenderer's methods.
+// IO/TransferFunction1D.h:53-101 over the C ABI's table functions: the same
+// methods, each giving the reference's table bit for bit.
+class TransferFunction1D {
+ public:
+  explicit TransferFunction1D(size_t iSize = 0) : data_(4 * iSize, 0.0f) {}
+  explicit TransferFunction1D(const std::string& filename) { Load(filename); }
+
+  size_t GetSize() const { return data_.size() / 4; }
+  void Resize(size_t iSize) { data_.resize(4 * iSize, 0.0f); }
+  void SetStdFunction(float fCenterPoint = 0.5f, float fInvGradient = 0.5f) {
+    check(tvk_tf1d_set_std_function(data_.data(), GetSize(), fCenterPoint, fInvGradient, -1, 0));
+    ComputeNonZeroLimits();
+  }
+  void SetStdFunction(float fCenterPoint, float fInvGradient, int iComponent, bool bInvertedStep) {
+    check(tvk_tf1d_set_std_function(data_.data(), GetSize(), fCenterPoint, fInvGradient,
+                                    iComponent, bInvertedStep ? 1 : 0));
+    ComputeNonZeroLimits();
+  }
+  void Set(const std::vector<unsigned char>& tf) {
+    std::vector<float> t(tf.size() / 4 * 4);
+    check(tvk_tf1d_from_bytes(tf.data(), tf.size() / 4, t.data()));
+    data_.swap(t);
+    ComputeNonZeroLimits();
+  }
+  void Resample(size_t iTargetSize) {
+    if (iTargetSize == GetSize()) return;  // the reference returns before recomputing the limits
+    std::vector<float> t(4 * iTargetSize);
+    check(tvk_tf1d_resample(data_.data(), GetSize(), t.data(), iTargetSize));
+    data_.swap(t);
+    ComputeNonZeroLimits();
+  }
+  void FillOrTruncate(size_t iTargetSize) {
+    std::vector<float> t(4 * iTargetSize);
+    check(tvk_tf1d_fill_or_truncate(data_.data(), GetSize(), t.data(), iTargetSize));
+    data_.swap(t);
+    ComputeNonZeroLimits();
+  }
+  void Clear() {
+    std::fill(data_.begin(), data_.end(), 0.0f);
+    limits_ = {0, 0};
+  }
+  void ComputeNonZeroLimits() {
+    uint64_t l[2];
+    check(tvk_tf1d_nonzero_limits(data_.data(), GetSize(), l));
+    limits_ = {l[0], l[1]};
+  }
+  const std::array<uint64_t, 2>& GetNonZeroLimits() const { return limits_; }
+  std::array<float, 4> GetColor(size_t i) const {
+    return {data_[4 * i], data_[4 * i + 1], data_[4 * i + 2], data_[4 * i + 3]};
+  }
+  void SetColor(size_t i, const std::array<float, 4>& c) {
+    for (int k = 0; k < 4; ++k) data_[4 * i + k] = c[k];
+  }
+  const std::vector<float>& GetColorData() const { return data_; }
+  void GetByteArray(std::vector<unsigned char>& v, unsigned char cUsedRange = 255) const {
+    v.resize(data_.size());
+    check(tvk_tf1d_byte_array(data_.data(), GetSize(), cUsedRange, v.data()));
+  }
+  bool Load(const std::string& filename) {
+    uint64_t n = 0;
+    if (tvk_tf1d_load(filename.c_str(), nullptr, 0, &n) != TVK_OK) return false;
+    std::vector<float> t(4 * n);
+    if (tvk_tf1d_load(filename.c_str(), t.data(), n, &n) != TVK_OK) return false;
+    data_.swap(t);
+    ComputeNonZeroLimits();
+    return true;
+  }
+  bool Load(const std::string& filename, size_t iTargetSize) {
+    if (!Load(filename)) return false;
+    Resample(iTargetSize);
+    return true;
+  }
+  bool Save(const std::string& filename) const {
+    return tvk_tf1d_save(filename.c_str(), data_.data(), GetSize()) == TVK_OK;
+  }
+
+ private:
+  std::vector<float> data_;
+  std::array<uint64_t, 2> limits_{{0, 0}};
+};
+
 class Renderer {
  public:
   enum ERenderMode { RM_1DTRANS = TVK_RM_1DTRANS, RM_2DTRANS = TVK_RM_2DTRANS,
@@ -158,6 +240,9 @@ class Renderer {
   void Set1DTransFloat(const std::vector<float>& rgba, bool rgba8_upload = false) {
     check(tvk_set_tf1d_float(r_, rgba.data(), uint32_t(rgba.size() / 4), rgba8_upload));
   }
+  // AbstrRenderer::Changed1DTrans after editing the TransferFunction1D: the
+  // reference uploads its bytes (GetByteArray) as GL_RGBA8
+  void Set1DTrans(const TransferFunction1D& tf) { Set1DTransFloat(tf.GetColorData(), true); }
   void Set2DTransFloat(const std::vector<float>& rgba, uint32_t w, uint32_t h) {
     check(tvk_set_tf2d_float(r_, rgba.data(), w, h, 0));
   }

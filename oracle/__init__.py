@@ -86,6 +86,8 @@ def lib():
         L.orc_lod_aspect.restype = None
         L.orc_render.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p]
         L.orc_render.restype = C.c_uint64
+        L.orc_pow01.argtypes = [C.c_float, C.c_float]
+        L.orc_pow01.restype = C.c_float
         L.orc_round_half.argtypes = [C.c_float]
         L.orc_round_half.restype = C.c_float
         L.orc_render_timed.argtypes = [C.POINTER(Scene), C.POINTER(C.c_float), _u32p,
@@ -235,6 +237,11 @@ def build_octree(raw, bsize, overlap, clamp=False, median=False):
     for s, o in zip(shapes, offs):
         out.append(pool[int(o):int(o) + s[0] * s[1] * s[2]].reshape((s[2], s[1], s[0]) + comps))
     return out
+
+
+def pow01(x, y):
+    """The FP32 oracle's GLSL pow(x, y) for x in [0, 1]."""
+    return lib().orc_pow01(float(x), float(y))
 
 
 def round_half(x):

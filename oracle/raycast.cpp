@@ -40,6 +40,8 @@
 #include <omp.h>
 #endif
 
+extern "C" float orc_pow01(float x, float y);
+
 extern "C" float orc_round_half(float x) {
   // IEEE 754 binary16, round to nearest, ties to even.
   if (std::isnan(x) || std::isinf(x) || x == 0.0f) return x;
@@ -169,12 +171,71 @@ inline T len3(T x, T y, T z) { return std::sqrt((x * x + y * y) + z * z); }
 template <class T>
 inline T dot3(const T a[3], const T b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 
+// GLSL pow(x, y) for x in [0, 1] (opacity correction, specular terms),
+// defined by the shading language as exp2(y * log2(x)) with an
+// implementation-chosen precision.  The FP32 oracle fixes one such
+// implementation in double operations that round the same on every IEEE
+// machine, rounded to float at the end:
+//  * log2(x) = e + (2 / ln 2) * atanh(s) with x = m * 2^e, m in
+//    [sqrt(1/2), sqrt(2)), s = (m - 1) / (m + 1), and the atanh series
+//    s + s^3/3 + ... + s^13/13 (|s| <= 0.172: truncation below 1e-12);
+//  * exp2(t) = 2^k * e^(f ln 2), k = floor(t + 1/2), |f| <= 1/2, and the
+//    Taylor series of e^z to z^9 (truncation below 1e-10).
+// Results below 2^-125 are 0 (callers take 1 - x^y, which that leaves
+// unchanged).  The FP64 oracle keeps libm's pow.
+inline float pow01f(float xf, float yf) {
+  if (yf == 0.0f || xf == 1.0f) return 1.0f;
+  if (!(xf > 0.0f)) return 0.0f;
+  if (xf > 1.0f) return 1.0f;
+  const double x = double(xf);
+  uint64_t bits;
+  std::memcpy(&bits, &x, sizeof bits);
+  double e = double(int((bits >> 52) & 0x7ffu) - 1022);
+  const uint64_t mb = (bits & 0x000fffffffffffffull) | 0x3fe0000000000000ull;
+  double m;
+  std::memcpy(&m, &mb, sizeof m);
+  if (m < 0.70710678118654752) {
+    m = m * 2.0;
+    e = e - 1.0;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double s2 = s * s;
+  const double inv_odd[7] = {1.0 / 13.0, 1.0 / 11.0, 1.0 / 9.0, 1.0 / 7.0,
+                             1.0 / 5.0,  1.0 / 3.0,  1.0};
+  double p = inv_odd[0];
+  for (int i = 1; i < 7; ++i) p = std::fma(p, s2, inv_odd[i]);
+  const double lg = std::fma(2.8853900817779268 * s, p, e);
+  const double t = double(yf) * lg;
+  if (!(t > -125.0)) return 0.0f;
+  if (t >= 128.0) return INFINITY;
+  const double k = std::floor(t + 0.5);
+  const double z = (t - k) * 0.69314718055994531;
+  const double inv_fact[10] = {1.0 / 362880.0, 1.0 / 40320.0, 1.0 / 5040.0, 1.0 / 720.0,
+                               1.0 / 120.0,    1.0 / 24.0,    1.0 / 6.0,    0.5,
+                               1.0,            1.0};
+  double q = inv_fact[0];
+  for (int i = 1; i < 10; ++i) q = std::fma(q, z, inv_fact[i]);
+  const uint64_t kb = uint64_t(int(k) + 1023) << 52;
+  double two_k;
+  std::memcpy(&two_k, &kb, sizeof two_k);
+  return float(q * two_k);
+}
+
+inline float glsl_pow(float x, float y) { return pow01f(x, y); }
+
+}  // namespace
+
+extern "C" float orc_pow01(float x, float y) { return pow01f(x, y); }
+
+namespace {
+inline double glsl_pow(double x, double y) { return std::pow(x, y); }
+
 template <class T>
 inline T pow_int_or_real(T x, float e) {
   // exponents 8 (reference) and 32 (Blinn-Phong) by repeated squaring
   if (e == 8.0f) { T a = x * x; a = a * a; return a * a; }
   if (e == 32.0f) { T a = x * x; a = a * a; a = a * a; a = a * a; return a * a; }
-  return std::pow(x, T(e));
+  return glsl_pow(x, T(e));
 }
 
 struct Setup {
@@ -588,7 +649,7 @@ void brick_march_color(const Setup& st, const BrickR& b, const float dir[3], flo
     fi = std::fmin(std::fmax(fi, T(0)), T(W - 1));
     const float* e = &st.tf[4 * size_t(fi)];
     T src[4] = {v[0] * T(e[0]), v[1] * T(e[1]), v[2] * T(e[2]), v[3] * T(e[3])};
-    src[3] = T(1) - std::pow(T(1) - src[3], T(st.step_scale));
+    src[3] = T(1) - glsl_pow(T(1) - src[3], T(st.step_scale));
     if (s.lighting && src[3] != T(0)) {
       T N[3], lc[3];
       color_normal<T>(st, vol, pos, vstep, N);
@@ -1302,6 +1363,16 @@ float leaper_sample(const LeaperBrick& b, int dtype, float l0, float l1, float l
 
 inline float len3f(float x, float y, float z) { return std::sqrt((x * x + y * y) + z * z); }
 
+// ComputeLOD's uint(log2(x)) (GLVolumePool.cpp:650-656) as the exact floor of
+// the base-2 logarithm: the binary exponent of x for x >= 2, level 0 below 2
+// and for a NaN, the coarsest level for an infinity.
+inline uint32_t lod_level(float x, uint32_t max_lod) {
+  if (!(x >= 2.0f)) return 0u;
+  uint32_t bits;
+  std::memcpy(&bits, &x, sizeof bits);
+  return std::min(max_lod, ((bits >> 23) & 0xffu) - 127u);
+}
+
 }  // namespace
 
 extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page, uint64_t n_page,
@@ -1479,8 +1550,7 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
       if (ray_len > voxel_eps) {
         for (uint32_t j = 0; j < 100; ++j) {
           const float depth = entry_depth * (1.0f - t) + exit_depth * t;
-          const float lv = std::log2(lod_factor * (-depth) / lod0_err);
-          uint32_t lod = lv > 0.0f ? std::min(max_lod, uint32_t(lv)) : 0u;
+          uint32_t lod = lod_level(lod_factor * (-depth) / lod0_err, max_lod);
           float p[3];
           for (int a = 0; a < 3; ++a) p[a] = std::fmin(std::fmax(cur[a], 0.0f), 1.0f);
           uint32_t bc[3];

@@ -97,3 +97,83 @@ def histograms(raw, brick_size, overlap, clamp=False, value_bins=0, scratch="/tm
     if rc != 0:
         raise RuntimeError(f"reference histograms failed ({rc})")
     return h1[:n1.value], h2[:nv.value * 256].reshape(nv.value, 256), g.value
+
+
+# ---- TransferFunction1D (oracle/ref/ref_tf1d.cpp over IO/TransferFunction1D.cpp)
+
+def _f32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def tf1d_std(table, center, inv_gradient, component=-1, inverted=False):
+    """SetStdFunction on a copy of table (n x 4); component -1 = the
+    2-argument overload.  Returns (table, (lo, hi) non-zero limits)."""
+    L = _load()
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    out = np.zeros_like(t)
+    lim = (C.c_uint64 * 2)()
+    L.ref_tf1d_std.argtypes = [C.POINTER(C.c_float), C.c_uint64, C.c_float, C.c_float, C.c_int,
+                               C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_uint64)]
+    L.ref_tf1d_std(_f32p(t), t.shape[0], center, inv_gradient, component, int(inverted),
+                   _f32p(out), lim)
+    return out, (lim[0], lim[1])
+
+
+def tf1d_set(rgba_bytes):
+    L = _load()
+    b = np.ascontiguousarray(rgba_bytes, dtype=np.uint8).reshape(-1)
+    out = np.zeros((b.size // 4, 4), dtype=np.float32)
+    lim = (C.c_uint64 * 2)()
+    L.ref_tf1d_set.argtypes = [C.POINTER(C.c_uint8), C.c_uint64, C.POINTER(C.c_float),
+                               C.POINTER(C.c_uint64)]
+    L.ref_tf1d_set(b.ctypes.data_as(C.POINTER(C.c_uint8)), b.size // 4, _f32p(out), lim)
+    return out, (lim[0], lim[1])
+
+
+def tf1d_resample(table, target):
+    L = _load()
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    out = np.zeros((target, 4), dtype=np.float32)
+    lim = (C.c_uint64 * 2)()
+    L.ref_tf1d_resample.argtypes = [C.POINTER(C.c_float), C.c_uint64, C.c_uint64,
+                                    C.POINTER(C.c_float), C.POINTER(C.c_uint64)]
+    L.ref_tf1d_resample(_f32p(t), t.shape[0], target, _f32p(out), lim)
+    return out, (lim[0], lim[1])
+
+
+def tf1d_fill_or_truncate(table, target):
+    L = _load()
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    out = np.zeros((target, 4), dtype=np.float32)
+    L.ref_tf1d_fill_or_truncate.argtypes = [C.POINTER(C.c_float), C.c_uint64, C.c_uint64,
+                                            C.POINTER(C.c_float)]
+    L.ref_tf1d_fill_or_truncate(_f32p(t), t.shape[0], target, _f32p(out))
+    return out
+
+
+def tf1d_bytes(table, used_range=255):
+    L = _load()
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    out = np.zeros(t.size, dtype=np.uint8)
+    L.ref_tf1d_bytes.argtypes = [C.POINTER(C.c_float), C.c_uint64, C.c_uint8,
+                                 C.POINTER(C.c_uint8)]
+    L.ref_tf1d_bytes(_f32p(t), t.shape[0], used_range, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return out
+
+
+def tf1d_save(table, path):
+    L = _load()
+    t = np.ascontiguousarray(table, dtype=np.float32)
+    L.ref_tf1d_save.argtypes = [C.POINTER(C.c_float), C.c_uint64, C.c_char_p]
+    return bool(L.ref_tf1d_save(_f32p(t), t.shape[0], str(path).encode()))
+
+
+def tf1d_load(path, cap=1 << 16):
+    """(table, ok) as TransferFunction1D::Load(filename) leaves it."""
+    L = _load()
+    out = np.zeros((cap, 4), dtype=np.float32)
+    n = C.c_uint64()
+    L.ref_tf1d_load.argtypes = [C.c_char_p, C.POINTER(C.c_float), C.c_uint64,
+                                C.POINTER(C.c_uint64)]
+    ok = L.ref_tf1d_load(str(path).encode(), _f32p(out), cap, C.byref(n))
+    return (out[:n.value].copy(), True) if ok else (None, False)

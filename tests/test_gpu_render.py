@@ -155,15 +155,18 @@ def test_gpu_isosurface_matches_oracle(cuda_ok, scenes, vk, iso, eye):
 
 def test_gpu_render_rgba8_bytes_interface(cuda_ok, scenes):
     """Set1DTrans(bytes): TransferFunction1D::Set stretches colour channels by
-    their min/max (TransferFunction1D.cpp:146-177) and uploads GL_RGBA8."""
+    their min/max (TransferFunction1D.cpp:146-177; minmax_component4 starts
+    every channel's range from the table's first byte) and uploads GL_RGBA8."""
     raw = scenes["u8"]
     rng = np.random.default_rng(9)
     b = rng.integers(0, 256, size=(256, 4)).astype(np.uint8)
     b[:60, 3] = 0
-    b[:, 1] = 200  # a constant channel: the reference's lerp divides by zero -> 0
+    b[0, 0] = 10  # below the green channel: the green range starts at 10
+    b[:, 1] = np.maximum(b[:, 1], 30)
+    b[:, 2] = 10  # constant and equal to the first byte: the lerp divides by zero -> 0
     f = np.zeros((256, 4), dtype=np.float32)
     for c in range(3):
-        lo, hi = int(b[:, c].min()), int(b[:, c].max())
+        lo, hi = min(int(b[:, c].min()), int(b[0, 0])), max(int(b[:, c].max()), int(b[0, 0]))
         with np.errstate(divide="ignore", invalid="ignore"):
             q = np.float64(1.0) / np.float64(hi - lo)
             f[:, c] = (0.0 + (b[:, c].astype(np.float64) - lo) * q).astype(np.float32)

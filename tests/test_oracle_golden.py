@@ -204,6 +204,29 @@ def test_round_half_is_ieee_rne():
         assert O.round_half(x) == float(np.float32(np.float16(x))), x
 
 
+def test_glsl_pow_is_within_a_few_ulp():
+    """The FP32 oracle's pow(x, y) = exp2(y log2 x) (opacity correction of
+    colour samples, specular exponents other than 8 and 32) stays within one
+    ulp of the exact power over opacity-correction and specular ranges."""
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([rng.uniform(0, 1, 600), 1 - rng.uniform(0, 1e-4, 150),
+                         rng.uniform(0, 1e-3, 100), [2.0 ** -24, 0.5, 0.25, 1 - 2.0 ** -24]])
+    ys = np.concatenate([[1 / 1.5, 1.0, 2.0, 1 / 0.75, 0.5, 3.7, 16.0, 64.0, 128.0],
+                         rng.uniform(0.1, 100, 6)])
+    worst = 0.0
+    for y in ys.astype(np.float32):
+        for x in xs.astype(np.float32):
+            got = np.float32(O.pow01(x, y))
+            exact = float(x) ** float(y)
+            if exact < 2.0 ** -125:
+                assert got <= 2.0 ** -124
+                continue
+            ulp = np.spacing(np.float32(exact))
+            worst = max(worst, abs(float(got) - exact) / float(ulp))
+    assert worst <= 1.0, worst
+    assert O.pow01(0.0, 1.5) == 0.0 and O.pow01(1.0, 1.5) == 1.0 and O.pow01(0.3, 0.0) == 1.0
+
+
 def test_oracle_clip_plane_properties():
     """The oracle's clip plane: a plane beyond the volume changes nothing, one
     that cuts everything leaves an empty frame, and a half cut removes samples."""

@@ -6,6 +6,8 @@ GLRaycaster ray march.  This package holds the build recipe, a ctypes binding
 and a thin Python mirror of Tuvok's AbstrRenderer / dataset interfaces.
 """
 from ._native import TvkError, lib  # noqa: F401  (raises if libtvk.so is missing)
-from .renderer import Batch, Pool, Renderer, Volume, generate_volume_device  # noqa: F401
+from .renderer import (Batch, Pool, Renderer, TransferFunction1D, Volume,  # noqa: F401
+                       generate_volume_device)
 
-__all__ = ["Batch", "Pool", "Renderer", "Volume", "TvkError", "generate_volume_device", "lib"]
+__all__ = ["Batch", "Pool", "Renderer", "TransferFunction1D", "Volume", "TvkError",
+           "generate_volume_device", "lib"]

@@ -133,6 +133,15 @@ PROTOTYPES = {
     "tvk_set_tf1d_rgba8": [_vp, C.POINTER(C.c_uint8), C.c_uint32],
     "tvk_set_tf1d_float": [_vp, _f32p, C.c_uint32, C.c_int],
     "tvk_set_tf2d_float": [_vp, _f32p, C.c_uint32, C.c_uint32, C.c_int],
+    "tvk_tf1d_set_std_function": [_f32p, C.c_uint64, C.c_float, C.c_float, C.c_int, C.c_int],
+    "tvk_tf1d_from_bytes": [C.POINTER(C.c_uint8), C.c_uint64, _f32p],
+    "tvk_tf1d_resample": [_f32p, C.c_uint64, _f32p, C.c_uint64],
+    "tvk_tf1d_fill_or_truncate": [_f32p, C.c_uint64, _f32p, C.c_uint64],
+    "tvk_tf1d_nonzero_limits": [_f32p, C.c_uint64, _u64p],
+    "tvk_tf1d_byte_array": [_f32p, C.c_uint64, C.c_uint8, C.POINTER(C.c_uint8)],
+    "tvk_tf1d_short_array": [_f32p, C.c_uint64, C.c_uint16, C.POINTER(C.c_uint16)],
+    "tvk_tf1d_load": [C.c_char_p, _f32p, C.c_uint64, _u64p],
+    "tvk_tf1d_save": [C.c_char_p, _f32p, C.c_uint64],
     "tvk_set_render_mode": [_vp, C.c_int],
     "tvk_set_lighting": [_vp, C.c_int],
     "tvk_set_sample_rate_modifier": [_vp, C.c_float],

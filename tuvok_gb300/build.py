@@ -30,7 +30,7 @@ HOST_FLAGS = "-fPIC,-ffp-contract=off,-O3,-Wall"
 # unless the source writes fmaf, so it matches the oracle bit for bit
 EXTRA = {"raycast.cu": ["-fmad=false"]}
 SOURCES = ["api.cpp", "bricking.cu", "cnn.cu", "eo.cpp", "lod.cu", "raycast.cu", "rebrick.cu",
-           "volgen.cu"]
+           "tf1d.cpp", "volgen.cu"]
 HEADERS = [CSRC / "tvk_internal.h", ROOT / "include" / "tvk.h"]
 ORACLE_SOURCES = [ROOT / "oracle" / "bricking.cpp", ROOT / "oracle" / "raycast.cpp",
                   ROOT / "oracle" / "rebrick.cpp"]
@@ -96,13 +96,18 @@ def build_oracle(verbose: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_reference(verbose: bool = False) -> Path | None:
-    """Builds oracle/_ref (the reference's own converter) when its sources exist."""
+def build_reference(verbose: bool = False, ref: Path | None = None) -> Path | None:
+    """Builds oracle/_ref (the reference's own converter) when its sources exist.
+
+    ref: the reference source tree (passed to the Makefile as REF); None keeps
+    the Makefile's default."""
     mk = ROOT / "oracle" / "ref" / "Makefile"
     if not mk.exists():
         return None
-    r = subprocess.run(["make", "-s", "-C", str(mk.parent), f"-j{os.cpu_count() or 4}"],
-                       capture_output=True, text=True)
+    cmd = ["make", "-s", "-C", str(mk.parent), f"-j{os.cpu_count() or 4}"]
+    if ref is not None:
+        cmd.append(f"REF={ref}")
+    r = subprocess.run(cmd, capture_output=True, text=True)
     if verbose:
         print(r.stdout + r.stderr)
     if r.returncode != 0:

@@ -2596,27 +2596,11 @@ tvk_status tvk_renderer_set_volume(tvk_renderer* r, const tvk_volume* v) {
 tvk_status tvk_set_tf1d_rgba8(tvk_renderer* r, const uint8_t* rgba, uint32_t n) {
   return guarded([&] {
     REQUIRE(r && rgba && n >= 2, "need a renderer and at least two TF entries");
-    // TransferFunction1D::Set (TransferFunction1D.cpp:146-177): colour channels
-    // lerped from their per-channel [min, max] onto [0, 1], alpha byte/255.
-    uint8_t mn[4] = {255, 255, 255, 255}, mx[4] = {0, 0, 0, 0};
-    for (uint32_t i = 0; i < n; ++i)
-      for (int c = 0; c < 4; ++c) {
-        mn[c] = std::min(mn[c], rgba[4 * i + c]);
-        mx[c] = std::max(mx[c], rgba[4 * i + c]);
-      }
-    // MathTools::lerp (Basics/MathTools.h:81-84):
-    //   out(omin + (value - imin) * (double(omax - omin) / (imax - imin)))
-    // A constant channel divides by zero; the NaN it yields becomes 0 in the
-    // RGBA8 upload below, as in the reference.
-    auto lerp = [](int value, int imin, int imax) {
-      const double q = double(1.0f - 0.0f) / double(imax - imin);
-      return float(0.0f + double(value - imin) * q);
-    };
+    // TransferFunction1D::Set (TransferFunction1D.cpp:146-177); a constant
+    // channel divides by zero, and the NaN it yields becomes 0 in the RGBA8
+    // upload below, as in the reference
     std::vector<float> f(size_t(4) * n);
-    for (uint32_t i = 0; i < n; ++i) {
-      for (int c = 0; c < 3; ++c) f[4 * i + c] = lerp(rgba[4 * i + c], mn[c], mx[c]);
-      f[4 * i + 3] = lerp(rgba[4 * i + 3], 0, 255);
-    }
+    tvk::tf1d_from_bytes(rgba, n, f.data());
     tvk::set_tf(r, f.data(), n, 1, true);
   });
 }

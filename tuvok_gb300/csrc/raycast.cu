@@ -245,10 +245,59 @@ __device__ __forceinline__ float clamp_u(float t, float fn, int n) {
   return fminf(fmaxf(fmaf(t, fn, -0.5f), 0.0f), float(n - 1));
 }
 
+// x^y for x in [0, 1] as exp2(y * log2(x)) (GLSL defines pow as that
+// composition and leaves its precision to the implementation), in double
+// operations that give the same bits on any IEEE machine, rounded to float:
+//  * log2(x) = e + (2 / ln 2) * atanh(s), x = m * 2^e with m in [sqrt(1/2),
+//    sqrt(2)), s = (m - 1) / (m + 1) (|s| <= 0.172), the atanh series
+//    s + s^3/3 + ... + s^13/13 (truncation below 1e-12);
+//  * exp2(t) = 2^k * e^(f ln 2), k = floor(t + 1/2), |f| <= 1/2, the Taylor
+//    series of e^z to z^9 (truncation below 1e-10).
+// Within one float ulp of the exact power.  Results below 2^-125 are
+// returned as 0: callers use 1 - x^y, which that leaves unchanged.
+__device__ __forceinline__ float pow01(float xf, float yf) {
+  if (yf == 0.0f || xf == 1.0f) return 1.0f;
+  if (!(xf > 0.0f)) return 0.0f;
+  if (xf > 1.0f) return 1.0f;  // a rounded dot product of unit vectors
+  const double x = double(xf);
+  const uint64_t bits = uint64_t(__double_as_longlong(x));
+  double e = double(int((bits >> 52) & 0x7ffu) - 1022);  // float inputs: never subnormal here
+  double m = __longlong_as_double(
+      (long long)((bits & 0x000fffffffffffffull) | 0x3fe0000000000000ull));  // [0.5, 1)
+  if (m < 0.70710678118654752) { m = m * 2.0; e = e - 1.0; }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double s2 = s * s;
+  double p = 1.0 / 13.0;
+  p = fma(p, s2, 1.0 / 11.0);
+  p = fma(p, s2, 1.0 / 9.0);
+  p = fma(p, s2, 1.0 / 7.0);
+  p = fma(p, s2, 1.0 / 5.0);
+  p = fma(p, s2, 1.0 / 3.0);
+  p = fma(p, s2, 1.0);
+  const double lg = fma(2.8853900817779268 * s, p, e);  // 2 / ln 2
+  const double t = double(yf) * lg;
+  if (!(t > -125.0)) return 0.0f;
+  if (t >= 128.0) return INFINITY;  // y < 0
+  const double k = floor(t + 0.5);
+  const double z = (t - k) * 0.69314718055994531;  // ln 2
+  double q = 1.0 / 362880.0;
+  q = fma(q, z, 1.0 / 40320.0);
+  q = fma(q, z, 1.0 / 5040.0);
+  q = fma(q, z, 1.0 / 720.0);
+  q = fma(q, z, 1.0 / 120.0);
+  q = fma(q, z, 1.0 / 24.0);
+  q = fma(q, z, 1.0 / 6.0);
+  q = fma(q, z, 0.5);
+  q = fma(q, z, 1.0);
+  q = fma(q, z, 1.0);
+  const double two_k = __longlong_as_double((long long)(uint64_t(int(k) + 1023) << 52));
+  return float(q * two_k);
+}
+
 __device__ __forceinline__ float pow_int_or_real(float x, float e) {
   if (e == 8.0f) { float a = x * x; a = a * a; return a * a; }
   if (e == 32.0f) { float a = x * x; a = a * a; a = a * a; a = a * a; return a * a; }
-  return powf(x, e);
+  return pow01(x, e);
 }
 
 __device__ __forceinline__ void lighting_ref(const RenderParams& P, const float pos[3],
@@ -932,7 +981,7 @@ __device__ __forceinline__ float4 march_brick_color(const RenderParams& P, const
     fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
     const float4 t = __ldg(&P.tf[int(fx)]);
     float4 src = make_float4(v0 * t.x, v1 * t.y, v2 * t.z, v3 * t.w);
-    src.w = 1.0f - powf(1.0f - src.w, P.step_scale);
+    src.w = 1.0f - pow01(1.0f - src.w, P.step_scale);
     if (lit && src.w != 0.0f) {
       ++graded;
       float N[3];
@@ -1587,6 +1636,17 @@ __device__ __forceinline__ void report_missing(const LeaperParams& L, const uint
 }
 
 // ComputeBrickCoords + GetBrickInfo
+// uint(log2(x)) of ComputeLOD as the exact floor of the base-2 logarithm:
+// for x >= 2 the binary exponent of x (an approximate log2 could round up to
+// the next integer within an ulp of a power of two), 0 below 2 -- [1, 2) has
+// level 0 and a negative logarithm is level 0 as well -- and for a NaN; an
+// infinity takes the coarsest level.
+__device__ __forceinline__ uint32_t lod_level(float x, uint32_t max_lod) {
+  if (!(x >= 2.0f)) return 0u;
+  const uint32_t e = ((__float_as_uint(x) >> 23) & 0xffu) - 127u;
+  return min(max_lod, e);
+}
+
 __device__ __forceinline__ uint32_t brick_info(const LeaperParams& L, const float p[3],
                                                uint32_t lod, uint32_t bc[3]) {
 #pragma unroll
@@ -1684,9 +1744,9 @@ __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(cons
   if (ray_len > voxel_eps) {
     for (uint32_t j = 0; j < 100; ++j) {
       const float depth = entry_depth * (1.0f - t) + exit_depth * t;
-      // ComputeLOD (GLVolumePool.cpp:650-653); a negative level is level 0
-      const float lv = log2f(L.lod_factor * (-depth) / L.lod0_err);
-      uint32_t lod = lv > 0.0f ? min(L.max_lod, uint32_t(lv)) : 0u;
+      // ComputeLOD (GLVolumePool.cpp:650-656): uint(log2(x)), a negative
+      // level is level 0
+      uint32_t lod = lod_level(L.lod_factor * (-depth) / L.lod0_err, L.max_lod);
       // GetBrick (GLVolumePool.cpp:553-612)
       float p[3];
 #pragma unroll

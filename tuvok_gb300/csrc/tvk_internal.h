@@ -67,6 +67,9 @@ void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
                          const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
                          uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
                          uint64_t* launches);
+// TransferFunction1D::Set byte semantics (tf1d.cpp)
+void tf1d_from_bytes(const uint8_t* bytes, uint64_t n, float* rgba);
+
 // ExtendedOctree tables and UVF metadata (api.cpp)
 std::vector<LodInfo> lod_table(const uint64_t dims[3], const uint32_t B[3], uint32_t ov);
 

@@ -208,6 +208,115 @@ class Volume:
         return tuple(out)
 
 
+class TransferFunction1D:
+    """Tuvok's TransferFunction1D (IO/TransferFunction1D.h:53-101) over the C
+    ABI's table functions: an n x 4 float32 RGBA table with the reference's
+    methods, each giving its table bit for bit.  Host only.  Hand it to a
+    renderer with ``Renderer.Set1DTransFloat(tf.GetColorData())``."""
+
+    def __init__(self, size=0):
+        self._t = np.zeros((int(size), 4), dtype=np.float32)
+        self._limits = (0, 0)
+
+    @classmethod
+    def FromFile(cls, path, target_size=None):
+        tf = cls()
+        tf.Load(path, target_size)
+        return tf
+
+    def _p(self, a=None):
+        a = self._t if a is None else a
+        return a.ctypes.data_as(N._f32p)
+
+    def GetSize(self):
+        return self._t.shape[0]
+
+    def Resize(self, size):
+        t = np.zeros((int(size), 4), dtype=np.float32)
+        k = min(int(size), self._t.shape[0])
+        t[:k] = self._t[:k]
+        self._t = t
+
+    def GetColorData(self):
+        return self._t
+
+    def GetColor(self, i):
+        return tuple(float(x) for x in self._t[i])
+
+    def SetColor(self, i, rgba):
+        self._t[i] = rgba
+
+    def SetStdFunction(self, center=0.5, inv_gradient=0.5, component=None, inverted=False):
+        """Both overloads: component None sets all four channels (not inverted)."""
+        c = -1 if component is None else int(component)
+        check(lib().tvk_tf1d_set_std_function(self._p(), self._t.shape[0], float(center),
+                                              float(inv_gradient), c, int(bool(inverted))))
+        self.ComputeNonZeroLimits()
+
+    def Set(self, rgba_bytes):
+        b = np.ascontiguousarray(np.asarray(rgba_bytes, dtype=np.uint8).reshape(-1))
+        t = np.zeros((b.size // 4, 4), dtype=np.float32)
+        with np.errstate(all="ignore"):
+            check(lib().tvk_tf1d_from_bytes(b.ctypes.data_as(C.POINTER(C.c_uint8)), b.size // 4,
+                                            self._p(t)))
+        self._t = t
+        self.ComputeNonZeroLimits()
+
+    def Resample(self, target_size):
+        target_size = int(target_size)
+        if target_size == self._t.shape[0]:
+            return  # the reference returns before recomputing the limits
+        t = np.zeros((target_size, 4), dtype=np.float32)
+        check(lib().tvk_tf1d_resample(self._p(), self._t.shape[0], self._p(t), target_size))
+        self._t = t
+        self.ComputeNonZeroLimits()
+
+    def FillOrTruncate(self, target_size):
+        t = np.zeros((int(target_size), 4), dtype=np.float32)
+        check(lib().tvk_tf1d_fill_or_truncate(self._p(), self._t.shape[0], self._p(t),
+                                              t.shape[0]))
+        self._t = t
+        self.ComputeNonZeroLimits()
+
+    def Clear(self):
+        self._t[:] = 0.0
+        self._limits = (0, 0)
+
+    def ComputeNonZeroLimits(self):
+        lim = (C.c_uint64 * 2)()
+        check(lib().tvk_tf1d_nonzero_limits(self._p(), self._t.shape[0], lim))
+        self._limits = (int(lim[0]), int(lim[1]))
+
+    def GetNonZeroLimits(self):
+        return self._limits
+
+    def GetByteArray(self, used_range=255):
+        out = np.zeros(self._t.size, dtype=np.uint8)
+        check(lib().tvk_tf1d_byte_array(self._p(), self._t.shape[0], int(used_range),
+                                        out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out
+
+    def GetShortArray(self, used_range=4095):
+        out = np.zeros(self._t.size, dtype=np.uint16)
+        check(lib().tvk_tf1d_short_array(self._p(), self._t.shape[0], int(used_range),
+                                         out.ctypes.data_as(C.POINTER(C.c_uint16))))
+        return out
+
+    def Load(self, path, target_size=None):
+        n = C.c_uint64()
+        p = str(path).encode()
+        check(lib().tvk_tf1d_load(p, None, 0, C.byref(n)))
+        t = np.zeros((n.value, 4), dtype=np.float32)
+        check(lib().tvk_tf1d_load(p, self._p(t), n.value, C.byref(n)))
+        self._t = t
+        self.ComputeNonZeroLimits()
+        if target_size is not None:
+            self.Resample(target_size)
+
+    def Save(self, path):
+        check(lib().tvk_tf1d_save(str(path).encode(), self._p(), self._t.shape[0]))
+
+
 class Renderer:
     """GLRaycaster-equivalent renderer (AbstrRenderer's API over libtvk.so)."""
 
