@@ -3,7 +3,7 @@
 // oracle/ref/Makefile into oracle/_ref/libtuvok_ref.so.
 //
 // TEST INFRASTRUCTURE ONLY: pins tuvok_gb300's tvk_tf1d_* table functions
-// (and the golden vectors tests/golden/make_tf1d_golden.py writes) to the
+// (and the golden vectors tests/golden/tf1d/make_tf1d_golden.py writes) to the
 // reference's methods on the same inputs.
 #include <cstdint>
 #include <cstring>

@@ -6,7 +6,7 @@ Every case stores its inputs and the reference's resulting table and non-zero
 limits; tests/test_tf1d.py compares tuvok_gb300's tvk_tf1d_* functions with
 them (and with the live reference where it is built).
 
-    python tests/golden/make_tf1d_golden.py
+    python tests/golden/tf1d/make_tf1d_golden.py
 """
 import sys
 from pathlib import Path
@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-sys.path.insert(0, str(HERE.parent))
+sys.path.insert(0, str(HERE.parent.parent))
 
 import refconv  # noqa: E402
 

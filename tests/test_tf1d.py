@@ -1,6 +1,6 @@
 """TransferFunction1D (IO/TransferFunction1D.cpp) as tuvok_gb300's table
 functions (tvk_tf1d_*, host code in libtvk.so, no GPU needed) against the
-reference's own class: the golden vectors tests/golden/make_tf1d_golden.py
+reference's own class: the golden vectors tests/golden/tf1d/make_tf1d_golden.py
 wrote from it, and the live class where oracle/_ref is built.  Tables, non-zero
 limits and byte arrays are compared bit for bit (NaN where the reference
 divides by zero)."""
@@ -12,7 +12,7 @@ import pytest
 import refconv
 from tuvok_gb300 import TransferFunction1D
 
-GOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "tf1d.npz")
+GOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "tf1d" / "tf1d.npz")
 
 
 def _cases(prefix):
