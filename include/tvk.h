@@ -760,13 +760,16 @@ tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out);
  * tvk_volume_get_brick_histograms reports to get the same bins).  Work is
  * queued on `stream` (a cudaStream_t, NULL for the legacy default stream) and
  * the call returns without waiting.
- *   - count above TVK_NOALLOC_MAX_BRICKS, or an output smaller than the
- *     bricks, is rejected with TVK_ERR_INVALID_ARG and a message;
+ *   - count above TVK_NOALLOC_MAX_BRICKS, an output smaller than the bricks,
+ *     or a pointer not aligned to its element (voxels to the voxel size,
+ *     device_minmax_out to 8 bytes, device_hist_out to 4) is rejected with
+ *     TVK_ERR_INVALID_ARG and a message before any GPU work is queued;
  *   - the fixed accumulators are shared: each call clears what it uses, and
  *     calls whose GPU work overlaps (different streams or host threads) race;
  *   - the first call on a device looks up the accumulators' device address for
  *     that device (the current device); make that first call before any stream
- *     capture starts. */
+ *     capture starts.  The address is kept for the life of the process, so the
+ *     entry point must not be used after a cudaDeviceReset of that device. */
 #define TVK_NOALLOC_MAX_BRICKS 64
 tvk_status tvk_brick_lod0_noalloc(const void* device_voxels, tvk_dtype dtype,
                                   const uint64_t dims[3], const uint32_t brick_size[3],

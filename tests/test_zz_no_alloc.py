@@ -63,6 +63,8 @@ def run_noalloc(torch, d_raw, dtype, dims, bs, ov, clamp, coords, shift, stream)
 @pytest.mark.parametrize("dims,dtype,bs,ov,clamp", [
     ((61, 47, 39), np.uint16, 18, 1, False),
     ((40, 33, 20), np.uint8, 12, 2, True),
+    # 10 x 10 x 10 bricks: both calls fill the array (exactly 64 bricks each)
+    ((80, 80, 80), np.uint16, 12, 2, False),
 ])
 def test_noalloc_matches_allocating_path_twice(cuda_ok, dims, dtype, bs, ov, clamp):
     import torch
@@ -79,6 +81,8 @@ def test_noalloc_matches_allocating_path_twice(cuda_ok, dims, dtype, bs, ov, cla
     # two calls in a row over different (and differently sized) brick sets
     first = all_coords[::2][:N_MAX]
     second = all_coords[1::2][:N_MAX][::-1]
+    if len(all_coords) >= 2 * N_MAX:
+        assert len(first) == len(second) == N_MAX
     for coords in (first, second):
         bricks, mm, hist = run_noalloc(torch, d_raw, dtype, dims, bs, ov, clamp, coords, shift,
                                        stream)
@@ -108,3 +112,14 @@ def test_noalloc_rejects_too_many_bricks(cuda_ok):
                                     1, 0, C.c_void_p(d.data_ptr()), 16,
                                     C.c_void_p(d.data_ptr()), C.c_void_p(d.data_ptr()), None)
     assert st == 1 and b"output buffer" in lib.tvk_last_error()
+    # misaligned outputs are refused before any GPU work
+    base = d.data_ptr()
+    for args, what in (((base + 1, base, base), b"voxel pointers"),
+                       ((base, base + 4, base), b"8-byte"),
+                       ((base, base, base + 2), b"4-byte")):
+        out, mm, hist = args
+        st = lib.tvk_brick_lod0_noalloc(C.c_void_p(base), 1, (C.c_uint64 * 3)(4, 4, 4),
+                                        (C.c_uint32 * 3)(6, 6, 6), 1, 0, (C.c_uint64 * 3)(0, 0, 0),
+                                        1, 0, C.c_void_p(out), 1 << 20, C.c_void_p(mm),
+                                        C.c_void_p(hist), None)
+        assert st == 1 and what in lib.tvk_last_error(), what

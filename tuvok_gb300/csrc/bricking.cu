@@ -519,7 +519,9 @@ __global__ void noalloc_finish_kernel(const uint32_t* scratch, uint32_t count,
   for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist_out[256u * b + i] = mine[2 + i];
 }
 
-// Device address of g_noalloc_scratch, looked up once per device.
+// Device address of g_noalloc_scratch, looked up once per device and kept for
+// the life of the process (a cudaDeviceReset ends the context it belongs to:
+// the entry point is not for use after one).
 uint32_t* noalloc_scratch_for_current_device() {
   static std::mutex mu;
   static void* addr[64] = {nullptr};
@@ -550,6 +552,15 @@ void brick_lod0_noalloc(const void* raw, tvk_dtype dtype, const uint64_t dims[3]
                                   " bricks per call (the fixed scratch holds that many)");
   if (shift > 16) fail(TVK_ERR_INVALID_ARG, "histogram shift above 16");
   const int bytes = dtype == TVK_U8 ? 1 : 2;
+  // every pointer the kernels dereference must be aligned to its element type:
+  // a misaligned one would fault on the GPU instead of returning an error here
+  auto misaligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) != 0; };
+  if (misaligned(raw, bytes) || misaligned(bricks_out, bytes))
+    fail(TVK_ERR_INVALID_ARG, "voxel pointers must be aligned to the voxel size (2 bytes for u16)");
+  if (misaligned(minmax_out, alignof(double)))
+    fail(TVK_ERR_INVALID_ARG, "device_minmax_out must be 8-byte aligned");
+  if (misaligned(hist_out, alignof(uint32_t)))
+    fail(TVK_ERR_INVALID_ARG, "device_hist_out must be 4-byte aligned");
   BrickGrid g;
   uint64_t lod_size[3];
   for (int a = 0; a < 3; ++a) {
@@ -557,11 +568,16 @@ void brick_lod0_noalloc(const void* raw, tvk_dtype dtype, const uint64_t dims[3]
     if (bsz[a] <= 2 * ov || bsz[a] > 4096)
       fail(TVK_ERR_INVALID_ARG, "brick size must exceed twice the overlap and be <= 4096");
     const uint64_t usable = bsz[a] - 2ull * ov;
+    const uint64_t cnt = (dims[a] + usable - 1) / usable;  // ExtendedOctree.cpp:231-236
+    if (cnt >= (1ull << 32)) fail(TVK_ERR_INVALID_ARG, "2^32 or more bricks along one axis");
     g.dims[a] = dims[a];
     g.B[a] = bsz[a];
-    g.cnt[a] = uint32_t((dims[a] + usable - 1) / usable);  // ExtendedOctree.cpp:231-236
+    g.cnt[a] = uint32_t(cnt);
     lod_size[a] = dims[a];
   }
+  if (dims[1] > UINT64_MAX / dims[0] || dims[2] > UINT64_MAX / (dims[0] * dims[1]) ||
+      dims[0] * dims[1] * dims[2] > UINT64_MAX / 2)
+    fail(TVK_ERR_INVALID_ARG, "volume dimensions overflow 64 bits");
   g.ov = ov;
   g.clamp = clamp ? 1 : 0;
   g.total = dims[0] * dims[1] * dims[2];

@@ -82,6 +82,11 @@ void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e)
   std::FILE* f = fh.f;
   e.path = path;
   e.base = offset;
+  if (fseeko(f, 0, SEEK_END) != 0) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: seek failed");
+  const off_t end = ftello(f);
+  if (end < 0) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: cannot size the file");
+  const uint64_t file_size = uint64_t(end);
+  if (offset > file_size) fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: offset beyond the file");
   seek(f, offset);
   // ExtendedOctree.cpp:91-118: the global header, in the writer's byte order
   // (both are little-endian here)
@@ -102,9 +107,15 @@ void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e)
   e.size = read_value<uint64_t>(f);
   e.compression_level = e.version > 1 ? read_value<uint32_t>(f) : 0;
   const double asp = e.aspect[0] * e.aspect[1] * e.aspect[2];
-  if (e.components == 0 || e.dims[0] * e.dims[1] * e.dims[2] == 0 || asp == 0 ||
-      e.brick_size[0] * e.brick_size[1] * e.brick_size[2] == 0)
+  if (e.components == 0 || e.dims[0] == 0 || e.dims[1] == 0 || e.dims[2] == 0 || asp == 0 ||
+      e.brick_size[0] == 0 || e.brick_size[1] == 0 || e.brick_size[2] == 0)
     fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: empty volume, aspect or brick size");
+  // the voxel count must fit 64 bits (a corrupt header could claim more)
+  if (e.dims[1] > UINT64_MAX / e.dims[0] || e.dims[2] > UINT64_MAX / (e.dims[0] * e.dims[1]))
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: volume dimensions overflow 64 bits");
+  // ExtendedOctree.cpp:131-133: precomputed normals need four components
+  if (e.normals && e.components != 4)
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: precomputed normals need four components");
   for (int a = 0; a < 3; ++a)
     if (e.brick_size[a] <= 2ull * e.overlap || e.brick_size[a] > 4096)
       fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: brick size out of range");
@@ -115,6 +126,10 @@ void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e)
   const std::vector<LodInfo> lods = lod_table(e.dims, bs32, e.overlap);
   uint64_t n = 0;
   for (const LodInfo& l : lods) n += l.bricks[0] * l.bricks[1] * l.bricks[2];
+  // the table must fit in what is left of the file (36 bytes per entry)
+  const off_t here = ftello(f);
+  if (here < 0 || n > (file_size - uint64_t(here)) / 36)
+    fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: the brick table runs past the end of the file");
   e.toc.resize(n);
   for (uint64_t k = 0; k < n; ++k) {
     EoFile::Entry& t = e.toc[k];
@@ -124,6 +139,8 @@ void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e)
     t.valid_length = read_value<uint64_t>(f);
     t.atlas[0] = read_value<uint32_t>(f);
     t.atlas[1] = read_value<uint32_t>(f);
+    if (t.offset > file_size - offset || t.length > file_size - offset - t.offset)
+      fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: a brick lies past the end of the file");
   }
 }
 
