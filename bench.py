@@ -11,8 +11,10 @@ consecutive frames use different poses and the inputs exceed L2.  ``e2e`` times
 the same frames through the C ABI with the image read back to pinned host
 memory each step.  ``--impl reference`` times the CPU restatement of the
 reference's ray march (the oracle) on all host cores on a bounded sample of
-rows of each frame.  Multi-GPU runs are independent replicas (the path does
-not shard): rank 0 prints the aggregate.
+rows of each frame; it generates the same volume on the host (the generator's
+host restatement) and loads nothing of the product.  Both lines carry the
+volume's digest in ``config``.  Multi-GPU runs are independent replicas (the
+path does not shard): rank 0 prints the aggregate.
 """
 from __future__ import annotations
 
@@ -175,6 +177,26 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def workload_config(w, ws, frame_ert, vol_hash):
+    """The `config` object of both arms' lines (same keys and values)."""
+    voxel = "u8" if w.dtype == np.uint8 else "u16"
+    if voxel == "u16" and w.vmax == 4095:
+        voxel += " (12-bit)"
+    if not w.lighting:
+        light = "none"
+    elif w.light_model == 1:
+        light = "blinn-phong ka0.2 kd0.6 ks0.2 n32"
+    else:
+        light = "reference (lighting.glsl)"
+    return {"workload": w.name, "dims": list(w.dims), "voxel": voxel,
+            "brick": list(w.brick_size), "width": w.width, "height": w.height, "srm": w.srm,
+            "lighting": light, "tf": w.tf_kind, "poses": w.n_poses, "frame_ert": frame_ert,
+            "l2": "inputs larger than L2 (the brick pool exceeds the 129 MB L2); each step a "
+                  "different pose",
+            "parallelism": f"replicas x{ws}",
+            "volume_fnv1a": vol_hash}
+
+
 def make_volume(w, torch):
     """Generates the workload's volume in HBM and bricks it on the GPU."""
     from tuvok_gb300 import Volume, generate_volume_device
@@ -203,50 +225,87 @@ def configure(r, w, vol, frame_ert):
     r.Resize(w.width, w.height)
 
 
-def cpu_baseline(w, raw_host, poses, seconds, samples_per_frame, threads):
-    """Times the oracle (CPU restatement of the reference march) on every
-    r-th row of one frame, r chosen for about `seconds` of work."""
+def parity_rows(img, cnt, ref, rc, rows):
+    d = np.abs(img[rows].astype(np.float64) - ref[rows].astype(np.float64))
+    out = {"max_255": float(d.max() * 255), "mean_255": float(d.mean() * 255),
+           "rows": int(len(rows))}
+    if cnt is not None and rc is not None:
+        out["counts_equal"] = bool(np.array_equal(cnt[rows], rc[rows]))
+    return out
+
+
+def cpu_leg(w, raw_host, poses, seconds, samples_per_frame, threads, frame0):
+    """The CPU side of the run (after every GPU measurement):
+    * march: the oracle (CPU restatement of the reference march) on every r-th
+      row of pose 0, r chosen for about `seconds` of work, on all host cores;
+    * parity: the GPU frame of pose 0 (frame0 = image, counts) against those
+      FP32 oracle rows, and against the FP64 oracle on a sparser row sample;
+    * bricking: the serial restatement of ExtendedOctreeConverter::Convert
+      (every LOD, ghost voxels, per-brick min/max, 1D histogram) on one core;
+    * the volume's digest."""
     import oracle as O
+    vol_hash = O.volume_hash(raw_host, threads)
     t0 = time.perf_counter()
     prep = O.Prepared(raw_host, w.brick_size, w.overlap, w.tf(), srm=w.srm, lighting=w.lighting,
                       light_model=w.light_model, threads=threads)
     setup_s = time.perf_counter() - t0
     eye, at, up = poses[0]
     # calibrate on a sparse pass, then size the sample
-    stride = 64
     _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
-                          row_stride=stride, threads=threads)
+                          row_stride=64, threads=threads)
     rate = max(n / max(t, 1e-6), 1.0)
     target = rate * seconds
     stride = max(1, min(w.height, int(math.ceil(samples_per_frame / max(target, 1.0)))))
-    _, n, t = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
-                          row_stride=stride, threads=threads)
-    rows = len(range(0, w.height, stride))
-    frac = rows / w.height
+    ref, n, t, rc = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                                row_stride=stride, threads=threads, want_counts=True)
+    rows = np.arange(0, w.height, stride)
+    frac = len(rows) / w.height
+    parity = None
+    if frame0 is not None:
+        img, cnt = frame0
+        parity = parity_rows(img, cnt, ref, rc, rows)
+        stride64 = max(stride, 8) if w.height > 512 else stride
+        ref64, _, _ = prep.render(eye=eye, at=at, up=up, width=w.width, height=w.height,
+                                  row_stride=stride64, threads=threads, use_double=True)
+        p64 = parity_rows(img, None, ref64, None, np.arange(0, w.height, stride64))
+        parity.update({"fp64_max_255": p64["max_255"], "fp64_mean_255": p64["mean_255"],
+                       "fp64_rows": p64["rows"], "pose": 0,
+                       "bar": "max <= 2/255, mean <= 0.25/255 vs the FP32 oracle, sample "
+                              "counts equal"})
     prep.close()
-    return {"fps": frac / t, "msamples_s": n / t / 1e6, "rows": rows, "stride": stride,
-            "march_s": t, "setup_s": setup_s, "samples": n}
+    conv_s, n_bricks, pool_bytes = O.convert_timed(raw_host, w.brick_size, w.overlap)
+    raw_bytes = raw_host.nbytes
+    return {"fps": frac / t, "msamples_s": n / t / 1e6, "rows": len(rows), "stride": stride,
+            "march_s": t, "setup_s": setup_s, "samples": n, "parity": parity,
+            "volume_fnv1a": vol_hash,
+            "bricking": {"seconds": conv_s, "cores": 1, "bricks": n_bricks,
+                         "raw_bytes": raw_bytes, "pool_bytes": pool_bytes,
+                         "gb_per_s": (raw_bytes + pool_bytes) / conv_s / 1e9,
+                         "kind": "port",
+                         "what": "serial restatement of ExtendedOctreeConverter::Convert "
+                                 "(every LOD + ghost voxels + per-brick min/max) plus the 1D "
+                                 "histogram, no file IO"}}
 
 
 def run_reference(args):
     """--impl reference: the oracle's CPU march on all host cores, bounded
-    samples of each frame; rank 0 only."""
+    samples of each frame; rank 0 only.  The volume comes from the host
+    restatement of the generator (the same bytes as the GPU arm's, digest in
+    config); nothing of the product is loaded."""
     ws, rank, local = dist_setup("reference")
     if rank != 0:
         return
-    import torch
     import oracle as O
     from tuvok_gb300.build import build_oracle
     from tuvok_gb300.workloads import WORKLOADS
     build_oracle()
     w = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
-    torch.cuda.set_device(local)
-    # input creation only: the volume is generated on the GPU and copied out
-    vol, raw, _ = make_volume(w, torch)
-    raw_host = raw.cpu().numpy().view(w.dtype).reshape(w.dims[2], w.dims[1], w.dims[0])
-    del vol, raw
-    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    raw_host = O.generate_volume(w.dims, w.dtype, w.blobs(), w.noise_amp, w.noise_octaves,
+                                 w.noise_cell, w.seed, int(w.int_noise), w.vmax, threads)
+    gen_s = time.perf_counter() - t0
+    vol_hash = O.volume_hash(raw_host, threads)
     prep = O.Prepared(raw_host, w.brick_size, w.overlap, w.tf(), srm=w.srm,
                       lighting=w.lighting, light_model=w.light_model, threads=threads)
     poses = w.poses()
@@ -277,14 +336,14 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * total_t / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded blobs + value noise, generated on the GPU, copied to host)",
-        "config": {"workload": w.name, "dims": list(w.dims), "brick": list(w.brick_size),
-                   "width": w.width, "height": w.height, "srm": w.srm,
-                   "lighting": "blinn-phong" if w.light_model else "reference"},
+        "data": "synthetic (seeded blobs + value noise, generated on the host by the "
+                "generator's restatement: the GPU arm's bytes)",
+        "config": workload_config(w, ws, args.frame_ert, vol_hash),
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
                          "sample": f"every {stride}-th row ({rows} of {w.height}) per frame, "
                                    f"{args.steps} poses; {total_n / total_t / 1e6:.2f} "
-                                   f"Msamples/s"},
+                                   f"Msamples/s (reference loop steps); volume generated "
+                                   f"in {gen_s:.1f} s"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -621,6 +680,88 @@ def run_only(args):
     print(json.dumps({"only": args.only, args.only: out}), flush=True)
 
 
+def time_frames(torch, r, poses, first, K):
+    """K frames at poses[first:], back to back on the renderer's stream, timed
+    with CUDA events on that stream: (total ms, per-step ms)."""
+    ext = torch.cuda.ExternalStream(r.GetStream())
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(ext)
+    for i in range(K):
+        eye, at, up = poses[(first + i) % len(poses)]
+        ev[i][0].record(ext)
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        r.Paint()
+        ev[i][1].record(ext)
+    stop.record(ext)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop), [a.elapsed_time(b) for a, b in ev]
+
+
+def frame_stats(r, poses, first, K):
+    """Per-frame sample statistics of the timed poses (re-rendered, untimed)."""
+    samples, shaded, graded = [], [], []
+    for i in range(K):
+        eye, at, up = poses[(first + i) % len(poses)]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        r.Paint()
+        st = r.GetStats()
+        samples.append(st.samples)
+        shaded.append(st.shaded_samples)
+        graded.append(st.gradient_samples)
+    return float(np.mean(samples)), float(np.mean(shaded)), float(np.mean(graded))
+
+
+def frame0(r, poses):
+    eye, at, up = poses[0]
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+    r.Paint()
+    return r.ReadBackPixels().copy(), r.ReadSampleCounts().copy()
+
+
+def run_plain_small(args, torch, want_host):
+    """The small plain configuration (256^3 u8, 64^3 + 1 bricks, 512x512, srm
+    1.0, unlit): GPU frame rate over the seeded orbit, executed-sample rate and
+    roofline; the host copy of the volume and the GPU frame of pose 0 go to the
+    CPU leg."""
+    from tuvok_gb300 import Renderer
+    from tuvok_gb300.workloads import WORKLOADS
+    w = WORKLOADS["plain_small"]
+    vol, raw, brick_s = make_volume(w, torch)
+    raw_host = (raw.cpu().numpy().view(w.dtype).reshape(w.dims[2], w.dims[1], w.dims[0])
+                if want_host else None)
+    del raw
+    r = Renderer()
+    configure(r, w, vol, args.frame_ert)
+    poses = w.poses()
+    for i in range(args.warmup):
+        eye, at, up = poses[i]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        r.Paint()
+    K = max(args.steps, 20)
+    ms, step_ms = time_frames(torch, r, poses, args.warmup, K)
+    samples, shaded, graded = frame_stats(r, poses, args.warmup, K)
+    kernel_s = float(np.mean(step_ms)) / 1000.0
+    unlit_bytes = 8 * 1 + 16  # one trilinear lookup of 8 u8 texels + FP32 TF entry
+    peak, peak_kind = measured_peaks()
+    achieved = shaded * unlit_bytes / kernel_s / 1e9
+    out = {"workload": w.name, "dims": list(w.dims), "voxel": "u8", "brick": list(w.brick_size),
+           "width": w.width, "height": w.height, "srm": w.srm, "lighting": "none",
+           "frames": K, "frames_per_s": K / (ms / 1000.0), "ms_per_frame": ms / K,
+           "msamples_per_s": shaded / kernel_s / 1e6,
+           "reference_steps_msamples_per_s": samples / kernel_s / 1e6,
+           "samples_per_frame": samples, "executed_samples_per_frame": shaded,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                        "bytes_per_executed_sample": unlit_bytes},
+           "gpu_bricking": {"seconds": brick_s, "raw_bytes": int(np.prod(w.dims)),
+                            "pool_bytes": int(vol.info.device_bytes)}}
+    f0 = frame0(r, poses) if want_host else None
+    return out, raw_host, f0
+
+
 def run_ours(args):
     import torch
     from tuvok_gb300 import Renderer
@@ -631,7 +772,8 @@ def run_ours(args):
     vol, raw, brick_s = make_volume(w, torch)
     raw_bytes = raw.numel()
     raw_host = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+    want_cpu = rank == 0 and ws == 1 and not args.no_cpu_baseline
+    if want_cpu:
         raw_host = raw.cpu().numpy().view(w.dtype).reshape(w.dims[2], w.dims[1], w.dims[0])
     del raw
     torch.cuda.empty_cache()
@@ -639,7 +781,6 @@ def run_ours(args):
     r = Renderer()
     configure(r, w, vol, args.frame_ert)
     poses = w.poses()
-    ext = torch.cuda.ExternalStream(r.GetStream())
 
     def frame(i):
         eye, at, up = poses[i % len(poses)]
@@ -650,46 +791,32 @@ def run_ours(args):
         frame(i)
     torch.cuda.synchronize()
     K = args.steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(K)]
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         barrier(ws)
-        torch.cuda.synchronize()
-        start.record(ext)
-        for i in range(K):
-            ev[i][0].record(ext)
-            frame(args.warmup + i)
-            ev[i][1].record(ext)
-        stop.record(ext)
-        torch.cuda.synchronize()
+        ms, step_ms = time_frames(torch, r, poses, args.warmup, K)
         barrier(ws)
-    ms = start.elapsed_time(stop)
     ms = max_over_ranks(ws, ms)
-    step_ms = [a.elapsed_time(b) for a, b in ev]
     value = ws * K / (ms / 1000.0)
+    clk = clocks.summary()
 
     # samples per frame of the timed poses (deterministic; re-rendered untimed)
-    samples, shaded, graded, kms, vis = [], [], [], [], []
-    for i in range(K):
-        frame(args.warmup + i)
-        st = r.GetStats()
-        samples.append(st.samples)
-        shaded.append(st.shaded_samples)
-        graded.append(st.gradient_samples)
-        kms.append(st.last_paint_ms)
-        vis.append(st.bricks_visible)
-    mean_samples = float(np.mean(samples))
+    mean_samples, mean_shaded, mean_graded = frame_stats(r, poses, args.warmup, K)
+    kms = r.GetStats().last_paint_ms
     kernel_ms = float(np.mean(step_ms))
+    kernel_s = kernel_ms / 1000.0
     peak, peak_kind = measured_peaks()
     # Algorithmic bytes of the samples the kernel executes (steps in empty
     # macro cells add exactly zero and fetch nothing): a lit sample with
     # non-zero opacity takes 7 trilinear lookups + its TF entry, any other
     # executed sample 1 lookup + its TF entry.
-    exec_bytes = (float(np.mean(graded)) * LIT_BYTES_PER_SAMPLE +
-                  (float(np.mean(shaded)) - float(np.mean(graded))) * (8 * 2 + 16))
-    achieved = exec_bytes / (kernel_ms / 1000.0) / 1e9
+    exec_bytes = (mean_graded * LIT_BYTES_PER_SAMPLE + (mean_shaded - mean_graded) * (8 * 2 + 16))
+    achieved = exec_bytes / kernel_s / 1e9
     traffic = read_profile_traffic(w.name)
+    # the same bytes against the L1/texture path they are served from: 152 SMs
+    # x 128 B per clock at the SM clock sampled in the timed region (nominal)
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    l1_peak = 152 * 128 * sm_mhz * 1e6 / 1e9
+    f0 = frame0(r, poses) if want_cpu else None
 
     # end to end through the C ABI: view upload, paint, image to pinned host memory
     img = torch.empty((w.height, w.width, 4), dtype=torch.float32, pin_memory=True)
@@ -705,7 +832,7 @@ def run_ours(args):
     e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
     e2e = ws * K / e2e_s
     dev_brick_bytes = 112  # sizeof(tvk::DevBrick)
-    h2d = int(np.mean(vis)) * dev_brick_bytes
+    h2d = int(r.GetStats().bricks_visible) * dev_brick_bytes
     d2h = w.width * w.height * 16 + 32
 
     def guarded_leg(fn, *a):
@@ -721,6 +848,11 @@ def run_ours(args):
         learned = guarded_leg(run_learned, args, torch, r, w, poses, value)
 
     import gc
+    small = guarded_leg(run_plain_small, args, torch, want_cpu)
+    small_host = small_f0 = None
+    if isinstance(small, tuple):
+        small, small_host, small_f0 = small
+
     batching = None
     if not args.no_batching:
         r = None
@@ -736,14 +868,30 @@ def run_ours(args):
         ooc = guarded_leg(run_ooc, args, torch)
 
     cpu = None
+    parity = None
+    vol_hash = None
     if raw_host is not None:
         threads = os.cpu_count() or 1
-        c = cpu_baseline(w, raw_host, poses, args.cpu_seconds, mean_samples, threads)
+        c = cpu_leg(w, raw_host, poses, args.cpu_seconds, mean_samples, threads, f0)
+        vol_hash = c["volume_fnv1a"]
+        parity = c["parity"]
         cpu = {"value": c["fps"], "unit": "frames/s", "cores": threads, "kind": "port",
                "sample": f"oracle march on every {c['stride']}-th row ({c['rows']} of "
                          f"{w.height}) of pose 0, {c['march_s']:.1f} s, "
-                         f"{c['msamples_s']:.2f} Msamples/s; set-up (CPU bricking) "
-                         f"{c['setup_s']:.1f} s not timed"}
+                         f"{c['msamples_s']:.2f} Msamples/s (reference loop steps); set-up "
+                         f"{c['setup_s']:.1f} s not timed",
+               "bricking": c["bricking"]}
+        if small_host is not None and isinstance(small, dict):
+            sw = WORKLOADS["plain_small"]
+            cs = cpu_leg(sw, small_host, sw.poses(), min(args.cpu_seconds, 5.0),
+                         small["samples_per_frame"], threads, small_f0)
+            small["parity"] = cs["parity"]
+            small["volume_fnv1a"] = cs["volume_fnv1a"]
+            small["cpu_baseline"] = {"value": cs["fps"], "unit": "frames/s", "cores": threads,
+                                     "kind": "port",
+                                     "sample": f"oracle march on every {cs['stride']}-th row of "
+                                               f"pose 0, {cs['msamples_s']:.2f} Msamples/s",
+                                     "bricking": cs["bricking"]}
 
     if rank == 0:
         line = {
@@ -755,33 +903,39 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded blobs + value noise, generated on the GPU)",
-            "config": {"workload": w.name, "dims": list(w.dims), "voxel": "u16 (12-bit)",
-                       "brick": list(w.brick_size), "width": w.width, "height": w.height,
-                       "srm": w.srm, "lighting": "blinn-phong ka0.2 kd0.6 ks0.2 n32",
-                       "poses": len(poses), "frame_ert": args.frame_ert,
-                       "l2": f"inputs larger than L2 (brick pool {pool_bytes / 1e9:.2f} GB); "
-                             "each step a different pose",
-                       "parallelism": f"replicas x{ws}"},
+            "config": workload_config(w, ws, args.frame_ert, vol_hash),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "note": "algorithmic bytes of executed samples: lit opaque "
                                  f"{LIT_BYTES_PER_SAMPLE} B (7 trilinear u16 lookups + FP32 TF), "
-                                 "others 32 B; texels are L1-served (hit rate ~97%), so the "
-                                 "kernel is issue/latency bound, far below this roof"},
-            "msamples_per_s": mean_samples / (kernel_ms / 1000.0) / 1e6,
-            "executed_msamples_per_s": float(np.mean(shaded)) / (kernel_ms / 1000.0) / 1e6,
+                                 "others 32 B, over the kernel's mean event time; texels are "
+                                 "served by L1 (roofline_l1), DRAM carries the compulsory "
+                                 "bytes (hbm_compulsory)"},
+            "roofline_l1": {"achieved": achieved, "peak": l1_peak, "unit": "GB/s",
+                            "frac": achieved / l1_peak,
+                            "peak_kind": "nominal: 152 SMs x 128 B/clk x sampled SM clock"},
+            "hbm_compulsory": ({"achieved": traffic / kernel_s / 1e9, "peak": peak,
+                                "unit": "GB/s", "frac": traffic / kernel_s / 1e9 / peak,
+                                "bytes_per_frame": traffic,
+                                "source": "ncu dram__bytes of one launch (profiles/)"}
+                               if traffic else None),
+            "msamples_per_s": mean_shaded / kernel_s / 1e6,
+            "reference_steps_msamples_per_s": mean_samples / kernel_s / 1e6,
             "samples_per_frame": mean_samples,
-            "shaded_fraction": float(np.sum(shaded) / max(np.sum(samples), 1)),
-            "gradient_fraction": float(np.sum(graded) / max(np.sum(samples), 1)),
-            "kernel_ms_lib_events": float(np.mean(kms)),
+            "executed_samples_per_frame": mean_shaded,
+            "shaded_fraction": mean_shaded / max(mean_samples, 1.0),
+            "gradient_fraction": mean_graded / max(mean_samples, 1.0),
+            "kernel_ms_lib_events": float(kms),
             "bricking": {"seconds": brick_s, "raw_bytes": raw_bytes, "pool_bytes": pool_bytes,
                          "gb_per_s": (raw_bytes + pool_bytes) / brick_s / 1e9},
+            "parity": parity,
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": K,
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
+            "clocks": clk,
+            "plain_small": small,
             "learned": learned,
             "batching": batching,
             "out_of_core": ooc,

@@ -785,8 +785,11 @@ tvk_status tvk_brick_lod0_noalloc(const void* device_voxels, tvk_dtype dtype,
  * floats each: cx, cy, cz, sigma, peak, 0, 0; voxel units, centre at voxel
  * centres) plus value noise of `noise_octaves` octaves (cell size halving from
  * noise_cell, amplitude noise_amp) or, with int_noise != 0, uniform integer
- * noise in [-noise_amp, noise_amp]; rounded and clamped to [0, vmax].
- * Input creation for tests and benchmarks only. */
+ * noise in [-noise_amp, noise_amp]; rounded and clamped to [0, vmax].  The
+ * Gaussians are evaluated separably (per-axis factors computed in double on
+ * the host) and combined in a fixed order of float operations, so the bytes
+ * are a function of the arguments alone on any IEEE machine.  Input creation
+ * for tests and benchmarks only. */
 tvk_status tvk_generate_volume(void* device_out, tvk_dtype dtype, const uint64_t dims[3],
                                const float* host_blobs, uint32_t n_blobs, float noise_amp,
                                uint32_t noise_octaves, float noise_cell, uint64_t seed,

@@ -106,6 +106,15 @@ def lib():
         L.orc_leaper_render.argtypes = [C.POINTER(Scene), _u32p, C.c_uint64,
                                         C.POINTER(C.c_float), _u32p, _u64p, C.c_uint64, _u64p]
         L.orc_leaper_render.restype = C.c_uint64
+        L.orc_generate_volume.argtypes = [C.c_void_p, C.c_int, _u64p, C.POINTER(C.c_float),
+                                          C.c_uint32, C.c_float, C.c_uint32, C.c_float,
+                                          C.c_uint64, C.c_int, C.c_float, C.c_int]
+        L.orc_generate_volume.restype = C.c_int
+        L.orc_convert_timed.argtypes = [C.c_void_p, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int,
+                                        C.POINTER(C.c_double), _u64p]
+        L.orc_convert_timed.restype = C.c_int64
+        L.orc_volume_hash.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
+        L.orc_volume_hash.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -244,6 +253,42 @@ def pow01(x, y):
     return lib().orc_pow01(float(x), float(y))
 
 
+def generate_volume(dims, dtype, blobs, noise_amp, octaves, cell, seed, int_noise, vmax,
+                    threads=0):
+    """The seeded volume tvk_generate_volume makes, restated on the host:
+    numpy [z, y, x] of dtype (uint8 / uint16), the same bytes."""
+    out = np.zeros((dims[2], dims[1], dims[0]), dtype=dtype)
+    b = np.ascontiguousarray(np.asarray(blobs, dtype=np.float32).reshape(-1, 7))
+    rc = lib().orc_generate_volume(out.ctypes.data_as(C.c_void_p), 0 if dtype == np.uint8 else 1,
+                                   _u64(dims), b.ctypes.data_as(C.POINTER(C.c_float)),
+                                   b.shape[0], float(noise_amp), int(octaves), float(cell),
+                                   int(seed), int(int_noise), float(vmax), int(threads))
+    if rc != 0:
+        raise ValueError("bad generator arguments")
+    return out
+
+
+def convert_timed(raw, bsize, overlap, clamp=False):
+    """The serial CPU bricking of ExtendedOctreeConverter::Convert restated
+    (every LOD's bricks with ghost voxels, per-brick min/max, the 1D
+    histogram) on one thread: (seconds, bricks, brick-pool bytes)."""
+    raw = np.ascontiguousarray(raw)
+    dims = (raw.shape[2], raw.shape[1], raw.shape[0])
+    t = C.c_double()
+    pb = C.c_uint64()
+    n = lib().orc_convert_timed(raw.ctypes.data_as(C.c_void_p), _dt(raw), _u64(dims),
+                                _u32(bsize), overlap, int(clamp), C.byref(t), C.byref(pb))
+    if n < 0:
+        raise ValueError("conversion failed")
+    return t.value, int(n), int(pb.value)
+
+
+def volume_hash(arr, threads=0):
+    """FNV-1a of the FNV-1a digests of every 1 MiB chunk of the bytes (hex)."""
+    a = np.ascontiguousarray(arr)
+    return f"{lib().orc_volume_hash(a.ctypes.data_as(C.c_void_p), a.nbytes, threads):016x}"
+
+
 def round_half(x):
     return lib().orc_round_half(float(x))
 
@@ -347,7 +392,10 @@ class Prepared:
         self._h = lib().orc_prepare(C.byref(self._scene))
 
     def render(self, *, eye, width, height, at=(0, 0, 0), up=(0, 1, 0), row_stride=1,
-               row_phase=0, threads=0, use_double=False):
+               row_phase=0, threads=0, use_double=False, want_counts=False):
+        """(image [h, w, 4], samples, march seconds), plus the per-pixel
+        sample counts [h, w] with want_counts.  Only the rows py with
+        py % row_stride == row_phase are marched; the others stay zero."""
         cam = Scene()
         cam.eye[:] = eye
         cam.at[:] = at
@@ -359,10 +407,14 @@ class Prepared:
         cam.threads = threads
         cam.use_double = int(use_double)
         img = np.zeros((height, width, 4), dtype=np.float32)
+        counts = np.zeros((height, width), dtype=np.uint32) if want_counts else None
         t = C.c_double()
         n = lib().orc_render_prepared(self._h, C.byref(cam),
-                                      img.ctypes.data_as(C.POINTER(C.c_float)), None,
+                                      img.ctypes.data_as(C.POINTER(C.c_float)),
+                                      counts.ctypes.data_as(_u32p) if want_counts else None,
                                       C.byref(t))
+        if want_counts:
+            return img, int(n), t.value, counts
         return img, int(n), t.value
 
     def close(self):

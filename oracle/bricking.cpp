@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -683,4 +684,50 @@ extern "C" int64_t orc_build_octree(const void* raw, int dtype, const uint64_t d
   return build_octree<uint16_t>(as<uint16_t>(raw), dims, brick_size, overlap, clamp_to_edge != 0,
                                 median != 0, static_cast<uint16_t*>(pool), pool_voxels,
                                 brick_offsets, max_bricks);
+}
+
+// The CPU bricking baseline: the serial work of ExtendedOctreeConverter::Convert
+// (ExtendedOctreeConverter.cpp:128-280) restated -- every brick of every LOD
+// with its ghost voxels (the octree above), ComputeBrickStats per brick
+// (.inc:408-444) -- plus the 1D histogram of Histogram1DDataBlock
+// (Histogram1DDataBlock.cpp:120-161), on one thread, timed without file IO.
+// Returns the bricks built (negative on failure); *seconds = wall time.
+extern "C" int64_t orc_convert_timed(const void* raw, int dtype, const uint64_t dims[3],
+                                     const uint32_t brick_size[3], uint32_t overlap,
+                                     int clamp_to_edge, double* seconds,
+                                     uint64_t* pool_bytes_out) {
+  if (dtype != 0 && dtype != 1) return -1;
+  const size_t bytes = dtype == 0 ? 1 : 2;
+  uint64_t lod[3 * 64], cnt[3 * 64];
+  const int n_lods = orc_lod_table(dims, brick_size, overlap, lod, cnt, 64);
+  uint64_t n_bricks = 0, total = 0;
+  for (int l = 0; l < n_lods; ++l)
+    for (uint64_t z = 0; z < cnt[3 * l + 2]; ++z)
+      for (uint64_t y = 0; y < cnt[3 * l + 1]; ++y)
+        for (uint64_t x = 0; x < cnt[3 * l]; ++x) {
+          const uint64_t c[3] = {x, y, z};
+          uint64_t bs[3];
+          orc_brick_size(&lod[3 * l], &cnt[3 * l], brick_size, overlap, c, bs);
+          total += bs[0] * bs[1] * bs[2];
+          ++n_bricks;
+        }
+  std::vector<uint8_t> pool(total * bytes);
+  std::vector<uint64_t> off(n_bricks);
+  std::vector<uint64_t> hist(size_t(1) << (8 * bytes));
+  const auto t0 = std::chrono::steady_clock::now();
+  const int64_t n = orc_build_octree(raw, dtype, dims, brick_size, overlap, clamp_to_edge, 0,
+                                     pool.data(), total, off.data(), n_bricks);
+  if (n < 0) return n;
+  double acc = 0.0;
+  for (uint64_t b = 0; b < n_bricks; ++b) {
+    const uint64_t end = b + 1 < n_bricks ? off[b + 1] : total;
+    double mn, mx;
+    orc_brick_stats(pool.data() + off[b] * bytes, dtype, end - off[b], &mn, &mx);
+    acc += mn + mx;
+  }
+  orc_histogram1d(raw, dtype, dims, brick_size, overlap, hist.data());
+  const auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count() + (acc < 0 ? 1 : 0);
+  if (pool_bytes_out) *pool_bytes_out = total * bytes;
+  return n;
 }

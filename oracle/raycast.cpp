@@ -1496,8 +1496,17 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
              iso = s.render_mode == ORC_RM_ISO;
   std::vector<char> wanted(first[n_lods], 0);
   uint64_t total = 0;
-
-  for (uint32_t py = 0; py < s.height; ++py)
+  // rows are independent (each writes its own pixels); the request set is the
+  // union over all rows.  row_stride / row_phase restrict the pass to a sample
+  // of rows, the rest are left untouched.
+  const uint32_t stride = s.row_stride ? s.row_stride : 1;
+#ifdef _OPENMP
+  if (s.threads > 0) omp_set_num_threads(s.threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+  for (int64_t py_ = 0; py_ < int64_t(s.height); ++py_) {
+    const uint32_t py = uint32_t(py_);
+    if (py % stride != s.row_phase % stride) continue;
     for (uint32_t px = 0; px < s.width; ++px) {
       const size_t pix = size_t(py) * s.width + px;
       float* o4 = out + 4 * pix;
@@ -1558,6 +1567,7 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
           uint32_t info = r.first;
           uint64_t id = r.second;
           if (info == 0) {
+#pragma omp atomic write
             wanted[id] = 1;
             while (info == 0 && lod < max_lod) {
               ++lod;
@@ -1732,6 +1742,7 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
       if (spp) spp[pix] = samples;
       total += samples;
     }
+  }
   uint64_t nm = 0;
   for (uint64_t i = 0; i < first[n_lods]; ++i)
     if (wanted[i]) {

@@ -57,3 +57,40 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     args = bench.parse()
     # rank 1 returns before touching the GPU, the oracle or the network
     assert bench.run_reference(args) is None
+
+
+def test_reference_arm_line_loads_no_product_code(tmp_path):
+    """The reference arm on a small workload (in a child process): it prints
+    one line with the GPU arm's config keys and the volume digest, and maps
+    the oracle but not libtvk.so."""
+    import json
+    import subprocess
+    code = f"""
+import sys, json, dataclasses
+sys.path.insert(0, {str(ROOT)!r})
+import bench
+from tuvok_gb300 import workloads as W
+small = dataclasses.replace(W.WORKLOADS["plain_small"], name="plain_tiny", dims=(48, 40, 36),
+                            width=64, height=48, n_poses=4, brick_core=16)
+W.WORKLOADS["plain_tiny"] = small
+sys.argv = ["bench.py", "--impl", "reference", "--workload", "plain_tiny", "--steps", "2",
+            "--warmup", "1"]
+bench.run_reference(bench.parse())
+maps = open("/proc/self/maps").read()
+print("MAPS", int("libtvk" in maps), int("liboracle" in maps))
+"""
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300,
+                       cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = r.stdout.strip().splitlines()
+    line = json.loads([x for x in lines if x.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"]["workload"] == "plain_tiny"
+    assert len(line["config"]["volume_fnv1a"]) == 16
+    import bench  # noqa: F401  (same keys as the GPU arm's config builder)
+    from tuvok_gb300 import workloads as W
+    import dataclasses
+    small = dataclasses.replace(W.WORKLOADS["plain_small"], name="plain_tiny", dims=(48, 40, 36),
+                                width=64, height=48, n_poses=4, brick_core=16)
+    assert set(line["config"]) == set(bench.workload_config(small, 1, 1.0, "x"))
+    assert [x for x in lines if x.startswith("MAPS")][-1] == "MAPS 0 1"

@@ -26,14 +26,15 @@ ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = "-fPIC,-ffp-contract=off,-O3,-Wall"
-# per-file extra flags: the ray march keeps every multiply and add separate
-# unless the source writes fmaf, so it matches the oracle bit for bit
-EXTRA = {"raycast.cu": ["-fmad=false"]}
+# per-file extra flags: the ray march and the volume generator keep every
+# multiply and add separate unless the source writes fmaf, so they match their
+# host restatements bit for bit
+EXTRA = {"raycast.cu": ["-fmad=false"], "volgen.cu": ["-fmad=false"]}
 SOURCES = ["api.cpp", "bricking.cu", "cnn.cu", "eo.cpp", "lod.cu", "raycast.cu", "rebrick.cu",
            "tf1d.cpp", "volgen.cu"]
 HEADERS = [CSRC / "tvk_internal.h", ROOT / "include" / "tvk.h"]
 ORACLE_SOURCES = [ROOT / "oracle" / "bricking.cpp", ROOT / "oracle" / "raycast.cpp",
-                  ROOT / "oracle" / "rebrick.cpp"]
+                  ROOT / "oracle" / "rebrick.cpp", ROOT / "oracle" / "volgen.cpp"]
 ORACLE_HEADERS = [ROOT / "oracle" / "oracle.h"]
 
 

@@ -3441,12 +3441,8 @@ tvk_status tvk_generate_volume(void* device_out, tvk_dtype dtype, const uint64_t
     REQUIRE(n_blobs == 0 || host_blobs, "null blob table");
     REQUIRE(dtype == TVK_U8 || dtype == TVK_U16, "bad dtype");
     REQUIRE(noise_octaves == 0 || noise_cell > 0, "noise cell must be > 0");
-    tvk::DevBuf d_blobs;
-    d_blobs.ensure(size_t(7) * std::max<uint32_t>(1, n_blobs) * sizeof(float));
-    if (n_blobs)
-      TVK_CUDA(cudaMemcpy(d_blobs.p, host_blobs, size_t(7) * n_blobs * sizeof(float),
-                          cudaMemcpyHostToDevice));
-    tvk::launch_generate(device_out, dtype == TVK_U8 ? 1 : 2, dims, d_blobs.as<float>(), n_blobs,
+    REQUIRE(dims[0] >= 1 && dims[1] >= 1 && dims[2] >= 1, "volume dimensions must be >= 1");
+    tvk::launch_generate(device_out, dtype == TVK_U8 ? 1 : 2, dims, host_blobs, n_blobs,
                          noise_amp, noise_octaves, noise_cell, seed, int_noise, vmax, 0);
     TVK_CUDA(cudaDeviceSynchronize());
   });

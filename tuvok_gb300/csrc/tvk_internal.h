@@ -127,7 +127,8 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
                       const uint32_t B[3], uint32_t ov, bool clamp, bool median,
                       uint32_t* d_min, uint32_t* d_max, uint32_t* d_wave, cudaStream_t s,
                       uint64_t* launches);
-void launch_generate(void* out, int bytes, const uint64_t dims[3], const float* d_blobs,
+// seeded synthetic volume (volgen.cu); host_blobs: 7 floats per blob
+void launch_generate(void* out, int bytes, const uint64_t dims[3], const float* host_blobs,
                      uint32_t n_blobs, float noise_amp, uint32_t octaves, float cell,
                      uint64_t seed, int int_noise, float vmax, cudaStream_t s);
 
