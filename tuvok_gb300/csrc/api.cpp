@@ -267,35 +267,29 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     V->total_cells = 0;
     return;
   }
-  // scratch: bmin, bmax, bhist, hist, max_grad bits, raw min/max
+  // scratch: bmin, bmax, bhist, hist, max_grad bits, per-brick largest Q
   const uint64_t gbins = uint64_t(1) << (8 * V->bytes);
   const size_t sz_bmin = V->n_bricks * 4, sz_bh = V->n_bricks * 256 * 4, sz_h = gbins * 8;
-  const size_t total = 2 * sz_bmin + sz_bh + sz_h + 8 + 8 + 64;
+  const size_t sz_q = V->n_bricks * 8;
+  const size_t total = sz_h + 8 + 8 + sz_q + 2 * sz_bmin + sz_bh + 64;
   d_scratch.ensure(total);
   uint8_t* base = d_scratch.as<uint8_t>();
   BrickScratch sc;
   sc.hist = reinterpret_cast<unsigned long long*>(base);
   sc.max_grad_bits = reinterpret_cast<unsigned long long*>(base + sz_h);
-  sc.raw_minmax = reinterpret_cast<uint32_t*>(base + sz_h + 8);
-  sc.bmin = reinterpret_cast<uint32_t*>(base + sz_h + 16);
+  sc.raw_minmax = nullptr;
+  unsigned long long* d_qmax = reinterpret_cast<unsigned long long*>(base + sz_h + 16);
+  sc.bmin = reinterpret_cast<uint32_t*>(base + sz_h + 16 + sz_q);
   sc.bmax = sc.bmin + V->n_bricks;
   sc.bhist = sc.bmax + V->n_bricks;
-  TVK_CUDA(cudaMemsetAsync(sc.hist, 0, sz_h, s));
+  TVK_CUDA(cudaMemsetAsync(base, 0, sz_h + 16 + sz_q, s));
   TVK_CUDA(cudaMemsetAsync(sc.bmin, 0xff, sz_bmin, s));
   TVK_CUDA(cudaMemsetAsync(sc.bmax, 0, sz_bmin, s));
   TVK_CUDA(cudaMemsetAsync(sc.bhist, 0, sz_bh, s));
 
-  // pass 1: data range (Dataset::GetRange), needed for the per-brick bin shift
-  launch_raw_minmax(d_raw, V->bytes, nvox, sc.raw_minmax, s, &launches);
-  uint32_t mm[2];
-  TVK_CUDA(cudaMemcpyAsync(mm, sc.raw_minmax, sizeof(mm), cudaMemcpyDeviceToHost, s));
-  TVK_CUDA(cudaStreamSynchronize(s));
-  V->range_min = mm[0];
-  V->range_max = mm[1];
-  const uint32_t b = bits_of(mm[1]);
-  V->hist_shift = b > 8 ? b - 8 : 0;
-
-  // pass 2: bricks + statistics + histograms
+  // pass 1: the LOD-0 bricks, their min/max and the global histogram of the
+  // inner voxels -- every voxel once, so it also gives the data range
+  // (Dataset::GetRange) that sets the per-brick bin shift
   BrickGrid g;
   for (int a = 0; a < 3; ++a) {
     g.dims[a] = V->dims[a];
@@ -305,11 +299,47 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   g.ov = V->overlap;
   g.clamp = V->clamp ? 1 : 0;
   g.total = nvox;
-  launch_brick_lod0(d_raw, V->bytes, g, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
-                    V->n_bricks, V->d_pool, sc, V->hist_shift, uint32_t(mm[1]) + 1, s, &launches);
-  // pass 3: maximum gradient magnitude over inner voxels
-  launch_max_gradient(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
-                      V->n_bricks, V->overlap, max_bz, sc.max_grad_bits, s, &launches);
+  launch_brick_copy(d_raw, V->bytes, g, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                    V->n_bricks, V->d_pool, sc, uint32_t(gbins), s, &launches);
+  V->hist.resize(gbins);
+  TVK_CUDA(cudaMemcpyAsync(V->hist.data(), sc.hist, sz_h, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaStreamSynchronize(s));
+  {
+    uint64_t lo = 0, hi = gbins - 1;
+    while (lo < gbins && V->hist[lo] == 0) ++lo;
+    while (hi > 0 && V->hist[hi] == 0) --hi;
+    REQUIRE(lo < gbins, "empty volume");
+    V->range_min = double(lo);
+    V->range_max = double(hi);
+    const uint32_t b = bits_of(hi);
+    V->hist_shift = b > 8 ? b - 8 : 0;
+  }
+  // pass 2: per-brick 256-bin histograms and the largest squared central
+  // difference per brick; the maximum |gradient| is then evaluated in the
+  // reference's double arithmetic at the voxels of the largest one only
+  launch_brick_sweep(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                     V->n_bricks, V->overlap, max_bz, V->hist_shift, sc.bhist, d_qmax, s,
+                     &launches);
+  std::vector<unsigned long long> qmax(V->n_bricks);
+  TVK_CUDA(cudaMemcpyAsync(qmax.data(), d_qmax, sz_q, cudaMemcpyDeviceToHost, s));
+  TVK_CUDA(cudaStreamSynchronize(s));
+  {
+    unsigned long long qm = 0;
+    for (unsigned long long q : qmax) qm = std::max(qm, q);
+    if (qm > 0) {  // stored as Q + 1; 0 = no inner voxel with neighbours
+      std::vector<uint32_t> list;
+      for (uint64_t b = 0; b < V->n_bricks; ++b)
+        if (qmax[b] == qm) list.push_back(uint32_t(b));
+      DevBuf d_list;
+      d_list.ensure(list.size() * sizeof(uint32_t));
+      TVK_CUDA(cudaMemcpyAsync(d_list.p, list.data(), list.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, s));
+      launch_max_gradient_at(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                             d_list.as<uint32_t>(), uint32_t(list.size()), V->overlap, max_bz,
+                             (long long)(qm - 1), sc.max_grad_bits, s, &launches);
+      TVK_CUDA(cudaStreamSynchronize(s));  // d_list is released here
+    }
+  }
   // pass 4: the coarser LODs (ComputeHierarchy + FillOverlap) and their min/max
   DevBuf d_lmm, d_wave;
   std::vector<uint32_t> lmin, lmax;
@@ -336,7 +366,7 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   V->cell_offsets.resize(nb_all);
   V->cell_counts.resize(nb_all);
   V->cell_dims.resize(nb_all);
-  uint32_t max_cells = 0;
+  uint32_t max_cell_rows = 0;
   V->total_cells = 0;
   for (uint64_t k = 0; k < nb_all; ++k) {
     const uint32_t cx = cells_per_axis(V->sizes[3 * k]), cy = cells_per_axis(V->sizes[3 * k + 1]),
@@ -347,7 +377,7 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     V->cell_counts[k] = cx * cy * cz;
     V->cell_offsets[k] = V->total_cells;
     V->total_cells += V->cell_counts[k];
-    max_cells = std::max(max_cells, V->cell_counts[k]);
+    max_cell_rows = std::max(max_cell_rows, cy * cz);
   }
   TVK_CUDA(cudaMalloc(&V->d_cells, V->total_cells * sizeof(uint32_t)));
   TVK_CUDA(cudaMalloc(&V->d_cell_meta, nb_all * (sizeof(uint64_t) + sizeof(uint32_t))));
@@ -358,16 +388,14 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
   TVK_CUDA(cudaMemcpyAsync(d_cell_cnt, V->cell_counts.data(), nb_all * sizeof(uint32_t),
                            cudaMemcpyHostToDevice, s));
   launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
-                     d_cell_off, nb_all, max_cells, static_cast<uint32_t*>(V->d_cells), s,
+                     d_cell_off, nb_all, max_cell_rows, static_cast<uint32_t*>(V->d_cells), s,
                      &launches);
 
   std::vector<uint32_t> bmin(V->n_bricks), bmax(V->n_bricks);
-  V->hist.resize(gbins);
   V->bhist.resize(V->n_bricks * 256);
   unsigned long long mg = 0;
   TVK_CUDA(cudaMemcpyAsync(bmin.data(), sc.bmin, sz_bmin, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaMemcpyAsync(bmax.data(), sc.bmax, sz_bmin, cudaMemcpyDeviceToHost, s));
-  TVK_CUDA(cudaMemcpyAsync(V->hist.data(), sc.hist, sz_h, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaMemcpyAsync(V->bhist.data(), sc.bhist, sz_bh, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaMemcpyAsync(&mg, sc.max_grad_bits, 8, cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaStreamSynchronize(s));
@@ -2346,12 +2374,13 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                           cudaMemcpyHostToDevice));
       TVK_CUDA(cudaMemcpy(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
                           cudaMemcpyHostToDevice));
-      uint32_t max_cells = 0;
-      for (uint32_t c : V->cell_counts) max_cells = std::max(max_cells, c);
+      uint32_t max_rows = 0;
+      for (uint32_t d : V->cell_dims)
+        max_rows = std::max(max_rows, ((d >> 10) & 1023u) * (d >> 20));
       uint64_t launches = 0;
       tvk::launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                               static_cast<const uint64_t*>(V->d_cell_meta), V->total_bricks,
-                              max_cells, static_cast<uint32_t*>(V->d_cells), nullptr, &launches);
+                              max_rows, static_cast<uint32_t*>(V->d_cells), nullptr, &launches);
       TVK_CUDA(cudaDeviceSynchronize());
       *out = best.release();
       return;

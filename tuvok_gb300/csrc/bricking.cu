@@ -33,25 +33,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr uint32_t kSmemGlobalBins = 11776;  // keeps the CTA under 48 KB of smem
 
-template <class T>
-__global__ void raw_minmax_kernel(const T* __restrict__ raw, uint64_t n, uint32_t* minmax) {
-  uint32_t lo = 0xffffffffu, hi = 0;
-  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const uint32_t v = raw[i];
-    lo = min(lo, v);
-    hi = max(hi, v);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(&minmax[0], lo);
-    atomicMax(&minmax[1], hi);
-  }
-}
-
 // Source voxel of brick-local position (i, j, k) of brick (cx, cy, cz).
 template <class T>
 __device__ __forceinline__ T source_voxel(const T* __restrict__ raw, const BrickGrid& g,
@@ -76,61 +57,243 @@ __device__ __forceinline__ T source_voxel(const T* __restrict__ raw, const Brick
   return L < g.total ? raw[L] : T(0);
 }
 
+// One histogram increment per lane with `in` set, merged into a single
+// atomic when every such lane of the warp holds the same key (uniform regions,
+// e.g. the zero background, would otherwise serialise on one bin).  All 32
+// lanes must call it.  Keys below n_shared go to the CTA's shared bins, others
+// to the global 64-bit bins.
+__device__ __forceinline__ void hist_add_warp(uint32_t* __restrict__ sh,
+                                              unsigned long long* __restrict__ gl,
+                                              uint32_t n_shared, bool in, uint32_t key,
+                                              uint32_t lane) {
+  const unsigned m = __ballot_sync(0xffffffffu, in);
+  if (m == 0u) return;
+  const int leader = __ffs(m) - 1;
+  const uint32_t k0 = __shfl_sync(0xffffffffu, key, leader);
+  if (__all_sync(0xffffffffu, !in || key == k0)) {
+    if (int(lane) == leader) {
+      if (k0 < n_shared) atomicAdd(&sh[k0], uint32_t(__popc(m)));
+      else atomicAdd(&gl[k0], (unsigned long long)__popc(m));
+    }
+  } else if (in) {
+    if (key < n_shared) atomicAdd(&sh[key], 1u);
+    else atomicAdd(&gl[key], 1ull);
+  }
+}
+
+// Source line of brick-local row (j, k): GetInputBrick's y and z terms
+// (ExtendedOctreeConverter.cpp:288-373, clamping :376-462), or a zero row.
+__device__ __forceinline__ bool source_row(const BrickGrid& g, const uint32_t c[3],
+                                           const uint32_t bs[3], uint32_t j, uint32_t k,
+                                           uint64_t& rowbase) {
+  const uint32_t loc[2] = {j, k};
+  uint64_t gc[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int a = q + 1;
+    uint32_t l = loc[q];
+    const bool first = c[a] == 0, last = c[a] == g.cnt[a] - 1;
+    if (g.clamp) {
+      if (first && l < g.ov) l = g.ov;
+      if (last && l > bs[a] - 1 - g.ov) l = bs[a] - 1 - g.ov;
+    }
+    const uint32_t s = first ? g.ov : 0;
+    const uint32_t e = bs[a] - (last ? g.ov : 0);
+    if (l < s || l >= e) return false;
+    gc[q] = uint64_t(c[a]) * (g.B[a] - 2u * g.ov) + l - g.ov;
+  }
+  rowbase = gc[0] * g.dims[0] + gc[1] * g.dims[0] * g.dims[1];
+  return true;
+}
+
+// LOD-0 bricking as a tile copy: one warp per brick row (x-scanline of the
+// brick), the row's source line found once, lanes copying consecutive voxels
+// (coalesced reads of the raw volume and writes of the pool).  On the way:
+// per-brick min/max over every voxel written (ComputeBrickStats, ghost
+// included) and the global histogram of inner voxels (Histogram1DDataBlock),
+// which counts every voxel of the volume exactly once, so its first and last
+// non-zero bins are the data range.  The per-brick 256-bin histograms need that
+// range (their bin shift) and are taken by brick_sweep_kernel.  Persistent:
+// each CTA takes (brick, z-chunk) items in turn and merges its shared
+// histogram into the global one once, at the end.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
-brick_lod0_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __restrict__ offsets,
+brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __restrict__ offsets,
                   const uint32_t* __restrict__ sizes, T* __restrict__ pool, BrickScratch sc,
-                  uint32_t shift, uint32_t smem_bins, uint32_t z_chunk) {
-  extern __shared__ uint32_t smem[];
-  uint32_t* bh = smem;            // 256 per-brick bins
-  uint32_t* gh = smem + 256;      // global bins (smem_bins of them, may be 0)
-  const uint32_t b = blockIdx.x;
-  for (uint32_t i = threadIdx.x; i < 256 + smem_bins; i += blockDim.x) smem[i] = 0;
+                  uint32_t smem_bins, uint32_t z_chunk, uint32_t chunks_per_brick,
+                  uint32_t n_items) {
+  extern __shared__ uint32_t gh[];  // global bins [0, smem_bins)
+  for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x) gh[i] = 0;
   __syncthreads();
-
-  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
-  const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
-  const uint32_t z0 = blockIdx.y * z_chunk;
-  const uint32_t z1 = min(bs[2], z0 + z_chunk);
-  T* out = pool + offsets[b];
-  const uint32_t sxy = bs[0] * bs[1];
-  uint32_t lo = 0xffffffffu, hi = 0;
-  if (z0 < z1) {
-    const uint32_t n = (z1 - z0) * sxy;
-    for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
-      const uint32_t k = z0 + t / sxy;
-      const uint32_t r = t - (k - z0) * sxy;
-      const uint32_t j = r / bs[0];
-      const uint32_t i = r - j * bs[0];
-      const T v = source_voxel<T>(raw, g, c, bs, i, j, k);
-      out[uint64_t(k) * sxy + r] = v;
-      const uint32_t u = v;
-      lo = min(lo, u);
-      hi = max(hi, u);
-      const bool inner = i >= g.ov && i < bs[0] - g.ov && j >= g.ov && j < bs[1] - g.ov &&
-                         k >= g.ov && k < bs[2] - g.ov;
-      if (inner) {
-        atomicAdd(&bh[min(u >> shift, 255u)], 1u);
-        if (u < smem_bins)
-          atomicAdd(&gh[u], 1u);
-        else
-          atomicAdd(&sc.hist[u], 1ull);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const uint32_t b = item / chunks_per_brick;
+    const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+    const uint32_t c[3] = {b % g.cnt[0], (b / g.cnt[0]) % g.cnt[1], b / (g.cnt[0] * g.cnt[1])};
+    const uint32_t z0 = (item - b * chunks_per_brick) * z_chunk;
+    const uint32_t z1 = min(bs[2], z0 + z_chunk);
+    const uint32_t ov = g.ov;
+    const bool fx = c[0] == 0, lx = c[0] == g.cnt[0] - 1;
+    const uint32_t sx = fx ? ov : 0, ex = bs[0] - (lx ? ov : 0);
+    const uint64_t xbase = uint64_t(c[0]) * (g.B[0] - 2u * ov);
+    T* const brick = pool + offsets[b];
+    uint32_t lo = 0xffffffffu, hi = 0;
+    const uint32_t rows = z1 > z0 ? (z1 - z0) * bs[1] : 0;
+    for (uint32_t r = warp; r < rows; r += nwarps) {
+      const uint32_t k = z0 + r / bs[1];
+      const uint32_t j = r - (k - z0) * bs[1];
+      uint64_t rowbase = 0;
+      const bool live = source_row(g, c, bs, j, k, rowbase);
+      const bool inner_row = j >= ov && j < bs[1] - ov && k >= ov && k < bs[2] - ov;
+      T* const out = brick + (uint64_t(k) * bs[1] + j) * bs[0];
+      for (uint32_t base = 0; base < bs[0]; base += 32) {
+        const uint32_t i = base + lane;
+        const bool act = i < bs[0];
+        T v = T(0);
+        if (act && live) {
+          uint32_t l = i;
+          if (g.clamp) {
+            if (fx && l < ov) l = ov;
+            if (lx && l > bs[0] - 1 - ov) l = bs[0] - 1 - ov;
+          }
+          if (l >= sx && l < ex) {
+            const uint64_t L = (xbase + l - ov) + rowbase;
+            if (L < g.total) v = __ldg(raw + L);
+          }
+        }
+        if (act) {
+          out[i] = v;
+          lo = min(lo, uint32_t(v));
+          hi = max(hi, uint32_t(v));
+        }
+        hist_add_warp(gh, sc.hist, smem_bins, act && inner_row && i >= ov && i < bs[0] - ov,
+                      uint32_t(v), lane);
       }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0 && lo <= hi) {
+      atomicMin(&sc.bmin[b], lo);
+      atomicMax(&sc.bmax[b], hi);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x)
+    if (gh[i]) atomicAdd(&sc.hist[i], (unsigned long long)gh[i]);
+}
+
+// Second pass over the LOD-0 bricks in the pool: each brick's 256-bin
+// histogram of inner voxels (bin = value >> shift) and the largest squared
+// central-difference sum Q = dx^2 + dy^2 + dz^2 over inner voxels
+// (Histogram2DDataBlock::ComputeGradient, Histogram2DDataBlock.cpp:327-345, in
+// integers).  One warp per inner row of a brick z-chunk.
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+brick_sweep_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                   const uint32_t* __restrict__ sizes, uint32_t ov, uint32_t shift,
+                   uint32_t z_chunk, uint32_t* __restrict__ bhist,
+                   unsigned long long* __restrict__ brick_qmax) {
+  __shared__ uint32_t bh[256];
+  __shared__ unsigned long long qs[kThreads / 32];
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) bh[i] = 0;
+  __syncthreads();
+  const uint32_t b = blockIdx.x;
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const T* const p = pool + offsets[b];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t iy = bs[1] > 2 * ov ? bs[1] - 2 * ov : 0;
+  const uint32_t z0 = ov + blockIdx.y * z_chunk;
+  const uint32_t z1 = bs[2] > ov ? min(bs[2] - ov, z0 + z_chunk) : 0;
+  const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
+  const bool grad = ov > 0;  // central differences need a ghost layer on every side
+  long long qmax = -1;
+  const uint32_t rows = z1 > z0 ? (z1 - z0) * iy : 0;
+  for (uint32_t r = warp; r < rows; r += nwarps) {
+    const uint32_t k = z0 + r / iy;
+    const uint32_t j = ov + (r - (k - z0) * iy);
+    const T* const line = p + uint64_t(k) * sxy + uint64_t(j) * sx;
+    for (uint32_t base = ov; base < bs[0] - ov; base += 32) {
+      const uint32_t i = base + lane;
+      const bool act = i < bs[0] - ov;
+      uint32_t v = 0;
+      if (act) {
+        const T* const c = line + i;
+        v = c[0];
+        if (grad) {
+          const int dx = int(c[-1]) - int(c[1]);
+          const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
+          const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
+          const long long q =
+              (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
+          qmax = q > qmax ? q : qmax;
+        }
+      }
+      hist_add_warp(bh, nullptr, 256u, act, min(v >> shift, 255u), lane);
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    const long long other = __shfl_xor_sync(0xffffffffu, qmax, o);
+    qmax = other > qmax ? other : qmax;
   }
-  if ((threadIdx.x & 31) == 0 && lo <= hi) {
-    atomicMin(&sc.bmin[b], lo);
-    atomicMax(&sc.bmax[b], hi);
-  }
+  if (lane == 0) qs[warp] = qmax < 0 ? 0ull : (unsigned long long)qmax + 1ull;
   __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = 0;
+    for (uint32_t w = 0; w < nwarps; ++w) m = qs[w] > m ? qs[w] : m;
+    if (m) atomicMax(&brick_qmax[b], m);  // Q + 1; 0 = no inner voxel
+  }
   for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x)
-    if (bh[i]) atomicAdd(&sc.bhist[256u * b + i], bh[i]);
-  for (uint32_t i = threadIdx.x; i < smem_bins; i += blockDim.x)
-    if (gh[i]) atomicAdd(&sc.hist[i], (unsigned long long)gh[i]);
+    if (bh[i]) atomicAdd(&bhist[256u * b + i], bh[i]);
+}
+
+// The reference's double |gradient| (Histogram2DDataBlock.cpp:327-345)
+// evaluated at the voxels whose integer Q equals the volume's largest Q, in
+// the bricks listed: distinct Q values give |gradient| values whose gap far
+// exceeds double rounding, so the maximum |gradient| is the largest of these.
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+max_gradient_at_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
+                       const uint32_t* __restrict__ sizes, const uint32_t* __restrict__ bricks,
+                       uint32_t ov, long long q_target, uint32_t z_chunk,
+                       unsigned long long* out_bits) {
+  const uint32_t b = bricks[blockIdx.x];
+  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
+  const T* const p = pool + offsets[b];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t iy = bs[1] - 2 * ov;
+  const uint32_t z0 = ov + blockIdx.y * z_chunk;
+  const uint32_t z1 = min(bs[2] - ov, z0 + z_chunk);
+  const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
+  const double nf2 = double(T(~T(0))) * 2.0;
+  unsigned long long best = 0;
+  const uint32_t rows = z1 > z0 ? (z1 - z0) * iy : 0;
+  for (uint32_t r = warp; r < rows; r += nwarps) {
+    const uint32_t k = z0 + r / iy;
+    const uint32_t j = ov + (r - (k - z0) * iy);
+    const T* const line = p + uint64_t(k) * sxy + uint64_t(j) * sx;
+    for (uint32_t i = ov + lane; i < bs[0] - ov; i += 32) {
+      const T* const c = line + i;
+      const int dx = int(c[-1]) - int(c[1]);
+      const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
+      const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
+      const long long q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
+      if (q != q_target) continue;
+      const double gx = __ddiv_rn(double(dx), nf2);
+      const double gy = __ddiv_rn(double(dy), nf2);
+      const double gz = __ddiv_rn(double(dz), nf2);
+      const double f = __dsqrt_rn(
+          __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz)));
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(f);
+      best = bits > best ? bits : best;  // positive doubles order like their bits
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    best = ob > best ? ob : best;
+  }
+  if (lane == 0 && best) atomicMax(out_bits, best);
 }
 
 // Colour (RGBA8) volumes: the LOD-0 bricks with their ghost voxels (zero or
@@ -155,63 +318,6 @@ brick_copy4_kernel(const uint32_t* __restrict__ raw, BrickGrid g,
     const uint32_t i = r - j * bs[0];
     out[uint64_t(k) * sxy + r] = source_voxel<uint32_t>(raw, g, c, bs, i, j, k);
   }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads)
-max_gradient_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
-                    const uint32_t* __restrict__ sizes, uint32_t ov, uint32_t z_chunk,
-                    unsigned long long* out_bits) {
-  // Every inner voxel: Q = dx^2 + dy^2 + dz^2 of the central differences.  Distinct
-  // integer Q values give |grad| values whose relative gap (>= 1/(2Q)) far exceeds
-  // double rounding, so the maximum |grad| sits at a voxel of maximum Q.  Each
-  // thread keeps its largest Q and evaluates the reference's double expression
-  // only when a voxel reaches it with another (|dx|, |dy|, |dz|); the largest
-  // of the threads' values is the maximum.  A warp walks x-rows (coalesced).
-  const uint32_t b = blockIdx.x;
-  const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
-  const T* p = pool + offsets[b];
-  const uint32_t ix = bs[0] - 2 * ov, iy = bs[1] - 2 * ov;
-  const uint32_t z0 = ov + blockIdx.y * z_chunk;
-  const uint32_t z1 = min(bs[2] - ov, z0 + z_chunk);
-  const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
-  const double nf2 = double(T(~T(0))) * 2.0;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  long long best_q = -1;
-  double best_f = 0.0;
-  int ba = -1, bb = -1, bc = -1;  // |dx|, |dy|, |dz| of the best value
-  const uint32_t rows = (z1 > z0) ? (z1 - z0) * iy : 0;
-  for (uint32_t row = warp; row < rows; row += kThreads / 32) {
-    const uint32_t k = z0 + row / iy, j = ov + row % iy;
-    const T* line = p + uint64_t(j) * sx + uint64_t(k) * sxy;
-    for (uint32_t i = ov + lane; i < ov + ix; i += 32) {
-      const T* c = line + i;
-      const int dx = int(c[-1]) - int(c[1]);
-      const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
-      const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
-      const long long q = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
-      if (q < best_q) continue;
-      const int ax = abs(dx), ay = abs(dy), az = abs(dz);
-      if (q == best_q && ax == ba && ay == bb && az == bc) continue;
-      const double gx = __ddiv_rn(double(dx), nf2);
-      const double gy = __ddiv_rn(double(dy), nf2);
-      const double gz = __ddiv_rn(double(dz), nf2);
-      const double sq = __dadd_rn(__dadd_rn(__dmul_rn(gx, gx), __dmul_rn(gy, gy)), __dmul_rn(gz, gz));
-      const double f = __dsqrt_rn(sq);
-      if (q > best_q || f > best_f) {
-        best_q = q;
-        best_f = f;
-        ba = ax; bb = ay; bc = az;
-      }
-    }
-  }
-  // positive doubles order like their bit patterns
-  unsigned long long bits = best_q >= 0 ? (unsigned long long)__double_as_longlong(best_f) : 0ull;
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
-    bits = ob > bits ? ob : bits;
-  }
-  if (lane == 0 && bits) atomicMax(out_bits, bits);
 }
 
 template <class T>
@@ -285,39 +391,7 @@ uint32_t blocks_for(uint64_t n) {
 
 }  // namespace
 
-void launch_raw_minmax(const void* raw, int bytes, uint64_t n, uint32_t* minmax, cudaStream_t s,
-                       uint64_t* launches) {
-  const uint32_t init[2] = {0xffffffffu, 0u};
-  TVK_CUDA(cudaMemcpyAsync(minmax, init, sizeof(init), cudaMemcpyHostToDevice, s));
-  if (bytes == 1)
-    raw_minmax_kernel<uint8_t><<<blocks_for(n), kThreads, 0, s>>>(
-        static_cast<const uint8_t*>(raw), n, minmax);
-  else
-    raw_minmax_kernel<uint16_t><<<blocks_for(n), kThreads, 0, s>>>(
-        static_cast<const uint16_t*>(raw), n, minmax);
-  TVK_CUDA(cudaGetLastError());
-  ++*launches;
-}
 
-void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g, const uint64_t* d_offsets,
-                       const uint32_t* d_sizes, uint64_t n_bricks, void* pool,
-                       const BrickScratch& sc, uint32_t hist_shift, uint32_t global_bins,
-                       cudaStream_t s, uint64_t* launches) {
-  const uint32_t z_chunk = 8;
-  const dim3 grid(uint32_t(n_bricks), (g.B[2] + z_chunk - 1) / z_chunk);
-  const uint32_t smem_bins = global_bins <= kSmemGlobalBins ? global_bins : 0;
-  const size_t smem = (256 + smem_bins) * sizeof(uint32_t);
-  if (bytes == 1)
-    brick_lod0_kernel<uint8_t><<<grid, kThreads, smem, s>>>(
-        static_cast<const uint8_t*>(raw), g, d_offsets, d_sizes, static_cast<uint8_t*>(pool), sc,
-        hist_shift, smem_bins, z_chunk);
-  else
-    brick_lod0_kernel<uint16_t><<<grid, kThreads, smem, s>>>(
-        static_cast<const uint16_t*>(raw), g, d_offsets, d_sizes, static_cast<uint16_t*>(pool),
-        sc, hist_shift, smem_bins, z_chunk);
-  TVK_CUDA(cudaGetLastError());
-  ++*launches;
-}
 
 void launch_brick_copy4(const void* raw, const BrickGrid& g, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, uint64_t n_bricks, void* pool, cudaStream_t s,
@@ -330,24 +404,6 @@ void launch_brick_copy4(const void* raw, const BrickGrid& g, const uint64_t* d_o
   ++*launches;
 }
 
-void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
-                         const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
-                         uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
-                         uint64_t* launches) {
-  TVK_CUDA(cudaMemsetAsync(out_bits, 0, sizeof(unsigned long long), s));
-  // without overlap a brick holds no neighbours of its boundary voxels
-  if (ov == 0 || max_bz <= 2 * ov) return;
-  const uint32_t z_chunk = 4;
-  const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
-  if (bytes == 1)
-    max_gradient_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
-        static_cast<const uint8_t*>(pool), d_offsets, d_sizes, ov, z_chunk, out_bits);
-  else
-    max_gradient_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
-        static_cast<const uint16_t*>(pool), d_offsets, d_sizes, ov, z_chunk, out_bits);
-  TVK_CUDA(cudaGetLastError());
-  ++*launches;
-}
 
 void launch_histogram2d(const void* pool, int bytes, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, uint64_t n_bricks, uint32_t max_bz,
@@ -369,43 +425,75 @@ void launch_histogram2d(const void* pool, int bytes, const uint64_t* d_offsets,
 
 namespace {
 
+// Macro-cell min/max (cell c covers voxels c*kCell .. c*kCell + kCell on each
+// axis, clamped to the brick).  One warp per row of cells (cy, cz): per voxel
+// column the min/max over the (kCell + 1)^2 voxel rows the cells span
+// (coalesced row reads), then across kCell + 1 columns with a shuffle; each
+// lane owns kCell consecutive columns of a 32 * kCell-column chunk.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
                    const uint32_t* __restrict__ sizes, const uint64_t* __restrict__ cell_off,
                    uint32_t* __restrict__ cells) {
-  // one thread per macro cell of brick blockIdx.y: min/max over voxels
-  // c*kCell .. (c+1)*kCell on each axis, clamped to the brick
   const uint32_t b = blockIdx.y;
   const uint32_t n0 = sizes[3 * b], n1 = sizes[3 * b + 1], n2 = sizes[3 * b + 2];
   const uint32_t cx = cells_per_axis(n0), cy = cells_per_axis(n1), cz = cells_per_axis(n2);
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cx * cy * cz) return;
-  const uint32_t x = c % cx, y = (c / cx) % cy, z = c / (cx * cy);
-  const T* p = pool + offsets[b];
-  const uint32_t x0 = x << kCellShift, x1 = min(x0 + kCell, n0 - 1);
-  const uint32_t y0 = y << kCellShift, y1 = min(y0 + kCell, n1 - 1);
-  const uint32_t z0 = z << kCellShift, z1 = min(z0 + kCell, n2 - 1);
-  uint32_t lo = 0xffffu, hi = 0;
-  for (uint32_t k = z0; k <= z1; ++k)
-    for (uint32_t j = y0; j <= y1; ++j) {
-      const T* row = p + (uint64_t(k) * n1 + j) * n0;
-      for (uint32_t i = x0; i <= x1; ++i) {
-        const uint32_t v = row[i];
-        lo = min(lo, v);
-        hi = max(hi, v);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t row = blockIdx.x * (kThreads / 32) + warp;  // cell row index
+  if (row >= cy * cz) return;  // whole warp
+  const uint32_t ry = row % cy, rz = row / cy;
+  const T* const p = pool + offsets[b];
+  const uint32_t y0 = ry << kCellShift, y1 = min(y0 + kCell, n1 - 1);
+  const uint32_t z0 = rz << kCellShift, z1 = min(z0 + kCell, n2 - 1);
+  uint32_t* const out = cells + cell_off[b] + uint64_t(rz * cy + ry) * cx;
+  for (uint32_t xb = 0; xb < n0; xb += 32u * kCell) {
+    // columns xb + lane * kCell + [0, kCell) of this lane, and the next lane's
+    // first column (lane 31: the chunk's next column)
+    uint32_t lo[kCell], hi[kCell];
+    uint32_t elo = 0xffffffffu, ehi = 0u;
+#pragma unroll
+    for (int q = 0; q < kCell; ++q) { lo[q] = 0xffffffffu; hi[q] = 0u; }
+    const uint32_t x_first = xb + lane * kCell;
+    const uint32_t x_extra = xb + 32u * kCell;
+    for (uint32_t z = z0; z <= z1; ++z)
+      for (uint32_t y = y0; y <= y1; ++y) {
+        const T* const line = p + (uint64_t(z) * n1 + y) * n0;
+#pragma unroll
+        for (int q = 0; q < kCell; ++q) {
+          const uint32_t x = x_first + q;
+          if (x < n0) {
+            const uint32_t v = __ldg(line + x);
+            lo[q] = min(lo[q], v);
+            hi[q] = max(hi[q], v);
+          }
+        }
+        if (lane == 31 && x_extra < n0) {
+          const uint32_t v = __ldg(line + x_extra);
+          elo = min(elo, v);
+          ehi = max(ehi, v);
+        }
       }
+    uint32_t nlo = __shfl_down_sync(0xffffffffu, lo[0], 1);
+    uint32_t nhi = __shfl_down_sync(0xffffffffu, hi[0], 1);
+    if (lane == 31) { nlo = elo; nhi = ehi; }
+    const uint32_t c = x_first >> kCellShift;  // this lane's cell
+    if (x_first < n0 && c < cx) {
+      uint32_t a = nlo, h = nhi;
+#pragma unroll
+      for (int q = 0; q < kCell; ++q) { a = min(a, lo[q]); h = max(h, hi[q]); }
+      out[c] = a | (h << 16);
     }
-  cells[cell_off[b] + c] = lo | (hi << 16);
+  }
 }
 
 }  // namespace
 
 void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, const uint64_t* d_cell_offsets,
-                        uint64_t n_bricks, uint32_t max_cells_per_brick, uint32_t* cells,
+                        uint64_t n_bricks, uint32_t max_cell_rows, uint32_t* cells,
                         cudaStream_t s, uint64_t* launches) {
-  const dim3 grid((max_cells_per_brick + kThreads - 1) / kThreads, uint32_t(n_bricks));
+  const uint32_t per_cta = kThreads / 32;
+  const dim3 grid((max_cell_rows + per_cta - 1) / per_cta, uint32_t(n_bricks));
   if (bytes == 1)
     cell_minmax_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
         static_cast<const uint8_t*>(pool), d_offsets, d_sizes, d_cell_offsets, cells);
@@ -415,6 +503,69 @@ void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
   TVK_CUDA(cudaGetLastError());
   ++*launches;
 }
+
+void launch_brick_copy(const void* raw, int bytes, const BrickGrid& g, const uint64_t* d_offsets,
+                       const uint32_t* d_sizes, uint64_t n_bricks, void* pool,
+                       const BrickScratch& sc, uint32_t global_bins, cudaStream_t s,
+                       uint64_t* launches) {
+  const uint32_t z_chunk = 4;
+  const uint32_t chunks = (g.B[2] + z_chunk - 1) / z_chunk;
+  const uint64_t items = n_bricks * chunks;
+  if (items >= (1ull << 32)) fail(TVK_ERR_UNSUPPORTED, "too many bricks for one bricking pass");
+  const uint32_t smem_bins = global_bins <= kSmemGlobalBins ? global_bins : kSmemGlobalBins;
+  const size_t smem = size_t(smem_bins) * sizeof(uint32_t);
+  // 8 CTAs of 256 threads per SM when the shared bins allow it
+  const uint32_t grid = uint32_t(std::min<uint64_t>(items, 152ull * 8));
+  if (bytes == 1)
+    brick_copy_kernel<uint8_t><<<grid, kThreads, smem, s>>>(
+        static_cast<const uint8_t*>(raw), g, d_offsets, d_sizes, static_cast<uint8_t*>(pool), sc,
+        smem_bins, z_chunk, chunks, uint32_t(items));
+  else
+    brick_copy_kernel<uint16_t><<<grid, kThreads, smem, s>>>(
+        static_cast<const uint16_t*>(raw), g, d_offsets, d_sizes, static_cast<uint16_t*>(pool),
+        sc, smem_bins, z_chunk, chunks, uint32_t(items));
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_brick_sweep(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov, uint32_t max_bz,
+                        uint32_t shift, uint32_t* bhist, unsigned long long* brick_qmax,
+                        cudaStream_t s, uint64_t* launches) {
+  if (max_bz <= 2 * ov) return;  // no inner voxels
+  const uint32_t z_chunk = 4;
+  const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
+  if (bytes == 1)
+    brick_sweep_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(pool), d_offsets, d_sizes, ov, shift, z_chunk, bhist,
+        brick_qmax);
+  else
+    brick_sweep_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(pool), d_offsets, d_sizes, ov, shift, z_chunk, bhist,
+        brick_qmax);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
+void launch_max_gradient_at(const void* pool, int bytes, const uint64_t* d_offsets,
+                            const uint32_t* d_sizes, const uint32_t* d_bricks, uint32_t n_list,
+                            uint32_t ov, uint32_t max_bz, long long q_target,
+                            unsigned long long* out_bits, cudaStream_t s, uint64_t* launches) {
+  if (n_list == 0 || ov == 0 || max_bz <= 2 * ov) return;
+  const uint32_t z_chunk = 4;
+  const dim3 grid(n_list, (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
+  if (bytes == 1)
+    max_gradient_at_kernel<uint8_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint8_t*>(pool), d_offsets, d_sizes, d_bricks, ov, q_target, z_chunk,
+        out_bits);
+  else
+    max_gradient_at_kernel<uint16_t><<<grid, kThreads, 0, s>>>(
+        static_cast<const uint16_t*>(pool), d_offsets, d_sizes, d_bricks, ov, q_target, z_chunk,
+        out_bits);
+  TVK_CUDA(cudaGetLastError());
+  ++*launches;
+}
+
 
 // ---------------------------------------------------------------------------
 // Allocation-free LOD-0 bricking (tvk_brick_lod0_noalloc).

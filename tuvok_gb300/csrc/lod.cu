@@ -108,29 +108,41 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
   const uint32_t z0 = blockIdx.y * z_chunk, z1 = min(n[2], z0 + z_chunk);
   if (z0 >= z1) return;
   const uint32_t sxy = n[0] * n[1];
-  const uint32_t total = (z1 - z0) * sxy;
-  for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
-    const uint32_t k = z0 + t / sxy, r = t % sxy, j = r / n[0], i = r % n[0];
-    const uint32_t v[3] = {i, j, k};
-    T out{};
-    bool covered = true;
+  // Which child voxels an output voxel filters, axis by axis: outside the
+  // inner region (ghost) or beyond the last child nothing (0, FillOverlap
+  // writes the ghosts later); else the child, the position in it and whether
+  // the axis has a pair of samples or the odd boundary sample.
+  auto axis = [&](int a, uint32_t va, uint32_t& child, uint32_t& l, uint32_t& cs,
+                  int& pair) -> bool {
+    if (va < ov || va >= n[a] - ov) return false;
+    const uint32_t tt = va - ov;
+    const uint32_t split = (B[a] - 2 * ov + 1) / 2;  // ceil(core / 2)
+    const uint32_t cc = tt >= split ? 1u : 0u;
+    child = 2 * c[a] + cc;
+    if (child >= lo.cnt[a]) return false;
+    l = tt - cc * split;
+    cs = brick_extent(lo, B, ov, a, child);
+    const uint32_t even = (cs - 2 * ov) / 2;
+    if (l < even) pair = 1;
+    else if (l == even && (cs & 1u)) pair = 0;
+    else return false;
+    return true;
+  };
+  // one warp per output row (y, z terms once per row), lanes along x
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t rows = (z1 - z0) * n[1];
+  for (uint32_t rr = warp; rr < rows; rr += nwarps) {
+    const uint32_t k = z0 + rr / n[1];
+    const uint32_t j = rr - (k - z0) * n[1];
+    const uint32_t r0 = j * n[0];
     uint32_t child[3], l[3], cs[3];
     int pair[3];  // 1: two samples along the axis, 0: the odd boundary sample
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if (v[a] < ov || v[a] >= n[a] - ov) { covered = false; break; }
-      const uint32_t tt = v[a] - ov;
-      const uint32_t split = (B[a] - 2 * ov + 1) / 2;  // ceil(core / 2)
-      const uint32_t cc = tt >= split ? 1u : 0u;
-      child[a] = 2 * c[a] + cc;
-      if (child[a] >= lo.cnt[a]) { covered = false; break; }
-      l[a] = tt - cc * split;
-      cs[a] = brick_extent(lo, B, ov, a, child[a]);
-      const uint32_t even = (cs[a] - 2 * ov) / 2;
-      if (l[a] < even) pair[a] = 1;
-      else if (l[a] == even && (cs[a] & 1u)) pair[a] = 0;
-      else { covered = false; break; }
-    }
+    const bool row_covered = axis(1, j, child[1], l[1], cs[1], pair[1]) &&
+                             axis(2, k, child[2], l[2], cs[2], pair[2]);
+   for (uint32_t i = lane; i < n[0]; i += 32) {
+    const uint32_t r = r0 + i;
+    T out{};
+    const bool covered = row_covered && axis(0, i, child[0], l[0], cs[0], pair[0]);
     if (covered) {
       const T* src = pool + offsets[lo.first + child[0] + child[1] * lo.cnt[0] +
                                     child[2] * lo.cnt[0] * lo.cnt[1]];
@@ -183,6 +195,7 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
       }
     }
     dst[uint64_t(k) * sxy + r] = out;
+   }
   }
 }
 

@@ -53,20 +53,26 @@ struct BrickGrid {
   uint64_t total;       // voxels of the raw volume
 };
 
-void launch_raw_minmax(const void* raw, int bytes, uint64_t n, uint32_t* minmax,
-                       cudaStream_t s, uint64_t* launches);
 // RGBA8 colour volumes: LOD-0 bricks with ghost voxels only
 void launch_brick_copy4(const void* raw, const BrickGrid& g, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, uint64_t n_bricks, void* pool, cudaStream_t s,
                         uint64_t* launches);
-void launch_brick_lod0(const void* raw, int bytes, const BrickGrid& g,
-                       const uint64_t* d_offsets, const uint32_t* d_sizes, uint64_t n_bricks,
-                       void* pool, const BrickScratch& sc, uint32_t hist_shift,
-                       uint32_t global_bins, cudaStream_t s, uint64_t* launches);
-void launch_max_gradient(const void* pool, int bytes, const uint64_t* d_offsets,
-                         const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov,
-                         uint32_t max_bz, unsigned long long* out_bits, cudaStream_t s,
-                         uint64_t* launches);
+// LOD-0 bricks + per-brick min/max + global histogram (pass 1), then per-brick
+// histograms and largest squared central difference (pass 2), then the exact
+// maximum |gradient| at the voxels of the largest one (bricking.cu)
+void launch_brick_copy(const void* raw, int bytes, const BrickGrid& g, const uint64_t* d_offsets,
+                       const uint32_t* d_sizes, uint64_t n_bricks, void* pool,
+                       const BrickScratch& sc, uint32_t global_bins, cudaStream_t s,
+                       uint64_t* launches);
+void launch_brick_sweep(const void* pool, int bytes, const uint64_t* d_offsets,
+                        const uint32_t* d_sizes, uint64_t n_bricks, uint32_t ov, uint32_t max_bz,
+                        uint32_t shift, uint32_t* bhist, unsigned long long* brick_qmax,
+                        cudaStream_t s, uint64_t* launches);
+void launch_max_gradient_at(const void* pool, int bytes, const uint64_t* d_offsets,
+                            const uint32_t* d_sizes, const uint32_t* d_bricks, uint32_t n_list,
+                            uint32_t ov, uint32_t max_bz, long long q_target,
+                            unsigned long long* out_bits, cudaStream_t s, uint64_t* launches);
+
 // TransferFunction1D::Set byte semantics (tf1d.cpp)
 void tf1d_from_bytes(const uint8_t* bytes, uint64_t n, float* rgba);
 
@@ -163,9 +169,11 @@ struct alignas(16) DevBrick {
 };
 
 // Per-cell min/max of every LOD-0 brick (volume creation); packed min | max << 16.
+// macro-cell min/max of every listed brick; max_cell_rows = the largest
+// (cells along y) x (cells along z) of a brick
 void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, const uint64_t* d_cell_offsets,
-                        uint64_t n_bricks, uint32_t max_cells_per_brick, uint32_t* cells,
+                        uint64_t n_bricks, uint32_t max_cell_rows, uint32_t* cells,
                         cudaStream_t s, uint64_t* launches);
 
 // Empty-cell bits for the current transfer function (1 = every reachable TF
