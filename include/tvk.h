@@ -168,8 +168,9 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
  * `offset` of `path` (ExtendedOctree::Open, IO/UVF/ExtendedOctree/
  * ExtendedOctree.cpp:67-172; headers of UVF version >= 5).  Bricks are read at
  * their table-of-contents offsets in any on-disk layout (scanline, Morton,
- * Hilbert, random) and expanded from LZ4 where stored so (GetBrickData,
- * :313-361); zlib, LZMA and bzip2 bricks return TVK_ERR_UNSUPPORTED.
+ * Hilbert, random) and expanded where stored compressed (GetBrickData,
+ * :313-361): zlib, LZMA, LZ4 and bzip2 bricks are decoded (CT_LZHAM is
+ * refused, as by the reference).
  * 1-component uint8 / uint16 and 4-component uint8 (TVK_RGBA8) volumes with a
  * 1:1:1 aspect.  The volume is rebuilt on the GPU from the LOD-0 bricks' inner
  * voxels (statistics, histograms, coarser LODs).  The header records neither
@@ -180,6 +181,15 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
  * from the file with their min/max recomputed (the converter leaves stale
  * buffer data in some ghost corners of coarser bricks under clamp-to-edge with
  * an overlap of 2 or more). */
+/* ExtendedOctree::GetBrickData (ExtendedOctree.cpp:313-361) on the host, no
+ * GPU involved: brick `index` (table-of-contents order: LODs finest first,
+ * x fastest) of the ExtendedOctree at byte `offset` of `path`, expanded from
+ * its stored form (uncompressed, zlib, LZMA, LZ4 or bzip2) into `out`, voxels
+ * x fastest with the ghost layers.  *n_bytes receives the brick's size; with
+ * out == NULL only the size is returned, otherwise capacity must hold it.
+ * Corrupt or truncated bricks return TVK_ERR_INVALID_ARG. */
+tvk_status tvk_eo_read_brick(const char* path, uint64_t offset, uint32_t uvf_version,
+                             uint64_t index, void* out, size_t capacity, size_t* n_bytes);
 tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                                            uint32_t uvf_version, uint32_t flags,
                                            tvk_volume** out);

@@ -27,12 +27,24 @@ OUT = Path(__file__).resolve().parent / "eo"
 # input (GetInputBrick, ExtendedOctreeConverter.cpp:288-373) and, with
 # clamp-to-edge, keeps whatever the reused buffer held there.
 # name, dims (x, y, z), dtype, components, brick size, overlap, clamp, median,
-# compression (0 none, 3 LZ4), level, layout (0 scanline, 1 Morton, 2 Hilbert, 3 random)
+# compression (0 none, 1 zlib, 2 LZMA, 3 LZ4, 4 bzip2), level, layout (0 scanline,
+# 1 Morton, 2 Hilbert, 3 random)
 CASES = [
     ("u8_none_scanline", (21, 17, 13), "u8", 1, (8, 8, 8), 1, False, False, 0, 0, 0),
     ("u16_lz4_morton_clamp_median", (20, 23, 11), "u16", 1, (10, 9, 8), 2, True, True, 3, 1, 1),
     ("u8_lz4hc_hilbert", (30, 9, 17), "u8", 1, (12, 6, 12), 1, False, False, 3, 9, 2),
     ("rgba_none_random", (14, 12, 10), "u8", 4, (8, 8, 8), 1, True, False, 0, 0, 3),
+    # compression 1 zlib, 2 LZMA, 4 bzip2 (ExtendedOctree.cpp:337-350)
+    ("u8_zlib_scanline", (21, 17, 13), "u8", 1, (8, 8, 8), 1, False, False, 1, 6, 0),
+    ("u16_zlib9_morton", (26, 20, 15), "u16", 1, (10, 10, 10), 2, True, False, 1, 9, 1),
+    # LZMA at levels 8 and 9: the converter compresses with level - 1 and
+    # asserts that the properties equal those of the level itself, which holds
+    # only where both levels have the same dictionary size
+    ("u8_lzma_hilbert", (30, 9, 17), "u8", 1, (12, 6, 12), 1, False, False, 2, 9, 2),
+    ("u16_lzma8_scanline_median", (20, 23, 11), "u16", 1, (10, 9, 8), 2, False, True, 2, 8, 0),
+    ("u8_bzip2_scanline", (23, 21, 19), "u8", 1, (10, 10, 10), 1, False, False, 4, 9, 0),
+    ("u16_bzip2_random", (18, 20, 22), "u16", 1, (9, 9, 9), 1, False, False, 4, 1, 3),
+    ("rgba_lzma_morton", (14, 12, 10), "u8", 4, (8, 8, 8), 1, False, False, 2, 9, 1),
 ]
 
 

@@ -182,6 +182,8 @@ PROTOTYPES = {
     "tvk_set_scaling_method": [_vp, C.c_int],
     "tvk_volume_open_extended_octree": [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint32,
                                         C.POINTER(_vp)],
+    "tvk_eo_read_brick": [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint64, _vp, C.c_size_t,
+                          C.POINTER(C.c_size_t)],
     "tvk_set_clearview": [_vp, C.c_int],
     "tvk_set_cv_isovalue": [_vp, C.c_float],
     "tvk_set_cv_color": [_vp, _f32p],

@@ -2247,6 +2247,44 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
   });
 }
 
+tvk_status tvk_eo_read_brick(const char* path, uint64_t offset, uint32_t uvf_version,
+                             uint64_t index, void* out, size_t capacity, size_t* n_bytes) {
+  return guarded([&] {
+    REQUIRE(path && n_bytes, "null argument");
+    tvk::EoFile e;
+    tvk::eo_open(path, offset, uvf_version, e);
+    REQUIRE(index < e.toc.size(), "brick index beyond the table of contents");
+    const uint32_t bs[3] = {uint32_t(e.brick_size[0]), uint32_t(e.brick_size[1]),
+                            uint32_t(e.brick_size[2])};
+    const std::vector<tvk::LodInfo> lods = tvk::lod_table(e.dims, bs, e.overlap);
+    // the brick's LOD and coordinates from its TOC index
+    uint64_t k = index;
+    size_t l = 0;
+    while (l < lods.size()) {
+      const uint64_t nl = lods[l].bricks[0] * lods[l].bricks[1] * lods[l].bricks[2];
+      if (k < nl) break;
+      k -= nl;
+      ++l;
+    }
+    REQUIRE(l < lods.size(), "brick index beyond the LOD table");
+    const uint64_t c[3] = {k % lods[l].bricks[0], (k / lods[l].bricks[0]) % lods[l].bricks[1],
+                           k / (lods[l].bricks[0] * lods[l].bricks[1])};
+    uint32_t n[3];
+    tvk::brick_size(lods[l], bs, e.overlap, c, n);
+    const size_t vb = size_t(e.component_type == 1 ? 2 : (e.component_type == 0 ? 1 : 0)) *
+                      size_t(e.components);
+    if (vb == 0)
+      tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: component types other than uint8/uint16");
+    const size_t nb = size_t(n[0]) * n[1] * n[2] * vb;
+    *n_bytes = nb;
+    if (!out) return;
+    REQUIRE(capacity >= nb, "output smaller than the brick");
+    std::vector<uint8_t> brick;
+    tvk::eo_read_brick(e, index, nb, brick);
+    std::memcpy(out, brick.data(), nb);
+  });
+}
+
 tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                                            uint32_t uvf_version, uint32_t flags,
                                            tvk_volume** out) {

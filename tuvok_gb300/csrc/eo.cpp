@@ -2,11 +2,12 @@
 // UVF TOC block holds (IO/UVF/ExtendedOctree/ExtendedOctree.cpp:67-172 Open,
 // :313-361 GetBrickData).  Host code: the header and brick table of contents
 // are parsed, bricks are read at their TOC offsets and expanded when they are
-// LZ4 blocks; the ABI entry in api.cpp rebuilds the volume from the LOD-0
+// stored compressed (codecs.cpp; LZ4 here); the ABI entry in api.cpp rebuilds the volume from the LOD-0
 // bricks and checks every stored brick against the rebuild.
 
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "tvk_internal.h"
 
@@ -159,14 +160,30 @@ void eo_read_brick(const EoFile& e, uint64_t index, size_t bytes, std::vector<ui
       fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: file ends inside a brick");
     return;
   }
-  if (t.compression != 3)  // CT_LZ4
-    fail(TVK_ERR_UNSUPPORTED,
-         "ExtendedOctree: only uncompressed and LZ4 bricks are read (zlib, LZMA and bzip2 "
-         "decoders are not built)");
+  // COMPRESSION_TYPE (ExtendedOctree.h): CT_ZLIB 1, CT_LZMA 2, CT_LZ4 3, CT_BZLIB 4;
+  // CT_LZHAM (5) is refused by the reference as well
+  if (t.compression < 1 || t.compression > 4)
+    fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: unknown or unsupported brick compression " +
+                                  std::to_string(t.compression));
   std::vector<uint8_t> buf(size_t(t.length));
   if (std::fread(buf.data(), 1, buf.size(), fh.f) != buf.size())
     fail(TVK_ERR_INVALID_ARG, "ExtendedOctree: file ends inside a brick");
-  lz4_decode_block(buf.data(), buf.size(), out.data(), bytes);
+  switch (t.compression) {
+    case 1:
+      zlib_decode(buf.data(), buf.size(), out.data(), bytes);
+      break;
+    case 2:
+      // LzmaCompression.cpp: LzmaEncProps defaults (lc 3, lp 0, pb 2) at every
+      // level, raw stream without end marker; the dictionary size does not
+      // matter when the whole brick is the window
+      lzma_decode(buf.data(), buf.size(), out.data(), bytes, 3, 0, 2);
+      break;
+    case 3:
+      lz4_decode_block(buf.data(), buf.size(), out.data(), bytes);
+      break;
+    default:
+      bzip2_decode(buf.data(), buf.size(), out.data(), bytes);
+  }
 }
 
 }  // namespace tvk

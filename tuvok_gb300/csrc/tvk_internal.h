@@ -79,6 +79,12 @@ void tf1d_from_bytes(const uint8_t* bytes, uint64_t n, float* rgba);
 // ExtendedOctree tables and UVF metadata (api.cpp)
 std::vector<LodInfo> lod_table(const uint64_t dims[3], const uint32_t B[3], uint32_t ov);
 
+// brick decoders (codecs.cpp): the whole stream into exactly out_n bytes
+void zlib_decode(const uint8_t* in, size_t n, uint8_t* out, size_t out_n);
+void lzma_decode(const uint8_t* in, size_t n, uint8_t* out, size_t out_n, uint32_t lc,
+                 uint32_t lp, uint32_t pb);
+void bzip2_decode(const uint8_t* in, size_t n, uint8_t* out, size_t out_n);
+
 // ExtendedOctree file (eo.cpp): header and table of contents
 struct EoFile {
   std::string path;
