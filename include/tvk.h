@@ -748,6 +748,23 @@ tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t
 tvk_status tvk_renderer_get_stream(tvk_renderer* r, void** stream);
 /* Blocks until the renderer's stream is idle and fills *out for the last paint. */
 tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out);
+/* The raw counters of the renderer's last paint: [0] reference loop steps
+ * (samples), [1] executed samples, [2] rays the march guard stopped, [3]
+ * samples that took the gradient; [4..7] are filled only by a library built
+ * with TVK_PROFILE_COUNTS=1 (leap iterations, steps they skipped,
+ * candidate-brick slab tests, brick marches) and are 0 otherwise.  A
+ * diagnostic with no counterpart in the reference. */
+tvk_status tvk_get_counters(tvk_renderer* r, uint64_t out[8]);
+
+/* The macro-cell table of brick `index` (TOC order, any LOD): cells of 2^3
+ * voxel positions, cell c covering voxels c*2 .. c*2 + 2 on each axis
+ * (clamped to the brick), each entry min | max << 16 of the raw values there.
+ * dims receives the cell counts (x, y, z); with out == NULL only dims is
+ * filled, otherwise capacity must hold x*y*z entries, x fastest.  Colour
+ * volumes have no cells (TVK_ERR_UNSUPPORTED).  A diagnostic with no
+ * counterpart in the reference (the ray march's empty-space tables). */
+tvk_status tvk_volume_cell_minmax(const tvk_volume* v, uint64_t index, uint32_t* out,
+                                  uint64_t capacity, uint32_t dims[3]);
 
 /* ---------------------------------------------------------------- allocation-free bricking */
 

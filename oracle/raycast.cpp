@@ -1335,8 +1335,10 @@ struct LeaperBrick {
   uint32_t n[3];
 };
 
-// texel-centre trilinear at local texel coordinates, clamp to the brick's edge
-float leaper_sample(const LeaperBrick& b, int dtype, float l0, float l1, float l2, float im) {
+// texel-centre trilinear at local texel coordinates, clamp to the brick's edge;
+// RGBA8 bricks (dtype 2): channel ch
+float leaper_sample(const LeaperBrick& b, int dtype, float l0, float l1, float l2, float im,
+                    int ch = 0) {
   const float u[3] = {std::fmin(std::fmax(l0 - 0.5f, 0.0f), float(b.n[0]) - 1.0f),
                       std::fmin(std::fmax(l1 - 0.5f, 0.0f), float(b.n[1]) - 1.0f),
                       std::fmin(std::fmax(l2 - 0.5f, 0.0f), float(b.n[2]) - 1.0f)};
@@ -1349,6 +1351,7 @@ float leaper_sample(const LeaperBrick& b, int dtype, float l0, float l1, float l
   }
   auto fetch = [&](int x, int y, int z) -> float {
     const size_t i = size_t(x) + size_t(y) * b.n[0] + size_t(z) * b.n[0] * b.n[1];
+    if (dtype == 2) return float(b.data[4 * i + size_t(ch)]);
     return dtype == 0 ? float(b.data[i]) : float(reinterpret_cast<const uint16_t*>(b.data)[i]);
   };
   auto lerp = [](float a, float c, float w) { return std::fma(w, c - a, a); };
@@ -1379,7 +1382,11 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
                                       float* out, uint32_t* spp, uint64_t* missing,
                                       uint64_t max_missing, uint64_t* n_missing) {
   const orc_scene& s = *sc;
-  const int bytes = s.dtype == 0 ? 1 : 2;
+  // RGBA8 colour volumes (dtype 2): 8 bits per channel, range [0, 255], no
+  // gradient statistics (fGradientScale 1)
+  const bool color = s.dtype == 2;
+  const int bytes = color ? 4 : (s.dtype == 0 ? 1 : 2);
+  const int cbits = color ? 8 : 8 * bytes;
   uint64_t lsz[3 * 64], lcnt[3 * 64];
   const int n_lods = orc_lod_table(s.dims, s.brick_size, s.overlap, lsz, lcnt, 64);
   std::vector<uint64_t> first(n_lods + 1, 0), shapes;
@@ -1419,20 +1426,20 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
     tf[4 * i + 2] = e[2];
     tf[4 * i + 3] = 1.0f - std::pow(1.0f - e[3], oc);
   }
-  double rmax = 0;
-  for (uint64_t i = 0; i < s.dims[0] * s.dims[1] * s.dims[2]; ++i)
+  double rmax = color ? 255.0 : 0.0;
+  for (uint64_t i = 0; !color && i < s.dims[0] * s.dims[1] * s.dims[2]; ++i)
     rmax = std::max(rmax, bytes == 1 ? double(static_cast<const uint8_t*>(s.raw)[i])
                                      : double(static_cast<const uint16_t*>(s.raw)[i]));
-  const uint32_t imax = (1u << (8 * bytes)) - 1;
+  const uint32_t imax = (1u << cbits) - 1;
   const float trans_scale = float(double(imax) / rmax);
   float grad_scale = 1.0f;
-  if (s.render_mode == ORC_RM_2D) {
+  if (s.render_mode == ORC_RM_2D && !color) {
     const float mg = float(orc_max_gradient(s.raw, s.dtype, s.dims, s.brick_size, s.overlap,
                                             s.clamp_to_edge));
     grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
   }
-  const float im = bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
-  const float iso_norm = float(double(s.isovalue) / double(1u << (8 * bytes)));
+  const float im = bytes == 2 ? 1.0f / 65535.0f : 1.0f / 255.0f;
+  const float iso_norm = float(double(s.isovalue) / double(1u << cbits));
   Setup st;  // the fields iso_compose reads
   st.s = &s;
   for (int a = 0; a < 3; ++a) {
@@ -1617,8 +1624,121 @@ extern "C" uint64_t orc_leaper_render(const orc_scene* sc, const uint32_t* page,
             steps = std::min(steps, int(std::ceil(len3f((exi[0] - cur[0]) * sc[0], (exi[1] - cur[1]) * sc[1],
                                                         (exi[2] - cur[2]) * sc[2]) / step_len)));
             auto smp = [&](float a0, float a1, float a2) { return leaper_sample(b, s.dtype, a0, a1, a2, im); };
+            auto chan = [&](int ch, float a0, float a1, float a2) {
+              return leaper_sample(b, s.dtype, a0, a1, a2, im, ch);
+            };
+            // lighting.glsl:33-43 with the model-space eye; tfc = diffuse colour
+            auto light = [&](const float N[3], const float mp[3], float src[4]) {
+              const float q0 = Em[0] - mp[0], q1 = Em[1] - mp[1], q2 = Em[2] - mp[2];
+              const float lq = len3f(q0, q1, q2);
+              const float V0 = q0 / lq, V1 = q1 / lq, V2 = q2 / lq;
+              const float dd = (N[0] * V0 + N[1] * V1) + N[2] * V2;
+              float R0 = V0 - (2.0f * dd) * N[0], R1 = V1 - (2.0f * dd) * N[1],
+                    R2 = V2 - (2.0f * dd) * N[2];
+              const float lr = len3f(R0, R1, R2);
+              R0 = R0 / lr; R1 = R1 / lr; R2 = R2 / lr;
+              const float diff = std::fmax(std::fabs((N[0] * Lm[0] + N[1] * Lm[1]) + N[2] * Lm[2]), 0.0f);
+              const float spec = pow_int_or_real(std::fmax((R0 * Lm[0] + R1 * Lm[1]) + R2 * Lm[2], 0.0f), 8.0f);
+              for (int c = 0; c < 3; ++c) {
+                const float dcol = st.light_d[c] * src[c];
+                float x = st.light_a[c] + dcol * diff;
+                x = x + st.light_s[c] * spec;
+                src[c] = std::fmin(std::fmax(x, 0.0f), 1.0f);
+              }
+            };
             for (int i = 0; i < steps; ++i) {
               ++samples;
+              if (color) {
+                // GLGridLeaper-Method-*-color.glsl: the filtered RGBA
+                const float cd[4] = {chan(0, pc[0], pc[1], pc[2]), chan(1, pc[0], pc[1], pc[2]),
+                                     chan(2, pc[0], pc[1], pc[2]), chan(3, pc[0], pc[1], pc[2])};
+                if (iso) {
+                  // GLGridLeaper-Method-iso-color.glsl: alpha >= fIsoval, bisection on
+                  // alpha, ComputeAlphaNormal = the red channel's gradient
+                  if (cd[3] >= iso_norm) {
+                    float rr2[3] = {sv[0] / 2.0f, sv[1] / 2.0f, sv[2] / 2.0f};
+                    float q[3] = {pc[0] - rr2[0], pc[1] - rr2[1], pc[2] - rr2[2]};
+                    for (int k = 0; k < 5; ++k) {
+                      for (int a = 0; a < 3; ++a) rr2[a] = rr2[a] / 2.0f;
+                      const float vv = chan(3, q[0], q[1], q[2]);
+                      for (int a = 0; a < 3; ++a) q[a] = vv >= iso_norm ? q[a] - rr2[a] : q[a] + rr2[a];
+                    }
+                    float g[3] = {(chan(0, q[0] - 1.0f, q[1], q[2]) - chan(0, q[0] + 1.0f, q[1], q[2])) / 2.0f,
+                                  (chan(0, q[0], q[1] - 1.0f, q[2]) - chan(0, q[0], q[1] + 1.0f, q[2])) / 2.0f,
+                                  (chan(0, q[0], q[1], q[2] - 1.0f) - chan(0, q[0], q[1], q[2] + 1.0f)) / 2.0f};
+                    const float gl = len3f(g[0], g[1], g[2]);
+                    if (gl > 0.0f) { g[0] = g[0] / gl; g[1] = g[1] / gl; g[2] = g[2] / gl; }
+                    float hp[3], he[3], hn[3];
+                    for (int a = 0; a < 3; ++a) hp[a] = (q[a] - tr[a]) / sc[a];
+                    for (int r2 = 0; r2 < 3; ++r2) {
+                      he[r2] = std::fma(norm2eye[r2][0], hp[0],
+                                        std::fma(norm2eye[r2][1], hp[1],
+                                                 std::fma(norm2eye[r2][2], hp[2], norm2eye[r2][3])));
+                      hn[r2] = std::fma(nte[r2][2], g[2], std::fma(nte[r2][1], g[1], nte[r2][0] * g[0]));
+                    }
+                    // GLGridLeaper-iso.glsl:169-171 packing, Compose-Color-FS unpacking
+                    const float enc_r = cd[0] + 1.0f;
+                    const float enc_gb = std::floor(cd[1] * 512.0f) + cd[2];
+                    const float rgb[3] = {enc_r - 1.0f, std::floor(enc_gb / 2.0f) / 256.0f,
+                                          enc_gb - std::floor(enc_gb)};
+                    float dcol[3], c3[3];
+                    for (int a = 0; a < 3; ++a) dcol[a] = rgb[a] * st.light_d[a];
+                    surface_lighting<float>(st, he, hn, dcol, c3);
+                    hitc[0] = c3[0]; hitc[1] = c3[1]; hitc[2] = c3[2]; hitc[3] = 1.0f;
+                    done = true;
+                    break;
+                  }
+                } else {
+                  const float u = cd[3] * trans_scale;
+                  float fx = std::floor(u * W);
+                  fx = std::fmin(std::fmax(fx, 0.0f), W - 1.0f);
+                  float al = 0.0f, g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, mag = 0.0f;
+                  if (two_d) {
+                    bool col_any = false;
+                    for (uint32_t y = 0; y < s.tf_h; ++y)
+                      if (tf[4 * (size_t(y) * s.tf_w + size_t(fx)) + 3] != 0.0f) col_any = true;
+                    if (col_any) {
+                      // ComputeGradientAlpha
+                      g0 = (chan(3, pc[0] - 1.0f, pc[1], pc[2]) - chan(3, pc[0] + 1.0f, pc[1], pc[2])) / 2.0f;
+                      g1 = (chan(3, pc[0], pc[1] - 1.0f, pc[2]) - chan(3, pc[0], pc[1] + 1.0f, pc[2])) / 2.0f;
+                      g2 = (chan(3, pc[0], pc[1], pc[2] - 1.0f) - chan(3, pc[0], pc[1], pc[2] + 1.0f)) / 2.0f;
+                      mag = len3f(g0, g1, g2);
+                      const float w = 1.0f - mag * grad_scale;
+                      float fy = std::floor(w * H);
+                      fy = std::fmin(std::fmax(fy, 0.0f), H - 1.0f);
+                      al = tf[4 * (size_t(fy) * s.tf_w + size_t(fx)) + 3];
+                    }
+                  } else {
+                    al = tf[4 * size_t(fx) + 3];
+                  }
+                  float src[4] = {cd[0], cd[1], cd[2], al};
+                  if (lit && al != 0.0f) {
+                    float N[3];
+                    if (two_d) {
+                      N[0] = mag > 0.0f ? g0 / mag : g0;
+                      N[1] = mag > 0.0f ? g1 / mag : g1;
+                      N[2] = mag > 0.0f ? g2 / mag : g2;
+                    } else {  // ComputeNormal on the red channel
+                      N[0] = (chan(0, pc[0] - 1.0f, pc[1], pc[2]) - chan(0, pc[0] + 1.0f, pc[1], pc[2])) / 2.0f;
+                      N[1] = (chan(0, pc[0], pc[1] - 1.0f, pc[2]) - chan(0, pc[0], pc[1] + 1.0f, pc[2])) / 2.0f;
+                      N[2] = (chan(0, pc[0], pc[1], pc[2] - 1.0f) - chan(0, pc[0], pc[1], pc[2] + 1.0f)) / 2.0f;
+                      const float l = len3f(N[0], N[1], N[2]);
+                      if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+                    }
+                    float mp[3];
+                    for (int a = 0; a < 3; ++a) mp[a] = (pc[a] - tr[a]) / sc[a];
+                    light(N, mp, src);
+                  }
+                  const float w = 1.0f - acc[3];
+                  acc[0] = std::fma(src[0] * w, src[3], acc[0]);
+                  acc[1] = std::fma(src[1] * w, src[3], acc[1]);
+                  acc[2] = std::fma(src[2] * w, src[3], acc[2]);
+                  acc[3] = std::fma(src[3], w, acc[3]);
+                  if (acc[3] > 0.99f) { done = true; break; }
+                }
+                for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
+                continue;
+              }
               const float val = smp(pc[0], pc[1], pc[2]);
               if (iso) {
                 if (val >= iso_norm) {

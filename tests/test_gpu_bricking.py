@@ -222,3 +222,39 @@ def test_gpu_brick_key_errors(cuda_ok):
     with pytest.raises(TvkError) as e:
         only0.GetBrick((0, 1, 0))
     assert "UNSUPPORTED" in str(e.value)
+
+
+def cell_tables(d):
+    """Macro-cell (min, max) of a brick [z, y, x]: cell c covers voxels 2c ..
+    2c + 2 on each axis, clamped to the brick."""
+    lo, hi = d.astype(np.int64), d.astype(np.int64)
+    for axis in (2, 1, 0):
+        n = d.shape[axis]
+        i0 = 2 * np.arange((n - 1) // 2 + 1)
+        idx = [i0, np.minimum(i0 + 1, n - 1), np.minimum(i0 + 2, n - 1)]
+        lo = np.minimum.reduce([np.take(lo, i, axis=axis) for i in idx])
+        hi = np.maximum.reduce([np.take(hi, i, axis=axis) for i in idx])
+    return lo, hi
+
+
+@pytest.mark.parametrize("dims,dtype,bs,ov", [
+    ((61, 47, 39), np.uint16, (18, 18, 18), 1),
+    ((50, 41, 33), np.uint8, (17, 12, 9), 1),      # odd and even brick sizes, odd LODs
+    ((250, 30, 21), np.uint16, (226, 18, 10), 1),  # > 96 cells along x: two passes
+    ((25, 14, 13), np.uint8, (16, 16, 16), 2),
+])
+def test_gpu_cell_minmax_equals_brick_data(cuda_ok, dims, dtype, bs, ov):
+    """The empty-space tables of every brick of every LOD: min/max of the
+    (up to) 3^3 voxels each cell's samples can touch, from the brick itself."""
+    vmax = 255 if dtype == np.uint8 else 4095
+    raw = numpy_blob_volume(dims, dtype, 7, (2, 8), (vmax * 0.2, vmax), vmax, seed=23, noise=5)
+    vol = Volume(raw, brick_size=bs, overlap=ov)
+    i = 0
+    for lod in range(vol.GetLODLevelCount()):
+        for k in range(vol.GetBrickCount(lod)):
+            b = vol.GetBrick((0, lod, k))
+            lo, hi = vol.GetCellMinMax(i)
+            rlo, rhi = cell_tables(b)
+            np.testing.assert_array_equal(lo, rlo, err_msg=f"lod {lod} brick {k} min")
+            np.testing.assert_array_equal(hi, rhi, err_msg=f"lod {lod} brick {k} max")
+            i += 1

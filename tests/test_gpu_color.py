@@ -5,7 +5,14 @@ channel's surface, GLRaycaster-Color-FS + Compose-Color-FS) with the usual
 image tolerance.  The opacity correction of a colour sample depends on the
 voxel's alpha, so it runs per sample; GLSL's pow(x, y) = exp2(y * log2(x)) is
 evaluated on both sides by the same float operations, so sample counts are
-equal pixel for pixel."""
+equal pixel for pixel.
+
+The GridLeaper over a colour pool (GLGridLeaper-Method-*-color.glsl: the
+voxel's colour with the TF's alpha at its alpha, 1D and 2D, lit and unlit; iso
+on the alpha channel with the red channel's normal): one pass and a converged
+frame against the oracle's pass over the same page table, sample counts and
+missing-brick requests equal.  Colour bricks carry no value statistics
+(range [0, 255]), so every brick is visible to a TF with any opacity."""
 import numpy as np
 import pytest
 
@@ -134,8 +141,73 @@ def test_gpu_color_refusals(cuda_ok, rgba):
     with pytest.raises(TvkError):
         Batch().Paint([r])
     with pytest.raises(TvkError):
-        Pool(vol, 1 << 26)
-    with pytest.raises(TvkError):
         vol.GetHistogram()
     with pytest.raises(TvkError):
         vol.Rebrick((9, 9, 9))
+
+
+LEAPER_CASES = [
+    # id, mode, lighting, eye, srm
+    ("leap_1d", 0, False, (0.3, 0.4, 1.5), 1.0),
+    ("leap_1d_lit", 0, True, (-1.1, 0.2, -0.7), 1.0),
+    ("leap_1d_lit_far", 0, True, (1.4, 1.9, 3.5), 1.7),
+    ("leap_2d", 1, False, (0.9, -0.6, 1.2), 1.0),
+    ("leap_2d_lit", 1, True, (0.3, 0.4, 1.5), 1.0),
+    ("leap_iso", 2, False, (0.9, 0.6, 1.0), 1.0),
+    ("leap_iso_far", 2, False, (-1.6, 1.4, 2.8), 1.0),
+]
+
+
+def leaper_setup(rgba, mode, lit, srm):
+    from test_gpu_render import tf2d
+    vol = Volume(rgba, brick_size=(BS,) * 3, overlap=1)
+    r = Renderer()
+    r.RegisterDataset(vol)
+    tf = tf2d(256, 32) if mode == 1 else color_tf(256)
+    if mode == 1:
+        r.Set2DTransFloat(tf)
+    elif mode == 0:
+        r.Set1DTransFloat(tf)
+    else:
+        r.SetIsoValue(130.0)
+    r.SetRendermode(mode)
+    r.SetUseLighting(lit)
+    r.SetSampleRateModifier(srm)
+    r.Resize(W, H)
+    return vol, r, tf
+
+
+def leaper_oracle(rgba, tf, page, mode, lit, srm, eye):
+    kw = dict(width=W, height=H, eye=eye, mode=mode, lighting=lit, srm=srm)
+    if mode == 2:
+        kw["isovalue"] = 130.0
+    return O.leaper_render(rgba, (BS,) * 3, 1, tf, page, **kw)
+
+
+@pytest.mark.parametrize("case", LEAPER_CASES, ids=[c[0] for c in LEAPER_CASES])
+def test_gpu_color_leaper_matches_oracle(cuda_ok, rgba, case):
+    from test_gpu_leaper import check_missing, compare_pass
+    name, mode, lit, eye, srm = case
+    vol, r, tf = leaper_setup(rgba, mode, lit, srm)
+    pool = Pool(vol, 1 << 30)
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+    # cold pass: only the coarsest brick cached, nothing flagged empty
+    info = pool.Paint(r, max_passes=1)
+    page = pool.GetPageTable()
+    assert info.passes == 1 and info.resident == 1 and page[-1] >= 3
+    assert (page[:-1] == 0).all(), name
+    img, cnt = r.ReadBackPixels(), r.ReadSampleCounts()
+    ref, n, rc, missing = leaper_oracle(rgba, tf, page, mode, lit, srm, eye)
+    compare_pass(img, cnt, ref, rc, name + " cold")
+    check_missing(pool.GetRequests(), missing, name)
+    assert missing.size > 0 and n > 0
+    # converged: every brick the view needs is resident
+    info = pool.Paint(r, max_passes=64)
+    assert info.converged == 1 and info.missing_last == 0
+    again = pool.Paint(r, max_passes=1)
+    assert again.passes == 1 and again.paged == 0 and again.missing_last <= 2
+    page = pool.GetPageTable()
+    img, cnt = r.ReadBackPixels(), r.ReadSampleCounts()
+    ref, n, rc, missing = leaper_oracle(rgba, tf, page, mode, lit, srm, eye)
+    compare_pass(img, cnt, ref, rc, name + " converged")
+    assert (img[..., 3] > 0).mean() > (0.02 if "far" in name else 0.05), name

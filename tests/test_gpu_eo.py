@@ -1,8 +1,12 @@
 """tvk_volume_open_extended_octree over the converter-written fixtures
-(tests/golden/eo, made by the reference's ExtendedOctreeConverter): the
-loaded volume equals the one bricked from the same voxels -- every brick of
-every LOD, the statistics and a rendered frame -- whatever flags the caller
-guesses; malformed files are refused without touching the GPU state."""
+(tests/golden/eo, made by the reference's ExtendedOctreeConverter), whatever
+flags the caller guesses: every brick of every LOD of the loaded volume is the
+file's brick (the decoded bytes), its statistics are those bricks' min/max,
+and LOD 0, the data range, the maximum gradient and a rendered frame equal the
+volume bricked from the same voxels.  (The converter leaves stale data of its
+reused buffers in some ghost voxels of coarser bricks -- the loader keeps those
+bricks from the file, a direct build has zeros there.)  Malformed files are
+refused without touching the GPU state."""
 import json
 import shutil
 from pathlib import Path
@@ -39,16 +43,20 @@ def test_gpu_eo_matches_direct_bricking(cuda_ok, case, guess):
                                   clamp_to_edge=case["clamp"] ^ flip,
                                   median=case["median"] ^ flip)
     color = case["components"] == 4
-    # LOD 0 always; coarser LODs where the converter's bricks are reproducible:
-    # with an overlap of 2 or more some coarser ghost corners keep stale data of
-    # the converter's reused buffers (clamped or not), which the loader keeps
-    # from the file and a direct build fills with zeros
-    lod0 = case["overlap"] >= 2
-    keys = [(0, 0, k) for k in range(ref.GetBrickCount(0))] if lod0 else all_keys(ref)
-    for key in keys:
-        np.testing.assert_array_equal(v.GetBrick(key), ref.GetBrick(key), err_msg=str(key))
-        mm, mr = v.MaxMinForKey(key), ref.MaxMinForKey(key)
-        assert (mm.min_scalar, mm.max_scalar) == (mr.min_scalar, mr.max_scalar)
+    import test_eo_fixtures as F
+    buf = (EO / f"{case['name']}.eo").read_bytes()
+    toc = F.parse(buf)["toc"]
+    for k, key in enumerate(all_keys(ref)):
+        got = v.GetBrick(key)
+        off, length, comp = toc[k][0], toc[k][1], toc[k][2]
+        want = np.frombuffer(F.expand(buf[off:off + length], comp, got.nbytes),
+                             dtype=got.dtype).reshape(got.shape)
+        np.testing.assert_array_equal(got, want, err_msg=f"file brick {key}")
+        if key[1] == 0:
+            np.testing.assert_array_equal(got, ref.GetBrick(key), err_msg=str(key))
+        if not color:
+            mm = v.MaxMinForKey(key)
+            assert (mm.min_scalar, mm.max_scalar) == (float(got.min()), float(got.max()))
     assert v.GetRange() == ref.GetRange()
     assert v.MaxGradientMagnitude() == ref.MaxGradientMagnitude()
     imgs = []

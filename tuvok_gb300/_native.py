@@ -218,6 +218,8 @@ PROTOTYPES = {
     "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],
     "tvk_renderer_get_stream": [_vp, C.POINTER(_vp)],
     "tvk_get_stats": [_vp, C.POINTER(Stats)],
+    "tvk_get_counters": [_vp, _u64p],
+    "tvk_volume_cell_minmax": [_vp, C.c_uint64, _u32p, C.c_uint64, _u32p],
     "tvk_generate_volume": [_vp, C.c_int, _u64p, _f32p, C.c_uint32, C.c_float, C.c_uint32,
                             C.c_float, C.c_uint64, C.c_int, C.c_float],
     "tvk_brick_lod0_noalloc": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, _u64p,

@@ -377,7 +377,7 @@ void build_volume(tvk_volume* V, const void* d_raw, cudaStream_t s) {
     V->cell_counts[k] = cx * cy * cz;
     V->cell_offsets[k] = V->total_cells;
     V->total_cells += V->cell_counts[k];
-    max_cell_rows = std::max(max_cell_rows, cy * cz);
+    max_cell_rows = std::max(max_cell_rows, cy);
   }
   TVK_CUDA(cudaMalloc(&V->d_cells, V->total_cells * sizeof(uint32_t)));
   TVK_CUDA(cudaMalloc(&V->d_cell_meta, nb_all * (sizeof(uint64_t) + sizeof(uint32_t))));
@@ -712,6 +712,10 @@ struct tvk_batch {
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> graph_sig;
   std::vector<cudaGraphNode_t> kernel_nodes;  // graph node of each launch
+  // launches 1.. run on their own streams, forked from and joined back into
+  // `stream`, so that one launch's tail overlaps the next launch's work
+  std::vector<cudaStream_t> aux;
+  std::vector<cudaEvent_t> fork_join;         // [0]: fork; [1 + k]: join of aux[k]
   tvk_batch_info info{};
 };
 
@@ -1218,7 +1222,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
   const size_t npix = size_t(R->width) * R->height;
   R->d_img.ensure(npix * sizeof(float4));
   R->d_spp.ensure(size_t(rw) * rh * sizeof(uint32_t));
-  st.d_counters->ensure(4 * sizeof(unsigned long long));
+  st.d_counters->ensure(8 * sizeof(unsigned long long));
   const bool upscale = rw != R->width || rh != R->height;
   if (upscale) R->d_lowimg.ensure(size_t(rw) * rh * sizeof(float4));
   P.out = upscale ? R->d_lowimg.as<float4>() : R->d_img.as<float4>();
@@ -1228,7 +1232,7 @@ PlannedFrame plan_frame(tvk_renderer* R, const Subframe& sf, const Stage* stage 
     P.depth = R->d_depth.as<float>();
   }
   P.counters = st.d_counters->as<unsigned long long>();
-  TVK_CUDA(cudaMemsetAsync(st.d_counters->p, 0, 4 * sizeof(unsigned long long), st.stream));
+  TVK_CUDA(cudaMemsetAsync(st.d_counters->p, 0, 8 * sizeof(unsigned long long), st.stream));
   R->stats.bricks_visible = nvis;
   R->stats.bricks_total = nbl;
   CvComposeParams cv;
@@ -1280,8 +1284,8 @@ void launch_upscale_of(tvk_renderer* R, const PlannedFrame& F, cudaStream_t s,
 void finish_frame(tvk_renderer* R, const PlannedFrame& F) {
   R->render_w = F.rw;
   R->render_h = F.rh;
-  R->h_counters.ensure(4 * sizeof(unsigned long long));
-  TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 4 * sizeof(unsigned long long),
+  R->h_counters.ensure(8 * sizeof(unsigned long long));
+  TVK_CUDA(cudaMemcpyAsync(R->h_counters.p, R->d_counters.p, 8 * sizeof(unsigned long long),
                            cudaMemcpyDeviceToHost, R->stream));
   R->stats.kernel_launches = R->launches - F.launches0;
   R->painted = true;
@@ -1454,9 +1458,29 @@ void enqueue_batch(tvk_batch* B, tvk_renderer* const* rs, const std::vector<Plan
   const size_t nl = B->launch.size();
   TVK_CUDA(cudaMemsetAsync(B->d_next.p, 0, nl * sizeof(uint32_t), B->stream));
   uint64_t dummy = 0;
-  for (size_t k = 0; k < nl; ++k)
-    launch_raycast_batch(B->launch[k], B->variant[k], B->d_next.as<uint32_t>() + k, ctas,
-                         B->stream, &dummy);
+  // the launches are independent (each has its own frames and work counter):
+  // run them concurrently, so a launch's last CTAs share the GPU with the next
+  while (B->aux.size() + 1 < nl) {
+    cudaStream_t st = nullptr;
+    TVK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    B->aux.push_back(st);
+  }
+  while (B->fork_join.size() < nl) {
+    cudaEvent_t e = nullptr;
+    TVK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    B->fork_join.push_back(e);
+  }
+  if (nl > 1) TVK_CUDA(cudaEventRecord(B->fork_join[0], B->stream));
+  for (size_t k = 0; k < nl; ++k) {
+    cudaStream_t st = k == 0 ? B->stream : B->aux[k - 1];
+    if (k > 0) TVK_CUDA(cudaStreamWaitEvent(st, B->fork_join[0], 0));
+    launch_raycast_batch(B->launch[k], B->variant[k], B->d_next.as<uint32_t>() + k, ctas, st,
+                         &dummy);
+  }
+  for (size_t k = 1; k < nl; ++k) {
+    TVK_CUDA(cudaEventRecord(B->fork_join[k], B->aux[k - 1]));
+    TVK_CUDA(cudaStreamWaitEvent(B->stream, B->fork_join[k], 0));
+  }
   for (size_t i = 0; i < F.size(); ++i) launch_upscale_of(rs[i], F[i], B->stream, &dummy);
 }
 
@@ -1957,10 +1981,15 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
   const uint64_t launches0 = R->launches;
   const float srm = R->srm;
   // GLGridLeaper-blend.glsl OpacityCorrectColor with ocFactor = 1 / srm
+  // (a colour pool's alpha is the TF's alpha, so the same corrected table)
   if (!R->tf.empty()) upload_tf(R, 1.0f / srm);
-  const uint32_t imax = (1u << (8 * V->bytes)) - 1;
+  // CalculateScaling and GetNormalizedIsovalue with the bit width per
+  // channel (8 for RGBA8 colour volumes)
+  const bool color = V->dtype == TVK_RGBA8;
+  const uint32_t cbits = color ? 8 : 8 * V->bytes;
+  const uint32_t imax = (1u << cbits) - 1;
   const float trans_scale = float(double(imax) / V->range_max);
-  const float iso_norm = float(double(R->isovalue) / double(1u << (8 * V->bytes)));
+  const float iso_norm = float(double(R->isovalue) / double(1u << cbits));
   // the visible range of the TF (AbstrRenderer::ContainsData's limits)
   uint64_t nz_lo = R->tf_w, nz_hi = 0;
   for (uint32_t y = 0; y < R->tf_h; ++y)
@@ -1992,8 +2021,9 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
     pool_upload_page_table(pool);
   }
 
-  // empty-cell distances of every brick for this TF / isovalue
-  if (R->cell_skip) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
+  // empty-cell distances of every brick for this TF / isovalue (colour
+  // bricks have no macro cells)
+  if (R->cell_skip && !color) update_empty_cells(R, V, trans_scale, iso_mode, iso_norm);
   const View view = make_view(R->eye, R->at, R->up, R->fovy, R->width, R->height, R->model);
   LeaperParams L;
   std::memset(&L, 0, sizeof(L));
@@ -2009,7 +2039,7 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
   P.trans_scale = trans_scale;
   const float mg = float(V->max_grad);
   P.grad_scale = (mg == 0) ? 1.0f : 1.0f / mg;
-  P.inv_max_raw = V->bytes == 1 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  P.inv_max_raw = V->bytes == 2 ? 1.0f / 65535.0f : 1.0f / 255.0f;
   for (int a = 0; a < 3; ++a) {
     P.light_a[a] = R->ambient[a] * R->ambient[3];
     P.light_d[a] = R->diffuse[a] * R->diffuse[3];
@@ -2104,7 +2134,7 @@ void leaper_paint(tvk_renderer* R, tvk_pool* pool, uint32_t max_passes, tvk_leap
   pool->d_resume_col.ensure(npix * sizeof(float4));
   L.resume_pos = pool->d_resume_pos.as<float4>();
   L.resume_col = pool->d_resume_col.as<float4>();
-  L.cell_dist = R->cell_skip ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
+  L.cell_dist = (R->cell_skip && !color) ? R->slots[R->slot].d_dist.as<uint8_t>() : nullptr;
   L.cell_off = static_cast<const uint64_t*>(V->d_cell_meta);
 
   std::memset(info, 0, sizeof(*info));
@@ -2414,7 +2444,7 @@ tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                           cudaMemcpyHostToDevice));
       uint32_t max_rows = 0;
       for (uint32_t d : V->cell_dims)
-        max_rows = std::max(max_rows, ((d >> 10) & 1023u) * (d >> 20));
+        max_rows = std::max(max_rows, (d >> 10) & 1023u);
       uint64_t launches = 0;
       tvk::launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
                               static_cast<const uint64_t*>(V->d_cell_meta), V->total_bricks,
@@ -2924,6 +2954,11 @@ tvk_status tvk_batch_destroy(tvk_batch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     for (cudaEvent_t e : {b->ev_start, b->ev_stop, b->ev_done})
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->fork_join) cudaEventDestroy(e);
+    for (cudaStream_t st : b->aux) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
   });
@@ -3292,7 +3327,6 @@ tvk_status tvk_pool_create(const tvk_volume* v, uint64_t budget_bytes, int host_
                            tvk_pool** out) {
   return guarded([&] {
     REQUIRE(v && out, "null argument");
-    tvk::require_scalar(v, "the GridLeaper pool");
     if (v->rebricked) tvk::fail(TVK_ERR_UNSUPPORTED, "pools are built over bricked volumes");
     const size_t n_lods = v->lod_first.size() - 1;
     if (n_lods != v->lods.size())
@@ -3496,6 +3530,41 @@ tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out) {
     if (c[2] != 0)
       tvk::fail(TVK_ERR_INTERNAL, "ray march guard tripped on " + std::to_string(c[2]) + " rays");
     *out = r->stats;
+  });
+}
+
+tvk_status tvk_volume_cell_minmax(const tvk_volume* v, uint64_t index, uint32_t* out,
+                                  uint64_t capacity, uint32_t dims[3]) {
+  return guarded([&] {
+    REQUIRE(v && dims, "null argument");
+    if (v->dtype == TVK_RGBA8) tvk::fail(TVK_ERR_UNSUPPORTED, "colour volumes have no macro cells");
+    REQUIRE(index < v->total_bricks && index < v->cell_dims.size(), "brick index out of range");
+    const uint32_t d = v->cell_dims[index];
+    dims[0] = d & 1023u;
+    dims[1] = (d >> 10) & 1023u;
+    dims[2] = d >> 20;
+    if (!out) return;
+    const uint64_t n = v->cell_counts[index];
+    REQUIRE(capacity >= n, "capacity below the brick's cell count");
+    TVK_CUDA(cudaSetDevice(v->device));
+    TVK_CUDA(cudaMemcpy(out, static_cast<const uint32_t*>(v->d_cells) + v->cell_offsets[index],
+                        n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  });
+}
+
+tvk_status tvk_get_counters(tvk_renderer* r, uint64_t out[8]) {
+  return guarded([&] {
+    REQUIRE(r && out, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    TVK_CUDA(cudaStreamSynchronize(r->stream));
+    if (r->h_counters.bytes < 8 * sizeof(unsigned long long)) {
+      for (int i = 0; i < 8; ++i) out[i] = 0;
+      const unsigned long long* c = r->h_counters.as<unsigned long long>();
+      for (int i = 0; i < 4 && r->h_counters.bytes >= (i + 1) * sizeof(*c); ++i) out[i] = c[i];
+      return;
+    }
+    const unsigned long long* c = r->h_counters.as<unsigned long long>();
+    for (int i = 0; i < 8; ++i) out[i] = c[i];
   });
 }
 

@@ -31,7 +31,11 @@ namespace tvk {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr uint32_t kSmemGlobalBins = 11776;  // keeps the CTA under 48 KB of smem
+// row segments of 32 voxels whose loads a warp of brick_copy_kernel issues together
+constexpr uint32_t kUnroll = 4;
+// global-histogram bins kept in a CTA's shared memory (16 KB: 12-bit data
+// entirely; larger values go to the global bins directly)
+constexpr uint32_t kSmemGlobalBins = 4096;
 
 // Source voxel of brick-local position (i, j, k) of brick (cx, cy, cz).
 template <class T>
@@ -117,7 +121,7 @@ __device__ __forceinline__ bool source_row(const BrickGrid& g, const uint32_t c[
 // each CTA takes (brick, z-chunk) items in turn and merges its shared
 // histogram into the global one once, at the end.
 template <class T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
 brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __restrict__ offsets,
                   const uint32_t* __restrict__ sizes, T* __restrict__ pool, BrickScratch sc,
                   uint32_t smem_bins, uint32_t z_chunk, uint32_t chunks_per_brick,
@@ -146,28 +150,39 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
       const bool live = source_row(g, c, bs, j, k, rowbase);
       const bool inner_row = j >= ov && j < bs[1] - ov && k >= ov && k < bs[2] - ov;
       T* const out = brick + (uint64_t(k) * bs[1] + j) * bs[0];
-      for (uint32_t base = 0; base < bs[0]; base += 32) {
-        const uint32_t i = base + lane;
-        const bool act = i < bs[0];
-        T v = T(0);
-        if (act && live) {
-          uint32_t l = i;
-          if (g.clamp) {
-            if (fx && l < ov) l = ov;
-            if (lx && l > bs[0] - 1 - ov) l = bs[0] - 1 - ov;
-          }
-          if (l >= sx && l < ex) {
-            const uint64_t L = (xbase + l - ov) + rowbase;
-            if (L < g.total) v = __ldg(raw + L);
+      // kUnroll row segments of 32 voxels per pass: their loads are all in
+      // flight before the first store
+      for (uint32_t base = 0; base < bs[0]; base += 32 * kUnroll) {
+        T v[kUnroll];
+#pragma unroll
+        for (uint32_t u = 0; u < kUnroll; ++u) {
+          const uint32_t i = base + 32 * u + lane;
+          v[u] = T(0);
+          if (i < bs[0] && live) {
+            uint32_t l = i;
+            if (g.clamp) {
+              if (fx && l < ov) l = ov;
+              if (lx && l > bs[0] - 1 - ov) l = bs[0] - 1 - ov;
+            }
+            if (l >= sx && l < ex) {
+              const uint64_t L = (xbase + l - ov) + rowbase;
+              if (L < g.total) v[u] = __ldg(raw + L);
+            }
           }
         }
-        if (act) {
-          out[i] = v;
-          lo = min(lo, uint32_t(v));
-          hi = max(hi, uint32_t(v));
+#pragma unroll
+        for (uint32_t u = 0; u < kUnroll; ++u) {
+          const uint32_t i = base + 32 * u + lane;
+          if (base + 32 * u >= bs[0]) break;  // warp-uniform
+          const bool act = i < bs[0];
+          if (act) {
+            out[i] = v[u];
+            lo = min(lo, uint32_t(v[u]));
+            hi = max(hi, uint32_t(v[u]));
+          }
+          hist_add_warp(gh, sc.hist, smem_bins,
+                        act && inner_row && i >= ov && i < bs[0] - ov, uint32_t(v[u]), lane);
         }
-        hist_add_warp(gh, sc.hist, smem_bins, act && inner_row && i >= ov && i < bs[0] - ov,
-                      uint32_t(v), lane);
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -188,7 +203,10 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
 // histogram of inner voxels (bin = value >> shift) and the largest squared
 // central-difference sum Q = dx^2 + dy^2 + dz^2 over inner voxels
 // (Histogram2DDataBlock::ComputeGradient, Histogram2DDataBlock.cpp:327-345, in
-// integers).  One warp per inner row of a brick z-chunk.
+// integers).  A warp owns 32 consecutive inner voxels of one row j and walks
+// them along z through the CTA's z-chunk: the z neighbours stay in registers
+// (one new load per voxel), the x neighbours come from the adjacent lanes (the
+// two end lanes load theirs), the y neighbours are two loads.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 brick_sweep_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
@@ -203,34 +221,51 @@ brick_sweep_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
   const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
   const T* const p = pool + offsets[b];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t ix = bs[0] > 2 * ov ? bs[0] - 2 * ov : 0;
   const uint32_t iy = bs[1] > 2 * ov ? bs[1] - 2 * ov : 0;
   const uint32_t z0 = ov + blockIdx.y * z_chunk;
   const uint32_t z1 = bs[2] > ov ? min(bs[2] - ov, z0 + z_chunk) : 0;
   const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
   const bool grad = ov > 0;  // central differences need a ghost layer on every side
   long long qmax = -1;
-  const uint32_t rows = z1 > z0 ? (z1 - z0) * iy : 0;
-  for (uint32_t r = warp; r < rows; r += nwarps) {
-    const uint32_t k = z0 + r / iy;
-    const uint32_t j = ov + (r - (k - z0) * iy);
-    const T* const line = p + uint64_t(k) * sxy + uint64_t(j) * sx;
-    for (uint32_t base = ov; base < bs[0] - ov; base += 32) {
-      const uint32_t i = base + lane;
-      const bool act = i < bs[0] - ov;
-      uint32_t v = 0;
-      if (act) {
-        const T* const c = line + i;
-        v = c[0];
-        if (grad) {
-          const int dx = int(c[-1]) - int(c[1]);
-          const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
-          const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
+  const uint32_t nseg = (ix + 31) / 32;
+  const uint32_t items = z1 > z0 ? iy * nseg : 0;
+  for (uint32_t item = warp; item < items; item += nwarps) {
+    const uint32_t j = ov + item / nseg;
+    const uint32_t i = ov + (item % nseg) * 32 + lane;
+    const bool act = i < bs[0] - ov;  // an inner voxel
+    const bool mem = i < bs[0];       // inside the brick row (feeds a neighbour's dx)
+    const T* const col = p + uint64_t(j) * sx + i;
+    uint32_t prev = 0, cur = 0;
+    if (mem) {
+      cur = col[uint64_t(z0) * sxy];
+      if (grad) prev = col[uint64_t(z0 - 1) * sxy];
+    }
+    for (uint32_t k = z0; k < z1; ++k) {
+      const uint64_t zo = uint64_t(k) * sxy;
+      uint32_t next = 0;
+      if (mem && grad) next = col[zo + sxy];
+      if (grad) {
+        uint32_t xm = __shfl_up_sync(0xffffffffu, cur, 1);
+        uint32_t xp = __shfl_down_sync(0xffffffffu, cur, 1);
+        if (act) {
+          if (lane == 0) xm = col[zo - 1];
+          if (lane == 31) xp = col[zo + 1];
+          const int dx = int(xm) - int(xp);
+          const int dy = int(col[zo - sx]) - int(col[zo + sx]);
+          const int dz = int(prev) - int(next);
           const long long q =
               (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
           qmax = q > qmax ? q : qmax;
         }
       }
-      hist_add_warp(bh, nullptr, 256u, act, min(v >> shift, 255u), lane);
+      hist_add_warp(bh, nullptr, 256u, act, min(cur >> shift, 255u), lane);
+      prev = cur;
+      if (grad) {
+        cur = next;
+      } else if (mem && k + 1 < z1) {
+        cur = col[zo + sxy];
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -426,10 +461,15 @@ void launch_histogram2d(const void* pool, int bytes, const uint64_t* d_offsets,
 namespace {
 
 // Macro-cell min/max (cell c covers voxels c*kCell .. c*kCell + kCell on each
-// axis, clamped to the brick).  One warp per row of cells (cy, cz): per voxel
-// column the min/max over the (kCell + 1)^2 voxel rows the cells span
-// (coalesced row reads), then across kCell + 1 columns with a shuffle; each
-// lane owns kCell consecutive columns of a 32 * kCell-column chunk.
+// axis, clamped to the brick).  One warp per cell row ry of a brick, walking
+// the brick's z planes: per plane and voxel column the min/max over the
+// kCell + 1 voxel rows the row spans (coalesced reads), folded into the
+// running cell of the current z range; a cell is complete at its last plane,
+// which also opens the next cell.  Each plane is read once per cell row.
+// Lane l owns cells base + l + 32 t (t < kCellT): their kCell own columns,
+// the shared column from the next cell's owner by a shuffle.
+constexpr int kCellT = 3;
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
@@ -437,51 +477,99 @@ cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
                    uint32_t* __restrict__ cells) {
   const uint32_t b = blockIdx.y;
   const uint32_t n0 = sizes[3 * b], n1 = sizes[3 * b + 1], n2 = sizes[3 * b + 2];
-  const uint32_t cx = cells_per_axis(n0), cy = cells_per_axis(n1), cz = cells_per_axis(n2);
+  const uint32_t cx = cells_per_axis(n0), cy = cells_per_axis(n1);
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t row = blockIdx.x * (kThreads / 32) + warp;  // cell row index
-  if (row >= cy * cz) return;  // whole warp
-  const uint32_t ry = row % cy, rz = row / cy;
+  const uint32_t ry = blockIdx.x * (kThreads / 32) + warp;  // cell row
+  if (ry >= cy) return;  // whole warp
   const T* const p = pool + offsets[b];
   const uint32_t y0 = ry << kCellShift, y1 = min(y0 + kCell, n1 - 1);
-  const uint32_t z0 = rz << kCellShift, z1 = min(z0 + kCell, n2 - 1);
-  uint32_t* const out = cells + cell_off[b] + uint64_t(rz * cy + ry) * cx;
-  for (uint32_t xb = 0; xb < n0; xb += 32u * kCell) {
-    // columns xb + lane * kCell + [0, kCell) of this lane, and the next lane's
-    // first column (lane 31: the chunk's next column)
-    uint32_t lo[kCell], hi[kCell];
+  uint32_t* const out = cells + cell_off[b] + uint64_t(ry) * cx;
+  const uint64_t cell_plane = uint64_t(cy) * cx;  // cells per z layer of cells
+  for (uint32_t cb = 0; cb < cx; cb += 32u * kCellT) {
+    // accumulators of the open cell (per owned column, and lane 31's column
+    // after its last cell)
+    uint32_t lo[kCellT][kCell], hi[kCellT][kCell];
     uint32_t elo = 0xffffffffu, ehi = 0u;
 #pragma unroll
-    for (int q = 0; q < kCell; ++q) { lo[q] = 0xffffffffu; hi[q] = 0u; }
-    const uint32_t x_first = xb + lane * kCell;
-    const uint32_t x_extra = xb + 32u * kCell;
-    for (uint32_t z = z0; z <= z1; ++z)
+    for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+      for (int q = 0; q < kCell; ++q) { lo[t][q] = 0xffffffffu; hi[t][q] = 0u; }
+    const uint32_t x_extra = (cb + 32u * kCellT) << kCellShift;
+    // writes cell layer rz of this row from the open cell's accumulators
+    auto emit = [&](uint32_t rz) {
+#pragma unroll
+      for (int t = 0; t < kCellT; ++t) {
+        // the column shared with the next cell is its owner's first column:
+        // the next lane's, for lane 31 lane 0's next cell (or its own extra)
+        const int tn = t + 1 < kCellT ? t + 1 : t;
+        uint32_t nlo = __shfl_down_sync(0xffffffffu, lo[t][0], 1);
+        uint32_t nhi = __shfl_down_sync(0xffffffffu, hi[t][0], 1);
+        const uint32_t wlo = __shfl_sync(0xffffffffu, lo[tn][0], 0);
+        const uint32_t whi = __shfl_sync(0xffffffffu, hi[tn][0], 0);
+        if (lane == 31) {
+          nlo = t + 1 < kCellT ? wlo : elo;
+          nhi = t + 1 < kCellT ? whi : ehi;
+        }
+        const uint32_t c = cb + lane + 32u * t;
+        if (c < cx) {
+          uint32_t a = nlo, h = nhi;
+#pragma unroll
+          for (int q = 0; q < kCell; ++q) { a = min(a, lo[t][q]); h = max(h, hi[t][q]); }
+          out[uint64_t(rz) * cell_plane + c] = a | (h << 16);
+        }
+      }
+    };
+    for (uint32_t z = 0; z < n2; ++z) {
+      // this plane's column min/max over rows y0..y1
+      uint32_t plo[kCellT][kCell], phi[kCellT][kCell];
+      uint32_t pelo = 0xffffffffu, pehi = 0u;
+#pragma unroll
+      for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+        for (int q = 0; q < kCell; ++q) { plo[t][q] = 0xffffffffu; phi[t][q] = 0u; }
       for (uint32_t y = y0; y <= y1; ++y) {
         const T* const line = p + (uint64_t(z) * n1 + y) * n0;
 #pragma unroll
-        for (int q = 0; q < kCell; ++q) {
-          const uint32_t x = x_first + q;
-          if (x < n0) {
-            const uint32_t v = __ldg(line + x);
-            lo[q] = min(lo[q], v);
-            hi[q] = max(hi[q], v);
+        for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+          for (int q = 0; q < kCell; ++q) {
+            const uint32_t x = ((cb + lane + 32u * t) << kCellShift) + q;
+            if (x < n0) {
+              const uint32_t v = __ldg(line + x);
+              plo[t][q] = min(plo[t][q], v);
+              phi[t][q] = max(phi[t][q], v);
+            }
           }
-        }
         if (lane == 31 && x_extra < n0) {
           const uint32_t v = __ldg(line + x_extra);
-          elo = min(elo, v);
-          ehi = max(ehi, v);
+          pelo = min(pelo, v);
+          pehi = max(pehi, v);
         }
       }
-    uint32_t nlo = __shfl_down_sync(0xffffffffu, lo[0], 1);
-    uint32_t nhi = __shfl_down_sync(0xffffffffu, hi[0], 1);
-    if (lane == 31) { nlo = elo; nhi = ehi; }
-    const uint32_t c = x_first >> kCellShift;  // this lane's cell
-    if (x_first < n0 && c < cx) {
-      uint32_t a = nlo, h = nhi;
+      // fold the plane into the open cell
 #pragma unroll
-      for (int q = 0; q < kCell; ++q) { a = min(a, lo[q]); h = max(h, hi[q]); }
-      out[c] = a | (h << 16);
+      for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+        for (int q = 0; q < kCell; ++q) {
+          lo[t][q] = min(lo[t][q], plo[t][q]);
+          hi[t][q] = max(hi[t][q], phi[t][q]);
+        }
+      elo = min(elo, pelo);
+      ehi = max(ehi, pehi);
+      // plane z closes cell layer z / kCell - 1 when it is a multiple of
+      // kCell (and then opens layer z / kCell with its own values); the last
+      // plane closes the layer it lies in
+      const bool on_edge = z > 0 && (z & (kCell - 1)) == 0;
+      if (on_edge) {
+        emit((z >> kCellShift) - 1);
+#pragma unroll
+        for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+          for (int q = 0; q < kCell; ++q) { lo[t][q] = plo[t][q]; hi[t][q] = phi[t][q]; }
+        elo = pelo;
+        ehi = pehi;
+      }
+      if (z == n2 - 1) emit(z >> kCellShift);
     }
   }
 }
@@ -533,7 +621,7 @@ void launch_brick_sweep(const void* pool, int bytes, const uint64_t* d_offsets,
                         uint32_t shift, uint32_t* bhist, unsigned long long* brick_qmax,
                         cudaStream_t s, uint64_t* launches) {
   if (max_bz <= 2 * ov) return;  // no inner voxels
-  const uint32_t z_chunk = 4;
+  const uint32_t z_chunk = 16;
   const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
   if (bytes == 1)
     brick_sweep_kernel<uint8_t><<<grid, kThreads, 0, s>>>(

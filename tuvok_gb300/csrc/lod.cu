@@ -139,13 +139,44 @@ downsample_kernel(T* __restrict__ pool, const uint64_t* __restrict__ offsets, Lo
     int pair[3];  // 1: two samples along the axis, 0: the odd boundary sample
     const bool row_covered = axis(1, j, child[1], l[1], cs[1], pair[1]) &&
                              axis(2, k, child[2], l[2], cs[2], pair[2]);
+    // the x axis per row: the two children this row's voxels fall in (the
+    // first and second half of the core), their x extents and pair limits
+    const uint32_t split0 = (B[0] - 2 * ov + 1) / 2;
+    uint32_t cs_a = 0, cs_b = 0, even_a = 0, even_b = 0;
+    const T* src_a = nullptr;
+    const T* src_b = nullptr;
+    if (row_covered) {
+      const uint64_t yz = lo.first + child[1] * lo.cnt[0] + child[2] * lo.cnt[0] * lo.cnt[1];
+      const uint32_t ch = 2 * c[0];
+      if (ch < lo.cnt[0]) {
+        cs_a = brick_extent(lo, B, ov, 0, ch);
+        even_a = (cs_a - 2 * ov) / 2;
+        src_a = pool + offsets[yz + ch];
+      }
+      if (ch + 1 < lo.cnt[0]) {
+        cs_b = brick_extent(lo, B, ov, 0, ch + 1);
+        even_b = (cs_b - 2 * ov) / 2;
+        src_b = pool + offsets[yz + ch + 1];
+      }
+    }
    for (uint32_t i = lane; i < n[0]; i += 32) {
     const uint32_t r = r0 + i;
     T out{};
-    const bool covered = row_covered && axis(0, i, child[0], l[0], cs[0], pair[0]);
+    bool covered = row_covered && i >= ov && i < n[0] - ov;
+    const T* src = nullptr;
+    if (covered) {  // axis(0, i, ...) from the row's two children
+      const uint32_t tt = i - ov;
+      const bool second = tt >= split0;
+      src = second ? src_b : src_a;
+      l[0] = second ? tt - split0 : tt;
+      cs[0] = second ? cs_b : cs_a;
+      const uint32_t even = second ? even_b : even_a;
+      if (!src) covered = false;
+      else if (l[0] < even) pair[0] = 1;
+      else if (l[0] == even && (cs[0] & 1u)) pair[0] = 0;
+      else covered = false;
+    }
     if (covered) {
-      const T* src = pool + offsets[lo.first + child[0] + child[1] * lo.cnt[0] +
-                                    child[2] * lo.cnt[0] * lo.cnt[1]];
       const uint32_t X = 2 * l[0] + ov, Y = 2 * l[1] + ov, Z = 2 * l[2] + ov;
       auto S = [&](uint32_t x, uint32_t y, uint32_t z) -> T {
         return src[x + (uint64_t(y) + uint64_t(z) * cs[1]) * cs[0]];

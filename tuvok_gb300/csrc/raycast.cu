@@ -41,6 +41,18 @@
 #define TVK_DEFER_SAMPLE 0
 #endif
 
+// 1: count leap iterations, the steps they skip, candidate-brick slab tests
+// and brick marches into the frame's counters [4..7] (one global atomic per
+// event: a profiling build, not for timing).
+#ifndef TVK_PROFILE_COUNTS
+#define TVK_PROFILE_COUNTS 0
+#endif
+#if TVK_PROFILE_COUNTS
+#define TVK_PROF(P, i, n) atomicAdd(&(P).counters[i], (unsigned long long)(n))
+#else
+#define TVK_PROF(P, i, n) ((void)0)
+#endif
+
 namespace tvk {
 namespace {
 
@@ -125,6 +137,11 @@ struct ColorView {
     const float u0 = fminf(fmaxf(fmaf(tx, fn0, -0.5f), 0.0f), float(n0 - 1));
     const float u1 = fminf(fmaxf(fmaf(ty, fn1, -0.5f), 0.0f), float(n1 - 1));
     const float u2 = fminf(fmaxf(fmaf(tz, fn2, -0.5f), 0.0f), float(n2 - 1));
+    return sample_u<kMask>(u0, u1, u2);
+  }
+  // the same from voxel coordinates already clamped to [0, n-1]
+  template <int kMask>
+  __device__ __forceinline__ float4 sample_u(float u0, float u1, float u2) const {
     const int x0 = int(u0), y0 = int(u1), z0 = int(u2);
     const float fx = u0 - float(x0), fy = u1 - float(y0), fz = u2 - float(z0);
     const int x1 = min(x0 + 1, n0 - 1), y1 = min(y0 + 1, n1 - 1), z1 = min(z0 + 1, n2 - 1);
@@ -455,6 +472,8 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
           k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
         }
         samples += uint32_t(k + 1);
+        TVK_PROF(P, 4, 1);
+        TVK_PROF(P, 5, k + 1);
         for (int j = 0; j <= k; ++j) {
 #pragma unroll
           for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
@@ -606,6 +625,8 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
         k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
       }
       samples += uint32_t(k + 1);
+      TVK_PROF(P, 4, 1);
+      TVK_PROF(P, 5, k + 1);
       for (int j = 0; j <= k; ++j) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
@@ -1224,6 +1245,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
       for (uint32_t c = 0; c < nc; ++c) {
         if (frame[r].w >= P.frame_ert) break;
         const DevBrick& bg = P.bricks[base + sh.cand[c]];
+        TVK_PROF(P, 6, 1);
         float tn = -INFINITY, tf = INFINITY;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -1291,6 +1313,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           col = march_brick_color(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
         else
           col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
+        TVK_PROF(P, 7, 1);
         const float w = 1.0f - frame[r].w;
         frame[r].x = fmaf(col.x, w, frame[r].x);
         frame[r].y = fmaf(col.y, w, frame[r].y);
@@ -1658,8 +1681,150 @@ __device__ __forceinline__ uint32_t brick_info(const LeaperParams& L, const floa
 #define TVK_LEAPER_MIN_BLOCKS 4
 #endif
 
+// samplePool of a pool texel (raw units): the scalar, or a colour pool's red
+// channel (GLVolumePool.cpp:637-639 texture(volumePool, coords).r)
+template <class V>
+__device__ __forceinline__ float pool_scalar(const V& v, float u0, float u1, float u2) {
+  return v.sample_u(u0, u1, u2);
+}
+template <>
+__device__ __forceinline__ float pool_scalar<ColorView>(const ColorView& v, float u0, float u1,
+                                                        float u2) {
+  return v.sample_u<1>(u0, u1, u2).x;
+}
+
+// One step of a colour pool at local texel position pc (raw channels * 1/255).
+// Blend modes (GLGridLeaper-Method-1D-color / -1D-L-color / -2D-color /
+// -2D-L-color.glsl): the filtered RGBA keeps its colour, its alpha becomes
+// the TF's alpha at data.a * fTransScale (2D: at the alpha gradient's
+// magnitude), opacity-corrected by the host table; lighting takes the data's
+// colour as the diffuse colour, the normal from the red channel's gradient
+// (1D, ComputeNormal) or domain scale * the alpha gradient / |gradient| (2D).
+// Under compositing into acc; returns true when the ray is saturated.
+// Iso (GLGridLeaper-Method-iso-color.glsl, GLGridLeaper-iso.glsl:160-172):
+// hit at data.a >= fIsoval, 5 bisections on alpha, the normal from the red
+// channel (ComputeAlphaNormal calls ComputeGradient), the colour of the
+// unrefined sample packed as red + 1 and floor(green * 512) + blue, composed
+// by Compose-Color-FS into hit_col; returns true on a hit.
+template <bool kIso>
+__device__ __forceinline__ bool leaper_color_step(const LeaperParams& L, const ColorView& vol,
+                                                  const float pc[3], const float sv[3],
+                                                  const float tr[3], const float sc[3], bool lit,
+                                                  bool two_d, float W, float H, float4& acc,
+                                                  float4& hit_col) {
+  const RenderParams& P = L.R;
+  const float im = P.inv_max_raw;
+  auto at = [&](float l0, float l1, float l2, float& u0, float& u1, float& u2) {
+    u0 = fminf(fmaxf(l0 - 0.5f, 0.0f), vol.fn0 - 1.0f);
+    u1 = fminf(fmaxf(l1 - 0.5f, 0.0f), vol.fn1 - 1.0f);
+    u2 = fminf(fmaxf(l2 - 0.5f, 0.0f), vol.fn2 - 1.0f);
+  };
+  auto red = [&](float l0, float l1, float l2) -> float {
+    float u0, u1, u2;
+    at(l0, l1, l2, u0, u1, u2);
+    return vol.sample_u<1>(u0, u1, u2).x * im;
+  };
+  auto alpha = [&](float l0, float l1, float l2) -> float {
+    float u0, u1, u2;
+    at(l0, l1, l2, u0, u1, u2);
+    return vol.sample_u<8>(u0, u1, u2).w * im;
+  };
+  float u0, u1, u2;
+  at(pc[0], pc[1], pc[2], u0, u1, u2);
+  const float4 raw = vol.sample_u<15>(u0, u1, u2);
+  const float4 c = make_float4(raw.x * im, raw.y * im, raw.z * im, raw.w * im);
+  if (kIso) {
+    if (!(c.w >= P.iso_norm)) return false;
+    float r[3] = {sv[0] / 2.0f, sv[1] / 2.0f, sv[2] / 2.0f};
+    float q[3] = {pc[0] - r[0], pc[1] - r[1], pc[2] - r[2]};
+    for (int k = 0; k < 5; ++k) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) r[a] = r[a] / 2.0f;
+      const float vv = alpha(q[0], q[1], q[2]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) q[a] = vv >= P.iso_norm ? q[a] - r[a] : q[a] + r[a];
+    }
+    float g[3], hp[3];
+    g[0] = ((red(q[0] - 1.0f, q[1], q[2]) - red(q[0] + 1.0f, q[1], q[2])) / 2.0f) * P.domain_scale[0];
+    g[1] = ((red(q[0], q[1] - 1.0f, q[2]) - red(q[0], q[1] + 1.0f, q[2])) / 2.0f) * P.domain_scale[1];
+    g[2] = ((red(q[0], q[1], q[2] - 1.0f) - red(q[0], q[1], q[2] + 1.0f)) / 2.0f) * P.domain_scale[2];
+    const float gl = len3(g[0], g[1], g[2]);
+    if (gl > 0.0f) { g[0] = g[0] / gl; g[1] = g[1] / gl; g[2] = g[2] / gl; }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) hp[a] = (q[a] - tr[a]) / sc[a];
+    IsoHit h;
+#pragma unroll
+    for (int r2 = 0; r2 < 3; ++r2) {
+      h.pos[r2] = affine_row(L.norm2eye[r2], hp[0], hp[1], hp[2]);
+      h.n[r2] = fmaf(L.norm_to_eye_n[r2][2], g[2],
+                     fmaf(L.norm_to_eye_n[r2][1], g[1], L.norm_to_eye_n[r2][0] * g[0]));
+    }
+    h.f = 1.0f;
+    h.depth = 0.0f;
+    h.enc_r = c.x + 1.0f;
+    h.enc_gb = floorf(c.y * 512.0f) + c.z;
+    hit_col = iso_compose_color(P, h);
+    return true;
+  } else {
+    const float u = c.w * P.trans_scale;
+    float fx = floorf(u * W);
+    fx = fminf(fmaxf(fx, 0.0f), W - 1.0f);
+    float a = 0.0f, g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, mag = 0.0f;
+    if (two_d) {
+      if (P.tf_col_nonzero[int(fx)] != 0) {
+        // GLGridLeaper-GradientTools.glsl ComputeGradientAlpha (Yp at -delta.y)
+        g0 = (alpha(pc[0] - 1.0f, pc[1], pc[2]) - alpha(pc[0] + 1.0f, pc[1], pc[2])) / 2.0f;
+        g1 = (alpha(pc[0], pc[1] - 1.0f, pc[2]) - alpha(pc[0], pc[1] + 1.0f, pc[2])) / 2.0f;
+        g2 = (alpha(pc[0], pc[1], pc[2] - 1.0f) - alpha(pc[0], pc[1], pc[2] + 1.0f)) / 2.0f;
+        mag = len3(g0, g1, g2);
+        const float w = 1.0f - mag * P.grad_scale;
+        float fy = floorf(w * H);
+        fy = fminf(fmaxf(fy, 0.0f), H - 1.0f);
+        a = __ldg(&P.tf[int(fy) * P.tf_w + int(fx)].w);
+      }
+    } else {
+      a = __ldg(&P.tf[int(fx)].w);
+    }
+    float4 src = make_float4(c.x, c.y, c.z, a);
+    if (lit && a != 0.0f) {
+      float N[3];
+      if (two_d) {
+        const float q0 = mag > 0.0f ? g0 / mag : g0, q1 = mag > 0.0f ? g1 / mag : g1,
+                    q2 = mag > 0.0f ? g2 / mag : g2;
+        N[0] = P.domain_scale[0] * q0; N[1] = P.domain_scale[1] * q1;
+        N[2] = P.domain_scale[2] * q2;
+      } else {
+        N[0] = ((red(pc[0] - 1.0f, pc[1], pc[2]) - red(pc[0] + 1.0f, pc[1], pc[2])) / 2.0f) *
+               P.domain_scale[0];
+        N[1] = ((red(pc[0], pc[1] - 1.0f, pc[2]) - red(pc[0], pc[1] + 1.0f, pc[2])) / 2.0f) *
+               P.domain_scale[1];
+        N[2] = ((red(pc[0], pc[1], pc[2] - 1.0f) - red(pc[0], pc[1], pc[2] + 1.0f)) / 2.0f) *
+               P.domain_scale[2];
+        const float l = len3(N[0], N[1], N[2]);
+        if (l > 0.0f) { N[0] = N[0] / l; N[1] = N[1] / l; N[2] = N[2] / l; }
+      }
+      float mp[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) mp[k] = (pc[k] - tr[k]) / sc[k];
+      const float tfc[3] = {c.x, c.y, c.z};
+      float lc[3];
+      lighting_eye(L, mp, N, tfc, lc);
+      src.x = lc[0]; src.y = lc[1]; src.z = lc[2];
+    }
+    const float w = 1.0f - acc.w;
+    acc.x = fmaf(src.x * w, src.w, acc.x);
+    acc.y = fmaf(src.y * w, src.w, acc.y);
+    acc.z = fmaf(src.z * w, src.w, acc.z);
+    acc.w = fmaf(src.w, w, acc.w);
+    return acc.w > 0.99f;
+  }
+}
+
 template <class T, bool kIso>
 __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(const LeaperParams L) {
+  // RGBA8 colour pool (GLGridLeaper-Method-*-color.glsl); no macro cells
+  constexpr bool kColor = std::is_same<T, uchar4>::value;
+  using View = typename std::conditional<kColor, ColorView, BrickView<T>>::type;
   const RenderParams& P = L.R;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t px = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -1796,7 +1961,7 @@ __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(cons
         const uint32_t gid = L.lod_offset[lod] + bc[0] + bc[1] * L.lod_lx[lod] +
                              bc[2] * L.lod_lxy[lod];
         const uint32_t dims = __ldg(&L.brick_dims[gid]);
-        BrickView<T> vol;
+        View vol;
         vol.p = static_cast<const T*>(L.slots) + size_t(info - kBiFlagCount) * L.slot_voxels;
         vol.n0 = int(dims & 1023u); vol.n1 = int((dims >> 10) & 1023u); vol.n2 = int(dims >> 20);
         vol.fn0 = float(vol.n0); vol.fn1 = float(vol.n1); vol.fn2 = float(vol.n2);
@@ -1817,12 +1982,13 @@ __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(cons
           const float u0 = fminf(fmaxf(l0 - 0.5f, 0.0f), vol.fn0 - 1.0f);
           const float u1 = fminf(fmaxf(l1 - 0.5f, 0.0f), vol.fn1 - 1.0f);
           const float u2 = fminf(fmaxf(l2 - 0.5f, 0.0f), vol.fn2 - 1.0f);
-          return vol.sample_u(u0, u1, u2) * im;
+          return pool_scalar(vol, u0, u1, u2) * im;
         };
         // macro cells of the brick (as in the brick-by-brick march): steps in
         // an empty cube add nothing and cannot hit, so they are leapt over,
         // the position keeping the chain of additions
-        const uint8_t* __restrict__ dist = L.cell_dist ? L.cell_dist + L.cell_off[gid] : nullptr;
+        const uint8_t* __restrict__ dist =
+            (!kColor && L.cell_dist) ? L.cell_dist + L.cell_off[gid] : nullptr;
         const int ncx = int(cells_per_axis(uint32_t(vol.n0))),
                   ncy = int(cells_per_axis(uint32_t(vol.n1))),
                   ncz = int(cells_per_axis(uint32_t(vol.n2)));
@@ -1865,6 +2031,16 @@ __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(cons
             }
           }
           ++samples;
+          if constexpr (kColor) {
+            if (leaper_color_step<kIso>(L, vol, pc, sv, tr, sc, lit, two_d, W, H, acc, hit_col)) {
+              hit = kIso;
+              done = true;
+              break;
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
+            continue;
+          }
           const float v = sample(pc[0], pc[1], pc[2]);
           if (kIso) {
             // GLGridLeaper-Method-iso.glsl: first sample >= fIsoval, 5 bisections
@@ -2074,7 +2250,10 @@ void launch_raycast_batch(const BatchLaunch& L, int variant, uint32_t* d_next_it
 void launch_leaper(const LeaperParams& p, cudaStream_t s, uint64_t* launches) {
   const dim3 grid((p.R.width + 15) / 16, (p.R.height + 7) / 8);
   const bool iso = p.R.mode == TVK_RM_ISOSURFACE;
-  if (p.R.bytes == 1) {
+  if (p.R.bytes == 4) {
+    if (iso) leaper_kernel<uchar4, true><<<grid, 128, 0, s>>>(p);
+    else leaper_kernel<uchar4, false><<<grid, 128, 0, s>>>(p);
+  } else if (p.R.bytes == 1) {
     if (iso) leaper_kernel<uint8_t, true><<<grid, 128, 0, s>>>(p);
     else leaper_kernel<uint8_t, false><<<grid, 128, 0, s>>>(p);
   } else {

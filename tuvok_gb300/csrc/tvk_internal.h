@@ -176,7 +176,7 @@ struct alignas(16) DevBrick {
 
 // Per-cell min/max of every LOD-0 brick (volume creation); packed min | max << 16.
 // macro-cell min/max of every listed brick; max_cell_rows = the largest
-// (cells along y) x (cells along z) of a brick
+// number of cells along y of a brick
 void launch_cell_minmax(const void* pool, int bytes, const uint64_t* d_offsets,
                         const uint32_t* d_sizes, const uint64_t* d_cell_offsets,
                         uint64_t n_bricks, uint32_t max_cell_rows, uint32_t* cells,

@@ -150,6 +150,16 @@ class Volume:
         check(lib().tvk_volume_get_minmax(self._h, ts, lod, idx, C.byref(mm)))
         return mm
 
+    def GetCellMinMax(self, index):
+        """Macro-cell (min, max) tables of brick `index` (TOC order), each
+        [cells z, cells y, cells x] (see tvk_volume_cell_minmax)."""
+        dims = (C.c_uint32 * 3)()
+        check(lib().tvk_volume_cell_minmax(self._h, index, None, 0, dims))
+        out = np.zeros((dims[2], dims[1], dims[0]), dtype=np.uint32)
+        check(lib().tvk_volume_cell_minmax(self._h, index, out.ctypes.data_as(N._u32p),
+                                           out.size, dims))
+        return out & 0xFFFF, out >> 16
+
     def GetHistogram(self):
         bins = 1 << (8 * (1 if self.info.dtype == N.TVK_U8 else 2))
         out = np.zeros(bins, dtype=np.uint64)
@@ -506,6 +516,12 @@ class Renderer:
         s = N.Stats()
         check(lib().tvk_get_stats(self._h, C.byref(s)))
         return s
+
+    def GetCounters(self):
+        """The last paint's raw counters (see tvk_get_counters)."""
+        out = (C.c_uint64 * 8)()
+        check(lib().tvk_get_counters(self._h, out))
+        return list(out)
 
     def GetStream(self):
         s = C.c_void_p()
