@@ -63,6 +63,8 @@ def parse():
                    help="run one secondary measurement alone (profiling cases)")
     p.add_argument("--no-ooc", action="store_true",
                    help="skip the out-of-core GridLeaper fly-through")
+    p.add_argument("--no-hw-filter", action="store_true",
+                   help="skip the hardware-filtered (texture) variant of the march")
     p.add_argument("--ooc-dim", type=int, default=0,
                    help="edge of the out-of-core volume; 0: 4096 (the configuration's size) "
                         "when the GPU has 220 GB and the host 120 GB free, else 2048")
@@ -714,6 +716,41 @@ def frame_stats(r, poses, first, K):
     return float(np.mean(samples)), float(np.mean(shaded)), float(np.mean(graded))
 
 
+def run_hw_filter(torch, r, poses, args, exact0):
+    """The march with hardware-filtered lookups (texture objects, the texture
+    unit's trilinear filter) on the same poses: frames/s, and its distance to
+    the exact frame of pose 0 (which equals the FP32 oracle where checked)."""
+    if exact0 is None:
+        exact0 = frame0(r, poses)
+    t0 = time.perf_counter()
+    r.SetHardwareFiltering(True)
+    try:
+        eye, at, up = poses[0]
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+        r.Paint()  # makes the volume's textures (untimed)
+        setup_s = time.perf_counter() - t0
+        for i in range(args.warmup):
+            eye, at, up = poses[(args.warmup + i) % len(poses)]
+            r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
+            r.Paint()
+        K = args.steps
+        ms, step_ms = time_frames(torch, r, poses, args.warmup, K)
+        out = {"value": K / (ms / 1000.0), "unit": "frames/s", "ms_per_step": ms / K,
+               "kernel_ms_mean": float(np.mean(step_ms)), "texture_setup_s": setup_s,
+               "what": "the same poses with every brick read through a texture object "
+                       "(tvk_set_hardware_filtering): the texture unit's trilinear filter "
+                       "with its fixed-point weights instead of the exact lookups"}
+        img, cnt = frame0(r, poses)
+        d = np.abs(img.astype(np.float64) - exact0[0].astype(np.float64))
+        out["vs_exact_pose0"] = {"max_255": float(d.max() * 255),
+                                 "mean_255": float(d.mean() * 255),
+                                 "p99_255": float(np.percentile(d.max(axis=2), 99) * 255),
+                                 "counts_equal_fraction": float((cnt == exact0[1]).mean())}
+        return out
+    finally:
+        r.SetHardwareFiltering(False)
+
+
 def frame0(r, poses):
     eye, at, up = poses[0]
     r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye, at=at, up=up)
@@ -843,6 +880,10 @@ def run_ours(args):
         except Exception as e:  # noqa: BLE001
             return {"error": f"{type(e).__name__}: {e}"}
 
+    hw = None
+    if not args.no_hw_filter:
+        hw = guarded_leg(run_hw_filter, torch, r, poses, args, f0)
+
     learned = None
     if not args.no_learned:
         learned = guarded_leg(run_learned, args, torch, r, w, poses, value)
@@ -936,6 +977,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "plain_small": small,
+            "hw_filter": hw,
             "learned": learned,
             "batching": batching,
             "out_of_core": ooc,

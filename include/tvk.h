@@ -756,6 +756,17 @@ tvk_status tvk_get_stats(tvk_renderer* r, tvk_stats* out);
  * diagnostic with no counterpart in the reference. */
 tvk_status tvk_get_counters(tvk_renderer* r, uint64_t out[8]);
 
+/* Hardware-filtered lookups (on != 0): the ray march samples each brick
+ * through a texture object (a 3D CUDA array copy of every brick, made on the
+ * first such frame of the volume) with the texture unit's trilinear filter,
+ * instead of the exact eight-texel lookups.  The filter's fixed-point weights
+ * make frames differ slightly from the reference restatement; the exact path
+ * (the default) is the parity path.  Scalar volumes, 1D / 2D / iso modes;
+ * ClearView frames, colour volumes and batches refuse it; the GridLeaper
+ * ignores it.  The texture sampling GLSL does (Volume3D.glsl:39-41 texture3D)
+ * on the GPU's texture unit, with no separate reference entry point. */
+tvk_status tvk_set_hardware_filtering(tvk_renderer* r, int on);
+
 /* The macro-cell table of brick `index` (TOC order, any LOD): cells of 2^3
  * voxel positions, cell c covering voxels c*2 .. c*2 + 2 on each axis
  * (clamped to the brick), each entry min | max << 16 of the raw values there.

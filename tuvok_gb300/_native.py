@@ -7,9 +7,12 @@ raises, so nothing silently runs on the CPU.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libtvk.so"
+# TVK_LIBRARY selects another build of the same ABI (the counting diagnostic
+# build of tuvok_gb300.profile_counts); by default the in-tree libtvk.so
+LIB_PATH = Path(os.environ.get("TVK_LIBRARY") or Path(__file__).resolve().parent / "libtvk.so")
 
 TVK_OK = 0
 TVK_U8, TVK_U16, TVK_RGBA8 = 0, 1, 2
@@ -220,6 +223,7 @@ PROTOTYPES = {
     "tvk_get_stats": [_vp, C.POINTER(Stats)],
     "tvk_get_counters": [_vp, _u64p],
     "tvk_volume_cell_minmax": [_vp, C.c_uint64, _u32p, C.c_uint64, _u32p],
+    "tvk_set_hardware_filtering": [_vp, C.c_int],
     "tvk_generate_volume": [_vp, C.c_int, _u64p, _f32p, C.c_uint32, C.c_float, C.c_uint32,
                             C.c_float, C.c_uint64, C.c_int, C.c_float],
     "tvk_brick_lod0_noalloc": [_vp, C.c_int, _u64p, _u32p, C.c_uint32, C.c_int, _u64p,

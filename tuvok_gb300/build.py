@@ -89,6 +89,25 @@ def build_library(verbose: bool = False, ptxas_verbose: bool = False) -> Path:
     return LIB
 
 
+def build_counting_library(verbose: bool = False) -> Path:
+    """``_build/libtvk_counts.so``: the library with the ray march's event
+    counters compiled in (TVK_PROFILE_COUNTS=1: leap iterations, steps leapt,
+    candidate-brick slab tests, brick marches).  A diagnostic build; its atomics
+    slow the march, so it is never the one timed."""
+    build_library(verbose)
+    nvcc = _nvcc()
+    src = CSRC / "raycast.cu"
+    o = BUILD / "raycast_counts.cu.o"
+    out = BUILD / "libtvk_counts.so"
+    if _stale(o, [src, *HEADERS]):
+        _run([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", HOST_FLAGS,
+              *EXTRA["raycast.cu"], "-DTVK_PROFILE_COUNTS=1", "-c", src, "-o", o], verbose)
+    objs = [o if s == "raycast.cu" else BUILD / (s + ".o") for s in SOURCES]
+    if _stale(out, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", out, *objs, "-lcudart"], verbose)
+    return out
+
+
 def build_oracle(verbose: bool = False) -> Path:
     if _stale(ORACLE_LIB, [*ORACLE_SOURCES, *ORACLE_HEADERS]):
         cxx = shutil.which("g++") or "g++"

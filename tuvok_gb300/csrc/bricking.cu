@@ -61,28 +61,21 @@ __device__ __forceinline__ T source_voxel(const T* __restrict__ raw, const Brick
   return L < g.total ? raw[L] : T(0);
 }
 
-// One histogram increment per lane with `in` set, merged into a single
-// atomic when every such lane of the warp holds the same key (uniform regions,
-// e.g. the zero background, would otherwise serialise on one bin).  All 32
-// lanes must call it.  Keys below n_shared go to the CTA's shared bins, others
-// to the global 64-bit bins.
+// One histogram increment per lane with `in` set: a plain atomic per voxel.
+// Keys below n_shared go to the CTA's shared bins, others to the global
+// 64-bit bins.  Measured on the 1024^3 u16 volume's whole build (12.3 ms with
+// warp merging, 11.2 ms without): merging a warp's increments when all its
+// keys agree, merging every group of equal keys (__match_any_sync) or every
+// run of equal keys in consecutive lanes all cost more than the same-address
+// serialisation they save.
 __device__ __forceinline__ void hist_add_warp(uint32_t* __restrict__ sh,
                                               unsigned long long* __restrict__ gl,
                                               uint32_t n_shared, bool in, uint32_t key,
                                               uint32_t lane) {
-  const unsigned m = __ballot_sync(0xffffffffu, in);
-  if (m == 0u) return;
-  const int leader = __ffs(m) - 1;
-  const uint32_t k0 = __shfl_sync(0xffffffffu, key, leader);
-  if (__all_sync(0xffffffffu, !in || key == k0)) {
-    if (int(lane) == leader) {
-      if (k0 < n_shared) atomicAdd(&sh[k0], uint32_t(__popc(m)));
-      else atomicAdd(&gl[k0], (unsigned long long)__popc(m));
-    }
-  } else if (in) {
-    if (key < n_shared) atomicAdd(&sh[key], 1u);
-    else atomicAdd(&gl[key], 1ull);
-  }
+  (void)lane;
+  if (!in) return;
+  if (key < n_shared) atomicAdd(&sh[key], 1u);
+  else atomicAdd(&gl[key], 1ull);
 }
 
 // Source line of brick-local row (j, k): GetInputBrick's y and z terms
@@ -121,7 +114,7 @@ __device__ __forceinline__ bool source_row(const BrickGrid& g, const uint32_t c[
 // each CTA takes (brick, z-chunk) items in turn and merges its shared
 // histogram into the global one once, at the end.
 template <class T>
-__global__ void __launch_bounds__(kThreads, 6)
+__global__ void __launch_bounds__(kThreads, 5)
 brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __restrict__ offsets,
                   const uint32_t* __restrict__ sizes, T* __restrict__ pool, BrickScratch sc,
                   uint32_t smem_bins, uint32_t z_chunk, uint32_t chunks_per_brick,
@@ -150,6 +143,10 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
       const bool live = source_row(g, c, bs, j, k, rowbase);
       const bool inner_row = j >= ov && j < bs[1] - ov && k >= ov && k < bs[2] - ov;
       T* const out = brick + (uint64_t(k) * bs[1] + j) * bs[0];
+      // an interior brick column reads its whole row from one source line
+      // segment that ends inside the volume: no per-voxel clamping or limits
+      const uint64_t src0 = xbase + rowbase - ov;
+      const bool fast = live && !fx && !lx && src0 + bs[0] <= g.total;
       // kUnroll row segments of 32 voxels per pass: their loads are all in
       // flight before the first store
       for (uint32_t base = 0; base < bs[0]; base += 32 * kUnroll) {
@@ -158,7 +155,9 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
         for (uint32_t u = 0; u < kUnroll; ++u) {
           const uint32_t i = base + 32 * u + lane;
           v[u] = T(0);
-          if (i < bs[0] && live) {
+          if (fast) {
+            if (i < bs[0]) v[u] = __ldg(raw + src0 + i);
+          } else if (i < bs[0] && live) {
             uint32_t l = i;
             if (g.clamp) {
               if (fx && l < ov) l = ov;
@@ -203,10 +202,10 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
 // histogram of inner voxels (bin = value >> shift) and the largest squared
 // central-difference sum Q = dx^2 + dy^2 + dz^2 over inner voxels
 // (Histogram2DDataBlock::ComputeGradient, Histogram2DDataBlock.cpp:327-345, in
-// integers).  A warp owns 32 consecutive inner voxels of one row j and walks
-// them along z through the CTA's z-chunk: the z neighbours stay in registers
-// (one new load per voxel), the x neighbours come from the adjacent lanes (the
-// two end lanes load theirs), the y neighbours are two loads.
+// integers).  One warp per inner row of a brick z-chunk, each lane loading its
+// voxel's six neighbours (L1 serves the overlap).  (A z-walk that keeps the z
+// neighbours in registers and takes x from the adjacent lanes loads half as
+// much but measured slower: 3.5 against 3.1 ms on a 1024^3 u16 volume.)
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 brick_sweep_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
@@ -221,51 +220,34 @@ brick_sweep_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
   const uint32_t bs[3] = {sizes[3 * b + 0], sizes[3 * b + 1], sizes[3 * b + 2]};
   const T* const p = pool + offsets[b];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const uint32_t ix = bs[0] > 2 * ov ? bs[0] - 2 * ov : 0;
   const uint32_t iy = bs[1] > 2 * ov ? bs[1] - 2 * ov : 0;
   const uint32_t z0 = ov + blockIdx.y * z_chunk;
   const uint32_t z1 = bs[2] > ov ? min(bs[2] - ov, z0 + z_chunk) : 0;
   const uint32_t sx = bs[0], sxy = bs[0] * bs[1];
   const bool grad = ov > 0;  // central differences need a ghost layer on every side
   long long qmax = -1;
-  const uint32_t nseg = (ix + 31) / 32;
-  const uint32_t items = z1 > z0 ? iy * nseg : 0;
-  for (uint32_t item = warp; item < items; item += nwarps) {
-    const uint32_t j = ov + item / nseg;
-    const uint32_t i = ov + (item % nseg) * 32 + lane;
-    const bool act = i < bs[0] - ov;  // an inner voxel
-    const bool mem = i < bs[0];       // inside the brick row (feeds a neighbour's dx)
-    const T* const col = p + uint64_t(j) * sx + i;
-    uint32_t prev = 0, cur = 0;
-    if (mem) {
-      cur = col[uint64_t(z0) * sxy];
-      if (grad) prev = col[uint64_t(z0 - 1) * sxy];
-    }
-    for (uint32_t k = z0; k < z1; ++k) {
-      const uint64_t zo = uint64_t(k) * sxy;
-      uint32_t next = 0;
-      if (mem && grad) next = col[zo + sxy];
-      if (grad) {
-        uint32_t xm = __shfl_up_sync(0xffffffffu, cur, 1);
-        uint32_t xp = __shfl_down_sync(0xffffffffu, cur, 1);
-        if (act) {
-          if (lane == 0) xm = col[zo - 1];
-          if (lane == 31) xp = col[zo + 1];
-          const int dx = int(xm) - int(xp);
-          const int dy = int(col[zo - sx]) - int(col[zo + sx]);
-          const int dz = int(prev) - int(next);
+  const uint32_t rows = z1 > z0 ? (z1 - z0) * iy : 0;
+  for (uint32_t r = warp; r < rows; r += nwarps) {
+    const uint32_t k = z0 + r / iy;
+    const uint32_t j = ov + (r - (k - z0) * iy);
+    const T* const line = p + uint64_t(k) * sxy + uint64_t(j) * sx;
+    for (uint32_t base = ov; base < bs[0] - ov; base += 32) {
+      const uint32_t i = base + lane;
+      const bool act = i < bs[0] - ov;
+      uint32_t v = 0;
+      if (act) {
+        const T* const c = line + i;
+        v = c[0];
+        if (grad) {
+          const int dx = int(c[-1]) - int(c[1]);
+          const int dy = int(c[-int64_t(sx)]) - int(c[sx]);
+          const int dz = int(c[-int64_t(sxy)]) - int(c[sxy]);
           const long long q =
               (long long)dx * dx + (long long)dy * dy + (long long)dz * dz;
           qmax = q > qmax ? q : qmax;
         }
       }
-      hist_add_warp(bh, nullptr, 256u, act, min(cur >> shift, 255u), lane);
-      prev = cur;
-      if (grad) {
-        cur = next;
-      } else if (mem && k + 1 < z1) {
-        cur = col[zo + sxy];
-      }
+      hist_add_warp(bh, nullptr, 256u, act, min(v >> shift, 255u), lane);
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -470,6 +452,18 @@ namespace {
 // the shared column from the next cell's owner by a shuffle.
 constexpr int kCellT = 3;
 
+// Two consecutive voxels from a 2-voxel-aligned address, as one load.
+__device__ __forceinline__ void load_pair(const uint8_t* p, uint32_t& a, uint32_t& b) {
+  const uint32_t w = __ldg(reinterpret_cast<const unsigned short*>(p));
+  a = w & 0xffu;
+  b = w >> 8;
+}
+__device__ __forceinline__ void load_pair(const uint16_t* p, uint32_t& a, uint32_t& b) {
+  const uint32_t w = __ldg(reinterpret_cast<const unsigned int*>(p));
+  a = w & 0xffffu;
+  b = w >> 16;
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offsets,
@@ -485,6 +479,7 @@ cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
   const uint32_t y0 = ry << kCellShift, y1 = min(y0 + kCell, n1 - 1);
   uint32_t* const out = cells + cell_off[b] + uint64_t(ry) * cx;
   const uint64_t cell_plane = uint64_t(cy) * cx;  // cells per z layer of cells
+  const bool pairs = (n0 & 1u) == 0 && (offsets[b] & 1u) == 0;
   for (uint32_t cb = 0; cb < cx; cb += 32u * kCellT) {
     // accumulators of the open cell (per owned column, and lane 31's column
     // after its last cell)
@@ -519,34 +514,61 @@ cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
         }
       }
     };
-    for (uint32_t z = 0; z < n2; ++z) {
-      // this plane's column min/max over rows y0..y1
-      uint32_t plo[kCellT][kCell], phi[kCellT][kCell];
-      uint32_t pelo = 0xffffffffu, pehi = 0u;
+    // one plane's column min/max over rows y0..y1 (every row's loads issued
+    // together)
+    auto plane = [&](uint32_t z, uint32_t (&plo)[kCellT][kCell], uint32_t (&phi)[kCellT][kCell],
+                     uint32_t& pelo, uint32_t& pehi) {
+      pelo = 0xffffffffu;
+      pehi = 0u;
 #pragma unroll
       for (int t = 0; t < kCellT; ++t)
 #pragma unroll
         for (int q = 0; q < kCell; ++q) { plo[t][q] = 0xffffffffu; phi[t][q] = 0u; }
-      for (uint32_t y = y0; y <= y1; ++y) {
+#pragma unroll
+      for (uint32_t r = 0; r <= uint32_t(kCell); ++r) {
+        const uint32_t y = y0 + r;
+        if (y > y1) break;  // warp-uniform
         const T* const line = p + (uint64_t(z) * n1 + y) * n0;
+        if (kCell == 2 && pairs) {
+          // both own columns in one aligned load (even row length: every row
+          // and every even column start on a 2-voxel boundary)
 #pragma unroll
-        for (int t = 0; t < kCellT; ++t)
-#pragma unroll
-          for (int q = 0; q < kCell; ++q) {
-            const uint32_t x = ((cb + lane + 32u * t) << kCellShift) + q;
+          for (int t = 0; t < kCellT; ++t) {
+            const uint32_t x = (cb + lane + 32u * t) << kCellShift;
             if (x < n0) {
-              const uint32_t v = __ldg(line + x);
-              plo[t][q] = min(plo[t][q], v);
-              phi[t][q] = max(phi[t][q], v);
+              uint32_t v0, v1;
+              load_pair(line + x, v0, v1);
+              plo[t][0] = min(plo[t][0], v0);
+              phi[t][0] = max(phi[t][0], v0);
+              plo[t][1 % kCell] = min(plo[t][1 % kCell], v1);
+              phi[t][1 % kCell] = max(phi[t][1 % kCell], v1);
             }
           }
+        } else {
+#pragma unroll
+          for (int t = 0; t < kCellT; ++t)
+#pragma unroll
+            for (int q = 0; q < kCell; ++q) {
+              const uint32_t x = ((cb + lane + 32u * t) << kCellShift) + q;
+              if (x < n0) {
+                const uint32_t v = __ldg(line + x);
+                plo[t][q] = min(plo[t][q], v);
+                phi[t][q] = max(phi[t][q], v);
+              }
+            }
+        }
         if (lane == 31 && x_extra < n0) {
           const uint32_t v = __ldg(line + x_extra);
           pelo = min(pelo, v);
           pehi = max(pehi, v);
         }
       }
-      // fold the plane into the open cell
+    };
+    // folds plane z into the open cell; plane z closes cell layer z / kCell - 1
+    // when it is a multiple of kCell (and then opens layer z / kCell with its
+    // own values); the last plane closes the layer it lies in
+    auto fold = [&](uint32_t z, const uint32_t (&plo)[kCellT][kCell],
+                    const uint32_t (&phi)[kCellT][kCell], uint32_t pelo, uint32_t pehi) {
 #pragma unroll
       for (int t = 0; t < kCellT; ++t)
 #pragma unroll
@@ -556,11 +578,7 @@ cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
         }
       elo = min(elo, pelo);
       ehi = max(ehi, pehi);
-      // plane z closes cell layer z / kCell - 1 when it is a multiple of
-      // kCell (and then opens layer z / kCell with its own values); the last
-      // plane closes the layer it lies in
-      const bool on_edge = z > 0 && (z & (kCell - 1)) == 0;
-      if (on_edge) {
+      if (z > 0 && (z & (kCell - 1)) == 0) {
         emit((z >> kCellShift) - 1);
 #pragma unroll
         for (int t = 0; t < kCellT; ++t)
@@ -570,6 +588,14 @@ cell_minmax_kernel(const T* __restrict__ pool, const uint64_t* __restrict__ offs
         ehi = pehi;
       }
       if (z == n2 - 1) emit(z >> kCellShift);
+    };
+    // (two planes per step, the second plane's loads in flight with the
+    // first's, measured slower: 2.10 against 1.87 ms on the 1024^3 u16 volume)
+    for (uint32_t z = 0; z < n2; ++z) {
+      uint32_t plo[kCellT][kCell], phi[kCellT][kCell];
+      uint32_t pelo, pehi;
+      plane(z, plo, phi, pelo, pehi);
+      fold(z, plo, phi, pelo, pehi);
     }
   }
 }
@@ -602,8 +628,19 @@ void launch_brick_copy(const void* raw, int bytes, const BrickGrid& g, const uin
   if (items >= (1ull << 32)) fail(TVK_ERR_UNSUPPORTED, "too many bricks for one bricking pass");
   const uint32_t smem_bins = global_bins <= kSmemGlobalBins ? global_bins : kSmemGlobalBins;
   const size_t smem = size_t(smem_bins) * sizeof(uint32_t);
-  // 8 CTAs of 256 threads per SM when the shared bins allow it
-  const uint32_t grid = uint32_t(std::min<uint64_t>(items, 152ull * 8));
+  // persistent: one wave of as many CTAs as fit on every SM at once (items
+  // are dealt out round-robin, so a second partial wave would idle most SMs)
+  int dev = 0, sms = 0, per_sm = 0;
+  TVK_CUDA(cudaGetDevice(&dev));
+  TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (bytes == 1)
+    TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brick_copy_kernel<uint8_t>,
+                                                           kThreads, smem));
+  else
+    TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brick_copy_kernel<uint16_t>,
+                                                           kThreads, smem));
+  const uint32_t grid =
+      uint32_t(std::min<uint64_t>(items, uint64_t(std::max(1, sms)) * std::max(1, per_sm)));
   if (bytes == 1)
     brick_copy_kernel<uint8_t><<<grid, kThreads, smem, s>>>(
         static_cast<const uint8_t*>(raw), g, d_offsets, d_sizes, static_cast<uint8_t*>(pool), sc,
@@ -621,7 +658,7 @@ void launch_brick_sweep(const void* pool, int bytes, const uint64_t* d_offsets,
                         uint32_t shift, uint32_t* bhist, unsigned long long* brick_qmax,
                         cudaStream_t s, uint64_t* launches) {
   if (max_bz <= 2 * ov) return;  // no inner voxels
-  const uint32_t z_chunk = 16;
+  const uint32_t z_chunk = 4;
   const dim3 grid(uint32_t(n_bricks), (max_bz - 2 * ov + z_chunk - 1) / z_chunk);
   if (bytes == 1)
     brick_sweep_kernel<uint8_t><<<grid, kThreads, 0, s>>>(

@@ -18,6 +18,8 @@
 // power of two then truncating is the same shift).  FillOverlap: one CTA per
 // brick of the wavefront; each ghost voxel takes the source of the last copy
 // (in the reference's order) whose target region holds it.
+#include <algorithm>
+
 #include "tvk_internal.h"
 
 namespace tvk {
@@ -437,7 +439,11 @@ void build_lod_levels(void* pool, int bytes, const uint64_t* d_offsets, const ui
   for (size_t l = 1; l < lods.size(); ++l) {
     const LodGeom lo = geom(l - 1), hi = geom(l);
     const uint64_t nb = uint64_t(hi.cnt[0]) * hi.cnt[1] * hi.cnt[2];
-    const uint32_t z_chunk = 8;
+    // z planes per CTA: up to 8, fewer for the coarse levels (few bricks), so
+    // that a level still spreads over about 8 CTAs per SM (a CTA's warps walk
+    // their rows one after the other)
+    const uint32_t z_chunk =
+        uint32_t(std::min<uint64_t>(8, std::max<uint64_t>(1, nb * B[2] / (152ull * 8))));
     const dim3 grid(uint32_t(nb), (B[2] + z_chunk - 1) / z_chunk);
     if (bytes == 4)
       downsample_kernel<Rgba8><<<grid, kThreads, 0, s>>>(static_cast<Rgba8*>(pool), d_offsets,

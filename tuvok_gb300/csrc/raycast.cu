@@ -258,6 +258,63 @@ __device__ __forceinline__ float shifted_z(const BrickView<T>& B, const Foot& f,
   return fmaf(w, c1 - c0, c0);
 }
 
+// Hardware-filtered bricks (the measured alternative to the exact lookups): a
+// brick's copy in a 3D CUDA array read through a texture object with linear
+// filtering, clamp to edge and normalised reads, at unnormalised coordinates
+// u + 0.5 (texel i's centre is at i + 0.5), so a lookup at clamped voxel
+// coordinate u filters the same eight texels as the exact path, with the
+// texture unit's fixed-point weights; `scale` (255 or 65535) returns raw
+// units.  Not bit-exact: its distance to the oracle is measured and reported.
+struct TexView {
+  cudaTextureObject_t obj;
+  int n0, n1, n2;
+  float fn0, fn1, fn2;
+  float scale;
+  __device__ __forceinline__ float sample_u(float u0, float u1, float u2) const {
+    return tex3D<float>(obj, u0 + 0.5f, u1 + 0.5f, u2 + 0.5f) * scale;
+  }
+  __device__ __forceinline__ float sample_raw(float tx, float ty, float tz) const {
+    const float u0 = fminf(fmaxf(fmaf(tx, fn0, -0.5f), 0.0f), float(n0 - 1));
+    const float u1 = fminf(fmaxf(fmaf(ty, fn1, -0.5f), 0.0f), float(n1 - 1));
+    const float u2 = fminf(fmaxf(fmaf(tz, fn2, -0.5f), 0.0f), float(n2 - 1));
+    return sample_u(u0, u1, u2);
+  }
+};
+
+// The centre sample and the shifted lookups of the gradient for a texture
+// view: the footprint keeps only the centre's coordinates (in fx, fy, fz).
+__device__ __forceinline__ float centre_sample(const TexView& B, float u0, float u1, float u2,
+                                               Foot& f) {
+  f.fx = u0; f.fy = u1; f.fz = u2;
+  return B.sample_u(u0, u1, u2);
+}
+__device__ __forceinline__ float shifted_x(const TexView& B, const Foot& f, float u) {
+  return B.sample_u(u, f.fy, f.fz);
+}
+__device__ __forceinline__ float shifted_y(const TexView& B, const Foot& f, float u) {
+  return B.sample_u(f.fx, u, f.fz);
+}
+__device__ __forceinline__ float shifted_z(const TexView& B, const Foot& f, float u) {
+  return B.sample_u(f.fx, f.fy, u);
+}
+
+// The brick's view for the march: its pool voxels, or its texture.
+template <class V, class T>
+__device__ __forceinline__ V brick_view(const RenderParams& P, const DevBrick& b) {
+  V v;
+  if constexpr (std::is_same<V, TexView>::value) {
+    v.obj = P.tex[b.id];
+    v.scale = sizeof(T) == 1 ? 255.0f : 65535.0f;
+  } else {
+    v.p = static_cast<const T*>(P.pool) + b.off;
+    v.sx = b.n[0];
+    v.sxy = b.n[0] * b.n[1];
+  }
+  v.n0 = int(b.n[0]); v.n1 = int(b.n[1]); v.n2 = int(b.n[2]);
+  v.fn0 = float(b.n[0]); v.fn1 = float(b.n[1]); v.fn2 = float(b.n[2]);
+  return v;
+}
+
 __device__ __forceinline__ float clamp_u(float t, float fn, int n) {
   return fminf(fmaxf(fmaf(t, fn, -0.5f), 0.0f), float(n - 1));
 }
@@ -364,8 +421,9 @@ __device__ __forceinline__ void lighting_bp(const RenderParams& P, const float p
   }
 }
 
-// Marches one brick; returns the brick's premultiplied RGBA.
-template <class T>
+// Marches one brick; returns the brick's premultiplied RGBA.  kTex: lookups
+// through the brick's texture (TexView) instead of its pool voxels.
+template <class T, bool kTex = false>
 __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBrick& b,
                                               const float dir[3], float t_in, float t_out,
                                               uint32_t& samples, uint32_t& shaded,
@@ -405,11 +463,8 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   einc[1] = (dy * ilen) * b.step;
   einc[2] = (dz * ilen) * b.step;
 
-  BrickView<T> vol;
-  vol.p = static_cast<const T*>(P.pool) + b.off;
-  vol.n0 = int(b.n[0]); vol.n1 = int(b.n[1]); vol.n2 = int(b.n[2]);
-  vol.fn0 = float(b.n[0]); vol.fn1 = float(b.n[1]); vol.fn2 = float(b.n[2]);
-  vol.sx = b.n[0]; vol.sxy = b.n[0] * b.n[1];
+  using View = typename std::conditional<kTex, TexView, BrickView<T>>::type;
+  const View vol = brick_view<View, T>(P, b);
   const float vs0 = 1.0f / float(b.n[0]), vs1 = 1.0f / float(b.n[1]), vs2 = 1.0f / float(b.n[2]);
   const bool lit = P.lighting != 0;
   const bool two_d = P.mode == TVK_RM_2DTRANS;
@@ -474,12 +529,21 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
         samples += uint32_t(k + 1);
         TVK_PROF(P, 4, 1);
         TVK_PROF(P, 5, k + 1);
-        for (int j = 0; j <= k; ++j) {
+        // the chain of k + 1 additions, unrolled (the same sums in order)
+        if (lit) {
+#pragma unroll 4
+          for (int j = 0; j <= k; ++j) {
 #pragma unroll
-          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
-          if (lit) {
+            for (int a = 0; a < 3; ++a) {
+              pos[a] = pos[a] + inc[a];
+              epos[a] = epos[a] + einc[a];
+            }
+          }
+        } else {
+#pragma unroll 4
+          for (int j = 0; j <= k; ++j) {
 #pragma unroll
-            for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
+            for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
           }
         }
         i += k + 1;
@@ -627,12 +691,21 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       samples += uint32_t(k + 1);
       TVK_PROF(P, 4, 1);
       TVK_PROF(P, 5, k + 1);
-      for (int j = 0; j <= k; ++j) {
+      // the chain of k + 1 additions, unrolled (the same sums in order)
+      if (lit) {
+#pragma unroll 4
+        for (int j = 0; j <= k; ++j) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
-        if (lit) {
+          for (int a = 0; a < 3; ++a) {
+            pos[a] = pos[a] + inc[a];
+            epos[a] = epos[a] + einc[a];
+          }
+        }
+      } else {
+#pragma unroll 4
+        for (int j = 0; j <= k; ++j) {
 #pragma unroll
-          for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
+          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
         }
       }
       i += k + 1;
@@ -741,7 +814,7 @@ struct IsoHit {
 // count and the eye-space hit interpolation keep the whole brick's entry.  The
 // hit's depth (of the brick's exit) is not computed: along a ray the first
 // brick with a focus hit wins the depth test.
-template <class T, bool kCV = false>
+template <class T, bool kCV = false, bool kTex = false>
 __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick& b,
                                           const float dir[3], float t_in, float t_out,
                                           IsoHit& h, uint32_t& samples, uint32_t& shaded,
@@ -776,11 +849,8 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
     inc[a] = (tout[a] - tin[a]) * iq;
     pos[a] = tin[a];
   }
-  BrickView<T> vol;
-  vol.p = static_cast<const T*>(P.pool) + b.off;
-  vol.n0 = int(b.n[0]); vol.n1 = int(b.n[1]); vol.n2 = int(b.n[2]);
-  vol.fn0 = float(b.n[0]); vol.fn1 = float(b.n[1]); vol.fn2 = float(b.n[2]);
-  vol.sx = b.n[0]; vol.sxy = b.n[0] * b.n[1];
+  using View = typename std::conditional<kTex, TexView, BrickView<T>>::type;
+  const View vol = brick_view<View, T>(P, b);
   const float im = P.inv_max_raw;
   const float iso = kCV ? iso_cv : P.iso_norm;
   // cells whose maximum stays below the isovalue cannot produce a hit
@@ -821,6 +891,7 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
           k = m > 0.0f ? int(fminf(m, float(n - 1 - i))) : 0;
         }
         samples += uint32_t(k + 1);
+#pragma unroll 4
         for (int j = 0; j <= k; ++j) {
 #pragma unroll
           for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
@@ -1159,7 +1230,7 @@ struct TileShared {
 // (nearest refined hit + compose); otherwise the compositing modes (1D/2D TF,
 // lit or unlit).  Every pixel's value does not depend on kRPT.  kCV (with
 // kIso): ClearView, both surfaces' hits go to P.cv_hits for cv_compose.
-template <class T, bool kIso, int kRPT, bool kCV = false>
+template <class T, bool kIso, int kRPT, bool kCV = false, bool kTex = false>
 __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, uint32_t by,
                                             TileShared& sh) {
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1278,7 +1349,8 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           if (!kCV) {
             if (settled) break;
             IsoHit h;
-            if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
+            if (iso_brick<T, false, kTex>(P, b, dir, ti, tc, h, samples, shaded) &&
+                h.depth < best_depth[r]) {
               best[r] = h;
               best_depth[r] = h.depth;
               have_hit[r] = true;
@@ -1294,7 +1366,8 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
           bool here = false;
           if (!settled) {
             IsoHit h;
-            if (iso_brick<T>(P, b, dir, ti, tc, h, samples, shaded) && h.depth < best_depth[r]) {
+            if (iso_brick<T, false, kTex>(P, b, dir, ti, tc, h, samples, shaded) &&
+                h.depth < best_depth[r]) {
               best[r] = h;
               best_depth[r] = h.depth;
               have_hit[r] = true;
@@ -1312,7 +1385,7 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
         if constexpr (kColor)
           col = march_brick_color(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
         else
-          col = march_brick<T>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
+          col = march_brick<T, kTex>(P, b, dir, ti, tc, samples, shaded, graded, first_t[r]);
         TVK_PROF(P, 7, 1);
         const float w = 1.0f - frame[r].w;
         frame[r].x = fmaf(col.x, w, frame[r].x);
@@ -1379,10 +1452,10 @@ __device__ __forceinline__ void render_tile(const RenderParams& P, uint32_t bx, 
 #define TVK_RAYCAST_RPT 1
 #endif
 
-template <class T, bool kIso, bool kCV = false>
+template <class T, bool kIso, bool kCV = false, bool kTex = false>
 __global__ void __launch_bounds__(128, TVK_RAYCAST_MIN_BLOCKS) raycast_kernel(const RenderParams P) {
   __shared__ TileShared sh;
-  render_tile<T, kIso, TVK_RAYCAST_RPT, kCV>(P, blockIdx.x, blockIdx.y, sh);
+  render_tile<T, kIso, TVK_RAYCAST_RPT, kCV, kTex>(P, blockIdx.x, blockIdx.y, sh);
 }
 
 // Compose-CV-FS.glsl:49-108, one thread per pixel.  Neighbour normals are
@@ -2022,6 +2095,7 @@ __global__ void __launch_bounds__(128, TVK_LEAPER_MIN_BLOCKS) leaper_kernel(cons
                 k = m > 0.0f ? int(fminf(m, float(steps - 1 - i))) : 0;
               }
               samples += uint32_t(k + 1);
+#pragma unroll 4
               for (int j = 0; j <= k; ++j) {
 #pragma unroll
                 for (int a = 0; a < 3; ++a) pc[a] = pc[a] + sv[a];
@@ -2273,6 +2347,14 @@ void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches) {
   if (p.bytes == 4) {
     if (iso) raycast_kernel<uchar4, true><<<grid, block, 0, s>>>(p);
     else raycast_kernel<uchar4, false><<<grid, block, 0, s>>>(p);
+  } else if (p.tex) {  // hardware-filtered lookups (scalar, no ClearView)
+    if (p.bytes == 1) {
+      if (iso) raycast_kernel<uint8_t, true, false, true><<<grid, block, 0, s>>>(p);
+      else raycast_kernel<uint8_t, false, false, true><<<grid, block, 0, s>>>(p);
+    } else {
+      if (iso) raycast_kernel<uint16_t, true, false, true><<<grid, block, 0, s>>>(p);
+      else raycast_kernel<uint16_t, false, false, true><<<grid, block, 0, s>>>(p);
+    }
   } else if (p.bytes == 1) {
     if (cv) raycast_kernel<uint8_t, true, true><<<grid, block, 0, s>>>(p);
     else if (iso) raycast_kernel<uint8_t, true><<<grid, block, 0, s>>>(p);

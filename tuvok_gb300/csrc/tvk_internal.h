@@ -169,7 +169,7 @@ struct alignas(16) DevBrick {
   uint32_t cells;       // cells per axis, packed x | y << 10 | z << 20
   float tex[3][4];      // eye -> brick texture coordinates
   uint32_t n[3];        // voxels incl. ghost
-  uint32_t pad1;
+  uint32_t id;          // TOC index of the brick (its texture, when filtering in hardware)
   unsigned long long off;        // voxel offset of the brick in the pool
   unsigned long long cell_off;   // offset of the brick's first macro cell
 };
@@ -266,6 +266,9 @@ struct RenderParams {
   float4* cv_hits;
   float step_scale;          // fStepScale (colour volumes correct opacity per sample)
   unsigned long long* counters;  // [samples, shaded, errors, gradient samples]
+  // hardware-filtered lookups: the texture object of every brick (TOC order),
+  // null for the exact lookups from the pool
+  const cudaTextureObject_t* tex;
 };
 
 void launch_raycast(const RenderParams& p, cudaStream_t s, uint64_t* launches);
@@ -408,6 +411,11 @@ struct tvk_volume {
   bool rebricked = false;
   int mm_mode = 0;
   std::vector<uint64_t> src_index;      // source TOC index per brick
+  // hardware-filtered copies of every brick (3D CUDA arrays with texture
+  // objects), made on a renderer's first frame with hardware filtering on
+  mutable std::vector<cudaArray_t> tex_arrays;
+  mutable std::vector<cudaTextureObject_t> tex_objs;
+  mutable void* d_tex = nullptr;        // the texture objects, TOC order
 };
 
 struct tvk_renderer;

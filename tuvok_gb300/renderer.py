@@ -517,6 +517,11 @@ class Renderer:
         check(lib().tvk_get_stats(self._h, C.byref(s)))
         return s
 
+    def SetHardwareFiltering(self, on):
+        """Texture-unit trilinear lookups instead of the exact ones (see
+        tvk_set_hardware_filtering): faster, not bit-exact."""
+        check(lib().tvk_set_hardware_filtering(self._h, int(bool(on))))
+
     def GetCounters(self):
         """The last paint's raw counters (see tvk_get_counters)."""
         out = (C.c_uint64 * 8)()
