@@ -249,6 +249,8 @@ class Renderer {
   void SetRendermode(ERenderMode m) { check(tvk_set_render_mode(r_, tvk_render_mode(m))); }
   void SetUseLighting(bool on) { check(tvk_set_lighting(r_, on ? 1 : 0)); }
   void SetSampleRateModifier(float f) { check(tvk_set_sample_rate_modifier(r_, f)); }
+  // texture-unit trilinear lookups instead of the exact ones (faster, not bit-exact)
+  void SetHardwareFiltering(bool on) { check(tvk_set_hardware_filtering(r_, on ? 1 : 0)); }
   void SetIsoValue(float v) { check(tvk_set_isovalue(r_, v)); }
   void SetColors(const float ambient[4], const float diffuse[4], const float specular[4],
                  const float light_dir[3]) {
