@@ -49,8 +49,11 @@ typedef enum tvk_status {
  * mode (the voxel's colour times the TF entry at (r + g + b) / 3,
  * VRender1D-Color.glsl / VRender1DLit-Color.glsl) and iso mode (the alpha
  * channel's isosurface with its colour, GLRaycaster-Color-FS.glsl and
- * Compose-Color-FS.glsl); 2D mode, ClearView, batches, the GridLeaper pool,
- * rebricking and the histograms refuse them. */
+ * Compose-Color-FS.glsl).  A GridLeaper pool over a colour volume renders
+ * every mode of GLGridLeaper-Method-*-color.glsl (1D and 2D, lit or not, iso),
+ * with every brick's value range taken as [0, 255].  The brick-by-brick 2D
+ * mode, ClearView, batches, rebricking, hardware filtering and the histograms
+ * refuse them. */
 typedef enum tvk_dtype { TVK_U8 = 0, TVK_U16 = 1, TVK_RGBA8 = 2 } tvk_dtype;
 
 /* AbstrRenderer::ERenderMode (Renderer/AbstrRenderer.h:120-126) */
