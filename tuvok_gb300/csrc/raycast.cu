@@ -78,7 +78,8 @@ struct BrickView {
   uint32_t sx, sxy;
 
   __device__ __forceinline__ float fetch(int x, int y, int z) const {
-    return float(__ldg(p + (size_t(x) + size_t(y) * sx + size_t(z) * sxy)));
+    // 32-bit voxel offset: a brick holds fewer than 2^32 voxels (at most 1023 per axis)
+    return float(__ldg(p + (uint32_t(x) + uint32_t(y) * sx + uint32_t(z) * sxy)));
   }
   // texel-centre trilinear, clamp to edge, raw units
   __device__ __forceinline__ float sample_raw(float tx, float ty, float tz) const {
@@ -118,7 +119,7 @@ struct ColorView {
   uint32_t sx, sxy;
 
   __device__ __forceinline__ uchar4 fetch(int x, int y, int z) const {
-    return __ldg(p + (size_t(x) + size_t(y) * sx + size_t(z) * sxy));
+    return __ldg(p + (uint32_t(x) + uint32_t(y) * sx + uint32_t(z) * sxy));
   }
   __device__ __forceinline__ static float tri(float fx, float fy, float fz, float v000,
                                               float v100, float v010, float v110, float v001,
