@@ -316,8 +316,10 @@ __device__ __forceinline__ V brick_view(const RenderParams& P, const DevBrick& b
   return v;
 }
 
+// (fn - 1.0f is float(n - 1) exactly: n < 2^24)
 __device__ __forceinline__ float clamp_u(float t, float fn, int n) {
-  return fminf(fmaxf(fmaf(t, fn, -0.5f), 0.0f), float(n - 1));
+  (void)n;
+  return fminf(fmaxf(fmaf(t, fn, -0.5f), 0.0f), fn - 1.0f);
 }
 
 // x^y for x in [0, 1] as exp2(y * log2(x)) (GLSL defines pow as that
@@ -487,6 +489,7 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
   // samples, until at least half of the lanes still marching are pending.
   // Every lane's arithmetic is unchanged; only the interleaving differs.
   int i = 0;
+  int epend = 0;  // additions of einc owed to epos (made before its next use)
   bool pend = false;
   Foot foot;
   float4 src = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -501,9 +504,9 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
       const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
       const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
-      u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
-      u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
-      u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+      u0 = fminf(fmaxf(uu0, 0.0f), (vol.fn0 - 1.0f));
+      u1 = fminf(fmaxf(uu1, 0.0f), (vol.fn1 - 1.0f));
+      u2 = fminf(fmaxf(uu2, 0.0f), (vol.fn2 - 1.0f));
       int dd = 0;
       int cx = 0, cy = 0, cz = 0;
       if (dist) {
@@ -530,23 +533,14 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
         samples += uint32_t(k + 1);
         TVK_PROF(P, 4, 1);
         TVK_PROF(P, 5, k + 1);
-        // the chain of k + 1 additions, unrolled (the same sums in order)
-        if (lit) {
+        // the chain of k + 1 additions, unrolled (the same sums in order);
+        // the eye-space position's own chain waits for a lit sample (epend)
 #pragma unroll 4
-          for (int j = 0; j <= k; ++j) {
+        for (int j = 0; j <= k; ++j) {
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-              pos[a] = pos[a] + inc[a];
-              epos[a] = epos[a] + einc[a];
-            }
-          }
-        } else {
-#pragma unroll 4
-          for (int j = 0; j <= k; ++j) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
-          }
+          for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
         }
+        epend += k + 1;
         i += k + 1;
         leaped = true;
       } else {
@@ -621,6 +615,11 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
         }
         const float tfc[3] = {src.x, src.y, src.z};
         float lc[3];
+        // the eye-space position of this step: its pending additions, in order
+        for (; epend > 0; --epend) {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) epos[a] = epos[a] + einc[a];
+        }
         if (P.light_model == TVK_LIGHT_BLINN_PHONG)
           lighting_bp(P, epos, N, tfc, lc);
         else
@@ -640,10 +639,8 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       c.z = fmaf(src.z * w, src.w, c.z);
       c.w = fmaf(src.w, w, c.w);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        pos[a] = pos[a] + inc[a];
-        epos[a] = epos[a] + einc[a];
-      }
+      for (int a = 0; a < 3; ++a) pos[a] = pos[a] + inc[a];
+      ++epend;
       ++i;
       if (c.w >= 0.99f) break;
     }
@@ -665,9 +662,9 @@ __device__ __forceinline__ float4 march_brick(const RenderParams& P, const DevBr
       const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
       const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
       const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
-      u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
-      u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
-      u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+      u0 = fminf(fmaxf(uu0, 0.0f), (vol.fn0 - 1.0f));
+      u1 = fminf(fmaxf(uu1, 0.0f), (vol.fn1 - 1.0f));
+      u2 = fminf(fmaxf(uu2, 0.0f), (vol.fn2 - 1.0f));
       if (!dist) break;
       const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
                 cz = int(u2) >> kCellShift;
@@ -867,9 +864,9 @@ __device__ __forceinline__ bool iso_brick(const RenderParams& P, const DevBrick&
     const float uu0 = fmaf(pos[0], vol.fn0, -0.5f);
     const float uu1 = fmaf(pos[1], vol.fn1, -0.5f);
     const float uu2 = fmaf(pos[2], vol.fn2, -0.5f);
-    const float u0 = fminf(fmaxf(uu0, 0.0f), float(vol.n0 - 1));
-    const float u1 = fminf(fmaxf(uu1, 0.0f), float(vol.n1 - 1));
-    const float u2 = fminf(fmaxf(uu2, 0.0f), float(vol.n2 - 1));
+    const float u0 = fminf(fmaxf(uu0, 0.0f), (vol.fn0 - 1.0f));
+    const float u1 = fminf(fmaxf(uu1, 0.0f), (vol.fn1 - 1.0f));
+    const float u2 = fminf(fmaxf(uu2, 0.0f), (vol.fn2 - 1.0f));
     if (dist) {
       const int cx = int(u0) >> kCellShift, cy = int(u1) >> kCellShift,
                 cz = int(u2) >> kCellShift;
