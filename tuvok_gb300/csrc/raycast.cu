@@ -57,9 +57,10 @@ namespace tvk {
 namespace {
 
 // CTAs of 128 threads the register allocation must leave room for per SM
-// (occupancy against spills; measured on GB300: 5 beats 4, 6 and 8 by 2-10 %).
+// (occupancy against spills; measured on GB300 with the 1024^3 lit frames:
+// 6 CTAs 3.42 ms, 5 3.48, 7 3.46, 8 3.61, 4 3.86).
 #ifndef TVK_RAYCAST_MIN_BLOCKS
-#define TVK_RAYCAST_MIN_BLOCKS 5
+#define TVK_RAYCAST_MIN_BLOCKS 6
 #endif
 
 __device__ __forceinline__ float affine_row(const float r[4], float x, float y, float z) {
