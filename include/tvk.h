@@ -742,6 +742,17 @@ tvk_status tvk_get_render_size(tvk_renderer* r, uint32_t* width, uint32_t* heigh
 tvk_status tvk_get_image_device(tvk_renderer* r, const float** device_rgba, uint32_t* width,
                                 uint32_t* height);
 tvk_status tvk_read_image(tvk_renderer* r, float* host_rgba, size_t n_floats);
+
+/* The last frame's image copied to host memory asynchronously: the frame is
+ * copied once on the device (on the renderer's stream, after the frame), then
+ * to host_rgba on a copy stream of the renderer while later frames render.
+ * host_rgba must stay valid until tvk_wait_image returns (page-locked memory
+ * lets the copy overlap rendering).  Copies complete in the order they were
+ * asked for; a new one waits (on the device) for the previous one.  No
+ * counterpart in the reference, whose GLRenderer::ReadBackPixels blocks. */
+tvk_status tvk_read_image_async(tvk_renderer* r, float* host_rgba, size_t n_floats);
+/* Blocks until every asynchronous image copy asked for so far is complete. */
+tvk_status tvk_wait_image(tvk_renderer* r);
 /* Per-pixel executed sample counts of the last paint (u32 per pixel of the
  * ray-marched image, tvk_get_render_size). */
 tvk_status tvk_read_sample_counts(tvk_renderer* r, uint32_t* host_counts, size_t n);

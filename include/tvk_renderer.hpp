@@ -275,6 +275,12 @@ class Renderer {
     check(tvk_read_image(r_, img.data(), img.size()));
     return img;
   }
+  // copies the last frame into rgba (w x h x 4 floats, valid until WaitImage)
+  // while later frames render
+  void ReadBackPixelsAsync(float* rgba, size_t n_floats) {
+    check(tvk_read_image_async(r_, rgba, n_floats));
+  }
+  void WaitImage() { check(tvk_wait_image(r_)); }
   tvk_stats Stats() {
     tvk_stats s;
     check(tvk_get_stats(r_, &s));

@@ -210,3 +210,27 @@ def test_gpu_fp64_distance_reported(cuda_ok, scenes):
     d = np.abs(img.astype(np.float64) - ref64)
     print(f"\nFP32 GPU vs FP64 oracle: max {d.max() * 255:.4f}/255 mean {d.mean() * 255:.5f}/255")
     assert d.max() <= MAX_TOL and d.mean() <= MEAN_TOL
+
+
+def test_gpu_async_readback_matches_sync(cuda_ok):
+    """tvk_read_image_async: each of several frames, copied to the host while
+    the next one renders, equals the same frame read back synchronously."""
+    raw = numpy_blob_volume((44, 50, 38), np.uint16, 7, (3, 9), (900, 4000), 4095, seed=5, noise=20)
+    vol = Volume(raw, brick_size=(18, 18, 18), overlap=1)
+    r = Renderer()
+    r.RegisterDataset(vol)
+    r.Set1DTransFloat(ramp_tf(1024))
+    r.SetUseLighting(True)
+    r.Resize(64, 48)
+    eyes = [(0.3, 0.4, 1.5), (-1.1, 0.2, -0.7), (0.9, -0.6, 1.2), (0.2, 1.3, 0.6)]
+    bufs = [np.zeros((48, 64, 4), np.float32) for _ in eyes]
+    for eye, b in zip(eyes, bufs):
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+        r.Paint()
+        r.ReadBackPixelsAsync(b)
+    r.WaitImage()
+    for eye, b in zip(eyes, bufs):
+        r.SetViewParameters(50.0, 0.01, 1000.0, eye=eye)
+        r.Paint()
+        np.testing.assert_array_equal(b, r.ReadBackPixels())
+    assert all(np.abs(b).sum() > 0 for b in bufs)

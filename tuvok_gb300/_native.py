@@ -218,6 +218,8 @@ PROTOTYPES = {
     "tvk_leaper_paint": [_vp, _vp, C.c_uint32, C.POINTER(LeaperInfo)],
     "tvk_get_image_device": [_vp, C.POINTER(_vp), _u32p, _u32p],
     "tvk_read_image": [_vp, _f32p, C.c_size_t],
+    "tvk_read_image_async": [_vp, _f32p, C.c_size_t],
+    "tvk_wait_image": [_vp],
     "tvk_read_sample_counts": [_vp, _u32p, C.c_size_t],
     "tvk_renderer_get_stream": [_vp, C.POINTER(_vp)],
     "tvk_get_stats": [_vp, C.POINTER(Stats)],

@@ -663,6 +663,11 @@ struct tvk_renderer {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr, ev_staged = nullptr;
   cudaEvent_t ev_ready = nullptr;  // a planned frame's uploads are queued (batch paints)
+  // asynchronous image readback: the frame is copied to d_img_ro on the render
+  // stream, then to the host on copy_stream while the next frame renders
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_img_ready = nullptr, ev_img_copied = nullptr;
+  bool img_pending = false;
   const tvk_volume* vol = nullptr;
   // transfer function (effective RGBA as the GPU samples it)
   std::vector<float> tf;
@@ -686,6 +691,7 @@ struct tvk_renderer {
   uint32_t width = 0, height = 0;
   // device buffers
   tvk::DevBuf d_img, d_spp, d_bricks, d_counters;
+  tvk::DevBuf d_img_ro;  // the image being read back asynchronously
   tvk::PinnedBuf h_bricks, h_counters;
   tvk::PinnedBuf h_tf;
   // empty-cell bits for the current TF and volume
@@ -2727,6 +2733,12 @@ tvk_status tvk_renderer_destroy(tvk_renderer* r) {
   return guarded([&] {
     if (!r) return;
     if (r->stream) cudaStreamSynchronize(r->stream);
+    if (r->copy_stream) {
+      cudaStreamSynchronize(r->copy_stream);
+      cudaStreamDestroy(r->copy_stream);
+    }
+    if (r->ev_img_ready) cudaEventDestroy(r->ev_img_ready);
+    if (r->ev_img_copied) cudaEventDestroy(r->ev_img_copied);
     if (r->ev_start) cudaEventDestroy(r->ev_start);
     if (r->ev_stop) cudaEventDestroy(r->ev_stop);
     if (r->ev_staged) cudaEventDestroy(r->ev_staged);
@@ -3563,6 +3575,40 @@ tvk_status tvk_read_image(tvk_renderer* r, float* host_rgba, size_t n_floats) {
     TVK_CUDA(cudaMemcpyAsync(host_rgba, r->d_img.p, n * sizeof(float), cudaMemcpyDeviceToHost,
                              r->stream));
     TVK_CUDA(cudaStreamSynchronize(r->stream));
+  });
+}
+
+tvk_status tvk_read_image_async(tvk_renderer* r, float* host_rgba, size_t n_floats) {
+  return guarded([&] {
+    REQUIRE(r && host_rgba, "null argument");
+    if (!r->painted) tvk::fail(TVK_ERR_STATE, "nothing painted yet");
+    const size_t n = size_t(r->width) * r->height * 4;
+    REQUIRE(n_floats >= n, "output buffer smaller than the image");
+    TVK_CUDA(cudaSetDevice(r->device));
+    if (!r->copy_stream) {
+      TVK_CUDA(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+      TVK_CUDA(cudaEventCreateWithFlags(&r->ev_img_ready, cudaEventDisableTiming));
+      TVK_CUDA(cudaEventCreateWithFlags(&r->ev_img_copied, cudaEventDisableTiming));
+    }
+    // the previous readback may still read d_img_ro
+    if (r->img_pending) TVK_CUDA(cudaStreamWaitEvent(r->stream, r->ev_img_copied, 0));
+    r->d_img_ro.ensure(n * sizeof(float));
+    TVK_CUDA(cudaMemcpyAsync(r->d_img_ro.p, r->d_img.p, n * sizeof(float),
+                             cudaMemcpyDeviceToDevice, r->stream));
+    TVK_CUDA(cudaEventRecord(r->ev_img_ready, r->stream));
+    TVK_CUDA(cudaStreamWaitEvent(r->copy_stream, r->ev_img_ready, 0));
+    TVK_CUDA(cudaMemcpyAsync(host_rgba, r->d_img_ro.p, n * sizeof(float),
+                             cudaMemcpyDeviceToHost, r->copy_stream));
+    TVK_CUDA(cudaEventRecord(r->ev_img_copied, r->copy_stream));
+    r->img_pending = true;
+  });
+}
+
+tvk_status tvk_wait_image(tvk_renderer* r) {
+  return guarded([&] {
+    REQUIRE(r, "null renderer");
+    if (r->img_pending) TVK_CUDA(cudaEventSynchronize(r->ev_img_copied));
+    r->img_pending = false;
   });
 }
 

@@ -419,6 +419,16 @@ class Renderer:
         check(lib().tvk_read_image(self._h, out.ctypes.data_as(N._f32p), out.size))
         return out
 
+    def ReadBackPixelsAsync(self, out):
+        """Starts copying the last frame into `out` (float32 [height, width, 4],
+        page-locked for overlap) while later frames render; WaitImage() ends it."""
+        check(lib().tvk_read_image_async(self._h, out.ctypes.data_as(N._f32p), out.size))
+        return out
+
+    def WaitImage(self):
+        """Waits for every asynchronous image copy asked for so far."""
+        check(lib().tvk_wait_image(self._h))
+
     def SetClipPlane(self, plane):
         """AbstrRenderer::SetClipPlane: (a, b, c, d) in world space; n.x + d >= 0 is cut."""
         pl = (C.c_float * 4)(*[float(v) for v in plane])
