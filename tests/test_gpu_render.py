@@ -234,3 +234,23 @@ def test_gpu_async_readback_matches_sync(cuda_ok):
         r.Paint()
         np.testing.assert_array_equal(b, r.ReadBackPixels())
     assert all(np.abs(b).sum() > 0 for b in bufs)
+
+
+def test_gpu_counters_match_stats(cuda_ok):
+    """tvk_get_counters: the regular build's first four counters are the
+    frame's statistics (loop steps, executed steps, bricks over the step
+    limit, gradient steps); the traversal's event counters are 0 without the
+    counting build."""
+    raw = numpy_blob_volume((44, 50, 38), np.uint16, 7, (3, 9), (900, 4000), 4095, seed=6, noise=20)
+    vol = Volume(raw, brick_size=(18, 18, 18), overlap=1)
+    r = Renderer()
+    r.RegisterDataset(vol)
+    r.Set1DTransFloat(ramp_tf(1024))
+    r.SetUseLighting(True)
+    r.Resize(64, 48)
+    r.SetViewParameters(50.0, 0.01, 1000.0, eye=(0.3, 0.4, 1.5))
+    r.Paint()
+    c, st = r.GetCounters(), r.GetStats()
+    assert c[0] == st.samples and c[1] == st.shaded_samples and c[3] == st.gradient_samples
+    assert c[0] > c[1] > c[3] > 0 and c[2] == 0
+    assert list(c[4:]) == [0, 0, 0, 0]
