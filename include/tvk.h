@@ -181,9 +181,9 @@ tvk_status tvk_volume_create_ex(const void* voxels, tvk_dtype dtype, const uint6
  * (TVK_VOLUME_CLAMP_TO_EDGE, TVK_VOLUME_MEDIAN, TVK_VOLUME_LOD0_ONLY) and tries
  * the others: the LOD-0 bricks must equal the file's byte for byte (else
  * TVK_ERR_INVALID_ARG), and coarser bricks that no filter reproduces are taken
- * from the file with their min/max recomputed (the converter leaves stale
- * buffer data in some ghost corners of coarser bricks under clamp-to-edge with
- * an overlap of 2 or more). */
+ * from the file with their min/max recomputed (the converter fills some
+ * ghost voxels of coarser bricks before their neighbours are written, so they
+ * can keep stale buffer data). */
 /* ExtendedOctree::GetBrickData (ExtendedOctree.cpp:313-361) on the host, no
  * GPU involved: brick `index` (table-of-contents order: LODs finest first,
  * x fastest) of the ExtendedOctree at byte `offset` of `path`, expanded from
@@ -196,6 +196,69 @@ tvk_status tvk_eo_read_brick(const char* path, uint64_t offset, uint32_t uvf_ver
 tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
                                            uint32_t uvf_version, uint32_t flags,
                                            tvk_volume** out);
+
+/* UVF container (IO/UVF/UVF.cpp:140-158 ParseGlobalHeader, :269-291
+ * ParseDataBlocks; GlobalHeader.cpp:37-46; DataBlock.cpp:51-75): the
+ * "UVF-DATA" magic, a one-byte big-endian flag, the file version, checksum
+ * semantics and bytes, then a chain of data blocks, each an id string, its
+ * semantics (UVFTables::BlockSemanticTable), compression and the distance to
+ * the next block (0 on the last).  Every value is in the writer's byte order,
+ * little-endian, whatever the big-endian flag says: the reference's byte swap
+ * (LargeRAWFile::ReadData / WriteData over EndianConvert::Swap, which returns
+ * the swapped value and leaves its argument unchanged) never swaps, and this
+ * reader does as it does. */
+enum {
+  TVK_UVF_BS_KEY_VALUE_PAIRS = 4,
+  TVK_UVF_BS_1D_HISTOGRAM = 5,
+  TVK_UVF_BS_2D_HISTOGRAM = 6,
+  TVK_UVF_BS_MAXMIN_VALUES = 7,
+  TVK_UVF_BS_TOC_BLOCK = 9,
+  TVK_UVF_CS_NONE = 0,
+  TVK_UVF_CS_CRC32 = 1,
+  TVK_UVF_CS_MD5 = 2,
+  /* flag of tvk_uvf_read_blocks and tvk_volume_open_uvf: check the stored
+   * MD5 checksum first (UVF::VerifyChecksum, UVF.cpp:232-266; TVK_ERR_INVALID_ARG
+   * on a mismatch).  CRC32 checksums are not checked (TVK_ERR_UNSUPPORTED): the
+   * reference's CRC32 pass runs over bytes past the end of the file
+   * (UVF.cpp:174-198), so a stored CRC32 cannot be reproduced. */
+  TVK_UVF_VERIFY_CHECKSUM = 256
+};
+typedef struct tvk_uvf_block {
+  uint64_t offset;         /* file offset of the block header */
+  uint64_t header_bytes;   /* 32 + id length: the payload starts at offset + header_bytes */
+  uint64_t offset_to_next; /* 0 on the last block */
+  uint64_t semantics;      /* UVFTables::BlockSemanticTable */
+  uint64_t compression;    /* UVFTables::CompressionSemanticTable */
+  char id[64];             /* the block id, truncated, NUL-terminated */
+} tvk_uvf_block;
+typedef struct tvk_uvf_info {
+  uint64_t file_version;       /* GlobalHeader::ulFileVersion */
+  uint64_t checksum_semantics; /* TVK_UVF_CS_* */
+  uint64_t checksum_bytes;
+  uint64_t data_offset;        /* GlobalHeader::GetDataPos: the first block */
+  uint64_t file_bytes;
+  uint32_t big_endian;         /* the header's flag (recorded, see above) */
+  uint32_t block_count;
+  /* TOC blocks that UVFDataset::VerifyTOCBlock accepts (1- or 4-component
+   * volumes, uvfDataset.cpp:527-542): the dataset's timesteps, in file order */
+  uint32_t timestep_count;
+  uint32_t checksum_verified;  /* 1 when TVK_UVF_VERIFY_CHECKSUM checked an MD5 */
+} tvk_uvf_info;
+/* Host only, no GPU: walks the container of `path` and fills *info and up to
+ * `capacity` entries of `blocks` (NULL with capacity 0 counts them).  A file
+ * that is not UVF, is truncated, or whose block chain leaves the file returns
+ * TVK_ERR_INVALID_ARG. */
+tvk_status tvk_uvf_read_blocks(const char* path, uint32_t flags, tvk_uvf_info* info,
+                               tvk_uvf_block* blocks, uint32_t capacity);
+/* UVFDataset::Open for a TOC-block dataset (IO/uvfDataset.cpp:83-216): the
+ * volume of timestep `timestep` (the timestep-th TOC block accepted as above),
+ * opened as tvk_volume_open_extended_octree opens the ExtendedOctree at the
+ * block's payload (TOCBlock::GetHeaderFromFile, TOCBlock.cpp:48-65) with the
+ * file's UVF version; `flags` are that call's, plus TVK_UVF_VERIFY_CHECKSUM.
+ * Files whose volumes are RasterDataBlocks (UVF before TOC blocks) return
+ * TVK_ERR_UNSUPPORTED. */
+tvk_status tvk_volume_open_uvf(const char* path, uint32_t timestep, uint32_t flags,
+                               tvk_volume** out);
 tvk_status tvk_volume_destroy(tvk_volume* v);
 tvk_status tvk_volume_get_info(const tvk_volume* v, tvk_volume_info* out);
 

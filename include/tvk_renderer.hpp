@@ -35,6 +35,18 @@ using BrickKey = std::tuple<uint64_t, uint64_t, uint64_t>;
 
 // A volume bricked on the GPU (the LOD-0 level of what
 // ExtendedOctreeConverter::Convert produces, with per-brick statistics).
+// UVF::Open's container walk (tvk_uvf_read_blocks): the data blocks in file
+// order; *info (optional) receives the global header.
+inline std::vector<tvk_uvf_block> ReadUVFBlocks(const std::string& path, uint32_t flags = 0,
+                                                tvk_uvf_info* info = nullptr) {
+  tvk_uvf_info i;
+  check(tvk_uvf_read_blocks(path.c_str(), flags, &i, nullptr, 0));
+  std::vector<tvk_uvf_block> blocks(i.block_count);
+  check(tvk_uvf_read_blocks(path.c_str(), flags, &i, blocks.data(), i.block_count));
+  if (info) *info = i;
+  return blocks;
+}
+
 class BrickedVolume {
  public:
   BrickedVolume(const void* host_voxels, tvk_dtype dtype, std::array<uint64_t, 3> dims,
@@ -53,14 +65,22 @@ class BrickedVolume {
                                &v->v_));
     return v;
   }
-  // ExtendedOctree::Open over a converter-written brick file (uncompressed or
-  // LZ4 bricks; tvk_volume_open_extended_octree)
+  // ExtendedOctree::Open over a converter-written brick file (uncompressed,
+  // zlib, LZMA, LZ4 or bzip2 bricks; tvk_volume_open_extended_octree)
   static std::unique_ptr<BrickedVolume> OpenExtendedOctree(const std::string& path,
                                                            uint64_t offset = 0,
                                                            uint32_t uvf_version = 5,
                                                            uint32_t flags = 0) {
     std::unique_ptr<BrickedVolume> v(new BrickedVolume());
     check(tvk_volume_open_extended_octree(path.c_str(), offset, uvf_version, flags, &v->v_));
+    return v;
+  }
+  // UVFDataset::Open of a TOC-block UVF file, timestep `timestep`
+  // (tvk_volume_open_uvf; flags as above plus TVK_UVF_VERIFY_CHECKSUM)
+  static std::unique_ptr<BrickedVolume> OpenUVF(const std::string& path, uint32_t timestep = 0,
+                                                uint32_t flags = 0) {
+    std::unique_ptr<BrickedVolume> v(new BrickedVolume());
+    check(tvk_volume_open_uvf(path.c_str(), timestep, flags, &v->v_));
     return v;
   }
   // DynamicBrickingDS over this volume (tvk_volume_rebrick)

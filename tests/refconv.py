@@ -177,3 +177,49 @@ def tf1d_load(path, cap=1 << 16):
                                 C.POINTER(C.c_uint64)]
     ok = L.ref_tf1d_load(str(path).encode(), _f32p(out), cap, C.byref(n))
     return (out[:n.value].copy(), True) if ok else (None, False)
+
+
+# ---- UVF container (oracle/ref/ref_uvf.cpp over IO/UVF/UVF.cpp and its blocks)
+
+def write_uvf(path, raw, brick_size, overlap, clamp=False, compression=0, level=0, layout=0,
+              checksum=2, big_endian=False, kv_first=False, histograms=2, components=1,
+              scratch="/tmp"):
+    """The reference's UVF writer, blocks as RAWConverter assembles them: raw
+    is [t, z, y, x] (or [t, z, y, x, 4]) uint8 / uint16, one TOC block per
+    timestep.  checksum 0 none, 1 CRC32, 2 MD5; histograms 0 none, 1 the 1D
+    block, 2 both."""
+    L = _load()
+    L.ref_write_uvf.restype = C.c_int
+    L.ref_write_uvf.argtypes = [C.c_char_p, C.c_char_p, C.c_void_p, C.c_uint32, C.c_int,
+                                C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                C.c_uint32, C.c_int, C.c_int, C.c_uint32, C.c_int, C.c_int,
+                                C.c_int, C.c_int, C.c_int]
+    raw = np.ascontiguousarray(raw)
+    dims = (C.c_uint64 * 3)(raw.shape[3], raw.shape[2], raw.shape[1])
+    ok = L.ref_write_uvf(str(path).encode(), str(scratch).encode(),
+                         raw.ctypes.data_as(C.c_void_p), raw.shape[0],
+                         0 if raw.dtype == np.uint8 else 1, components, dims,
+                         (C.c_uint32 * 3)(*brick_size), overlap, int(clamp), compression, level,
+                         layout, checksum, int(big_endian), int(kv_first), histograms)
+    if ok != 1:
+        raise RuntimeError("reference UVF writer failed")
+
+
+def read_uvf(path, verify=False):
+    """UVF::Open(bMustBeSameVersion = false, bVerify = verify) and its block
+    table: ({version, big_endian, blocks: rows of (offset, semantics,
+    compression, offset to next, id length, octree offset, components, LOD
+    count)}, "") or (None, the parser's reason)."""
+    L = _load()
+    L.ref_read_uvf.restype = C.c_int64
+    L.ref_read_uvf.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_int),
+                               C.POINTER(C.c_uint64), C.c_size_t, C.c_char_p, C.c_size_t]
+    version, be = C.c_uint64(), C.c_int()
+    rows = (C.c_uint64 * (8 * 256))()
+    why = C.create_string_buffer(512)
+    n = L.ref_read_uvf(str(path).encode(), int(verify), C.byref(version), C.byref(be), rows, 256,
+                       why, 512)
+    if n < 0:
+        return None, why.value.decode(errors="replace")
+    return dict(version=version.value, big_endian=be.value,
+                blocks=[list(rows[8 * i:8 * i + 8]) for i in range(min(n, 256))]), ""

@@ -1,0 +1,285 @@
+"""UVF container reading (tvk_uvf_read_blocks, host code) against the
+reference's own parser.
+
+* The committed fixtures (written by the reference's UVF writer, see
+  tests/golden/make_uvf_fixtures.py) hold, in cases.json, the block table that
+  UVF::Open reported for them (UVF.cpp:74-95, 269-291): the library's walk
+  gives the same offsets, semantics, compression and chain links, the same
+  octree offsets for the TOC blocks, and checks the same MD5 checksums.
+* The ExtendedOctree at each TOC block's payload holds that timestep's volume:
+  its LOD-0 bricks, decoded on the host, equal the oracle's bricks of the saved
+  volume.
+* Damaged files (checksum, magic, truncation, broken chain links) are refused
+  with a message, never read past their end.
+* Where the reference's sources were built into oracle/_ref, files written
+  there and then (2D histograms, three timesteps, either big-endian flag,
+  metadata first or last) are walked by both parsers and compared.  The flag
+  changes no byte: the reference's swap is a no-op, and files flagged
+  big-endian hold little-endian values.
+"""
+import ctypes as C
+import json
+import struct
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+import refconv
+from test_eo_fixtures import expand, parse
+from tuvok_gb300 import TvkError, read_uvf_blocks
+from tuvok_gb300 import _native as N
+
+UVF = Path(__file__).resolve().parent / "golden" / "uvf"
+CASES = json.loads((UVF / "cases.json").read_text())
+TOC = N.TVK_UVF_BS_TOC_BLOCK
+
+
+def assert_same_table(path, head, blocks, ref):
+    assert head["file_version"] == ref["version"]
+    assert head["big_endian"] == ref["big_endian"]
+    assert head["file_bytes"] == Path(path).stat().st_size
+    assert head["block_count"] == len(ref["blocks"]) == len(blocks)
+    for i, (b, r) in enumerate(zip(blocks, ref["blocks"])):
+        got = (b["offset"], b["semantics"], b["compression"], b["offset_to_next"],
+               b["header_bytes"] - 32)
+        assert got == tuple(r[:5]), f"block {i}"
+        if r[1] == TOC:
+            assert b["offset"] + b["header_bytes"] == r[5], f"octree offset of block {i}"
+    assert blocks[-1]["offset_to_next"] == 0
+    accepted = [r for r in ref["blocks"] if r[1] == TOC and r[6] in (1, 4)]
+    assert head["timestep_count"] == len(accepted)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_uvf_fixture_block_table_equals_reference_parser(case):
+    path = UVF / f"{case['name']}.uvf"
+    verify = case["checksum"] == 2
+    head, blocks = read_uvf_blocks(path, verify=verify)
+    assert_same_table(path, head, blocks, case["reference"])
+    assert head["timestep_count"] == case["timesteps"]
+    assert head["checksum_semantics"] == case["checksum"]
+    assert head["checksum_verified"] == int(verify)
+    assert head["big_endian"] == int(case["big_endian"])
+    sem = [b["semantics"] for b in blocks]
+    assert (sem[0] == N.TVK_UVF_BS_KEY_VALUE_PAIRS) == case["kv_first"]
+    assert sem.count(N.TVK_UVF_BS_MAXMIN_VALUES) == case["timesteps"]
+    assert sem.count(N.TVK_UVF_BS_1D_HISTOGRAM) == case["timesteps"] * case["histograms"]
+    assert all(b["id"] for b in blocks)
+
+
+def lib_brick(path, offset, index):
+    n = C.c_size_t()
+    N.check(N.lib().tvk_eo_read_brick(str(path).encode(), offset, 5, index, None, 0,
+                                      C.byref(n)))
+    out = (C.c_uint8 * n.value)()
+    N.check(N.lib().tvk_eo_read_brick(str(path).encode(), offset, 5, index, out, n.value,
+                                      C.byref(n)))
+    return bytes(out)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_uvf_fixture_toc_blocks_hold_each_timestep(case):
+    """Timestep t's TOC block holds the octree of volume t: every LOD-0 brick,
+    decoded by the restatement and by tvk_eo_read_brick at the block's payload,
+    equals the oracle's brick of the saved volume."""
+    path = UVF / f"{case['name']}.uvf"
+    buf = path.read_bytes()
+    raw = np.load(UVF / f"{case['name']}.npy")
+    _, blocks = read_uvf_blocks(path)
+    tocs = [b for b in blocks if b["semantics"] == TOC]
+    assert len(tocs) == case["timesteps"] == raw.shape[0]
+    vb = (1 if case["dtype"] == "u8" else 2) * case["components"]
+    dt = np.uint8 if case["dtype"] == "u8" else np.uint16
+    for t, b in enumerate(tocs):
+        base = b["offset"] + b["header_bytes"]
+        h = parse(buf[base:])
+        assert tuple(h["dims"]) == tuple(case["dims"]) and h["comps"] == case["components"]
+        lc = h["counts"][0]
+        for k in range(lc[0] * lc[1] * lc[2]):
+            c = (k % lc[0], (k // lc[0]) % lc[1], k // (lc[0] * lc[1]))
+            n = O.brick_size(h["sizes"][0], lc, case["brick_size"], case["overlap"], c)
+            off, length, comp, _, _, _ = h["toc"][k]
+            nbytes = n[0] * n[1] * n[2] * vb
+            data = expand(buf[base + off:base + off + length], comp, nbytes)
+            assert lib_brick(path, base, k) == data, f"t {t} brick {k}"
+            shape = (n[2], n[1], n[0]) + ((4,) if case["components"] == 4 else ())
+            ref = O.lod0_brick(raw[t], case["brick_size"], case["overlap"], case["clamp"], c)
+            np.testing.assert_array_equal(np.frombuffer(data, dt).reshape(shape), ref,
+                                          err_msg=f"{case['name']} t {t} brick {c}")
+
+
+def status_of(path, verify=False):
+    try:
+        read_uvf_blocks(path, verify=verify)
+    except TvkError as e:
+        return e.status, str(e)
+    return N.TVK_OK, ""
+
+
+def test_uvf_checksum_mismatch_is_refused(tmp_path):
+    """One flipped payload byte (the file's last, inside a metadata string):
+    the MD5 no longer matches (refused with verification, the reference's
+    parser agrees where it is built), while the block walk alone still reads
+    the file."""
+    case = next(c for c in CASES if c["checksum"] == 2)
+    buf = bytearray((UVF / f"{case['name']}.uvf").read_bytes())
+    buf[-1] ^= 0x5A
+    bad = tmp_path / "bad.uvf"
+    bad.write_bytes(bytes(buf))
+    st, msg = status_of(bad, verify=True)
+    assert st == 1 and "checksum mismatch" in msg
+    assert status_of(bad, verify=False)[0] == N.TVK_OK
+    if refconv.available():
+        table, why = refconv.read_uvf(bad, verify=True)
+        assert table is None and "checksum" in why
+        assert refconv.read_uvf(bad, verify=False)[0] is not None
+
+
+def test_uvf_crc32_checksums_are_not_verified():
+    case = next(c for c in CASES if c["checksum"] == 1)
+    path = UVF / f"{case['name']}.uvf"
+    st, msg = status_of(path, verify=True)
+    assert st == 4 and "CRC32" in msg
+    head, _ = read_uvf_blocks(path)
+    assert head["checksum_semantics"] == N.TVK_UVF_CS_CRC32 and head["checksum_bytes"] == 4
+
+
+def test_uvf_damaged_headers_are_refused(tmp_path):
+    """Wrong magic, chain links past the end or shorter than a header, an id
+    longer than the file, and truncation anywhere before the last block's
+    header: all TVK_ERR_INVALID_ARG."""
+    case = next(c for c in CASES if c["timesteps"] == 2)
+    src = (UVF / f"{case['name']}.uvf").read_bytes()
+    head, blocks = read_uvf_blocks(UVF / f"{case['name']}.uvf")
+
+    def refused(buf, name):
+        p = tmp_path / name
+        p.write_bytes(bytes(buf))
+        st, msg = status_of(p)
+        assert st == 1, (name, st, msg)
+        return msg
+
+    bad = bytearray(src)
+    bad[3] = ord("X")
+    assert "magic" in refused(bad, "magic.uvf")
+    b1 = blocks[1]
+    for name, value in (("far", len(src)), ("short", 5), ("huge", 1 << 62)):
+        bad = bytearray(src)
+        at = b1["offset"] + b1["header_bytes"] - 8
+        struct.pack_into("<Q", bad, at, value)
+        refused(bad, f"next_{name}.uvf")
+    bad = bytearray(src)
+    struct.pack_into("<Q", bad, b1["offset"], 1 << 40)
+    assert "id" in refused(bad, "idlen.uvf")
+    cuts = [0, 7, 20, 40, head["data_offset"], head["data_offset"] + 10,
+            blocks[1]["offset"] + 4, blocks[-1]["offset"] + 20]
+    for cut in cuts:
+        refused(src[:cut], f"cut{cut}.uvf")
+
+
+def test_uvf_truncation_never_reads_past_the_end(tmp_path):
+    """Every cut of a small file returns TVK_OK or TVK_ERR_INVALID_ARG; the
+    walk never reads past the end of the file."""
+    case = next(c for c in CASES if c["checksum"] == 1)
+    src = (UVF / f"{case['name']}.uvf").read_bytes()
+    rng = np.random.default_rng(7)
+    for cut in sorted(set(int(x) for x in rng.integers(0, len(src), 60))):
+        p = tmp_path / f"cut{cut}.uvf"
+        p.write_bytes(src[:cut])
+        assert status_of(p)[0] in (N.TVK_OK, 1)
+
+
+def minimal_uvf(blocks, big_endian=False):
+    """A hand-assembled UVF file: the global header (no checksum) and blocks of
+    (semantics, payload bytes) chained in order.  Values are little-endian
+    whatever the flag, as the reference writes them (its byte swap is a
+    no-op)."""
+    e = "<"
+    out = bytearray(b"UVF-DATA") + bytes([1 if big_endian else 0])
+    out += struct.pack(e + "QQQQ", 5, 0, 0, 0)
+    for i, (sem, payload) in enumerate(blocks):
+        ident = f"block {i}".encode()
+        size = 32 + len(ident) + len(payload)
+        nxt = 0 if i == len(blocks) - 1 else size
+        out += struct.pack(e + "Q", len(ident)) + ident + struct.pack(e + "QQQ", sem, 0, nxt)
+        out += payload
+    return bytes(out)
+
+
+@pytest.mark.parametrize("big_endian", [False, True])
+def test_uvf_hand_assembled_chain(tmp_path, big_endian):
+    """A chain built by hand, with either big-endian flag, is walked block by
+    block; TOC blocks of 2-component volumes are not timesteps
+    (VerifyTOCBlock)."""
+    eo2 = struct.pack("<IQ", 0, 2) + bytes(20)
+    eo1 = struct.pack("<IQ", 1, 1) + bytes(20)
+    p = tmp_path / "hand.uvf"
+    p.write_bytes(minimal_uvf([(4, b"kv"), (TOC, eo2), (TOC, eo1), (7, bytes(16))], big_endian))
+    head, blocks = read_uvf_blocks(p)
+    assert head["big_endian"] == int(big_endian) and head["data_offset"] == 41
+    assert [b["semantics"] for b in blocks] == [4, TOC, TOC, 7]
+    assert [b["id"] for b in blocks] == [f"block {i}" for i in range(4)]
+    assert head["timestep_count"] == 1
+    off = 41
+    for b in blocks:
+        assert b["offset"] == off
+        off += b["offset_to_next"]
+
+
+def open_status(path, timestep=0):
+    h = C.c_void_p()
+    st = N.lib().tvk_volume_open_uvf(str(path).encode(), timestep, 0, C.byref(h))
+    assert not h.value
+    return st, N.lib().tvk_last_error().decode()
+
+
+def test_uvf_open_refusals_before_any_device_work(tmp_path):
+    """tvk_volume_open_uvf refuses, before touching the GPU: a timestep past
+    the last TOC block, a file of RasterDataBlock volumes (UVF without TOC
+    blocks), and a file with no volume at all."""
+    case = next(c for c in CASES if c["timesteps"] == 2)
+    st, msg = open_status(UVF / f"{case['name']}.uvf", timestep=2)
+    assert st == 1 and "timestep" in msg
+    p = tmp_path / "raster.uvf"
+    p.write_bytes(minimal_uvf([(1, bytes(64))]))
+    st, msg = open_status(p)
+    assert st == 4 and "RasterDataBlock" in msg
+    p = tmp_path / "kv.uvf"
+    p.write_bytes(minimal_uvf([(4, b"x")]))
+    st, msg = open_status(p)
+    assert st == 1 and "TOC" in msg
+
+
+LIVE = [
+    # dtype, components, timesteps, brick, overlap, clamp, compression, level, layout,
+    # checksum, big-endian, metadata first, histograms
+    ("u8", 1, 3, (8, 8, 8), 1, False, 0, 0, 0, 2, False, False, 2),
+    ("u16", 1, 2, (10, 9, 8), 2, True, 3, 1, 1, 2, True, True, 2),
+    ("u8", 4, 2, (8, 8, 8), 1, False, 1, 4, 2, 0, True, False, 0),
+    ("u16", 1, 1, (16, 16, 16), 1, False, 4, 9, 3, 2, False, True, 1),
+]
+
+
+@pytest.mark.skipif(not refconv.available(), reason="reference sources not built (oracle/_ref)")
+@pytest.mark.parametrize("cfg", LIVE, ids=[f"live{i}" for i in range(len(LIVE))])
+def test_uvf_walk_equals_reference_parser_live(tmp_path, cfg):
+    dt, comps, ts, bs, ov, clamp, comp, level, layout, checksum, be, kv_first, hist = cfg
+    rng = np.random.default_rng(len(tmp_path.name))
+    dims = (19, 15, 12)
+    shape = (ts, dims[2], dims[1], dims[0]) + ((4,) if comps == 4 else ())
+    top = 255 if dt == "u8" else 4095
+    raw = rng.integers(0, top + 1, size=shape).astype(np.uint8 if dt == "u8" else np.uint16)
+    path = tmp_path / "live.uvf"
+    refconv.write_uvf(path, raw, bs, ov, clamp=clamp, compression=comp, level=level,
+                      layout=layout, checksum=checksum, big_endian=be, kv_first=kv_first,
+                      histograms=hist, components=comps, scratch=str(tmp_path))
+    verify = checksum == 2
+    table, why = refconv.read_uvf(path, verify=verify)
+    assert table is not None, why
+    head, blocks = read_uvf_blocks(path, verify=verify)
+    assert_same_table(path, head, blocks, table)
+    assert head["timestep_count"] == ts and head["checksum_verified"] == int(verify)
+    if hist == 2 and comps == 1:
+        assert sum(b["semantics"] == N.TVK_UVF_BS_2D_HISTOGRAM for b in blocks) == ts

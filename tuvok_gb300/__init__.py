@@ -7,7 +7,7 @@ and a thin Python mirror of Tuvok's AbstrRenderer / dataset interfaces.
 """
 from ._native import TvkError, lib  # noqa: F401  (raises if libtvk.so is missing)
 from .renderer import (Batch, Pool, Renderer, TransferFunction1D, Volume,  # noqa: F401
-                       generate_volume_device)
+                       generate_volume_device, read_uvf_blocks)
 
 __all__ = ["Batch", "Pool", "Renderer", "TransferFunction1D", "Volume", "TvkError",
-           "generate_volume_device", "lib"]
+           "generate_volume_device", "lib", "read_uvf_blocks"]

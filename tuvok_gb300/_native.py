@@ -19,6 +19,10 @@ TVK_U8, TVK_U16, TVK_RGBA8 = 0, 1, 2
 TVK_RM_1DTRANS, TVK_RM_2DTRANS, TVK_RM_ISOSURFACE = 0, 1, 2
 TVK_LIGHT_REFERENCE, TVK_LIGHT_BLINN_PHONG = 0, 1
 TVK_MM_SOURCE, TVK_MM_PRECOMPUTE, TVK_MM_DYNAMIC = 0, 1, 2
+TVK_UVF_BS_KEY_VALUE_PAIRS, TVK_UVF_BS_1D_HISTOGRAM, TVK_UVF_BS_2D_HISTOGRAM = 4, 5, 6
+TVK_UVF_BS_MAXMIN_VALUES, TVK_UVF_BS_TOC_BLOCK = 7, 9
+TVK_UVF_CS_NONE, TVK_UVF_CS_CRC32, TVK_UVF_CS_MD5 = 0, 1, 2
+TVK_UVF_VERIFY_CHECKSUM = 256
 
 STATUS_NAMES = {0: "TVK_OK", 1: "TVK_ERR_INVALID_ARG", 2: "TVK_ERR_CUDA",
                 3: "TVK_ERR_OUT_OF_MEMORY", 4: "TVK_ERR_UNSUPPORTED", 5: "TVK_ERR_STATE",
@@ -95,6 +99,20 @@ class LeaperInfo(C.Structure):
                 ("converged", C.c_int), ("resident", C.c_uint32), ("ms", C.c_float),
                 ("ms_traversal", C.c_float), ("bytes_paged", C.c_uint64),
                 ("samples", C.c_uint64), ("ms_host", C.c_float)]
+
+
+class UvfBlock(C.Structure):
+    _fields_ = [("offset", C.c_uint64), ("header_bytes", C.c_uint64),
+                ("offset_to_next", C.c_uint64), ("semantics", C.c_uint64),
+                ("compression", C.c_uint64), ("id", C.c_char * 64)]
+
+
+class UvfInfo(C.Structure):
+    _fields_ = [("file_version", C.c_uint64), ("checksum_semantics", C.c_uint64),
+                ("checksum_bytes", C.c_uint64), ("data_offset", C.c_uint64),
+                ("file_bytes", C.c_uint64), ("big_endian", C.c_uint32),
+                ("block_count", C.c_uint32), ("timestep_count", C.c_uint32),
+                ("checksum_verified", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -187,6 +205,9 @@ PROTOTYPES = {
                                         C.POINTER(_vp)],
     "tvk_eo_read_brick": [C.c_char_p, C.c_uint64, C.c_uint32, C.c_uint64, _vp, C.c_size_t,
                           C.POINTER(C.c_size_t)],
+    "tvk_uvf_read_blocks": [C.c_char_p, C.c_uint32, C.POINTER(UvfInfo), C.POINTER(UvfBlock),
+                            C.c_uint32],
+    "tvk_volume_open_uvf": [C.c_char_p, C.c_uint32, C.c_uint32, C.POINTER(_vp)],
     "tvk_set_clearview": [_vp, C.c_int],
     "tvk_set_cv_isovalue": [_vp, C.c_float],
     "tvk_set_cv_color": [_vp, _f32p],

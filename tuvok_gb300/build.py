@@ -31,7 +31,7 @@ HOST_FLAGS = "-fPIC,-ffp-contract=off,-O3,-Wall"
 # host restatements bit for bit
 EXTRA = {"raycast.cu": ["-fmad=false"], "volgen.cu": ["-fmad=false"]}
 SOURCES = ["api.cpp", "bricking.cu", "cnn.cu", "codecs.cpp", "eo.cpp", "lod.cu", "raycast.cu",
-           "rebrick.cu", "tf1d.cpp", "volgen.cu"]
+           "rebrick.cu", "tf1d.cpp", "uvf.cpp", "volgen.cu"]
 HEADERS = [CSRC / "tvk_internal.h", ROOT / "include" / "tvk.h"]
 ORACLE_SOURCES = [ROOT / "oracle" / "bricking.cpp", ROOT / "oracle" / "raycast.cpp",
                   ROOT / "oracle" / "rebrick.cpp", ROOT / "oracle" / "volgen.cpp"]

@@ -2392,147 +2392,198 @@ tvk_status tvk_eo_read_brick(const char* path, uint64_t offset, uint32_t uvf_ver
   });
 }
 
-tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
-                                           uint32_t uvf_version, uint32_t flags,
-                                           tvk_volume** out) {
-  return guarded([&] {
-    REQUIRE(path && out, "null argument");
-    *out = nullptr;
-    tvk::EoFile e;
-    tvk::eo_open(path, offset, uvf_version, e);
-    tvk_dtype dt;
-    if (e.component_type == 0 && e.components == 1) dt = TVK_U8;
-    else if (e.component_type == 1 && e.components == 1) dt = TVK_U16;
-    else if (e.component_type == 0 && e.components == 4) dt = TVK_RGBA8;
-    else
-      tvk::fail(TVK_ERR_UNSUPPORTED,
-                "ExtendedOctree: 1-component uint8 / uint16 and 4-component uint8 volumes only");
-    if (e.normals) tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: precomputed normals");
-    if (e.aspect[0] != 1.0 || e.aspect[1] != 1.0 || e.aspect[2] != 1.0)
-      tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: volume aspect other than 1:1:1");
-    const uint32_t bs[3] = {uint32_t(e.brick_size[0]), uint32_t(e.brick_size[1]),
-                            uint32_t(e.brick_size[2])};
-    const uint32_t ov = e.overlap;
-    const size_t vb = size_t(dt == TVK_U16 ? 2 : 1) * e.components;  // bytes per voxel
-    // the flat volume from the LOD-0 bricks' inner voxels
-    const std::vector<tvk::LodInfo> lods = tvk::lod_table(e.dims, bs, ov);
-    std::vector<tvk_brick_md> md0;
-    tvk::brick_metadata(lods[0], bs, ov, md0);
-    std::vector<uint8_t> raw(size_t(e.dims[0] * e.dims[1] * e.dims[2]) * vb), brick;
-    const uint64_t core[3] = {bs[0] - 2ull * ov, bs[1] - 2ull * ov, bs[2] - 2ull * ov};
-    for (uint64_t k = 0; k < md0.size(); ++k) {
-      const uint32_t* n = md0[k].n_voxels;
-      tvk::eo_read_brick(e, k, size_t(n[0]) * n[1] * n[2] * vb, brick);
-      const uint64_t c[3] = {k % lods[0].bricks[0], (k / lods[0].bricks[0]) % lods[0].bricks[1],
-                             k / (lods[0].bricks[0] * lods[0].bricks[1])};
-      for (uint32_t z = ov; z + ov < n[2]; ++z)
-        for (uint32_t y = ov; y + ov < n[1]; ++y) {
-          const uint64_t gx = c[0] * core[0], gy = c[1] * core[1] + (y - ov),
-                         gz = c[2] * core[2] + (z - ov);
-          std::memcpy(raw.data() + ((gz * e.dims[1] + gy) * e.dims[0] + gx) * vb,
-                      brick.data() + ((size_t(z) * n[1] + y) * n[0] + ov) * vb,
-                      size_t(n[0] - 2 * ov) * vb);
-        }
+namespace {
+
+// The volume of the ExtendedOctree at byte `offset` of `path`; throws tvk::Error.
+void open_eo_volume(const char* path, uint64_t offset, uint32_t uvf_version, uint32_t flags,
+                    tvk_volume** out) {
+  REQUIRE(path && out, "null argument");
+  *out = nullptr;
+  tvk::EoFile e;
+  tvk::eo_open(path, offset, uvf_version, e);
+  tvk_dtype dt;
+  if (e.component_type == 0 && e.components == 1) dt = TVK_U8;
+  else if (e.component_type == 1 && e.components == 1) dt = TVK_U16;
+  else if (e.component_type == 0 && e.components == 4) dt = TVK_RGBA8;
+  else
+    tvk::fail(TVK_ERR_UNSUPPORTED,
+              "ExtendedOctree: 1-component uint8 / uint16 and 4-component uint8 volumes only");
+  if (e.normals) tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: precomputed normals");
+  if (e.aspect[0] != 1.0 || e.aspect[1] != 1.0 || e.aspect[2] != 1.0)
+    tvk::fail(TVK_ERR_UNSUPPORTED, "ExtendedOctree: volume aspect other than 1:1:1");
+  const uint32_t bs[3] = {uint32_t(e.brick_size[0]), uint32_t(e.brick_size[1]),
+                          uint32_t(e.brick_size[2])};
+  const uint32_t ov = e.overlap;
+  const size_t vb = size_t(dt == TVK_U16 ? 2 : 1) * e.components;  // bytes per voxel
+  // the flat volume from the LOD-0 bricks' inner voxels
+  const std::vector<tvk::LodInfo> lods = tvk::lod_table(e.dims, bs, ov);
+  std::vector<tvk_brick_md> md0;
+  tvk::brick_metadata(lods[0], bs, ov, md0);
+  std::vector<uint8_t> raw(size_t(e.dims[0] * e.dims[1] * e.dims[2]) * vb), brick;
+  const uint64_t core[3] = {bs[0] - 2ull * ov, bs[1] - 2ull * ov, bs[2] - 2ull * ov};
+  for (uint64_t k = 0; k < md0.size(); ++k) {
+    const uint32_t* n = md0[k].n_voxels;
+    tvk::eo_read_brick(e, k, size_t(n[0]) * n[1] * n[2] * vb, brick);
+    const uint64_t c[3] = {k % lods[0].bricks[0], (k / lods[0].bricks[0]) % lods[0].bricks[1],
+                           k / (lods[0].bricks[0] * lods[0].bricks[1])};
+    for (uint32_t z = ov; z + ov < n[2]; ++z)
+      for (uint32_t y = ov; y + ov < n[1]; ++y) {
+        const uint64_t gx = c[0] * core[0], gy = c[1] * core[1] + (y - ov),
+                       gz = c[2] * core[2] + (z - ov);
+        std::memcpy(raw.data() + ((gz * e.dims[1] + gy) * e.dims[0] + gx) * vb,
+                    brick.data() + ((size_t(z) * n[1] + y) * n[0] + ov) * vb,
+                    size_t(n[0] - 2 * ov) * vb);
+      }
+  }
+  // Rebuild from the LOD-0 data: the border setting (not recorded in the
+  // header) is the one whose LOD-0 bricks equal the file's, trying `flags`
+  // first; then the filter whose coarser bricks equal the file's.  Where no
+  // filter reproduces a coarser brick the file's bytes are kept: the
+  // converter's coarser bricks can carry stale buffer contents in some ghost
+  // corners (DownsampleBrick skips its memset under clamp, ExtendedOctree
+  // Converter.inc:261-262, and FillOverlap copies corners from neighbours
+  // not yet filled), which no rebuild reproduces.
+  const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0;
+  const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
+             median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && !lod0_only;
+  std::vector<uint8_t> dev;
+  struct Drop {
+    void operator()(tvk_volume* v) const {
+      tvk::free_volume_device(v);
+      delete v;
     }
-    // Rebuild from the LOD-0 data: the border setting (not recorded in the
-    // header) is the one whose LOD-0 bricks equal the file's, trying `flags`
-    // first; then the filter whose coarser bricks equal the file's.  Where no
-    // filter reproduces a coarser brick the file's bytes are kept: with
-    // clamp-to-edge and an overlap of 2 or more, the converter's coarser
-    // bricks carry stale buffer contents in some ghost corners
-    // (DownsampleBrick skips its memset under clamp, ExtendedOctreeConverter.
-    // inc:261-262, and FillOverlap copies corners from neighbours not yet
-    // filled), which no rebuild reproduces.
-    const bool lod0_only = (flags & TVK_VOLUME_LOD0_ONLY) != 0;
-    const bool clamp0 = (flags & TVK_VOLUME_CLAMP_TO_EDGE) != 0,
-               median0 = (flags & TVK_VOLUME_MEDIAN) != 0 && !lod0_only;
-    std::vector<uint8_t> dev;
-    struct Drop {
-      void operator()(tvk_volume* v) const {
-        tvk::free_volume_device(v);
-        delete v;
-      }
-    };
-    using VolPtr = std::unique_ptr<tvk_volume, Drop>;
-    auto brick_bytes = [&](const tvk_volume* V, uint64_t k) {
-      return size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
-    };
-    auto same_as_file = [&](const tvk_volume* V, uint64_t k) {
-      const size_t nb = brick_bytes(V, k);
-      tvk::eo_read_brick(e, k, nb, brick);
-      dev.resize(nb);
-      TVK_CUDA(cudaMemcpy(dev.data(), static_cast<const uint8_t*>(V->d_pool) + V->offsets[k] * vb,
-                          nb, cudaMemcpyDeviceToHost));
-      return std::memcmp(dev.data(), brick.data(), nb) == 0;
-    };
-    for (int ci = 0; ci < 2; ++ci) {
-      const bool clamp = clamp0 ^ (ci == 1);
-      VolPtr best;
-      std::vector<uint64_t> best_bad;
-      for (int mi = 0; mi < (lod0_only ? 1 : 2); ++mi) {
-        const bool median = median0 ^ (mi == 1);
-        VolPtr V(tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
-                                    !lod0_only));
-        bool lod0 = true;
-        for (uint64_t k = 0; k < V->n_bricks && lod0; ++k) lod0 = same_as_file(V.get(), k);
-        if (!lod0) break;  // LOD 0 does not depend on the filter
-        std::vector<uint64_t> bad;
-        for (uint64_t k = V->n_bricks; k < V->total_bricks; ++k)
-          if (!same_as_file(V.get(), k)) bad.push_back(k);
-        if (bad.empty()) {
-          *out = V.release();
-          return;
-        }
-        if (!best || bad.size() < best_bad.size()) {
-          best = std::move(V);
-          best_bad = std::move(bad);
-        }
-      }
-      if (!best) continue;
-      // keep the file's coarser bricks that no filter reproduced, with their
-      // statistics (min/max over the whole brick, ComputeBrickStats) and macro cells
-      tvk_volume* V = best.get();
-      for (uint64_t k : best_bad) {
-        const size_t nb = brick_bytes(V, k);
-        tvk::eo_read_brick(e, k, nb, brick);
-        TVK_CUDA(cudaMemcpy(static_cast<uint8_t*>(V->d_pool) + V->offsets[k] * vb, brick.data(), nb,
-                            cudaMemcpyHostToDevice));
-        if (dt == TVK_RGBA8) continue;  // colour bricks carry no statistics
-        double lo = 1e300, hi = -1e300;
-        for (size_t i = 0; i < nb / vb; ++i) {
-          const double x = vb == 1 ? double(brick[i])
-                                   : double(reinterpret_cast<const uint16_t*>(brick.data())[i]);
-          lo = std::min(lo, x);
-          hi = std::max(hi, x);
-        }
-        V->bmin[k] = lo;
-        V->bmax[k] = hi;
-      }
-      if (dt == TVK_RGBA8) {  // no macro cells to refresh
-        *out = best.release();
+  };
+  using VolPtr = std::unique_ptr<tvk_volume, Drop>;
+  auto brick_bytes = [&](const tvk_volume* V, uint64_t k) {
+    return size_t(V->sizes[3 * k]) * V->sizes[3 * k + 1] * V->sizes[3 * k + 2] * vb;
+  };
+  auto same_as_file = [&](const tvk_volume* V, uint64_t k) {
+    const size_t nb = brick_bytes(V, k);
+    tvk::eo_read_brick(e, k, nb, brick);
+    dev.resize(nb);
+    TVK_CUDA(cudaMemcpy(dev.data(), static_cast<const uint8_t*>(V->d_pool) + V->offsets[k] * vb,
+                        nb, cudaMemcpyDeviceToHost));
+    return std::memcmp(dev.data(), brick.data(), nb) == 0;
+  };
+  for (int ci = 0; ci < 2; ++ci) {
+    const bool clamp = clamp0 ^ (ci == 1);
+    VolPtr best;
+    std::vector<uint64_t> best_bad;
+    for (int mi = 0; mi < (lod0_only ? 1 : 2); ++mi) {
+      const bool median = median0 ^ (mi == 1);
+      VolPtr V(tvk::create_volume(raw.data(), false, dt, e.dims, bs, ov, clamp ? 1 : 0, median,
+                                  !lod0_only));
+      bool lod0 = true;
+      for (uint64_t k = 0; k < V->n_bricks && lod0; ++k) lod0 = same_as_file(V.get(), k);
+      if (!lod0) break;  // LOD 0 does not depend on the filter
+      std::vector<uint64_t> bad;
+      for (uint64_t k = V->n_bricks; k < V->total_bricks; ++k)
+        if (!same_as_file(V.get(), k)) bad.push_back(k);
+      if (bad.empty()) {
+        *out = V.release();
         return;
       }
-      tvk::DevBuf d_off, d_sizes;
-      d_off.ensure(V->total_bricks * sizeof(uint64_t));
-      d_sizes.ensure(V->total_bricks * 3 * sizeof(uint32_t));
-      TVK_CUDA(cudaMemcpy(d_off.p, V->offsets.data(), V->total_bricks * sizeof(uint64_t),
+      if (!best || bad.size() < best_bad.size()) {
+        best = std::move(V);
+        best_bad = std::move(bad);
+      }
+    }
+    if (!best) continue;
+    // keep the file's coarser bricks that no filter reproduced, with their
+    // statistics (min/max over the whole brick, ComputeBrickStats) and macro cells
+    tvk_volume* V = best.get();
+    for (uint64_t k : best_bad) {
+      const size_t nb = brick_bytes(V, k);
+      tvk::eo_read_brick(e, k, nb, brick);
+      TVK_CUDA(cudaMemcpy(static_cast<uint8_t*>(V->d_pool) + V->offsets[k] * vb, brick.data(), nb,
                           cudaMemcpyHostToDevice));
-      TVK_CUDA(cudaMemcpy(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
-                          cudaMemcpyHostToDevice));
-      uint32_t max_rows = 0;
-      for (uint32_t d : V->cell_dims)
-        max_rows = std::max(max_rows, (d >> 10) & 1023u);
-      uint64_t launches = 0;
-      tvk::launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
-                              static_cast<const uint64_t*>(V->d_cell_meta), V->total_bricks,
-                              max_rows, static_cast<uint32_t*>(V->d_cells), nullptr, &launches);
-      TVK_CUDA(cudaDeviceSynchronize());
+      if (dt == TVK_RGBA8) continue;  // colour bricks carry no statistics
+      double lo = 1e300, hi = -1e300;
+      for (size_t i = 0; i < nb / vb; ++i) {
+        const double x = vb == 1 ? double(brick[i])
+                                 : double(reinterpret_cast<const uint16_t*>(brick.data())[i]);
+        lo = std::min(lo, x);
+        hi = std::max(hi, x);
+      }
+      V->bmin[k] = lo;
+      V->bmax[k] = hi;
+    }
+    if (dt == TVK_RGBA8) {  // no macro cells to refresh
       *out = best.release();
       return;
     }
-    tvk::fail(TVK_ERR_INVALID_ARG,
-              "ExtendedOctree: the file's LOD-0 bricks differ from a rebricking of their own "
-              "inner voxels with zero or clamped borders");
+    tvk::DevBuf d_off, d_sizes;
+    d_off.ensure(V->total_bricks * sizeof(uint64_t));
+    d_sizes.ensure(V->total_bricks * 3 * sizeof(uint32_t));
+    TVK_CUDA(cudaMemcpy(d_off.p, V->offsets.data(), V->total_bricks * sizeof(uint64_t),
+                        cudaMemcpyHostToDevice));
+    TVK_CUDA(cudaMemcpy(d_sizes.p, V->sizes.data(), V->total_bricks * 3 * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice));
+    uint32_t max_rows = 0;
+    for (uint32_t d : V->cell_dims)
+      max_rows = std::max(max_rows, (d >> 10) & 1023u);
+    uint64_t launches = 0;
+    tvk::launch_cell_minmax(V->d_pool, V->bytes, d_off.as<uint64_t>(), d_sizes.as<uint32_t>(),
+                            static_cast<const uint64_t*>(V->d_cell_meta), V->total_bricks,
+                            max_rows, static_cast<uint32_t*>(V->d_cells), nullptr, &launches);
+    TVK_CUDA(cudaDeviceSynchronize());
+    *out = best.release();
+    return;
+  }
+  tvk::fail(TVK_ERR_INVALID_ARG,
+            "ExtendedOctree: the file's LOD-0 bricks differ from a rebricking of their own "
+            "inner voxels with zero or clamped borders");
+}
+
+}  // namespace
+
+tvk_status tvk_volume_open_extended_octree(const char* path, uint64_t offset,
+                                           uint32_t uvf_version, uint32_t flags,
+                                           tvk_volume** out) {
+  return guarded([&] { open_eo_volume(path, offset, uvf_version, flags, out); });
+}
+
+tvk_status tvk_uvf_read_blocks(const char* path, uint32_t flags, tvk_uvf_info* info,
+                               tvk_uvf_block* blocks, uint32_t capacity) {
+  return guarded([&] {
+    REQUIRE(path && info, "null argument");
+    REQUIRE(blocks || capacity == 0, "null block array with a non-zero capacity");
+    REQUIRE((flags & ~uint32_t(TVK_UVF_VERIFY_CHECKSUM)) == 0, "unknown flag");
+    tvk::UvfFile u;
+    tvk::uvf_open(path, (flags & TVK_UVF_VERIFY_CHECKSUM) != 0, u);
+    *info = tvk_uvf_info{};
+    info->file_version = u.version;
+    info->checksum_semantics = u.checksum_semantics;
+    info->checksum_bytes = u.checksum_bytes;
+    info->data_offset = u.data_offset;
+    info->file_bytes = u.file_bytes;
+    info->big_endian = u.big_endian ? 1 : 0;
+    info->block_count = uint32_t(u.blocks.size());
+    info->timestep_count = uint32_t(u.timesteps.size());
+    info->checksum_verified = u.checksum_verified ? 1 : 0;
+    for (size_t i = 0; i < u.blocks.size() && i < capacity; ++i) blocks[i] = u.blocks[i];
+  });
+}
+
+tvk_status tvk_volume_open_uvf(const char* path, uint32_t timestep, uint32_t flags,
+                               tvk_volume** out) {
+  return guarded([&] {
+    REQUIRE(path && out, "null argument");
+    *out = nullptr;
+    tvk::UvfFile u;
+    tvk::uvf_open(path, (flags & TVK_UVF_VERIFY_CHECKSUM) != 0, u);
+    if (u.timesteps.empty()) {
+      if (u.has_raster)
+        tvk::fail(TVK_ERR_UNSUPPORTED,
+                  "UVF: volumes stored as RasterDataBlocks (files without TOC blocks) are not read");
+      tvk::fail(TVK_ERR_INVALID_ARG,
+                "UVF: no TOC block of a 1- or 4-component volume in the file");
+    }
+    REQUIRE(timestep < u.timesteps.size(), "timestep out of range");
+    if (u.version > 0xffffffffull) tvk::fail(TVK_ERR_INVALID_ARG, "UVF: file version out of range");
+    const tvk_uvf_block& b = u.blocks[u.timesteps[timestep]];
+    open_eo_volume(path, b.offset + b.header_bytes, uint32_t(u.version),
+                   flags & ~uint32_t(TVK_UVF_VERIFY_CHECKSUM), out);
   });
 }
 

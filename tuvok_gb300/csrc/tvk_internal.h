@@ -108,6 +108,16 @@ struct EoFile {
 void eo_open(const char* path, uint64_t offset, uint32_t uvf_version, EoFile& e);
 void eo_read_brick(const EoFile& e, uint64_t index, size_t bytes, std::vector<uint8_t>& out);
 size_t lz4_decode_block(const uint8_t* src, size_t src_len, uint8_t* dst, size_t dst_len);
+
+// UVF container (uvf.cpp): global header and the chain of data-block headers
+struct UvfFile {
+  uint64_t version = 0, checksum_semantics = 0, checksum_bytes = 0;
+  uint64_t data_offset = 0, file_bytes = 0;
+  bool big_endian = false, checksum_verified = false, has_raster = false;
+  std::vector<tvk_uvf_block> blocks;
+  std::vector<uint32_t> timesteps;  // indices into blocks of the accepted TOC blocks
+};
+void uvf_open(const char* path, bool verify_checksum, UvfFile& u);
 void brick_size(const LodInfo& l, const uint32_t B[3], uint32_t ov, const uint64_t c[3],
                 uint32_t out[3]);
 void brick_metadata(const LodInfo& l, const uint32_t B[3], uint32_t ov,

@@ -83,6 +83,19 @@ class Volume:
                                                     int(uvf_version), flags, C.byref(h)))
         return cls(None, _handle=h)
 
+    @classmethod
+    def FromUVF(cls, path, timestep=0, verify=False, clamp_to_edge=False, median=False,
+                lod0_only=False):
+        """UVFDataset::Open of a TOC-block UVF file: the ExtendedOctree of
+        timestep `timestep`, opened as FromExtendedOctree opens it; `verify`
+        checks the file's MD5 checksum first (UVF::VerifyChecksum)."""
+        flags = ((cls.CLAMP_TO_EDGE if clamp_to_edge else 0) | (cls.MEDIAN if median else 0) |
+                 (cls.LOD0_ONLY if lod0_only else 0) |
+                 (N.TVK_UVF_VERIFY_CHECKSUM if verify else 0))
+        h = C.c_void_p()
+        check(lib().tvk_volume_open_uvf(str(path).encode(), int(timestep), flags, C.byref(h)))
+        return cls(None, _handle=h)
+
     @property
     def handle(self):
         return self._h
@@ -646,6 +659,24 @@ class Pool:
         info = N.LeaperInfo()
         check(lib().tvk_leaper_paint(renderer._h, self._h, int(max_passes), C.byref(info)))
         return info
+
+
+def read_uvf_blocks(path, verify=False):
+    """UVF::Open's container walk (tvk_uvf_read_blocks): the global header as a
+    dict and one dict per data block (offset, header_bytes, offset_to_next,
+    semantics, compression, id), in file order."""
+    flags = N.TVK_UVF_VERIFY_CHECKSUM if verify else 0
+    info = N.UvfInfo()
+    check(lib().tvk_uvf_read_blocks(str(path).encode(), flags, C.byref(info), None, 0))
+    blocks = (N.UvfBlock * max(1, info.block_count))()
+    check(lib().tvk_uvf_read_blocks(str(path).encode(), flags, C.byref(info), blocks,
+                                    info.block_count))
+    head = {k: getattr(info, k) for k, _ in N.UvfInfo._fields_}
+    rows = [{"offset": b.offset, "header_bytes": b.header_bytes,
+             "offset_to_next": b.offset_to_next, "semantics": b.semantics,
+             "compression": b.compression, "id": b.id.decode("latin-1")}
+            for b in blocks[:info.block_count]]
+    return head, rows
 
 
 def generate_volume_device(ptr, dims, dtype, blobs, noise_amp, octaves, cell, seed, int_noise,
