@@ -598,6 +598,11 @@ typedef struct tvk_cnn_wgrad {
 /* y = act(conv3x3(concat(x1, x2), W) + b), zero padding (forward); with the
  * flipped-transposed weights of tvk_cnn_weights_bf16 it is the data gradient. */
 tvk_status tvk_cnn_conv3x3(const tvk_cnn_conv* args, void* stream);
+/* Waits for `stream` and reports a tensor-core convolution that gave up
+ * waiting for its MMAs (bounded at 2 s per patch; TVK_ERR_INTERNAL, output
+ * undefined).  Convolutions whose channel counts are multiples of 16 run on
+ * tcgen05 with TMEM accumulators, the others on mma.sync. */
+tvk_status tvk_cnn_check(void* stream);
 /* dW += sum_p G[p] (x) X[p + tap], db += sum_p G[p]. */
 tvk_status tvk_cnn_conv3x3_wgrad(const tvk_cnn_wgrad* args, void* stream);
 /* G = dY * LeakyReLU'(Y) as BF16 (y = NULL or slope < 0: G = dY). */

@@ -42,7 +42,10 @@ def weights_bf16(w32, cout, cin):
 
 
 CASES = [  # n, h, w, c1, c2, cout, slope
+    # channel counts that are multiples of 16 run on tcgen05 (16x8-pixel
+    # patches, TMEM accumulators), the others on mma.sync
     (2, 13, 21, 16, 0, 32, 0.1),
+    (1, 40, 24, 16, 0, 8, 0.1),       # cout 8: mma.sync
     (1, 16, 16, 32, 0, 48, 0.1),
     (2, 9, 8, 48, 0, 64, -1.0),
     (1, 12, 20, 64, 64, 64, 0.1),
@@ -80,6 +83,7 @@ def test_gpu_conv3x3_forward_and_gradients(cuda_ok, case):
                   cout=cout, slope=slope, y_bf16=p(y), y_f32=p(yf), y2_f32=None, split=cout,
                   accumulate=0)
     check(lib().tvk_cnn_conv3x3(C.byref(a), stream()))
+    check(lib().tvk_cnn_check(stream()))
     z, yref = K.conv3x3(x, wt, b, slope)
     np.testing.assert_allclose(host(yf), yref, rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(host(y), K.bf16(yref), rtol=1e-2, atol=1e-2)
@@ -101,6 +105,7 @@ def test_gpu_conv3x3_forward_and_gradients(cuda_ok, case):
                     cout=cin, slope=-1.0, y_bf16=None, y_f32=p(dx1), y2_f32=p(dx2),
                     split=c1 if c2 else cin, accumulate=0)
     check(lib().tvk_cnn_conv3x3(C.byref(bwd), stream()))
+    check(lib().tvk_cnn_check(stream()))
     dxr, dwr, dbr, _ = K.conv3x3_backward(x, wt, z, gref, -1.0)
     got = host(dx1) if not c2 else np.concatenate([host(dx1), host(dx2)], axis=3)
     np.testing.assert_allclose(got, dxr, rtol=1e-4, atol=1e-4)

@@ -184,6 +184,7 @@ PROTOTYPES = {
     "tvk_paint_progressive": [_vp, C.c_int, C.POINTER(SubframeInfo)],
     "tvk_get_render_size": [_vp, _u32p, _u32p],
     "tvk_cnn_conv3x3": [C.POINTER(CnnConv), _vp],
+    "tvk_cnn_check": [_vp],
     "tvk_cnn_conv3x3_wgrad": [C.POINTER(CnnWgrad), _vp],
     "tvk_cnn_act_grad": [_vp, _vp, C.c_float, _vp, C.c_size_t, _vp],
     "tvk_cnn_avgpool2": [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp],

@@ -1907,6 +1907,8 @@ void paint_learned(tvk_renderer* R, tvk_learned* N, float threshold_db, tvk_lear
   TVK_CUDA(cudaMemcpyAsync(N->h_sum.p, sum, sizeof(float), cudaMemcpyDeviceToHost, s));
   TVK_CUDA(cudaEventRecord(N->ev[3], s));
   TVK_CUDA(cudaEventSynchronize(N->ev[3]));
+  if (cnn_tc_timeouts(true))
+    fail(TVK_ERR_INTERNAL, "a tensor-core convolution gave up waiting for its MMAs");
   const double mse = double(*N->h_sum.as<float>()) / (4.0 * P.out_w * P.out_h);
   const float psnr = mse > 0 ? float(10.0 * std::log10(1.0 / mse)) : 1000.0f;
   const bool fall_back = psnr < threshold_db;
@@ -3357,6 +3359,15 @@ tvk_status tvk_cnn_conv3x3(const tvk_cnn_conv* a, void* stream) {
     REQUIRE(a->y_bf16 || a->y_f32, "no output");
     REQUIRE(!a->y2_f32 || (a->split > 0 && a->split < a->cout && a->y_f32), "bad split");
     tvk::cnn_conv3x3(*a, as_stream(stream));
+  });
+}
+
+tvk_status tvk_cnn_check(void* stream) {
+  return guarded([&] {
+    TVK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    if (tvk::cnn_tc_timeouts(true))
+      tvk::fail(TVK_ERR_INTERNAL,
+                "a tensor-core convolution gave up waiting for its MMAs; its output is undefined");
   });
 }
 

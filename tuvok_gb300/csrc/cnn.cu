@@ -274,6 +274,243 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
   }
 }
 
+// ------------------------------------------------ convolution on tcgen05 / TMEM
+//
+// The same convolution on the fifth-generation tensor cores.  A CTA of 4 warps
+// owns a 16 x 8 output patch = the M = 128 rows of one tcgen05.mma.kind::f16
+// (BF16 operands, FP32 accumulator in tensor memory), N = all output channels,
+// and loops over patches (persistent grid).  Shared memory holds, in the
+// no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core matrix):
+//   halo    [cin / 8][18][10][8]  the patch's input with a 1-pixel border
+//   weights [9][cin / 8][cout][8] all taps, loaded once per CTA
+// so the A operand of tap (ky, kx) is the halo itself, offset by
+// (ky * 10 + kx) * 16 bytes: 8-row groups (patch rows) 160 bytes apart, K core
+// matrices (channel octets) 2880 bytes apart.  No im2col copy is made.  One
+// thread issues the 9 x cin / 16 MMAs of a patch and commits them to an
+// mbarrier; the four warps then read their 32 TMEM lanes (pixels) and run the
+// epilogue of the other kernels.
+constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
+constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
+constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
+// longest wait for the tensor cores to finish a patch before the kernel gives
+// up (reported through g_cnn_tc_timeouts); a patch takes microseconds
+constexpr uint64_t kTcWaitNs = 2000000000ull;
+
+__device__ unsigned int g_cnn_tc_timeouts;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Shared-memory matrix descriptor, no swizzle: start, leading (K) and stride
+// (M / N) byte offsets in 16-byte units, descriptor version 1 at bit 46.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9, 10-12 = 1), both K-major, N / 8 at bit 17, M / 16 at bit 24.
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t m, uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n.reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for phase `parity` of the barrier for at most kTcWaitNs.
+__device__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kTcWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+               "r"(valid ? 16 : 0)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_raw + 8);
+  int* flag = reinterpret_cast<int*>(smem_raw + 12);
+  unsigned char* halo = smem_raw + kTcCtrlBytes;                       // [kc][18][10][8]
+  unsigned char* wsm = halo + size_t(kc_n) * kTcHR * kTcHC * 16;       // [9][kc][cout][8]
+  const uint32_t bar_a = smem_addr(bar), halo_a = smem_addr(halo), w_a = smem_addr(wsm);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_x = (a.w + kTcCols - 1) / kTcCols, tiles_y = (a.h + kTcRows - 1) / kTcRows;
+  const int n_tiles = a.n * tiles_x * tiles_y;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_addr(tmem_slot)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    *flag = 0;
+  }
+  // all taps' weights, re-laid from [tap][cout][cin] into core matrices
+  for (int i = tid; i < 9 * kc_n * cout; i += kThreads) {
+    const int co = i % cout, kc = (i / cout) % kc_n, tap = i / (cout * kc_n);
+    cp_async16(w_a + uint32_t(i) * 16, a.wt + (size_t(tap) * cout + co) * cin + kc * 8, true);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = tc_idesc(128, uint32_t(cout));
+  constexpr uint32_t kLboA = kTcHR * kTcHC * 16, kSboA = kTcHC * 16;
+  const uint32_t lbo_b = uint32_t(cout) * 16, sbo_b = 128;
+  uint32_t phase = 0;
+  bool ok = true;
+
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int img = t / (tiles_x * tiles_y);
+    const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
+    const int y0 = ty * kTcRows - 1, x0 = tx * kTcCols - 1;
+    // the halo, 8 channels per 16-byte copy, zero outside the image
+    for (int i = tid; i < kc_n * kTcHR * kTcHC; i += kThreads) {
+      const int c = i % kTcHC, r = (i / kTcHC) % kTcHR, kc = i / (kTcHC * kTcHR);
+      const int yy = y0 + r, xx = x0 + c;
+      const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
+      const size_t p = in ? (size_t(img) * a.h + yy) * a.w + xx : 0;
+      const int ch = kc * 8;
+      const __nv_bfloat16* src =
+          ch < a.c1 ? a.x1 + p * a.c1 + ch : a.x2 + p * a.c2 + (ch - a.c1);
+      cp_async16(halo_a + uint32_t(i) * 16, src, in);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    // make the copies visible to the tensor cores' (async proxy) reads
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      uint32_t acc = 0;
+      for (int tap = 0; tap < 9; ++tap) {
+        const int ky = tap / 3, kx = tap % 3;
+        for (int s = 0; s < kc_n / 2; ++s) {
+          const uint64_t ad =
+              tc_desc(halo_a + uint32_t(((2 * s * kTcHR + ky) * kTcHC + kx) * 16), kLboA, kSboA);
+          const uint64_t bd =
+              tc_desc(w_a + uint32_t((tap * kc_n + 2 * s) * cout * 16), lbo_b, sbo_b);
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+              : "memory");
+          acc = 1;
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              bar_a)
+          : "memory");
+      if (!mbar_wait_bounded(bar_a, phase)) *flag = 1;
+    }
+    __syncthreads();
+    phase ^= 1u;
+    if (*flag) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // epilogue: warp w holds TMEM lanes (pixels) 32w .. 32w + 31
+    const int m = warp * 32 + lane;
+    const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
+    const bool live = oy < a.h && ox < a.w;
+    const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
+    for (int c0 = 0; c0 < cout; c0 += 16) {
+      float v[16];
+      tc_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+      if (!live) continue;
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int co = c0 + e;
+        if (a.bias) v[e] += a.bias[co];
+        if (a.slope >= 0.0f && v[e] < 0.0f) v[e] *= a.slope;
+      }
+      if (a.y_bf16) {
+        uint32_t w8[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          w8[e] = pack_bf16(__float2bfloat16_rn(v[2 * e]), __float2bfloat16_rn(v[2 * e + 1]));
+        uint4* dst = reinterpret_cast<uint4*>(a.y_bf16 + p * cout + c0);
+        dst[0] = make_uint4(w8[0], w8[1], w8[2], w8[3]);
+        dst[1] = make_uint4(w8[4], w8[5], w8[6], w8[7]);
+      }
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int co = c0 + e;
+        if (co < a.split) {
+          if (a.y_f32) {
+            float* o = a.y_f32 + p * a.split + co;
+            *o = a.accumulate ? *o + v[e] : v[e];
+          }
+        } else if (a.y2_f32) {
+          float* o = a.y2_f32 + p * (cout - a.split) + (co - a.split);
+          *o = a.accumulate ? *o + v[e] : v[e];
+        }
+      }
+    }
+    // TMEM read and halo consumed before the next patch overwrites them
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+  }
+  if (!ok && tid == 0) {
+    atomicAdd(&g_cnn_tc_timeouts, 1u);
+    mbar_wait_bounded(bar_a, phase ^ 1u);  // the abandoned patch's MMAs, bounded again
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                 "r"(tmem_cols)
+                 : "memory");
+  }
+}
+
 // ------------------------------------------------------------- weight gradient
 
 struct WgradArgs {
@@ -569,7 +806,65 @@ uint32_t grid_for(size_t n) {
   return uint32_t(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
 }
 
+// Shared memory of conv3x3_tc_kernel: control words, halo, weights, and room
+// for the largest address any MMA descriptor of the launch can reach (also
+// were its leading and stride offsets taken the other way round), so that no
+// descriptor points past the allocation.
+size_t conv_tc_smem(int cin, int cout) {
+  const size_t kc = size_t(cin) / 8;
+  const size_t halo = kc * kTcHR * kTcHC * 16, wts = 9 * kc * size_t(cout) * 16;
+  const size_t end = kTcCtrlBytes + halo + wts;
+  const size_t lbo_a = size_t(kTcHR) * kTcHC * 16, sbo_a = size_t(kTcHC) * 16;
+  const size_t a_last = kTcCtrlBytes + ((size_t(2 * (kc / 2 - 1)) * kTcHR + 2) * kTcHC + 2) * 16;
+  const size_t a_reach = a_last + std::max(lbo_a + 15 * sbo_a, 15 * lbo_a + sbo_a) + 128;
+  const size_t lbo_b = size_t(cout) * 16, sbo_b = 128;
+  const size_t b_last = kTcCtrlBytes + halo + (8 * kc + 2 * (kc / 2 - 1)) * size_t(cout) * 16;
+  const size_t nb = size_t(cout) / 8;
+  const size_t b_reach = b_last + std::max(lbo_b + (nb - 1) * sbo_b, (nb - 1) * lbo_b + sbo_b) + 128;
+  return (std::max({end, a_reach, b_reach}) + 127) / 128 * 128;
+}
+
+// The tcgen05 convolution takes the launch when its shapes fit: input and
+// output channels multiples of 16 (M = 128, N = cout, K steps of 16), at most
+// 128 output channels (a power-of-two TMEM allocation of 32 to 128 columns),
+// 16-byte aligned tensors, and halo + weights in shared memory.
+bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
+  const int cin = a.c1 + a.c2;
+  auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  if (cin % 16 || a.c1 % 8 || a.c2 % 8 || cin > 128) return false;
+  if (a.cout % 16 || a.cout < 16 || a.cout > 128) return false;
+  if (!aligned(a.x1) || (a.c2 && !aligned(a.x2)) || !aligned(a.wt) || !aligned(a.y_bf16))
+    return false;
+  const size_t smem = conv_tc_smem(cin, a.cout);
+  if (smem > 227 * 1024) return false;
+  const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
+  TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem)));
+  int dev = 0, sms = 0, per_sm = 0;
+  TVK_CUDA(cudaGetDevice(&dev));
+  TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3x3_tc_kernel, kThreads,
+                                                         smem));
+  // resident CTAs never wait on one another for tensor memory (512 columns)
+  per_sm = std::max(1, std::min(per_sm, int(512 / cols)));
+  const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
+  const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
+  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols);
+  TVK_CUDA(cudaGetLastError());
+  return true;
+}
+
 }  // namespace
+
+uint32_t cnn_tc_timeouts(bool reset) {
+  uint32_t n = 0;
+  TVK_CUDA(cudaMemcpyFromSymbol(&n, g_cnn_tc_timeouts, sizeof(n)));
+  if (reset && n) {
+    const uint32_t zero = 0;
+    TVK_CUDA(cudaMemcpyToSymbol(g_cnn_tc_timeouts, &zero, sizeof(zero)));
+  }
+  return n;
+}
 
 void cnn_conv3x3(const CnnConv& c, cudaStream_t s) {
   ConvArgs a{};
@@ -591,6 +886,7 @@ void cnn_conv3x3(const CnnConv& c, cudaStream_t s) {
   a.accumulate = c.accumulate;
   const int cin = c.c1 + c.c2;
   const int nt = (c.cout + 7) / 8;
+  if (launch_conv_tc(a, s)) return;
   // large images: 16x16 patches (all taps' weights staged when they fit in
   // 64 KB with the halo), while there are at least two waves of them
   const unsigned wide_blocks =

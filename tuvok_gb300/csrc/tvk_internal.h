@@ -359,6 +359,9 @@ void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, ui
 using CnnConv = tvk_cnn_conv;
 using CnnWgrad = tvk_cnn_wgrad;
 void cnn_conv3x3(const CnnConv& c, cudaStream_t s);
+// Tensor-core convolutions that gave up waiting for their MMAs since the last
+// reset (0 normally).
+uint32_t cnn_tc_timeouts(bool reset);
 void cnn_conv3x3_wgrad(const CnnWgrad& c, cudaStream_t s);
 void cnn_act_grad(const float* dy, const void* y, float slope, void* g, size_t n, cudaStream_t s);
 void cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s);
