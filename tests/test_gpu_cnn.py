@@ -45,7 +45,8 @@ CASES = [  # n, h, w, c1, c2, cout, slope
     # channel counts that are multiples of 16 run on tcgen05 (16x8-pixel
     # patches, TMEM accumulators), the others on mma.sync
     (2, 13, 21, 16, 0, 32, 0.1),
-    (1, 40, 24, 16, 0, 8, 0.1),       # cout 8: mma.sync
+    (1, 40, 24, 4, 12, 32, 0.1),      # c1 = 4: forward on mma.sync
+    (1, 290, 300, 4, 12, 32, 0.1),    # the same with 16x16 patches
     (1, 16, 16, 32, 0, 48, 0.1),
     (2, 9, 8, 48, 0, 64, -1.0),
     (1, 12, 20, 64, 64, 64, 0.1),

@@ -7,10 +7,11 @@
 // Layout: activations NHWC (channels innermost), BF16; weights of a layer as
 // [tap = ky * 3 + kx][cout][cin] (cin innermost), FP32 masters and BF16 copies.
 // A convolution is an implicit GEMM: M = output pixels, N = output channels,
-// K = 9 taps x input channels.  One CTA (4 warps) computes an 8x8 pixel patch
-// for every output channel: the 10x10 input halo and the current tap's weights
-// are staged in shared memory and each warp issues mma.sync.m16n8k16 over its
-// 16 pixels.  The skip connections of the U-Net concatenate two tensors along
+// K = 9 taps x input channels.  Channel counts that are multiples of 16 run on
+// tcgen05 (conv3x3_tc_kernel: 16x8-pixel patches as M = 128, accumulators in
+// tensor memory); the others on mma.sync.m16n8k16, one CTA (4 warps) per 8x8
+// patch or (8 warps) per 16x16 patch, the halo and the weights staged in shared
+// memory.  The skip connections of the U-Net concatenate two tensors along
 // channels; the convolution reads them in place (x1: c1 channels, x2: c2).
 #include <cuda_bf16.h>
 
@@ -806,22 +807,13 @@ uint32_t grid_for(size_t n) {
   return uint32_t(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
 }
 
-// Shared memory of conv3x3_tc_kernel: control words, halo, weights, and room
-// for the largest address any MMA descriptor of the launch can reach (also
-// were its leading and stride offsets taken the other way round), so that no
-// descriptor points past the allocation.
+// Shared memory of conv3x3_tc_kernel: control words, halo, weights.  Every
+// MMA descriptor stays inside its region: the A operand of the last K step of
+// tap (2, 2) ends at ((2 (kc/2 - 1) * 18 + 2) * 10 + 2) * 16 + 2880 + 15 * 160
+// + 128 <= kc * 2880 bytes, and B's at the end of the weights.
 size_t conv_tc_smem(int cin, int cout) {
   const size_t kc = size_t(cin) / 8;
-  const size_t halo = kc * kTcHR * kTcHC * 16, wts = 9 * kc * size_t(cout) * 16;
-  const size_t end = kTcCtrlBytes + halo + wts;
-  const size_t lbo_a = size_t(kTcHR) * kTcHC * 16, sbo_a = size_t(kTcHC) * 16;
-  const size_t a_last = kTcCtrlBytes + ((size_t(2 * (kc / 2 - 1)) * kTcHR + 2) * kTcHC + 2) * 16;
-  const size_t a_reach = a_last + std::max(lbo_a + 15 * sbo_a, 15 * lbo_a + sbo_a) + 128;
-  const size_t lbo_b = size_t(cout) * 16, sbo_b = 128;
-  const size_t b_last = kTcCtrlBytes + halo + (8 * kc + 2 * (kc / 2 - 1)) * size_t(cout) * 16;
-  const size_t nb = size_t(cout) / 8;
-  const size_t b_reach = b_last + std::max(lbo_b + (nb - 1) * sbo_b, (nb - 1) * lbo_b + sbo_b) + 128;
-  return (std::max({end, a_reach, b_reach}) + 127) / 128 * 128;
+  return kTcCtrlBytes + kc * kTcHR * kTcHC * 16 + 9 * kc * size_t(cout) * 16;
 }
 
 // The tcgen05 convolution takes the launch when its shapes fit: input and
