@@ -363,18 +363,39 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
                : "memory");
 }
 
-__global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols) {
+__global__ void __launch_bounds__(kThreads)
+    conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_raw + 8);
   int* flag = reinterpret_cast<int*>(smem_raw + 12);
-  unsigned char* halo = smem_raw + kTcCtrlBytes;                       // [kc][18][10][8]
-  unsigned char* wsm = halo + size_t(kc_n) * kTcHR * kTcHC * 16;       // [9][kc][cout][8]
-  const uint32_t bar_a = smem_addr(bar), halo_a = smem_addr(halo), w_a = smem_addr(wsm);
+  const uint32_t halo_bytes = uint32_t(kc_n) * kTcHR * kTcHC * 16;
+  unsigned char* halo0 = smem_raw + kTcCtrlBytes;                 // n_halos x [kc][18][10][8]
+  unsigned char* wsm = halo0 + size_t(n_halos) * halo_bytes;      // [9][kc][cout][8]
+  const uint32_t bar_a = smem_addr(bar), halo_a = smem_addr(halo0), w_a = smem_addr(wsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_x = (a.w + kTcCols - 1) / kTcCols, tiles_y = (a.h + kTcRows - 1) / kTcRows;
   const int n_tiles = a.n * tiles_x * tiles_y;
+
+  // the halo of patch t into halo buffer `buf`, 8 channels per 16-byte copy,
+  // zero outside the image
+  auto load_halo = [&](int t, int buf) {
+    const int img = t / (tiles_x * tiles_y);
+    const int y0 = ((t / tiles_x) % tiles_y) * kTcRows - 1, x0 = (t % tiles_x) * kTcCols - 1;
+    const uint32_t dst = halo_a + uint32_t(buf) * halo_bytes;
+    for (int i = tid; i < kc_n * kTcHR * kTcHC; i += kThreads) {
+      const int c = i % kTcHC, r = (i / kTcHC) % kTcHR, kc = i / (kTcHC * kTcHR);
+      const int yy = y0 + r, xx = x0 + c;
+      const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
+      const size_t p = in ? (size_t(img) * a.h + yy) * a.w + xx : 0;
+      const int ch = kc * 8;
+      const __nv_bfloat16* src =
+          ch < a.c1 ? a.x1 + p * a.c1 + ch : a.x2 + p * a.c2 + (ch - a.c1);
+      cp_async16(dst + uint32_t(i) * 16, src, in);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -388,12 +409,14 @@ __global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, 
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     *flag = 0;
   }
-  // all taps' weights, re-laid from [tap][cout][cin] into core matrices
+  // all taps' weights, re-laid from [tap][cout][cin] into core matrices, and
+  // the first patch's halo
   for (int i = tid; i < 9 * kc_n * cout; i += kThreads) {
     const int co = i % cout, kc = (i / cout) % kc_n, tap = i / (cout * kc_n);
     cp_async16(w_a + uint32_t(i) * 16, a.wt + (size_t(tap) * cout + co) * cin + kc * 8, true);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
+  if (int(blockIdx.x) < n_tiles) load_halo(blockIdx.x, 0);
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -403,35 +426,24 @@ __global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, 
   const uint32_t lbo_b = uint32_t(cout) * 16, sbo_b = 128;
   uint32_t phase = 0;
   bool ok = true;
+  int buf = 0;
 
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    const int img = t / (tiles_x * tiles_y);
-    const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
-    const int y0 = ty * kTcRows - 1, x0 = tx * kTcCols - 1;
-    // the halo, 8 channels per 16-byte copy, zero outside the image
-    for (int i = tid; i < kc_n * kTcHR * kTcHC; i += kThreads) {
-      const int c = i % kTcHC, r = (i / kTcHC) % kTcHR, kc = i / (kTcHC * kTcHR);
-      const int yy = y0 + r, xx = x0 + c;
-      const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
-      const size_t p = in ? (size_t(img) * a.h + yy) * a.w + xx : 0;
-      const int ch = kc * 8;
-      const __nv_bfloat16* src =
-          ch < a.c1 ? a.x1 + p * a.c1 + ch : a.x2 + p * a.c2 + (ch - a.c1);
-      cp_async16(halo_a + uint32_t(i) * 16, src, in);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    const int tn = t + int(gridDim.x);
+    // this patch's halo has landed (the only copies in flight)
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     // make the copies visible to the tensor cores' (async proxy) reads
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t h_a = halo_a + uint32_t(buf) * halo_bytes;
       uint32_t acc = 0;
       for (int tap = 0; tap < 9; ++tap) {
         const int ky = tap / 3, kx = tap % 3;
         for (int s = 0; s < kc_n / 2; ++s) {
           const uint64_t ad =
-              tc_desc(halo_a + uint32_t(((2 * s * kTcHR + ky) * kTcHC + kx) * 16), kLboA, kSboA);
+              tc_desc(h_a + uint32_t(((2 * s * kTcHR + ky) * kTcHC + kx) * 16), kLboA, kSboA);
           const uint64_t bd =
               tc_desc(w_a + uint32_t((tap * kc_n + 2 * s) * cout * 16), lbo_b, sbo_b);
           asm volatile(
@@ -446,16 +458,22 @@ __global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, 
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
               bar_a)
           : "memory");
-      if (!mbar_wait_bounded(bar_a, phase)) *flag = 1;
     }
+    // with two halo buffers the next patch's halo streams in under the MMAs
+    if (n_halos == 2 && tn < n_tiles) load_halo(tn, buf ^ 1);
+    if (tid == 0 && !mbar_wait_bounded(bar_a, phase)) *flag = 1;
     __syncthreads();
     phase ^= 1u;
     if (*flag) {
       ok = false;
       break;
     }
+    // with one, under the epilogue (the MMAs no longer read it)
+    if (n_halos == 1 && tn < n_tiles) load_halo(tn, 0);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     // epilogue: warp w holds TMEM lanes (pixels) 32w .. 32w + 31
+    const int img = t / (tiles_x * tiles_y);
+    const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
     const int m = warp * 32 + lane;
     const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
     const bool live = oy < a.h && ox < a.w;
@@ -493,9 +511,9 @@ __global__ void __launch_bounds__(kThreads) conv3x3_tc_kernel(const ConvArgs a, 
         }
       }
     }
-    // TMEM read and halo consumed before the next patch overwrites them
+    // TMEM read before the next patch's MMAs overwrite it
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    if (n_halos == 2) buf ^= 1;
   }
   if (!ok && tid == 0) {
     atomicAdd(&g_cnn_tc_timeouts, 1u);
@@ -807,19 +825,21 @@ uint32_t grid_for(size_t n) {
   return uint32_t(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
 }
 
-// Shared memory of conv3x3_tc_kernel: control words, halo, weights.  Every
-// MMA descriptor stays inside its region: the A operand of the last K step of
-// tap (2, 2) ends at ((2 (kc/2 - 1) * 18 + 2) * 10 + 2) * 16 + 2880 + 15 * 160
-// + 128 <= kc * 2880 bytes, and B's at the end of the weights.
-size_t conv_tc_smem(int cin, int cout) {
+// Shared memory of conv3x3_tc_kernel: control words, one or two halos, the
+// weights.  Every MMA descriptor stays inside its operand: the A operand of
+// the last K step of tap (2, 2) ends at ((2 (kc/2 - 1) * 18 + 2) * 10 + 2) * 16
+// + 2880 + 15 * 160 + 128 <= kc * 2880 bytes, and B's at the end of the weights.
+size_t conv_tc_smem(int cin, int cout, int n_halos) {
   const size_t kc = size_t(cin) / 8;
-  return kTcCtrlBytes + kc * kTcHR * kTcHC * 16 + 9 * kc * size_t(cout) * 16;
+  return kTcCtrlBytes + size_t(n_halos) * kc * kTcHR * kTcHC * 16 + 9 * kc * size_t(cout) * 16;
 }
 
 // The tcgen05 convolution takes the launch when its shapes fit: input and
 // output channels multiples of 16 (M = 128, N = cout, K steps of 16), at most
 // 128 output channels (a power-of-two TMEM allocation of 32 to 128 columns),
-// 16-byte aligned tensors, and halo + weights in shared memory.
+// 16-byte aligned tensors, and halo + weights in shared memory.  A second halo
+// buffer (the next patch's input streaming in under the MMAs) is used when
+// it fits and costs no CTA per SM.
 bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   const int cin = a.c1 + a.c2;
   auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
@@ -827,21 +847,31 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   if (a.cout % 16 || a.cout < 16 || a.cout > 128) return false;
   if (!aligned(a.x1) || (a.c2 && !aligned(a.x2)) || !aligned(a.wt) || !aligned(a.y_bf16))
     return false;
-  const size_t smem = conv_tc_smem(cin, a.cout);
-  if (smem > 227 * 1024) return false;
+  constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
+  const int tmem_ctas = int(512 / cols);
+  // CTAs per SM by shared memory (each also reserves 1 KB), tensor memory and threads
+  auto ctas = [&](size_t smem) {
+    return std::min({int(kSmPerSm / (smem + kReserved)), tmem_ctas, 2048 / kThreads});
+  };
+  const size_t one = conv_tc_smem(cin, a.cout, 1), two = conv_tc_smem(cin, a.cout, 2);
+  if (one > kMaxSmem) return false;
+  const int n_halos = (two <= kMaxSmem && ctas(two) >= std::min(ctas(one), 2)) ? 2 : 1;
+  const size_t smem = n_halos == 2 ? two : one;
   TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
+  TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                int(cudaSharedmemCarveoutMaxShared)));
   int dev = 0, sms = 0, per_sm = 0;
   TVK_CUDA(cudaGetDevice(&dev));
   TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3x3_tc_kernel, kThreads,
                                                          smem));
   // resident CTAs never wait on one another for tensor memory (512 columns)
-  per_sm = std::max(1, std::min(per_sm, int(512 / cols)));
+  per_sm = std::max(1, std::min(per_sm, ctas(smem)));
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
-  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols);
+  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols, n_halos);
   TVK_CUDA(cudaGetLastError());
   return true;
 }
