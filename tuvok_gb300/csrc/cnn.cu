@@ -497,6 +497,13 @@ __global__ void __launch_bounds__(kThreads)
         dst[0] = make_uint4(w8[0], w8[1], w8[2], w8[3]);
         dst[1] = make_uint4(w8[4], w8[5], w8[6], w8[7]);
       }
+      if (a.y_f32 && !a.y2_f32 && !a.accumulate) {  // plain FP32 output: 16-byte stores
+        float4* dst = reinterpret_cast<float4*>(a.y_f32 + p * cout + c0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          dst[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+        continue;
+      }
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const int co = c0 + e;
@@ -845,7 +852,8 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
   if (cin % 16 || a.c1 % 8 || a.c2 % 8 || cin > 128) return false;
   if (a.cout % 16 || a.cout < 16 || a.cout > 128) return false;
-  if (!aligned(a.x1) || (a.c2 && !aligned(a.x2)) || !aligned(a.wt) || !aligned(a.y_bf16))
+  if (!aligned(a.x1) || (a.c2 && !aligned(a.x2)) || !aligned(a.wt) || !aligned(a.y_bf16) ||
+      !aligned(a.y_f32))
     return false;
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
@@ -862,13 +870,13 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
                                 int(smem)));
   TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 int(cudaSharedmemCarveoutMaxShared)));
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0;
   TVK_CUDA(cudaGetDevice(&dev));
   TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  TVK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3x3_tc_kernel, kThreads,
-                                                         smem));
-  // resident CTAs never wait on one another for tensor memory (512 columns)
-  per_sm = std::max(1, std::min(per_sm, ctas(smem)));
+  // a persistent grid of the CTAs that fit on an SM together (48 registers a
+  // thread never limit them); resident CTAs never wait on one another for
+  // tensor memory (512 columns)
+  const int per_sm = std::max(1, ctas(smem));
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
   conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols, n_halos);
