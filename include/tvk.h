@@ -583,6 +583,12 @@ typedef struct tvk_cnn_conv {
   float* y2_f32;         /* FP32 output of channels >= split, or NULL (no split) */
   int split;
   int accumulate;        /* FP32 outputs: add to the values there */
+  /* 1: x1 is at half resolution, h1 x w1, and is read through a 2x nearest
+   * upsampling clamped at its last row and column (x1 pixel (min(y / 2, h1 - 1),
+   * min(x / 2, w1 - 1))), so a decoder layer needs no upsampled copy, also when
+   * h or w is odd; 0: x1 is h x w. */
+  int upsample1;
+  int h1, w1;
 } tvk_cnn_conv;
 
 typedef struct tvk_cnn_wgrad {

@@ -120,6 +120,41 @@ def test_gpu_conv3x3_forward_and_gradients(cuda_ok, case):
     np.testing.assert_allclose(host(db), dbr, rtol=1e-4, atol=1e-4)
 
 
+UP_CASES = [  # h, w (output), c1 (read upsampled from h // 2 x w // 2), c2, cout
+    (15, 21, 16, 16, 32),     # tcgen05
+    (15, 21, 4, 12, 32),      # mma.sync (c1 not a multiple of 8)
+    (300, 290, 32, 16, 32),   # tcgen05, many patches
+    (301, 289, 4, 12, 32),    # mma.sync, 16x16 patches
+]
+
+
+@pytest.mark.parametrize("case", UP_CASES, ids=[str(c) for c in UP_CASES])
+def test_gpu_conv3x3_upsampled_input(cuda_ok, case):
+    """A decoder layer reads the coarser level through the convolution's own
+    2x nearest upsampling, clamped at the coarse tensor's last row and column
+    when the output size is odd."""
+    h, w, c1, c2, cout = case
+    h1, w1 = h // 2, w // 2
+    rng = np.random.default_rng(h + w + c1)
+    x1 = K.bf16(rng.normal(size=(1, h1, w1, c1)))
+    x2 = K.bf16(rng.normal(size=(1, h, w, c2)))
+    wt = K.bf16(rng.normal(size=(9, cout, c1 + c2)) * (1.0 / np.sqrt(9 * (c1 + c2))))
+    b = rng.normal(size=cout) * 0.1
+    rows = np.minimum(np.arange(h) // 2, h1 - 1)
+    cols = np.minimum(np.arange(w) // 2, w1 - 1)
+    x = np.concatenate([x1[:, rows][:, :, cols], x2], axis=3)
+    yf = torch.empty((1, h, w, cout), dtype=torch.float32, device="cuda")
+    x1_t, x2_t = dev(x1, torch.bfloat16), dev(x2, torch.bfloat16)
+    wf, b32 = dev(wt, torch.bfloat16), dev(b, torch.float32)
+    a = N.CnnConv(x1=p(x1_t), x2=p(x2_t), c1=c1, c2=c2, n=1, h=h, w=w, weights=p(wf),
+                  bias=p(b32), cout=cout, slope=0.1, y_bf16=None, y_f32=p(yf), y2_f32=None,
+                  split=cout, accumulate=0, upsample1=1, h1=h1, w1=w1)
+    check(lib().tvk_cnn_conv3x3(C.byref(a), stream()))
+    check(lib().tvk_cnn_check(stream()))
+    _, yref = K.conv3x3(x, wt, b, 0.1)
+    np.testing.assert_allclose(host(yf), yref, rtol=1e-5, atol=1e-5)
+
+
 def test_gpu_pool_upsample_head(cuda_ok):
     rng = np.random.default_rng(5)
     x = K.bf16(rng.normal(size=(2, 6, 10, 32)))
@@ -127,6 +162,12 @@ def test_gpu_pool_upsample_head(cuda_ok):
     y = torch.empty((2, 3, 5, 32), dtype=torch.bfloat16, device="cuda")
     check(lib().tvk_cnn_avgpool2(p(xt), 2, 6, 10, 32, p(y), stream()))
     np.testing.assert_array_equal(host(y), K.bf16(K.avgpool2(x)))
+    # channel counts that are not a multiple of 8 take the one-value-per-thread path
+    x6 = K.bf16(rng.normal(size=(1, 6, 10, 6)))
+    x6t = dev(x6, torch.bfloat16)
+    y6 = torch.empty((1, 3, 5, 6), dtype=torch.bfloat16, device="cuda")
+    check(lib().tvk_cnn_avgpool2(p(x6t), 1, 6, 10, 6, p(y6), stream()))
+    np.testing.assert_array_equal(host(y6), K.bf16(K.avgpool2(x6)))
     u = torch.empty((2, 12, 20, 32), dtype=torch.bfloat16, device="cuda")
     check(lib().tvk_cnn_upsample2(p(xt), 2, 6, 10, 32, p(u), stream()))
     np.testing.assert_array_equal(host(u), K.upsample2(x))

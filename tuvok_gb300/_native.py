@@ -72,7 +72,8 @@ class CnnConv(C.Structure):
                 ("n", C.c_int), ("h", C.c_int), ("w", C.c_int), ("weights", C.c_void_p),
                 ("bias", C.c_void_p), ("cout", C.c_int), ("slope", C.c_float),
                 ("y_bf16", C.c_void_p), ("y_f32", C.c_void_p), ("y2_f32", C.c_void_p),
-                ("split", C.c_int), ("accumulate", C.c_int)]
+                ("split", C.c_int), ("accumulate", C.c_int), ("upsample1", C.c_int),
+                ("h1", C.c_int), ("w1", C.c_int)]
 
 
 class CnnWgrad(C.Structure):

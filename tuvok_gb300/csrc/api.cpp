@@ -1767,25 +1767,30 @@ void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int o
   const int h0 = N->hp, w0 = N->wp;
   const size_t px0 = size_t(h0) * w0, px1 = px0 / 4, px2 = px0 / 16, px3 = px0 / 64;
   // activation buffers (BF16 elements), carved from one allocation
-  const size_t sizes[] = {px0 * 32, px0 * 32, px1 * 32, px1 * 48, px1 * 48, px2 * 48, px2 * 64,
-                          px2 * 64, px3 * 64, px3 * 64, px2 * 64, px2 * 64, px1 * 64, px1 * 48,
-                          px0 * 48, px0 * 32};
+  constexpr int kBufs = 13;
+  const size_t sizes[kBufs] = {px0 * 32, px0 * 32, px1 * 32, px1 * 48, px1 * 48, px2 * 48, px2 * 64,
+                               px2 * 64, px3 * 64, px3 * 64, px2 * 64, px1 * 48, px0 * 32};
   size_t total = 0;
   for (size_t z : sizes) total += (z + 127) / 128 * 128;
   N->d_act.ensure(total * 2);
   N->d_head.ensure(px0 * 16 * sizeof(float));
-  void* buf[16];
+  void* buf[kBufs];
   size_t off = 0;
-  for (int i = 0; i < 16; ++i) {
+  for (int i = 0; i < kBufs; ++i) {
     buf[i] = static_cast<uint8_t*>(N->d_act.p) + off * 2;
     off += (sizes[i] + 127) / 128 * 128;
   }
   void *a0 = buf[0], *s0 = buf[1], *p0 = buf[2], *a1 = buf[3], *s1 = buf[4], *p1 = buf[5];
-  void *a2 = buf[6], *s2 = buf[7], *p2 = buf[8], *bt = buf[9], *u2 = buf[10], *d2 = buf[11];
-  void *u1 = buf[12], *d1 = buf[13], *u0 = buf[14], *d0 = buf[15];
-  auto conv = [&](int li, const void* x1, const void* x2, int h, int w, void* ybf, float* yf) {
+  void *a2 = buf[6], *s2 = buf[7], *p2 = buf[8], *bt = buf[9], *d2 = buf[10], *d1 = buf[11];
+  void *d0 = buf[12];
+  // up_h > 0: x1 is the coarser level's up_h x up_w output, upsampled on the fly
+  auto conv = [&](int li, const void* x1, const void* x2, int h, int w, void* ybf, float* yf,
+                  int up_h = 0, int up_w = 0) {
     const UNetLayer& L = kUNet[li];
     CnnConv c{};
+    c.upsample1 = up_h > 0 ? 1 : 0;
+    c.h1 = up_h;
+    c.w1 = up_w;
     c.x1 = x1;
     c.x2 = x2;
     c.c1 = L.c1;
@@ -1812,14 +1817,24 @@ void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int o
   conv(5, a2, nullptr, h0 / 4, w0 / 4, s2, nullptr);
   cnn_avgpool2(s2, 1, h0 / 4, w0 / 4, 64, p2, s);
   conv(6, p2, nullptr, h0 / 8, w0 / 8, bt, nullptr);
-  cnn_upsample2(bt, 1, h0 / 8, w0 / 8, 64, u2, s);
-  conv(7, u2, s2, h0 / 4, w0 / 4, d2, nullptr);
-  cnn_upsample2(d2, 1, h0 / 4, w0 / 4, 64, u1, s);
-  conv(8, u1, s1, h0 / 2, w0 / 2, d1, nullptr);
-  cnn_upsample2(d1, 1, h0 / 2, w0 / 2, 48, u0, s);
-  conv(9, u0, s0, h0, w0, d0, nullptr);
-  conv(10, d0, nullptr, h0, w0, nullptr, N->d_head.as<float>());
-  cnn_head(N->d_head.as<float>(), base_out, 1, h0, w0, out_h, out_w, base_out, s);
+  conv(7, bt, s2, h0 / 4, w0 / 4, d2, nullptr, h0 / 8, w0 / 8);
+  conv(8, d2, s1, h0 / 2, w0 / 2, d1, nullptr, h0 / 4, w0 / 4);
+  conv(9, d1, s0, h0, w0, d0, nullptr, h0 / 2, w0 / 2);
+  // the head's residual, pixel-shuffled into the upscaled frame by the epilogue
+  const UNetLayer& H = kUNet[10];
+  CnnConv c{};
+  c.x1 = d0;
+  c.c1 = H.c1;
+  c.n = 1;
+  c.h = h0;
+  c.w = w0;
+  c.weights = static_cast<const uint16_t*>(N->d_w.p) + N->w_off[10];
+  c.bias = N->d_b.as<float>() + N->b_off[10];
+  c.cout = H.cout;
+  c.slope = H.slope;
+  c.y_f32 = N->d_head.as<float>();
+  c.split = H.cout;
+  cnn_conv3x3_shuffle(c, base_out, out_h, out_w, s);
 }
 
 // One learned frame: the reduced frame (half resolution, half sample rate) and
@@ -3358,6 +3373,10 @@ tvk_status tvk_cnn_conv3x3(const tvk_cnn_conv* a, void* stream) {
     REQUIRE(a->n >= 1 && a->h >= 1 && a->w >= 1, "empty tensor");
     REQUIRE(a->y_bf16 || a->y_f32, "no output");
     REQUIRE(!a->y2_f32 || (a->split > 0 && a->split < a->cout && a->y_f32), "bad split");
+    REQUIRE(!a->upsample1 || (a->h1 >= 1 && a->w1 >= 1 && a->h1 >= a->h / 2 &&
+                              a->w1 >= a->w / 2 && a->h1 <= (a->h + 1) / 2 &&
+                              a->w1 <= (a->w + 1) / 2),
+            "an upsampled input must be half the output size");
     tvk::cnn_conv3x3(*a, as_stream(stream));
   });
 }

@@ -57,7 +57,19 @@ struct ConvArgs {
   float* y2_f32;              // FP32 output of channels >= split or null
   int split;                  // channel where y2 starts (== cout: no split)
   int accumulate;             // FP32 outputs: add to the existing values
+  int up1, h1, w1;            // x1 read through a clamped 2x nearest upsampling of h1 x w1
+  // tcgen05 kernel only: the 16 output channels are a pixel-shuffled RGBA
+  // residual (channel c * 4 + dy * 2 + dx of pixel (y, x) -> channel c of pixel
+  // (2y + dy, 2x + dx)) added in place to this FP32 [oh][ow][4] image
+  float* shuffle;
+  int oh, ow;
 };
+
+// Pixel index of x1 for output-grid pixel (yy, xx) of image img.
+__device__ __forceinline__ size_t x1_pixel(const ConvArgs& a, int img, int yy, int xx) {
+  if (!a.up1) return (size_t(img) * a.h + yy) * a.w + xx;
+  return (size_t(img) * a.h1 + min(yy >> 1, a.h1 - 1)) * a.w1 + min(xx >> 1, a.w1 - 1);
+}
 
 template <int kNT>  // n-tiles of 8 output channels
 __global__ void __launch_bounds__(kThreads) conv3x3_kernel(const ConvArgs a) {
@@ -82,7 +94,7 @@ __global__ void __launch_bounds__(kThreads) conv3x3_kernel(const ConvArgs a) {
     uint32_t v = 0;
     if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
       const size_t p = (size_t(img) * a.h + yy) * a.w + xx;
-      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + p * a.c1 + c)
+      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + x1_pixel(a, img, yy, xx) * a.c1 + c)
                    : *reinterpret_cast<const uint32_t*>(a.x2 + p * a.c2 + (c - a.c1));
     }
     *reinterpret_cast<uint32_t*>(halo + pix * cpad + c) = v;
@@ -184,7 +196,7 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
     uint32_t v = 0;
     if (yy >= 0 && yy < a.h && xx >= 0 && xx < a.w) {
       const size_t p = (size_t(img) * a.h + yy) * a.w + xx;
-      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + p * a.c1 + c)
+      v = c < a.c1 ? *reinterpret_cast<const uint32_t*>(a.x1 + x1_pixel(a, img, yy, xx) * a.c1 + c)
                    : *reinterpret_cast<const uint32_t*>(a.x2 + p * a.c2 + (c - a.c1));
     }
     *reinterpret_cast<uint32_t*>(halo + pix * cpad + c) = v;
@@ -388,10 +400,10 @@ __global__ void __launch_bounds__(kThreads)
       const int c = i % kTcHC, r = (i / kTcHC) % kTcHR, kc = i / (kTcHC * kTcHR);
       const int yy = y0 + r, xx = x0 + c;
       const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
-      const size_t p = in ? (size_t(img) * a.h + yy) * a.w + xx : 0;
       const int ch = kc * 8;
       const __nv_bfloat16* src =
-          ch < a.c1 ? a.x1 + p * a.c1 + ch : a.x2 + p * a.c2 + (ch - a.c1);
+          ch < a.c1 ? a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1 + ch
+                    : a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2 + (ch - a.c1);
       cp_async16(dst + uint32_t(i) * 16, src, in);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -487,6 +499,21 @@ __global__ void __launch_bounds__(kThreads)
         const int co = c0 + e;
         if (a.bias) v[e] += a.bias[co];
         if (a.slope >= 0.0f && v[e] < 0.0f) v[e] *= a.slope;
+      }
+      if (a.shuffle) {  // cout == 16: the whole 2 x 2 block of output pixels
+#pragma unroll
+        for (int sub = 0; sub < 4; ++sub) {
+          const int yy = 2 * oy + (sub >> 1), xx = 2 * ox + (sub & 1);
+          if (yy >= a.oh || xx >= a.ow) continue;
+          float4* o = reinterpret_cast<float4*>(a.shuffle) + (size_t(img) * a.oh + yy) * a.ow + xx;
+          float4 q = *o;
+          q.x += v[sub];
+          q.y += v[4 + sub];
+          q.z += v[8 + sub];
+          q.w += v[12 + sub];
+          *o = q;
+        }
+        continue;
       }
       if (a.y_bf16) {
         uint32_t w8[8];
@@ -676,6 +703,38 @@ __global__ void avgpool2_backward_kernel(const float* __restrict__ dy, int n, in
     const size_t o = ((size_t(img) * (h / 2) + yy / 2) * (w / 2) + xx / 2) * c + ch;
     const float v = dy[o] * 0.25f;
     dx[i] = accumulate ? dx[i] + v : v;
+  }
+}
+
+// The same, eight channels (16 bytes) per thread; c8 = channels / 8.
+__global__ void avgpool2_vec8_kernel(const uint4* __restrict__ x, int n, int h, int w, int c8,
+                                     uint4* __restrict__ y) {
+  const int ho = h / 2, wo = w / 2;
+  const size_t total = size_t(n) * ho * wo * c8;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int ch = int(i % c8);
+    const size_t p = i / c8;
+    const int xo = int(p % wo), yo = int((p / wo) % ho), img = int(p / (size_t(wo) * ho));
+    const size_t b = ((size_t(img) * h + 2 * yo) * w + 2 * xo) * c8 + ch;
+    uint4 q[4] = {x[b], x[b + c8], x[b + size_t(w) * c8], x[b + size_t(w) * c8 + c8]};
+    const __nv_bfloat16* e[4];
+    for (int k = 0; k < 4; ++k) e[k] = reinterpret_cast<const __nv_bfloat16*>(&q[k]);
+    uint4 r;
+    uint32_t* rw = reinterpret_cast<uint32_t*>(&r);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      __nv_bfloat16 o[2];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int k = 2 * j + t;
+        const float s = (__bfloat162float(e[0][k]) + __bfloat162float(e[1][k])) +
+                        (__bfloat162float(e[2][k]) + __bfloat162float(e[3][k]));
+        o[t] = __float2bfloat16_rn(s * 0.25f);
+      }
+      rw[j] = pack_bf16(o[0], o[1]);
+    }
+    y[i] = r;
   }
 }
 
@@ -886,6 +945,30 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
 
 }  // namespace
 
+void cnn_conv3x3_shuffle(const CnnConv& c, float* out, int oh, int ow, cudaStream_t s) {
+  ConvArgs a{};
+  a.x1 = static_cast<const __nv_bfloat16*>(c.x1);
+  a.c1 = c.c1;
+  a.n = c.n;
+  a.h = c.h;
+  a.w = c.w;
+  a.wt = static_cast<const __nv_bfloat16*>(c.weights);
+  a.bias = c.bias;
+  a.cout = c.cout;
+  a.slope = c.slope;
+  a.split = c.cout;
+  a.shuffle = out;
+  a.oh = oh;
+  a.ow = ow;
+  if (c.cout == 16 && c.c2 == 0 && !c.upsample1 &&
+      (reinterpret_cast<uintptr_t>(out) & 15u) == 0 && launch_conv_tc(a, s))
+    return;
+  // other shapes: the FP32 convolution, then the shuffle as its own pass
+  if (!c.y_f32) fail(TVK_ERR_INTERNAL, "shuffle convolution without a fallback buffer");
+  cnn_conv3x3(c, s);
+  cnn_head(c.y_f32, out, c.n, c.h, c.w, oh, ow, out, s);
+}
+
 uint32_t cnn_tc_timeouts(bool reset) {
   uint32_t n = 0;
   TVK_CUDA(cudaMemcpyFromSymbol(&n, g_cnn_tc_timeouts, sizeof(n)));
@@ -914,6 +997,9 @@ void cnn_conv3x3(const CnnConv& c, cudaStream_t s) {
   a.y2_f32 = c.y2_f32;
   a.split = c.y2_f32 ? c.split : c.cout;
   a.accumulate = c.accumulate;
+  a.up1 = c.upsample1 ? 1 : 0;
+  a.h1 = c.h1;
+  a.w1 = c.w1;
   const int cin = c.c1 + c.c2;
   const int nt = (c.cout + 7) / 8;
   if (launch_conv_tc(a, s)) return;
@@ -1024,8 +1110,15 @@ void cnn_act_grad(const float* dy, const void* y, float slope, void* g, size_t n
 }
 
 void cnn_avgpool2(const void* x, int n, int h, int w, int c, void* y, cudaStream_t s) {
-  avgpool2_kernel<<<grid_for(size_t(n) * (h / 2) * (w / 2) * c), 256, 0, s>>>(
-      static_cast<const __nv_bfloat16*>(x), n, h, w, c, static_cast<__nv_bfloat16*>(y));
+  const bool vec = c % 8 == 0 && (reinterpret_cast<uintptr_t>(x) & 15u) == 0 &&
+                   (reinterpret_cast<uintptr_t>(y) & 15u) == 0;
+  if (vec) {
+    avgpool2_vec8_kernel<<<grid_for(size_t(n) * (h / 2) * (w / 2) * (c / 8)), 256, 0, s>>>(
+        static_cast<const uint4*>(x), n, h, w, c / 8, static_cast<uint4*>(y));
+  } else {
+    avgpool2_kernel<<<grid_for(size_t(n) * (h / 2) * (w / 2) * c), 256, 0, s>>>(
+        static_cast<const __nv_bfloat16*>(x), n, h, w, c, static_cast<__nv_bfloat16*>(y));
+  }
   TVK_CUDA(cudaGetLastError());
 }
 

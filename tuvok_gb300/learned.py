@@ -102,12 +102,15 @@ class UNet:
         return {n: (d[n + "_w"], d[n + "_b"]) for n, *_ in ARCH}
 
     # ---- kernels
-    def _conv(self, name, x1, x2, n, h, w, y_bf16=None, y_f32=None):
+    def _conv(self, name, x1, x2, n, h, w, y_bf16=None, y_f32=None, up=None):
+        """up = (h1, w1): x1 is the coarser level's output, read through the
+        convolution's clamped 2x upsampling."""
         L = self.layers[name]
         a = N.CnnConv(x1=_p(x1), x2=_p(x2), c1=L["c1"], c2=L["c2"], n=n, h=h, w=w,
                       weights=_p(L["wf"]), bias=_p(L["b"]), cout=L["cout"], slope=L["slope"],
                       y_bf16=_p(y_bf16), y_f32=_p(y_f32), y2_f32=None, split=L["cout"],
-                      accumulate=0)
+                      accumulate=0, upsample1=1 if up else 0, h1=up[0] if up else 0,
+                      w1=up[1] if up else 0)
         check(lib().tvk_cnn_conv3x3(C.byref(a), self.stream()))
 
     def _new(self, n, h, w, c, dtype=None):
@@ -119,20 +122,15 @@ class UNet:
         n, h, w, _ = x16.shape
         S = {"x": x16}
 
-        def conv(name, a, b, hh, ww):
+        def conv(name, a, b, hh, ww, up=None):
             y = self._new(n, hh, ww, self.layers[name]["cout"])
-            self._conv(name, S[a], S[b] if b else None, n, hh, ww, y_bf16=y)
+            self._conv(name, S[a], S[b] if b else None, n, hh, ww, y_bf16=y, up=up)
             S[name] = y
 
         def pool(src, dst, hh, ww):
             c = S[src].shape[3]
             S[dst] = self._new(n, hh // 2, ww // 2, c)
             check(lib().tvk_cnn_avgpool2(_p(S[src]), n, hh, ww, c, _p(S[dst]), self.stream()))
-
-        def up(src, dst, hh, ww):
-            c = S[src].shape[3]
-            S[dst] = self._new(n, 2 * hh, 2 * ww, c)
-            check(lib().tvk_cnn_upsample2(_p(S[src]), n, hh, ww, c, _p(S[dst]), self.stream()))
 
         conv("e0a", "x", None, h, w)
         conv("e0b", "e0a", None, h, w)
@@ -144,12 +142,10 @@ class UNet:
         conv("e2b", "e2a", None, h // 4, w // 4)
         pool("e2b", "p2", h // 4, w // 4)
         conv("b", "p2", None, h // 8, w // 8)
-        up("b", "u2", h // 8, w // 8)
-        conv("d2", "u2", "e2b", h // 4, w // 4)
-        up("d2", "u1", h // 4, w // 4)
-        conv("d1", "u1", "e1b", h // 2, w // 2)
-        up("d1", "u0", h // 2, w // 2)
-        conv("d0", "u0", "e0b", h, w)
+        # decoder layers read the coarser level upsampled on the fly
+        conv("d2", "b", "e2b", h // 4, w // 4, up=(h // 8, w // 8))
+        conv("d1", "d2", "e1b", h // 2, w // 2, up=(h // 4, w // 4))
+        conv("d0", "d1", "e0b", h, w, up=(h // 2, w // 2))
         hd = self._new(n, h, w, 16, self.torch.float32)
         self._conv("head", S["d0"], None, n, h, w, y_f32=hd)
         S["head"] = hd
@@ -187,6 +183,15 @@ class UNet:
         t = self.torch
         n, h, w = self.shape
         st = self.stream()
+        if h % 8 or w % 8:
+            raise ValueError("training sizes must be multiples of 8")
+        S = self.S
+        # the decoders' upsampled inputs, which the weight gradients read
+        for src, dst, hh, ww in (("b", "u2", h // 8, w // 8), ("d2", "u1", h // 4, w // 4),
+                                 ("d1", "u0", h // 2, w // 2)):
+            c = S[src].shape[3]
+            S[dst] = t.empty((n, 2 * hh, 2 * ww, c), dtype=t.bfloat16, device="cuda")
+            check(lib().tvk_cnn_upsample2(_p(S[src]), n, hh, ww, c, _p(S[dst]), st))
         dh = t.empty((n, h, w, 16), dtype=t.float32, device="cuda")
         check(lib().tvk_cnn_head_backward(_p(dout), n, h, w, _p(dh), st))
 
