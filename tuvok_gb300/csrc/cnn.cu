@@ -301,7 +301,8 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 // matrices (channel octets) 2880 bytes apart.  No im2col copy is made.  One
 // thread issues the 9 x cin / 16 MMAs of a patch and commits them to an
 // mbarrier; the four warps then read their 32 TMEM lanes (pixels) and run the
-// epilogue of the other kernels.
+// epilogue of the other kernels.  The halos of the following patches stream in
+// with cp.async meanwhile, through a ring of up to 4 buffers.
 constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
 constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
 constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
@@ -377,6 +378,8 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
 
 __global__ void __launch_bounds__(kThreads)
     conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
+  // n_halos halo buffers in a ring (1 to 4): the halos of the next n_halos - 1
+  // patches are in flight while a patch's MMAs and epilogue run
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
@@ -391,8 +394,12 @@ __global__ void __launch_bounds__(kThreads)
   const int n_tiles = a.n * tiles_x * tiles_y;
 
   // the halo of patch t into halo buffer `buf`, 8 channels per 16-byte copy,
-  // zero outside the image
+  // zero outside the image; one cp.async group per call (empty past the last patch)
   auto load_halo = [&](int t, int buf) {
+    if (t >= n_tiles) {
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      return;
+    }
     const int img = t / (tiles_x * tiles_y);
     const int y0 = ((t / tiles_x) % tiles_y) * kTcRows - 1, x0 = (t % tiles_x) * kTcCols - 1;
     const uint32_t dst = halo_a + uint32_t(buf) * halo_bytes;
@@ -428,7 +435,8 @@ __global__ void __launch_bounds__(kThreads)
     cp_async16(w_a + uint32_t(i) * 16, a.wt + (size_t(tap) * cout + co) * cin + kc * 8, true);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
-  if (int(blockIdx.x) < n_tiles) load_halo(blockIdx.x, 0);
+  const int stride = int(gridDim.x);
+  for (int k = 0; k < max(1, n_halos - 1); ++k) load_halo(int(blockIdx.x) + k * stride, k);
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -438,12 +446,22 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t lbo_b = uint32_t(cout) * 16, sbo_b = 128;
   uint32_t phase = 0;
   bool ok = true;
-  int buf = 0;
+  int k = 0;  // this CTA's patch counter: patch blockIdx.x + k * gridDim.x, buffer k % n_halos
 
-  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-    const int tn = t + int(gridDim.x);
-    // this patch's halo has landed (the only copies in flight)
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
+  for (int t = blockIdx.x; t < n_tiles; t += stride, ++k) {
+    const int buf = k % n_halos;
+    if (n_halos >= 2) {
+      // the ring's free buffer (patch k - 1's, whose MMAs are done) takes the
+      // patch n_halos - 1 ahead; then patch k's group, the oldest, has landed
+      load_halo(t + (n_halos - 1) * stride, (k + n_halos - 1) % n_halos);
+      switch (n_halos) {
+        case 2: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+        case 3: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+      }
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
     // make the copies visible to the tensor cores' (async proxy) reads
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
@@ -471,8 +489,6 @@ __global__ void __launch_bounds__(kThreads)
               bar_a)
           : "memory");
     }
-    // with two halo buffers the next patch's halo streams in under the MMAs
-    if (n_halos == 2 && tn < n_tiles) load_halo(tn, buf ^ 1);
     if (tid == 0 && !mbar_wait_bounded(bar_a, phase)) *flag = 1;
     __syncthreads();
     phase ^= 1u;
@@ -480,8 +496,9 @@ __global__ void __launch_bounds__(kThreads)
       ok = false;
       break;
     }
-    // with one, under the epilogue (the MMAs no longer read it)
-    if (n_halos == 1 && tn < n_tiles) load_halo(tn, 0);
+    // with one buffer the next halo streams in under the epilogue (the MMAs
+    // no longer read it)
+    if (n_halos == 1) load_halo(t + stride, 0);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     // epilogue: warp w holds TMEM lanes (pixels) 32w .. 32w + 31
     const int img = t / (tiles_x * tiles_y);
@@ -547,7 +564,6 @@ __global__ void __launch_bounds__(kThreads)
     }
     // TMEM read before the next patch's MMAs overwrite it
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    if (n_halos == 2) buf ^= 1;
   }
   if (!ok && tid == 0) {
     atomicAdd(&g_cnn_tc_timeouts, 1u);
@@ -891,7 +907,7 @@ uint32_t grid_for(size_t n) {
   return uint32_t(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
 }
 
-// Shared memory of conv3x3_tc_kernel: control words, one or two halos, the
+// Shared memory of conv3x3_tc_kernel: control words, a ring of halos, the
 // weights.  Every MMA descriptor stays inside its operand: the A operand of
 // the last K step of tap (2, 2) ends at ((2 (kc/2 - 1) * 18 + 2) * 10 + 2) * 16
 // + 2880 + 15 * 160 + 128 <= kc * 2880 bytes, and B's at the end of the weights.
@@ -903,9 +919,7 @@ size_t conv_tc_smem(int cin, int cout, int n_halos) {
 // The tcgen05 convolution takes the launch when its shapes fit: input and
 // output channels multiples of 16 (M = 128, N = cout, K steps of 16), at most
 // 128 output channels (a power-of-two TMEM allocation of 32 to 128 columns),
-// 16-byte aligned tensors, and halo + weights in shared memory.  A second halo
-// buffer (the next patch's input streaming in under the MMAs) is used when
-// it fits and costs no CTA per SM.
+// 16-byte aligned tensors, and halo + weights in shared memory.
 bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   const int cin = a.c1 + a.c2;
   auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
@@ -916,15 +930,26 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     return false;
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
-  const int tmem_ctas = int(512 / cols);
-  // CTAs per SM by shared memory (each also reserves 1 KB), tensor memory and threads
-  auto ctas = [&](size_t smem) {
-    return std::min({int(kSmPerSm / (smem + kReserved)), tmem_ctas, 2048 / kThreads});
+  const int max_ctas = std::min(int(512 / cols), 2048 / kThreads);  // tensor memory, threads
+  // The most CTAs per SM whose shared memory (each also reserves 1 KB) holds a
+  // ring of 3 halos (2 patches in flight); else one CTA with the deepest ring
+  // that fits, up to 4.
+  const size_t halo = size_t(cin) / 8 * kTcHR * kTcHC * 16;
+  const size_t base = conv_tc_smem(cin, a.cout, 0);
+  auto ring = [&](int c) {
+    const size_t per = kSmPerSm / size_t(c) - kReserved;
+    const size_t room = std::min(per, kMaxSmem);
+    return room > base ? int(std::min<size_t>((room - base) / halo, 4)) : 0;
   };
-  const size_t one = conv_tc_smem(cin, a.cout, 1), two = conv_tc_smem(cin, a.cout, 2);
-  if (one > kMaxSmem) return false;
-  const int n_halos = (two <= kMaxSmem && ctas(two) >= std::min(ctas(one), 2)) ? 2 : 1;
-  const size_t smem = n_halos == 2 ? two : one;
+  int per_sm = 1, n_halos = ring(1);
+  for (int c = max_ctas; c >= 1; --c)
+    if (ring(c) >= 3) {
+      per_sm = c;
+      n_halos = ring(c);
+      break;
+    }
+  if (n_halos < 1) return false;
+  const size_t smem = conv_tc_smem(cin, a.cout, n_halos);
   TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem)));
   TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -935,7 +960,6 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   // a persistent grid of the CTAs that fit on an SM together (48 registers a
   // thread never limit them); resident CTAs never wait on one another for
   // tensor memory (512 columns)
-  const int per_sm = std::max(1, ctas(smem));
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
   conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols, n_halos);
