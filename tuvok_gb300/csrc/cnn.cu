@@ -376,15 +376,10 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
                : "memory");
 }
 
-constexpr int kTcMaxCtas = 8;  // CTAs per SM the register budget leaves room for
-
-__global__ void __launch_bounds__(kThreads, kTcMaxCtas)
-    conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos, int n_acc) {
+__global__ void __launch_bounds__(kThreads)
+    conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
   // n_halos halo buffers in a ring (1 to 4): the halos of the next n_halos - 1
-  // patches are in flight while a patch's MMAs and epilogue run.  n_acc (1, 2
-  // or 4) accumulators of tmem_cols / n_acc columns each: MMA j of a patch adds
-  // into accumulator j % n_acc, so n_acc dependency chains run side by side on
-  // the tensor cores, and the epilogue sums them.
+  // patches are in flight while a patch's MMAs and epilogue run
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
@@ -480,19 +475,17 @@ __global__ void __launch_bounds__(kThreads, kTcMaxCtas)
       uint64_t bd = tc_desc(w_a, lbo_b, sbo_b);
       const int ksteps = kc_n / 2;
       const uint64_t a_step = 2 * kTcHR * kTcHC, b_step = uint64_t(2 * cout);
-      const uint32_t acc_cols = tmem_cols / uint32_t(n_acc);
-      int j = 0;
+      uint32_t acc = 0;
 #pragma unroll
       for (int tap = 0; tap < 9; ++tap) {
         uint64_t ad = a0 + uint64_t((tap / 3) * kTcHC + tap % 3);
-        for (int s = 0; s < ksteps; ++s, ++j) {
-          const int chain = j & (n_acc - 1);
+        for (int s = 0; s < ksteps; ++s) {
           asm volatile(
               "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-                  tmem + uint32_t(chain) * acc_cols),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(uint32_t(j >= n_acc))
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
               : "memory");
+          acc = 1;
           ad += a_step;
           bd += b_step;
         }
@@ -520,18 +513,9 @@ __global__ void __launch_bounds__(kThreads, kTcMaxCtas)
     const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
     const bool live = oy < a.h && ox < a.w;
     const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
-    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
-    const uint32_t acc_cols = tmem_cols / uint32_t(n_acc);
-    const int chains = min(n_acc, 9 * (kc_n / 2));  // accumulators that received an MMA
     for (int c0 = 0; c0 < cout; c0 += 16) {
       float v[16];
-      tc_ld16(lane_base + uint32_t(c0), v);
-      for (int ch = 1; ch < chains; ++ch) {
-        float u[16];
-        tc_ld16(lane_base + uint32_t(ch) * acc_cols + uint32_t(c0), u);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) v[e] += u[e];
-      }
+      tc_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
       if (!live) continue;
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
@@ -952,7 +936,7 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     return false;
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
-  const int max_ctas = std::min(int(512 / cols), kTcMaxCtas);  // tensor memory, registers
+  const int max_ctas = std::min(int(512 / cols), 2048 / kThreads);  // tensor memory, threads
   // The most CTAs per SM whose shared memory (each also reserves 1 KB) holds a
   // ring of 2 halos, each with the deepest ring (up to 4) its share holds; else
   // one CTA with one halo.  (More CTAs per SM measured faster than deeper
@@ -983,13 +967,9 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   // a persistent grid of the CTAs that fit on an SM together (48 registers a
   // thread never limit them); resident CTAs never wait on one another for
   // tensor memory (512 columns)
-  // independent accumulation chains in the tensor memory the resident CTAs
-  // leave free (successive MMAs into one accumulator serialise)
-  int n_acc = 4;
-  while (n_acc > 1 && uint32_t(per_sm) * cols * uint32_t(n_acc) > 512u) n_acc /= 2;
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
-  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols * uint32_t(n_acc), n_halos, n_acc);
+  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols, n_halos);
   TVK_CUDA(cudaGetLastError());
   return true;
 }
