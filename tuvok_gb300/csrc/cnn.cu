@@ -403,15 +403,19 @@ __global__ void __launch_bounds__(kThreads)
     const int img = t / (tiles_x * tiles_y);
     const int y0 = ((t / tiles_x) % tiles_y) * kTcRows - 1, x0 = (t % tiles_x) * kTcCols - 1;
     const uint32_t dst = halo_a + uint32_t(buf) * halo_bytes;
-    for (int i = tid; i < kc_n * kTcHR * kTcHC; i += kThreads) {
-      const int c = i % kTcHC, r = (i / kTcHC) % kTcHR, kc = i / (kTcHC * kTcHR);
-      const int yy = y0 + r, xx = x0 + c;
+    constexpr int kPos = kTcHR * kTcHC;  // 180 halo pixels; a thread takes one or two
+    const int kc1 = a.c1 / 8;
+    for (int pos = tid; pos < kPos; pos += kThreads) {
+      const int yy = y0 + pos / kTcHC, xx = x0 + pos % kTcHC;
       const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
-      const int ch = kc * 8;
-      const __nv_bfloat16* src =
-          ch < a.c1 ? a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1 + ch
-                    : a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2 + (ch - a.c1);
-      cp_async16(dst + uint32_t(i) * 16, src, in);
+      // the pixel's channels are contiguous: one 16-byte copy per octet
+      const __nv_bfloat16* s1 = a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1;
+      uint32_t d = dst + uint32_t(pos) * 16;
+      for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) cp_async16(d, s1 + kc * 8, in);
+      if (kc1 < kc_n) {
+        const __nv_bfloat16* s2 = a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2;
+        for (int kc = 0; kc < kc_n - kc1; ++kc, d += kPos * 16) cp_async16(d, s2 + kc * 8, in);
+      }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
