@@ -147,52 +147,6 @@ brick_copy_kernel(const T* __restrict__ raw, BrickGrid g, const uint64_t* __rest
       // segment that ends inside the volume: no per-voxel clamping or limits
       const uint64_t src0 = xbase + rowbase - ov;
       const bool fast = live && !fx && !lx && src0 + bs[0] <= g.total;
-      if constexpr (sizeof(T) == 2) {
-        // 16-bit voxels two at a time where the row's output starts on a
-        // 4-byte boundary: 32-bit stores, and 32-bit loads of the source line
-        // (realigned by a funnel shift when it starts on an odd voxel; that
-        // reads one voxel past the segment, so the line must go on)
-        const uint64_t obase = offsets[b] + (uint64_t(k) * bs[1] + j) * bs[0];
-        const bool odd = (src0 & 1) != 0;
-        if (fast && (bs[0] & 1) == 0 && (obase & 1) == 0 &&
-            (reinterpret_cast<uintptr_t>(raw) & 3u) == 0 &&
-            (reinterpret_cast<uintptr_t>(pool) & 3u) == 0 &&
-            (!odd || src0 + bs[0] + 1 <= g.total)) {
-          const uint32_t nw = bs[0] / 2;
-          const uint32_t* sw = reinterpret_cast<const uint32_t*>(raw) + (src0 >> 1);
-          uint32_t* ow = reinterpret_cast<uint32_t*>(pool + obase);
-          constexpr uint32_t kW = 3;  // 96 words a pass: a 130-voxel row in one
-          for (uint32_t m0 = 0; m0 < nw; m0 += 32 * kW) {
-            uint32_t w[kW];
-#pragma unroll
-            for (uint32_t u = 0; u < kW; ++u) {
-              const uint32_t m = m0 + 32 * u + lane;
-              w[u] = 0;
-              if (m < nw) {
-                const uint32_t a0 = __ldg(sw + m);
-                w[u] = odd ? __funnelshift_r(a0, __ldg(sw + m + 1), 16) : a0;
-              }
-            }
-#pragma unroll
-            for (uint32_t u = 0; u < kW; ++u) {
-              const uint32_t m = m0 + 32 * u + lane;
-              if (m0 + 32 * u >= nw) break;  // warp-uniform
-              const bool act = m < nw;
-              const uint32_t v0 = w[u] & 0xffffu, v1 = w[u] >> 16, i0 = 2 * m;
-              if (act) {
-                ow[m] = w[u];
-                lo = min(lo, min(v0, v1));
-                hi = max(hi, max(v0, v1));
-              }
-              hist_add_warp(gh, sc.hist, smem_bins,
-                            act && inner_row && i0 >= ov && i0 < bs[0] - ov, v0, lane);
-              hist_add_warp(gh, sc.hist, smem_bins,
-                            act && inner_row && i0 + 1 >= ov && i0 + 1 < bs[0] - ov, v1, lane);
-            }
-          }
-          continue;
-        }
-      }
       // kUnroll row segments of 32 voxels per pass: their loads are all in
       // flight before the first store
       for (uint32_t base = 0; base < bs[0]; base += 32 * kUnroll) {
