@@ -306,6 +306,11 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
 constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
 constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
+// halos each CTA's shared memory must hold at least (the launch takes the most
+// CTAs per SM for which it does)
+#ifndef TVK_TC_MIN_HALOS
+#define TVK_TC_MIN_HALOS 2
+#endif
 // longest wait for the tensor cores to finish a patch before the kernel gives
 // up (reported through g_cnn_tc_timeouts); a patch takes microseconds
 constexpr uint64_t kTcWaitNs = 2000000000ull;
@@ -954,7 +959,7 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   };
   int per_sm = 1, n_halos = ring(1);
   for (int c = max_ctas; c >= 1; --c)
-    if (ring(c) >= 2) {
+    if (ring(c) >= TVK_TC_MIN_HALOS) {
       per_sm = c;
       n_halos = ring(c);
       break;
