@@ -306,11 +306,6 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
 constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
 constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
-// halos each CTA's shared memory must hold at least (the launch takes the most
-// CTAs per SM for which it does)
-#ifndef TVK_TC_MIN_HALOS
-#define TVK_TC_MIN_HALOS 2
-#endif
 // longest wait for the tensor cores to finish a patch before the kernel gives
 // up (reported through g_cnn_tc_timeouts); a patch takes microseconds
 constexpr uint64_t kTcWaitNs = 2000000000ull;
@@ -385,13 +380,13 @@ __global__ void __launch_bounds__(kThreads)
     conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
   // n_halos halo buffers in a ring (1 to 4): the halos of the next n_halos - 1
   // patches are in flight while a patch's MMAs and epilogue run
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_tc[];
   const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_raw + 8);
-  int* flag = reinterpret_cast<int*>(smem_raw + 12);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_tc);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_tc + 8);
+  int* flag = reinterpret_cast<int*>(smem_tc + 12);
   const uint32_t halo_bytes = uint32_t(kc_n) * kTcHR * kTcHC * 16;
-  unsigned char* halo0 = smem_raw + kTcCtrlBytes;                 // n_halos x [kc][18][10][8]
+  unsigned char* halo0 = smem_tc + kTcCtrlBytes;                 // n_halos x [kc][18][10][8]
   unsigned char* wsm = halo0 + size_t(n_halos) * halo_bytes;      // [9][kc][cout][8]
   const uint32_t bar_a = smem_addr(bar), halo_a = smem_addr(halo0), w_a = smem_addr(wsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -946,10 +941,13 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
   const int max_ctas = std::min(int(512 / cols), 2048 / kThreads);  // tensor memory, threads
-  // The most CTAs per SM whose shared memory (each also reserves 1 KB) holds a
-  // ring of 2 halos, each with the deepest ring (up to 4) its share holds; else
-  // one CTA with one halo.  (More CTAs per SM measured faster than deeper
-  // rings: 104 against 174 us for 960x540, 80 -> 32 channels.)
+  // CTAs per SM and halos per CTA (each CTA also reserves 1 KB of shared
+  // memory): the most CTAs whose shares hold 2 halos each (the next patch's
+  // input streaming in under the MMAs), when that is at least 3; otherwise the
+  // most CTAs that hold one.  Each CTA takes the deepest ring (up to 4) its
+  // share holds.  Measured on the network's layers at 960x540: 80 -> 32
+  // channels 85 us with 3 CTAs of one halo against 105 us with 2 of two; 16 ->
+  // 32 channels 51 us with 10 CTAs of two against 56 us with 13 of one.
   const size_t halo = size_t(cin) / 8 * kTcHR * kTcHC * 16;
   const size_t base = conv_tc_smem(cin, a.cout, 0);
   auto ring = [&](int c) {
@@ -957,13 +955,14 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     const size_t room = std::min(per, kMaxSmem);
     return room > base ? int(std::min<size_t>((room - base) / halo, 4)) : 0;
   };
-  int per_sm = 1, n_halos = ring(1);
-  for (int c = max_ctas; c >= 1; --c)
-    if (ring(c) >= TVK_TC_MIN_HALOS) {
-      per_sm = c;
-      n_halos = ring(c);
-      break;
-    }
+  auto most_ctas = [&](int min_halos) {
+    for (int c = max_ctas; c >= 1; --c)
+      if (ring(c) >= min_halos) return c;
+    return 0;
+  };
+  int per_sm = most_ctas(2);
+  if (per_sm < 3) per_sm = std::max(most_ctas(1), 1);
+  const int n_halos = ring(per_sm);
   if (n_halos < 1) return false;
   const size_t smem = conv_tc_smem(cin, a.cout, n_halos);
   TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
