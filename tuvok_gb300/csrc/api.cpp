@@ -1807,30 +1807,16 @@ void run_unet(tvk_learned* N, const void* x16, float* base_out, int out_h, int o
     c.split = L.cout;
     cnn_conv3x3(c, s);
   };
-  // the first layer of each coarser level reads the finer level average-pooled on the fly
-  auto conv_pooled = [&](int li, const void* x1, int h, int w, void* ybf, void* pooled) {
-    const UNetLayer& L = kUNet[li];
-    CnnConv c{};
-    c.x1 = x1;
-    c.c1 = L.c1;
-    c.n = 1;
-    c.h = h / 2;
-    c.w = w / 2;
-    c.weights = static_cast<const uint16_t*>(N->d_w.p) + N->w_off[li];
-    c.bias = N->d_b.as<float>() + N->b_off[li];
-    c.cout = L.cout;
-    c.slope = L.slope;
-    c.y_bf16 = ybf;
-    c.split = L.cout;
-    cnn_conv3x3_pooled(c, h, w, pooled, s);
-  };
   conv(0, x16, nullptr, h0, w0, a0, nullptr);
   conv(1, a0, nullptr, h0, w0, s0, nullptr);
-  conv_pooled(2, s0, h0, w0, a1, p0);
+  cnn_avgpool2(s0, 1, h0, w0, 32, p0, s);
+  conv(2, p0, nullptr, h0 / 2, w0 / 2, a1, nullptr);
   conv(3, a1, nullptr, h0 / 2, w0 / 2, s1, nullptr);
-  conv_pooled(4, s1, h0 / 2, w0 / 2, a2, p1);
+  cnn_avgpool2(s1, 1, h0 / 2, w0 / 2, 48, p1, s);
+  conv(4, p1, nullptr, h0 / 4, w0 / 4, a2, nullptr);
   conv(5, a2, nullptr, h0 / 4, w0 / 4, s2, nullptr);
-  conv_pooled(6, s2, h0 / 4, w0 / 4, bt, p2);
+  cnn_avgpool2(s2, 1, h0 / 4, w0 / 4, 64, p2, s);
+  conv(6, p2, nullptr, h0 / 8, w0 / 8, bt, nullptr);
   conv(7, bt, s2, h0 / 4, w0 / 4, d2, nullptr, h0 / 8, w0 / 8);
   conv(8, d2, s1, h0 / 2, w0 / 2, d1, nullptr, h0 / 4, w0 / 4);
   conv(9, d1, s0, h0, w0, d0, nullptr, h0 / 2, w0 / 2);

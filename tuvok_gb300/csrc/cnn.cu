@@ -58,9 +58,6 @@ struct ConvArgs {
   int split;                  // channel where y2 starts (== cout: no split)
   int accumulate;             // FP32 outputs: add to the existing values
   int up1, h1, w1;            // x1 read through a clamped 2x nearest upsampling of h1 x w1
-  // tcgen05 kernel only: x1 is at twice the resolution (h1 x w1) and each of
-  // its pixels is read as the mean of a 2 x 2 block, as avgpool2_kernel rounds it
-  int pool1;
   // tcgen05 kernel only: the 16 output channels are a pixel-shuffled RGBA
   // residual (channel c * 4 + dy * 2 + dx of pixel (y, x) -> channel c of pixel
   // (2y + dy, 2x + dx)) added in place to this FP32 [oh][ow][4] image
@@ -411,44 +408,10 @@ __global__ void __launch_bounds__(kThreads)
     for (int pos = tid; pos < kPos; pos += kThreads) {
       const int yy = y0 + pos / kTcHC, xx = x0 + pos % kTcHC;
       const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
+      // the pixel's channels are contiguous: one 16-byte copy per octet
+      const __nv_bfloat16* s1 = a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1;
       uint32_t d = dst + uint32_t(pos) * 16;
-      if (a.pool1) {
-        // the 2 x 2 block of the finer level, averaged in FP32 and rounded to
-        // BF16 as avgpool2_kernel does, stored with ordinary shared stores
-        const size_t row = size_t(a.w1) * a.c1;
-        const __nv_bfloat16* q =
-            a.x1 + (in ? ((size_t(img) * a.h1 + 2 * yy) * a.w1 + 2 * xx) * a.c1 : 0);
-        for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) {
-          uint32_t r[4] = {0u, 0u, 0u, 0u};
-          if (in) {
-            const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(q + kc * 8));
-            const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(q + a.c1 + kc * 8));
-            const uint4 v2 = __ldg(reinterpret_cast<const uint4*>(q + row + kc * 8));
-            const uint4 v3 = __ldg(reinterpret_cast<const uint4*>(q + row + a.c1 + kc * 8));
-            const uint32_t w0[4] = {v0.x, v0.y, v0.z, v0.w}, w1[4] = {v1.x, v1.y, v1.z, v1.w};
-            const uint32_t w2[4] = {v2.x, v2.y, v2.z, v2.w}, w3[4] = {v3.x, v3.y, v3.z, v3.w};
-            // a BF16 is the high half of the FP32 with the same bits
-            auto f = [](uint32_t w, int hi) { return __uint_as_float(hi ? w & 0xffff0000u : w << 16); };
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              __nv_bfloat16 o[2];
-#pragma unroll
-              for (int u = 0; u < 2; ++u) {
-                const float sum = (f(w0[j], u) + f(w1[j], u)) + (f(w2[j], u) + f(w3[j], u));
-                o[u] = __float2bfloat16_rn(sum * 0.25f);
-              }
-              r[j] = pack_bf16(o[0], o[1]);
-            }
-          }
-          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(d), "r"(r[0]),
-                       "r"(r[1]), "r"(r[2]), "r"(r[3])
-                       : "memory");
-        }
-      } else {
-        // the pixel's channels are contiguous: one 16-byte copy per octet
-        const __nv_bfloat16* s1 = a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1;
-        for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) cp_async16(d, s1 + kc * 8, in);
-      }
+      for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) cp_async16(d, s1 + kc * 8, in);
       if (kc1 < kc_n) {
         const __nv_bfloat16* s2 = a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2;
         for (int kc = 0; kc < kc_n - kc1; ++kc, d += kPos * 16) cp_async16(d, s2 + kc * 8, in);
@@ -1020,32 +983,6 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
 }
 
 }  // namespace
-
-void cnn_conv3x3_pooled(const CnnConv& c, int h1, int w1, void* pooled, cudaStream_t s) {
-  ConvArgs a{};
-  a.x1 = static_cast<const __nv_bfloat16*>(c.x1);
-  a.c1 = c.c1;
-  a.n = c.n;
-  a.h = c.h;
-  a.w = c.w;
-  a.wt = static_cast<const __nv_bfloat16*>(c.weights);
-  a.bias = c.bias;
-  a.cout = c.cout;
-  a.slope = c.slope;
-  a.y_bf16 = static_cast<__nv_bfloat16*>(c.y_bf16);
-  a.split = c.cout;
-  a.pool1 = 1;
-  a.h1 = h1;
-  a.w1 = w1;
-  if (c.c2 == 0 && !c.y_f32 && !c.upsample1 && h1 / 2 == c.h && w1 / 2 == c.w &&
-      launch_conv_tc(a, s))
-    return;
-  // other shapes: the pooling as its own pass into `pooled`, then the convolution
-  cnn_avgpool2(c.x1, c.n, h1, w1, c.c1, pooled, s);
-  CnnConv d = c;
-  d.x1 = pooled;
-  cnn_conv3x3(d, s);
-}
 
 void cnn_conv3x3_shuffle(const CnnConv& c, float* out, int oh, int ow, cudaStream_t s) {
   ConvArgs a{};

@@ -359,9 +359,6 @@ void launch_upscale(const float4* low, uint32_t lw, uint32_t lh, float4* out, ui
 using CnnConv = tvk_cnn_conv;
 using CnnWgrad = tvk_cnn_wgrad;
 void cnn_conv3x3(const CnnConv& c, cudaStream_t s);
-// c's convolution with its input x1 (c.c1 channels, h1 x w1) average-pooled 2x2
-// on the fly (avgpool2's rounding); `pooled` is the buffer of the unfused fallback.
-void cnn_conv3x3_pooled(const CnnConv& c, int h1, int w1, void* pooled, cudaStream_t s);
 // c's convolution (16 output channels) with the head's pixel shuffle fused:
 // out[oh][ow][4] += shuffle(conv); c.y_f32 is the buffer of the unfused fallback.
 void cnn_conv3x3_shuffle(const CnnConv& c, float* out, int oh, int ow, cudaStream_t s);
