@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 
 // ------------------------------------------------ convolution on tcgen05 / TMEM
 //
-// The same convolution on the fifth-generation tensor cores.  A CTA of 4 warps
+// The same convolution on the fifth-generation tensor cores.  A CTA of 8 warps
 // owns a 16 x 8 output patch = the M = 128 rows of one tcgen05.mma.kind::f16
 // (BF16 operands, FP32 accumulator in tensor memory), N = all output channels,
 // and loops over patches (persistent grid).  Shared memory holds, in the
@@ -300,12 +300,15 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 // (ky * 10 + kx) * 16 bytes: 8-row groups (patch rows) 160 bytes apart, K core
 // matrices (channel octets) 2880 bytes apart.  No im2col copy is made.  One
 // thread issues the 9 x cin / 16 MMAs of a patch and commits them to an
-// mbarrier; the four warps then read their 32 TMEM lanes (pixels) and run the
+// mbarrier; the warps then read their 32 TMEM lanes (pixels) and run the
 // epilogue of the other kernels.  The halos of the following patches stream in
 // with cp.async meanwhile, through a ring of up to 4 buffers.
 constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
 constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
 constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
+// 8 warps: warps w and w + 4 read the same 32 TMEM lanes (a warp reaches only
+// its quarter) and take alternate 16-column chunks of the epilogue
+constexpr int kTcThreads = 256;
 // longest wait for the tensor cores to finish a patch before the kernel gives
 // up (reported through g_cnn_tc_timeouts); a patch takes microseconds
 constexpr uint64_t kTcWaitNs = 2000000000ull;
@@ -376,7 +379,7 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
                : "memory");
 }
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kTcThreads)
     conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
   // n_halos halo buffers in a ring (1 to 4): the halos of the next n_halos - 1
   // patches are in flight while a patch's MMAs and epilogue run
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t dst = halo_a + uint32_t(buf) * halo_bytes;
     constexpr int kPos = kTcHR * kTcHC;  // 180 halo pixels; a thread takes one or two
     const int kc1 = a.c1 / 8;
-    for (int pos = tid; pos < kPos; pos += kThreads) {
+    for (int pos = tid; pos < kPos; pos += kTcThreads) {
       const int yy = y0 + pos / kTcHC, xx = x0 + pos % kTcHC;
       const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
       // the pixel's channels are contiguous: one 16-byte copy per octet
@@ -434,7 +437,7 @@ __global__ void __launch_bounds__(kThreads)
   }
   // all taps' weights, re-laid from [tap][cout][cin] into core matrices, and
   // the first patch's halo
-  for (int i = tid; i < 9 * kc_n * cout; i += kThreads) {
+  for (int i = tid; i < 9 * kc_n * cout; i += kTcThreads) {
     const int co = i % cout, kc = (i / cout) % kc_n, tap = i / (cout * kc_n);
     cp_async16(w_a + uint32_t(i) * 16, a.wt + (size_t(tap) * cout + co) * cin + kc * 8, true);
   }
@@ -510,16 +513,17 @@ __global__ void __launch_bounds__(kThreads)
     // no longer read it)
     if (n_halos == 1) load_halo(t + stride, 0);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // epilogue: warp w holds TMEM lanes (pixels) 32w .. 32w + 31
+    // epilogue: warps w and w + 4 hold TMEM lanes (pixels) 32w .. 32w + 31
     const int img = t / (tiles_x * tiles_y);
     const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
-    const int m = warp * 32 + lane;
+    const int quad = warp & 3, half = warp >> 2;
+    const int m = quad * 32 + lane;
     const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
     const bool live = oy < a.h && ox < a.w;
     const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
-    for (int c0 = 0; c0 < cout; c0 += 16) {
+    for (int c0 = 16 * half; c0 < cout; c0 += 32) {
       float v[16];
-      tc_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+      tc_ld16(tmem + (uint32_t(quad * 32) << 16) + uint32_t(c0), v);
       if (!live) continue;
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
@@ -940,7 +944,7 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     return false;
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
-  const int max_ctas = std::min(int(512 / cols), 2048 / kThreads);  // tensor memory, threads
+  const int max_ctas = std::min(int(512 / cols), 2048 / kTcThreads);  // tensor memory, threads
   // CTAs per SM and halos per CTA (each CTA also reserves 1 KB of shared
   // memory): the most CTAs whose shares hold 2 halos each (the next patch's
   // input streaming in under the MMAs), when that is at least 3; otherwise the
@@ -977,7 +981,7 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   // tensor memory (512 columns)
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
-  conv3x3_tc_kernel<<<grid, kThreads, smem, s>>>(a, cols, n_halos);
+  conv3x3_tc_kernel<<<grid, kTcThreads, smem, s>>>(a, cols, n_halos);
   TVK_CUDA(cudaGetLastError());
   return true;
 }
