@@ -944,7 +944,15 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     return false;
   constexpr size_t kMaxSmem = 227 * 1024, kSmPerSm = 228 * 1024, kReserved = 1024;
   const uint32_t cols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : 128u;
-  const int max_ctas = std::min(int(512 / cols), 2048 / kTcThreads);  // tensor memory, threads
+  // CTAs per SM that tensor memory (512 columns), threads and registers allow
+  static int regs = 0;
+  if (!regs) {
+    cudaFuncAttributes fa{};
+    TVK_CUDA(cudaFuncGetAttributes(&fa, conv3x3_tc_kernel));
+    regs = std::max(1, fa.numRegs);
+  }
+  const int max_ctas = std::max(1, std::min({int(512 / cols), 2048 / kTcThreads,
+                                             65536 / (regs * kTcThreads)}));
   // CTAs per SM and halos per CTA (each CTA also reserves 1 KB of shared
   // memory): the most CTAs whose shares hold 2 halos each (the next patch's
   // input streaming in under the MMAs), when that is at least 3; otherwise the
