@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "tvk_internal.h"
 
@@ -977,16 +978,30 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   const int n_halos = ring(per_sm);
   if (n_halos < 1) return false;
   const size_t smem = conv_tc_smem(cin, a.cout, n_halos);
-  TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem)));
-  TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                int(cudaSharedmemCarveoutMaxShared)));
-  int dev = 0, sms = 0;
+  // once per device: the kernel's shared-memory limit and carveout, and the SM
+  // count (host calls between the network's short launches would leave the
+  // GPU waiting)
+  int dev = 0;
   TVK_CUDA(cudaGetDevice(&dev));
-  TVK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  // a persistent grid of the CTAs that fit on an SM together (48 registers a
-  // thread never limit them); resident CTAs never wait on one another for
-  // tensor memory (512 columns)
+  static std::mutex mu;
+  static int sms_of[64] = {0};
+  int sms = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64) fail(TVK_ERR_INTERNAL, "device ordinal out of range");
+    if (!sms_of[dev]) {
+      TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(kMaxSmem)));
+      TVK_CUDA(cudaFuncSetAttribute(conv3x3_tc_kernel,
+                                    cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    int(cudaSharedmemCarveoutMaxShared)));
+      TVK_CUDA(cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev));
+    }
+    sms = sms_of[dev];
+  }
+  // a persistent grid of the CTAs that fit on an SM together; resident CTAs
+  // never wait on one another for tensor memory (512 columns)
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
   conv3x3_tc_kernel<<<grid, kTcThreads, smem, s>>>(a, cols, n_halos);
