@@ -283,3 +283,34 @@ def test_uvf_walk_equals_reference_parser_live(tmp_path, cfg):
     assert head["timestep_count"] == ts and head["checksum_verified"] == int(verify)
     if hist == 2 and comps == 1:
         assert sum(b["semantics"] == N.TVK_UVF_BS_2D_HISTOGRAM for b in blocks) == ts
+
+
+def md5_uvf(payload_len):
+    """A hand-assembled UVF file with an MD5 checksum (computed with hashlib)
+    over everything after the checksum, and one metadata block whose payload
+    makes the checksummed range payload_len + 32 + id bytes long."""
+    import hashlib
+    ident = b"md5 case"
+    block = struct.pack("<Q", len(ident)) + ident + struct.pack("<QQQ", 4, 0, 0) + bytes(
+        (i * 7) & 255 for i in range(payload_len))
+    tail = struct.pack("<Q", 0) + block  # offset to the first block, then the block
+    head = b"UVF-DATA" + bytes([0]) + struct.pack("<QQQ", 5, N.TVK_UVF_CS_MD5, 16)
+    return head + hashlib.md5(tail).digest() + tail
+
+
+@pytest.mark.parametrize("payload_len", [0, 7, 8, 15, 16, 23, 24, 100, 5_000_000],
+                         ids=lambda n: f"payload{n}")
+def test_uvf_md5_matches_hashlib(tmp_path, payload_len):
+    """The library's MD5 (RFC 1321) against Python's over lengths around the
+    64-byte block and 56-byte padding boundaries, and across its 4 MiB read
+    chunks; one flipped byte fails the check."""
+    buf = md5_uvf(payload_len)
+    p = tmp_path / "md5.uvf"
+    p.write_bytes(buf)
+    head, blocks = read_uvf_blocks(p, verify=True)
+    assert head["checksum_verified"] == 1 and len(blocks) == 1
+    bad = bytearray(buf)
+    bad[-1 if payload_len else 60] ^= 1
+    p.write_bytes(bytes(bad))
+    st, msg = status_of(p, verify=True)
+    assert st == 1 and "checksum" in msg
