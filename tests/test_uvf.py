@@ -314,3 +314,39 @@ def test_uvf_md5_matches_hashlib(tmp_path, payload_len):
     p.write_bytes(bytes(bad))
     st, msg = status_of(p, verify=True)
     assert st == 1 and "checksum" in msg
+
+
+def test_uvf_cpp_host_lists_the_same_blocks(tmp_path):
+    """A C++ host over include/tvk_renderer.hpp (tests/cpp/uvf_list.cpp)
+    lists the same blocks as the Python binding, and reports a damaged
+    checksum as an error."""
+    import re
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = Path(__file__).resolve().parent.parent
+    lib_dir = Path(N.LIB_PATH).resolve().parent
+    exe = tmp_path / "uvf_list"
+    subprocess.run([gxx, "-std=c++17", "-O2", f"-I{root / 'include'}",
+                    "-I/usr/local/cuda/include", str(root / "tests" / "cpp" / "uvf_list.cpp"),
+                    "-o", str(exe), f"-L{lib_dir}", "-ltvk", f"-Wl,-rpath,{lib_dir}",
+                    "-L/usr/local/cuda/lib64", "-Wl,-rpath,/usr/local/cuda/lib64"], check=True)
+    case = next(c for c in CASES if c["checksum"] == 2)
+    path = UVF / f"{case['name']}.uvf"
+    out = subprocess.run([str(exe), str(path), "verify"], check=True, capture_output=True,
+                         text=True).stdout
+    head, blocks = read_uvf_blocks(path, verify=True)
+    first = dict(re.findall(r"(\w+)=(\d+)", out.splitlines()[0]))
+    assert int(first["blocks"]) == head["block_count"] and int(first["verified"]) == 1
+    assert int(first["timesteps"]) == head["timestep_count"]
+    rows = [dict(re.findall(r"(\w+)=(\d+)", line)) for line in out.splitlines()[1:]]
+    assert [(int(r["offset"]), int(r["next"]), int(r["semantics"])) for r in rows] == \
+        [(b["offset"], b["offset_to_next"], b["semantics"]) for b in blocks]
+    bad = bytearray(path.read_bytes())
+    bad[-1] ^= 0x5A
+    p = tmp_path / "bad.uvf"
+    p.write_bytes(bytes(bad))
+    r = subprocess.run([str(exe), str(p), "verify"], capture_output=True, text=True)
+    assert r.returncode == 1 and "checksum" in r.stderr
