@@ -302,12 +302,13 @@ __global__ void __launch_bounds__(kWideThreads) conv3x3_wide_kernel(const ConvAr
 // matrices (channel octets) 2880 bytes apart.  No im2col copy is made.  One
 // thread issues the 9 x cin / 16 MMAs of a patch and commits them to an
 // mbarrier; the warps then read their 32 TMEM lanes (pixels) and run the
-// epilogue of the other kernels, warp-specialised (conv3x3_tc_kernel).
+// epilogue of the other kernels.  The halos of the following patches stream in
+// with cp.async meanwhile, through a ring of up to 4 buffers.
 constexpr int kTcRows = 16, kTcCols = 8;                  // output patch
 constexpr int kTcHR = kTcRows + 2, kTcHC = kTcCols + 2;  // halo
 constexpr uint32_t kTcCtrlBytes = 128;                   // mbarrier, TMEM address, flags
-// 8 warps: 4 producers (halo copies, MMA issue) and 4 consumers (epilogue; a
-// warp reaches only its quarter of the TMEM lanes)
+// 8 warps: warps w and w + 4 read the same 32 TMEM lanes (a warp reaches only
+// its quarter) and take alternate 16-column chunks of the epilogue
 constexpr int kTcThreads = 256;
 // longest wait for the tensor cores to finish a patch before the kernel gives
 // up (reported through g_cnn_tc_timeouts); a patch takes microseconds
@@ -379,52 +380,49 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
                : "memory");
 }
 
-// Waits, for at most kTcWaitNs, until phase `parity` of the barrier completes;
-// every lane of the (fully active) warp takes the same decision.
-__device__ bool mbar_wait_warp(uint32_t bar, uint32_t parity) {
-  const uint64_t t0 = global_ns();
-  for (;;) {
-    const bool done = mbar_try_wait(bar, parity);
-    if (__all_sync(0xffffffffu, done)) return true;
-    if (__shfl_sync(0xffffffffu, global_ns() - t0 > kTcWaitNs ? 1 : 0, 0)) return false;
-  }
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(bar)
-               : "memory");
-}
-
-// the producer warps' own barrier (barrier 0 is __syncthreads)
-__device__ __forceinline__ void producer_sync() {
-  asm volatile("bar.sync 1, 128;\n" ::: "memory");
-}
-
-// Warp-specialised: warps 0-3 produce (halo copies; one thread issues the
-// MMAs of patch k into accumulator k mod 2), warps 4-7 consume (the epilogue of
-// patch k from accumulator k mod 2), so a patch's epilogue runs while the next
-// patch's halo lands and its MMAs run.  mbarriers: full[b] (the MMAs' commit)
-// and empty[b] (the 128 consumer threads, once they have read accumulator b).
-// n_halos (1 or 2) halo buffers: with two, the next halo lands under the MMAs.
-// Every wait is bounded; a timeout is counted and ends both roles' loops.
 __global__ void __launch_bounds__(kTcThreads)
     conv3x3_tc_kernel(const ConvArgs a, uint32_t tmem_cols, int n_halos) {
+  // n_halos halo buffers in a ring (1 to 4): the halos of the next n_halos - 1
+  // patches are in flight while a patch's MMAs and epilogue run
   extern __shared__ __align__(128) unsigned char smem_tc[];
   const int cin = a.c1 + a.c2, kc_n = cin / 8, cout = a.cout;
-  // control block: full[2], empty[2], TMEM address, flag
-  const uint32_t ctrl = smem_addr(smem_tc);
-  const uint32_t full_a = ctrl, empty_a = ctrl + 16;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_tc + 32);
-  volatile int* pflag = reinterpret_cast<volatile int*>(smem_tc + 36);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_tc);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_tc + 8);
+  int* flag = reinterpret_cast<int*>(smem_tc + 12);
   const uint32_t halo_bytes = uint32_t(kc_n) * kTcHR * kTcHC * 16;
   unsigned char* halo0 = smem_tc + kTcCtrlBytes;                 // n_halos x [kc][18][10][8]
   unsigned char* wsm = halo0 + size_t(n_halos) * halo_bytes;      // [9][kc][cout][8]
-  const uint32_t halo_a = smem_addr(halo0), w_a = smem_addr(wsm);
+  const uint32_t bar_a = smem_addr(bar), halo_a = smem_addr(halo0), w_a = smem_addr(wsm);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_x = (a.w + kTcCols - 1) / kTcCols, tiles_y = (a.h + kTcRows - 1) / kTcRows;
   const int n_tiles = a.n * tiles_x * tiles_y;
-  const int stride = int(gridDim.x);
-  const uint32_t acc_cols = tmem_cols / 2;
+
+  // the halo of patch t into halo buffer `buf`, 8 channels per 16-byte copy,
+  // zero outside the image; one cp.async group per call (empty past the last patch)
+  auto load_halo = [&](int t, int buf) {
+    if (t >= n_tiles) {
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      return;
+    }
+    const int img = t / (tiles_x * tiles_y);
+    const int y0 = ((t / tiles_x) % tiles_y) * kTcRows - 1, x0 = (t % tiles_x) * kTcCols - 1;
+    const uint32_t dst = halo_a + uint32_t(buf) * halo_bytes;
+    constexpr int kPos = kTcHR * kTcHC;  // 180 halo pixels; a thread takes one or two
+    const int kc1 = a.c1 / 8;
+    for (int pos = tid; pos < kPos; pos += kTcThreads) {
+      const int yy = y0 + pos / kTcHC, xx = x0 + pos % kTcHC;
+      const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
+      // the pixel's channels are contiguous: one 16-byte copy per octet
+      const __nv_bfloat16* s1 = a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1;
+      uint32_t d = dst + uint32_t(pos) * 16;
+      for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) cp_async16(d, s1 + kc * 8, in);
+      if (kc1 < kc_n) {
+        const __nv_bfloat16* s2 = a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2;
+        for (int kc = 0; kc < kc_n - kc1; ++kc, d += kPos * 16) cp_async16(d, s2 + kc * 8, in);
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
@@ -434,130 +432,99 @@ __global__ void __launch_bounds__(kTcThreads)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
   if (tid == 0) {
-    for (int b = 0; b < 2; ++b) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full_a + 8 * b) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;\n" ::"r"(empty_a + 8 * b)
-                   : "memory");
-    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    *pflag = 0;
+    *flag = 0;
   }
-  // all taps' weights, re-laid from [tap][cout][cin] into core matrices
+  // all taps' weights, re-laid from [tap][cout][cin] into core matrices, and
+  // the first patch's halo
   for (int i = tid; i < 9 * kc_n * cout; i += kTcThreads) {
     const int co = i % cout, kc = (i / cout) % kc_n, tap = i / (cout * kc_n);
     cp_async16(w_a + uint32_t(i) * 16, a.wt + (size_t(tap) * cout + co) * cin + kc * 8, true);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  const int stride = int(gridDim.x);
+  for (int k = 0; k < max(1, n_halos - 1); ++k) load_halo(int(blockIdx.x) + k * stride, k);
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = tc_idesc(128, uint32_t(cout));
+  constexpr uint32_t kLboA = kTcHR * kTcHC * 16, kSboA = kTcHC * 16;
+  const uint32_t lbo_b = uint32_t(cout) * 16, sbo_b = 128;
+  uint32_t phase = 0;
+  bool ok = true;
+  int k = 0;  // this CTA's patch counter: patch blockIdx.x + k * gridDim.x, buffer k % n_halos
 
-  if (warp < 4) {
-    // ---------------------------------------------------------------- producer
-    const uint32_t idesc = tc_idesc(128, uint32_t(cout));
-    constexpr uint32_t kLboA = kTcHR * kTcHC * 16, kSboA = kTcHC * 16;
-    const uint32_t lbo_b = uint32_t(cout) * 16, sbo_b = 128;
-    const int kc1 = a.c1 / 8;
-    int last = -1;  // the last patch whose MMAs were committed
-    int k = 0;
-    for (int t = blockIdx.x; t < n_tiles; t += stride, ++k) {
-      const int b = k & 1, h = n_halos == 2 ? (k & 1) : 0;
-      if (k >= n_halos) {  // halo buffer h is free once patch k - n_halos's MMAs are done
-        const int kk = k - n_halos;
-        if (tid == 0 && !mbar_wait_bounded(full_a + 8 * (kk & 1), (kk >> 1) & 1)) *pflag = 1;
-        producer_sync();
-        if (*pflag) break;
+  for (int t = blockIdx.x; t < n_tiles; t += stride, ++k) {
+    const int buf = k % n_halos;
+    if (n_halos >= 2) {
+      // the ring's free buffer (patch k - 1's, whose MMAs are done) takes the
+      // patch n_halos - 1 ahead; then patch k's group, the oldest, has landed
+      load_halo(t + (n_halos - 1) * stride, (k + n_halos - 1) % n_halos);
+      switch (n_halos) {
+        case 2: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+        case 3: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
       }
-      // the halo of patch t, 8 channels per 16-byte copy, zero outside the image
-      {
-        const int img = t / (tiles_x * tiles_y);
-        const int y0 = ((t / tiles_x) % tiles_y) * kTcRows - 1, x0 = (t % tiles_x) * kTcCols - 1;
-        constexpr int kPos = kTcHR * kTcHC;
-        const uint32_t dst = halo_a + uint32_t(h) * halo_bytes;
-        for (int pos = tid; pos < kPos; pos += 128) {
-          const int yy = y0 + pos / kTcHC, xx = x0 + pos % kTcHC;
-          const bool in = yy >= 0 && yy < a.h && xx >= 0 && xx < a.w;
-          const __nv_bfloat16* s1 = a.x1 + (in ? x1_pixel(a, img, yy, xx) : 0) * a.c1;
-          uint32_t d = dst + uint32_t(pos) * 16;
-          for (int kc = 0; kc < kc1; ++kc, d += kPos * 16) cp_async16(d, s1 + kc * 8, in);
-          if (kc1 < kc_n) {
-            const __nv_bfloat16* s2 =
-                a.x2 + (in ? (size_t(img) * a.h + yy) * a.w + xx : 0) * a.c2;
-            for (int kc = 0; kc < kc_n - kc1; ++kc, d += kPos * 16)
-              cp_async16(d, s2 + kc * 8, in);
-          }
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_all;\n" ::: "memory");
-        // make the copies visible to the tensor cores' (async proxy) reads
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      }
-      producer_sync();
-      if (tid == 0) {
-        // accumulator b is free once the consumers have read patch k - 2
-        if (k >= 2 && !mbar_wait_bounded(empty_a + 8 * b, ((k - 2) >> 1) & 1)) {
-          *pflag = 1;
-        } else {
-          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-          // descriptors advance in their start-address field (16-byte units;
-          // every address is below 256 KB, so nothing carries out of it)
-          const uint64_t a0 = tc_desc(halo_a + uint32_t(h) * halo_bytes, kLboA, kSboA);
-          uint64_t bd = tc_desc(w_a, lbo_b, sbo_b);
-          const uint64_t a_step = 2 * kTcHR * kTcHC, b_step = uint64_t(2 * cout);
-          const uint32_t d_tmem = tmem + uint32_t(b) * acc_cols;
-          uint32_t acc = 0;
-#pragma unroll
-          for (int tap = 0; tap < 9; ++tap) {
-            uint64_t ad = a0 + uint64_t((tap / 3) * kTcHC + tap % 3);
-            for (int s = 0; s < kc_n / 2; ++s) {
-              asm volatile(
-                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                  : "memory");
-              acc = 1;
-              ad += a_step;
-              bd += b_step;
-            }
-          }
-          asm volatile(
-              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                  full_a + 8 * b)
-              : "memory");
-          last = k;
-        }
-      }
-      producer_sync();
-      if (*pflag) break;
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
+    // make the copies visible to the tensor cores' (async proxy) reads
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
     if (tid == 0) {
-      if (*pflag) atomicAdd(&g_cnn_tc_timeouts, 1u);
-      // no MMA may still write tensor memory when it is freed (bounded)
-      if (last >= 0) mbar_wait_bounded(full_a + 8 * (last & 1), (last >> 1) & 1);
-    }
-  } else {
-    // ---------------------------------------------------------------- consumer
-    const int quad = warp & 3;  // TMEM lanes (pixels) 32 quad .. 32 quad + 31
-    int k = 0;
-    for (int t = blockIdx.x; t < n_tiles; t += stride, ++k) {
-      const int b = k & 1;
-      if (!mbar_wait_warp(full_a + 8 * b, (k >> 1) & 1)) {
-        if (lane == 0) atomicAdd(&g_cnn_tc_timeouts, 1u);
-        break;
-      }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const int img = t / (tiles_x * tiles_y);
-      const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
-      const int m = quad * 32 + lane;
-      const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
-      const bool live = oy < a.h && ox < a.w;
-      const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
-      for (int c0 = 0; c0 < cout; c0 += 16) {
-        float v[16];
-        tc_ld16(tmem + (uint32_t(quad * 32) << 16) + uint32_t(b) * acc_cols + uint32_t(c0), v);
+      // The descriptors advance by adding to their start-address field (in
+      // 16-byte units; every address is below 256 KB, so nothing carries out of
+      // the field): A by one channel-octet pair per K step and by the tap's
+      // (ky * 10 + kx) offset, B through the weights in order.
+      const uint64_t a0 = tc_desc(halo_a + uint32_t(buf) * halo_bytes, kLboA, kSboA);
+      uint64_t bd = tc_desc(w_a, lbo_b, sbo_b);
+      const int ksteps = kc_n / 2;
+      const uint64_t a_step = 2 * kTcHR * kTcHC, b_step = uint64_t(2 * cout);
+      uint32_t acc = 0;
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        uint64_t ad = a0 + uint64_t((tap / 3) * kTcHC + tap % 3);
+        for (int s = 0; s < ksteps; ++s) {
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+              : "memory");
+          acc = 1;
+          ad += a_step;
+          bd += b_step;
+        }
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              bar_a)
+          : "memory");
+    }
+    if (tid == 0 && !mbar_wait_bounded(bar_a, phase)) *flag = 1;
+    __syncthreads();
+    phase ^= 1u;
+    if (*flag) {
+      ok = false;
+      break;
+    }
+    // with one buffer the next halo streams in under the epilogue (the MMAs
+    // no longer read it)
+    if (n_halos == 1) load_halo(t + stride, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // epilogue: warps w and w + 4 hold TMEM lanes (pixels) 32w .. 32w + 31
+    const int img = t / (tiles_x * tiles_y);
+    const int ty = (t / tiles_x) % tiles_y, tx = t % tiles_x;
+    const int quad = warp & 3, half = warp >> 2;
+    const int m = quad * 32 + lane;
+    const int oy = ty * kTcRows + m / kTcCols, ox = tx * kTcCols + m % kTcCols;
+    const bool live = oy < a.h && ox < a.w;
+    const size_t p = (size_t(img) * a.h + oy) * a.w + ox;
+    for (int c0 = 16 * half; c0 < cout; c0 += 32) {
+      float v[16];
+      tc_ld16(tmem + (uint32_t(quad * 32) << 16) + uint32_t(c0), v);
       if (!live) continue;
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
@@ -609,11 +576,13 @@ __global__ void __launch_bounds__(kTcThreads)
           *o = a.accumulate ? *o + v[e] : v[e];
         }
       }
-      }
-      // accumulator b read: the producer may overwrite it
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      mbar_arrive(empty_a + 8 * b);
     }
+    // TMEM read before the next patch's MMAs overwrite it
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  }
+  if (!ok && tid == 0) {
+    atomicAdd(&g_cnn_tc_timeouts, 1u);
+    mbar_wait_bounded(bar_a, phase ^ 1u);  // the abandoned patch's MMAs, bounded again
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -983,27 +952,30 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
     TVK_CUDA(cudaFuncGetAttributes(&fa, conv3x3_tc_kernel));
     regs = std::max(1, fa.numRegs);
   }
-  const int max_ctas = std::max(1, std::min({int(512 / (2 * cols)), 2048 / kTcThreads,
+  const int max_ctas = std::max(1, std::min({int(512 / cols), 2048 / kTcThreads,
                                              65536 / (regs * kTcThreads)}));
   // CTAs per SM and halos per CTA (each CTA also reserves 1 KB of shared
-  // memory and holds two accumulators): the most CTAs whose shares hold two
-  // halos (the next patch's input landing under the MMAs), else the most that
-  // hold one.
+  // memory): the most CTAs whose shares hold 2 halos each (the next patch's
+  // input streaming in under the MMAs), when that is at least 3; otherwise the
+  // most CTAs that hold one.  Each CTA takes the deepest ring (up to 4) its
+  // share holds.  Measured on the network's layers at 960x540: 80 -> 32
+  // channels 85 us with 3 CTAs of one halo against 105 us with 2 of two; 16 ->
+  // 32 channels 51 us with 10 CTAs of two against 56 us with 13 of one.
   const size_t halo = size_t(cin) / 8 * kTcHR * kTcHC * 16;
   const size_t base = conv_tc_smem(cin, a.cout, 0);
-  auto halos = [&](int c) {
+  auto ring = [&](int c) {
     const size_t per = kSmPerSm / size_t(c) - kReserved;
     const size_t room = std::min(per, kMaxSmem);
-    return room > base ? int(std::min<size_t>((room - base) / halo, 2)) : 0;
+    return room > base ? int(std::min<size_t>((room - base) / halo, 4)) : 0;
   };
   auto most_ctas = [&](int min_halos) {
     for (int c = max_ctas; c >= 1; --c)
-      if (halos(c) >= min_halos) return c;
+      if (ring(c) >= min_halos) return c;
     return 0;
   };
   int per_sm = most_ctas(2);
-  if (per_sm == 0) per_sm = std::max(most_ctas(1), 1);
-  const int n_halos = halos(per_sm);
+  if (per_sm < 3) per_sm = std::max(most_ctas(1), 1);
+  const int n_halos = ring(per_sm);
   if (n_halos < 1) return false;
   const size_t smem = conv_tc_smem(cin, a.cout, n_halos);
   // once per device: the kernel's shared-memory limit and carveout, and the SM
@@ -1032,7 +1004,7 @@ bool launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   // never wait on one another for tensor memory (512 columns)
   const long tiles = long(a.n) * ((a.w + kTcCols - 1) / kTcCols) * ((a.h + kTcRows - 1) / kTcRows);
   const unsigned grid = unsigned(std::min<long>(tiles, long(per_sm) * sms));
-  conv3x3_tc_kernel<<<grid, kTcThreads, smem, s>>>(a, 2 * cols, n_halos);
+  conv3x3_tc_kernel<<<grid, kTcThreads, smem, s>>>(a, cols, n_halos);
   TVK_CUDA(cudaGetLastError());
   return true;
 }
