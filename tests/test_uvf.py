@@ -350,3 +350,18 @@ def test_uvf_cpp_host_lists_the_same_blocks(tmp_path):
     p.write_bytes(bytes(bad))
     r = subprocess.run([str(exe), str(p), "verify"], capture_output=True, text=True)
     assert r.returncode == 1 and "checksum" in r.stderr
+
+
+def test_uvf_offset_to_first_block_is_honoured(tmp_path):
+    """GlobalHeader::GetDataPos adds ulOffsetToFirstDataBlock (GlobalHeader.cpp:
+    33-36, 59-61): bytes between the header and the first block are skipped."""
+    body = minimal_uvf([(4, b"kv"), (7, bytes(16))])
+    pad = 24
+    head = bytearray(body[:41])
+    struct.pack_into("<Q", head, 33, pad)  # no checksum: the offset follows the length
+    p = tmp_path / "pad.uvf"
+    p.write_bytes(bytes(head) + bytes(pad) + body[41:])
+    info, blocks = read_uvf_blocks(p)
+    assert info["data_offset"] == 41 + pad
+    assert [b["offset"] for b in blocks] == [41 + pad, 41 + pad + blocks[0]["offset_to_next"]]
+    assert [b["semantics"] for b in blocks] == [4, 7]
